@@ -1,0 +1,222 @@
+"""GB300-native ParHDE layout pipeline.
+
+Python mirror of the reference's operator interface (``variants/DrawingBase.h:41-47``): the classes
+``ParHDE``, ``WParHDE``, ``PivotMDS`` and ``PHDE`` take the same constructor arguments as the C++
+classes, ``run()`` computes the layout and ``getCoordinates()`` returns the unit-norm coordinates
+as the reference's column-major ``double*`` (coordinate j of vertex i at ``i + j*n``).  ``DOBFS`` and
+``DeltaStep`` mirror the two distance kernels (``variants/DrawingBase.h:62-67``).  Everything runs in
+``libparhde_gb300.so`` on the GPU through the C ABI of ``include/parhde.h``; where the reference calls
+``exit``/``abort`` these raise ``ParHDEError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .csr_io import CSRGraph, read_csr, write_csr, format_nxyz, write_nxyz, read_nxyz  # noqa: F401
+
+__all__ = ["Context", "ParHDEError", "LayoutResult", "DrawingBase", "ParHDE", "WParHDE", "PivotMDS", "PHDE",
+           "DOBFS", "DeltaStep", "CSRGraph", "read_csr", "write_csr", "write_nxyz", "read_nxyz"]
+
+
+class ParHDEError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.name = _lib.STATUS.get(status, str(status))
+        super().__init__(f"{self.name}: {message}")
+
+
+def _ptr(a, ct):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ct))
+
+
+@dataclass
+class LayoutResult:
+    coords: np.ndarray  # (n, c)
+    sources: np.ndarray
+    stats: dict
+    basis: np.ndarray | None = None  # (n, k)
+    gram: np.ndarray | None = None  # (k, k): entry (p, q) = <S_p, (L S)_q>
+    evecs: np.ndarray | None = None  # (k, k) eigenvectors in columns
+    evals: np.ndarray | None = None  # (k,)
+    extra: dict = field(default_factory=dict)
+
+
+class Context:
+    """One device context: a CUDA stream, the uploaded graph and the device workspace."""
+
+    def __init__(self, device: int = 0):
+        self._L = _lib.load()
+        h = C.c_void_p()
+        rc = self._L.phde_create(C.byref(h), device)
+        if rc != 0:
+            raise ParHDEError(rc, "could not create a context on device %d (CUDA missing or no GPU)" % device)
+        self._h = h
+        self.n = 0
+        self.nnz = 0
+        self.weighted = False
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.phde_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise ParHDEError(rc, self._L.phde_last_error(self._h).decode())
+
+    @property
+    def launch_count(self) -> int:
+        return int(self._L.phde_launch_count(self._h))
+
+    def upload(self, g: CSRGraph) -> None:
+        off = np.ascontiguousarray(g.offsets)
+        width = 8 if off.dtype in (np.int64, np.uint64) else 4
+        off = off.astype(np.int64 if width == 8 else np.uint32, copy=False)
+        adj = np.ascontiguousarray(g.adj, dtype=np.uint32)
+        w = None if g.weights is None else np.ascontiguousarray(g.weights, dtype=np.int32)
+        self._check(self._L.phde_graph_upload(self._h, off.ctypes.data_as(C.c_void_p), width, _ptr(adj, C.c_uint32),
+                                              _ptr(w, C.c_int32), g.n, g.nnz))
+        self.n, self.nnz, self.weighted = g.n, g.nnz, w is not None
+
+    def layout(self, algo: str = "ParHDE", strategy: str = "Kcenters", k: int = 10, c: int = 2,
+               precision: str = "fp64", eig: str = "power", seed: int = 1, verbose: bool = False,
+               extra: bool = False, coords_out: np.ndarray | None = None) -> LayoutResult:
+        o = _lib.LayoutOpts(_lib.ALGOS[algo], _lib.STRATEGIES[strategy], k, c, _lib.PRECISIONS[precision],
+                            _lib.EIGS[eig], seed, 1 if verbose else 0)
+        n = self.n
+        coords = coords_out if coords_out is not None else np.empty(n * c, dtype=np.float64)
+        sources = np.full(3 * k, -1, dtype=np.int64)
+        st = _lib.LayoutStats()
+        ex = None
+        bufs = {}
+        if extra:
+            bufs = {"basis": np.empty(n * k), "gram": np.empty(k * k), "evecs": np.empty(k * k),
+                    "evals": np.empty(k)}
+            ex = _lib.LayoutExtra(*(_ptr(bufs[f], C.c_double) for f in ("basis", "gram", "evecs", "evals")))
+        rc = self._L.phde_layout(self._h, C.byref(o), _ptr(coords, C.c_double), _ptr(sources, C.c_int64),
+                                 C.byref(ex) if ex is not None else None, C.byref(st))
+        self._check(rc)
+        res = LayoutResult(coords.reshape(c, n).T, sources[: st.npasses].copy(), st.as_dict())
+        if extra:
+            res.basis = bufs["basis"].reshape(k, n).T.copy()
+            res.gram = bufs["gram"].reshape(k, k).T.copy()
+            res.evecs = bufs["evecs"].reshape(k, k).T.copy()
+            res.evals = bufs["evals"]
+        return res
+
+    def distances(self, sources) -> np.ndarray:
+        src = np.ascontiguousarray(np.atleast_1d(sources), dtype=np.int64)
+        out = np.empty(self.n * src.shape[0], dtype=np.int32)
+        self._check(self._L.phde_distances(self._h, _ptr(src, C.c_int64), src.shape[0], _ptr(out, C.c_int32)))
+        return out.reshape(src.shape[0], self.n).T
+
+    def kcenters(self, passes: int, variant: int = 0, want_dist: bool = True):
+        D = np.empty(self.n * passes, dtype=np.int32) if want_dist else None
+        src = np.empty(passes, dtype=np.int64)
+        self._check(self._L.phde_kcenters(self._h, passes, variant, _ptr(D, C.c_int32), _ptr(src, C.c_int64)))
+        return (D.reshape(passes, self.n).T if D is not None else None), src
+
+    def selftest_barrier_timeout(self, timeout_ms: int = 50) -> int:
+        return int(self._L.phde_selftest_barrier_timeout(self._h, timeout_ms))
+
+
+# ---------------------------------------------------------------------------------------------
+# The reference's class interface (variants/DrawingBase.h:41-47, ParHDE.h, WParHDE.h, PivotMDS.h, PHDE.h).
+
+class DrawingBase:
+    """``DrawingBase(rowPtrs, adj, weights, n, m, numSources, doRand, numCoord=2)``."""
+
+    _algo = "ParHDE"
+
+    def __init__(self, rowPtrs, adj, weights, n, m, numSources, doRand, numCoord=2, *, precision="fp64",
+                 eig="power", seed=1, device=0, verbose=True):
+        self.g = CSRGraph(np.asarray(rowPtrs), np.asarray(adj), None if weights is None else np.asarray(weights))
+        if self.g.n != n or self.g.nnz != m:
+            raise ParHDEError(-1, "n/m do not match the CSR arrays")
+        self.numSources, self.doRand, self.numCoord = int(numSources), int(doRand), int(numCoord)
+        self.precision, self.eig, self.seed, self.verbose = precision, eig, seed, verbose
+        self.ctx = Context(device)
+        self.ctx.upload(self.g)
+        self.result: LayoutResult | None = None
+        self.coordinates = np.zeros(n * self.numCoord)
+
+    def run(self, tries: int = 11, alpha: int = 15, beta: int = 18, delta: int = 1) -> int:
+        strategy = {0: "RandCoarse", 1: "RandFine", 2: "Kcenters"}[self.doRand]
+        for _ in range(max(1, tries)):
+            self.result = self.ctx.layout(self._algo, strategy, self.numSources, self.numCoord, self.precision,
+                                          self.eig, self.seed, self.verbose)
+        self.coordinates = np.asfortranarray(self.result.coords).ravel(order="F")
+        return 0
+
+    def getCoordinates(self) -> np.ndarray:
+        """Unit-norm coordinates, column-major: coordinate j of vertex i at index i + j*n."""
+        return self.coordinates
+
+
+class ParHDE(DrawingBase):
+    _algo = "ParHDE"
+
+    def __init__(self, rowPtrs, adj, weights, n, m, s, r, numCoord, **kw):
+        if weights is not None:
+            raise ParHDEError(-10, "ParHDE code doesn't requires the weighted edges")
+        super().__init__(rowPtrs, adj, None, n, m, s, r, numCoord, **kw)
+
+
+class WParHDE(DrawingBase):
+    """``WParHDE(rowPtrs, adj, weights, n, m, s, numCoord)``: always Kcenters (WParHDE.cpp:40-218).
+    Unlike the reference (whose constructor drops numCoord, WParHDE.cpp:12-13), numCoord is honoured."""
+
+    _algo = "wParHDE"
+
+    def __init__(self, rowPtrs, adj, weights, n, m, s, numCoord=2, **kw):
+        if weights is None:
+            raise ParHDEError(-10, "Weighted ParHDE code requires the weighted edges")
+        super().__init__(rowPtrs, adj, weights, n, m, s, 2, numCoord, **kw)
+
+
+class PivotMDS(DrawingBase):
+    _algo = "PivotMDS"
+
+
+class PHDE(DrawingBase):
+    _algo = "PHDE"
+
+
+def DOBFS(row, col, source, numNodes, numEdges, dists, alpha=15, beta=18) -> None:
+    """Hop distances from ``source`` into ``dists`` (float64, only reached entries written; bfs.cc:144-185)."""
+    L = _lib.load()
+    row = np.ascontiguousarray(row, dtype=np.uint32)
+    col = np.ascontiguousarray(col, dtype=np.uint32)
+    rc = L.phde_DOBFS(_ptr(row, C.c_uint32), _ptr(col, C.c_uint32), source, numNodes, numEdges,
+                      _ptr(dists, C.c_double), alpha, beta)
+    if rc != 0:
+        raise ParHDEError(rc, "DOBFS failed")
+
+
+def DeltaStep(row, col, weights, source, numNodes, numEdges, dist, delta) -> np.ndarray:
+    """Weighted distances from ``source`` into ``dist`` (float64; kDistInf when unreached; sssp.cc:53-140)."""
+    L = _lib.load()
+    row = np.ascontiguousarray(row, dtype=np.uint32)
+    col = np.ascontiguousarray(col, dtype=np.uint32)
+    w = np.ascontiguousarray(weights, dtype=np.int32)
+    rc = L.phde_DeltaStep(_ptr(row, C.c_uint32), _ptr(col, C.c_uint32), _ptr(w, C.c_int32), source, numNodes,
+                          numEdges, _ptr(dist, C.c_double), delta)
+    if rc != 0:
+        raise ParHDEError(rc, "DeltaStep failed")
+    return dist

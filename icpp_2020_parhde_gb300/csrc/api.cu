@@ -1,0 +1,584 @@
+// api.cu -- C ABI entry points (include/parhde.h) and the host orchestration of the layout pipelines.
+//
+// phde_layout reproduces the control flow of the reference variants' run() methods (ParHDE.cpp:45-352,
+// WParHDE.cpp:40-292, PivotMDS.cpp:68-147, PHDE.cpp:50-136) and of getCoordinates()
+// (DrawingBase.cpp:196-205); every numeric stage runs on the GPU.  The host only sequences launches,
+// reads a handful of status words and copies the n x c coordinates back.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+
+int phde_fill_i32(phde_ctx *ctx, int32_t *p, int64_t n, int32_t v);
+int phde_degrees(phde_ctx *ctx, double *deg);
+int phde_cgs(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, double *S, int k,
+             int *h_state, double *h_dlog);
+int phde_mgs_pass(phde_ctx *ctx, const int32_t *col, const ull *sumsq, double *U, int xcol, int jcount,
+                  const double *deg, double *h_nrm2);
+int phde_const_col(phde_ctx *ctx, double *U);
+int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale, double *S, int k, int scol);
+int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS, int k);
+int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M);
+int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C);
+int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X);
+int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
+                    double *d_evals, double *d_Y, int *h_iters);
+
+namespace {
+
+__global__ void widen_offsets_kernel(const uint32_t *in, int64_t *out, int64_t count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int64_t)in[i];
+}
+
+// Device-side CSR validation: offsets start at 0, never decrease, end at nnz; neighbours < n.
+__global__ void validate_csr_kernel(const int64_t *off, const uint32_t *adj, int64_t n, int64_t nnz, int *bad) {
+  int b = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    if (off[i + 1] < off[i]) b = 1;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += stride)
+    if ((int64_t)adj[e] >= n) b = 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[n] != nnz)) b = 1;
+  if (b) atomicExch(bad, 1);
+}
+
+// A barrier that waits for one more block than is launched: the bounded wait must give up.
+__global__ void barrier_timeout_kernel(GridSync *gs, int *err, uint64_t timeout_ns) {
+  grid_barrier(gs, err, timeout_ns, gridDim.x + 1);
+}
+
+// Published glibc TYPE_3 rand() stream (see eigen.cu); the reference draws random pivots with rand() % n.
+void glibc_rand_host(uint32_t seed, int count, std::vector<int32_t> &out) {
+  std::vector<int32_t> r((size_t)count + 344);
+  if (seed == 0) seed = 1;
+  r[0] = (int32_t)seed;
+  for (int i = 1; i < 31; i++) {
+    int32_t hi = r[i - 1] / 127773, lo = r[i - 1] % 127773;
+    int32_t word = 16807 * lo - 2836 * hi;
+    if (word < 0) word += 2147483647;
+    r[i] = word;
+  }
+  for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+  for (int i = 34; i < count + 344; i++) r[i] = (int32_t)((uint32_t)r[i - 31] + (uint32_t)r[i - 3]);
+  out.resize(count);
+  for (int i = 0; i < count; i++) out[i] = (int32_t)(((uint32_t)r[i + 344]) >> 1);
+}
+
+struct Timer {
+  phde_ctx *ctx;
+  explicit Timer(phde_ctx *c) : ctx(c) {}
+  void mark(int i) { cudaEventRecord(ctx->ev[i], ctx->stream); }
+  double ms(int a, int b) {
+    float t = 0;
+    cudaEventElapsedTime(&t, ctx->ev[a], ctx->ev[b]);
+    return t;
+  }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+int phde_fail(phde_ctx *ctx, int status, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return status;
+}
+
+void *phde_buf(phde_ctx *ctx, const char *name, size_t bytes) {
+  auto it = ctx->ws.find(name);
+  if (it != ctx->ws.end() && it->second.second >= bytes) return it->second.first;
+  if (it != ctx->ws.end()) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(it->second.first);
+    ctx->ws.erase(it);
+  }
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->err = std::string("device allocation of ") + std::to_string(bytes) + " bytes for " + name + " failed";
+    return nullptr;
+  }
+  ctx->ws[name] = {p, bytes};
+  return p;
+}
+
+int phde_reset_sync(phde_ctx *ctx) {
+  PHDE_CK(ctx, cudaMemsetAsync(ctx->d_sync, 0, sizeof(GridSync), ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+  return PHDE_OK;
+}
+
+int phde_check_device_err(phde_ctx *ctx, const char *what) {
+  int e = 0;
+  PHDE_CK(ctx, cudaMemcpyAsync(&e, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (e == PHDE_ERR_DISCONNECTED) return phde_fail(ctx, e, std::string(what) + ": the graph is not connected");
+  if (e == PHDE_ERR_TIMEOUT) return phde_fail(ctx, e, std::string(what) + ": a bounded device wait gave up");
+  if (e) return phde_fail(ctx, e, std::string(what) + ": device error " + std::to_string(e));
+  return PHDE_OK;
+}
+
+extern "C" {
+
+int phde_version(void) { return 10000; }
+
+const char *phde_status_string(int s) {
+  switch (s) {
+    case PHDE_OK: return "ok";
+    case PHDE_ERR_INVALID: return "invalid argument";
+    case PHDE_ERR_CSR: return "malformed CSR";
+    case PHDE_ERR_DISCONNECTED: return "graph is not connected";
+    case PHDE_ERR_K_RANGE: return "k or c out of range";
+    case PHDE_ERR_TOO_FEW_PIVOTS: return "too few pivots survived D-orthogonalisation";
+    case PHDE_ERR_OOM: return "out of device memory";
+    case PHDE_ERR_NOCONVERGE: return "eigensolver did not converge";
+    case PHDE_ERR_TIMEOUT: return "bounded device wait timed out";
+    case PHDE_ERR_CUDA: return "CUDA error";
+    case PHDE_ERR_WEIGHTS: return "weights missing or unexpected";
+    case PHDE_ERR_NO_GRAPH: return "no graph uploaded";
+    default: return "unknown status";
+  }
+}
+
+int phde_create(phde_ctx **out, int device) {
+  if (!out) return PHDE_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return PHDE_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) return PHDE_ERR_INVALID;
+  phde_ctx *c = new phde_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaMalloc(&c->d_sync, sizeof(GridSync)) != cudaSuccess || cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return PHDE_ERR_CUDA;
+  }
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) {
+    delete c;
+    return PHDE_ERR_CUDA;
+  }
+  for (auto &e : c->ev) cudaEventCreate(&e);
+  if (const char *t = getenv("PHDE_WAIT_LIMIT_MS")) c->timeout_ns = (uint64_t)atoll(t) * 1000000ull;
+  *out = c;
+  return PHDE_OK;
+}
+
+void phde_destroy(phde_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->ws) cudaFree(kv.second.first);
+  cudaFree(c->d_off);
+  cudaFree(c->d_adj);
+  cudaFree(c->d_w);
+  cudaFree(c->d_sync);
+  cudaFree(c->d_err);
+  for (auto &e : c->ev) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *phde_last_error(const phde_ctx *c) { return c ? c->err.c_str() : "no context"; }
+int64_t phde_graph_n(const phde_ctx *c) { return c ? c->n : 0; }
+int64_t phde_graph_nnz(const phde_ctx *c) { return c ? c->nnz : 0; }
+int64_t phde_launch_count(const phde_ctx *c) { return c ? c->launches : 0; }
+
+int phde_graph_upload(phde_ctx *ctx, const void *offsets, int offset_bytes, const uint32_t *adj,
+                      const int32_t *weights, int64_t n, int64_t nnz) {
+  if (!ctx) return PHDE_ERR_INVALID;
+  if (!offsets || (!adj && nnz > 0) || n <= 0 || nnz < 0 || (offset_bytes != 4 && offset_bytes != 8))
+    return phde_fail(ctx, PHDE_ERR_INVALID, "phde_graph_upload: bad arguments");
+  if (n >= 0xffffffffll || nnz >= 0xffffffffll)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "phde_graph_upload: n and nnz must be below 2^32");
+  PHDE_CK(ctx, cudaSetDevice(ctx->device));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (n + 1 > (ctx->n ? ctx->n + 1 : 0) || !ctx->d_off) {
+    cudaFree(ctx->d_off);
+    ctx->d_off = nullptr;
+    PHDE_CK(ctx, cudaMalloc(&ctx->d_off, sizeof(int64_t) * (n + 1)));
+  }
+  if (nnz > ctx->nnz || !ctx->d_adj) {
+    cudaFree(ctx->d_adj);
+    ctx->d_adj = nullptr;
+    PHDE_CK(ctx, cudaMalloc(&ctx->d_adj, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
+    cudaFree(ctx->d_w);
+    ctx->d_w = nullptr;
+  }
+  ctx->n = n;
+  ctx->nnz = nnz;
+  if (offset_bytes == 8) {
+    PHDE_CK(ctx, cudaMemcpyAsync(ctx->d_off, offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    uint32_t *stage = (uint32_t *)phde_buf(ctx, "upload.off32", sizeof(uint32_t) * (n + 1));
+    if (!stage) return PHDE_ERR_OOM;
+    PHDE_CK(ctx, cudaMemcpyAsync(stage, offsets, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+    widen_offsets_kernel<<<(int)std::min<int64_t>((n + 256) / 256, ctx->nsm * 8), 256, 0, ctx->stream>>>(stage, ctx->d_off,
+                                                                                                       n + 1);
+    PHDE_LAUNCHED(ctx);
+  }
+  if (nnz > 0)
+    PHDE_CK(ctx, cudaMemcpyAsync(ctx->d_adj, adj, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->weighted = weights != nullptr;
+  if (weights) {
+    if (!ctx->d_w) PHDE_CK(ctx, cudaMalloc(&ctx->d_w, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+    if (nnz > 0)
+      PHDE_CK(ctx, cudaMemcpyAsync(ctx->d_w, weights, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  int *bad = (int *)phde_buf(ctx, "upload.bad", sizeof(int));
+  if (!bad) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  validate_csr_kernel<<<(int)std::max<int64_t>(1, std::min<int64_t>((std::max(n, nnz) + 255) / 256, ctx->nsm * 8)), 256, 0,
+                        ctx->stream>>>(ctx->d_off, ctx->d_adj, n, nnz, bad);
+  PHDE_LAUNCHED(ctx);
+  int h = 0;
+  PHDE_CK(ctx, cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h) {
+    ctx->n = ctx->nnz = 0;
+    return phde_fail(ctx, PHDE_ERR_CSR, "phde_graph_upload: offsets must start at 0, never decrease and end at nnz; "
+                                        "neighbours must be < n");
+  }
+  return PHDE_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, int64_t *sources_out,
+                       phde_layout_extra *extra, phde_layout_stats *st) {
+  const int64_t n = ctx->n;
+  const int k = o->k, c = o->c;
+  const int algo = o->algo;
+  const bool hde = algo == PHDE_ALGO_PARHDE || algo == PHDE_ALGO_WPARHDE;
+  Timer tm(ctx);
+  const long long launches0 = ctx->launches;
+  tm.mark(0);
+  double *deg = (double *)phde_buf(ctx, "deg", sizeof(double) * n);
+  ull *edges = (ull *)phde_buf(ctx, "edges", sizeof(ull));
+  if (!deg || !edges) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(edges, 0, sizeof(ull), ctx->stream));
+  int rc = phde_degrees(ctx, deg);
+  if (rc) return rc;
+
+  const int P = hde ? 3 * k : k;
+  int64_t *d_src = (int64_t *)phde_buf(ctx, "layout.src", sizeof(int64_t) * (P + 2));
+  ull *sumsq = (ull *)phde_buf(ctx, "layout.sumsq", sizeof(ull) * P);
+  double *Sbuf = (double *)phde_buf(ctx, "layout.S", sizeof(double) * n * k);  // S (HDE) or C (MDS), row-major
+  double *M = (double *)phde_buf(ctx, "layout.M", sizeof(double) * k * k);
+  double *K = (double *)phde_buf(ctx, "layout.K", sizeof(double) * k * k);
+  double *ev = (double *)phde_buf(ctx, "layout.ev", sizeof(double) * k);
+  double *Y = (double *)phde_buf(ctx, "layout.Y", sizeof(double) * k * c);
+  if (!d_src || !sumsq || !Sbuf || !M || !K || !ev || !Y) return PHDE_ERR_OOM;
+  int npasses = 0, naccepted = 0, ndiscarded = 0;
+  double ms_dist = 0, ms_orth = 0;
+  const bool random = algo != PHDE_ALGO_WPARHDE && o->strategy != PHDE_STRAT_KCENTERS;
+
+  if (algo == PHDE_ALGO_WPARHDE) {
+    // ---- coupled SSSP + MGS loop (WParHDE.cpp:113-224) ----
+    double *U = (double *)phde_buf(ctx, "wp.U", sizeof(double) * n * (k + 1));
+    int32_t *col = (int32_t *)phde_buf(ctx, "wp.col", sizeof(int32_t) * n);
+    int32_t *min_d = (int32_t *)phde_buf(ctx, "wp.min_d", sizeof(int32_t) * n);
+    int64_t *hist = (int64_t *)phde_buf(ctx, "wp.hist", sizeof(int64_t) * P);
+    int64_t *cur = (int64_t *)phde_buf(ctx, "wp.cur", sizeof(int64_t) * 2);
+    if (!U || !col || !min_d || !hist || !cur) return PHDE_ERR_OOM;
+    if ((rc = phde_const_col(ctx, U))) return rc;
+    if ((rc = phde_fill_i32(ctx, min_d, n, 0x7fffffff))) return rc;
+    PHDE_CK(ctx, cudaMemsetAsync(cur, 0, sizeof(int64_t) * 2, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(sumsq, 0, sizeof(ull) * P, ctx->stream));
+    int correct = 1;
+    for (int r = 0; r < P; r++) {
+      if (correct > k) break;
+      tm.mark(6);
+      PHDE_CK(ctx, cudaMemcpyAsync(d_src + r, cur, sizeof(int64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+      if ((rc = phde_reset_sync(ctx))) return rc;
+      if ((rc = phde_run_sssp(ctx, cur, col, 10000, edges))) return rc;  // delta: WParHDE.cpp:104
+      if ((rc = phde_run_select(ctx, col, min_d, r, correct != 1, hist, cur + 1, sumsq + r))) return rc;
+      PHDE_CK(ctx, cudaMemcpyAsync(cur, cur + 1, sizeof(int64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+      tm.mark(7);
+      double nrm2 = 0;
+      if ((rc = phde_mgs_pass(ctx, col, sumsq + r, U, correct, correct, deg, &nrm2))) return rc;
+      if ((rc = phde_check_device_err(ctx, "WParHDE distance pass"))) return rc;
+      npasses++;
+      ms_dist += tm.ms(6, 7);
+      const double nrm = std::sqrt(nrm2);
+      if (nrm < 0.001) {
+        ndiscarded++;
+        if (o->verbose) printf("discarding vec %d, normdist %g\n", correct, nrm);
+      } else {
+        if ((rc = phde_accept_col(ctx, U, correct, 1.0 / nrm, Sbuf, k, correct - 1))) return rc;
+        correct++;
+      }
+      tm.mark(6);
+      PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+      ms_orth += tm.ms(7, 6);
+    }
+    naccepted = correct - 1;
+    if (naccepted < k)
+      return phde_fail(ctx, PHDE_ERR_TOO_FEW_PIVOTS,
+                       "Number of Pivots obtained: " + std::to_string(naccepted) + " inadequate, increase the Pivots Limits: " +
+                           std::to_string(P));
+    tm.mark(2);
+  } else {
+    // ---- distance phase: Kcenters (or random) BFS passes into D ----
+    int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);
+    if (!D) return PHDE_ERR_OOM;
+    if (random) {
+      std::vector<int32_t> r;
+      glibc_rand_host((uint32_t)o->seed, P, r);
+      std::vector<int64_t> s(P);
+      for (int i = 0; i < P; i++) s[i] = (int64_t)r[i] % n;
+      PHDE_CK(ctx, cudaMemcpyAsync(d_src, s.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, ctx->stream));
+      int64_t *d_src2 = (int64_t *)phde_buf(ctx, "layout.src2", sizeof(int64_t) * P);
+      if (!d_src2) return PHDE_ERR_OOM;
+      // a layout needs every vertex reached: require_all turns an unreached vertex into an error
+      if ((rc = phde_run_bfs_passes(ctx, P, 1, d_src, D, d_src2, sumsq, edges, 1))) return rc;
+    } else {
+      if ((rc = phde_run_bfs_passes(ctx, P, hde ? 0 : 2, nullptr, D, d_src, sumsq, edges, 1))) return rc;
+    }
+    if ((rc = phde_check_device_err(ctx, "distance passes"))) return rc;
+    npasses = P;
+    tm.mark(1);
+    if (hde) {
+      int state[4] = {0, 0, 0, 0};
+      std::vector<double> dlog(P);
+      if ((rc = phde_cgs(ctx, D, P, sumsq, deg, Sbuf, k, state, dlog.data()))) return rc;
+      if ((rc = phde_check_device_err(ctx, "D-orthogonalisation"))) return rc;
+      naccepted = state[0];
+      ndiscarded = state[1];
+      if (o->verbose) {
+        int j = 1;
+        for (int r = 0; r < state[2]; r++) {
+          if (std::isnan(dlog[r]))
+            j++;
+          else
+            printf("discarding vec %d, normdist %g\n", j, dlog[r]);
+        }
+      }
+      if (naccepted < k)
+        return phde_fail(ctx, PHDE_ERR_TOO_FEW_PIVOTS,
+                         "Number of Pivots obtained: " + std::to_string(naccepted) +
+                             " inadequate, increase the Pivots Limits: " + std::to_string(P));
+    } else {
+      if ((rc = phde_centre(ctx, D, k, algo == PHDE_ALGO_PIVOTMDS, Sbuf))) return rc;
+      naccepted = k;
+    }
+    tm.mark(2);
+    PHDE_CK(ctx, cudaEventSynchronize(ctx->ev[2]));
+    ms_dist = tm.ms(0, 1);
+    ms_orth = tm.ms(1, 2);
+  }
+
+  // ---- Laplacian SpMM + Gram (HDE) or C^T C (MDS) ----
+  if (hde) {
+    double *LS = (double *)phde_buf(ctx, "layout.LS", sizeof(double) * n * k);
+    if (!LS) return PHDE_ERR_OOM;
+    if ((rc = phde_lap_spmm(ctx, deg, Sbuf, LS, k))) return rc;
+    if ((rc = phde_gram(ctx, Sbuf, LS, k, M))) return rc;
+  } else {
+    if ((rc = phde_gram(ctx, Sbuf, Sbuf, k, M))) return rc;
+  }
+  tm.mark(3);
+  if (extra && extra->gram)
+    PHDE_CK(ctx, cudaMemcpyAsync(extra->gram, M, sizeof(double) * k * k, cudaMemcpyDeviceToHost, ctx->stream));
+  int iters = 0;
+  if ((rc = phde_eigensolve(ctx, M, k, c, hde ? 0 : 1, o->eig, K, ev, Y, &iters))) return rc;
+  tm.mark(4);
+  double *X = (double *)phde_buf(ctx, "layout.X", sizeof(double) * n * c);
+  if (!X) return PHDE_ERR_OOM;
+  if ((rc = phde_coords(ctx, Sbuf, Y, k, c, X))) return rc;
+  PHDE_CK(ctx, cudaMemcpyAsync(coords_out, X, sizeof(double) * n * c, cudaMemcpyDeviceToHost, ctx->stream));
+  tm.mark(5);
+  if (sources_out && npasses > 0)
+    PHDE_CK(ctx, cudaMemcpyAsync(sources_out, d_src, sizeof(int64_t) * npasses, cudaMemcpyDeviceToHost, ctx->stream));
+  ull h_edges = 0;
+  PHDE_CK(ctx, cudaMemcpyAsync(&h_edges, edges, sizeof(ull), cudaMemcpyDeviceToHost, ctx->stream));
+  if (extra && extra->evecs)
+    PHDE_CK(ctx, cudaMemcpyAsync(extra->evecs, K, sizeof(double) * k * k, cudaMemcpyDeviceToHost, ctx->stream));
+  if (extra && extra->evals)
+    PHDE_CK(ctx, cudaMemcpyAsync(extra->evals, ev, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<double> Srow;
+  if (extra && extra->basis) {
+    Srow.resize((size_t)n * k);
+    PHDE_CK(ctx, cudaMemcpyAsync(Srow.data(), Sbuf, sizeof(double) * n * k, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (extra && extra->basis)
+    for (int64_t i = 0; i < n; i++)
+      for (int q = 0; q < k; q++) extra->basis[i + (int64_t)q * n] = Srow[(size_t)i * k + q];
+  if (st) {
+    st->npasses = npasses;
+    st->naccepted = naccepted;
+    st->ndiscarded = ndiscarded;
+    st->eig_iters = iters;
+    st->ms_dist = ms_dist;
+    st->ms_orth = ms_orth;
+    st->ms_mmult = tm.ms(2, 3);
+    st->ms_eig = tm.ms(3, 4);
+    st->ms_coords = tm.ms(4, 5);
+    st->ms_total = tm.ms(0, 5);
+    st->edges_examined = (int64_t)h_edges;
+    st->gpu_launches = (int)(ctx->launches - launches0);
+  }
+  return PHDE_OK;
+}
+
+int phde_layout(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, int64_t *sources_out,
+                phde_layout_extra *extra, phde_layout_stats *st) {
+  if (st) memset(st, 0, sizeof(*st));
+  if (!ctx || !o || !coords_out) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout: null argument");
+  if (ctx->n <= 0) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_layout: no graph uploaded");
+  if (o->algo < 0 || o->algo > 3) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized algorithm");
+  if (o->strategy < 0 || o->strategy > 2) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized Strategy");
+  if (o->eig != PHDE_EIG_POWER && o->eig != PHDE_EIG_EXACT) return phde_fail(ctx, PHDE_ERR_INVALID, "unknown eigensolver");
+  if (o->precision != PHDE_PREC_FP64 && o->precision != PHDE_PREC_MIXED)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "unknown precision");
+  if (o->k < 1 || o->k > PHDE_MAX_K || o->k >= ctx->n || o->c < 1 || o->c > o->k)
+    return phde_fail(ctx, PHDE_ERR_K_RANGE, "need 1 <= k <= 256, k < n and 1 <= c <= k");
+  if (o->algo == PHDE_ALGO_WPARHDE && !ctx->weighted)
+    return phde_fail(ctx, PHDE_ERR_WEIGHTS, "Weighted ParHDE code requires the weighted edges");
+  if (o->algo != PHDE_ALGO_WPARHDE && ctx->weighted)
+    return phde_fail(ctx, PHDE_ERR_WEIGHTS, "ParHDE code doesn't requires the weighted edges");
+  cudaSetDevice(ctx->device);
+  int rc = layout_impl(ctx, o, coords_out, sources_out, extra, st);
+  if (st) st->status = rc;
+  if (rc != PHDE_OK) cudaStreamSynchronize(ctx->stream);
+  return rc;
+}
+
+int phde_distances(phde_ctx *ctx, const int64_t *sources, int nsrc, int32_t *out) {
+  if (!ctx || !sources || !out || nsrc < 1) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_distances: bad arguments");
+  if (ctx->n <= 0) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_distances: no graph uploaded");
+  for (int i = 0; i < nsrc; i++)
+    if (sources[i] < 0 || sources[i] >= ctx->n) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_distances: source out of range");
+  cudaSetDevice(ctx->device);
+  const int64_t n = ctx->n;
+  int64_t *d_src = (int64_t *)phde_buf(ctx, "dist.src", sizeof(int64_t) * nsrc);
+  int64_t *d_src2 = (int64_t *)phde_buf(ctx, "dist.src2", sizeof(int64_t) * nsrc);
+  ull *sumsq = (ull *)phde_buf(ctx, "dist.sumsq", sizeof(ull) * nsrc);
+  if (!d_src || !d_src2 || !sumsq) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemcpyAsync(d_src, sources, sizeof(int64_t) * nsrc, cudaMemcpyHostToDevice, ctx->stream));
+  int rc;
+  if (!ctx->weighted) {
+    int32_t *D = (int32_t *)phde_buf(ctx, "dist.D", sizeof(int32_t) * n * nsrc);
+    if (!D) return PHDE_ERR_OOM;
+    if ((rc = phde_run_bfs_passes(ctx, nsrc, 1, d_src, D, d_src2, sumsq, nullptr, 0))) return rc;
+    PHDE_CK(ctx, cudaMemcpyAsync(out, D, sizeof(int32_t) * n * nsrc, cudaMemcpyDeviceToHost, ctx->stream));
+    return phde_check_device_err(ctx, "BFS");
+  }
+  int32_t *col = (int32_t *)phde_buf(ctx, "dist.col", sizeof(int32_t) * n);
+  if (!col) return PHDE_ERR_OOM;
+  for (int i = 0; i < nsrc; i++) {
+    if ((rc = phde_run_sssp(ctx, d_src + i, col, 10000, nullptr))) return rc;
+    PHDE_CK(ctx, cudaMemcpyAsync(out + (int64_t)i * n, col, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = phde_check_device_err(ctx, "SSSP"))) return rc;
+  }
+  return PHDE_OK;
+}
+
+int phde_kcenters(phde_ctx *ctx, int passes, int variant, int32_t *dist_out, int64_t *sources_out) {
+  if (!ctx || passes < 1 || !sources_out || (variant != 0 && variant != 2))
+    return phde_fail(ctx, PHDE_ERR_INVALID, "phde_kcenters: bad arguments");
+  if (ctx->n <= 0) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_kcenters: no graph uploaded");
+  cudaSetDevice(ctx->device);
+  const int64_t n = ctx->n;
+  int64_t *d_src = (int64_t *)phde_buf(ctx, "kcx.src", sizeof(int64_t) * (passes + 2));
+  ull *sumsq = (ull *)phde_buf(ctx, "kcx.sumsq", sizeof(ull) * passes);
+  if (!d_src || !sumsq) return PHDE_ERR_OOM;
+  int rc;
+  if (!ctx->weighted) {
+    int32_t *D = (int32_t *)phde_buf(ctx, "kcx.D", sizeof(int32_t) * n * passes);
+    if (!D) return PHDE_ERR_OOM;
+    if ((rc = phde_run_bfs_passes(ctx, passes, variant, nullptr, D, d_src, sumsq, nullptr, 1))) return rc;
+    if (dist_out) PHDE_CK(ctx, cudaMemcpyAsync(dist_out, D, sizeof(int32_t) * n * passes, cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    int32_t *col = (int32_t *)phde_buf(ctx, "kcx.col", sizeof(int32_t) * n);
+    int32_t *min_d = (int32_t *)phde_buf(ctx, "kcx.min_d", sizeof(int32_t) * n);
+    int64_t *hist = (int64_t *)phde_buf(ctx, "kcx.hist", sizeof(int64_t) * passes);
+    int64_t *cur = (int64_t *)phde_buf(ctx, "kcx.cur", sizeof(int64_t) * 2);
+    if (!col || !min_d || !hist || !cur) return PHDE_ERR_OOM;
+    if ((rc = phde_fill_i32(ctx, min_d, n, 0x7fffffff))) return rc;
+    PHDE_CK(ctx, cudaMemsetAsync(cur, 0, sizeof(int64_t) * 2, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(sumsq, 0, sizeof(ull) * passes, ctx->stream));
+    for (int r = 0; r < passes; r++) {
+      PHDE_CK(ctx, cudaMemcpyAsync(d_src + r, cur, sizeof(int64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+      if ((rc = phde_run_sssp(ctx, cur, col, 10000, nullptr))) return rc;
+      if ((rc = phde_run_select(ctx, col, min_d, r, r != 0, hist, cur + 1, sumsq + r))) return rc;
+      PHDE_CK(ctx, cudaMemcpyAsync(cur, cur + 1, sizeof(int64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+      if (dist_out)
+        PHDE_CK(ctx, cudaMemcpyAsync(dist_out + (int64_t)r * n, col, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+  }
+  PHDE_CK(ctx, cudaMemcpyAsync(sources_out, d_src, sizeof(int64_t) * passes, cudaMemcpyDeviceToHost, ctx->stream));
+  return phde_check_device_err(ctx, "Kcenters");
+}
+
+// ---- reference-shaped distance drop-ins ----
+static thread_local phde_ctx *g_default_ctx = nullptr;
+
+static phde_ctx *default_ctx() {
+  if (!g_default_ctx) {
+    int dev = 0;
+    if (const char *d = getenv("PHDE_DEVICE")) dev = atoi(d);
+    if (phde_create(&g_default_ctx, dev) != PHDE_OK) g_default_ctx = nullptr;
+  }
+  return g_default_ctx;
+}
+
+int phde_DOBFS(const uint32_t *row, const uint32_t *col, long source, long numNodes, long numEdges, double *dists,
+               int alpha, int beta) {
+  (void)alpha;
+  (void)beta;
+  phde_ctx *ctx = default_ctx();
+  if (!ctx) return PHDE_ERR_CUDA;
+  if (!dists || source < 0 || source >= numNodes) return PHDE_ERR_INVALID;
+  int rc = phde_graph_upload(ctx, row, 4, col, nullptr, numNodes, numEdges);
+  if (rc) return rc;
+  std::vector<int32_t> d((size_t)numNodes);
+  int64_t s = source;
+  if ((rc = phde_distances(ctx, &s, 1, d.data()))) return rc;
+  for (long v = 0; v < numNodes; v++)
+    if (d[v] >= 0) dists[v] = (double)d[v];  // unreached entries are left as they were (bfs.cc:144-185)
+  return PHDE_OK;
+}
+
+int phde_DeltaStep(const uint32_t *row, const uint32_t *col, const int32_t *weights, long source, long numNodes,
+                   long numEdges, double *dist, int32_t delta) {
+  (void)delta;
+  phde_ctx *ctx = default_ctx();
+  if (!ctx) return PHDE_ERR_CUDA;
+  if (!dist || !weights || source < 0 || source >= numNodes) return PHDE_ERR_INVALID;
+  int rc = phde_graph_upload(ctx, row, 4, col, weights, numNodes, numEdges);
+  if (rc) return rc;
+  std::vector<int32_t> d((size_t)numNodes);
+  int64_t s = source;
+  if ((rc = phde_distances(ctx, &s, 1, d.data()))) return rc;
+  for (long v = 0; v < numNodes; v++) dist[v] = (double)d[v];  // every entry, kDistInf when unreached (sssp.cc:137-139)
+  return PHDE_OK;
+}
+
+int phde_selftest_barrier_timeout(phde_ctx *ctx, int timeout_ms) {
+  if (!ctx || timeout_ms < 1 || timeout_ms > 10000) return PHDE_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  int rc = phde_reset_sync(ctx);
+  if (rc) return rc;
+  barrier_timeout_kernel<<<1, 32, 0, ctx->stream>>>(ctx->d_sync, ctx->d_err, (uint64_t)timeout_ms * 1000000ull);
+  PHDE_LAUNCHED(ctx);
+  int e = 0;
+  PHDE_CK(ctx, cudaMemcpyAsync(&e, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if ((rc = phde_reset_sync(ctx))) return rc;
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return e;
+}
+
+}  // extern "C"

@@ -1,0 +1,191 @@
+// common.cuh -- device helpers shared by the layout kernels (sm_103a).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "parhde.h"
+
+#define PHDE_FULL_MASK 0xffffffffu
+
+typedef unsigned long long ull;
+
+// ---------------------------------------------------------------------------------------------
+// Grid-wide barrier for cooperative launches.
+//
+// Every wait is bounded: the waiting thread gives up after `timeout_ns` of %globaltimer, records
+// PHDE_ERR_TIMEOUT in the kernel's error word and returns false; a block that sees any error word
+// also returns false.  Callers leave the kernel on false, so a kernel can never spin forever.
+// Memory ordering: all threads' writes are ordered before thread 0's release (bar.sync, then a
+// gpu-scope fence and an acq_rel arrival); after the generation flips, thread 0 acquires and the
+// block's threads are ordered after it by the closing bar.sync.
+struct GridSync {
+  unsigned int count;
+  unsigned int gen;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned *p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ int ld_volatile_i32(const int *p) { return *(const volatile int *)p; }
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// `expected` is the number of blocks that must arrive (gridDim.x for a real barrier).
+__device__ __forceinline__ bool grid_barrier(GridSync *gs, int *err, uint64_t timeout_ns, unsigned expected) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned gen = ld_acquire_u32(&gs->gen);
+    __threadfence();
+    unsigned arrived = atom_add_acq_rel_u32(&gs->count, 1u);
+    if (arrived == expected - 1) {
+      gs->count = 0;
+      __threadfence();
+      st_release_u32(&gs->gen, gen + 1);
+    } else {
+      uint64_t t0 = global_timer_ns();
+      unsigned spins = 0;
+      while (ld_acquire_u32(&gs->gen) == gen) {
+        if (ld_volatile_i32(err) != 0) {
+          ok = 0;
+          break;
+        }
+        if ((++spins & 15u) == 0 && global_timer_ns() - t0 > timeout_ns) {
+          atomicCAS(err, 0, PHDE_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (ok && ld_volatile_i32(err) != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_sync(GridSync *gs, int *err, uint64_t timeout_ns) {
+  return grid_barrier(gs, err, timeout_ns, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Reductions.
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(PHDE_FULL_MASK, v, o);
+  return v;
+}
+
+__device__ __forceinline__ ull warp_max_u64(ull v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ull w = __shfl_xor_sync(PHDE_FULL_MASK, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+// Block sum of one value per thread; result valid in every thread.  `scratch` holds >= 32 entries.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T *scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  T r = 0;
+  for (int w = 0; w < nw; w++) r += scratch[w];  // fixed order: deterministic
+  return r;
+}
+
+__device__ __forceinline__ ull block_max_u64(ull v, ull *scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_max_u64(v);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  ull r = 0;
+  for (int w = 0; w < nw; w++) r = scratch[w] > r ? scratch[w] : r;
+  return r;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Block-aggregated append to a frontier queue.  Each flagged thread appends vertex v with out-degree
+// dv.  One 64-bit atomic per block advances both the slot count (high 32 bits) and the running edge
+// total (low 32 bits), so the start-edge array qe[] is non-decreasing in slot order -- that is what
+// lets the next top-down step find the owner of an edge by binary search.  Edge totals stay below
+// 2^32 because nnz < 2^32 (uint32 adjacency).  Must be called by every thread of the block.
+struct PushScratch {
+  ull warp_tot[32];
+  ull base;
+};
+
+__device__ __forceinline__ void block_push(bool flag, uint32_t v, uint32_t dv, uint32_t *qv, uint32_t *qe, ull *ctr,
+                                           PushScratch *sc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const ull mine = flag ? ((1ull << 32) | (ull)dv) : 0ull;
+  ull x = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    ull y = __shfl_up_sync(PHDE_FULL_MASK, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sc->warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    ull w = lane < nw ? sc->warp_tot[lane] : 0ull;
+    ull incl = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      ull y = __shfl_up_sync(PHDE_FULL_MASK, incl, o);
+      if (lane >= o) incl += y;
+    }
+    ull total = __shfl_sync(PHDE_FULL_MASK, incl, 31);
+    if (lane < nw) sc->warp_tot[lane] = incl - w;  // exclusive prefix per warp
+    if (lane == 0) sc->base = total ? atomicAdd(ctr, total) : 0ull;
+  }
+  __syncthreads();
+  if (flag) {
+    ull pos = sc->base + sc->warp_tot[warp] + (x - mine);
+    uint32_t slot = (uint32_t)(pos >> 32);
+    qv[slot] = v;
+    qe[slot] = (uint32_t)(pos & 0xffffffffull);
+  }
+  __syncthreads();
+}
+
+// Largest index s in [0, f) with qe[s] <= e (qe non-decreasing, qe[0] == 0).
+__device__ __forceinline__ uint32_t owner_slot(const uint32_t *qe, uint32_t f, uint32_t e) {
+  uint32_t lo = 0, hi = f;  // invariant: qe[lo] <= e, answer in [lo, hi)
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (qe[mid] <= e)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host-side helpers.
+struct LaunchCounter {
+  long long n = 0;
+};

@@ -1,0 +1,76 @@
+// ctx.h -- the library context (one CUDA stream, the uploaded graph, grow-only device workspace).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+
+#include "common.cuh"
+#include "parhde.h"
+
+struct phde_ctx {
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long long launches = 0;
+  uint64_t timeout_ns = 5000000000ull;  // bounded device waits: 5 s per wait
+
+  // uploaded graph (offsets widened to int64)
+  int64_t n = 0, nnz = 0;
+  bool weighted = false;
+  int64_t *d_off = nullptr;
+  uint32_t *d_adj = nullptr;
+  int32_t *d_w = nullptr;
+
+  // device control block for persistent kernels: barrier + error word
+  GridSync *d_sync = nullptr;
+  int *d_err = nullptr;
+
+  std::map<std::string, std::pair<void *, size_t>> ws;
+  cudaEvent_t ev[8] = {};
+};
+
+// Set the context error message and return `status`.
+int phde_fail(phde_ctx *ctx, int status, const std::string &msg);
+
+// Grow-only named device buffer; returns nullptr on allocation failure (ctx->err set).
+void *phde_buf(phde_ctx *ctx, const char *name, size_t bytes);
+
+#define PHDE_CK(ctx, call)                                                                      \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return phde_fail((ctx), e_ == cudaErrorMemoryAllocation ? PHDE_ERR_OOM : PHDE_ERR_CUDA, \
+                       std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+  } while (0)
+
+// After a launch: count it and surface launch-configuration errors.
+#define PHDE_LAUNCHED(ctx)                                                                                  \
+  do {                                                                                                      \
+    (ctx)->launches++;                                                                                      \
+    cudaError_t e_ = cudaGetLastError();                                                                    \
+    if (e_ != cudaSuccess)                                                                                  \
+      return phde_fail((ctx), PHDE_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Reset the device error word and barrier before a persistent kernel.
+int phde_reset_sync(phde_ctx *ctx);
+// Read the device error word after the stream drained; returns PHDE_OK or the recorded status.
+int phde_check_device_err(phde_ctx *ctx, const char *what);
+
+// ---- kernels (kcenters.cu) ----
+// Kcenters / fixed-source BFS passes into D (n * P int32, column-major).  variant: 0 ParHDE history
+// rule, 1 fixed sources (no selection; unreached vertices allowed), 2 DrawingBase history rule.
+// require_all: an unreached vertex is an error (PHDE_ERR_DISCONNECTED); otherwise it keeps distance -1.
+int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixed_src, int32_t *d_D,
+                        int64_t *d_sources, unsigned long long *d_sumsq, unsigned long long *d_edges, int require_all);
+
+// ---- kernels (sssp.cu) ----
+// One exact SSSP pass from *d_src into d_col (int32, INF = INT32_MAX/2 for unreachable).
+int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t delta, unsigned long long *d_edges);
+// Kcenters selection for one WParHDE pass (WParHDE.cpp:117-153): fold d_col into d_min, choose the
+// next source into *d_next_src, append the raw argmax to the history, add sum(d^2) into *d_sumsq.
+int phde_run_select(phde_ctx *ctx, const int32_t *d_col, int32_t *d_min, int pass, int check_fix, int64_t *d_hist,
+                    int64_t *d_next_src, unsigned long long *d_sumsq);

@@ -1,0 +1,625 @@
+// dense.cu -- the dense stages of the layout pipeline in FP64 (the reference's arithmetic).
+//
+//   cgs_kernel        ParHDE D-orthogonalisation (ParHDE.cpp:190-285): one persistent cooperative launch
+//                     runs the whole candidate loop -- coefficient dots, projection update, norm test and
+//                     acceptance -- with device-side control, so no host round trip per candidate.
+//   mgs_step_kernel   WParHDE modified Gram-Schmidt step (WParHDE.cpp:167-190), fused: apply step q-1's
+//                     projection and accumulate step q's dot products in the same sweep.
+//   lap_spmm_kernel   LS = D*S - A*S (ParHDE.cpp:288-300, WParHDE.cpp:229-241): one warp per row, lanes
+//                     across the k columns of a row-major S, neighbours in CSR order with separate
+//                     multiply/subtract roundings -- the reference's exact operation sequence.
+//   gram_kernel       C = A^T B for row-major n x k operands (matrixTransMultiplication,
+//                     DrawingBase.cpp:221-244): 64x64 output tiles, split over row ranges, partials summed
+//                     in a fixed order.
+//   centring kernels  PivotMDS double centring (PivotMDS.cpp:30-66) and PHDE column centring
+//                     (PHDE.cpp:30-47) from exact integer sums.
+//   coords kernels    X = M * Y (DrawingBase.cpp:207-219) and the unit-norm scaling of getCoordinates
+//                     (DrawingBase.cpp:196-205).
+// Layout: S, LS and C are row-major n x k (a row is one vertex's k values, so the SpMM's neighbour
+// gathers are contiguous k-vectors); distance columns are column-major n x P int32.
+#include <vector>
+
+#include "ctx.h"
+
+namespace {
+
+constexpr int CGS_THREADS = 512;
+constexpr int MAXQ = 8;  // columns per lane: k <= 256
+
+// ------------------------------------------------------------------------------------------------
+struct CgsArgs {
+  const int32_t *D;
+  int64_t n;
+  int P;
+  const ull *sumsq;
+  const double *deg;
+  double *S;  // row-major n x k
+  int k;
+  double *X;       // [n] projected candidate
+  double *part;    // [gridDim][k+2]
+  double *part2;   // [gridDim]
+  double *coef;    // [k+1]
+  double *inv_den; // [k+1], slot k = the constant column
+  int *state;      // [0] accepted, [1] discarded, [2] candidates examined
+  double *dlog;    // [P] norm of every discarded candidate (NaN otherwise)
+  GridSync *gs;
+  int *err;
+  uint64_t timeout_ns;
+};
+
+__global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
+  extern __shared__ double sm[];  // [nwarps][k+2]
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t n = a.n;
+  const int k = a.k, ld = k + 2;
+  const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
+  const double inv0 = 1.0 / sqrt((double)n);  // the constant column: 1 * (1/||1||), ParHDE.cpp:96-108
+
+  // denominator of the constant column, sum_i u0*u0*d_i
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += __dmul_rn(__dmul_rn(inv0, inv0), a.deg[i]);
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) a.part2[blockIdx.x] = acc;
+  if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+  double den0 = 0;
+  for (int b = 0; b < (int)gridDim.x; b++) den0 += __ldcg(a.part2 + b);
+  const double inv_den0 = 1.0 / den0;
+  if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+
+  int j = 1, ndisc = 0, ncand = 0;
+  bool newcol = false;
+  for (int rc = 0; rc < a.P; rc++) {
+    if (j > k) break;
+    ncand++;
+    const int32_t *Dc = a.D + (int64_t)rc * n;
+    const double inv_rc = 1.0 / sqrt((double)__ldcg(a.sumsq + rc));  // ParHDE.cpp:179-184
+    const int jm1 = j - 1;
+    // ---- A: dots against the accepted columns and the constant column ----
+    double accq[MAXQ];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) accq[t] = 0;
+    double acc0 = 0, accd = 0;
+    for (int64_t i = gw; i < n; i += gws) {
+      const double x = __dmul_rn((double)Dc[i], inv_rc);
+      const double di = a.deg[i];
+      const double *Si = a.S + i * k;
+#pragma unroll
+      for (int t = 0; t < MAXQ; t++) {
+        const int q = lane + 32 * t;
+        if (q < jm1) accq[t] += __dmul_rn(__dmul_rn(x, __ldcg(Si + q)), di);
+      }
+      if (lane == 0) {
+        acc0 += __dmul_rn(__dmul_rn(x, inv0), di);
+        if (newcol) {
+          const double s = __ldcg(Si + (j - 2));
+          accd += __dmul_rn(__dmul_rn(s, s), di);
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < jm1) sm[warp * ld + q] = accq[t];
+    }
+    if (lane == 0) {
+      sm[warp * ld + k] = acc0;
+      sm[warp * ld + k + 1] = accd;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < k + 2; q += blockDim.x) {
+      if (q < jm1 || q >= k) {
+        double s = 0;
+        for (int w = 0; w < nw; w++) s += sm[w * ld + q];
+        a.part[(int64_t)blockIdx.x * ld + q] = s;
+      }
+    }
+    if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    // ---- C: one block per coefficient sums the block partials in a fixed order ----
+    for (int q = blockIdx.x; q < j; q += gridDim.x) {
+      const int slot = q == jm1 ? k : q;  // q == j-1 stands for the constant column
+      double s = 0, sd = 0;
+      for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        s += __ldcg(a.part + (int64_t)b * ld + slot);
+        if (newcol && q == j - 2) sd += __ldcg(a.part + (int64_t)b * ld + k + 1);
+      }
+      s = block_sum(s, red);
+      if (newcol && q == j - 2) {
+        sd = block_sum(sd, red);
+        if (threadIdx.x == 0) a.inv_den[q] = 1.0 / sd;
+      }
+      if (threadIdx.x == 0) {
+        const double id = slot == k ? inv_den0 : (newcol && q == j - 2 ? 1.0 / sd : __ldcg(a.inv_den + q));
+        a.coef[slot] = __dmul_rn(s, id);
+      }
+      __syncthreads();
+    }
+    if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    // ---- E: x' = x - (sum_q coef_q S_q + coef_0 u0), and its squared norm ----
+    double cq[MAXQ];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      cq[t] = q < jm1 ? __ldcg(a.coef + q) : 0.0;
+    }
+    const double c0 = __ldcg(a.coef + k);
+    double ssq = 0;
+    for (int64_t i = gw; i < n; i += gws) {
+      const double x = __dmul_rn((double)Dc[i], inv_rc);
+      const double *Si = a.S + i * k;
+      double part = 0;
+#pragma unroll
+      for (int t = 0; t < MAXQ; t++) {
+        const int q = lane + 32 * t;
+        if (q < jm1) part += __dmul_rn(cq[t], __ldcg(Si + q));
+      }
+      part = warp_sum(part);
+      if (lane == 0) {
+        const double xp = __dsub_rn(x, __dadd_rn(part, __dmul_rn(c0, inv0)));
+        a.X[i] = xp;
+        ssq += __dmul_rn(xp, xp);
+      }
+    }
+    ssq = block_sum(ssq, red);
+    if (threadIdx.x == 0) a.part2[blockIdx.x] = ssq;
+    if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    // ---- G: norm test (ParHDE.cpp:267) and acceptance ----
+    double nrm2 = 0;
+    for (int b = 0; b < (int)gridDim.x; b++) nrm2 += __ldcg(a.part2 + b);
+    const double nrm = sqrt(nrm2);
+    if (nrm < 0.001) {
+      ndisc++;
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.dlog[rc] = nrm;
+      newcol = false;
+    } else {
+      const double scale = 1.0 / nrm;
+      for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a.S[i * k + (j - 1)] = __dmul_rn(__ldcg(a.X + i), scale);
+      j++;
+      newcol = true;
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.state[0] = j - 1;
+    a.state[1] = ndisc;
+    a.state[2] = ncand;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// WParHDE MGS step q over column-major U (n x (k+1)).  If q > 0 the block first sums step q-1's partials
+// (fixed order) and applies x -= (num * y_{q-1}) * (1/den) (WParHDE.cpp:184-188).  If q < jcount it then
+// accumulates step q's partials den = sum y_q*(y_q*d), num = sum x*(y_q*d) (WParHDE.cpp:176-181); at
+// q == jcount it accumulates sum x^2 instead (the norm test, WParHDE.cpp:195-197).
+__global__ void mgs_step_kernel(double *U, int64_t n, int xcol, int q, int jcount, const double *deg,
+                                const double *part_in, double *part_out, int nparts_in) {
+  __shared__ double red[32];
+  __shared__ double s_num, s_dinv;
+  double *x = U + (int64_t)xcol * n;
+  if (q > 0) {
+    if (threadIdx.x == 0) {
+      double num = 0, den = 0;
+      for (int b = 0; b < nparts_in; b++) {
+        den += part_in[2 * b];
+        num += part_in[2 * b + 1];
+      }
+      s_num = num;
+      s_dinv = 1.0 / den;
+    }
+    __syncthreads();
+  }
+  const double num = q > 0 ? s_num : 0.0, dinv = q > 0 ? s_dinv : 0.0;
+  const double *yp = q > 0 ? U + (int64_t)(q - 1) * n : U;
+  const double *y = U + (int64_t)q * n;
+  double a0 = 0, a1 = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double xi = x[i];
+    if (q > 0) {
+      xi = __dsub_rn(xi, __dmul_rn(__dmul_rn(num, yp[i]), dinv));
+      x[i] = xi;
+    }
+    if (q < jcount) {
+      const double dy = __dmul_rn(y[i], deg[i]);
+      a0 += __dmul_rn(y[i], dy);
+      a1 += __dmul_rn(xi, dy);
+    } else {
+      a0 += __dmul_rn(xi, xi);
+    }
+  }
+  a0 = block_sum(a0, red);
+  a1 = block_sum(a1, red);
+  if (threadIdx.x == 0) {
+    part_out[2 * blockIdx.x] = a0;
+    part_out[2 * blockIdx.x + 1] = a1;
+  }
+}
+
+// x = col * (1/sqrt(sumsq)) into U column xcol (WParHDE.cpp:154-162)
+__global__ void normalise_col_kernel(const int32_t *col, const ull *sumsq, double *U, int64_t n, int xcol) {
+  const double inv = 1.0 / sqrt((double)*sumsq);
+  double *x = U + (int64_t)xcol * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = __dmul_rn((double)col[i], inv);
+}
+
+// Accept: x *= 1/nrm, copy into row-major S column j-1 (WParHDE.cpp:205-213).
+__global__ void accept_col_kernel(double *U, int64_t n, int xcol, double scale, double *S, int k, int scol) {
+  double *x = U + (int64_t)xcol * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = __dmul_rn(x[i], scale);
+    x[i] = v;
+    S[i * k + scol] = v;
+  }
+}
+
+__global__ void const_col_kernel(double *U, int64_t n) {
+  const double inv0 = 1.0 / sqrt((double)n);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    U[i] = inv0;
+}
+
+// ------------------------------------------------------------------------------------------------
+__global__ void degrees_kernel(const int64_t *off, const int32_t *w, int64_t n, double *deg) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (w == nullptr) {
+      deg[i] = (double)(off[i + 1] - off[i]);  // ParHDE.cpp:58-59
+    } else {
+      double d = 0;  // WParHDE.cpp:53-58: summed in CSR order
+      for (int64_t e = off[i]; e < off[i + 1]; e++) d = __dadd_rn(d, (double)w[e]);
+      deg[i] = d;
+    }
+  }
+}
+
+// LS[i,q] = d_i*S[i,q] - sum_{e in row i} w_e*S[adj_e,q], neighbours in CSR order.
+__global__ void lap_spmm_kernel(const int64_t *off, const uint32_t *adj, const int32_t *w, const double *deg,
+                                const double *S, double *LS, int64_t n, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < n; i += gws) {
+    const double di = deg[i];
+    double acc[MAXQ];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      acc[t] = q < k ? __dmul_rn(di, S[i * k + q]) : 0.0;
+    }
+    const int64_t e0 = off[i], e1 = off[i + 1];
+    for (int64_t e = e0; e < e1; e++) {
+      const int64_t v = __ldg(adj + e);
+      const double *Sv = S + v * k;
+      if (w == nullptr) {
+#pragma unroll
+        for (int t = 0; t < MAXQ; t++) {
+          const int q = lane + 32 * t;
+          if (q < k) acc[t] = __dsub_rn(acc[t], Sv[q]);
+        }
+      } else {
+        const double we = (double)__ldg(w + e);
+#pragma unroll
+        for (int t = 0; t < MAXQ; t++) {
+          const int q = lane + 32 * t;
+          if (q < k) acc[t] = __dsub_rn(acc[t], __dmul_rn(we, Sv[q]));
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) LS[i * k + q] = acc[t];
+    }
+  }
+}
+
+// Partial C = A^T B over one row range.  Block (16,16) computes a 64x64 output tile (4x4 per thread).
+// grid = (tiles_p * tiles_q, splits).  part: [splits][k*k] column-major (entry (p,q) at q + p*k, the
+// reference's C[k + i*mdim] layout).
+constexpr int GT = 64, GR = 16;
+__global__ void __launch_bounds__(256) gram_kernel(const double *A, const double *B, int64_t n, int k,
+                                                   double *part) {
+  __shared__ double sA[GR][GT + 1];
+  __shared__ double sB[GR][GT + 1];
+  const int tiles = (k + GT - 1) / GT;
+  const int tp = blockIdx.x / tiles, tq = blockIdx.x % tiles;
+  const int p0 = tp * GT, q0 = tq * GT;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t rows_per = (n + gridDim.y - 1) / gridDim.y;
+  const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+  const int64_t r1 = min(n, r0 + rows_per);
+  double acc[4][4] = {};
+  for (int64_t rb = r0; rb < r1; rb += GR) {
+    for (int idx = threadIdx.x; idx < GR * GT; idx += 256) {
+      const int rr = idx / GT, cc = idx % GT;
+      const int64_t r = rb + rr;
+      sA[rr][cc] = (r < r1 && p0 + cc < k) ? A[r * k + p0 + cc] : 0.0;
+      sB[rr][cc] = (r < r1 && q0 + cc < k) ? B[r * k + q0 + cc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < GR; rr++) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        av[u] = sA[rr][ty + 16 * u];
+        bv[u] = sB[rr][tx + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] = fma(av[u], bv[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  double *out = part + (int64_t)blockIdx.y * k * k;
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const int p = p0 + ty + 16 * u, q = q0 + tx + 16 * v;
+      if (p < k && q < k) out[q + (int64_t)p * k] = acc[u][v];
+    }
+}
+
+__global__ void sum_parts_kernel(const double *part, int splits, int64_t len, double *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int b = 0; b < splits; b++) s += part[(int64_t)b * len + i];
+    out[i] = s;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Exact integer sums of the raw distance columns: colsq[q] = sum_i d^2, colsum[q] = sum_i d, and
+// rowsq[i] = sum_q d^2 (exact in FP64 for BFS distances).
+__global__ void dist_sums_kernel(const int32_t *D, int64_t n, int k, ull *colsq, ull *colsum, double *rowsq) {
+  __shared__ ull red[32];
+  for (int q = 0; q < k; q++) {
+    ull s2 = 0, s1 = 0;
+    const int32_t *col = D + (int64_t)q * n;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      const ull d = (ull)col[i];
+      s2 += d * d;
+      s1 += d;
+    }
+    s2 = block_sum(s2, red);
+    s1 = block_sum(s1, red);
+    if (threadIdx.x == 0) {
+      atomicAdd(colsq + q, s2);
+      atomicAdd(colsum + q, s1);
+    }
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double r = 0;
+    for (int q = 0; q < k; q++) {
+      const double d = (double)D[i + (int64_t)q * n];
+      r = __dadd_rn(r, __dmul_rn(d, d));
+    }
+    rowsq[i] = r;
+  }
+}
+
+// C[i,q] = -0.5*(d^2 - rN*colsum_q - rK*rowsum_i + rK*rN*total) (PivotMDS.cpp:42-53), or for PHDE
+// C[i,q] = d - colsum_q/n (PHDE.cpp:32-46).  Row-major output.
+__global__ void centre_kernel(const int32_t *D, int64_t n, int k, const ull *colsq, const ull *colsum,
+                              const double *rowsq, int pivotmds, double *C) {
+  double total = 0;
+  for (int q = 0; q < k; q++) total = __dadd_rn(total, (double)colsq[q]);
+  const double rN = 1.0 / (double)n, rK = 1.0 / (double)k;
+  const double t4 = __dmul_rn(__dmul_rn(rK, rN), total);
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / k;
+    const int q = (int)(idx % k);
+    const double d = (double)D[i + (int64_t)q * n];
+    double v;
+    if (pivotmds) {
+      const double t = __dadd_rn(__dsub_rn(__dsub_rn(__dmul_rn(d, d), __dmul_rn(rN, (double)colsq[q])),
+                                           __dmul_rn(rK, rowsq[i])),
+                                 t4);
+      v = __dmul_rn(-0.5, t);
+    } else {
+      v = __dsub_rn(d, __ddiv_rn((double)colsum[q], (double)n));
+    }
+    C[idx] = v;
+  }
+}
+
+// X[i + t*n] = sum_q M[i,q] * Y[q + t*k]; per-block partial sums of squares per coordinate.
+__global__ void coords_kernel(const double *M, const double *Y, int64_t n, int k, int c, double *X,
+                              double *part) {
+  extern __shared__ double sm[];  // [nwarps][c]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
+  for (int t = 0; t < c; t++) {
+    double ss = 0;
+    for (int64_t i = gw; i < n; i += gws) {
+      double s = 0;
+      for (int q = lane; q < k; q += 32) s += __dmul_rn(M[i * k + q], Y[q + (int64_t)t * k]);
+      s = warp_sum(s);
+      if (lane == 0) {
+        X[i + (int64_t)t * n] = s;
+        ss += __dmul_rn(s, s);
+      }
+    }
+    if (lane == 0) sm[warp * c + t] = ss;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < c; t += blockDim.x) {
+    double s = 0;
+    for (int w = 0; w < nw; w++) s += sm[w * c + t];
+    part[(int64_t)blockIdx.x * c + t] = s;
+  }
+}
+
+__global__ void scale_coords_kernel(double *X, int64_t n, int c, const double *part, int nparts) {
+  __shared__ double inv[PHDE_MAX_K];
+  for (int t = threadIdx.x; t < c; t += blockDim.x) {
+    double s = 0;
+    for (int b = 0; b < nparts; b++) s += part[(int64_t)b * c + t];
+    inv[t] = 1.0 / sqrt(s);
+  }
+  __syncthreads();
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * c;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    X[idx] = __dmul_rn(X[idx], inv[idx / n]);
+}
+
+}  // namespace
+
+// ==================================================================================================
+// host launchers
+int phde_reset_sync(phde_ctx *ctx);
+
+static int grid_for(phde_ctx *ctx, int64_t work, int threads, int per_sm = 8) {
+  int64_t b = (work + threads - 1) / threads;
+  b = std::min<int64_t>(b, (int64_t)ctx->nsm * per_sm);
+  return (int)std::max<int64_t>(b, 1);
+}
+
+int phde_degrees(phde_ctx *ctx, double *deg) {
+  degrees_kernel<<<grid_for(ctx, ctx->n, 256), 256, 0, ctx->stream>>>(ctx->d_off, ctx->weighted ? ctx->d_w : nullptr,
+                                                                      ctx->n, deg);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// ParHDE CGS: candidates are the P distance columns of D; accepted vectors go to row-major S.
+int phde_cgs(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, double *S, int k,
+             int *h_state, double *h_dlog) {
+  const int64_t n = ctx->n;
+  int per_sm = 0;
+  const size_t smem = sizeof(double) * (CGS_THREADS / 32) * (size_t)(k + 2);
+  PHDE_CK(ctx, cudaFuncSetAttribute(cgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cgs_kernel, CGS_THREADS, smem));
+  if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "cgs kernel cannot be resident");
+  per_sm = std::min(per_sm, 2);
+  const int grid = ctx->nsm * per_sm;
+  double *X = (double *)phde_buf(ctx, "cgs.X", sizeof(double) * n);
+  double *part = (double *)phde_buf(ctx, "cgs.part", sizeof(double) * grid * (size_t)(k + 2));
+  double *part2 = (double *)phde_buf(ctx, "cgs.part2", sizeof(double) * grid);
+  double *coef = (double *)phde_buf(ctx, "cgs.coef", sizeof(double) * (k + 1));
+  double *inv_den = (double *)phde_buf(ctx, "cgs.inv_den", sizeof(double) * (k + 1));
+  int *state = (int *)phde_buf(ctx, "cgs.state", sizeof(int) * 4);
+  double *dlog = (double *)phde_buf(ctx, "cgs.dlog", sizeof(double) * P);
+  if (!X || !part || !part2 || !coef || !inv_den || !state || !dlog) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(dlog, 0xff, sizeof(double) * P, ctx->stream));  // NaN: not discarded
+  PHDE_CK(ctx, cudaMemsetAsync(state, 0, sizeof(int) * 4, ctx->stream));
+  int rc = phde_reset_sync(ctx);
+  if (rc) return rc;
+  CgsArgs a;
+  a.D = D;
+  a.n = n;
+  a.P = P;
+  a.sumsq = sumsq;
+  a.deg = deg;
+  a.S = S;
+  a.k = k;
+  a.X = X;
+  a.part = part;
+  a.part2 = part2;
+  a.coef = coef;
+  a.inv_den = inv_den;
+  a.state = state;
+  a.dlog = dlog;
+  a.gs = ctx->d_sync;
+  a.err = ctx->d_err;
+  a.timeout_ns = ctx->timeout_ns;
+  void *args[] = {&a};
+  PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)cgs_kernel, dim3(grid), dim3(CGS_THREADS), args, smem,
+                                           ctx->stream));
+  PHDE_LAUNCHED(ctx);
+  PHDE_CK(ctx, cudaMemcpyAsync(h_state, state, sizeof(int) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaMemcpyAsync(h_dlog, dlog, sizeof(double) * P, cudaMemcpyDeviceToHost, ctx->stream));
+  return PHDE_OK;
+}
+
+// WParHDE: normalise the new distance column into U column xcol and run MGS against columns
+// 0..jcount-1; returns the squared norm of the projected vector in *h_nrm2 (synchronises).
+int phde_mgs_pass(phde_ctx *ctx, const int32_t *col, const ull *sumsq, double *U, int xcol, int jcount,
+                  const double *deg, double *h_nrm2) {
+  const int64_t n = ctx->n;
+  const int threads = 512;
+  const int grid = grid_for(ctx, n, threads, 2);
+  double *pa = (double *)phde_buf(ctx, "mgs.pa", sizeof(double) * 2 * grid);
+  double *pb = (double *)phde_buf(ctx, "mgs.pb", sizeof(double) * 2 * grid);
+  if (!pa || !pb) return PHDE_ERR_OOM;
+  normalise_col_kernel<<<grid, threads, 0, ctx->stream>>>(col, sumsq, U, n, xcol);
+  PHDE_LAUNCHED(ctx);
+  for (int q = 0; q <= jcount; q++) {
+    double *pin = (q & 1) ? pa : pb, *pout = (q & 1) ? pb : pa;
+    mgs_step_kernel<<<grid, threads, 0, ctx->stream>>>(U, n, xcol, q, jcount, deg, pin, pout, grid);
+    PHDE_LAUNCHED(ctx);
+  }
+  double *pfinal = (jcount & 1) ? pb : pa;
+  std::vector<double> h(2 * grid);
+  PHDE_CK(ctx, cudaMemcpyAsync(h.data(), pfinal, sizeof(double) * 2 * grid, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  double s = 0;
+  for (int b = 0; b < grid; b++) s += h[2 * b];
+  *h_nrm2 = s;
+  return PHDE_OK;
+}
+
+int phde_const_col(phde_ctx *ctx, double *U) {
+  const_col_kernel<<<grid_for(ctx, ctx->n, 256), 256, 0, ctx->stream>>>(U, ctx->n);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale, double *S, int k, int scol) {
+  accept_col_kernel<<<grid_for(ctx, ctx->n, 256), 256, 0, ctx->stream>>>(U, ctx->n, xcol, scale, S, k, scol);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS, int k) {
+  const int threads = 256;
+  const int grid = grid_for(ctx, ctx->n * 32, threads, 8);
+  lap_spmm_kernel<<<grid, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, ctx->weighted ? ctx->d_w : nullptr, deg,
+                                                     S, LS, ctx->n, k);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// M (k x k, column-major as the reference stores it) = A^T B.
+int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M) {
+  const int tiles = (k + GT - 1) / GT;
+  int splits = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * 4 / (tiles * tiles), (ctx->n + 255) / 256));
+  double *part = (double *)phde_buf(ctx, "gram.part", sizeof(double) * (size_t)splits * k * k);
+  if (!part) return PHDE_ERR_OOM;
+  gram_kernel<<<dim3(tiles * tiles, splits), 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+  PHDE_LAUNCHED(ctx);
+  sum_parts_kernel<<<grid_for(ctx, (int64_t)k * k, 256), 256, 0, ctx->stream>>>(part, splits, (int64_t)k * k, M);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C) {
+  const int64_t n = ctx->n;
+  ull *colsq = (ull *)phde_buf(ctx, "ctr.colsq", sizeof(ull) * k);
+  ull *colsum = (ull *)phde_buf(ctx, "ctr.colsum", sizeof(ull) * k);
+  double *rowsq = (double *)phde_buf(ctx, "ctr.rowsq", sizeof(double) * n);
+  if (!colsq || !colsum || !rowsq) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(colsq, 0, sizeof(ull) * k, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(colsum, 0, sizeof(ull) * k, ctx->stream));
+  dist_sums_kernel<<<grid_for(ctx, n, 256, 4), 256, 0, ctx->stream>>>(D, n, k, colsq, colsum, rowsq);
+  PHDE_LAUNCHED(ctx);
+  centre_kernel<<<grid_for(ctx, n * k, 256), 256, 0, ctx->stream>>>(D, n, k, colsq, colsum, rowsq, pivotmds, C);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X) {
+  const int threads = 256;
+  const int grid = grid_for(ctx, ctx->n * 32, threads, 4);
+  double *part = (double *)phde_buf(ctx, "coords.part", sizeof(double) * grid * (size_t)c);
+  if (!part) return PHDE_ERR_OOM;
+  coords_kernel<<<grid, threads, sizeof(double) * (threads / 32) * c, ctx->stream>>>(M, Y, ctx->n, k, c, X, part);
+  PHDE_LAUNCHED(ctx);
+  scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}

@@ -1,0 +1,305 @@
+// eigen.cu -- the k x k symmetric eigensolve, one CTA, FP64.
+//
+// power_kernel: the reference's non-MKL eigensolver (ParallelComponents.cpp:48-158, reached through
+//   compute_eigens, DrawingBase.cpp:39-108): N start vectors rand()/RAND_MAX after srand(1), repeated
+//   multiply-by-K, Gram-Schmidt of every vector against the ones before it, renormalisation, stop when
+//   every vector moved less than |cos| = 0.999; output columns in ascending |eigenvalue| order with the
+//   reference's sign rule.  The glibc rand() stream is regenerated on the device (the published TYPE_3
+//   additive-feedback generator).  The multiply keeps the reference's summation order; the Gram-Schmidt
+//   runs as a wavefront (vector i takes its projection onto vector j at step i+j, when vector j is final),
+//   so its N(N-1)/2 dependent projections take 2N-3 block-synchronous steps.
+// jacobi_kernel: exact solve (the LAPACKE_dsyev role of the MKL build): cyclic Jacobi on the symmetric
+//   part with the round-robin pairing, N/2 disjoint rotations per step; eigenvalues ascending; every
+//   eigenvector signed so that its largest-magnitude entry (lowest index on ties) is positive.
+// pick_kernel: eigenVectors columns for First (0..c-1) or Largest (N-1-j), DrawingBase.cpp:51-108.
+#include "ctx.h"
+
+namespace {
+
+constexpr int EIG_THREADS = 1024;
+
+__device__ double warp_dot(const double *a, const double *b, int N, int lane) {
+  double s = 0;
+  for (int r = lane; r < N; r += 32) s += __dmul_rn(a[r], b[r]);
+  return warp_sum(s);
+}
+
+// Work arrays live in global memory (a few N*N doubles, L2/L1 resident).
+__global__ void __launch_bounds__(EIG_THREADS) power_kernel(const double *Kin, int N, double *K, double *E,
+                                                            double *T, double *evals, int *iters, int *status,
+                                                            int max_iter) {
+  __shared__ double red[32];
+  __shared__ double s_r;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int NN = N * N;
+  for (int i = tid; i < NN; i += blockDim.x) K[i] = Kin[i];
+  // start vectors: glibc rand() after srand(1), E[j + i*N] = r[i*N + j] / RAND_MAX (column i filled first)
+  if (tid == 0) {
+    int32_t ring[34];
+    ring[0] = 1;
+    for (int i = 1; i < 31; i++) {
+      int32_t hi = ring[i - 1] / 127773, lo = ring[i - 1] % 127773;
+      int32_t word = 16807 * lo - 2836 * hi;
+      if (word < 0) word += 2147483647;
+      ring[i] = word;
+    }
+    for (int i = 31; i < 34; i++) ring[i] = ring[i - 31];
+    // r[i] for i >= 34 is r[i-31] + r[i-3]; keep the last 34 values in a ring indexed mod 34
+    int out = 0;
+    for (int i = 34; out < NN; i++) {
+      const int32_t v = (int32_t)((uint32_t)ring[(i - 31) % 34] + (uint32_t)ring[(i - 3) % 34]);
+      ring[i % 34] = v;
+      if (i >= 344) {
+        E[out] = (double)(int32_t)(((uint32_t)v) >> 1) / 2147483647.0;
+        out++;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = warp; i < N; i += nw) {
+    const double nv = sqrt(warp_dot(E + i * N, E + i * N, N, lane));
+    for (int r = lane; r < N; r += 32) E[r + i * N] = E[r + i * N] / nv;
+    if (lane == 0) evals[i] = nv;
+  }
+  __syncthreads();
+  double r = 0;
+  int it = 0;
+  while (r < 1.0 - 1e-3) {
+    it++;
+    if (isnan(r) || isinf(r) || it > max_iter) {
+      if (tid == 0) *status = PHDE_ERR_NOCONVERGE;
+      return;
+    }
+    for (int i = tid; i < NN; i += blockDim.x) T[i] = E[i];
+    __syncthreads();
+    // E[:, i] = K * T[:, i], accumulated over j in order (ParallelComponents.cpp:82-90)
+    for (int idx = tid; idx < NN; idx += blockDim.x) {
+      const int row = idx % N, col = idx / N;
+      double s = 0;
+      for (int j = 0; j < N; j++) s = __dadd_rn(s, __dmul_rn(K[row + j * N], T[j + col * N]));
+      E[idx] = s;
+    }
+    __syncthreads();
+    // Gram-Schmidt wavefront: at step t vector i projects out vector j = t - i (j < i)
+    for (int t = 1; t <= 2 * N - 3; t++) {
+      for (int i = warp; i < N; i += nw) {
+        const int j = t - i;
+        if (j < 0 || j >= i) continue;
+        const double num = warp_dot(E + j * N, E + i * N, N, lane);
+        const double den = warp_dot(E + j * N, E + j * N, N, lane);
+        const double fac = num / den;
+        for (int q = lane; q < N; q += 32) E[q + i * N] = __dsub_rn(E[q + i * N], __dmul_rn(fac, E[q + j * N]));
+        __syncwarp();
+      }
+      __syncthreads();
+    }
+    for (int i = warp; i < N; i += nw) {
+      const double nv = sqrt(warp_dot(E + i * N, E + i * N, N, lane));
+      for (int q = lane; q < N; q += 32) E[q + i * N] = E[q + i * N] / nv;
+      if (lane == 0) evals[i] = nv;
+    }
+    __syncthreads();
+    // r = min_i |<E_i, T_i>|
+    double mn = 1.0;
+    for (int i = warp; i < N; i += nw) {
+      double d = fabs(warp_dot(E + i * N, T + i * N, N, lane));
+      mn = d < mn ? d : mn;
+    }
+    if (lane == 0) red[warp] = mn;
+    __syncthreads();
+    if (tid == 0) {
+      double m = 1.0;
+      for (int w = 0; w < nw; w++) m = red[w] < m ? red[w] : m;
+      s_r = m;
+    }
+    __syncthreads();
+    r = s_r;
+  }
+  __syncthreads();
+  if (tid == 0) {  // ascending order of the norms (ParallelComponents.cpp:131-139)
+    for (int a = 0, b = N - 1; a < b; a++, b--) {
+      double t = evals[a];
+      evals[a] = evals[b];
+      evals[b] = t;
+    }
+    *iters = it;
+    *status = PHDE_OK;
+  }
+  // K[:, N-1-i] = +-E[:, i]; the sign follows the first entry of E column N-1-i (ParallelComponents.cpp:140-153)
+  for (int idx = tid; idx < NN; idx += blockDim.x) {
+    const int i = idx / N, row = idx % N;
+    const bool neg = E[(N - i - 1) * N] < 0;
+    K[row + (N - i - 1) * N] = neg ? -E[row + i * N] : E[row + i * N];
+  }
+}
+
+// Exact symmetric eigensolve by parallel cyclic Jacobi (Brent-Luk round-robin ordering).
+__global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(const double *Kin, int N, double *A, double *V,
+                                                             double *K, double *evals, int *sweeps, int *status,
+                                                             int max_sweeps) {
+  __shared__ double red[32];
+  __shared__ double s_cs[PHDE_MAX_K / 2 + 1], s_sn[PHDE_MAX_K / 2 + 1];
+  __shared__ int s_p[PHDE_MAX_K / 2 + 1], s_q[PHDE_MAX_K / 2 + 1];
+  __shared__ int s_order[PHDE_MAX_K + 1];
+  __shared__ int s_done;
+  const int tid = threadIdx.x;
+  const int M = (N + 1) & ~1;  // even number of slots; slot N (if any) is a dummy
+  for (int idx = tid; idx < N * N; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    A[idx] = 0.5 * (Kin[i + j * N] + Kin[j + i * N]);
+    V[idx] = i == j ? 1.0 : 0.0;
+  }
+  for (int i = tid; i < M; i += blockDim.x) s_order[i] = i;
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < max_sweeps; sweep++) {
+    double off = 0, tot = 0;
+    for (int idx = tid; idx < N * N; idx += blockDim.x) {
+      const int i = idx % N, j = idx / N;
+      const double a2 = A[idx] * A[idx];
+      tot += a2;
+      if (i != j) off += a2;
+    }
+    off = block_sum(off, red);
+    tot = block_sum(tot, red);
+    if (tid == 0) s_done = (off <= 1e-30 * tot) || off == 0.0;
+    __syncthreads();
+    if (s_done) break;
+    for (int round = 0; round < M - 1; round++) {
+      // pairs (order[2m], order[2m+1]) of the current round
+      for (int m = tid; m < M / 2; m += blockDim.x) {
+        int p = s_order[2 * m], q = s_order[2 * m + 1];
+        if (p > q) {
+          int t = p;
+          p = q;
+          q = t;
+        }
+        double cs = 1.0, sn = 0.0;
+        if (q < N) {
+          const double apq = A[p + q * N];
+          if (apq != 0.0) {
+            const double app = A[p + p * N], aqq = A[q + q * N];
+            const double theta = (aqq - app) / (2.0 * apq);
+            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            cs = 1.0 / sqrt(t * t + 1.0);
+            sn = t * cs;
+          }
+        }
+        s_p[m] = p;
+        s_q[m] = q;
+        s_cs[m] = cs;
+        s_sn[m] = sn;
+      }
+      __syncthreads();
+      // A <- A J (columns p, q) and V <- V J
+      for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
+        const int m = idx / N, row = idx % N;
+        const int p = s_p[m], q = s_q[m];
+        if (q >= N || s_sn[m] == 0.0) continue;
+        const double cs = s_cs[m], sn = s_sn[m];
+        const double akp = A[row + p * N], akq = A[row + q * N];
+        A[row + p * N] = cs * akp - sn * akq;
+        A[row + q * N] = sn * akp + cs * akq;
+        const double vkp = V[row + p * N], vkq = V[row + q * N];
+        V[row + p * N] = cs * vkp - sn * vkq;
+        V[row + q * N] = sn * vkp + cs * vkq;
+      }
+      __syncthreads();
+      // A <- J^T A (rows p, q)
+      for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
+        const int m = idx / N, col = idx % N;
+        const int p = s_p[m], q = s_q[m];
+        if (q >= N || s_sn[m] == 0.0) continue;
+        const double cs = s_cs[m], sn = s_sn[m];
+        const double apk = A[p + col * N], aqk = A[q + col * N];
+        A[p + col * N] = cs * apk - sn * aqk;
+        A[q + col * N] = sn * apk + cs * aqk;
+      }
+      __syncthreads();
+      // round-robin rotation of the slots, slot 0 fixed
+      if (tid == 0) {
+        const int last = s_order[M - 1];
+        for (int i = M - 1; i > 1; i--) s_order[i] = s_order[i - 1];
+        s_order[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  if (tid == 0) {
+    // ascending selection sort of the diagonal (stable on ties)
+    for (int i = 0; i < N; i++) s_order[i] = i;
+    for (int i = 0; i < N; i++) {
+      int b = i;
+      for (int j = i + 1; j < N; j++)
+        if (A[s_order[j] + s_order[j] * N] < A[s_order[b] + s_order[b] * N]) b = j;
+      const int t = s_order[i];
+      s_order[i] = s_order[b];
+      s_order[b] = t;
+    }
+    for (int c = 0; c < N; c++) evals[c] = A[s_order[c] + s_order[c] * N];
+    *sweeps = sweep;
+    *status = sweep < max_sweeps ? PHDE_OK : PHDE_ERR_NOCONVERGE;
+  }
+  __syncthreads();
+  const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int c = warp; c < N; c += nw) {
+    const int src = s_order[c];
+    // index of the largest |entry| (lowest index on ties)
+    double best = -1.0;
+    int arg = 0;
+    for (int i = lane; i < N; i += 32) {
+      const double a = fabs(V[i + src * N]);
+      if (a > best) {
+        best = a;
+        arg = i;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double b2 = __shfl_xor_sync(PHDE_FULL_MASK, best, o);
+      const int a2 = __shfl_xor_sync(PHDE_FULL_MASK, arg, o);
+      if (b2 > best || (b2 == best && a2 < arg)) {
+        best = b2;
+        arg = a2;
+      }
+    }
+    const double sg = V[arg + src * N] < 0 ? -1.0 : 1.0;
+    for (int i = lane; i < N; i += 32) K[i + c * N] = sg * V[i + src * N];
+  }
+}
+
+__global__ void pick_kernel(const double *K, int N, int c, int largest, double *Y) {
+  for (int idx = threadIdx.x; idx < N * c; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    const int col = largest ? N - 1 - j : j;
+    Y[idx] = K[i + col * N];
+  }
+}
+
+}  // namespace
+
+// Solve the k x k problem in d_M (column-major).  On success d_K holds the eigenvector matrix,
+// d_evals the eigenvalues (ascending), d_Y the c picked eigenvectors.  Synchronises to read the status.
+int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
+                    double *d_evals, double *d_Y, int *h_iters) {
+  double *w1 = (double *)phde_buf(ctx, "eig.w1", sizeof(double) * N * N);
+  double *w2 = (double *)phde_buf(ctx, "eig.w2", sizeof(double) * N * N);
+  int *st = (int *)phde_buf(ctx, "eig.st", sizeof(int) * 2);
+  if (!w1 || !w2 || !st) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(st, 0, sizeof(int) * 2, ctx->stream));
+  if (eig == PHDE_EIG_EXACT) {
+    jacobi_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, w1, w2, d_K, d_evals, st, st + 1, 100);
+  } else {
+    power_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000);
+  }
+  PHDE_LAUNCHED(ctx);
+  pick_kernel<<<1, 256, 0, ctx->stream>>>(d_K, N, c, largest, d_Y);
+  PHDE_LAUNCHED(ctx);
+  int h[2];
+  PHDE_CK(ctx, cudaMemcpyAsync(h, st, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *h_iters = h[0];
+  if (h[1] != PHDE_OK)
+    return phde_fail(ctx, h[1], eig == PHDE_EIG_EXACT ? "Jacobi eigensolver did not converge"
+                                                      : "power iteration did not converge (iteration cap reached)");
+  return PHDE_OK;
+}

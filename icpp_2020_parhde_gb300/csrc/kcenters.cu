@@ -1,0 +1,300 @@
+// kcenters.cu -- Kcenters pivot distances: P breadth-first searches in ONE persistent cooperative launch.
+//
+// Replaces the serial Kcenters loop of variants/ParHDE.cpp:118-157 (and DrawingBase.cpp:119-172), whose
+// every pass calls gapbs DOBFS (gapbs/bfs.cc:144-185) and then an OpenMP min/argmax reduction.  Each pass
+// here is a level-synchronous direction-optimising BFS over the device CSR, followed by the Kcenters
+// selection folded into one sweep; grid barriers (bounded waits) separate the levels, so the 3k
+// dependent passes cost no host round trip.
+//
+// Per level, with frontier F_L (vertices at hop distance L):
+//   top-down  : edge-balanced -- thread e takes the e-th out-edge of F_L, finds its owner vertex by
+//               binary search over the frontier's start-edge prefix array, and claims the neighbour
+//               with a CAS on its distance entry (-1 -> L+1);
+//   bottom-up : every unvisited vertex scans its neighbours for one at distance L and stops at the
+//               first;
+//   both append the new frontier with block-aggregated 64-bit atomics that keep (slot, edge prefix)
+//   together, so the next top-down step is load balanced even around hub vertices.
+// The top-down / bottom-up switch follows the reference rule (alpha = 15, beta = 18): go bottom-up
+// when the frontier's out-edges exceed edges_to_check / alpha, stay there while the frontier grows
+// or exceeds n / beta (bfs.cc:159-183).  Hop distances are unique, so the result is bit-exact
+// whatever the direction schedule.
+//
+// Selection (ParHDE.cpp:127-155): min_d[v] = min(min_d[v], d_p[v]); the next source is the vertex of
+// largest min_d, lowest index first (a 64-bit atomicMax on (min_d << 32) | ~v); if that vertex is in
+// the history, the duplicate fix-up takes the highest-index vertex with the same min_d that is not.
+#include "ctx.h"
+
+namespace {
+
+constexpr int KC_THREADS = 512;
+
+struct KcArgs {
+  const int64_t *off;
+  const uint32_t *adj;
+  int64_t n, nnz;
+  int32_t *D;  // n * P, column-major, pre-filled with -1
+  int P;
+  int variant;  // 0: ParHDE history (raw argmax), 1: fixed sources, 2: DrawingBase history (used source)
+  int require_all;  // an unreached vertex is an error (always for the Kcenters variants)
+  const int64_t *fixed_src;
+  int64_t *sources;
+  int32_t *min_d;   // [n], INT32_MAX initially
+  ull *sumsq;       // [P]
+  ull *keys;        // [P]
+  ull *fixkey;      // [P]
+  uint32_t *qv0, *qv1, *qe0, *qe1;
+  ull *ctr;         // [4] ring of (count << 32 | edges)
+  ull *edges;       // [1] adjacency entries read
+  GridSync *gs;
+  int *err;
+  uint64_t timeout_ns;
+  int alpha, beta;
+};
+
+__global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
+  __shared__ PushScratch psc;
+  __shared__ ull red[32];
+  extern __shared__ uint32_t s_hist[];  // [P]: every block keeps the same selection history
+  const int64_t n = a.n;
+  const int tid = threadIdx.x;
+  const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t gbase = (int64_t)blockIdx.x * blockDim.x;
+  int64_t src = a.variant == 1 ? a.fixed_src[0] : 0;
+  uint32_t step = 0;
+  ull edges_local = 0;
+
+  for (int p = 0; p < a.P; p++) {
+    int32_t *Dp = a.D + (int64_t)p * n;
+    if (tid == 0) {
+      Dp[src] = 0;
+      if (blockIdx.x == 0) a.sources[p] = src;
+    }
+    __syncthreads();
+    const int64_t s_off = a.off[src];
+    const uint32_t sdeg = (uint32_t)(a.off[src + 1] - s_off);
+    uint32_t f_cnt = 1, f_edges = sdeg;
+    int64_t edges_to_check = a.nnz, scout = sdeg;
+    bool in_bu = false;
+    int64_t awake = 0, old_awake = 0;
+    int32_t L = 0;
+
+    while (f_cnt > 0) {
+      if (!in_bu) {
+        if (scout > edges_to_check / a.alpha) {
+          in_bu = true;
+          awake = f_cnt;
+        } else {
+          edges_to_check -= scout;
+        }
+      }
+      if (in_bu) old_awake = awake;
+      const uint32_t *qin_v = (step & 1) ? a.qv1 : a.qv0;
+      const uint32_t *qin_e = (step & 1) ? a.qe1 : a.qe0;
+      uint32_t *qout_v = (step & 1) ? a.qv0 : a.qv1;
+      uint32_t *qout_e = (step & 1) ? a.qe0 : a.qe1;
+      ull *octr = a.ctr + (step & 3);
+      if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 2) & 3] = 0ull;
+
+      if (!in_bu) {
+        const int64_t E = f_edges;
+        for (int64_t base = gbase; base < E; base += gstride) {
+          const int64_t e = base + tid;
+          bool claimed = false;
+          uint32_t v = 0, dv = 0;
+          if (e < E) {
+            int64_t j;
+            if (L == 0) {
+              j = s_off + e;
+            } else {
+              const uint32_t s = owner_slot(qin_e, f_cnt, (uint32_t)e);
+              j = a.off[qin_v[s]] + (e - (int64_t)qin_e[s]);
+            }
+            v = __ldg(a.adj + j);
+            edges_local++;
+            if (Dp[v] == -1 && atomicCAS(Dp + v, -1, L + 1) == -1) {
+              claimed = true;
+              dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+            }
+          }
+          block_push(claimed, v, dv, qout_v, qout_e, octr, &psc);
+        }
+      } else {
+        for (int64_t base = gbase; base < n; base += gstride) {
+          const int64_t v = base + tid;
+          bool found = false;
+          uint32_t dv = 0;
+          if (v < n && Dp[v] == -1) {
+            const int64_t j0 = a.off[v], j1 = a.off[v + 1];
+            for (int64_t j = j0; j < j1; j++) {
+              edges_local++;
+              if (Dp[__ldg(a.adj + j)] == L) {
+                found = true;
+                break;
+              }
+            }
+            if (found) {
+              Dp[v] = L + 1;
+              dv = (uint32_t)(j1 - j0);
+            }
+          }
+          block_push(found, (uint32_t)v, dv, qout_v, qout_e, octr, &psc);
+        }
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      const ull out = __ldcg(octr);
+      f_cnt = (uint32_t)(out >> 32);
+      f_edges = (uint32_t)(out & 0xffffffffull);
+      if (in_bu) {
+        awake = f_cnt;
+        if (!(awake >= old_awake || awake > n / a.beta)) {
+          in_bu = false;
+          scout = 1;
+        }
+      } else {
+        scout = f_edges;
+      }
+      L++;
+      step++;
+    }
+
+    // ---- fold the finished column: min distance, farthest vertex, sum of squares ----
+    ull kbest = 0, ssq = 0;
+    int bad = 0;
+    for (int64_t v = gbase + tid; v < n; v += gstride) {
+      const int32_t d = Dp[v];
+      if (d < 0) {
+        bad = 1;
+        continue;
+      }
+      ssq += (ull)d * (ull)d;
+      if (a.variant != 1) {
+        int32_t m = a.min_d[v];
+        if (d < m) {
+          m = d;
+          a.min_d[v] = m;
+        }
+        const ull key = ((ull)(uint32_t)m << 32) | (ull)(0xffffffffu - (uint32_t)v);
+        kbest = key > kbest ? key : kbest;
+      }
+    }
+    if ((a.variant != 1 || a.require_all) && __syncthreads_or(bad)) {
+      if (tid == 0) atomicCAS(a.err, 0, PHDE_ERR_DISCONNECTED);
+      return;
+    }
+    ssq = block_sum(ssq, red);
+    if (tid == 0) atomicAdd(a.sumsq + p, ssq);
+    if (a.variant != 1) {
+      kbest = block_max_u64(kbest, red);
+      if (tid == 0) atomicMax(a.keys + p, kbest);
+    }
+    if (p + 1 == a.P) break;
+    if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+
+    if (a.variant == 1) {
+      src = a.fixed_src[p + 1];
+      continue;
+    }
+    const ull key = __ldcg(a.keys + p);
+    const uint32_t raw = 0xffffffffu - (uint32_t)(key & 0xffffffffull);
+    const int32_t maxval = (int32_t)(key >> 32);
+    int hit = 0;
+    for (int i = tid; i < p; i += blockDim.x) hit |= (s_hist[i] == raw);
+    hit = __syncthreads_or(hit);
+    int64_t next = raw;
+    if (p >= 1 && hit) {
+      // duplicate fix-up (ParHDE.cpp:144-154 at one thread): highest-index vertex with the same
+      // minimum distance that is not in the history
+      for (int64_t v = gbase + tid; v < n; v += gstride) {
+        if (a.min_d[v] != maxval) continue;
+        bool inh = false;
+        for (int i = 0; i < p && !inh; i++) inh = (s_hist[i] == (uint32_t)v);
+        if (!inh) atomicMax(a.fixkey + p, (ull)v + 1ull);
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      const ull fk = __ldcg(a.fixkey + p);
+      if (fk) next = (int64_t)(fk - 1ull);
+    }
+    __syncthreads();
+    if (tid == 0) s_hist[p] = a.variant == 2 ? (uint32_t)src : raw;
+    __syncthreads();
+    src = next;
+  }
+  ull etot = block_sum(edges_local, red);
+  if (tid == 0 && a.edges) atomicAdd(a.edges, etot);
+}
+
+__global__ void fill_i32_kernel(int32_t *p, int64_t n, int32_t v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+}  // namespace
+
+int phde_fill_i32(phde_ctx *ctx, int32_t *p, int64_t n, int32_t v) {
+  int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->nsm * 8);
+  if (blocks < 1) blocks = 1;
+  fill_i32_kernel<<<blocks, 256, 0, ctx->stream>>>(p, n, v);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixed_src, int32_t *d_D,
+                        int64_t *d_sources, unsigned long long *d_sumsq, unsigned long long *d_edges, int require_all) {
+  const int64_t n = ctx->n;
+  if (ctx->nnz >= (int64_t)0xffffffffll || n >= (int64_t)0xffffffffll)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "graphs with 2^32 or more vertices or adjacency entries are not supported");
+  int32_t *min_d = (int32_t *)phde_buf(ctx, "kc.min_d", sizeof(int32_t) * n);
+  ull *keys = (ull *)phde_buf(ctx, "kc.keys", sizeof(ull) * P);
+  ull *fixkey = (ull *)phde_buf(ctx, "kc.fixkey", sizeof(ull) * P);
+  uint32_t *qv0 = (uint32_t *)phde_buf(ctx, "q.v0", sizeof(uint32_t) * n);
+  uint32_t *qv1 = (uint32_t *)phde_buf(ctx, "q.v1", sizeof(uint32_t) * n);
+  uint32_t *qe0 = (uint32_t *)phde_buf(ctx, "q.e0", sizeof(uint32_t) * n);
+  uint32_t *qe1 = (uint32_t *)phde_buf(ctx, "q.e1", sizeof(uint32_t) * n);
+  ull *ctr = (ull *)phde_buf(ctx, "q.ctr", sizeof(ull) * 4);
+  if (!min_d || !keys || !fixkey || !qv0 || !qv1 || !qe0 || !qe1 || !ctr) return PHDE_ERR_OOM;
+
+  PHDE_CK(ctx, cudaMemsetAsync(d_D, 0xff, sizeof(int32_t) * (size_t)n * (size_t)P, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(keys, 0, sizeof(ull) * P, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(fixkey, 0, sizeof(ull) * P, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(ctr, 0, sizeof(ull) * 4, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(d_sumsq, 0, sizeof(ull) * P, ctx->stream));
+  int rc = phde_fill_i32(ctx, min_d, n, 0x7fffffff);
+  if (rc) return rc;
+  if ((rc = phde_reset_sync(ctx))) return rc;
+
+  int per_sm = 0;
+  const size_t smem = sizeof(uint32_t) * (size_t)P;
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kcenters_bfs_kernel, KC_THREADS, smem));
+  if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "kcenters kernel cannot be resident");
+  per_sm = std::min(per_sm, 4);
+  KcArgs a;
+  a.off = ctx->d_off;
+  a.adj = ctx->d_adj;
+  a.n = n;
+  a.nnz = ctx->nnz;
+  a.D = d_D;
+  a.P = P;
+  a.variant = variant;
+  a.require_all = require_all || variant != 1;
+  a.fixed_src = d_fixed_src;
+  a.sources = d_sources;
+  a.min_d = min_d;
+  a.sumsq = d_sumsq;
+  a.keys = keys;
+  a.fixkey = fixkey;
+  a.qv0 = qv0;
+  a.qv1 = qv1;
+  a.qe0 = qe0;
+  a.qe1 = qe1;
+  a.ctr = ctr;
+  a.edges = d_edges;
+  a.gs = ctx->d_sync;
+  a.err = ctx->d_err;
+  a.timeout_ns = ctx->timeout_ns;
+  a.alpha = 15;
+  a.beta = 18;
+  void *args[] = {&a};
+  PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)kcenters_bfs_kernel, dim3(ctx->nsm * per_sm),
+                                           dim3(KC_THREADS), args, smem, ctx->stream));
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}

@@ -1,0 +1,330 @@
+// sssp.cu -- exact weighted shortest paths for WParHDE, one persistent cooperative launch per source.
+//
+// Replaces gapbs DeltaStep (gapbs/sssp.cc:53-140) as called from WParHDE (WParHDE.cpp:116 through
+// DrawingBase.cpp:116).  The reference runs delta-stepping with thread-local bins of width delta and
+// CAS-min relaxations; this kernel keeps the same bucketing idea in a GPU shape (near-far):
+//   near set  : vertices whose tentative distance is below the current band limit T, processed in
+//               rounds; every round relaxes all out-edges of the near frontier, edge-balanced exactly
+//               like the top-down BFS step (owner found by binary search over the frontier's
+//               start-edge prefix array), with atomicMin on the distance;
+//   far pile  : improved vertices at or beyond T; when the near frontier empties, T jumps to the band
+//               holding the smallest far distance and the pile is split into the new near frontier and
+//               what stays far.
+// Both lists are de-duplicated with per-vertex stamps.  Shortest-path distances are unique, so the
+// result is bit-exact against the reference whatever the band width or relaxation order.
+#include "ctx.h"
+
+namespace {
+
+constexpr int SS_THREADS = 512;
+constexpr int32_t SSSP_INF = 0x7fffffff / 2;  // kDistInf, gapbs/sssp.cc:50
+
+struct SsArgs {
+  const int64_t *off;
+  const uint32_t *adj;
+  const int32_t *w;
+  int64_t n;
+  const int64_t *src;
+  int32_t *dist;  // [n], SSSP_INF initially
+  int32_t delta;
+  uint32_t *qv0, *qv1, *qe0, *qe1;  // near frontier (vertex, start-edge prefix)
+  uint32_t *far0, *far1;            // far pile
+  int32_t *stamp_near, *stamp_far;  // [n], -1 initially
+  ull *ctr;                         // [4] near ring
+  unsigned *farctr;                 // [2]
+  ull *minfar;                      // [2], alternating by phase
+  ull *edges;
+  GridSync *gs;
+  int *err;
+  uint64_t timeout_ns;
+};
+
+__device__ __forceinline__ void block_append(bool flag, uint32_t v, uint32_t *arr, unsigned *ctr, unsigned *s_base,
+                                             unsigned *s_warp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const unsigned bal = __ballot_sync(PHDE_FULL_MASK, flag);
+  const unsigned before = __popc(bal & ((1u << lane) - 1u));
+  if (lane == 0) s_warp[warp] = __popc(bal);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned tot = 0;
+    for (int i = 0; i < nw; i++) {
+      unsigned c = s_warp[i];
+      s_warp[i] = tot;
+      tot += c;
+    }
+    *s_base = tot ? atomicAdd(ctr, tot) : 0u;
+  }
+  __syncthreads();
+  if (flag) arr[*s_base + s_warp[warp] + before] = v;
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(SS_THREADS) sssp_nearfar_kernel(SsArgs a) {
+  __shared__ PushScratch psc;
+  __shared__ unsigned s_warp[32];
+  __shared__ unsigned s_base;
+  __shared__ ull red[32];
+  const int tid = threadIdx.x;
+  const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t gbase = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t src = *a.src;
+  if (blockIdx.x == 0 && tid == 0) {
+    a.dist[src] = 0;
+    a.qv0[0] = (uint32_t)src;
+    a.qe0[0] = 0;
+    a.stamp_near[src] = 0;
+  }
+  ull edges_local = 0;
+  uint32_t f_cnt = 1, f_edges = (uint32_t)(a.off[src + 1] - a.off[src]);
+  unsigned far_cnt = 0;
+  int64_t T = a.delta;
+  int32_t it = 0, phase = 0;
+  uint32_t step = 0;
+  if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+
+  while (true) {
+    // ---- relaxation rounds over the near frontier ----
+    while (f_cnt > 0) {
+      const uint32_t *qin_v = (step & 1) ? a.qv1 : a.qv0;
+      const uint32_t *qin_e = (step & 1) ? a.qe1 : a.qe0;
+      uint32_t *qout_v = (step & 1) ? a.qv0 : a.qv1;
+      uint32_t *qout_e = (step & 1) ? a.qe0 : a.qe1;
+      ull *octr = a.ctr + (step & 3);
+      uint32_t *far_in = (phase & 1) ? a.far1 : a.far0;
+      unsigned *fctr = a.farctr + (phase & 1);
+      if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 1) & 3] = 0ull;
+      const int64_t E = f_edges;
+      for (int64_t base = gbase; base < E; base += gstride) {
+        const int64_t e = base + tid;
+        bool to_near = false, to_far = false;
+        uint32_t v = 0, dv = 0;
+        if (e < E) {
+          const uint32_t s = owner_slot(qin_e, f_cnt, (uint32_t)e);
+          const uint32_t u = qin_v[s];
+          const int64_t j = a.off[u] + (e - (int64_t)qin_e[s]);
+          v = __ldg(a.adj + j);
+          edges_local++;
+          const int32_t du = __ldcg(a.dist + u);
+          const int32_t nd = du + __ldg(a.w + j);
+          if (nd < __ldcg(a.dist + v)) {
+            const int32_t old = atomicMin(a.dist + v, nd);
+            if (nd < old) {
+              if (nd < T) {
+                if (atomicExch(a.stamp_near + v, it + 1) != it + 1) {
+                  to_near = true;
+                  dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+                }
+              } else if (atomicExch(a.stamp_far + v, phase) != phase) {
+                to_far = true;
+              }
+            }
+          }
+        }
+        block_push(to_near, v, dv, qout_v, qout_e, octr, &psc);
+        block_append(to_far, v, far_in, fctr, &s_base, s_warp);
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      const ull out = __ldcg(octr);
+      f_cnt = (uint32_t)(out >> 32);
+      f_edges = (uint32_t)(out & 0xffffffffull);
+      it++;
+      step++;
+    }
+    // ---- near frontier empty: move to the band of the closest far vertex ----
+    far_cnt = __ldcg(a.farctr + (phase & 1));
+    if (far_cnt == 0) break;
+    const uint32_t *far_in = (phase & 1) ? a.far1 : a.far0;
+    uint32_t *far_out = (phase & 1) ? a.far0 : a.far1;
+    unsigned *fout_ctr = a.farctr + ((phase + 1) & 1);
+    ull *mslot = a.minfar + (phase & 1);
+    ull mloc = ~0ull;
+    for (int64_t i = gbase + tid; i < far_cnt; i += gstride) {
+      const int32_t d = __ldcg(a.dist + far_in[i]);
+      if (d >= T) mloc = (ull)d < mloc ? (ull)d : mloc;
+    }
+    const ull bm = block_max_u64(~mloc, red);  // block minimum through the complement
+    if (tid == 0 && bm != 0ull) atomicMin(mslot, ~bm);
+    if (blockIdx.x == 0 && tid == 0) {
+      *fout_ctr = 0u;
+      a.minfar[(phase + 1) & 1] = ~0ull;
+    }
+    if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    const ull mf = __ldcg(mslot);
+    const int64_t T_old = T;
+    if (mf != ~0ull) T = ((int64_t)mf / a.delta + 1) * (int64_t)a.delta;
+    // split the pile: this is a step of its own, writing the next round's input queue
+    uint32_t *qout_v = (step & 1) ? a.qv0 : a.qv1;
+    uint32_t *qout_e = (step & 1) ? a.qe0 : a.qe1;
+    ull *octr = a.ctr + (step & 3);
+    if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 1) & 3] = 0ull;
+    for (int64_t base = gbase; base < (int64_t)far_cnt; base += gstride) {
+      const int64_t i = base + tid;
+      bool to_near = false, keep = false;
+      uint32_t v = 0, dv = 0;
+      if (i < far_cnt) {
+        v = far_in[i];
+        const int32_t d = __ldcg(a.dist + v);
+        if (d >= T_old && d < T) {
+          if (atomicExch(a.stamp_near + v, it + 1) != it + 1) {
+            to_near = true;
+            dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+          }
+        } else if (d >= T) {
+          keep = atomicExch(a.stamp_far + v, phase + 1) != phase + 1;
+        }
+      }
+      block_push(to_near, v, dv, qout_v, qout_e, octr, &psc);
+      block_append(keep, v, far_out, fout_ctr, &s_base, s_warp);
+    }
+    if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    const ull out = __ldcg(octr);
+    f_cnt = (uint32_t)(out >> 32);
+    f_edges = (uint32_t)(out & 0xffffffffull);
+    it++;
+    step++;
+    phase++;
+    if (f_cnt == 0 && __ldcg(a.farctr + (phase & 1)) == 0) break;
+  }
+  ull etot = block_sum(edges_local, red);
+  if (tid == 0 && a.edges) atomicAdd(a.edges, etot);
+}
+
+// Fold one finished distance column into the Kcenters state (WParHDE.cpp:117-136).
+__global__ void fold_kernel(const int32_t *col, int64_t n, int32_t *min_d, ull *key_out, ull *ssq_out, int *err) {
+  __shared__ ull red[32];
+  ull kbest = 0, ssq = 0;
+  int bad = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t d = col[v];
+    if (d >= SSSP_INF || d < 0) {
+      bad = 1;
+      continue;
+    }
+    ssq += (ull)d * (ull)d;
+    int32_t m = min_d[v];
+    if (d < m) {
+      m = d;
+      min_d[v] = m;
+    }
+    const ull key = ((ull)(uint32_t)m << 32) | (ull)(0xffffffffu - (uint32_t)v);
+    kbest = key > kbest ? key : kbest;
+  }
+  if (__syncthreads_or(bad)) {
+    if (threadIdx.x == 0) atomicCAS(err, 0, PHDE_ERR_DISCONNECTED);
+    return;
+  }
+  ssq = block_sum(ssq, red);
+  kbest = block_max_u64(kbest, red);
+  if (threadIdx.x == 0) {
+    atomicAdd(ssq_out, ssq);
+    atomicMax(key_out, kbest);
+  }
+}
+
+// Choose the next source (one block): raw argmax, duplicate fix-up against the history of raw argmaxes
+// (WParHDE.cpp:137-153), append the raw argmax to the history.
+__global__ void select_kernel(const ull *key_in, const int32_t *min_d, int64_t n, int pass, int check_fix,
+                              int64_t *hist, int64_t *next_src) {
+  __shared__ ull red[32];
+  const ull key = *key_in;
+  const int64_t raw = (int64_t)(0xffffffffu - (uint32_t)(key & 0xffffffffull));
+  const int32_t maxval = (int32_t)(key >> 32);
+  int hit = 0;
+  for (int i = threadIdx.x; i < pass; i += blockDim.x) hit |= (hist[i] == raw);
+  hit = __syncthreads_or(hit);
+  int64_t next = raw;
+  if (check_fix && hit) {
+    ull best = 0;
+    for (int64_t v = threadIdx.x; v < n; v += blockDim.x) {
+      if (min_d[v] != maxval) continue;
+      bool inh = false;
+      for (int i = 0; i < pass && !inh; i++) inh = hist[i] == v;
+      if (!inh) best = (ull)v + 1 > best ? (ull)v + 1 : best;
+    }
+    best = block_max_u64(best, red);
+    if (best) next = (int64_t)best - 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    hist[pass] = raw;
+    *next_src = next;
+  }
+}
+
+}  // namespace
+
+int phde_fill_i32(phde_ctx *ctx, int32_t *p, int64_t n, int32_t v);
+
+int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t delta, unsigned long long *d_edges) {
+  const int64_t n = ctx->n;
+  if (ctx->nnz >= (int64_t)0xffffffffll || n >= (int64_t)0xffffffffll)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "graphs with 2^32 or more vertices or adjacency entries are not supported");
+  if (!ctx->d_w) return phde_fail(ctx, PHDE_ERR_WEIGHTS, "SSSP needs edge weights");
+  if (delta < 1) delta = 1;
+  uint32_t *qv0 = (uint32_t *)phde_buf(ctx, "q.v0", sizeof(uint32_t) * n);
+  uint32_t *qv1 = (uint32_t *)phde_buf(ctx, "q.v1", sizeof(uint32_t) * n);
+  uint32_t *qe0 = (uint32_t *)phde_buf(ctx, "q.e0", sizeof(uint32_t) * n);
+  uint32_t *qe1 = (uint32_t *)phde_buf(ctx, "q.e1", sizeof(uint32_t) * n);
+  uint32_t *far0 = (uint32_t *)phde_buf(ctx, "ss.far0", sizeof(uint32_t) * n);
+  uint32_t *far1 = (uint32_t *)phde_buf(ctx, "ss.far1", sizeof(uint32_t) * n);
+  int32_t *stn = (int32_t *)phde_buf(ctx, "ss.stamp_near", sizeof(int32_t) * n);
+  int32_t *stf = (int32_t *)phde_buf(ctx, "ss.stamp_far", sizeof(int32_t) * n);
+  ull *ctr = (ull *)phde_buf(ctx, "q.ctr", sizeof(ull) * 4);
+  unsigned *farctr = (unsigned *)phde_buf(ctx, "ss.farctr", sizeof(unsigned) * 2);
+  ull *minfar = (ull *)phde_buf(ctx, "ss.minfar", sizeof(ull) * 2);
+  if (!qv0 || !qv1 || !qe0 || !qe1 || !far0 || !far1 || !stn || !stf || !ctr || !farctr || !minfar) return PHDE_ERR_OOM;
+  int rc;
+  if ((rc = phde_fill_i32(ctx, d_col, n, SSSP_INF))) return rc;
+  PHDE_CK(ctx, cudaMemsetAsync(stn, 0xff, sizeof(int32_t) * n, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(stf, 0xff, sizeof(int32_t) * n, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(ctr, 0, sizeof(ull) * 4, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(farctr, 0, sizeof(unsigned) * 2, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(minfar, 0xff, sizeof(ull) * 2, ctx->stream));
+  if ((rc = phde_reset_sync(ctx))) return rc;
+  int per_sm = 0;
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_nearfar_kernel, SS_THREADS, 0));
+  if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "sssp kernel cannot be resident");
+  per_sm = std::min(per_sm, 4);
+  SsArgs a;
+  a.off = ctx->d_off;
+  a.adj = ctx->d_adj;
+  a.w = ctx->d_w;
+  a.n = n;
+  a.src = d_src;
+  a.dist = d_col;
+  a.delta = delta;
+  a.qv0 = qv0;
+  a.qv1 = qv1;
+  a.qe0 = qe0;
+  a.qe1 = qe1;
+  a.far0 = far0;
+  a.far1 = far1;
+  a.stamp_near = stn;
+  a.stamp_far = stf;
+  a.ctr = ctr;
+  a.farctr = farctr;
+  a.minfar = minfar;
+  a.edges = d_edges;
+  a.gs = ctx->d_sync;
+  a.err = ctx->d_err;
+  a.timeout_ns = ctx->timeout_ns;
+  void *args[] = {&a};
+  PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)sssp_nearfar_kernel, dim3(ctx->nsm * per_sm),
+                                           dim3(SS_THREADS), args, 0, ctx->stream));
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_run_select(phde_ctx *ctx, const int32_t *d_col, int32_t *d_min, int pass, int check_fix, int64_t *d_hist,
+                    int64_t *d_next_src, unsigned long long *d_sumsq) {
+  ull *key = (ull *)phde_buf(ctx, "sel.key", sizeof(ull));
+  if (!key) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(key, 0, sizeof(ull), ctx->stream));
+  int blocks = (int)std::min<int64_t>((ctx->n + 511) / 512, (int64_t)ctx->nsm * 4);
+  fold_kernel<<<std::max(blocks, 1), 512, 0, ctx->stream>>>(d_col, ctx->n, d_min, key, d_sumsq, ctx->d_err);
+  PHDE_LAUNCHED(ctx);
+  select_kernel<<<1, 1024, 0, ctx->stream>>>(key, d_min, ctx->n, pass, check_fix, d_hist, d_next_src);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}

@@ -1,0 +1,153 @@
+/*
+ * parhde.h -- C ABI of the GB300 ParHDE layout library (libparhde_gb300.so).
+ *
+ * Plain pointers and sizes only.  Host buffers are owned by the caller; device buffers are owned
+ * by the context.  Every call returns an int status (PHDE_OK == 0, negative on error); the message
+ * of the last error is available from phde_last_error().  One context per host thread.
+ *
+ * Reference interfaces replaced (paths relative to the ParHDE source tree):
+ *   - DrawingBase / ParHDE / WParHDE / PivotMDS / PHDE construction + run() + getCoordinates()
+ *     (variants/DrawingBase.h:41-47, spectralDrawing.cpp:176-193)      -> phde_graph_upload + phde_layout
+ *   - DOBFS (gapbs/bfs.cc:144-185, declared variants/DrawingBase.h:62-64) -> phde_DOBFS
+ *   - DeltaStep (gapbs/sssp.cc:53-140, declared variants/DrawingBase.h:65-67) -> phde_DeltaStep
+ *   - the Kcenters distance phase (variants/ParHDE.cpp:118-157, variants/DrawingBase.cpp:119-172)
+ *                                                                        -> phde_kcenters
+ *   - distance columns for given sources (the bit-exactness hook)         -> phde_distances
+ */
+#ifndef PARHDE_GB300_H_
+#define PARHDE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------------------------- */
+#define PHDE_OK 0
+#define PHDE_ERR_INVALID (-1)         /* bad argument (null pointer, unknown algorithm, ...)          */
+#define PHDE_ERR_CSR (-2)             /* malformed CSR: offsets not monotone / not ending at nnz, ...  */
+#define PHDE_ERR_DISCONNECTED (-3)    /* a distance pass did not reach every vertex                   */
+#define PHDE_ERR_K_RANGE (-4)         /* k < 1, k > 256, k >= n, c < 1 or c > k                       */
+#define PHDE_ERR_TOO_FEW_PIVOTS (-5)  /* fewer than k vectors survived D-orthogonalisation           */
+#define PHDE_ERR_OOM (-6)             /* device allocation failed                                     */
+#define PHDE_ERR_NOCONVERGE (-7)      /* eigensolver iteration cap reached                            */
+#define PHDE_ERR_TIMEOUT (-8)         /* a bounded device-side wait gave up                           */
+#define PHDE_ERR_CUDA (-9)            /* CUDA runtime error                                           */
+#define PHDE_ERR_WEIGHTS (-10)        /* weighted algorithm without weights, or the reverse           */
+#define PHDE_ERR_NO_GRAPH (-11)       /* no graph uploaded to the context                             */
+
+/* ---- algorithm / strategy / precision / eigensolver ids ------------------------------------- */
+/* algorithm numbering follows spectralDrawing.cpp:101-109 */
+#define PHDE_ALGO_PIVOTMDS 0
+#define PHDE_ALGO_PHDE 1
+#define PHDE_ALGO_WPARHDE 2
+#define PHDE_ALGO_PARHDE 3
+/* pivot strategies follow the doRand values of spectralDrawing.cpp:88-94 */
+#define PHDE_STRAT_RANDCOARSE 0
+#define PHDE_STRAT_RANDFINE 1
+#define PHDE_STRAT_KCENTERS 2
+/* precision of the dense stages (distances are always exact integers) */
+#define PHDE_PREC_FP64 0  /* every dense stage in FP64, the reference's arithmetic            */
+#define PHDE_PREC_MIXED 1 /* FP32 storage/SpMM, compensated Gram products; FP64 k x k solves  */
+/* eigensolver of the k x k problem */
+#define PHDE_EIG_POWER 0  /* subspace power iteration, ParallelComponents.cpp:48-158 (non-MKL build) */
+#define PHDE_EIG_EXACT 1  /* exact symmetric eigensolve, the LAPACKE_dsyev role (MKL build)          */
+
+#define PHDE_MAX_K 256
+
+typedef struct phde_ctx phde_ctx;
+
+typedef struct {
+  int algo;       /* PHDE_ALGO_*                                                                 */
+  int strategy;   /* PHDE_STRAT_*  (WParHDE always uses Kcenters, as WParHDE.cpp:40-218 does)      */
+  int k;          /* pivots (-r), 1..256                                                          */
+  int c;          /* coordinates (-c), 1..k                                                       */
+  int precision;  /* PHDE_PREC_*                                                                  */
+  int eig;        /* PHDE_EIG_*                                                                   */
+  uint64_t seed;  /* random strategies: glibc rand() stream seed (1 = an unseeded process)          */
+  int verbose;    /* print the reference's progress lines ("discarding vec ...")                  */
+} phde_layout_opts;
+
+typedef struct {
+  int status;
+  int npasses;       /* distance passes (BFS / SSSP) executed                                       */
+  int naccepted;     /* vectors accepted by the D-orthogonalisation                                 */
+  int ndiscarded;    /* candidates discarded (norm < 1e-3 after projection)                         */
+  int eig_iters;     /* power-method sweeps, or Jacobi sweeps                                        */
+  int gpu_launches;  /* kernels this call launched                                                  */
+  double ms_dist;    /* distance phase (device events): BFS/SSSP + Kcenters selection + normalisation */
+  double ms_orth;    /* D-orthogonalisation (or centring for PivotMDS/PHDE)                         */
+  double ms_mmult;   /* Laplacian SpMM + Gram product                                               */
+  double ms_eig;     /* k x k eigensolve                                                             */
+  double ms_coords;  /* coordinates, normalisation and the copy to the host                          */
+  double ms_total;   /* whole call                                                                   */
+  int64_t edges_examined; /* adjacency entries read by the distance passes                          */
+} phde_layout_stats;
+
+/* optional extra outputs of phde_layout (any member may be NULL) */
+typedef struct {
+  double *basis;   /* n*k column-major: the D-orthogonal basis S (ParHDE/WParHDE) or C (PivotMDS/PHDE) */
+  double *gram;    /* k*k column-major: the matrix handed to the eigensolver (S^T L S or C^T C)         */
+  double *evecs;   /* k*k column-major: eigenvector matrix after the solve                              */
+  double *evals;   /* k: eigenvalues (|lambda| for the power method), ascending                         */
+} phde_layout_extra;
+
+/* ---- context -------------------------------------------------------------------------------- */
+int phde_create(phde_ctx **out, int device);
+void phde_destroy(phde_ctx *ctx);
+const char *phde_last_error(const phde_ctx *ctx);
+const char *phde_status_string(int status);
+int phde_version(void);
+
+/* Copy a CSR graph to the device (replaces the CSR arrays handed to the DrawingBase constructor,
+ * variants/DrawingBase.cpp:16-26).  offsets: n+1 entries of offset_bytes (4: uint32 as in the .csr
+ * file, 8: int64); adj: nnz uint32; weights: nnz int32 or NULL.  The offsets are widened to int64 on
+ * the device.  Validates monotone offsets ending at nnz and neighbours < n. */
+int phde_graph_upload(phde_ctx *ctx, const void *offsets, int offset_bytes, const uint32_t *adj,
+                      const int32_t *weights, int64_t n, int64_t nnz);
+int64_t phde_graph_n(const phde_ctx *ctx);
+int64_t phde_graph_nnz(const phde_ctx *ctx);
+
+/* The layout pipeline behind DrawingBase::run() + getCoordinates() (variants/ParHDE.cpp:45-352,
+ * WParHDE.cpp:40-292, PivotMDS.cpp:68-147, PHDE.cpp:50-136, DrawingBase.cpp:196-219) on the uploaded
+ * graph.  coords_out: n*c doubles, column-major (coordinate j of vertex i at i + j*n), each column of
+ * unit L2 norm.  sources_out (optional): the source vertex of every distance pass, capacity 3k.
+ * extra (optional): intermediate matrices.  stats (optional). */
+int phde_layout(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out, int64_t *sources_out,
+                phde_layout_extra *extra, phde_layout_stats *stats);
+
+/* Exact distance columns from the given sources on the uploaded graph: hop counts (unweighted graph)
+ * or weighted shortest-path lengths (weighted graph).  out: n*nsrc int32, column-major; unreachable
+ * vertices get -1 (BFS) or 1073741823 (SSSP, gapbs/sssp.cc:50). */
+int phde_distances(phde_ctx *ctx, const int64_t *sources, int nsrc, int32_t *out);
+
+/* Kcenters distance phase: `passes` distance passes, each starting from the vertex farthest from all
+ * previous sources (lowest index on ties; ParHDE.cpp:118-157).  variant 0 = ParHDE/WParHDE history
+ * rule, 2 = DrawingBase (PivotMDS/PHDE) history rule (DrawingBase.cpp:119-172).  dist_out: n*passes
+ * int32 column-major (may be NULL); sources_out: passes entries. */
+int phde_kcenters(phde_ctx *ctx, int passes, int variant, int32_t *dist_out, int64_t *sources_out);
+
+/* Reference-shaped drop-ins for the two distance kernels (variants/DrawingBase.h:62-67), on host CSR
+ * arrays.  They use a per-thread default context, upload the graph on every call (the reference
+ * functions receive raw CSR pointers), and write only the entries of reached vertices, as the
+ * reference does.  alpha/beta are accepted for signature compatibility; they tune the direction
+ * switch and do not change the result. */
+int phde_DOBFS(const uint32_t *row, const uint32_t *col, long source, long numNodes, long numEdges, double *dists,
+               int alpha, int beta);
+int phde_DeltaStep(const uint32_t *row, const uint32_t *col, const int32_t *weights, long source, long numNodes,
+                   long numEdges, double *dist, int32_t delta);
+
+/* Diagnostics used by the tests: run a grid barrier that can never complete (the kernel expects one
+ * more block than it launches) with the given wait limit, and report the status the kernel returned.
+ * Returns PHDE_ERR_TIMEOUT when the bounded wait gave up as designed. */
+int phde_selftest_barrier_timeout(phde_ctx *ctx, int timeout_ms);
+
+/* Kernel launches issued through this context since it was created. */
+int64_t phde_launch_count(const phde_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARHDE_GB300_H_ */

@@ -559,7 +559,7 @@ static int power_method(double *K, double *evals, int N, int *iters_out) {
   int it = 0, status = ORC_OK;
   while (rr < 1.0 - 1e-3) {
     it++;
-    if (isnan(rr) || isinf(rr) || it > 1000000) {
+    if (isnan(rr) || isinf(rr) || it > 20000) {
       status = ORC_ERR_NOCONVERGE;
       break;
     }
