@@ -113,10 +113,22 @@ int phde_reset_sync(phde_ctx *ctx) {
   return PHDE_OK;
 }
 
+void phde_collect_kernel_time(phde_ctx *ctx) {
+  if (!ctx->kev_pending) return;
+  float t = 0;
+  if (cudaEventElapsedTime(&t, ctx->kev[0], ctx->kev[1]) == cudaSuccess) {
+    ctx->kernel_ms += t;
+    ctx->kernel_launches++;
+  }
+  cudaGetLastError();
+  ctx->kev_pending = false;
+}
+
 int phde_check_device_err(phde_ctx *ctx, const char *what) {
   int e = 0;
   PHDE_CK(ctx, cudaMemcpyAsync(&e, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  phde_collect_kernel_time(ctx);
   if (e == PHDE_ERR_DISCONNECTED) return phde_fail(ctx, e, std::string(what) + ": the graph is not connected");
   if (e == PHDE_ERR_TIMEOUT) return phde_fail(ctx, e, std::string(what) + ": a bounded device wait gave up");
   if (e) return phde_fail(ctx, e, std::string(what) + ": device error " + std::to_string(e));
@@ -170,6 +182,7 @@ int phde_create(phde_ctx **out, int device) {
     return PHDE_ERR_CUDA;
   }
   for (auto &e : c->ev) cudaEventCreate(&e);
+  for (auto &e : c->kev) cudaEventCreate(&e);
   if (const char *t = getenv("PHDE_WAIT_LIMIT_MS")) c->timeout_ns = (uint64_t)atoll(t) * 1000000ull;
   *out = c;
   return PHDE_OK;
@@ -186,6 +199,7 @@ void phde_destroy(phde_ctx *c) {
   cudaFree(c->d_sync);
   cudaFree(c->d_err);
   for (auto &e : c->ev) cudaEventDestroy(e);
+  for (auto &e : c->kev) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -262,6 +276,9 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   const bool hde = algo == PHDE_ALGO_PARHDE || algo == PHDE_ALGO_WPARHDE;
   Timer tm(ctx);
   const long long launches0 = ctx->launches;
+  ctx->kernel_ms = 0;
+  ctx->kernel_launches = 0;
+  ctx->kev_pending = false;
   tm.mark(0);
   double *deg = (double *)phde_buf(ctx, "deg", sizeof(double) * n);
   ull *edges = (ull *)phde_buf(ctx, "edges", sizeof(ull));
@@ -428,6 +445,8 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     st->ms_total = tm.ms(0, 5);
     st->edges_examined = (int64_t)h_edges;
     st->gpu_launches = (int)(ctx->launches - launches0);
+    st->ms_dist_kernel = ctx->kernel_ms;
+    st->dist_kernel_launches = ctx->kernel_launches;
   }
   return PHDE_OK;
 }

@@ -30,7 +30,15 @@ struct phde_ctx {
 
   std::map<std::string, std::pair<void *, size_t>> ws;
   cudaEvent_t ev[8] = {};
+  // events bracketing each distance-kernel launch; kev_pending says a pair was recorded
+  cudaEvent_t kev[2] = {};
+  bool kev_pending = false;
+  double kernel_ms = 0;  // accumulated by phde_collect_kernel_time()
+  int kernel_launches = 0;
 };
+
+// Add the elapsed time of the last bracketed distance-kernel launch (the stream must have drained).
+void phde_collect_kernel_time(phde_ctx *ctx);
 
 // Set the context error message and return `status`.
 int phde_fail(phde_ctx *ctx, int status, const std::string &msg);

@@ -293,8 +293,11 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   a.alpha = 15;
   a.beta = 18;
   void *args[] = {&a};
+  cudaEventRecord(ctx->kev[0], ctx->stream);
   PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)kcenters_bfs_kernel, dim3(ctx->nsm * per_sm),
                                            dim3(KC_THREADS), args, smem, ctx->stream));
   PHDE_LAUNCHED(ctx);
+  cudaEventRecord(ctx->kev[1], ctx->stream);
+  ctx->kev_pending = true;
   return PHDE_OK;
 }

@@ -310,9 +310,12 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   a.err = ctx->d_err;
   a.timeout_ns = ctx->timeout_ns;
   void *args[] = {&a};
+  cudaEventRecord(ctx->kev[0], ctx->stream);
   PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)sssp_nearfar_kernel, dim3(ctx->nsm * per_sm),
                                            dim3(SS_THREADS), args, 0, ctx->stream));
   PHDE_LAUNCHED(ctx);
+  cudaEventRecord(ctx->kev[1], ctx->stream);
+  ctx->kev_pending = true;
   return PHDE_OK;
 }
 

@@ -84,6 +84,8 @@ typedef struct {
   double ms_coords;  /* coordinates, normalisation and the copy to the host                          */
   double ms_total;   /* whole call                                                                   */
   int64_t edges_examined; /* adjacency entries read by the distance passes                          */
+  double ms_dist_kernel;  /* device time of the distance kernel launches alone (events around each launch) */
+  int dist_kernel_launches; /* number of distance kernel launches (1 for the Kcenters BFS)           */
 } phde_layout_stats;
 
 /* optional extra outputs of phde_layout (any member may be NULL) */

@@ -626,7 +626,7 @@ static int jacobi_eig(double *K, double *evals, int N, int *sweeps_out) {
         tot += a;
         if (i != j) off += a;
       }
-    if (off <= 1e-30 * tot || off == 0) break;
+    if (off <= 1e-28 * tot || off == 0) break;
     for (int p = 0; p < N - 1; p++)
       for (int q = p + 1; q < N; q++) {
         double apq = A[p + q * N];

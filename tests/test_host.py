@@ -1,0 +1,89 @@
+"""Host-side logic that needs no GPU: file formats, generators, and the C ABI library's exports."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+from icpp_2020_parhde_gb300 import csr_io, graphs
+from icpp_2020_parhde_gb300 import build as pbuild
+
+
+def test_csr_roundtrip(tmp_path):
+    g, _ = load_golden("grid12w")
+    p = str(tmp_path / "g.csr")
+    csr_io.write_csr(p, g)
+    h = csr_io.read_csr(p, weighted=True)
+    assert np.array_equal(h.offsets, g.offsets) and np.array_equal(h.adj, g.adj)
+    assert np.array_equal(h.weights, g.weights)
+    hdr = np.fromfile(p, dtype="<i8", count=6)
+    assert list(hdr) == [g.n, g.nnz, 1, 0, 1, 0]  # mtx2csr.cpp:281-291
+    with open(p, "r+b") as f:
+        f.truncate(100)
+    with pytest.raises(ValueError):
+        csr_io.read_csr(p)
+
+
+def test_nxyz_format_matches_ostream_default():
+    # std::ostream default float format: %g, 6 significant digits (spectralDrawing.cpp:59-61)
+    xy = np.array([[0.1234567, -1e-7], [12345678.0, 0.0], [-0.5, 1.0 / 3.0]])
+    assert csr_io.format_nxyz(xy) == "0.123457,-1e-07\n1.23457e+07,0\n-0.5,0.333333\n"
+
+
+def test_generators_sizes():
+    g = graphs.mesh(125, 125, seed=1)
+    assert g.n == 15625 and g.nnz == 2 * 46376
+    g = graphs.grid3d(8, weighted=True, seed=2)
+    assert g.n == 512 and g.nnz == 2 * 3 * 7 * 64
+    assert g.weights.min() >= 1 and g.weights.max() <= 255
+    # weights are symmetric
+    deg = np.diff(g.offsets.astype(np.int64))
+    src = np.repeat(np.arange(g.n), deg)
+    w = {(int(a), int(b)): int(c) for a, b, c in zip(src, g.adj, g.weights)}
+    assert all(w[(b, a)] == c for (a, b), c in w.items())
+    g = graphs.rmat(10, seed=4)
+    assert np.all(np.diff(g.offsets.astype(np.int64)) > 0)  # LCC: no isolated vertices
+    for i in range(0, g.n, 97):
+        row = g.adj[g.offsets[i]:g.offsets[i + 1]]
+        assert np.all(np.diff(row.astype(np.int64)) > 0) and i not in row  # sorted, no dups, no self loops
+
+
+def _declared_functions():
+    decl = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            decl |= set(re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(phde_\w+)\s*\(", txt, re.M))
+    return decl
+
+
+def test_library_exports_every_declared_symbol():
+    path = pbuild.build()
+    lib = ctypes.CDLL(path)
+    decl = _declared_functions()
+    assert len(decl) >= 15
+    missing = [f for f in sorted(decl) if not hasattr(lib, f)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    for f in decl:
+        assert re.search(r"\bT %s$" % f, out, re.M), f
+
+
+def test_status_strings_without_gpu():
+    lib = ctypes.CDLL(pbuild.build())
+    lib.phde_status_string.restype = ctypes.c_char_p
+    assert lib.phde_status_string(0) == b"ok"
+    assert b"connected" in lib.phde_status_string(-3)
+    assert lib.phde_version() >= 10000
+
+
+def test_status_codes_agree_with_oracle():
+    txt = open(os.path.join(ROOT, "include", "parhde.h")).read()
+    codes = dict(re.findall(r"#define PHDE_(ERR_\w+|OK)\s+\(?(-?\d+)\)?", txt))
+    src = open(os.path.join(ROOT, "oracle", "parhde_oracle.c")).read()
+    for name, val in re.findall(r"#define ORC_(ERR_\w+|OK)\s+\(?(-?\d+)\)?", src):
+        key = {"ERR_K_RANGE": "ERR_K_RANGE"}.get(name, name)
+        assert codes[key] == val, name

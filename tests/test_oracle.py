@@ -1,0 +1,96 @@
+"""The oracle (CPU restatement, oracle/parhde_oracle.c) against the golden fixtures recorded from the
+reference itself, and against the live reference build when it is present (this container only)."""
+import ctypes
+import ctypes.util
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_NAMES, golden_runs, load_golden
+from oracle import oracle as orc
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_distances_match_reference_goldens(name):
+    g, rec = load_golden(name)
+    for i, s in enumerate(rec["bfs_src"]):
+        want = rec["bfs_dist"][:, i]
+        if g.weights is not None:
+            assert np.array_equal(orc.sssp(g, int(s)), want)
+            assert np.array_equal(orc.sssp(g, int(s), parallel=True), want)
+        else:
+            assert np.array_equal(orc.bfs(g, int(s)), want)
+            assert np.array_equal(orc.bfs(g, int(s), parallel=True), want)
+
+
+@pytest.mark.parametrize("case", golden_runs(), ids=lambda c: "%s-%s-k%d-c%d" % c)
+def test_layout_matches_reference_goldens(case):
+    name, algo, k, c = case
+    g, rec = load_golden(name)
+    ref_src = rec[f"{algo}_k{k}_c{c}_sources"]
+    ref_xy = rec[f"{algo}_k{k}_c{c}_coords"]
+    for dist_algo in ("serial", "parallel"):
+        L = orc.layout(g, algo, "Kcenters", k, c, nthreads=1, dist_algo=dist_algo)
+        if L.status == -5:
+            # the reference's pivot-count check is off by one (ParHDE.cpp:192,281): it carries on with
+            # k-1 vectors where the oracle reports too few pivots
+            assert L.stats.naccepted == k - 1
+            continue
+        assert L.status == 0
+        assert np.array_equal(L.sources, ref_src[: len(L.sources)])
+        # one thread, same operation order: the restatement reproduces the reference to the last bit or two
+        np.testing.assert_allclose(L.coords, ref_xy, rtol=0, atol=1e-12)
+
+
+def test_kcenters_variants_agree_on_connected_graph():
+    g, _ = load_golden("rmat13")
+    d0, s0 = orc.kcenters(g, 30, 0)
+    d1, s1 = orc.kcenters(g, 30, 0, parallel=True, nthreads=4)
+    assert np.array_equal(s0, s1) and np.array_equal(d0, d1)
+
+
+def test_glibc_rand_stream_matches_libc():
+    libc = ctypes.CDLL(ctypes.util.find_library("c"))
+    for seed in (1, 7, 12345):
+        libc.srand(seed)
+        want = np.array([libc.rand() for _ in range(1000)], dtype=np.int32)
+        assert np.array_equal(orc.glibc_rand(seed, 1000), want)
+
+
+def test_exact_eigensolve_matches_numpy():
+    g, _ = load_golden("rmat13")
+    L = orc.layout(g, "ParHDE", k=20, c=3, eig="exact", nthreads=2)
+    assert L.status == 0
+    M = 0.5 * (L.M + L.M.T)
+    w, V = np.linalg.eigh(M)
+    np.testing.assert_allclose(L.evals, w, rtol=0, atol=1e-12 * np.abs(w).max())
+    # eigenvector columns agree up to sign
+    for j in range(20):
+        assert abs(abs(np.dot(L.evecs[:, j], V[:, j])) - 1) < 1e-8
+
+
+def test_oracle_errors():
+    g, _ = load_golden("mesh125")
+    assert orc.layout(g, "ParHDE", k=300, c=2).status == -4  # k out of range
+    assert orc.layout(g, "ParHDE", k=10, c=11).status == -4
+    gw, _ = load_golden("grid12w")
+    from icpp_2020_parhde_gb300.csr_io import CSRGraph
+    unweighted = CSRGraph(gw.offsets, gw.adj, None)
+    with pytest.raises(ValueError):
+        orc.layout(unweighted, "wParHDE", k=5, c=2)
+    # two disjoint triangles: disconnected
+    off = np.array([0, 2, 4, 6, 8, 10, 12], dtype=np.uint32)
+    adj = np.array([1, 2, 0, 2, 0, 1, 4, 5, 3, 5, 3, 4], dtype=np.uint32)
+    assert orc.layout(CSRGraph(off, adj), "ParHDE", k=2, c=2).status == -3
+
+
+@pytest.mark.skipif(not orc.ref_available(), reason="reference build (oracle/_ref) not present")
+@pytest.mark.parametrize("algo,k,c", [("ParHDE", 10, 2), ("PivotMDS", 8, 2), ("PHDE", 8, 3)])
+def test_oracle_matches_live_reference_rgg(algo, k, c):
+    from icpp_2020_parhde_gb300 import graphs
+    g = graphs.rgg(5000, dim=2, avg_degree=8, seed=11)
+    L = orc.layout(g, algo, "Kcenters", k, c, nthreads=1)
+    xy, src = orc.ref_layout(g, algo, "Kcenters", k, c, nthreads=1)
+    assert L.status == 0
+    assert np.array_equal(L.sources, src)
+    np.testing.assert_allclose(L.coords, xy, rtol=0, atol=1e-12)
