@@ -25,9 +25,10 @@ int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale, double *S,
 int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS, int k);
 int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M);
 int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C);
-int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X);
+int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X, int seq);
+int phde_gram_seq(phde_ctx *ctx, const double *C, int k, double *M);
 int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
-                    double *d_evals, double *d_Y, int *h_iters);
+                    double *d_evals, double *d_Y, int *h_iters, int seq);
 
 namespace {
 
@@ -232,6 +233,7 @@ int phde_graph_upload(phde_ctx *ctx, const void *offsets, int offset_bytes, cons
   }
   ctx->n = n;
   ctx->nnz = nnz;
+  ctx->graph_epoch++;
   if (offset_bytes == 8) {
     PHDE_CK(ctx, cudaMemcpyAsync(ctx->d_off, offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
   } else {
@@ -402,17 +404,17 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     if ((rc = phde_lap_spmm(ctx, deg, Sbuf, LS, k))) return rc;
     if ((rc = phde_gram(ctx, Sbuf, LS, k, M))) return rc;
   } else {
-    if ((rc = phde_gram(ctx, Sbuf, Sbuf, k, M))) return rc;
+    if ((rc = phde_gram_seq(ctx, Sbuf, k, M))) return rc;  // reference summation order: bit-exact C^T C
   }
   tm.mark(3);
   if (extra && extra->gram)
     PHDE_CK(ctx, cudaMemcpyAsync(extra->gram, M, sizeof(double) * k * k, cudaMemcpyDeviceToHost, ctx->stream));
   int iters = 0;
-  if ((rc = phde_eigensolve(ctx, M, k, c, hde ? 0 : 1, o->eig, K, ev, Y, &iters))) return rc;
+  if ((rc = phde_eigensolve(ctx, M, k, c, hde ? 0 : 1, o->eig, K, ev, Y, &iters, !hde))) return rc;
   tm.mark(4);
   double *X = (double *)phde_buf(ctx, "layout.X", sizeof(double) * n * c);
   if (!X) return PHDE_ERR_OOM;
-  if ((rc = phde_coords(ctx, Sbuf, Y, k, c, X))) return rc;
+  if ((rc = phde_coords(ctx, Sbuf, Y, k, c, X, !hde))) return rc;
   PHDE_CK(ctx, cudaMemcpyAsync(coords_out, X, sizeof(double) * n * c, cudaMemcpyDeviceToHost, ctx->stream));
   tm.mark(5);
   if (sources_out && npasses > 0)

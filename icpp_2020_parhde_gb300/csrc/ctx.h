@@ -23,6 +23,9 @@ struct phde_ctx {
   int64_t *d_off = nullptr;
   uint32_t *d_adj = nullptr;
   int32_t *d_w = nullptr;
+  long long graph_epoch = 0;  // bumped by every upload; caches keyed on it (the SpMM chunk plan)
+  long long spmm_plan_epoch = -1;
+  int64_t spmm_nheavy = 0, spmm_nchunks = 0;
 
   // device control block for persistent kernels: barrier + error word
   GridSync *d_sync = nullptr;

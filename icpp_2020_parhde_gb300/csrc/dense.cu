@@ -23,7 +23,7 @@
 
 namespace {
 
-constexpr int CGS_THREADS = 512;
+constexpr int CGS_THREADS = 256;
 constexpr int MAXQ = 8;  // columns per lane: k <= 256
 
 // ------------------------------------------------------------------------------------------------
@@ -48,18 +48,19 @@ struct CgsArgs {
 };
 
 __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
-  extern __shared__ double sm[];  // [nwarps][k+2]
+  extern __shared__ double sm[];  // [nwarps][k+2] reduction scratch, then coefficients
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int64_t n = a.n;
   const int k = a.k, ld = k + 2;
   const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
   const double inv0 = 1.0 / sqrt((double)n);  // the constant column: 1 * (1/||1||), ParHDE.cpp:96-108
 
   // denominator of the constant column, sum_i u0*u0*d_i
   double acc = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    acc += __dmul_rn(__dmul_rn(inv0, inv0), a.deg[i]);
+  const double u02 = inv0 * inv0;
+  for (int64_t i = gt; i < n; i += gts) acc = fma(u02, a.deg[i], acc);
   acc = block_sum(acc, red);
   if (threadIdx.x == 0) a.part2[blockIdx.x] = acc;
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
@@ -76,40 +77,30 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
     const int32_t *Dc = a.D + (int64_t)rc * n;
     const double inv_rc = 1.0 / sqrt((double)__ldcg(a.sumsq + rc));  // ParHDE.cpp:179-184
     const int jm1 = j - 1;
-    // ---- A: dots against the accepted columns and the constant column ----
+    // ---- A: dots <x, D S_q> for the accepted columns q < j-1, and <x, D u0> in slot q == j-1 ----
     double accq[MAXQ];
 #pragma unroll
     for (int t = 0; t < MAXQ; t++) accq[t] = 0;
-    double acc0 = 0, accd = 0;
     for (int64_t i = gw; i < n; i += gws) {
-      const double x = __dmul_rn((double)Dc[i], inv_rc);
-      const double di = a.deg[i];
+      const double xd = (double)Dc[i] * inv_rc * a.deg[i];
       const double *Si = a.S + i * k;
 #pragma unroll
       for (int t = 0; t < MAXQ; t++) {
         const int q = lane + 32 * t;
-        if (q < jm1) accq[t] += __dmul_rn(__dmul_rn(x, __ldcg(Si + q)), di);
-      }
-      if (lane == 0) {
-        acc0 += __dmul_rn(__dmul_rn(x, inv0), di);
-        if (newcol) {
-          const double s = __ldcg(Si + (j - 2));
-          accd += __dmul_rn(__dmul_rn(s, s), di);
-        }
+        if (q < jm1)
+          accq[t] = fma(xd, __ldcg(Si + q), accq[t]);
+        else if (q == jm1)
+          accq[t] = fma(xd, inv0, accq[t]);
       }
     }
 #pragma unroll
     for (int t = 0; t < MAXQ; t++) {
       const int q = lane + 32 * t;
-      if (q < jm1) sm[warp * ld + q] = accq[t];
-    }
-    if (lane == 0) {
-      sm[warp * ld + k] = acc0;
-      sm[warp * ld + k + 1] = accd;
+      if (q <= jm1) sm[warp * ld + (q == jm1 ? k : q)] = accq[t];
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < k + 2; q += blockDim.x) {
-      if (q < jm1 || q >= k) {
+    for (int q = threadIdx.x; q < k + 1; q += blockDim.x) {
+      if (q < jm1 || q == k) {
         double s = 0;
         for (int w = 0; w < nw; w++) s += sm[w * ld + q];
         a.part[(int64_t)blockIdx.x * ld + q] = s;
@@ -119,52 +110,47 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
     // ---- C: one block per coefficient sums the block partials in a fixed order ----
     for (int q = blockIdx.x; q < j; q += gridDim.x) {
       const int slot = q == jm1 ? k : q;  // q == j-1 stands for the constant column
+      const bool fresh = newcol && q == j - 2;  // column accepted by the previous candidate
       double s = 0, sd = 0;
       for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
         s += __ldcg(a.part + (int64_t)b * ld + slot);
-        if (newcol && q == j - 2) sd += __ldcg(a.part + (int64_t)b * ld + k + 1);
+        if (fresh) sd += __ldcg(a.part + (int64_t)b * ld + k + 1);
       }
       s = block_sum(s, red);
-      if (newcol && q == j - 2) {
-        sd = block_sum(sd, red);
-        if (threadIdx.x == 0) a.inv_den[q] = 1.0 / sd;
-      }
+      if (fresh) sd = block_sum(sd, red);
       if (threadIdx.x == 0) {
-        const double id = slot == k ? inv_den0 : (newcol && q == j - 2 ? 1.0 / sd : __ldcg(a.inv_den + q));
-        a.coef[slot] = __dmul_rn(s, id);
+        double id;
+        if (slot == k) {
+          id = inv_den0;
+        } else if (fresh) {
+          id = 1.0 / sd;
+          a.inv_den[q] = id;
+        } else {
+          id = __ldcg(a.inv_den + q);
+        }
+        a.coef[slot] = s * id;
       }
       __syncthreads();
     }
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-    // ---- E: x' = x - (sum_q coef_q S_q + coef_0 u0), and its squared norm ----
-    double cq[MAXQ];
-#pragma unroll
-    for (int t = 0; t < MAXQ; t++) {
-      const int q = lane + 32 * t;
-      cq[t] = q < jm1 ? __ldcg(a.coef + q) : 0.0;
-    }
-    const double c0 = __ldcg(a.coef + k);
+    // ---- E: x' = x - (sum_q coef_q S_q + coef_0 u0), one thread per row; and ||x'||^2 ----
+    __syncthreads();
+    for (int q = threadIdx.x; q < jm1; q += blockDim.x) sm[q] = __ldcg(a.coef + q);
+    __syncthreads();
+    const double c0u0 = __ldcg(a.coef + k) * inv0;
     double ssq = 0;
-    for (int64_t i = gw; i < n; i += gws) {
-      const double x = __dmul_rn((double)Dc[i], inv_rc);
+    for (int64_t i = gt; i < n; i += gts) {
       const double *Si = a.S + i * k;
-      double part = 0;
-#pragma unroll
-      for (int t = 0; t < MAXQ; t++) {
-        const int q = lane + 32 * t;
-        if (q < jm1) part += __dmul_rn(cq[t], __ldcg(Si + q));
-      }
-      part = warp_sum(part);
-      if (lane == 0) {
-        const double xp = __dsub_rn(x, __dadd_rn(part, __dmul_rn(c0, inv0)));
-        a.X[i] = xp;
-        ssq += __dmul_rn(xp, xp);
-      }
+      double p = 0;
+      for (int q = 0; q < jm1; q++) p = fma(sm[q], __ldcg(Si + q), p);
+      const double xp = (double)Dc[i] * inv_rc - (p + c0u0);
+      a.X[i] = xp;
+      ssq = fma(xp, xp, ssq);
     }
     ssq = block_sum(ssq, red);
     if (threadIdx.x == 0) a.part2[blockIdx.x] = ssq;
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-    // ---- G: norm test (ParHDE.cpp:267) and acceptance ----
+    // ---- G: norm test (ParHDE.cpp:267) and acceptance; the new column's D-norm partials ----
     double nrm2 = 0;
     for (int b = 0; b < (int)gridDim.x; b++) nrm2 += __ldcg(a.part2 + b);
     const double nrm = sqrt(nrm2);
@@ -174,8 +160,14 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
       newcol = false;
     } else {
       const double scale = 1.0 / nrm;
-      for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        a.S[i * k + (j - 1)] = __dmul_rn(__ldcg(a.X + i), scale);
+      double dd = 0;
+      for (int64_t i = gt; i < n; i += gts) {
+        const double v = __ldcg(a.X + i) * scale;
+        a.S[i * k + (j - 1)] = v;
+        dd = fma(v * v, a.deg[i], dd);
+      }
+      dd = block_sum(dd, red);
+      if (threadIdx.x == 0) a.part[(int64_t)blockIdx.x * ld + k + 1] = dd;
       j++;
       newcol = true;
       if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
@@ -273,13 +265,84 @@ __global__ void degrees_kernel(const int64_t *off, const int32_t *w, int64_t n, 
   }
 }
 
-// LS[i,q] = d_i*S[i,q] - sum_{e in row i} w_e*S[adj_e,q], neighbours in CSR order.
-__global__ void lap_spmm_kernel(const int64_t *off, const uint32_t *adj, const int32_t *w, const double *deg,
-                                const double *S, double *LS, int64_t n, int k) {
+// ---- Laplacian SpMM, load balanced ----
+// Rows of degree <= SPMM_HEAVY are done by one warp each, neighbours in CSR order (the reference's
+// exact subtraction sequence, ParHDE.cpp:293-298), four neighbour rows in flight.  Heavier rows (R-MAT
+// hubs) are cut into chunks of SPMM_CHUNK neighbours; one warp sums each chunk, and a fix-up pass forms
+// LS = d*S - (sum of the chunk partials in chunk order), so the result is deterministic.
+constexpr int SPMM_HEAVY = 512, SPMM_CHUNK = 512;
+
+struct HeavyRow {
+  int64_t row;
+  int64_t first_chunk;
+  int64_t nchunks;
+};
+struct Chunk {
+  int64_t e0, e1;
+};
+
+__global__ void spmm_plan_kernel(const int64_t *off, int64_t n, HeavyRow *heavy, Chunk *chunks, ull *counts) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e0 = off[i], e1 = off[i + 1], deg = e1 - e0;
+    if (deg <= SPMM_HEAVY) continue;
+    const int64_t nch = (deg + SPMM_CHUNK - 1) / SPMM_CHUNK;
+    const int64_t base = (int64_t)atomicAdd(counts + 1, (ull)nch);
+    const int64_t h = (int64_t)atomicAdd(counts, 1ull);
+    heavy[h] = HeavyRow{i, base, nch};
+    for (int64_t c = 0; c < nch; c++) chunks[base + c] = Chunk{e0 + c * SPMM_CHUNK, min(e1, e0 + (c + 1) * SPMM_CHUNK)};
+  }
+}
+
+template <bool W>
+__device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32_t *w, const double *S, int k,
+                                                int lane, int64_t e0, int64_t e1, double (&acc)[MAXQ]) {
+  int64_t e = e0;
+  for (; e + 4 <= e1; e += 4) {
+    const int64_t v0 = __ldg(adj + e), v1 = __ldg(adj + e + 1), v2 = __ldg(adj + e + 2), v3 = __ldg(adj + e + 3);
+    double w0 = 1, w1 = 1, w2 = 1, w3 = 1;
+    if (W) {
+      w0 = (double)__ldg(w + e);
+      w1 = (double)__ldg(w + e + 1);
+      w2 = (double)__ldg(w + e + 2);
+      w3 = (double)__ldg(w + e + 3);
+    }
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) {
+        const double s0 = S[v0 * k + q], s1 = S[v1 * k + q], s2 = S[v2 * k + q], s3 = S[v3 * k + q];
+        if (W) {
+          acc[t] = __dsub_rn(acc[t], __dmul_rn(w0, s0));
+          acc[t] = __dsub_rn(acc[t], __dmul_rn(w1, s1));
+          acc[t] = __dsub_rn(acc[t], __dmul_rn(w2, s2));
+          acc[t] = __dsub_rn(acc[t], __dmul_rn(w3, s3));
+        } else {
+          acc[t] = __dsub_rn(__dsub_rn(__dsub_rn(__dsub_rn(acc[t], s0), s1), s2), s3);
+        }
+      }
+    }
+  }
+  for (; e < e1; e++) {
+    const int64_t v = __ldg(adj + e);
+    const double we = W ? (double)__ldg(w + e) : 1.0;
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) acc[t] = W ? __dsub_rn(acc[t], __dmul_rn(we, S[v * k + q])) : __dsub_rn(acc[t], S[v * k + q]);
+    }
+  }
+}
+
+// Light rows: LS[i,q] = d_i*S[i,q] - sum_e w_e*S[adj_e,q].  Heavy rows are skipped here.
+template <bool W>
+__global__ void spmm_light_kernel(const int64_t *off, const uint32_t *adj, const int32_t *w, const double *deg,
+                                  const double *S, double *LS, int64_t n, int k) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = gw; i < n; i += gws) {
+    const int64_t e0 = off[i], e1 = off[i + 1];
+    if (e1 - e0 > SPMM_HEAVY) continue;
     const double di = deg[i];
     double acc[MAXQ];
 #pragma unroll
@@ -287,29 +350,53 @@ __global__ void lap_spmm_kernel(const int64_t *off, const uint32_t *adj, const i
       const int q = lane + 32 * t;
       acc[t] = q < k ? __dmul_rn(di, S[i * k + q]) : 0.0;
     }
-    const int64_t e0 = off[i], e1 = off[i + 1];
-    for (int64_t e = e0; e < e1; e++) {
-      const int64_t v = __ldg(adj + e);
-      const double *Sv = S + v * k;
-      if (w == nullptr) {
-#pragma unroll
-        for (int t = 0; t < MAXQ; t++) {
-          const int q = lane + 32 * t;
-          if (q < k) acc[t] = __dsub_rn(acc[t], Sv[q]);
-        }
-      } else {
-        const double we = (double)__ldg(w + e);
-#pragma unroll
-        for (int t = 0; t < MAXQ; t++) {
-          const int q = lane + 32 * t;
-          if (q < k) acc[t] = __dsub_rn(acc[t], __dmul_rn(we, Sv[q]));
-        }
-      }
-    }
+    spmm_accumulate<W>(adj, w, S, k, lane, e0, e1, acc);
 #pragma unroll
     for (int t = 0; t < MAXQ; t++) {
       const int q = lane + 32 * t;
       if (q < k) LS[i * k + q] = acc[t];
+    }
+  }
+}
+
+// Heavy-row chunks: part[c, q] = sum over the chunk of w_e*S[adj_e,q].
+template <bool W>
+__global__ void spmm_chunk_kernel(const uint32_t *adj, const int32_t *w, const double *S, const Chunk *chunks,
+                                  int64_t nchunks, double *part, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = gw; c < nchunks; c += gws) {
+    double acc[MAXQ];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) acc[t] = 0.0;
+    const Chunk ch = chunks[c];
+    spmm_accumulate<W>(adj, w, S, k, lane, ch.e0, ch.e1, acc);  // accumulates -sum
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) part[c * k + q] = acc[t];
+    }
+  }
+}
+
+__global__ void spmm_heavy_fix_kernel(const HeavyRow *heavy, int64_t nheavy, const double *deg, const double *S,
+                                      const double *part, double *LS, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t h = gw; h < nheavy; h += gws) {
+    const HeavyRow hr = heavy[h];
+    const int64_t i = hr.row;
+    const double di = deg[i];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) {
+        double a = __dmul_rn(di, S[i * k + q]);
+        for (int64_t c = 0; c < hr.nchunks; c++) a = __dadd_rn(a, part[(hr.first_chunk + c) * k + q]);
+        LS[i * k + q] = a;
+      }
     }
   }
 }
@@ -369,6 +456,40 @@ __global__ void sum_parts_kernel(const double *part, int splits, int64_t len, do
     for (int b = 0; b < splits; b++) s += part[(int64_t)b * len + i];
     out[i] = s;
   }
+}
+
+// ---- reference-order kernels (PivotMDS / PHDE) ----
+// The centred matrix C of PivotMDS/PHDE is bit-identical to the reference's (exact integer sums), so
+// when every later sum follows the reference's one-thread order -- C^T C entry by entry over rows in
+// order (DrawingBase.cpp:226-237), X = C*Y over pivots in order (DrawingBase.cpp:212-217), the norm of
+// each coordinate over vertices in order (ParallelComponents.cpp:13-20) -- the coordinates are too.
+__global__ void gram_seq_kernel(const double *C, int64_t n, int k, double *M) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= k * k) return;
+  const int p = idx / k, q = idx % k;
+  double s = 0;
+  for (int64_t i = 0; i < n; i++) s = __dadd_rn(s, __dmul_rn(C[i * k + p], C[i * k + q]));
+  M[q + (int64_t)p * k] = s;
+}
+
+__global__ void coords_seq_kernel(const double *M, const double *Y, int64_t n, int k, int c, double *X) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * c;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % n;
+    const int t = (int)(idx / n);
+    double s = 0;
+    for (int j = 0; j < k; j++) s = __dadd_rn(s, __dmul_rn(M[i * k + j], Y[j + (int64_t)t * k]));
+    X[idx] = s;
+  }
+}
+
+// one block per coordinate; lane 0 sums the squares in vertex order
+__global__ void colnorm_seq_kernel(const double *X, int64_t n, double *part) {
+  if (threadIdx.x != 0) return;
+  const double *x = X + (int64_t)blockIdx.x * n;
+  double s = 0;
+  for (int64_t i = 0; i < n; i++) s = __dadd_rn(s, __dmul_rn(x[i], x[i]));
+  part[blockIdx.x] = s;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -495,7 +616,7 @@ int phde_cgs(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const dou
   PHDE_CK(ctx, cudaFuncSetAttribute(cgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cgs_kernel, CGS_THREADS, smem));
   if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "cgs kernel cannot be resident");
-  per_sm = std::min(per_sm, 2);
+  per_sm = std::min(per_sm, 4);
   const int grid = ctx->nsm * per_sm;
   double *X = (double *)phde_buf(ctx, "cgs.X", sizeof(double) * n);
   double *part = (double *)phde_buf(ctx, "cgs.part", sizeof(double) * grid * (size_t)(k + 2));
@@ -575,12 +696,56 @@ int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale, double *S,
   return PHDE_OK;
 }
 
+// Heavy-row chunk plan, built once per uploaded graph (ctx->spmm_plan_n tracks which graph).
+static int spmm_plan(phde_ctx *ctx, HeavyRow **heavy, Chunk **chunks, int64_t *nheavy, int64_t *nchunks) {
+  const int64_t cap_h = ctx->nnz / SPMM_HEAVY + 1, cap_c = ctx->nnz / SPMM_CHUNK + cap_h + 1;
+  *heavy = (HeavyRow *)phde_buf(ctx, "spmm.heavy", sizeof(HeavyRow) * cap_h);
+  *chunks = (Chunk *)phde_buf(ctx, "spmm.chunks", sizeof(Chunk) * cap_c);
+  ull *counts = (ull *)phde_buf(ctx, "spmm.counts", sizeof(ull) * 2);
+  if (!*heavy || !*chunks || !counts) return PHDE_ERR_OOM;
+  if (ctx->spmm_plan_epoch != ctx->graph_epoch) {
+    PHDE_CK(ctx, cudaMemsetAsync(counts, 0, sizeof(ull) * 2, ctx->stream));
+    spmm_plan_kernel<<<grid_for(ctx, ctx->n, 256), 256, 0, ctx->stream>>>(ctx->d_off, ctx->n, *heavy, *chunks, counts);
+    PHDE_LAUNCHED(ctx);
+    ull h[2];
+    PHDE_CK(ctx, cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->spmm_nheavy = (int64_t)h[0];
+    ctx->spmm_nchunks = (int64_t)h[1];
+    ctx->spmm_plan_epoch = ctx->graph_epoch;
+  }
+  *nheavy = ctx->spmm_nheavy;
+  *nchunks = ctx->spmm_nchunks;
+  return PHDE_OK;
+}
+
 int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS, int k) {
+  HeavyRow *heavy;
+  Chunk *chunks;
+  int64_t nheavy, nchunks;
+  int rc = spmm_plan(ctx, &heavy, &chunks, &nheavy, &nchunks);
+  if (rc) return rc;
   const int threads = 256;
+  const int32_t *w = ctx->weighted ? ctx->d_w : nullptr;
   const int grid = grid_for(ctx, ctx->n * 32, threads, 8);
-  lap_spmm_kernel<<<grid, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, ctx->weighted ? ctx->d_w : nullptr, deg,
-                                                     S, LS, ctx->n, k);
+  if (w)
+    spmm_light_kernel<true><<<grid, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, w, deg, S, LS, ctx->n, k);
+  else
+    spmm_light_kernel<false><<<grid, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, w, deg, S, LS, ctx->n, k);
   PHDE_LAUNCHED(ctx);
+  if (nheavy > 0) {
+    double *part = (double *)phde_buf(ctx, "spmm.part", sizeof(double) * nchunks * k);
+    if (!part) return PHDE_ERR_OOM;
+    const int g2 = grid_for(ctx, nchunks * 32, threads, 8);
+    if (w)
+      spmm_chunk_kernel<true><<<g2, threads, 0, ctx->stream>>>(ctx->d_adj, w, S, chunks, nchunks, part, k);
+    else
+      spmm_chunk_kernel<false><<<g2, threads, 0, ctx->stream>>>(ctx->d_adj, w, S, chunks, nchunks, part, k);
+    PHDE_LAUNCHED(ctx);
+    spmm_heavy_fix_kernel<<<grid_for(ctx, nheavy * 32, threads, 8), threads, 0, ctx->stream>>>(heavy, nheavy, deg, S,
+                                                                                              part, LS, k);
+    PHDE_LAUNCHED(ctx);
+  }
   return PHDE_OK;
 }
 
@@ -612,14 +777,32 @@ int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C)
   return PHDE_OK;
 }
 
-int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X) {
+int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X, int seq) {
   const int threads = 256;
+  if (seq) {
+    double *part = (double *)phde_buf(ctx, "coords.part", sizeof(double) * c);
+    if (!part) return PHDE_ERR_OOM;
+    coords_seq_kernel<<<grid_for(ctx, ctx->n * c, threads), threads, 0, ctx->stream>>>(M, Y, ctx->n, k, c, X);
+    PHDE_LAUNCHED(ctx);
+    colnorm_seq_kernel<<<c, 32, 0, ctx->stream>>>(X, ctx->n, part);
+    PHDE_LAUNCHED(ctx);
+    scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, 1);
+    PHDE_LAUNCHED(ctx);
+    return PHDE_OK;
+  }
   const int grid = grid_for(ctx, ctx->n * 32, threads, 4);
   double *part = (double *)phde_buf(ctx, "coords.part", sizeof(double) * grid * (size_t)c);
   if (!part) return PHDE_ERR_OOM;
   coords_kernel<<<grid, threads, sizeof(double) * (threads / 32) * c, ctx->stream>>>(M, Y, ctx->n, k, c, X, part);
   PHDE_LAUNCHED(ctx);
   scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// M = C^T C in the reference's summation order (one thread per entry).
+int phde_gram_seq(phde_ctx *ctx, const double *C, int k, double *M) {
+  gram_seq_kernel<<<(k * k + 127) / 128, 128, 0, ctx->stream>>>(C, ctx->n, k, M);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

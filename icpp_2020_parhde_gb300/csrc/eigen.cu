@@ -18,16 +18,27 @@ namespace {
 
 constexpr int EIG_THREADS = 1024;
 
-__device__ double warp_dot(const double *a, const double *b, int N, int lane) {
+// <a, b> for one warp.  SEQ: lane 0 sums in index order with separate roundings (the reference's
+// one-thread prodSeq / normL2, ParallelComponents.cpp:13-46) and broadcasts; otherwise a lane-strided
+// sum and a shuffle tree.
+template <bool SEQ>
+__device__ __forceinline__ double warp_dot(const double *a, const double *b, int N, int lane) {
+  if (SEQ) {
+    double s = 0;
+    if (lane == 0)
+      for (int r = 0; r < N; r++) s = __dadd_rn(s, __dmul_rn(a[r], b[r]));
+    return __shfl_sync(PHDE_FULL_MASK, s, 0);
+  }
   double s = 0;
-  for (int r = lane; r < N; r += 32) s += __dmul_rn(a[r], b[r]);
+  for (int r = lane; r < N; r += 32) s = fma(a[r], b[r], s);
   return warp_sum(s);
 }
 
-// Work arrays live in global memory (a few N*N doubles, L2/L1 resident).
+// Work arrays live in global memory (a few N*N doubles, L2/L1 resident); dd caches <E_j, E_j>.
+template <bool SEQ>
 __global__ void __launch_bounds__(EIG_THREADS) power_kernel(const double *Kin, int N, double *K, double *E,
                                                             double *T, double *evals, int *iters, int *status,
-                                                            int max_iter) {
+                                                            int max_iter, double *dd) {
   __shared__ double red[32];
   __shared__ double s_r;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -57,7 +68,7 @@ __global__ void __launch_bounds__(EIG_THREADS) power_kernel(const double *Kin, i
   }
   __syncthreads();
   for (int i = warp; i < N; i += nw) {
-    const double nv = sqrt(warp_dot(E + i * N, E + i * N, N, lane));
+    const double nv = sqrt(warp_dot<SEQ>(E + i * N, E + i * N, N, lane));
     for (int r = lane; r < N; r += 32) E[r + i * N] = E[r + i * N] / nv;
     if (lane == 0) evals[i] = nv;
   }
@@ -80,21 +91,32 @@ __global__ void __launch_bounds__(EIG_THREADS) power_kernel(const double *Kin, i
       E[idx] = s;
     }
     __syncthreads();
-    // Gram-Schmidt wavefront: at step t vector i projects out vector j = t - i (j < i)
-    for (int t = 1; t <= 2 * N - 3; t++) {
+    // Gram-Schmidt wavefront: at step t vector i projects out vector j = t - i (j < i).  Vector j is
+    // final once t > 2j - 1; its <E_j, E_j> is cached the step it becomes final (t == 2j, i.e. when
+    // vector i = j has no projection left to take).
+    if (warp == 0) {
+      const double d0 = warp_dot<SEQ>(E, E, N, lane);
+      if (lane == 0) dd[0] = d0;
+    }
+    __syncthreads();
+    for (int t = 1; t <= 2 * N - 2; t++) {
       for (int i = warp; i < N; i += nw) {
         const int j = t - i;
-        if (j < 0 || j >= i) continue;
-        const double num = warp_dot(E + j * N, E + i * N, N, lane);
-        const double den = warp_dot(E + j * N, E + j * N, N, lane);
-        const double fac = num / den;
+        if (j == i) {  // vector i just became final
+          const double d = warp_dot<SEQ>(E + i * N, E + i * N, N, lane);
+          if (lane == 0) dd[i] = d;
+          continue;
+        }
+        if (j < 0 || j > i) continue;
+        const double num = warp_dot<SEQ>(E + j * N, E + i * N, N, lane);
+        const double fac = num / dd[j];
         for (int q = lane; q < N; q += 32) E[q + i * N] = __dsub_rn(E[q + i * N], __dmul_rn(fac, E[q + j * N]));
         __syncwarp();
       }
       __syncthreads();
     }
     for (int i = warp; i < N; i += nw) {
-      const double nv = sqrt(warp_dot(E + i * N, E + i * N, N, lane));
+      const double nv = sqrt(warp_dot<SEQ>(E + i * N, E + i * N, N, lane));
       for (int q = lane; q < N; q += 32) E[q + i * N] = E[q + i * N] / nv;
       if (lane == 0) evals[i] = nv;
     }
@@ -102,7 +124,7 @@ __global__ void __launch_bounds__(EIG_THREADS) power_kernel(const double *Kin, i
     // r = min_i |<E_i, T_i>|
     double mn = 1.0;
     for (int i = warp; i < N; i += nw) {
-      double d = fabs(warp_dot(E + i * N, T + i * N, N, lane));
+      double d = fabs(warp_dot<SEQ>(E + i * N, T + i * N, N, lane));
       mn = d < mn ? d : mn;
     }
     if (lane == 0) red[warp] = mn;
@@ -287,16 +309,20 @@ __global__ void pick_kernel(const double *K, int N, int c, int largest, double *
 // Solve the k x k problem in d_M (column-major).  On success d_K holds the eigenvector matrix,
 // d_evals the eigenvalues (ascending), d_Y the c picked eigenvectors.  Synchronises to read the status.
 int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
-                    double *d_evals, double *d_Y, int *h_iters) {
+                    double *d_evals, double *d_Y, int *h_iters, int seq) {
   double *w1 = (double *)phde_buf(ctx, "eig.w1", sizeof(double) * N * N);
   double *w2 = (double *)phde_buf(ctx, "eig.w2", sizeof(double) * N * N);
+  double *dd = (double *)phde_buf(ctx, "eig.dd", sizeof(double) * N);
   int *st = (int *)phde_buf(ctx, "eig.st", sizeof(int) * 2);
-  if (!w1 || !w2 || !st) return PHDE_ERR_OOM;
+  if (!w1 || !w2 || !dd || !st) return PHDE_ERR_OOM;
   PHDE_CK(ctx, cudaMemsetAsync(st, 0, sizeof(int) * 2, ctx->stream));
   if (eig == PHDE_EIG_EXACT) {
     jacobi_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, w1, w2, d_K, d_evals, st, st + 1, 100);
   } else {
-    power_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000);
+    if (seq)
+      power_kernel<true><<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000, dd);
+    else
+      power_kernel<false><<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000, dd);
   }
   PHDE_LAUNCHED(ctx);
   pick_kernel<<<1, 256, 0, ctx->stream>>>(d_K, N, c, largest, d_Y);
