@@ -47,6 +47,14 @@ struct CgsArgs {
   uint64_t timeout_ns;
 };
 
+// Sum of one value per block (written before a grid barrier), in a fixed order for a given grid size;
+// the result is valid in every thread of the calling block.
+__device__ __forceinline__ double grid_partials_sum(const double *part, double *red) {
+  double s = 0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(part + b);
+  return block_sum(s, red);
+}
+
 __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
   extern __shared__ double sm[];  // [nwarps][k+2] reduction scratch, then coefficients
   __shared__ double red[32];
@@ -64,9 +72,7 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
   acc = block_sum(acc, red);
   if (threadIdx.x == 0) a.part2[blockIdx.x] = acc;
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-  double den0 = 0;
-  for (int b = 0; b < (int)gridDim.x; b++) den0 += __ldcg(a.part2 + b);
-  const double inv_den0 = 1.0 / den0;
+  const double inv_den0 = 1.0 / grid_partials_sum(a.part2, red);
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
 
   int j = 1, ndisc = 0, ncand = 0;
@@ -77,27 +83,35 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
     const int32_t *Dc = a.D + (int64_t)rc * n;
     const double inv_rc = 1.0 / sqrt((double)__ldcg(a.sumsq + rc));  // ParHDE.cpp:179-184
     const int jm1 = j - 1;
-    // ---- A: dots <x, D S_q> for the accepted columns q < j-1, and <x, D u0> in slot q == j-1 ----
+    // ---- A: dots <x, D S_q> for the accepted columns q < j-1 (lanes across q), and <x, D u0> ----
+    // A warp takes 32 rows at a time: lane r forms row r's x_i*d_i once and the warp broadcasts it, so
+    // the per-row FP64 work is one FMA per 32 columns.  The constant column's dot is inv0 * sum_i x_i d_i.
     double accq[MAXQ];
 #pragma unroll
     for (int t = 0; t < MAXQ; t++) accq[t] = 0;
-    for (int64_t i = gw; i < n; i += gws) {
-      const double xd = (double)Dc[i] * inv_rc * a.deg[i];
-      const double *Si = a.S + i * k;
+    double xsum = 0;
+    for (int64_t i0 = gw * 32; i0 < n; i0 += gws * 32) {
+      const int64_t il = i0 + lane;
+      const double xdl = il < n ? (double)Dc[il] * inv_rc * a.deg[il] : 0.0;
+      xsum += xdl;
+      const int rows = n - i0 < 32 ? (int)(n - i0) : 32;
+      for (int rr = 0; rr < rows; rr++) {
+        const double xd = __shfl_sync(PHDE_FULL_MASK, xdl, rr);
+        const double *Si = a.S + (i0 + rr) * k;
 #pragma unroll
-      for (int t = 0; t < MAXQ; t++) {
-        const int q = lane + 32 * t;
-        if (q < jm1)
-          accq[t] = fma(xd, __ldcg(Si + q), accq[t]);
-        else if (q == jm1)
-          accq[t] = fma(xd, inv0, accq[t]);
+        for (int t = 0; t < MAXQ; t++) {
+          const int q = lane + 32 * t;
+          if (q < jm1) accq[t] = fma(xd, Si[q], accq[t]);
+        }
       }
     }
+    xsum = warp_sum(xsum);
 #pragma unroll
     for (int t = 0; t < MAXQ; t++) {
       const int q = lane + 32 * t;
-      if (q <= jm1) sm[warp * ld + (q == jm1 ? k : q)] = accq[t];
+      if (q < jm1) sm[warp * ld + q] = accq[t];
     }
+    if (lane == 0) sm[warp * ld + k] = xsum * inv0;
     __syncthreads();
     for (int q = threadIdx.x; q < k + 1; q += blockDim.x) {
       if (q < jm1 || q == k) {
@@ -142,7 +156,7 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
     for (int64_t i = gt; i < n; i += gts) {
       const double *Si = a.S + i * k;
       double p = 0;
-      for (int q = 0; q < jm1; q++) p = fma(sm[q], __ldcg(Si + q), p);
+      for (int q = 0; q < jm1; q++) p = fma(sm[q], Si[q], p);
       const double xp = (double)Dc[i] * inv_rc - (p + c0u0);
       a.X[i] = xp;
       ssq = fma(xp, xp, ssq);
@@ -151,9 +165,7 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
     if (threadIdx.x == 0) a.part2[blockIdx.x] = ssq;
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
     // ---- G: norm test (ParHDE.cpp:267) and acceptance; the new column's D-norm partials ----
-    double nrm2 = 0;
-    for (int b = 0; b < (int)gridDim.x; b++) nrm2 += __ldcg(a.part2 + b);
-    const double nrm = sqrt(nrm2);
+    const double nrm = sqrt(grid_partials_sum(a.part2, red));
     if (nrm < 0.001) {
       ndisc++;
       if (blockIdx.x == 0 && threadIdx.x == 0) a.dlog[rc] = nrm;
