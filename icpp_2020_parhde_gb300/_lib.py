@@ -13,8 +13,9 @@ PHDE_OK = 0
 STATUS = {
     0: "PHDE_OK", -1: "PHDE_ERR_INVALID", -2: "PHDE_ERR_CSR", -3: "PHDE_ERR_DISCONNECTED", -4: "PHDE_ERR_K_RANGE",
     -5: "PHDE_ERR_TOO_FEW_PIVOTS", -6: "PHDE_ERR_OOM", -7: "PHDE_ERR_NOCONVERGE", -8: "PHDE_ERR_TIMEOUT",
-    -9: "PHDE_ERR_CUDA", -10: "PHDE_ERR_WEIGHTS", -11: "PHDE_ERR_NO_GRAPH",
+    -9: "PHDE_ERR_CUDA", -10: "PHDE_ERR_WEIGHTS", -11: "PHDE_ERR_NO_GRAPH", -12: "PHDE_ERR_TOO_LARGE",
 }
+NOALLOC_MAX_VERTICES = 1048576
 ALGOS = {"PivotMDS": 0, "PHDE": 1, "wParHDE": 2, "WParHDE": 2, "ParHDE": 3}
 STRATEGIES = {"RandCoarse": 0, "RandFine": 1, "Kcenters": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1}
@@ -24,7 +25,7 @@ EIGS = {"power": 0, "exact": 1}
 EXPORTS = [
     "phde_create", "phde_destroy", "phde_last_error", "phde_status_string", "phde_version", "phde_graph_upload",
     "phde_graph_n", "phde_graph_nnz", "phde_layout", "phde_distances", "phde_kcenters", "phde_DOBFS",
-    "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count",
+    "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
 ]
 
 
@@ -87,5 +88,6 @@ def load(path: str | None = None):
     L.phde_selftest_barrier_timeout.argtypes = [vp, C.c_int]
     L.phde_launch_count.argtypes = [vp]
     L.phde_launch_count.restype = i64
+    L.phde_bfs_noalloc.argtypes = [vp, vp, i64, i64, i64, vp, vp]
     _lib = L
     return L

@@ -37,6 +37,7 @@ extern "C" {
 #define PHDE_ERR_CUDA (-9)            /* CUDA runtime error                                           */
 #define PHDE_ERR_WEIGHTS (-10)        /* weighted algorithm without weights, or the reverse           */
 #define PHDE_ERR_NO_GRAPH (-11)       /* no graph uploaded to the context                             */
+#define PHDE_ERR_TOO_LARGE (-12)      /* input exceeds the fixed scratch capacity of phde_bfs_noalloc  */
 
 /* ---- algorithm / strategy / precision / eigensolver ids ------------------------------------- */
 /* algorithm numbering follows spectralDrawing.cpp:101-109 */
@@ -148,6 +149,22 @@ int phde_selftest_barrier_timeout(phde_ctx *ctx, int timeout_ms);
 
 /* Kernel launches issued through this context since it was created. */
 int64_t phde_launch_count(const phde_ctx *ctx);
+
+/* Hop distances from one source, for callers that must not allocate device memory.  This entry point
+ * has no counterpart in the reference.  It is meant for host code that cannot call cudaMalloc -- code
+ * whose device memory is owned by its own pool allocator, code on a latency-critical path where an
+ * allocation would synchronise the device, or a plugin that is only handed pre-allocated buffers.
+ * Inputs and output are DEVICE pointers: d_offsets (n+1 int64), d_adj (nnz uint32), d_dist (n int32,
+ * overwritten: hop count, -1 when unreachable); stream is a cudaStream_t (NULL = the legacy default
+ * stream).  The kernel's scratch is a fixed array inside the library (16 MiB, held by every GPU that
+ * loads the library until the process exits), so n is limited to PHDE_NOALLOC_MAX_VERTICES; larger
+ * inputs return PHDE_ERR_TOO_LARGE with a message on stderr.  The call allocates nothing, waits for
+ * its own kernel on `stream`, and returns PHDE_OK or PHDE_ERR_TIMEOUT.  All calls share the scratch:
+ * calls whose kernels overlap on the GPU race and must be serialised by the caller.  The first call on
+ * a device looks up the scratch address (one-time set-up); make it before any stream capture. */
+#define PHDE_NOALLOC_MAX_VERTICES 1048576
+int phde_bfs_noalloc(const int64_t *d_offsets, const uint32_t *d_adj, int64_t n, int64_t nnz, int64_t source,
+                     int32_t *d_dist, void *stream);
 
 #ifdef __cplusplus
 }
