@@ -87,3 +87,17 @@ def test_status_codes_agree_with_oracle():
     for name, val in re.findall(r"#define ORC_(ERR_\w+|OK)\s+\(?(-?\d+)\)?", src):
         key = {"ERR_K_RANGE": "ERR_K_RANGE"}.get(name, name)
         assert codes[key] == val, name
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "embed")), reason="reference build absent")
+def test_nxyz_writer_matches_reference_embed(tmp_path):
+    """The reference's own embed binary writes the .nxyz; our formatter reproduces it byte for byte."""
+    from oracle import oracle as orc
+    g, rec = load_golden("mesh125")
+    p = str(tmp_path / "mesh.csr")
+    csr_io.write_csr(p, g)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.run([orc.REF_EMBED_PATH, p, "-a", "PivotMDS", "-r", "10", "-c", "2"], check=True, env=env,
+                   stdout=subprocess.DEVNULL)
+    ref_text = open(p + "_hde.nxyz").read()
+    assert csr_io.format_nxyz(rec["PivotMDS_k10_c2_coords"]) == ref_text
