@@ -27,6 +27,11 @@ int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M)
 int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C);
 int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X, int seq);
 int phde_gram_seq(phde_ctx *ctx, const double *C, int k, double *M);
+int phde_cgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, float *S, int k,
+                    int *h_state, double *h_dlog);
+int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float *LS, int k);
+int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double *M);
+int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X);
 int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
                     double *d_evals, double *d_Y, int *h_iters, int seq);
 
@@ -298,6 +303,12 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   double *ev = (double *)phde_buf(ctx, "layout.ev", sizeof(double) * k);
   double *Y = (double *)phde_buf(ctx, "layout.Y", sizeof(double) * k * c);
   if (!d_src || !sumsq || !Sbuf || !M || !K || !ev || !Y) return PHDE_ERR_OOM;
+  const bool mixed = o->precision == PHDE_PREC_MIXED;
+  float *S32 = nullptr;
+  if (mixed) {
+    S32 = (float *)phde_buf(ctx, "layout.S32", sizeof(float) * n * k);
+    if (!S32) return PHDE_ERR_OOM;
+  }
   int npasses = 0, naccepted = 0, ndiscarded = 0;
   double ms_dist = 0, ms_orth = 0;
   const bool random = algo != PHDE_ALGO_WPARHDE && o->strategy != PHDE_STRAT_KCENTERS;
@@ -370,7 +381,11 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     if (hde) {
       int state[4] = {0, 0, 0, 0};
       std::vector<double> dlog(P);
-      if ((rc = phde_cgs(ctx, D, P, sumsq, deg, Sbuf, k, state, dlog.data()))) return rc;
+      if (mixed)
+        rc = phde_cgs2_mixed(ctx, D, P, sumsq, deg, S32, k, state, dlog.data());
+      else
+        rc = phde_cgs(ctx, D, P, sumsq, deg, Sbuf, k, state, dlog.data());
+      if (rc) return rc;
       if ((rc = phde_check_device_err(ctx, "D-orthogonalisation"))) return rc;
       naccepted = state[0];
       ndiscarded = state[1];
@@ -398,7 +413,12 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   }
 
   // ---- Laplacian SpMM + Gram (HDE) or C^T C (MDS) ----
-  if (hde) {
+  if (hde && mixed) {
+    float *LS32 = (float *)phde_buf(ctx, "layout.LS32", sizeof(float) * n * k);
+    if (!LS32) return PHDE_ERR_OOM;
+    if ((rc = phde_lap_spmm_mixed(ctx, deg, S32, LS32, k))) return rc;
+    if ((rc = phde_gram_mixed(ctx, S32, LS32, k, M))) return rc;
+  } else if (hde) {
     double *LS = (double *)phde_buf(ctx, "layout.LS", sizeof(double) * n * k);
     if (!LS) return PHDE_ERR_OOM;
     if ((rc = phde_lap_spmm(ctx, deg, Sbuf, LS, k))) return rc;
@@ -414,7 +434,11 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   tm.mark(4);
   double *X = (double *)phde_buf(ctx, "layout.X", sizeof(double) * n * c);
   if (!X) return PHDE_ERR_OOM;
-  if ((rc = phde_coords(ctx, Sbuf, Y, k, c, X, !hde))) return rc;
+  if (mixed)
+    rc = phde_coords_mixed(ctx, S32, Y, k, c, X);
+  else
+    rc = phde_coords(ctx, Sbuf, Y, k, c, X, !hde);
+  if (rc) return rc;
   PHDE_CK(ctx, cudaMemcpyAsync(coords_out, X, sizeof(double) * n * c, cudaMemcpyDeviceToHost, ctx->stream));
   tm.mark(5);
   if (sources_out && npasses > 0)
@@ -426,14 +450,21 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   if (extra && extra->evals)
     PHDE_CK(ctx, cudaMemcpyAsync(extra->evals, ev, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
   std::vector<double> Srow;
+  std::vector<float> Srow32;
   if (extra && extra->basis) {
-    Srow.resize((size_t)n * k);
-    PHDE_CK(ctx, cudaMemcpyAsync(Srow.data(), Sbuf, sizeof(double) * n * k, cudaMemcpyDeviceToHost, ctx->stream));
+    if (mixed) {
+      Srow32.resize((size_t)n * k);
+      PHDE_CK(ctx, cudaMemcpyAsync(Srow32.data(), S32, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->stream));
+    } else {
+      Srow.resize((size_t)n * k);
+      PHDE_CK(ctx, cudaMemcpyAsync(Srow.data(), Sbuf, sizeof(double) * n * k, cudaMemcpyDeviceToHost, ctx->stream));
+    }
   }
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
   if (extra && extra->basis)
     for (int64_t i = 0; i < n; i++)
-      for (int q = 0; q < k; q++) extra->basis[i + (int64_t)q * n] = Srow[(size_t)i * k + q];
+      for (int q = 0; q < k; q++)
+        extra->basis[i + (int64_t)q * n] = mixed ? (double)Srow32[(size_t)i * k + q] : Srow[(size_t)i * k + q];
   if (st) {
     st->npasses = npasses;
     st->naccepted = naccepted;
@@ -469,6 +500,8 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, in
     return phde_fail(ctx, PHDE_ERR_WEIGHTS, "Weighted ParHDE code requires the weighted edges");
   if (o->algo != PHDE_ALGO_WPARHDE && ctx->weighted)
     return phde_fail(ctx, PHDE_ERR_WEIGHTS, "ParHDE code doesn't requires the weighted edges");
+  if (o->precision == PHDE_PREC_MIXED && o->algo != PHDE_ALGO_PARHDE)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "mixed precision is implemented for ParHDE; use PHDE_PREC_FP64");
   cudaSetDevice(ctx->device);
   int rc = layout_impl(ctx, o, coords_out, sources_out, extra, st);
   if (st) st->status = rc;

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "ctx.h"
+#include "spmm_plan.cuh"
 
 namespace {
 
@@ -282,17 +283,6 @@ __global__ void degrees_kernel(const int64_t *off, const int32_t *w, int64_t n, 
 // exact subtraction sequence, ParHDE.cpp:293-298), four neighbour rows in flight.  Heavier rows (R-MAT
 // hubs) are cut into chunks of SPMM_CHUNK neighbours; one warp sums each chunk, and a fix-up pass forms
 // LS = d*S - (sum of the chunk partials in chunk order), so the result is deterministic.
-constexpr int SPMM_HEAVY = 512, SPMM_CHUNK = 512;
-
-struct HeavyRow {
-  int64_t row;
-  int64_t first_chunk;
-  int64_t nchunks;
-};
-struct Chunk {
-  int64_t e0, e1;
-};
-
 __global__ void spmm_plan_kernel(const int64_t *off, int64_t n, HeavyRow *heavy, Chunk *chunks, ull *counts) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e0 = off[i], e1 = off[i + 1], deg = e1 - e0;
@@ -708,8 +698,8 @@ int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale, double *S,
   return PHDE_OK;
 }
 
-// Heavy-row chunk plan, built once per uploaded graph (ctx->spmm_plan_n tracks which graph).
-static int spmm_plan(phde_ctx *ctx, HeavyRow **heavy, Chunk **chunks, int64_t *nheavy, int64_t *nchunks) {
+// Heavy-row chunk plan, built once per uploaded graph (ctx->spmm_plan_epoch tracks which graph).
+int phde_spmm_plan(phde_ctx *ctx, HeavyRow **heavy, Chunk **chunks, int64_t *nheavy, int64_t *nchunks) {
   const int64_t cap_h = ctx->nnz / SPMM_HEAVY + 1, cap_c = ctx->nnz / SPMM_CHUNK + cap_h + 1;
   *heavy = (HeavyRow *)phde_buf(ctx, "spmm.heavy", sizeof(HeavyRow) * cap_h);
   *chunks = (Chunk *)phde_buf(ctx, "spmm.chunks", sizeof(Chunk) * cap_c);
@@ -735,7 +725,7 @@ int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS,
   HeavyRow *heavy;
   Chunk *chunks;
   int64_t nheavy, nchunks;
-  int rc = spmm_plan(ctx, &heavy, &chunks, &nheavy, &nchunks);
+  int rc = phde_spmm_plan(ctx, &heavy, &chunks, &nheavy, &nchunks);
   if (rc) return rc;
   const int threads = 256;
   const int32_t *w = ctx->weighted ? ctx->d_w : nullptr;

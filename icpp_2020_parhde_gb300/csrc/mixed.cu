@@ -1,0 +1,481 @@
+// mixed.cu -- the mixed-precision dense stages of ParHDE (PHDE_PREC_MIXED).
+//
+// GB300 runs FP64 at 1/64 of its FP32 rate, so the FP64 path is bound by the FP64 pipe.  Here the
+// n-sized work is FP32 and only what is k-sized or a cross-block sum is FP64:
+//   cgs2_kernel      D-orthogonalisation of ParHDE.cpp:190-285 as CGS2: every candidate is projected
+//                    twice against the accepted columns and the constant column (single-pass classical
+//                    Gram-Schmidt in FP32 would lose orthogonality on these nearly collinear distance
+//                    columns); FP32 products, FP64 sums across warps and blocks; same norm test
+//                    (||x|| < 1e-3 discards, ParHDE.cpp:267) and the same acceptance order.
+//   spmm32 kernels   LS = D*S - A*S with an FP32 basis (half the bytes of every neighbour gather; the
+//                    R-MAT-20 basis is 129 MB and stays largely in the 129 MB L2), same heavy-row plan.
+//   gram32_kernel    S^T LS with FP32 products accumulated in FP32 over 16-row slabs and in FP64 across
+//                    slabs and blocks.
+//   coords32_kernel  X = S*Y with the FP64 eigenvectors, FP64 accumulation.
+// The k x k eigensolve stays FP64 (eigen.cu).
+#include "ctx.h"
+#include "spmm_plan.cuh"
+
+namespace {
+
+constexpr int C2_THREADS = 256;
+constexpr int MAXQ = 8;  // columns per lane: k <= 256
+
+__device__ __forceinline__ double partials_sum(const double *part, double *red) {
+  double s = 0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(part + b);
+  return block_sum(s, red);
+}
+
+struct Cgs2Args {
+  const int32_t *D;
+  int64_t n;
+  int P;
+  const ull *sumsq;
+  const double *deg;
+  float *S;  // row-major n x k
+  int k;
+  float *X;        // [n] candidate after the current pass
+  double *part;    // [gridDim][k+2]
+  double *part2;   // [gridDim]
+  double *coef;    // [k+1]
+  double *inv_den; // [k+1]
+  int *state;
+  double *dlog;
+  GridSync *gs;
+  int *err;
+  uint64_t timeout_ns;
+};
+
+__global__ void __launch_bounds__(C2_THREADS) cgs2_kernel(Cgs2Args a) {
+  extern __shared__ double sm[];  // [nwarps][k+2], then the coefficients as float
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t n = a.n;
+  const int k = a.k, ld = k + 2;
+  const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
+  const double inv0 = 1.0 / sqrt((double)n);
+
+  double acc0 = 0;
+  for (int64_t i = gt; i < n; i += gts) acc0 += a.deg[i];
+  acc0 = block_sum(acc0, red);
+  if (threadIdx.x == 0) a.part2[blockIdx.x] = acc0 * inv0 * inv0;
+  if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+  const double inv_den0 = 1.0 / partials_sum(a.part2, red);
+  if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+
+  int j = 1, ndisc = 0, ncand = 0;
+  bool newcol = false;
+  for (int rc = 0; rc < a.P; rc++) {
+    if (j > k) break;
+    ncand++;
+    const int32_t *Dc = a.D + (int64_t)rc * n;
+    const float inv_rc = (float)(1.0 / sqrt((double)__ldcg(a.sumsq + rc)));
+    const int jm1 = j - 1;
+    double ssq = 0;
+    for (int pass = 0; pass < 2; pass++) {
+      // ---- A: dots <v, D S_q> (q < j-1) and <v, D u0>; v = the candidate (pass 0) or X (pass 1) ----
+      float accq[MAXQ];
+#pragma unroll
+      for (int t = 0; t < MAXQ; t++) accq[t] = 0.f;
+      double vsum = 0;
+      for (int64_t i0 = gw * 32; i0 < n; i0 += gws * 32) {
+        const int64_t il = i0 + lane;
+        float vdl = 0.f;
+        if (il < n) {
+          const float v = pass == 0 ? (float)Dc[il] * inv_rc : __ldcg(a.X + il);
+          vdl = v * (float)a.deg[il];
+        }
+        vsum += (double)vdl;
+        const int rows = n - i0 < 32 ? (int)(n - i0) : 32;
+        for (int rr = 0; rr < rows; rr++) {
+          const float vd = __shfl_sync(PHDE_FULL_MASK, vdl, rr);
+          const float *Si = a.S + (i0 + rr) * k;
+#pragma unroll
+          for (int t = 0; t < MAXQ; t++) {
+            const int q = lane + 32 * t;
+            if (q < jm1) accq[t] = fmaf(vd, Si[q], accq[t]);
+          }
+        }
+      }
+      vsum = warp_sum(vsum);
+#pragma unroll
+      for (int t = 0; t < MAXQ; t++) {
+        const int q = lane + 32 * t;
+        if (q < jm1) sm[warp * ld + q] = (double)accq[t];
+      }
+      if (lane == 0) sm[warp * ld + k] = vsum * inv0;
+      __syncthreads();
+      for (int q = threadIdx.x; q < k + 1; q += blockDim.x) {
+        if (q < jm1 || q == k) {
+          double s = 0;
+          for (int w = 0; w < nw; w++) s += sm[w * ld + q];
+          a.part[(int64_t)blockIdx.x * ld + q] = s;
+        }
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      // ---- C: coefficients ----
+      for (int q = blockIdx.x; q < j; q += gridDim.x) {
+        const int slot = q == jm1 ? k : q;
+        const bool fresh = pass == 0 && newcol && q == j - 2;
+        double s = 0, sd = 0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+          s += __ldcg(a.part + (int64_t)b * ld + slot);
+          if (fresh) sd += __ldcg(a.part + (int64_t)b * ld + k + 1);
+        }
+        s = block_sum(s, red);
+        if (fresh) sd = block_sum(sd, red);
+        if (threadIdx.x == 0) {
+          double id;
+          if (slot == k) {
+            id = inv_den0;
+          } else if (fresh) {
+            id = 1.0 / sd;
+            a.inv_den[q] = id;
+          } else {
+            id = __ldcg(a.inv_den + q);
+          }
+          a.coef[slot] = s * id;
+        }
+        __syncthreads();
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      // ---- E: v' = v - (sum_q coef_q S_q + coef_0 u0), thread per row ----
+      float *cf = (float *)sm;
+      __syncthreads();
+      for (int q = threadIdx.x; q < jm1; q += blockDim.x) cf[q] = (float)__ldcg(a.coef + q);
+      __syncthreads();
+      const float c0u0 = (float)(__ldcg(a.coef + k) * inv0);
+      ssq = 0;
+      for (int64_t i = gt; i < n; i += gts) {
+        const float *Si = a.S + i * k;
+        float p = 0.f;
+        for (int q = 0; q < jm1; q++) p = fmaf(cf[q], Si[q], p);
+        const float v = pass == 0 ? (float)Dc[i] * inv_rc : __ldcg(a.X + i);
+        const float vp = v - (p + c0u0);
+        a.X[i] = vp;
+        ssq += (double)vp * (double)vp;
+      }
+      if (pass == 1) {
+        ssq = block_sum(ssq, red);
+        if (threadIdx.x == 0) a.part2[blockIdx.x] = ssq;
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    }
+    // ---- G: norm test and acceptance ----
+    const double nrm = sqrt(partials_sum(a.part2, red));
+    if (nrm < 0.001) {
+      ndisc++;
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.dlog[rc] = nrm;
+      newcol = false;
+    } else {
+      const float scale = (float)(1.0 / nrm);
+      double dd = 0;
+      for (int64_t i = gt; i < n; i += gts) {
+        const float v = __ldcg(a.X + i) * scale;
+        a.S[i * k + (j - 1)] = v;
+        dd += (double)v * (double)v * a.deg[i];
+      }
+      dd = block_sum(dd, red);
+      if (threadIdx.x == 0) a.part[(int64_t)blockIdx.x * ld + k + 1] = dd;
+      j++;
+      newcol = true;
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.state[0] = j - 1;
+    a.state[1] = ndisc;
+    a.state[2] = ncand;
+  }
+}
+
+// ---- FP32 Laplacian SpMM ----
+__device__ __forceinline__ void spmm32_acc(const uint32_t *adj, const float *S, int k, int lane, int64_t e0,
+                                           int64_t e1, float (&acc)[MAXQ]) {
+  int64_t e = e0;
+  for (; e + 4 <= e1; e += 4) {
+    const int64_t v0 = __ldg(adj + e), v1 = __ldg(adj + e + 1), v2 = __ldg(adj + e + 2), v3 = __ldg(adj + e + 3);
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) acc[t] -= (S[v0 * k + q] + S[v1 * k + q]) + (S[v2 * k + q] + S[v3 * k + q]);
+    }
+  }
+  for (; e < e1; e++) {
+    const int64_t v = __ldg(adj + e);
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) acc[t] -= S[v * k + q];
+    }
+  }
+}
+
+__global__ void spmm32_light_kernel(const int64_t *off, const uint32_t *adj, const double *deg, const float *S,
+                                    float *LS, int64_t n, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < n; i += gws) {
+    const int64_t e0 = off[i], e1 = off[i + 1];
+    if (e1 - e0 > SPMM_HEAVY) continue;
+    const float di = (float)deg[i];
+    float acc[MAXQ];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      acc[t] = q < k ? di * S[i * k + q] : 0.f;
+    }
+    spmm32_acc(adj, S, k, lane, e0, e1, acc);
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) LS[i * k + q] = acc[t];
+    }
+  }
+}
+
+__global__ void spmm32_chunk_kernel(const uint32_t *adj, const float *S, const Chunk *chunks, int64_t nchunks,
+                                    float *part, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = gw; c < nchunks; c += gws) {
+    float acc[MAXQ];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) acc[t] = 0.f;
+    const Chunk ch = chunks[c];
+    spmm32_acc(adj, S, k, lane, ch.e0, ch.e1, acc);
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) part[c * k + q] = acc[t];
+    }
+  }
+}
+
+__global__ void spmm32_fix_kernel(const HeavyRow *heavy, int64_t nheavy, const double *deg, const float *S,
+                                  const float *part, float *LS, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t h = gw; h < nheavy; h += gws) {
+    const HeavyRow hr = heavy[h];
+    const int64_t i = hr.row;
+    const float di = (float)deg[i];
+#pragma unroll
+    for (int t = 0; t < MAXQ; t++) {
+      const int q = lane + 32 * t;
+      if (q < k) {
+        float s = di * S[i * k + q];
+        for (int64_t c = 0; c < hr.nchunks; c++) s += part[(hr.first_chunk + c) * k + q];
+        LS[i * k + q] = s;
+      }
+    }
+  }
+}
+
+// ---- Gram A^T B with FP32 inputs: 64x64 tile per block, FP32 over 16-row slabs, FP64 across slabs ----
+constexpr int GT = 64, GR = 16;
+__global__ void __launch_bounds__(256) gram32_kernel(const float *A, const float *B, int64_t n, int k, double *part) {
+  __shared__ float sA[GR][GT + 1];
+  __shared__ float sB[GR][GT + 1];
+  const int tiles = (k + GT - 1) / GT;
+  const int tp = blockIdx.x / tiles, tq = blockIdx.x % tiles;
+  const int p0 = tp * GT, q0 = tq * GT;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t rows_per = (n + gridDim.y - 1) / gridDim.y;
+  const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+  const int64_t r1 = min(n, r0 + rows_per);
+  double accd[4][4] = {};
+  for (int64_t rb = r0; rb < r1; rb += GR) {
+    for (int idx = threadIdx.x; idx < GR * GT; idx += 256) {
+      const int rr = idx / GT, cc = idx % GT;
+      const int64_t r = rb + rr;
+      sA[rr][cc] = (r < r1 && p0 + cc < k) ? A[r * k + p0 + cc] : 0.f;
+      sB[rr][cc] = (r < r1 && q0 + cc < k) ? B[r * k + q0 + cc] : 0.f;
+    }
+    __syncthreads();
+    float acc[4][4] = {};
+#pragma unroll 4
+    for (int rr = 0; rr < GR; rr++) {
+      float av[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        av[u] = sA[rr][ty + 16 * u];
+        bv[u] = sB[rr][tx + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int v = 0; v < 4; v++) accd[u][v] += (double)acc[u][v];
+    __syncthreads();
+  }
+  double *out = part + (int64_t)blockIdx.y * k * k;
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const int p = p0 + ty + 16 * u, q = q0 + tx + 16 * v;
+      if (p < k && q < k) out[q + (int64_t)p * k] = accd[u][v];
+    }
+}
+
+__global__ void sum_parts32_kernel(const double *part, int splits, int64_t len, double *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int b = 0; b < splits; b++) s += part[(int64_t)b * len + i];
+    out[i] = s;
+  }
+}
+
+// X[i + t*n] = sum_q S[i,q] * Y[q + t*k] (FP32 basis, FP64 eigenvectors and accumulation)
+__global__ void coords32_kernel(const float *S, const double *Y, int64_t n, int k, int c, double *X, double *part) {
+  extern __shared__ double smc[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
+  for (int t = 0; t < c; t++) {
+    double ss = 0;
+    for (int64_t i = gw; i < n; i += gws) {
+      double s = 0;
+      for (int q = lane; q < k; q += 32) s = fma((double)S[i * k + q], Y[q + (int64_t)t * k], s);
+      s = warp_sum(s);
+      if (lane == 0) {
+        X[i + (int64_t)t * n] = s;
+        ss = fma(s, s, ss);
+      }
+    }
+    if (lane == 0) smc[warp * c + t] = ss;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < c; t += blockDim.x) {
+    double s = 0;
+    for (int w = 0; w < nw; w++) s += smc[w * c + t];
+    part[(int64_t)blockIdx.x * c + t] = s;
+  }
+}
+
+__global__ void scale32_kernel(double *X, int64_t n, int c, const double *part, int nparts) {
+  __shared__ double inv[PHDE_MAX_K];
+  for (int t = threadIdx.x; t < c; t += blockDim.x) {
+    double s = 0;
+    for (int b = 0; b < nparts; b++) s += part[(int64_t)b * c + t];
+    inv[t] = 1.0 / sqrt(s);
+  }
+  __syncthreads();
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * c;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    X[idx] *= inv[idx / n];
+}
+
+int grid_of(phde_ctx *ctx, int64_t work, int threads, int per_sm) {
+  int64_t b = (work + threads - 1) / threads;
+  b = std::min<int64_t>(b, (int64_t)ctx->nsm * per_sm);
+  return (int)std::max<int64_t>(b, 1);
+}
+
+}  // namespace
+
+int phde_cgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, float *S, int k,
+                    int *h_state, double *h_dlog) {
+  const int64_t n = ctx->n;
+  const size_t smem = sizeof(double) * (C2_THREADS / 32) * (size_t)(k + 2);
+  int per_sm = 0;
+  PHDE_CK(ctx, cudaFuncSetAttribute(cgs2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cgs2_kernel, C2_THREADS, smem));
+  if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "cgs2 kernel cannot be resident");
+  per_sm = std::min(per_sm, 4);
+  const int grid = ctx->nsm * per_sm;
+  float *X = (float *)phde_buf(ctx, "cgs2.X", sizeof(float) * n);
+  double *part = (double *)phde_buf(ctx, "cgs2.part", sizeof(double) * grid * (size_t)(k + 2));
+  double *part2 = (double *)phde_buf(ctx, "cgs2.part2", sizeof(double) * grid);
+  double *coef = (double *)phde_buf(ctx, "cgs2.coef", sizeof(double) * (k + 1));
+  double *inv_den = (double *)phde_buf(ctx, "cgs2.inv_den", sizeof(double) * (k + 1));
+  int *state = (int *)phde_buf(ctx, "cgs2.state", sizeof(int) * 4);
+  double *dlog = (double *)phde_buf(ctx, "cgs2.dlog", sizeof(double) * P);
+  if (!X || !part || !part2 || !coef || !inv_den || !state || !dlog) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(dlog, 0xff, sizeof(double) * P, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(state, 0, sizeof(int) * 4, ctx->stream));
+  int rc = phde_reset_sync(ctx);
+  if (rc) return rc;
+  Cgs2Args a;
+  a.D = D;
+  a.n = n;
+  a.P = P;
+  a.sumsq = sumsq;
+  a.deg = deg;
+  a.S = S;
+  a.k = k;
+  a.X = X;
+  a.part = part;
+  a.part2 = part2;
+  a.coef = coef;
+  a.inv_den = inv_den;
+  a.state = state;
+  a.dlog = dlog;
+  a.gs = ctx->d_sync;
+  a.err = ctx->d_err;
+  a.timeout_ns = ctx->timeout_ns;
+  void *args[] = {&a};
+  PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)cgs2_kernel, dim3(grid), dim3(C2_THREADS), args, smem,
+                                           ctx->stream));
+  PHDE_LAUNCHED(ctx);
+  PHDE_CK(ctx, cudaMemcpyAsync(h_state, state, sizeof(int) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaMemcpyAsync(h_dlog, dlog, sizeof(double) * P, cudaMemcpyDeviceToHost, ctx->stream));
+  return PHDE_OK;
+}
+
+int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float *LS, int k) {
+  HeavyRow *heavy;
+  Chunk *chunks;
+  int64_t nheavy, nchunks;
+  int rc = phde_spmm_plan(ctx, &heavy, &chunks, &nheavy, &nchunks);
+  if (rc) return rc;
+  const int threads = 256;
+  spmm32_light_kernel<<<grid_of(ctx, ctx->n * 32, threads, 8), threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, deg,
+                                                                                          S, LS, ctx->n, k);
+  PHDE_LAUNCHED(ctx);
+  if (nheavy > 0) {
+    float *part = (float *)phde_buf(ctx, "spmm32.part", sizeof(float) * nchunks * k);
+    if (!part) return PHDE_ERR_OOM;
+    spmm32_chunk_kernel<<<grid_of(ctx, nchunks * 32, threads, 8), threads, 0, ctx->stream>>>(ctx->d_adj, S, chunks,
+                                                                                             nchunks, part, k);
+    PHDE_LAUNCHED(ctx);
+    spmm32_fix_kernel<<<grid_of(ctx, nheavy * 32, threads, 8), threads, 0, ctx->stream>>>(heavy, nheavy, deg, S, part,
+                                                                                          LS, k);
+    PHDE_LAUNCHED(ctx);
+  }
+  return PHDE_OK;
+}
+
+int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double *M) {
+  const int tiles = (k + GT - 1) / GT;
+  const int splits =
+      (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * 8 / (tiles * tiles), (ctx->n + 255) / 256));
+  double *part = (double *)phde_buf(ctx, "gram32.part", sizeof(double) * (size_t)splits * k * k);
+  if (!part) return PHDE_ERR_OOM;
+  gram32_kernel<<<dim3(tiles * tiles, splits), 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+  PHDE_LAUNCHED(ctx);
+  sum_parts32_kernel<<<grid_of(ctx, (int64_t)k * k, 256, 8), 256, 0, ctx->stream>>>(part, splits, (int64_t)k * k, M);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X) {
+  const int threads = 256;
+  const int grid = grid_of(ctx, ctx->n * 32, threads, 4);
+  double *part = (double *)phde_buf(ctx, "coords32.part", sizeof(double) * grid * (size_t)c);
+  if (!part) return PHDE_ERR_OOM;
+  coords32_kernel<<<grid, threads, sizeof(double) * (threads / 32) * c, ctx->stream>>>(S, Y, ctx->n, k, c, X, part);
+  PHDE_LAUNCHED(ctx);
+  scale32_kernel<<<grid_of(ctx, ctx->n * c, 256, 8), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
