@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=3)
+    ap.add_argument("--no-mixed", action="store_true")
     return ap.parse_args()
 
 
@@ -149,6 +150,17 @@ def allmax(ws, x: float) -> float:
     t = torch.tensor([x], dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rayleigh_quotients(g, X):
+    """x^T L x / x^T x per coordinate column (L = D - A)."""
+    import scipy.sparse as sp
+    n = g.n
+    A = sp.csr_matrix((np.ones(g.nnz, dtype=np.float64), g.adj.astype(np.int64), g.offsets.astype(np.int64)),
+                      shape=(n, n))
+    d = np.asarray(A.sum(axis=1)).ravel()
+    LX = d[:, None] * X - A @ X
+    return np.einsum("ij,ij->j", X, LX) / np.einsum("ij,ij->j", X, X)
 
 
 def cpu_baseline(g, args, reps):
@@ -266,6 +278,25 @@ def run_gb300(args):
             traffic = json.load(open(tp)).get("bytes_per_launch")
         except Exception:
             traffic = None
+    mixed = None
+    if not args.no_mixed:
+        # mixed precision (FP32 basis / CGS2 / SpMM, FP64 k x k solve): same workload, stated error vs FP64
+        xy64 = xy_h.numpy().reshape(c, n).T.copy()
+        ms_mixed = []
+        for _ in range(args.warmup):
+            ctx.layout("ParHDE", "Kcenters", k, c, precision="mixed", coords_out=xy_h.numpy())
+        for _ in range(args.steps):
+            flush_l2()
+            rm = ctx.layout("ParHDE", "Kcenters", k, c, precision="mixed", coords_out=xy_h.numpy())
+            ms_mixed.append(rm.stats["ms_total"])
+        xym = xy_h.numpy().reshape(c, n).T.copy()
+        rq64, rqm = rayleigh_quotients(g, xy64), rayleigh_quotients(g, xym)
+        msm = allmax(ws, float(np.mean(ms_mixed)))
+        mixed = {"value": ws * k * nnz / (msm * 1e-3), "unit": UNIT, "ms_per_graph": msm, "dtype": "f32+f64",
+                 "phases_ms": {kk: rm.stats[kk] for kk in ("ms_dist", "ms_orth", "ms_mmult", "ms_eig", "ms_coords")},
+                 "rayleigh_fp64": rq64.tolist(), "rayleigh_mixed": rqm.tolist(),
+                 "rayleigh_rel_err_max": float(np.max(np.abs(rqm - rq64) / np.abs(rq64))),
+                 "eig_iters": rm.stats["eig_iters"], "naccepted": rm.stats["naccepted"]}
     if rank != 0:
         return
     line = {
@@ -289,6 +320,7 @@ def run_gb300(args):
                      "algorithmic_bytes_per_launch": P * bytes_per_pass, "kernel_ms": kern_ms},
         "clocks": clk.summary(),
         "stats_last": stats[-1],
+        "mixed_precision": mixed,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g, args, args.cpu_reps)
