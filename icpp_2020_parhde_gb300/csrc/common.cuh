@@ -12,15 +12,18 @@ typedef unsigned long long ull;
 // ---------------------------------------------------------------------------------------------
 // Grid-wide barrier for cooperative launches.
 //
-// Every wait is bounded: the waiting thread gives up after `timeout_ns` of %globaltimer, records
-// PHDE_ERR_TIMEOUT in the kernel's error word and returns false; a block that sees any error word
-// also returns false.  Callers leave the kernel on false, so a kernel can never spin forever.
-// Memory ordering: all threads' writes are ordered before thread 0's release (bar.sync, then a
-// gpu-scope fence and an acq_rel arrival); after the generation flips, thread 0 acquires and the
-// block's threads are ordered after it by the closing bar.sync.
+// Monotonic arrival counter: thread 0 of every block adds 1 with release semantics (after bar.sync, so
+// the whole block's writes are ordered before it), then polls the counter with acquire loads until it
+// reaches the next multiple of the number of blocks; the closing bar.sync orders the block's threads
+// after that acquire.  One round trip to arrive, one to observe -- no reset, no generation word.  The
+// counter is zeroed before each launch (phde_reset_sync); 2^32 arrivals bound the barriers per launch.
+//
+// Every wait is bounded: after `timeout_ns` of %globaltimer the waiting thread records
+// PHDE_ERR_TIMEOUT in the kernel's error word and the block returns false; a block that sees any error
+// word also returns false.  Callers leave the kernel on false, so a kernel never spins forever.
 struct GridSync {
   unsigned int count;
-  unsigned int gen;
+  unsigned int spare;
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
@@ -28,12 +31,9 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned *p, unsigned v) {
+__device__ __forceinline__ unsigned atom_add_release_u32(unsigned *p, unsigned v) {
   unsigned old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  asm volatile("atom.release.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
   return old;
 }
 __device__ __forceinline__ int ld_volatile_i32(const int *p) { return *(const volatile int *)p; }
@@ -49,31 +49,25 @@ __device__ __forceinline__ bool grid_barrier(GridSync *gs, int *err, uint64_t ti
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    unsigned gen = ld_acquire_u32(&gs->gen);
-    __threadfence();
-    unsigned arrived = atom_add_acq_rel_u32(&gs->count, 1u);
-    if (arrived == expected - 1) {
-      gs->count = 0;
-      __threadfence();
-      st_release_u32(&gs->gen, gen + 1);
-    } else {
-      uint64_t t0 = global_timer_ns();
+    const unsigned arrived = atom_add_release_u32(&gs->count, 1u);
+    const unsigned target = (arrived / expected + 1u) * expected;
+    if (ld_acquire_u32(&gs->count) - target > 0x80000000u) {  // not yet reached (wrap-safe compare)
+      const uint64_t t0 = global_timer_ns();
       unsigned spins = 0;
-      while (ld_acquire_u32(&gs->gen) == gen) {
-        if (ld_volatile_i32(err) != 0) {
-          ok = 0;
-          break;
+      while (ld_acquire_u32(&gs->count) - target > 0x80000000u) {
+        if ((++spins & 7u) == 0) {
+          if (ld_volatile_i32(err) != 0) {
+            ok = 0;
+            break;
+          }
+          if (global_timer_ns() - t0 > timeout_ns) {
+            atomicCAS(err, 0, PHDE_ERR_TIMEOUT);
+            ok = 0;
+            break;
+          }
         }
-        if ((++spins & 15u) == 0 && global_timer_ns() - t0 > timeout_ns) {
-          atomicCAS(err, 0, PHDE_ERR_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
       }
     }
-    __threadfence();
-    if (ok && ld_volatile_i32(err) != 0) ok = 0;
     s_ok = ok;
   }
   __syncthreads();

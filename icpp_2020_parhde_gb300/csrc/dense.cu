@@ -56,12 +56,27 @@ __device__ __forceinline__ double grid_partials_sum(const double *part, double *
   return block_sum(s, red);
 }
 
+// Stage rows [i0, i0+rows) x columns [c0, c0+nc) of a row-major n x k matrix into a warp's tile
+// (row r at tile[r*TILE_LD]); every load is independent and coalesced along the row.
+constexpr int TILE_LD = 33;
+template <typename T>
+__device__ __forceinline__ void stage_tile(const T *S, int64_t i0, int rows, int k, int c0, int nc, T *tile, int lane) {
+  __syncwarp();
+  if (lane < nc) {
+    const T *src = S + i0 * k + c0 + lane;
+#pragma unroll 8
+    for (int r = 0; r < rows; r++) tile[r * TILE_LD + lane] = src[(int64_t)r * k];
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
-  extern __shared__ double sm[];  // [nwarps][k+2] reduction scratch, then coefficients
+  extern __shared__ double sm[];  // [nwarps][k+2] reduction scratch (coefficients in phase E), then tiles
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int64_t n = a.n;
   const int k = a.k, ld = k + 2;
+  double *tile = sm + nw * ld + warp * 32 * TILE_LD;
   const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
   const double inv0 = 1.0 / sqrt((double)n);  // the constant column: 1 * (1/||1||), ParHDE.cpp:96-108
@@ -85,8 +100,9 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
     const double inv_rc = 1.0 / sqrt((double)__ldcg(a.sumsq + rc));  // ParHDE.cpp:179-184
     const int jm1 = j - 1;
     // ---- A: dots <x, D S_q> for the accepted columns q < j-1 (lanes across q), and <x, D u0> ----
-    // A warp takes 32 rows at a time: lane r forms row r's x_i*d_i once and the warp broadcasts it, so
-    // the per-row FP64 work is one FMA per 32 columns.  The constant column's dot is inv0 * sum_i x_i d_i.
+    // A warp takes 32 rows at a time and stages them 32 columns at a time in shared memory (coalesced,
+    // independent loads); lane r forms row r's x_i*d_i once and the warp broadcasts it.  The constant
+    // column's dot is inv0 * sum_i x_i d_i.
     double accq[MAXQ];
 #pragma unroll
     for (int t = 0; t < MAXQ; t++) accq[t] = 0;
@@ -96,14 +112,19 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
       const double xdl = il < n ? (double)Dc[il] * inv_rc * a.deg[il] : 0.0;
       xsum += xdl;
       const int rows = n - i0 < 32 ? (int)(n - i0) : 32;
-      for (int rr = 0; rr < rows; rr++) {
-        const double xd = __shfl_sync(PHDE_FULL_MASK, xdl, rr);
-        const double *Si = a.S + (i0 + rr) * k;
 #pragma unroll
-        for (int t = 0; t < MAXQ; t++) {
-          const int q = lane + 32 * t;
-          if (q < jm1) accq[t] = fma(xd, Si[q], accq[t]);
+      for (int t = 0; t < MAXQ; t++) {
+        const int c0 = 32 * t;
+        if (c0 >= jm1) break;
+        const int nc = jm1 - c0 < 32 ? jm1 - c0 : 32;
+        stage_tile(a.S, i0, rows, k, c0, nc, tile, lane);
+        double acc = accq[t];
+        for (int rr = 0; rr < rows; rr++) {
+          const double xd = __shfl_sync(PHDE_FULL_MASK, xdl, rr);
+          if (lane < nc) acc = fma(xd, tile[rr * TILE_LD + lane], acc);
         }
+        accq[t] = acc;
+        __syncwarp();
       }
     }
     xsum = warp_sum(xsum);
@@ -148,19 +169,28 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
       __syncthreads();
     }
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-    // ---- E: x' = x - (sum_q coef_q S_q + coef_0 u0), one thread per row; and ||x'||^2 ----
+    // ---- E: x' = x - (sum_q coef_q S_q + coef_0 u0), one lane per row of a staged tile; ||x'||^2 ----
     __syncthreads();
     for (int q = threadIdx.x; q < jm1; q += blockDim.x) sm[q] = __ldcg(a.coef + q);
     __syncthreads();
     const double c0u0 = __ldcg(a.coef + k) * inv0;
     double ssq = 0;
-    for (int64_t i = gt; i < n; i += gts) {
-      const double *Si = a.S + i * k;
+    for (int64_t i0 = gw * 32; i0 < n; i0 += gws * 32) {
+      const int rows = n - i0 < 32 ? (int)(n - i0) : 32;
       double p = 0;
-      for (int q = 0; q < jm1; q++) p = fma(sm[q], Si[q], p);
-      const double xp = (double)Dc[i] * inv_rc - (p + c0u0);
-      a.X[i] = xp;
-      ssq = fma(xp, xp, ssq);
+      for (int c0 = 0; c0 < jm1; c0 += 32) {
+        const int nc = jm1 - c0 < 32 ? jm1 - c0 : 32;
+        stage_tile(a.S, i0, rows, k, c0, nc, tile, lane);
+        if (lane < rows)
+          for (int q = 0; q < nc; q++) p = fma(sm[c0 + q], tile[lane * TILE_LD + q], p);
+        __syncwarp();
+      }
+      if (lane < rows) {
+        const int64_t i = i0 + lane;
+        const double xp = (double)Dc[i] * inv_rc - (p + c0u0);
+        a.X[i] = xp;
+        ssq = fma(xp, xp, ssq);
+      }
     }
     ssq = block_sum(ssq, red);
     if (threadIdx.x == 0) a.part2[blockIdx.x] = ssq;
@@ -614,7 +644,7 @@ int phde_cgs(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const dou
              int *h_state, double *h_dlog) {
   const int64_t n = ctx->n;
   int per_sm = 0;
-  const size_t smem = sizeof(double) * (CGS_THREADS / 32) * (size_t)(k + 2);
+  const size_t smem = sizeof(double) * (CGS_THREADS / 32) * ((size_t)(k + 2) + 32 * TILE_LD);
   PHDE_CK(ctx, cudaFuncSetAttribute(cgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cgs_kernel, CGS_THREADS, smem));
   if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "cgs kernel cannot be resident");

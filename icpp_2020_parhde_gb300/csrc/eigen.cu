@@ -12,6 +12,9 @@
 //   part with the round-robin pairing, N/2 disjoint rotations per step; eigenvalues ascending; every
 //   eigenvector signed so that its largest-magnitude entry (lowest index on ties) is positive.
 // pick_kernel: eigenVectors columns for First (0..c-1) or Largest (N-1-j), DrawingBase.cpp:51-108.
+#include <cooperative_groups.h>
+#include <cstdlib>
+
 #include "ctx.h"
 
 namespace {
@@ -153,6 +156,152 @@ __global__ void __launch_bounds__(EIG_THREADS) power_kernel(const double *Kin, i
     const bool neg = E[(N - i - 1) * N] < 0;
     K[row + (N - i - 1) * N] = neg ? -E[row + i * N] : E[row + i * N];
   }
+}
+
+// ---- the same power iteration on a cluster of PW_CL CTAs (one per SM) ----
+// GB300 runs FP64 at 1/64 of FP32, so one SM's FP64 pipe bounds the single-CTA kernel.  Here CTA c of
+// the cluster owns vectors i = c, c + PW_CL, ...; each CTA keeps K in its shared memory, multiplies its
+// own vectors, and in the Gram-Schmidt wavefront reads the finished vector j (and its cached <E_j,E_j>)
+// straight from the owner's shared memory through distributed shared memory.  A hardware cluster
+// barrier separates wavefront steps.  Every floating-point operation is the one power_kernel<false>
+// performs, in the same order, so the two kernels return identical bits.
+constexpr int PW_CL = 8;
+constexpr int PW_MAX_N = 128;
+
+__global__ void __cluster_dims__(PW_CL, 1, 1) __launch_bounds__(EIG_THREADS)
+    power_cluster_kernel(const double *Kin, int N, double *Kout, double *evals_out, int *iters, int *status,
+                         int max_iter) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  extern __shared__ double psm[];
+  const int NO = (N + PW_CL - 1) / PW_CL;  // vectors owned per CTA
+  double *Ks = psm;                         // N*N, column-major
+  double *Eo = Ks + N * N;                  // NO*N: owned vector li at Eo + li*N
+  double *To = Eo + NO * N;
+  double *ddo = To + NO * N;                // NO
+  double *evo = ddo + NO;                   // NO
+  double *rmin = evo + NO;                  // 1 slot read by the whole cluster
+  __shared__ double red[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int NN = N * N;
+  for (int i = tid; i < NN; i += blockDim.x) Ks[i] = Kin[i];
+  // start vectors: every CTA replays the glibc stream and keeps the columns it owns
+  if (tid == 0) {
+    int32_t ring[34];
+    ring[0] = 1;
+    for (int i = 1; i < 31; i++) {
+      int32_t hi = ring[i - 1] / 127773, lo = ring[i - 1] % 127773;
+      int32_t word = 16807 * lo - 2836 * hi;
+      if (word < 0) word += 2147483647;
+      ring[i] = word;
+    }
+    for (int i = 31; i < 34; i++) ring[i] = ring[i - 31];
+    int out = 0;
+    for (int i = 34; out < NN; i++) {
+      const int32_t v = (int32_t)((uint32_t)ring[(i - 31) % 34] + (uint32_t)ring[(i - 3) % 34]);
+      ring[i % 34] = v;
+      if (i >= 344) {
+        const int col = out / N, row = out % N;
+        if (col % PW_CL == rank) Eo[(col / PW_CL) * N + row] = (double)(int32_t)(((uint32_t)v) >> 1) / 2147483647.0;
+        out++;
+      }
+    }
+  }
+  __syncthreads();
+  for (int li = warp; li < NO; li += nw) {
+    const int i = rank + li * PW_CL;
+    if (i >= N) continue;
+    const double nv = sqrt(warp_dot<false>(Eo + li * N, Eo + li * N, N, lane));
+    for (int r = lane; r < N; r += 32) Eo[li * N + r] = Eo[li * N + r] / nv;
+    if (lane == 0) evo[li] = nv;
+  }
+  double r = 0;
+  int it = 0;
+  while (r < 1.0 - 1e-3) {
+    it++;
+    if (isnan(r) || isinf(r) || it > max_iter) {
+      if (rank == 0 && tid == 0) *status = PHDE_ERR_NOCONVERGE;
+      return;  // uniform across the cluster: every CTA holds the same r and it
+    }
+    __syncthreads();
+    for (int x = tid; x < NO * N; x += blockDim.x) To[x] = Eo[x];
+    __syncthreads();
+    for (int idx = tid; idx < NO * N; idx += blockDim.x) {
+      const int li = idx / N, row = idx % N;
+      if (rank + li * PW_CL >= N) continue;
+      double acc = 0;
+      for (int j = 0; j < N; j++) acc = __dadd_rn(acc, __dmul_rn(Ks[row + j * N], To[j + li * N]));
+      Eo[idx] = acc;
+    }
+    cluster.sync();
+    if (rank == 0 && warp == 0) {  // vector 0 is final from the start
+      const double d0 = warp_dot<false>(Eo, Eo, N, lane);
+      if (lane == 0) ddo[0] = d0;
+    }
+    cluster.sync();
+    for (int t = 1; t <= 2 * N - 2; t++) {
+      for (int li = warp; li < NO; li += nw) {
+        const int i = rank + li * PW_CL;
+        const int j = t - i;
+        if (i >= N || j < 0 || j > i) continue;
+        if (j == i) {
+          const double d = warp_dot<false>(Eo + li * N, Eo + li * N, N, lane);
+          if (lane == 0) ddo[li] = d;
+          continue;
+        }
+        const double *Ej = cluster.map_shared_rank(Eo, j % PW_CL) + (j / PW_CL) * N;
+        const double djj = *cluster.map_shared_rank(ddo + j / PW_CL, j % PW_CL);
+        const double num = warp_dot<false>(Ej, Eo + li * N, N, lane);
+        const double fac = num / djj;
+        for (int q = lane; q < N; q += 32) Eo[li * N + q] = __dsub_rn(Eo[li * N + q], __dmul_rn(fac, Ej[q]));
+        __syncwarp();
+      }
+      cluster.sync();
+    }
+    double mn = 1.0;
+    for (int li = warp; li < NO; li += nw) {
+      const int i = rank + li * PW_CL;
+      if (i >= N) continue;
+      const double nv = sqrt(warp_dot<false>(Eo + li * N, Eo + li * N, N, lane));
+      for (int q = lane; q < N; q += 32) Eo[li * N + q] = Eo[li * N + q] / nv;
+      if (lane == 0) evo[li] = nv;
+      __syncwarp();
+      const double d = fabs(warp_dot<false>(Eo + li * N, To + li * N, N, lane));
+      mn = d < mn ? d : mn;
+    }
+    if (lane == 0) red[warp] = mn;
+    __syncthreads();
+    if (tid == 0) {
+      double m = 1.0;
+      for (int w = 0; w < nw; w++) m = red[w] < m ? red[w] : m;
+      *rmin = m;
+    }
+    cluster.sync();
+    double m = 1.0;
+    for (int c = 0; c < PW_CL; c++) {
+      const double v = *cluster.map_shared_rank(rmin, c);
+      m = v < m ? v : m;
+    }
+    r = m;
+    cluster.sync();  // every CTA has read the slots before the next sweep overwrites them
+  }
+  // output: column N-1-i <- +-E_i, sign from the first entry of E_{N-1-i} (ParallelComponents.cpp:140-153);
+  // eigenvalue norms reversed into ascending order
+  for (int idx = tid; idx < NO * N; idx += blockDim.x) {
+    const int li = idx / N, row = idx % N;
+    const int i = rank + li * PW_CL;
+    if (i >= N) continue;
+    const int o = N - 1 - i;
+    const double first = *cluster.map_shared_rank(Eo + (o / PW_CL) * N, o % PW_CL);
+    Kout[row + o * N] = first < 0 ? -Eo[li * N + row] : Eo[li * N + row];
+    if (row == 0) evals_out[o] = evo[li];
+  }
+  if (rank == 0 && tid == 0) {
+    *iters = it;
+    *status = PHDE_OK;
+  }
+  cluster.sync();  // keep every CTA's shared memory alive until the others have read it
 }
 
 // Exact symmetric eigensolve by parallel cyclic Jacobi (Brent-Luk round-robin ordering).
@@ -319,10 +468,17 @@ int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest,
   if (eig == PHDE_EIG_EXACT) {
     jacobi_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, w1, w2, d_K, d_evals, st, st + 1, 100);
   } else {
-    if (seq)
-      power_kernel<true><<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000, dd);
-    else
-      power_kernel<false><<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000, dd);
+    const int NO = (N + PW_CL - 1) / PW_CL;
+    const size_t csmem = sizeof(double) * ((size_t)N * N + 2 * (size_t)NO * N + 2 * NO + 1);
+    if (seq || N > PW_MAX_N || getenv("PHDE_POWER_SINGLE_CTA")) {
+      if (seq)
+        power_kernel<true><<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000, dd);
+      else
+        power_kernel<false><<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, d_K, w1, w2, d_evals, st, st + 1, 20000, dd);
+    } else {
+      PHDE_CK(ctx, cudaFuncSetAttribute(power_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem));
+      power_cluster_kernel<<<PW_CL, EIG_THREADS, csmem, ctx->stream>>>(d_M, N, d_K, d_evals, st, st + 1, 20000);
+    }
   }
   PHDE_LAUNCHED(ctx);
   pick_kernel<<<1, 256, 0, ctx->stream>>>(d_K, N, c, largest, d_Y);

@@ -10,8 +10,10 @@
 //   top-down  : edge-balanced -- thread e takes the e-th out-edge of F_L, finds its owner vertex by
 //               binary search over the frontier's start-edge prefix array, and claims the neighbour
 //               with a CAS on its distance entry (-1 -> L+1);
-//   bottom-up : every unvisited vertex scans its neighbours for one at distance L and stops at the
-//               first;
+//   bottom-up : every unvisited vertex scans its neighbours for one in the frontier and stops at the
+//               first; the frontier is a bitmap (one bit per vertex) that every block copies into
+//               shared memory at the start of the level when it fits (80 KB for 646k vertices), so the
+//               membership test is a shared-memory hit;
 //   both append the new frontier with block-aggregated 64-bit atomics that keep (slot, edge prefix)
 //   together, so the next top-down step is load balanced even around hub vertices.
 // The top-down / bottom-up switch follows the reference rule (alpha = 15, beta = 18): go bottom-up
@@ -22,11 +24,15 @@
 // Selection (ParHDE.cpp:127-155): min_d[v] = min(min_d[v], d_p[v]); the next source is the vertex of
 // largest min_d, lowest index first (a 64-bit atomicMax on (min_d << 32) | ~v); if that vertex is in
 // the history, the duplicate fix-up takes the highest-index vertex with the same min_d that is not.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
 #include "ctx.h"
 
 namespace {
 
-constexpr int KC_THREADS = 512;
+constexpr int KC_THREADS = 1024;
 
 struct KcArgs {
   const int64_t *off;
@@ -43,8 +49,13 @@ struct KcArgs {
   ull *keys;        // [P]
   ull *fixkey;      // [P]
   uint32_t *qv0, *qv1, *qe0, *qe1;
+  uint32_t *bm[3];  // frontier bitmaps, W words each, rotating with the global step (zero initially)
+  int64_t W;        // words per bitmap
+  int smem_bm;      // copy the frontier bitmap into shared memory for bottom-up levels
   ull *ctr;         // [4] ring of (count << 32 | edges)
   ull *edges;       // [1] adjacency entries read
+  ull *trace;       // optional timeline: per level {globaltimer, pass<<40 | level<<32 | in_bu, frontier count, edges}
+  int trace_cap;    // entries of 4 words
   GridSync *gs;
   int *err;
   uint64_t timeout_ns;
@@ -54,7 +65,8 @@ struct KcArgs {
 __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
   __shared__ PushScratch psc;
   __shared__ ull red[32];
-  extern __shared__ uint32_t s_hist[];  // [P]: every block keeps the same selection history
+  extern __shared__ uint32_t s_hist[];  // [P]: every block keeps the same selection history, then the bitmap
+  uint32_t *s_bm = s_hist + ((a.P + 3) & ~3);
   const int64_t n = a.n;
   const int tid = threadIdx.x;
   const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
@@ -67,6 +79,8 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
     int32_t *Dp = a.D + (int64_t)p * n;
     if (tid == 0) {
       Dp[src] = 0;
+      // the level-0 frontier bitmap holds only the source (the previous pass left it empty)
+      atomicOr(a.bm[step % 3] + (src >> 5), 1u << (src & 31));
       if (blockIdx.x == 0) a.sources[p] = src;
     }
     __syncthreads();
@@ -94,6 +108,12 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
       uint32_t *qout_e = (step & 1) ? a.qe0 : a.qe1;
       ull *octr = a.ctr + (step & 3);
       if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 2) & 3] = 0ull;
+      const uint32_t *bm_cur = a.bm[step % 3];
+      uint32_t *bm_next = a.bm[(step + 1) % 3];
+      {  // the bitmap of the previous level becomes the next level's (empty) output
+        uint32_t *bm_clr = a.bm[(step + 2) % 3];
+        for (int64_t w = gbase + tid; w < a.W; w += gstride) bm_clr[w] = 0u;
+      }
 
       if (!in_bu) {
         const int64_t E = f_edges;
@@ -114,11 +134,17 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
             if (Dp[v] == -1 && atomicCAS(Dp + v, -1, L + 1) == -1) {
               claimed = true;
               dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+              atomicOr(bm_next + (v >> 5), 1u << (v & 31));
             }
           }
           block_push(claimed, v, dv, qout_v, qout_e, octr, &psc);
         }
       } else {
+        if (a.smem_bm) {
+          for (int64_t w = tid; w < a.W; w += blockDim.x) s_bm[w] = __ldcg(bm_cur + w);
+          __syncthreads();
+        }
+        const uint32_t *front = a.smem_bm ? s_bm : bm_cur;
         for (int64_t base = gbase; base < n; base += gstride) {
           const int64_t v = base + tid;
           bool found = false;
@@ -127,7 +153,9 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
             const int64_t j0 = a.off[v], j1 = a.off[v + 1];
             for (int64_t j = j0; j < j1; j++) {
               edges_local++;
-              if (Dp[__ldg(a.adj + j)] == L) {
+              const uint32_t u = __ldg(a.adj + j);
+              const uint32_t word = a.smem_bm ? front[u >> 5] : __ldcg(front + (u >> 5));
+              if ((word >> (u & 31)) & 1u) {
                 found = true;
                 break;
               }
@@ -137,6 +165,10 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
               dv = (uint32_t)(j1 - j0);
             }
           }
+          // one bitmap word per warp: the warp covers 32 consecutive, 32-aligned vertices
+          const uint32_t bal = __ballot_sync(PHDE_FULL_MASK, found);
+          const int64_t v0 = v - (tid & 31);
+          if ((tid & 31) == 0 && v0 < n) bm_next[v0 >> 5] = bal;
           block_push(found, (uint32_t)v, dv, qout_v, qout_e, octr, &psc);
         }
       }
@@ -144,6 +176,13 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
       const ull out = __ldcg(octr);
       f_cnt = (uint32_t)(out >> 32);
       f_edges = (uint32_t)(out & 0xffffffffull);
+      if (a.trace && blockIdx.x == 0 && tid == 0 && step < (uint32_t)a.trace_cap) {
+        ull *tr = a.trace + 4 * (size_t)step;
+        tr[0] = global_timer_ns();
+        tr[1] = ((ull)p << 40) | ((ull)(uint32_t)L << 32) | (in_bu ? 1ull : 0ull);
+        tr[2] = f_cnt;
+        tr[3] = f_edges;
+      }
       if (in_bu) {
         awake = f_cnt;
         if (!(awake >= old_awake || awake > n / a.beta)) {
@@ -250,6 +289,10 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   uint32_t *qe0 = (uint32_t *)phde_buf(ctx, "q.e0", sizeof(uint32_t) * n);
   uint32_t *qe1 = (uint32_t *)phde_buf(ctx, "q.e1", sizeof(uint32_t) * n);
   ull *ctr = (ull *)phde_buf(ctx, "q.ctr", sizeof(ull) * 4);
+  const int64_t W = (n + 31) / 32;
+  uint32_t *bms = (uint32_t *)phde_buf(ctx, "kc.bitmaps", sizeof(uint32_t) * 3 * W);
+  if (!bms) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(bms, 0, sizeof(uint32_t) * 3 * W, ctx->stream));
   if (!min_d || !keys || !fixkey || !qv0 || !qv1 || !qe0 || !qe1 || !ctr) return PHDE_ERR_OOM;
 
   PHDE_CK(ctx, cudaMemsetAsync(d_D, 0xff, sizeof(int32_t) * (size_t)n * (size_t)P, ctx->stream));
@@ -262,10 +305,15 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   if ((rc = phde_reset_sync(ctx))) return rc;
 
   int per_sm = 0;
-  const size_t smem = sizeof(uint32_t) * (size_t)P;
+  // shared memory: the selection history, then (when it fits two blocks per SM) the frontier bitmap
+  const size_t hist_bytes = sizeof(uint32_t) * (size_t)((P + 3) & ~3);
+  const size_t bm_bytes = sizeof(uint32_t) * (size_t)W;
+  const int smem_bm = hist_bytes + bm_bytes <= 100 * 1024;
+  const size_t smem = hist_bytes + (smem_bm ? bm_bytes : 0);
+  PHDE_CK(ctx, cudaFuncSetAttribute(kcenters_bfs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kcenters_bfs_kernel, KC_THREADS, smem));
   if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "kcenters kernel cannot be resident");
-  per_sm = std::min(per_sm, 4);
+  per_sm = std::min(per_sm, 2);
   KcArgs a;
   a.off = ctx->d_off;
   a.adj = ctx->d_adj;
@@ -286,7 +334,24 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   a.qe0 = qe0;
   a.qe1 = qe1;
   a.ctr = ctr;
+  a.bm[0] = bms;
+  a.bm[1] = bms + W;
+  a.bm[2] = bms + 2 * W;
+  a.W = W;
+  a.smem_bm = smem_bm;
   a.edges = d_edges;
+  // PHDE_BFS_TRACE=<file>: write the per-level timeline of this launch as CSV after it completes
+  const char *trace_file = getenv("PHDE_BFS_TRACE");
+  const int trace_cap = 1 << 16;
+  a.trace = nullptr;
+  a.trace_cap = 0;
+  if (trace_file) {
+    a.trace = (ull *)phde_buf(ctx, "kc.trace", sizeof(ull) * 4 * trace_cap);
+    if (a.trace) {
+      PHDE_CK(ctx, cudaMemsetAsync(a.trace, 0, sizeof(ull) * 4 * trace_cap, ctx->stream));
+      a.trace_cap = trace_cap;
+    }
+  }
   a.gs = ctx->d_sync;
   a.err = ctx->d_err;
   a.timeout_ns = ctx->timeout_ns;
@@ -299,5 +364,17 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   PHDE_LAUNCHED(ctx);
   cudaEventRecord(ctx->kev[1], ctx->stream);
   ctx->kev_pending = true;
+  if (a.trace) {
+    std::vector<ull> h((size_t)4 * trace_cap);
+    PHDE_CK(ctx, cudaMemcpyAsync(h.data(), a.trace, sizeof(ull) * 4 * trace_cap, cudaMemcpyDeviceToHost, ctx->stream));
+    PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (FILE *f = fopen(trace_file, "w")) {
+      fprintf(f, "step,t_ns,pass,level,bottom_up,frontier,frontier_edges\n");
+      for (int i = 0; i < trace_cap && h[4 * i]; i++)
+        fprintf(f, "%d,%llu,%llu,%llu,%llu,%llu,%llu\n", i, h[4 * i], h[4 * i + 1] >> 40, (h[4 * i + 1] >> 32) & 0xff,
+                h[4 * i + 1] & 1, h[4 * i + 2], h[4 * i + 3]);
+      fclose(f);
+    }
+  }
   return PHDE_OK;
 }

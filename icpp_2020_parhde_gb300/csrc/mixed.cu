@@ -47,12 +47,25 @@ struct Cgs2Args {
   uint64_t timeout_ns;
 };
 
+constexpr int TILE_LD = 33;
+__device__ __forceinline__ void stage_tile32(const float *S, int64_t i0, int rows, int k, int c0, int nc, float *tile,
+                                             int lane) {
+  __syncwarp();
+  if (lane < nc) {
+    const float *src = S + i0 * k + c0 + lane;
+#pragma unroll 8
+    for (int r = 0; r < rows; r++) tile[r * TILE_LD + lane] = src[(int64_t)r * k];
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(C2_THREADS) cgs2_kernel(Cgs2Args a) {
-  extern __shared__ double sm[];  // [nwarps][k+2], then the coefficients as float
+  extern __shared__ double sm[];  // [nwarps][k+2] (coefficients as float in phase E), then float tiles
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int64_t n = a.n;
   const int k = a.k, ld = k + 2;
+  float *tile = (float *)(sm + nw * ld) + warp * 32 * TILE_LD;
   const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
   const double inv0 = 1.0 / sqrt((double)n);
@@ -89,14 +102,19 @@ __global__ void __launch_bounds__(C2_THREADS) cgs2_kernel(Cgs2Args a) {
         }
         vsum += (double)vdl;
         const int rows = n - i0 < 32 ? (int)(n - i0) : 32;
-        for (int rr = 0; rr < rows; rr++) {
-          const float vd = __shfl_sync(PHDE_FULL_MASK, vdl, rr);
-          const float *Si = a.S + (i0 + rr) * k;
 #pragma unroll
-          for (int t = 0; t < MAXQ; t++) {
-            const int q = lane + 32 * t;
-            if (q < jm1) accq[t] = fmaf(vd, Si[q], accq[t]);
+        for (int t = 0; t < MAXQ; t++) {
+          const int c0 = 32 * t;
+          if (c0 >= jm1) break;
+          const int nc = jm1 - c0 < 32 ? jm1 - c0 : 32;
+          stage_tile32(a.S, i0, rows, k, c0, nc, tile, lane);
+          float acc = accq[t];
+          for (int rr = 0; rr < rows; rr++) {
+            const float vd = __shfl_sync(PHDE_FULL_MASK, vdl, rr);
+            if (lane < nc) acc = fmaf(vd, tile[rr * TILE_LD + lane], acc);
           }
+          accq[t] = acc;
+          __syncwarp();
         }
       }
       vsum = warp_sum(vsum);
@@ -148,14 +166,23 @@ __global__ void __launch_bounds__(C2_THREADS) cgs2_kernel(Cgs2Args a) {
       __syncthreads();
       const float c0u0 = (float)(__ldcg(a.coef + k) * inv0);
       ssq = 0;
-      for (int64_t i = gt; i < n; i += gts) {
-        const float *Si = a.S + i * k;
+      for (int64_t i0 = gw * 32; i0 < n; i0 += gws * 32) {
+        const int rows = n - i0 < 32 ? (int)(n - i0) : 32;
         float p = 0.f;
-        for (int q = 0; q < jm1; q++) p = fmaf(cf[q], Si[q], p);
-        const float v = pass == 0 ? (float)Dc[i] * inv_rc : __ldcg(a.X + i);
-        const float vp = v - (p + c0u0);
-        a.X[i] = vp;
-        ssq += (double)vp * (double)vp;
+        for (int c0 = 0; c0 < jm1; c0 += 32) {
+          const int nc = jm1 - c0 < 32 ? jm1 - c0 : 32;
+          stage_tile32(a.S, i0, rows, k, c0, nc, tile, lane);
+          if (lane < rows)
+            for (int q = 0; q < nc; q++) p = fmaf(cf[c0 + q], tile[lane * TILE_LD + q], p);
+          __syncwarp();
+        }
+        if (lane < rows) {
+          const int64_t i = i0 + lane;
+          const float v = pass == 0 ? (float)Dc[i] * inv_rc : __ldcg(a.X + i);
+          const float vp = v - (p + c0u0);
+          a.X[i] = vp;
+          ssq += (double)vp * (double)vp;
+        }
       }
       if (pass == 1) {
         ssq = block_sum(ssq, red);
@@ -386,7 +413,7 @@ int grid_of(phde_ctx *ctx, int64_t work, int threads, int per_sm) {
 int phde_cgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, float *S, int k,
                     int *h_state, double *h_dlog) {
   const int64_t n = ctx->n;
-  const size_t smem = sizeof(double) * (C2_THREADS / 32) * (size_t)(k + 2);
+  const size_t smem = sizeof(double) * (C2_THREADS / 32) * (size_t)(k + 2) + sizeof(float) * (C2_THREADS / 32) * 32 * TILE_LD;
   int per_sm = 0;
   PHDE_CK(ctx, cudaFuncSetAttribute(cgs2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cgs2_kernel, C2_THREADS, smem));

@@ -16,7 +16,7 @@
 
 namespace {
 
-constexpr int SS_THREADS = 512;
+constexpr int SS_THREADS = 1024;
 constexpr int32_t SSSP_INF = 0x7fffffff / 2;  // kDistInf, gapbs/sssp.cc:50
 
 struct SsArgs {
@@ -285,7 +285,7 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   int per_sm = 0;
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_nearfar_kernel, SS_THREADS, 0));
   if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "sssp kernel cannot be resident");
-  per_sm = std::min(per_sm, 4);
+  per_sm = std::min(per_sm, 2);
   SsArgs a;
   a.off = ctx->d_off;
   a.adj = ctx->d_adj;

@@ -130,3 +130,17 @@ def test_reference_class_interface(gpu_ctx):
                                atol=COORD_ATOL)
     with pytest.raises(ParHDEError):
         ParHDE(gw.offsets, gw.adj, gw.weights, gw.n, gw.nnz, 10, 2, 2)
+
+
+def test_cluster_power_iteration_matches_single_cta_bitwise(gpu_ctx, monkeypatch):
+    """The 8-CTA cluster power iteration performs the single-CTA kernel's operations in the same order."""
+    g = graphs.rmat(14, seed=8)
+    gpu_ctx.upload(g)
+    for k in (10, 50):
+        a = gpu_ctx.layout("ParHDE", "Kcenters", k, 3, extra=True)
+        monkeypatch.setenv("PHDE_POWER_SINGLE_CTA", "1")
+        b = gpu_ctx.layout("ParHDE", "Kcenters", k, 3, extra=True)
+        monkeypatch.delenv("PHDE_POWER_SINGLE_CTA")
+        assert a.stats["eig_iters"] == b.stats["eig_iters"]
+        assert np.array_equal(a.evecs, b.evecs) and np.array_equal(a.evals, b.evals)
+        assert np.array_equal(a.coords, b.coords)
