@@ -370,8 +370,11 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       PHDE_CK(ctx, cudaMemcpyAsync(d_src, s.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, ctx->stream));
       int64_t *d_src2 = (int64_t *)phde_buf(ctx, "layout.src2", sizeof(int64_t) * P);
       if (!d_src2) return PHDE_ERR_OOM;
-      // a layout needs every vertex reached: require_all turns an unreached vertex into an error
-      if ((rc = phde_run_bfs_passes(ctx, P, 1, d_src, D, d_src2, sumsq, edges, 1))) return rc;
+      // all sources are known up front: one multi-source sweep per 256 sources
+      int unreached = 0;
+      (void)d_src2;
+      if ((rc = phde_msbfs(ctx, d_src, P, D, sumsq, &unreached))) return rc;
+      if (unreached) return phde_fail(ctx, PHDE_ERR_DISCONNECTED, "distance passes: the graph is not connected");
     } else {
       if ((rc = phde_run_bfs_passes(ctx, P, hde ? 0 : 2, nullptr, D, d_src, sumsq, edges, 1))) return rc;
     }
@@ -525,7 +528,11 @@ int phde_distances(phde_ctx *ctx, const int64_t *sources, int nsrc, int32_t *out
   if (!ctx->weighted) {
     int32_t *D = (int32_t *)phde_buf(ctx, "dist.D", sizeof(int32_t) * n * nsrc);
     if (!D) return PHDE_ERR_OOM;
-    if ((rc = phde_run_bfs_passes(ctx, nsrc, 1, d_src, D, d_src2, sumsq, nullptr, 0))) return rc;
+    if (nsrc >= 4)  // several sources: one bitset sweep per level for all of them
+      rc = phde_msbfs(ctx, d_src, nsrc, D, nullptr, nullptr);
+    else
+      rc = phde_run_bfs_passes(ctx, nsrc, 1, d_src, D, d_src2, sumsq, nullptr, 0);
+    if (rc) return rc;
     PHDE_CK(ctx, cudaMemcpyAsync(out, D, sizeof(int32_t) * n * nsrc, cudaMemcpyDeviceToHost, ctx->stream));
     return phde_check_device_err(ctx, "BFS");
   }

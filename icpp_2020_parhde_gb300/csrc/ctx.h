@@ -26,6 +26,8 @@ struct phde_ctx {
   long long graph_epoch = 0;  // bumped by every upload; caches keyed on it (the SpMM chunk plan)
   long long spmm_plan_epoch = -1;
   int64_t spmm_nheavy = 0, spmm_nchunks = 0;
+  long long ms_plan_epoch = -1;  // multi-source BFS heavy-row plan
+  int64_t ms_nheavy = 0, ms_nchunks = 0;
 
   // device control block for persistent kernels: barrier + error word
   GridSync *d_sync = nullptr;
@@ -77,6 +79,12 @@ int phde_check_device_err(phde_ctx *ctx, const char *what);
 // require_all: an unreached vertex is an error (PHDE_ERR_DISCONNECTED); otherwise it keeps distance -1.
 int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixed_src, int32_t *d_D,
                         int64_t *d_sources, unsigned long long *d_sumsq, unsigned long long *d_edges, int require_all);
+
+// ---- kernels (msbfs.cu) ----
+// Distance columns for nsrc given sources (device array) into D (n * nsrc int32, -1 unreached), up to 256
+// sources per sweep.  With sumsq: exact per-column sums of squares and *h_unreached (synchronises).
+int phde_msbfs(phde_ctx *ctx, const int64_t *d_src, int nsrc, int32_t *D, unsigned long long *sumsq,
+               int *h_unreached);
 
 // ---- kernels (sssp.cu) ----
 // One exact SSSP pass from *d_src into d_col (int32, INF = INT32_MAX/2 for unreachable).

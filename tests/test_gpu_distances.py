@@ -122,3 +122,31 @@ def test_bounded_wait_times_out_and_context_survives(gpu_ctx):
     g, rec = load_golden("mesh125")
     gpu_ctx.upload(g)
     assert np.array_equal(gpu_ctx.distances(rec["bfs_src"]), rec["bfs_dist"])
+
+
+@pytest.mark.parametrize("nsrc", [5, 64, 100, 300])
+def test_multi_source_bfs_bit_exact(gpu_ctx, nsrc):
+    """phde_distances with several sources runs the bitset multi-source BFS (up to 256 sources per sweep)."""
+    g = graphs.rmat(15, seed=12)
+    gpu_ctx.upload(g)
+    rng = np.random.default_rng(nsrc)
+    src = rng.integers(0, g.n, size=nsrc)
+    src[1] = src[0]  # a repeated source is allowed
+    d = gpu_ctx.distances(src)
+    for i in range(0, nsrc, max(1, nsrc // 7)):
+        assert np.array_equal(d[:, i], orc.bfs(g, int(src[i]))), i
+    assert np.array_equal(d[:, 0], d[:, 1])
+
+
+def test_multi_source_bfs_on_mesh_and_disconnected(gpu_ctx):
+    g, rec = load_golden("mesh125")
+    gpu_ctx.upload(g)
+    src = np.concatenate([rec["bfs_src"], np.arange(0, 15625, 1000)])
+    d = gpu_ctx.distances(src)
+    assert np.array_equal(d[:, :3], rec["bfs_dist"])
+    for i in range(3, len(src)):
+        assert np.array_equal(d[:, i], orc.bfs(g, int(src[i])))
+    g2 = _two_triangles()
+    gpu_ctx.upload(g2)
+    d = gpu_ctx.distances([0, 1, 3, 5])
+    assert list(d[:, 0]) == [0, 1, 1, -1, -1, -1] and list(d[:, 2]) == [-1, -1, -1, 0, 1, 1]
