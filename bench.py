@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=3)
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     return ap.parse_args()
 
 
@@ -297,6 +298,37 @@ def run_gb300(args):
                  "rayleigh_fp64": rq64.tolist(), "rayleigh_mixed": rqm.tolist(),
                  "rayleigh_rel_err_max": float(np.max(np.abs(rqm - rq64) / np.abs(rq64))),
                  "eig_iters": rm.stats["eig_iters"], "naccepted": rm.stats["naccepted"]}
+    learned = None
+    if not args.no_learned:
+        # learned pivots (one multi-source BFS instead of 3k serial passes), same workload and precision;
+        # accepted when every coordinate's Rayleigh quotient is within 2% of the plain Kcenters layout's
+        xy64 = None
+        r64 = ctx.layout("ParHDE", "Kcenters", k, c, coords_out=xy_h.numpy())
+        xy64 = xy_h.numpy().reshape(c, n).T.copy()
+        for _ in range(args.warmup):
+            ctx.layout("ParHDE", "Learned", k, c, coords_out=xy_h.numpy())
+        ms_l = []
+        for _ in range(args.steps):
+            flush_l2()
+            rl = ctx.layout("ParHDE", "Learned", k, c, coords_out=xy_h.numpy())
+            ms_l.append(rl.stats["ms_total"])
+        xyl = xy_h.numpy().reshape(c, n).T.copy()
+        ms_lm = []
+        for _ in range(args.steps):
+            flush_l2()
+            rlm = ctx.layout("ParHDE", "Learned", k, c, precision="mixed", coords_out=xy_h.numpy())
+            ms_lm.append(rlm.stats["ms_total"])
+        xylm = xy_h.numpy().reshape(c, n).T.copy()
+        rq_p, rq_l, rq_lm = rayleigh_quotients(g, xy64), rayleigh_quotients(g, xyl), rayleigh_quotients(g, xylm)
+        msl, mslm = allmax(ws, float(np.mean(ms_l))), allmax(ws, float(np.mean(ms_lm)))
+        learned = {"value": ws * k * nnz / (msl * 1e-3), "unit": UNIT, "ms_per_graph": msl, "dtype": "f64",
+                   "speedup_vs_plain": ms_max / msl,
+                   "phases_ms": {kk: rl.stats[kk] for kk in ("ms_dist", "ms_orth", "ms_mmult", "ms_eig", "ms_coords")},
+                   "rayleigh_plain": rq_p.tolist(), "rayleigh_learned": rq_l.tolist(),
+                   "accepted_within_2pct": bool(np.all(rq_l <= 1.02 * rq_p)),
+                   "mixed": {"value": ws * k * nnz / (mslm * 1e-3), "ms_per_graph": mslm, "dtype": "f32+f64",
+                             "speedup_vs_plain": ms_max / mslm, "rayleigh": rq_lm.tolist(),
+                             "accepted_within_2pct": bool(np.all(rq_lm <= 1.02 * rq_p))}}
     if rank != 0:
         return
     line = {
@@ -321,6 +353,7 @@ def run_gb300(args):
         "clocks": clk.summary(),
         "stats_last": stats[-1],
         "mixed_precision": mixed,
+        "learned_pivots": learned,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g, args, args.cpu_reps)

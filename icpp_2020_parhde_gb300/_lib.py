@@ -17,7 +17,7 @@ STATUS = {
 }
 NOALLOC_MAX_VERTICES = 1048576
 ALGOS = {"PivotMDS": 0, "PHDE": 1, "wParHDE": 2, "WParHDE": 2, "ParHDE": 3}
-STRATEGIES = {"RandCoarse": 0, "RandFine": 1, "Kcenters": 2}
+STRATEGIES = {"RandCoarse": 0, "RandFine": 1, "Kcenters": 2, "Learned": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 EIGS = {"power": 0, "exact": 1}
 
@@ -26,6 +26,7 @@ EXPORTS = [
     "phde_create", "phde_destroy", "phde_last_error", "phde_status_string", "phde_version", "phde_graph_upload",
     "phde_graph_n", "phde_graph_nnz", "phde_layout", "phde_distances", "phde_kcenters", "phde_DOBFS",
     "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
+    "phde_set_pivot_model",
 ]
 
 
@@ -89,5 +90,6 @@ def load(path: str | None = None):
     L.phde_launch_count.argtypes = [vp]
     L.phde_launch_count.restype = i64
     L.phde_bfs_noalloc.argtypes = [vp, vp, i64, i64, i64, vp, vp]
+    L.phde_set_pivot_model.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
     _lib = L
     return L

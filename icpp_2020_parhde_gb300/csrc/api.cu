@@ -32,6 +32,10 @@ int phde_cgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, co
 int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float *LS, int k);
 int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double *M);
 int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X);
+int phde_default_pivot_model(const float **w, int *count);
+int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, int32_t *d_d0, std::vector<int64_t> &h_cand,
+                          std::vector<float> &h_score);
+int phde_cand_submatrix(phde_ctx *ctx, const int32_t *D, const int64_t *d_cand, int M, std::vector<int32_t> &h_sub);
 int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
                     double *d_evals, double *d_Y, int *h_iters, int seq);
 
@@ -310,8 +314,10 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     if (!S32) return PHDE_ERR_OOM;
   }
   int npasses = 0, naccepted = 0, ndiscarded = 0;
+  int P_used = P;  // distance columns handed to the D-orthogonalisation
   double ms_dist = 0, ms_orth = 0;
-  const bool random = algo != PHDE_ALGO_WPARHDE && o->strategy != PHDE_STRAT_KCENTERS;
+  const bool random = algo != PHDE_ALGO_WPARHDE && (o->strategy == PHDE_STRAT_RANDFINE ||
+                                                    o->strategy == PHDE_STRAT_RANDCOARSE);
 
   if (algo == PHDE_ALGO_WPARHDE) {
     // ---- coupled SSSP + MGS loop (WParHDE.cpp:113-224) ----
@@ -362,7 +368,61 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     // ---- distance phase: Kcenters (or random) BFS passes into D ----
     int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);
     if (!D) return PHDE_ERR_OOM;
-    if (random) {
+    if (o->strategy == PHDE_STRAT_LEARNED) {
+      // ---- learned pivots: MLP candidates, one multi-source BFS, farthest-point order ----
+      const int M = (int)std::min<int64_t>(PHDE_LEARNED_CANDIDATES, n);
+      int32_t *d0 = (int32_t *)phde_buf(ctx, "lp.d0", sizeof(int32_t) * n);
+      int32_t *DM = (int32_t *)phde_buf(ctx, "lp.DM", sizeof(int32_t) * n * M);
+      int64_t *dc = (int64_t *)phde_buf(ctx, "lp.dcand", sizeof(int64_t) * M);
+      ull *ssqM = (ull *)phde_buf(ctx, "lp.ssqM", sizeof(ull) * M);
+      if (!d0 || !DM || !dc || !ssqM) return PHDE_ERR_OOM;
+      if (ctx->pivot_model.empty()) {
+        const float *w0;
+        int cnt;
+        if ((rc = phde_default_pivot_model(&w0, &cnt))) return phde_fail(ctx, rc, "built-in pivot model has the wrong size");
+        ctx->pivot_model.assign(w0, w0 + cnt);
+      }
+      std::vector<int64_t> cand;
+      std::vector<float> cscore;
+      if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), M, d0, cand, cscore))) return rc;
+      const int Mc = (int)cand.size();
+      PHDE_CK(ctx, cudaMemcpyAsync(dc, cand.data(), sizeof(int64_t) * Mc, cudaMemcpyHostToDevice, ctx->stream));
+      int unreached = 0;
+      if ((rc = phde_msbfs(ctx, dc, Mc, DM, ssqM, &unreached))) return rc;
+      if (unreached) return phde_fail(ctx, PHDE_ERR_DISCONNECTED, "distance passes: the graph is not connected");
+      std::vector<int32_t> sub;
+      if ((rc = phde_cand_submatrix(ctx, DM, dc, Mc, sub))) return rc;
+      // farthest-point order on the exact candidate distances: start from the best-scored candidate,
+      // then repeatedly the candidate farthest from those chosen (best score first on ties)
+      const int Pl = std::min(P, Mc);
+      std::vector<int> order;
+      std::vector<int32_t> mind(Mc, INT32_MAX);
+      std::vector<char> used(Mc, 0);
+      int next = 0;
+      for (int p = 0; p < Pl; p++) {
+        order.push_back(next);
+        used[next] = 1;
+        int best = -1;
+        for (int i = 0; i < Mc; i++) {
+          mind[i] = std::min(mind[i], sub[(size_t)i * Mc + next]);
+          if (!used[i] && (best < 0 || mind[i] > mind[best])) best = i;
+        }
+        next = best < 0 ? 0 : best;
+      }
+      std::vector<ull> hs(Mc), hs2(Pl);
+      std::vector<int64_t> srcs(Pl);
+      PHDE_CK(ctx, cudaMemcpyAsync(hs.data(), ssqM, sizeof(ull) * Mc, cudaMemcpyDeviceToHost, ctx->stream));
+      PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+      for (int p = 0; p < Pl; p++) {
+        PHDE_CK(ctx, cudaMemcpyAsync(D + (int64_t)p * n, DM + (int64_t)order[p] * n, sizeof(int32_t) * n,
+                                     cudaMemcpyDeviceToDevice, ctx->stream));
+        hs2[p] = hs[order[p]];
+        srcs[p] = cand[order[p]];
+      }
+      PHDE_CK(ctx, cudaMemcpyAsync(sumsq, hs2.data(), sizeof(ull) * Pl, cudaMemcpyHostToDevice, ctx->stream));
+      PHDE_CK(ctx, cudaMemcpyAsync(d_src, srcs.data(), sizeof(int64_t) * Pl, cudaMemcpyHostToDevice, ctx->stream));
+      P_used = Pl;
+    } else if (random) {
       std::vector<int32_t> r;
       glibc_rand_host((uint32_t)o->seed, P, r);
       std::vector<int64_t> s(P);
@@ -379,15 +439,15 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       if ((rc = phde_run_bfs_passes(ctx, P, hde ? 0 : 2, nullptr, D, d_src, sumsq, edges, 1))) return rc;
     }
     if ((rc = phde_check_device_err(ctx, "distance passes"))) return rc;
-    npasses = P;
+    npasses = P_used;
     tm.mark(1);
     if (hde) {
       int state[4] = {0, 0, 0, 0};
       std::vector<double> dlog(P);
       if (mixed)
-        rc = phde_cgs2_mixed(ctx, D, P, sumsq, deg, S32, k, state, dlog.data());
+        rc = phde_cgs2_mixed(ctx, D, P_used, sumsq, deg, S32, k, state, dlog.data());
       else
-        rc = phde_cgs(ctx, D, P, sumsq, deg, Sbuf, k, state, dlog.data());
+        rc = phde_cgs(ctx, D, P_used, sumsq, deg, Sbuf, k, state, dlog.data());
       if (rc) return rc;
       if ((rc = phde_check_device_err(ctx, "D-orthogonalisation"))) return rc;
       naccepted = state[0];
@@ -493,7 +553,9 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, in
   if (!ctx || !o || !coords_out) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout: null argument");
   if (ctx->n <= 0) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_layout: no graph uploaded");
   if (o->algo < 0 || o->algo > 3) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized algorithm");
-  if (o->strategy < 0 || o->strategy > 2) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized Strategy");
+  if (o->strategy < 0 || o->strategy > 3) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized Strategy");
+  if (o->strategy == PHDE_STRAT_LEARNED && o->algo != PHDE_ALGO_PARHDE)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "learned pivots are implemented for ParHDE");
   if (o->eig != PHDE_EIG_POWER && o->eig != PHDE_EIG_EXACT) return phde_fail(ctx, PHDE_ERR_INVALID, "unknown eigensolver");
   if (o->precision != PHDE_PREC_FP64 && o->precision != PHDE_PREC_MIXED)
     return phde_fail(ctx, PHDE_ERR_INVALID, "unknown precision");
@@ -624,6 +686,15 @@ int phde_DeltaStep(const uint32_t *row, const uint32_t *col, const int32_t *weig
   int64_t s = source;
   if ((rc = phde_distances(ctx, &s, 1, d.data()))) return rc;
   for (long v = 0; v < numNodes; v++) dist[v] = (double)d[v];  // every entry, kDistInf when unreached (sssp.cc:137-139)
+  return PHDE_OK;
+}
+
+int phde_set_pivot_model(phde_ctx *ctx, const float *weights, int count) {
+  const float *w0;
+  int cnt = 0;
+  phde_default_pivot_model(&w0, &cnt);
+  if (!ctx || !weights || count != cnt) return phde_fail(ctx, PHDE_ERR_INVALID, "pivot model: wrong weight count");
+  ctx->pivot_model.assign(weights, weights + count);
   return PHDE_OK;
 }
 

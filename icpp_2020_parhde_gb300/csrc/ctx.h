@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "parhde.h"
@@ -26,6 +27,7 @@ struct phde_ctx {
   long long graph_epoch = 0;  // bumped by every upload; caches keyed on it (the SpMM chunk plan)
   long long spmm_plan_epoch = -1;
   int64_t spmm_nheavy = 0, spmm_nchunks = 0;
+  std::vector<float> pivot_model;  // MLP weights of the learned pivot strategy
   long long ms_plan_epoch = -1;  // multi-source BFS heavy-row plan
   int64_t ms_nheavy = 0, ms_nchunks = 0;
 

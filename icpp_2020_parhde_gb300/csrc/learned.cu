@@ -1,0 +1,213 @@
+// learned.cu -- learned pivot proposal: per-vertex features and the pivot-scoring MLP.
+//
+// Kcenters picks pivots one at a time (ParHDE.cpp:118-157): every pivot needs the BFS of the previous
+// one, so 3k dependent passes run back to back.  The learned strategy proposes candidates at once:
+//   features (one BFS from vertex 0, Kcenters' own first source):
+//     f0 = log(1+deg v) / log(1+max deg)
+//     f1 = log(1+sum of neighbour degrees) / log(1+max of that sum)
+//     f2 = d0(v) / max d0                  (hop distance from vertex 0)
+//     f3 = |{u in N(v): d0(u) > d0(v)}| / deg v   (share of neighbours farther from the seed)
+//   score = MLP(f): 4 -> 64 -> 64 -> 1, ReLU, FP32 (weights trained on Kcenters pivot sets,
+//           icpp_2020_parhde_gb300/train_pivot_mlp.py, compiled in from pivot_mlp_weights.h)
+// The host then takes the M best-scored vertices, runs ONE multi-source BFS from all of them, and
+// orders P pivots among them by farthest-point selection on their exact pairwise distances.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ctx.h"
+#include "pivot_mlp_weights.h"
+
+namespace {
+
+constexpr int MLP_IN = 4, MLP_H = 64;
+constexpr int MLP_WEIGHTS = MLP_H * MLP_IN + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1;
+
+// deg, neighbour-degree sum, outward-neighbour count; maxima of deg, hop2 and d0
+__global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, const int32_t *d0, int64_t n,
+                                   ull *hop2, uint32_t *outw, ull *maxes) {
+  __shared__ ull red[32];
+  ull mdeg = 0, mhop = 0, md0 = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e0 = off[v], e1 = off[v + 1];
+    const int32_t dv = d0[v];
+    ull h = 0;
+    uint32_t o = 0;
+    for (int64_t e = e0; e < e1; e++) {
+      const int64_t u = __ldg(adj + e);
+      h += (ull)(off[u + 1] - off[u]);
+      o += d0[u] > dv ? 1u : 0u;
+    }
+    hop2[v] = h;
+    outw[v] = o;
+    mdeg = max(mdeg, (ull)(e1 - e0));
+    mhop = max(mhop, h);
+    md0 = max(md0, (ull)(dv < 0 ? 0 : dv));
+  }
+  mdeg = block_max_u64(mdeg, red);
+  mhop = block_max_u64(mhop, red);
+  md0 = block_max_u64(md0, red);
+  if (threadIdx.x == 0) {
+    atomicMax(maxes, mdeg);
+    atomicMax(maxes + 1, mhop);
+    atomicMax(maxes + 2, md0);
+  }
+}
+
+__global__ void mlp_score_kernel(const int64_t *off, const int32_t *d0, const ull *hop2, const uint32_t *outw,
+                                 const ull *maxes, int64_t n, const float *weights, float *score,
+                                 unsigned *hist, int nbins) {
+  __shared__ float w[MLP_WEIGHTS];
+  extern __shared__ unsigned s_hist[];  // [nbins] per-block histogram, merged at the end
+  for (int i = threadIdx.x; i < MLP_WEIGHTS; i += blockDim.x) w[i] = weights[i];
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) s_hist[i] = 0u;
+  __syncthreads();
+  const float *W1 = w, *b1 = W1 + MLP_H * MLP_IN, *W2 = b1 + MLP_H, *b2 = W2 + MLP_H * MLP_H, *w3 = b2 + MLP_H,
+              *b3 = w3 + MLP_H;
+  const float ldeg = logf(1.f + (float)maxes[0]), lhop = logf(1.f + (float)maxes[1]);
+  const float md0 = maxes[2] ? (float)maxes[2] : 1.f;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const float deg = (float)(off[v + 1] - off[v]);
+    float f[MLP_IN];
+    f[0] = ldeg > 0.f ? logf(1.f + deg) / ldeg : 0.f;
+    f[1] = lhop > 0.f ? logf(1.f + (float)hop2[v]) / lhop : 0.f;
+    f[2] = (float)(d0[v] < 0 ? 0 : d0[v]) / md0;
+    f[3] = deg > 0.f ? (float)outw[v] / deg : 0.f;
+    float h1[MLP_H];
+#pragma unroll
+    for (int o = 0; o < MLP_H; o++) {
+      float a = b1[o];
+#pragma unroll
+      for (int i = 0; i < MLP_IN; i++) a = fmaf(W1[o * MLP_IN + i], f[i], a);
+      h1[o] = a > 0.f ? a : 0.f;
+    }
+    float out = b3[0];
+    for (int o = 0; o < MLP_H; o++) {
+      float a = b2[o];
+#pragma unroll
+      for (int i = 0; i < MLP_H; i++) a = fmaf(W2[o * MLP_H + i], h1[i], a);
+      out = fmaf(w3[o], a > 0.f ? a : 0.f, out);
+    }
+    const float p = 1.f / (1.f + expf(-out));
+    score[v] = p;
+    int bin = (int)(p * nbins);
+    bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+    atomicAdd(s_hist + bin, 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+    if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
+}
+
+// vertices whose score bin is >= bmin, compacted (order fixed afterwards on the host)
+__global__ void collect_kernel(const float *score, int64_t n, int bmin, int nbins, int64_t *cand, float *cscore,
+                               unsigned *count, unsigned cap) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const float p = score[v];
+    int bin = (int)(p * nbins);
+    bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+    if (bin >= bmin) {
+      const unsigned at = atomicAdd(count, 1u);
+      if (at < cap) {
+        cand[at] = v;
+        cscore[at] = p;
+      }
+    }
+  }
+}
+
+// M x M distances between the candidates: sub[i*M + j] = d(cand_i, cand_j) from candidate j's column
+__global__ void cand_submatrix_kernel(const int32_t *D, int64_t n, const int64_t *cand, int M, int32_t *sub) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < M * M; idx += gridDim.x * blockDim.x) {
+    const int i = idx / M, j = idx % M;
+    sub[idx] = D[(int64_t)j * n + cand[i]];
+  }
+}
+
+}  // namespace
+
+int phde_default_pivot_model(const float **w, int *count) {
+  *w = kPivotMlpWeights;
+  *count = (int)(sizeof(kPivotMlpWeights) / sizeof(float));
+  return *count == MLP_WEIGHTS ? PHDE_OK : PHDE_ERR_INVALID;
+}
+
+// Score every vertex and return the M best candidates (score descending, index ascending on ties) in
+// h_cand; writes d0 (hop distance from vertex 0) into d_d0.  Synchronises.
+int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, int32_t *d_d0, std::vector<int64_t> &h_cand,
+                          std::vector<float> &h_score) {
+  const int64_t n = ctx->n;
+  const int nbins = 4096;
+  ull *hop2 = (ull *)phde_buf(ctx, "lp.hop2", sizeof(ull) * n);
+  uint32_t *outw = (uint32_t *)phde_buf(ctx, "lp.outw", sizeof(uint32_t) * n);
+  ull *maxes = (ull *)phde_buf(ctx, "lp.max", sizeof(ull) * 3);
+  float *score = (float *)phde_buf(ctx, "lp.score", sizeof(float) * n);
+  unsigned *hist = (unsigned *)phde_buf(ctx, "lp.hist", sizeof(unsigned) * nbins);
+  float *wts = (float *)phde_buf(ctx, "lp.w", sizeof(float) * MLP_WEIGHTS);
+  const unsigned cap = (unsigned)std::max<int64_t>(4 * M, 65536);
+  int64_t *cand = (int64_t *)phde_buf(ctx, "lp.cand", sizeof(int64_t) * cap);
+  float *cscore = (float *)phde_buf(ctx, "lp.cscore", sizeof(float) * cap);
+  unsigned *count = (unsigned *)phde_buf(ctx, "lp.count", sizeof(unsigned));
+  int64_t *src0 = (int64_t *)phde_buf(ctx, "lp.src0", sizeof(int64_t) * 2);
+  ull *ssq = (ull *)phde_buf(ctx, "lp.ssq", sizeof(ull));
+  if (!hop2 || !outw || !maxes || !score || !hist || !wts || !cand || !cscore || !count || !src0 || !ssq)
+    return PHDE_ERR_OOM;
+  // d0: one BFS from vertex 0
+  PHDE_CK(ctx, cudaMemsetAsync(src0, 0, sizeof(int64_t) * 2, ctx->stream));
+  int rc = phde_run_bfs_passes(ctx, 1, 1, src0, d_d0, src0 + 1, ssq, nullptr, 1);
+  if (rc) return rc;
+  if ((rc = phde_check_device_err(ctx, "learned pivots: seed BFS"))) return rc;
+  PHDE_CK(ctx, cudaMemsetAsync(maxes, 0, sizeof(ull) * 3, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(hist, 0, sizeof(unsigned) * nbins, ctx->stream));
+  PHDE_CK(ctx, cudaMemcpyAsync(wts, h_weights, sizeof(float) * MLP_WEIGHTS, cudaMemcpyHostToDevice, ctx->stream));
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->nsm * 8));
+  feature_raw_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, d_d0, n, hop2, outw, maxes);
+  PHDE_LAUNCHED(ctx);
+  mlp_score_kernel<<<g, 256, sizeof(unsigned) * nbins, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts,
+                                                                      score, hist, nbins);
+  PHDE_LAUNCHED(ctx);
+  std::vector<unsigned> hh(nbins);
+  PHDE_CK(ctx, cudaMemcpyAsync(hh.data(), hist, sizeof(unsigned) * nbins, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  // lowest bin such that the bins at or above it hold at least M vertices
+  int bmin = nbins - 1;
+  int64_t acc = 0;
+  for (; bmin > 0; bmin--) {
+    acc += hh[bmin];
+    if (acc >= M) break;
+  }
+  PHDE_CK(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned), ctx->stream));
+  collect_kernel<<<g, 256, 0, ctx->stream>>>(score, n, bmin, nbins, cand, cscore, count, cap);
+  PHDE_LAUNCHED(ctx);
+  unsigned hc = 0;
+  PHDE_CK(ctx, cudaMemcpyAsync(&hc, count, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  hc = std::min(hc, cap);
+  std::vector<int64_t> c(hc);
+  std::vector<float> cs(hc);
+  PHDE_CK(ctx, cudaMemcpyAsync(c.data(), cand, sizeof(int64_t) * hc, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaMemcpyAsync(cs.data(), cscore, sizeof(float) * hc, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<int> ord(hc);
+  for (unsigned i = 0; i < hc; i++) ord[i] = (int)i;
+  std::sort(ord.begin(), ord.end(), [&](int x, int y) { return cs[x] != cs[y] ? cs[x] > cs[y] : c[x] < c[y]; });
+  const int take = (int)std::min<int64_t>(M, hc);
+  h_cand.resize(take);
+  h_score.resize(take);
+  for (int i = 0; i < take; i++) {
+    h_cand[i] = c[ord[i]];
+    h_score[i] = cs[ord[i]];
+  }
+  return PHDE_OK;
+}
+
+int phde_cand_submatrix(phde_ctx *ctx, const int32_t *D, const int64_t *d_cand, int M, std::vector<int32_t> &h_sub) {
+  int32_t *sub = (int32_t *)phde_buf(ctx, "lp.sub", sizeof(int32_t) * M * M);
+  if (!sub) return PHDE_ERR_OOM;
+  cand_submatrix_kernel<<<(M * M + 255) / 256, 256, 0, ctx->stream>>>(D, ctx->n, d_cand, M, sub);
+  PHDE_LAUNCHED(ctx);
+  h_sub.resize((size_t)M * M);
+  PHDE_CK(ctx, cudaMemcpyAsync(h_sub.data(), sub, sizeof(int32_t) * M * M, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return PHDE_OK;
+}

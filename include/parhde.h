@@ -49,6 +49,11 @@ extern "C" {
 #define PHDE_STRAT_RANDCOARSE 0
 #define PHDE_STRAT_RANDFINE 1
 #define PHDE_STRAT_KCENTERS 2
+/* No counterpart in the reference: pivots proposed at once by a per-vertex MLP and ordered by
+ * farthest-point selection on their exact pairwise distances; one multi-source BFS replaces the 3k
+ * serial Kcenters passes (ParHDE only). */
+#define PHDE_STRAT_LEARNED 3
+#define PHDE_LEARNED_CANDIDATES 256
 /* precision of the dense stages (distances are always exact integers) */
 #define PHDE_PREC_FP64 0  /* every dense stage in FP64, the reference's arithmetic            */
 #define PHDE_PREC_MIXED 1 /* FP32 storage/SpMM, compensated Gram products; FP64 k x k solves  */
@@ -146,6 +151,11 @@ int phde_DeltaStep(const uint32_t *row, const uint32_t *col, const int32_t *weig
  * more block than it launches) with the given wait limit, and report the status the kernel returned.
  * Returns PHDE_ERR_TIMEOUT when the bounded wait gave up as designed. */
 int phde_selftest_barrier_timeout(phde_ctx *ctx, int timeout_ms);
+
+/* Replace the pivot-scoring MLP used by PHDE_STRAT_LEARNED (4 -> 64 -> 64 -> 1, ReLU): `count` floats,
+ * W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3[1] (row-major).  The library starts with the
+ * weights trained by icpp_2020_parhde_gb300/train_pivot_mlp.py.  No counterpart in the reference. */
+int phde_set_pivot_model(phde_ctx *ctx, const float *weights, int count);
 
 /* Kernel launches issued through this context since it was created. */
 int64_t phde_launch_count(const phde_ctx *ctx);
