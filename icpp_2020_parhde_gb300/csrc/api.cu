@@ -33,9 +33,10 @@ int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float 
 int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double *M);
 int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X);
 int phde_default_pivot_model(const float **w, int *count);
-int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, int32_t *d_d0, std::vector<int64_t> &h_cand,
-                          std::vector<float> &h_score);
-int phde_cand_submatrix(phde_ctx *ctx, const int32_t *D, const int64_t *d_cand, int M, std::vector<int32_t> &h_sub);
+int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const int32_t *d_d0,
+                          std::vector<int64_t> &h_cand, std::vector<float> &h_score);
+int phde_cand_distances(phde_ctx *ctx, const int32_t *D, int P0, const uint16_t *R, int RW, const int64_t *d_cand,
+                        int M, std::vector<int32_t> &h_sub, std::vector<int32_t> &h_csub);
 int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
                     double *d_evals, double *d_Y, int *h_iters, int seq);
 
@@ -369,59 +370,56 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);
     if (!D) return PHDE_ERR_OOM;
     if (o->strategy == PHDE_STRAT_LEARNED) {
-      // ---- learned pivots: MLP candidates, one multi-source BFS, farthest-point order ----
+      // ---- learned pivots: Kcenters warm start, MLP candidates, one multi-source BFS, farthest-point ----
+      const int P0 = std::min(P, 8);  // exact Kcenters passes (serial, few)
       const int M = (int)std::min<int64_t>(PHDE_LEARNED_CANDIDATES, n);
-      int32_t *d0 = (int32_t *)phde_buf(ctx, "lp.d0", sizeof(int32_t) * n);
-      int32_t *DM = (int32_t *)phde_buf(ctx, "lp.DM", sizeof(int32_t) * n * M);
       int64_t *dc = (int64_t *)phde_buf(ctx, "lp.dcand", sizeof(int64_t) * M);
-      ull *ssqM = (ull *)phde_buf(ctx, "lp.ssqM", sizeof(ull) * M);
-      if (!d0 || !DM || !dc || !ssqM) return PHDE_ERR_OOM;
+      if (!dc) return PHDE_ERR_OOM;
       if (ctx->pivot_model.empty()) {
         const float *w0;
         int cnt;
         if ((rc = phde_default_pivot_model(&w0, &cnt))) return phde_fail(ctx, rc, "built-in pivot model has the wrong size");
         ctx->pivot_model.assign(w0, w0 + cnt);
       }
-      std::vector<int64_t> cand;
+      if ((rc = phde_run_bfs_passes(ctx, P0, 0, nullptr, D, d_src, sumsq, edges, 1))) return rc;
+      if ((rc = phde_check_device_err(ctx, "learned pivots: warm start"))) return rc;
+      std::vector<int64_t> cand, warm(P0);
       std::vector<float> cscore;
-      if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), M, d0, cand, cscore))) return rc;
+      if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), M, D, cand, cscore))) return rc;
       const int Mc = (int)cand.size();
       PHDE_CK(ctx, cudaMemcpyAsync(dc, cand.data(), sizeof(int64_t) * Mc, cudaMemcpyHostToDevice, ctx->stream));
-      int unreached = 0;
-      if ((rc = phde_msbfs(ctx, dc, Mc, DM, ssqM, &unreached))) return rc;
-      if (unreached) return phde_fail(ctx, PHDE_ERR_DISCONNECTED, "distance passes: the graph is not connected");
-      std::vector<int32_t> sub;
-      if ((rc = phde_cand_submatrix(ctx, DM, dc, Mc, sub))) return rc;
-      // farthest-point order on the exact candidate distances: start from the best-scored candidate,
-      // then repeatedly the candidate farthest from those chosen (best score first on ties)
-      const int Pl = std::min(P, Mc);
-      std::vector<int> order;
+      uint16_t *R;
+      int RW;
+      if ((rc = phde_msbfs_record(ctx, dc, Mc, &R, &RW))) return rc;
+      std::vector<int32_t> sub, csub;
+      if ((rc = phde_cand_distances(ctx, D, P0, R, RW, dc, Mc, sub, csub))) return rc;
+      // farthest-point selection over the candidates: distance to the pivots chosen so far (warm start
+      // included), best score first on ties
+      const int Pl = std::min(P, P0 + Mc);
       std::vector<int32_t> mind(Mc, INT32_MAX);
+      for (int i = 0; i < Mc; i++)
+        for (int j = 0; j < P0; j++) mind[i] = std::min(mind[i], sub[(size_t)i * P0 + j]);
       std::vector<char> used(Mc, 0);
-      int next = 0;
-      for (int p = 0; p < Pl; p++) {
-        order.push_back(next);
-        used[next] = 1;
+      std::vector<int> order;
+      for (int p = P0; p < Pl; p++) {
         int best = -1;
-        for (int i = 0; i < Mc; i++) {
-          mind[i] = std::min(mind[i], sub[(size_t)i * Mc + next]);
+        for (int i = 0; i < Mc; i++)
           if (!used[i] && (best < 0 || mind[i] > mind[best])) best = i;
-        }
-        next = best < 0 ? 0 : best;
+        if (best < 0) break;
+        used[best] = 1;
+        order.push_back(best);
+        for (int i = 0; i < Mc; i++) mind[i] = std::min(mind[i], csub[(size_t)i * Mc + best]);
       }
-      std::vector<ull> hs(Mc), hs2(Pl);
-      std::vector<int64_t> srcs(Pl);
-      PHDE_CK(ctx, cudaMemcpyAsync(hs.data(), ssqM, sizeof(ull) * Mc, cudaMemcpyDeviceToHost, ctx->stream));
-      PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-      for (int p = 0; p < Pl; p++) {
-        PHDE_CK(ctx, cudaMemcpyAsync(D + (int64_t)p * n, DM + (int64_t)order[p] * n, sizeof(int32_t) * n,
-                                     cudaMemcpyDeviceToDevice, ctx->stream));
-        hs2[p] = hs[order[p]];
-        srcs[p] = cand[order[p]];
-      }
-      PHDE_CK(ctx, cudaMemcpyAsync(sumsq, hs2.data(), sizeof(ull) * Pl, cudaMemcpyHostToDevice, ctx->stream));
-      PHDE_CK(ctx, cudaMemcpyAsync(d_src, srcs.data(), sizeof(int64_t) * Pl, cudaMemcpyHostToDevice, ctx->stream));
-      P_used = Pl;
+      const int Pn = (int)order.size();
+      int unreached = 0;
+      if ((rc = phde_record_columns(ctx, R, RW, order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0, &unreached)))
+        return rc;
+      if (unreached) return phde_fail(ctx, PHDE_ERR_DISCONNECTED, "distance passes: the graph is not connected");
+      std::vector<int64_t> srcs(Pn);
+      for (int p = 0; p < Pn; p++) srcs[p] = cand[order[p]];
+      if (Pn > 0)
+        PHDE_CK(ctx, cudaMemcpyAsync(d_src + P0, srcs.data(), sizeof(int64_t) * Pn, cudaMemcpyHostToDevice, ctx->stream));
+      P_used = P0 + Pn;
     } else if (random) {
       std::vector<int32_t> r;
       glibc_rand_host((uint32_t)o->seed, P, r);

@@ -87,6 +87,13 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
 // sources per sweep.  With sumsq: exact per-column sums of squares and *h_unreached (synchronises).
 int phde_msbfs(phde_ctx *ctx, const int64_t *d_src, int nsrc, int32_t *D, unsigned long long *sumsq,
                int *h_unreached);
+// The same search, leaving the row-major uint16 record (level + 1, 0 = unreached; RW = nsrc rounded up to
+// 64) in the context, and a gather of chosen columns of it into int32 column-major D.
+int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **R_out, int *RW_out);
+int phde_heavy_chunks(phde_ctx *ctx, const int64_t **chunk_row, const int64_t **chunk_e0, int64_t *nchunks,
+                      int64_t *chunk);
+int phde_record_columns(phde_ctx *ctx, const uint16_t *R, int RW, const int *h_cols, int ncols, int32_t *D,
+                        unsigned long long *sumsq, int *h_unreached);
 
 // ---- kernels (sssp.cu) ----
 // One exact SSSP pass from *d_src into d_col (int32, INF = INT32_MAX/2 for unreachable).

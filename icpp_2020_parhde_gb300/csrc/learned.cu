@@ -9,8 +9,10 @@
 //     f3 = |{u in N(v): d0(u) > d0(v)}| / deg v   (share of neighbours farther from the seed)
 //   score = MLP(f): 4 -> 64 -> 64 -> 1, ReLU, FP32 (weights trained on Kcenters pivot sets,
 //           icpp_2020_parhde_gb300/train_pivot_mlp.py, compiled in from pivot_mlp_weights.h)
-// The host then takes the M best-scored vertices, runs ONE multi-source BFS from all of them, and
-// orders P pivots among them by farthest-point selection on their exact pairwise distances.
+// The first LP_WARM pivots are exact Kcenters passes (the farthest-first rule of ParHDE.cpp:118-157;
+// the first column also gives the seed distances above).  The host takes the M best-scored vertices as
+// candidates, runs ONE multi-source BFS from all of them, and picks the remaining pivots among them by
+// farthest-point selection on exact distances, seeded with the warm-start pivots.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -23,26 +25,70 @@ namespace {
 constexpr int MLP_IN = 4, MLP_H = 64;
 constexpr int MLP_WEIGHTS = MLP_H * MLP_IN + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1;
 
-// deg, neighbour-degree sum, outward-neighbour count; maxima of deg, hop2 and d0
+// neighbour-degree sum and outward-neighbour count.  Rows up to FEAT_HEAVY neighbours: a group of 8 lanes
+// per vertex; heavier rows (R-MAT hubs): one warp per chunk of the multi-source BFS plan, integer
+// atomicAdd (exact, order-free).  hop2/outw are zeroed before the launch.
+constexpr int64_t FEAT_HEAVY = 256;
 __global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, const int32_t *d0, int64_t n,
-                                   ull *hop2, uint32_t *outw, ull *maxes) {
-  __shared__ ull red[32];
-  ull mdeg = 0, mhop = 0, md0 = 0;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e0 = off[v], e1 = off[v + 1];
+                                   const int64_t *chunk_row, const int64_t *chunk_e0, int64_t nchunks, int64_t chunk,
+                                   ull *hop2, uint32_t *outw) {
+  const int lane = threadIdx.x & 31, gl = lane & 7;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
+  const int64_t gstr = gts / 8, wfirst = (gt >> 5) * 4;
+  for (int64_t i0 = wfirst; i0 < n; i0 += gstr) {
+    const int64_t v = i0 + (lane >> 3);
+    ull h = 0;
+    unsigned o = 0;
+    bool act = v < n;
+    if (act) {
+      const int64_t e0 = off[v], e1 = off[v + 1];
+      if (e1 - e0 > FEAT_HEAVY) {
+        act = false;
+      } else {
+        const int32_t dv = d0[v];
+        for (int64_t e = e0 + gl; e < e1; e += 8) {
+          const int64_t u = __ldg(adj + e);
+          h += (ull)(off[u + 1] - off[u]);
+          o += d0[u] > dv ? 1u : 0u;
+        }
+      }
+    }
+    for (int s = 4; s > 0; s >>= 1) {
+      h += __shfl_xor_sync(PHDE_FULL_MASK, h, s, 8);
+      o += __shfl_xor_sync(PHDE_FULL_MASK, o, s, 8);
+    }
+    if (act && gl == 0) {
+      hop2[v] = h;
+      outw[v] = o;
+    }
+  }
+  const int64_t gw = gt >> 5, gws = gts >> 5;
+  for (int64_t c = gw; c < nchunks; c += gws) {
+    const int64_t v = chunk_row[c], e0 = chunk_e0[c], e1 = min(off[v + 1], e0 + chunk);
     const int32_t dv = d0[v];
     ull h = 0;
-    uint32_t o = 0;
-    for (int64_t e = e0; e < e1; e++) {
+    unsigned o = 0;
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
       const int64_t u = __ldg(adj + e);
       h += (ull)(off[u + 1] - off[u]);
       o += d0[u] > dv ? 1u : 0u;
     }
-    hop2[v] = h;
-    outw[v] = o;
-    mdeg = max(mdeg, (ull)(e1 - e0));
-    mhop = max(mhop, h);
-    md0 = max(md0, (ull)(dv < 0 ? 0 : dv));
+    h = warp_sum(h);
+    o = warp_sum(o);
+    if (lane == 0) {
+      atomicAdd(hop2 + v, h);
+      atomicAdd(outw + v, o);
+    }
+  }
+}
+
+__global__ void feature_max_kernel(const int64_t *off, const int32_t *d0, const ull *hop2, int64_t n, ull *maxes) {
+  __shared__ ull red[32];
+  ull mdeg = 0, mhop = 0, md0 = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    mdeg = max(mdeg, (ull)(off[v + 1] - off[v]));
+    mhop = max(mhop, hop2[v]);
+    md0 = max(md0, (ull)(d0[v] < 0 ? 0 : d0[v]));
   }
   mdeg = block_max_u64(mdeg, red);
   mhop = block_max_u64(mhop, red);
@@ -116,11 +162,16 @@ __global__ void collect_kernel(const float *score, int64_t n, int bmin, int nbin
   }
 }
 
-// M x M distances between the candidates: sub[i*M + j] = d(cand_i, cand_j) from candidate j's column
-__global__ void cand_submatrix_kernel(const int32_t *D, int64_t n, const int64_t *cand, int M, int32_t *sub) {
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < M * M; idx += gridDim.x * blockDim.x) {
-    const int i = idx / M, j = idx % M;
-    sub[idx] = D[(int64_t)j * n + cand[i]];
+// Distances of every candidate to the warm-start pivots: sub[i*P0 + j] = D[j*n + cand_i]; and to the other
+// candidates from the row-major record: csub[i*M + j] = R[cand_i*RW + j] - 1.
+__global__ void cand_distances_kernel(const int32_t *D, int P0, const uint16_t *R, int RW, int64_t n,
+                                      const int64_t *cand, int M, int32_t *sub, int32_t *csub) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < M * (M + P0); idx += gridDim.x * blockDim.x) {
+    const int i = idx / (M + P0), j = idx % (M + P0);
+    if (j < P0)
+      sub[i * P0 + j] = D[(int64_t)j * n + cand[i]];
+    else
+      csub[i * M + (j - P0)] = (int32_t)R[cand[i] * RW + (j - P0)] - 1;
   }
 }
 
@@ -133,9 +184,9 @@ int phde_default_pivot_model(const float **w, int *count) {
 }
 
 // Score every vertex and return the M best candidates (score descending, index ascending on ties) in
-// h_cand; writes d0 (hop distance from vertex 0) into d_d0.  Synchronises.
-int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, int32_t *d_d0, std::vector<int64_t> &h_cand,
-                          std::vector<float> &h_score) {
+// h_cand; d_d0 holds the hop distances from vertex 0.  Synchronises.
+int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const int32_t *d_d0,
+                          std::vector<int64_t> &h_cand, std::vector<float> &h_score) {
   const int64_t n = ctx->n;
   const int nbins = 4096;
   ull *hop2 = (ull *)phde_buf(ctx, "lp.hop2", sizeof(ull) * n);
@@ -148,20 +199,20 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, int32_t 
   int64_t *cand = (int64_t *)phde_buf(ctx, "lp.cand", sizeof(int64_t) * cap);
   float *cscore = (float *)phde_buf(ctx, "lp.cscore", sizeof(float) * cap);
   unsigned *count = (unsigned *)phde_buf(ctx, "lp.count", sizeof(unsigned));
-  int64_t *src0 = (int64_t *)phde_buf(ctx, "lp.src0", sizeof(int64_t) * 2);
-  ull *ssq = (ull *)phde_buf(ctx, "lp.ssq", sizeof(ull));
-  if (!hop2 || !outw || !maxes || !score || !hist || !wts || !cand || !cscore || !count || !src0 || !ssq)
-    return PHDE_ERR_OOM;
-  // d0: one BFS from vertex 0
-  PHDE_CK(ctx, cudaMemsetAsync(src0, 0, sizeof(int64_t) * 2, ctx->stream));
-  int rc = phde_run_bfs_passes(ctx, 1, 1, src0, d_d0, src0 + 1, ssq, nullptr, 1);
-  if (rc) return rc;
-  if ((rc = phde_check_device_err(ctx, "learned pivots: seed BFS"))) return rc;
+  if (!hop2 || !outw || !maxes || !score || !hist || !wts || !cand || !cscore || !count) return PHDE_ERR_OOM;
   PHDE_CK(ctx, cudaMemsetAsync(maxes, 0, sizeof(ull) * 3, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(hist, 0, sizeof(unsigned) * nbins, ctx->stream));
   PHDE_CK(ctx, cudaMemcpyAsync(wts, h_weights, sizeof(float) * MLP_WEIGHTS, cudaMemcpyHostToDevice, ctx->stream));
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->nsm * 8));
-  feature_raw_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, d_d0, n, hop2, outw, maxes);
+  const int64_t *crow, *ce0;
+  int64_t nch, chunk;
+  int rc = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
+  if (rc) return rc;
+  PHDE_CK(ctx, cudaMemsetAsync(hop2, 0, sizeof(ull) * n, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(outw, 0, sizeof(uint32_t) * n, ctx->stream));
+  feature_raw_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, d_d0, n, crow, ce0, nch, chunk, hop2, outw);
+  PHDE_LAUNCHED(ctx);
+  feature_max_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, n, maxes);
   PHDE_LAUNCHED(ctx);
   mlp_score_kernel<<<g, 256, sizeof(unsigned) * nbins, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts,
                                                                       score, hist, nbins);
@@ -201,13 +252,19 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, int32_t 
   return PHDE_OK;
 }
 
-int phde_cand_submatrix(phde_ctx *ctx, const int32_t *D, const int64_t *d_cand, int M, std::vector<int32_t> &h_sub) {
-  int32_t *sub = (int32_t *)phde_buf(ctx, "lp.sub", sizeof(int32_t) * M * M);
-  if (!sub) return PHDE_ERR_OOM;
-  cand_submatrix_kernel<<<(M * M + 255) / 256, 256, 0, ctx->stream>>>(D, ctx->n, d_cand, M, sub);
+int phde_cand_distances(phde_ctx *ctx, const int32_t *D, int P0, const uint16_t *R, int RW, const int64_t *d_cand,
+                        int M, std::vector<int32_t> &h_sub, std::vector<int32_t> &h_csub) {
+  int32_t *sub = (int32_t *)phde_buf(ctx, "lp.sub", sizeof(int32_t) * (size_t)M * std::max(P0, 1));
+  int32_t *csub = (int32_t *)phde_buf(ctx, "lp.csub", sizeof(int32_t) * (size_t)M * M);
+  if (!sub || !csub) return PHDE_ERR_OOM;
+  const int total = M * (M + P0);
+  cand_distances_kernel<<<(total + 255) / 256, 256, 0, ctx->stream>>>(D, P0, R, RW, ctx->n, d_cand, M, sub, csub);
   PHDE_LAUNCHED(ctx);
-  h_sub.resize((size_t)M * M);
-  PHDE_CK(ctx, cudaMemcpyAsync(h_sub.data(), sub, sizeof(int32_t) * M * M, cudaMemcpyDeviceToHost, ctx->stream));
+  h_sub.resize((size_t)M * P0);
+  h_csub.resize((size_t)M * M);
+  if (P0 > 0)
+    PHDE_CK(ctx, cudaMemcpyAsync(h_sub.data(), sub, sizeof(int32_t) * M * P0, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaMemcpyAsync(h_csub.data(), csub, sizeof(int32_t) * M * M, cudaMemcpyDeviceToHost, ctx->stream));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return PHDE_OK;
 }
