@@ -29,6 +29,8 @@ int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, d
 int phde_gram_seq(phde_ctx *ctx, const double *C, int k, double *M);
 int phde_cgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, float *S, int k,
                     int *h_state, double *h_dlog);
+int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, float *S, int k,
+                     int *h_state, double *h_dlog);
 int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float *LS, int k);
 int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double *M);
 int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X);
@@ -195,6 +197,7 @@ int phde_create(phde_ctx **out, int device) {
   for (auto &e : c->ev) cudaEventCreate(&e);
   for (auto &e : c->kev) cudaEventCreate(&e);
   if (const char *t = getenv("PHDE_WAIT_LIMIT_MS")) c->timeout_ns = (uint64_t)atoll(t) * 1000000ull;
+  if (const char *t = getenv("PHDE_CGS2")) c->column_cgs2 = std::string(t) == "column";
   *out = c;
   return PHDE_OK;
 }
@@ -371,7 +374,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     if (!D) return PHDE_ERR_OOM;
     if (o->strategy == PHDE_STRAT_LEARNED) {
       // ---- learned pivots: Kcenters warm start, MLP candidates, one multi-source BFS, farthest-point ----
-      const int P0 = std::min(P, 8);  // exact Kcenters passes (serial, few)
+      const int P0 = std::min(P, PHDE_LEARNED_WARM);  // exact Kcenters passes (serial, few)
       const int M = (int)std::min<int64_t>(PHDE_LEARNED_CANDIDATES, n);
       int64_t *dc = (int64_t *)phde_buf(ctx, "lp.dcand", sizeof(int64_t) * M);
       if (!dc) return PHDE_ERR_OOM;
@@ -385,7 +388,10 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       if ((rc = phde_check_device_err(ctx, "learned pivots: warm start"))) return rc;
       std::vector<int64_t> cand, warm(P0);
       std::vector<float> cscore;
-      if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), M, D, cand, cscore))) return rc;
+      // the candidates are scored on the warm start's running minimum distance (Kcenters' own criterion)
+      const int32_t *mind0 = (const int32_t *)phde_buf(ctx, "kc.min_d", sizeof(int32_t) * n);
+      if (!mind0) return PHDE_ERR_OOM;
+      if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), M, mind0, cand, cscore))) return rc;
       const int Mc = (int)cand.size();
       PHDE_CK(ctx, cudaMemcpyAsync(dc, cand.data(), sizeof(int64_t) * Mc, cudaMemcpyHostToDevice, ctx->stream));
       uint16_t *R;
@@ -442,7 +448,9 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     if (hde) {
       int state[4] = {0, 0, 0, 0};
       std::vector<double> dlog(P);
-      if (mixed)
+      if (mixed && !ctx->column_cgs2)
+        rc = phde_bcgs2_mixed(ctx, D, P_used, sumsq, deg, S32, k, state, dlog.data());
+      else if (mixed)
         rc = phde_cgs2_mixed(ctx, D, P_used, sumsq, deg, S32, k, state, dlog.data());
       else
         rc = phde_cgs(ctx, D, P_used, sumsq, deg, Sbuf, k, state, dlog.data());

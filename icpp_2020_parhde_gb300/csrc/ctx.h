@@ -17,6 +17,7 @@ struct phde_ctx {
   std::string err;
   long long launches = 0;
   uint64_t timeout_ns = 5000000000ull;  // bounded device waits: 5 s per wait
+  bool column_cgs2 = false;             // mixed path: column-at-a-time CGS2 (PHDE_CGS2=column) instead of blocked
 
   // uploaded graph (offsets widened to int64)
   int64_t n = 0, nnz = 0;

@@ -1,18 +1,19 @@
 // learned.cu -- learned pivot proposal: per-vertex features and the pivot-scoring MLP.
 //
 // Kcenters picks pivots one at a time (ParHDE.cpp:118-157): every pivot needs the BFS of the previous
-// one, so 3k dependent passes run back to back.  The learned strategy proposes candidates at once:
-//   features (one BFS from vertex 0, Kcenters' own first source):
+// one, so 3k dependent passes run back to back.  The learned strategy runs the first PHDE_LEARNED_WARM
+// pivots as exact Kcenters passes (the farthest-first rule of ParHDE.cpp:118-157), then proposes the
+// rest at once.  With d0(v) = the warm start's minimum distance from v to its pivots (Kcenters' own
+// selection key):
 //     f0 = log(1+deg v) / log(1+max deg)
 //     f1 = log(1+sum of neighbour degrees) / log(1+max of that sum)
-//     f2 = d0(v) / max d0                  (hop distance from vertex 0)
-//     f3 = |{u in N(v): d0(u) > d0(v)}| / deg v   (share of neighbours farther from the seed)
-//   score = MLP(f): 4 -> 64 -> 64 -> 1, ReLU, FP32 (weights trained on Kcenters pivot sets,
-//           icpp_2020_parhde_gb300/train_pivot_mlp.py, compiled in from pivot_mlp_weights.h)
-// The first LP_WARM pivots are exact Kcenters passes (the farthest-first rule of ParHDE.cpp:118-157;
-// the first column also gives the seed distances above).  The host takes the M best-scored vertices as
-// candidates, runs ONE multi-source BFS from all of them, and picks the remaining pivots among them by
-// farthest-point selection on exact distances, seeded with the warm-start pivots.
+//     f2 = d0(v) / max d0
+//     f3 = |{u in N(v): d0(u) > d0(v)}| / deg v   (share of neighbours farther from the pivots)
+//   score = MLP(f): 4 -> 64 -> 64 -> 1, ReLU, FP32 (weights trained on the pivots Kcenters picks after
+//           the warm start, icpp_2020_parhde_gb300/train_pivot_mlp.py, compiled in from pivot_mlp_weights.h)
+// The host takes the M best-scored vertices as candidates, runs ONE multi-source BFS from all of them,
+// and picks the remaining pivots among them by farthest-point selection on exact distances, seeded with
+// the warm-start pivots.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -184,7 +185,7 @@ int phde_default_pivot_model(const float **w, int *count) {
 }
 
 // Score every vertex and return the M best candidates (score descending, index ascending on ties) in
-// h_cand; d_d0 holds the hop distances from vertex 0.  Synchronises.
+// h_cand; d_d0 holds the warm start's minimum distance to its pivots.  Synchronises.
 int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const int32_t *d_d0,
                           std::vector<int64_t> &h_cand, std::vector<float> &h_score) {
   const int64_t n = ctx->n;

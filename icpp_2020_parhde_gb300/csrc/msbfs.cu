@@ -12,6 +12,8 @@
 // phde_distances -- so the reference's one-BFS-per-pivot loop (ParHDE.cpp:158-175,
 // DrawingBase.cpp:173-190) becomes one sweep per level.  Hop distances are unique: every column equals
 // the one-source BFS column bit for bit.
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "ctx.h"
@@ -28,8 +30,7 @@ struct MsArgs {
   const int64_t *off;
   const uint32_t *adj;
   int64_t n;
-  int W;           // words per vertex
-  int nsrc;        // sources this sweep
+  int nsrc;        // sources this sweep (the word count W is the kernel's template argument)
   const int64_t *src;
   uint16_t *R;     // row-major n x RW distance record: R[v*RW + b] = level + 1 (0 = unreached)
   int RW;          // row width (all sources of all sweeps, a multiple of 64)
@@ -42,48 +43,105 @@ struct MsArgs {
   const int64_t *chunk_row;   // heavy-row chunks: row and first edge
   const int64_t *chunk_e0;
   int64_t nchunks;
-  unsigned *active;           // [3] new-bit flags: level L sets slot L%3 and clears slot (L+1)%3
+  unsigned *active;           // [3] vertices given new bits: level L adds to slot L%3 and clears slot (L+1)%3
   int *levels_out;
+  ull *trace;                 // optional [2*trace_cap]: per level end time (ns) and vertices given new bits
+  int trace_cap;
   GridSync *gs;
   int *err;
   uint64_t timeout_ns;
 };
 
-// 4-bit group -> 4 x 16-bit lanes of ones (the lanes whose source bit is set)
-__constant__ ull kNibbleLanes[16] = {
-    0x0000000000000000ull, 0x000000000000ffffull, 0x00000000ffff0000ull, 0x00000000ffffffffull,
-    0x0000ffff00000000ull, 0x0000ffff0000ffffull, 0x0000ffffffff0000ull, 0x0000ffffffffffffull,
-    0xffff000000000000ull, 0xffff00000000ffffull, 0xffff0000ffff0000ull, 0xffff0000ffffffffull,
-    0xffffffff00000000ull, 0xffffffff0000ffffull, 0xffffffffffff0000ull, 0xffffffffffffffffull};
-
-__device__ __forceinline__ void ms_finalise(const MsArgs &a, int64_t v, const ull *acc, ull *fnext, int32_t L,
-                                            bool &any) {
-  const ull lvl = 0x0001000100010001ull * (ull)(uint16_t)(L + 2);  // level L+1, stored +1
-  for (int w = 0; w < a.W; w++) {
-    const ull s = a.seen[v * a.W + w];
-    const ull nw = acc[w] & ~s;
-    fnext[v * a.W + w] = nw;
-    if (nw) {
-      any = true;
-      a.seen[v * a.W + w] = s | nw;
-      ull *row = (ull *)(a.R + v * a.RW + a.col0 + 64 * w);  // 16 groups of 4 sources, 8 bytes each
-      for (int gi = 0; gi < 16; gi++) {
-        const unsigned nib = (unsigned)(nw >> (4 * gi)) & 15u;
-        if (nib) row[gi] |= kNibbleLanes[nib] & lvl;
-      }
-    }
+// Frontier words of one vertex through the L2 (other blocks wrote them during the previous level).
+template <int W>
+__device__ __forceinline__ void ld_words(const ull *p, ull (&x)[W]) {
+  if constexpr (W == 4) {
+    const uint4 a = __ldcg((const uint4 *)p), b = __ldcg((const uint4 *)(p + 2));
+    x[0] = ((ull)a.y << 32) | a.x;
+    x[1] = ((ull)a.w << 32) | a.z;
+    x[2] = ((ull)b.y << 32) | b.x;
+    x[3] = ((ull)b.w << 32) | b.z;
+  } else if constexpr (W == 2) {
+    const uint4 a = __ldcg((const uint4 *)p);
+    x[0] = ((ull)a.y << 32) | a.x;
+    x[1] = ((ull)a.w << 32) | a.z;
+  } else {
+#pragma unroll
+    for (int w = 0; w < W; w++) x[w] = __ldcg(p + w);
   }
 }
 
+// Record word for 4 sources: the 4 bits of `nib` select which of the four 16-bit lanes get value `val`.
+__device__ __forceinline__ ull nibble_lanes(unsigned nib, unsigned val) {
+  const ull e = (ull)(nib & 1u) | ((ull)(nib & 2u) << 15) | ((ull)(nib & 4u) << 30) | ((ull)(nib & 8u) << 45);
+  return e * (ull)val;  // the lanes do not overlap: no carries
+}
+
+// New bits of vertex v at level L (OR of its neighbours' frontier words `acc`, seen words `s`), finalised
+// by the MS_GROUP lanes of its group: lane gl writes record words gl, gl+8, ... (4 sources per word) and
+// seen/frontier word gl.  Returns whether any bit is new.
+template <int W>
+__device__ __forceinline__ bool ms_group_finalise(const MsArgs &a, int64_t v, const ull (&acc)[W], const ull (&s)[W],
+                                                  ull *fnext, int32_t L, int gl) {
+  const unsigned val = (unsigned)(L + 2);  // level L+1, stored +1
+  ull nw[W];
+  bool any = false;
+#pragma unroll
+  for (int w = 0; w < W; w++) {
+    nw[w] = acc[w] & ~s[w];
+    any |= nw[w] != 0ull;
+  }
+  ull *row = (ull *)(a.R + v * a.RW + a.col0);
+#pragma unroll
+  for (int i = 0; i < 2 * W; i++) {
+    const int gi = gl + 8 * (i & 1);
+    const unsigned nib = (unsigned)(nw[i >> 1] >> (4 * gi)) & 15u;
+    if (nib) atomicOr(row + gl + 8 * i, nibble_lanes(nib, val));  // result unused: a reduction in L2
+  }
+#pragma unroll
+  for (int w = 0; w < W; w++)
+    if (w == gl) {
+      fnext[v * W + w] = nw[w];
+      if (nw[w]) a.seen[v * W + w] = s[w] | nw[w];
+    }
+  return any;
+}
+
+// Same, one thread for the whole row (heavy rows: few).
+template <int W>
+__device__ __forceinline__ bool ms_thread_finalise(const MsArgs &a, int64_t v, const ull (&acc)[W], ull *fnext,
+                                                   int32_t L) {
+  const unsigned val = (unsigned)(L + 2);
+  bool any = false;
+  ull *row = (ull *)(a.R + v * a.RW + a.col0);
+#pragma unroll
+  for (int w = 0; w < W; w++) {
+    const ull s = a.seen[v * W + w];
+    const ull nw = acc[w] & ~s;
+    fnext[v * W + w] = nw;
+    if (nw) {
+      any = true;
+      a.seen[v * W + w] = s | nw;
+      for (int gi = 0; gi < 16; gi++) {
+        const unsigned nib = (unsigned)(nw >> (4 * gi)) & 15u;
+        if (nib) atomicOr(row + 16 * w + gi, nibble_lanes(nib, val));
+      }
+    }
+  }
+  return any;
+}
+
+template <int W>
 __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
+  __shared__ unsigned s_cnt;
   const int64_t n = a.n;
-  const int W = a.W;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
   const int64_t gw = gt >> 5, gws = gts >> 5;
   // full mask of the valid source bits per word
-  ull full[MS_MAXW];
-  for (int w = 0; w < MS_MAXW; w++) {
+  ull full[W];
+#pragma unroll
+  for (int w = 0; w < W; w++) {
     const int bits = a.nsrc - 64 * w;
     full[w] = bits >= 64 ? ~0ull : (bits <= 0 ? 0ull : ((1ull << bits) - 1ull));
   }
@@ -98,18 +156,23 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
   int32_t L = 0;
   for (;; L++) {
+    if (L > 65533) {  // the 16-bit record holds levels up to 65534; every block sees the same L
+      if (gt == 0) atomicCAS(a.err, 0, PHDE_ERR_TOO_LARGE);
+      return;
+    }
     const ull *fcur = a.front[L & 1];
     ull *fnext = a.front[(L + 1) & 1];
     // slot (L+1)%3 was last read after level L-2's final barrier, which every block has passed
     if (gt == 0) a.active[(L + 1) % 3] = 0u;
-    bool any = false;
-    // light rows: a group of MS_GROUP lanes per vertex, neighbours strided across the group.  A warp holds
-    // 32/MS_GROUP groups with consecutive ids; the loop runs over the warp's first group id so its trip
-    // count is warp-uniform and every lane reaches the group shuffles.
+    if (threadIdx.x == 0) s_cnt = 0u;
+    unsigned cnt = 0;
+    // light rows: a group of MS_GROUP lanes per vertex, neighbours strided across the group, two neighbour
+    // loads in flight per lane.  A warp holds 32/MS_GROUP groups with consecutive ids; the loop runs over
+    // the warp's first group id so its trip count is warp-uniform and every lane reaches the shuffles.
     {
       const int gl = lane & (MS_GROUP - 1);
-      const int64_t gstr = gts / MS_GROUP;                         // groups in the grid
-      const int64_t wfirst = (gt >> 5) * (32 / MS_GROUP);          // this warp's first group id
+      const int64_t gstr = gts / MS_GROUP;                 // groups in the grid
+      const int64_t wfirst = (gt >> 5) * (32 / MS_GROUP);  // this warp's first group id
       for (int64_t i0 = wfirst; i0 < n; i0 += gstr) {
         const int64_t v = i0 + (lane / MS_GROUP);
         bool act = v < n;
@@ -119,22 +182,41 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
           e1 = a.off[v + 1];
           if (e1 - e0 > MS_HEAVY) act = false;
         }
+        ull s[W];
         bool sat = true;
-        if (act)
-          for (int w = 0; w < W; w++) sat &= (a.seen[v * W + w] == full[w]);
-        ull acc[MS_MAXW] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+        for (int w = 0; w < W; w++) s[w] = 0ull;
+        if (act) {
+          ld_words<W>(a.seen + v * W, s);
+#pragma unroll
+          for (int w = 0; w < W; w++) sat &= (s[w] == full[w]);
+        }
+        ull acc[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) acc[w] = 0ull;
         if (act && !sat)
-          for (int64_t e = e0 + gl; e < e1; e += MS_GROUP) {
-            const int64_t u = __ldg(a.adj + e);
-            for (int w = 0; w < W; w++) acc[w] |= __ldcg(fcur + u * W + w);
+          for (int64_t e = e0 + gl; e < e1; e += 2 * MS_GROUP) {
+            const int64_t e2 = e + MS_GROUP;
+            const uint32_t u0 = __ldg(a.adj + e);
+            const uint32_t u1 = e2 < e1 ? __ldg(a.adj + e2) : u0;
+            ull x0[W], x1[W];
+            ld_words<W>(fcur + (int64_t)u0 * W, x0);
+            ld_words<W>(fcur + (int64_t)u1 * W, x1);
+#pragma unroll
+            for (int w = 0; w < W; w++) acc[w] |= x0[w] | x1[w];
           }
-        for (int w = 0; w < MS_MAXW; w++)
+#pragma unroll
+        for (int w = 0; w < W; w++)
+#pragma unroll
           for (int o = MS_GROUP / 2; o > 0; o >>= 1) acc[w] |= __shfl_xor_sync(PHDE_FULL_MASK, acc[w], o, MS_GROUP);
-        if (act && gl == 0) {
+        // every lane of the group read `seen` above, before the shuffles; the writes come after them
+        if (act) {
           if (sat) {
-            for (int w = 0; w < W; w++) fnext[v * W + w] = 0ull;
-          } else {
-            ms_finalise(a, v, acc, fnext, L, any);
+#pragma unroll
+            for (int w = 0; w < W; w++)
+              if (w == gl) fnext[v * W + w] = 0ull;
+          } else if (ms_group_finalise<W>(a, v, acc, s, fnext, L, gl) && gl == 0) {
+            cnt++;
           }
         }
       }
@@ -142,13 +224,25 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
     // heavy-row chunks: one warp per chunk, OR-reduced, combined with atomicOr
     for (int64_t c = gw; c < a.nchunks; c += gws) {
       const int64_t v = a.chunk_row[c], e0 = a.chunk_e0[c], e1 = min(a.off[v + 1], e0 + MS_CHUNK);
-      ull acc[MS_MAXW] = {0ull, 0ull, 0ull, 0ull};
-      for (int64_t e = e0 + lane; e < e1; e += 32) {
-        const int64_t u = __ldg(a.adj + e);
-        for (int w = 0; w < W; w++) acc[w] |= __ldcg(fcur + u * W + w);
+      ull acc[W];
+      ld_words<W>(a.seen + v * W, acc);  // seen changes only in the finalisation after the barrier
+      bool sat = true;
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        sat &= acc[w] == full[w];
+        acc[w] = 0ull;
       }
+      if (sat) continue;  // the row's finalisation writes zero new bits either way
+      for (int64_t e = e0 + lane; e < e1; e += 32) {
+        ull x[W];
+        ld_words<W>(fcur + (int64_t)__ldg(a.adj + e) * W, x);
+#pragma unroll
+        for (int w = 0; w < W; w++) acc[w] |= x[w];
+      }
+#pragma unroll
       for (int w = 0; w < W; w++) {
         ull x = acc[w];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1) x |= __shfl_xor_sync(PHDE_FULL_MASK, x, o);
         if (lane == 0 && x) atomicOr(a.hacc + v * W + w, x);
       }
@@ -156,16 +250,25 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
     for (int64_t h = gt; h < a.nheavy; h += gts) {
       const int64_t v = a.heavy_rows[h];
-      ull acc[MS_MAXW] = {0ull, 0ull, 0ull, 0ull};
+      ull acc[W];
+#pragma unroll
       for (int w = 0; w < W; w++) {
         acc[w] = __ldcg(a.hacc + v * W + w);
         a.hacc[v * W + w] = 0ull;
       }
-      ms_finalise(a, v, acc, fnext, L, any);
+      if (ms_thread_finalise<W>(a, v, acc, fnext, L)) cnt++;
     }
-    if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(a.active + (L % 3), 1u);
+    cnt = warp_sum(cnt);
+    if (lane == 0 && cnt) atomicAdd(&s_cnt, cnt);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cnt) atomicAdd(a.active + (L % 3), s_cnt);
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-    if (__ldcg(a.active + (L % 3)) == 0u) break;
+    const unsigned tot = __ldcg(a.active + (L % 3));
+    if (a.trace && gt == 0 && L < a.trace_cap) {
+      a.trace[2 * L] = global_timer_ns();
+      a.trace[2 * L + 1] = tot;
+    }
+    if (tot == 0u) break;
   }
   if (gt == 0) *a.levels_out = L + 1;
 }
@@ -268,13 +371,21 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
   const int64_t *hrows = (const int64_t *)phde_buf(ctx, "ms.hrows", 0);
   PHDE_CK(ctx, cudaMemsetAsync(R, 0, sizeof(uint16_t) * (size_t)n * RW, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(hacc, 0, sizeof(ull) * n * Wmax, ctx->stream));
-  int per_sm = 0;
-  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msbfs_kernel, MS_THREADS, 0));
-  if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "msbfs kernel cannot be resident");
-  per_sm = std::min(per_sm, 4);
+  // optional per-level trace (PHDE_MSBFS_TRACE=<file>): end time and vertices given new bits per level
+  const char *trace_path = getenv("PHDE_MSBFS_TRACE");
+  const int trace_cap = 4096;
+  ull *trace = trace_path ? (ull *)phde_buf(ctx, "ms.trace", sizeof(ull) * 2 * trace_cap) : nullptr;
   for (int s0 = 0; s0 < nsrc; s0 += 64 * Wmax) {
     const int ns = std::min(nsrc - s0, 64 * Wmax);
     const int W = (ns + 63) / 64;
+    const void *fn = W == 1 ? (const void *)msbfs_kernel<1>
+                   : W == 2 ? (const void *)msbfs_kernel<2>
+                   : W == 3 ? (const void *)msbfs_kernel<3>
+                            : (const void *)msbfs_kernel<4>;
+    int per_sm = 0;
+    PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, MS_THREADS, 0));
+    if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "msbfs kernel cannot be resident");
+    per_sm = std::min(per_sm, 4);
     PHDE_CK(ctx, cudaMemsetAsync(seen, 0, sizeof(ull) * n * W, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(f0, 0, sizeof(ull) * n * W, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(active, 0, sizeof(unsigned) * 3, ctx->stream));
@@ -284,7 +395,6 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.off = ctx->d_off;
     a.adj = ctx->d_adj;
     a.n = n;
-    a.W = W;
     a.nsrc = ns;
     a.src = d_src + s0;
     a.R = R;
@@ -301,17 +411,32 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.nchunks = nch;
     a.active = active;
     a.levels_out = levels;
+    a.trace = trace;
+    a.trace_cap = trace_cap;
     a.gs = ctx->d_sync;
     a.err = ctx->d_err;
     a.timeout_ns = ctx->timeout_ns;
     void *args[] = {&a};
     cudaEventRecord(ctx->kev[0], ctx->stream);
-    PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)msbfs_kernel, dim3(ctx->nsm * per_sm), dim3(MS_THREADS),
-                                             args, 0, ctx->stream));
+    PHDE_CK(ctx, cudaLaunchCooperativeKernel(fn, dim3(ctx->nsm * per_sm), dim3(MS_THREADS), args, 0, ctx->stream));
     PHDE_LAUNCHED(ctx);
     cudaEventRecord(ctx->kev[1], ctx->stream);
     ctx->kev_pending = true;
     if ((rc = phde_check_device_err(ctx, "multi-source BFS"))) return rc;
+    if (trace) {
+      int nl = 0;
+      std::vector<ull> h(2 * trace_cap);
+      PHDE_CK(ctx, cudaMemcpyAsync(&nl, levels, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      PHDE_CK(ctx, cudaMemcpyAsync(h.data(), trace, sizeof(ull) * h.size(), cudaMemcpyDeviceToHost, ctx->stream));
+      PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+      if (FILE *f = fopen(trace_path, "a")) {
+        fprintf(f, "# sweep col0=%d W=%d levels=%d grid=%d\n", s0, W, nl, ctx->nsm * per_sm);
+        for (int l = 0; l < std::min(nl, trace_cap); l++)
+          fprintf(f, "%d,%llu,%llu\n", l, (unsigned long long)(l ? h[2 * l] - h[2 * l - 2] : 0ull),
+                  (unsigned long long)h[2 * l + 1]);
+        fclose(f);
+      }
+    }
   }
   *R_out = R;
   *RW_out = RW;

@@ -230,3 +230,21 @@ def with_random_weights(g: CSRGraph, seed: int = 1, wmin: int = 1, wmax: int = 2
     uk, inv = np.unique(key, return_inverse=True)
     wu = rng.integers(wmin, wmax + 1, size=uk.shape[0], dtype=np.int32)
     return CSRGraph(g.offsets, g.adj, wu[inv].astype(np.int32), g.name + f"_w{seed}")
+
+
+def relabel(g: CSRGraph, perm: np.ndarray) -> CSRGraph:
+    """The same graph with vertex v renamed perm[v] (rows and neighbour lists re-sorted).  Kcenters starts
+    at vertex 0 and breaks ties by the lowest index, so a relabelled copy shows how a layout depends on that
+    choice rather than on the graph."""
+    n = g.n
+    perm = np.asarray(perm, dtype=np.int64)
+    deg = np.diff(g.offsets.astype(np.int64))
+    src = perm[np.repeat(np.arange(n, dtype=np.int64), deg)]
+    dst = perm[g.adj.astype(np.int64)]
+    order = np.argsort(src * n + dst, kind="stable")
+    counts = np.bincount(src, minlength=n)
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=off[1:])
+    w = g.weights[order] if g.weights is not None else None
+    return CSRGraph(off.astype(np.uint32) if off[-1] < 2**32 else off, dst[order].astype(np.uint32), w,
+                    g.name + "_relabelled")

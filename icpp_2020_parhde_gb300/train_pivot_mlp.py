@@ -1,10 +1,11 @@
 """Train the pivot-scoring MLP of the learned pivot strategy (PHDE_STRAT_LEARNED).
 
-Training data: seeded R-MAT and random geometric (2-D and 3-D) graphs; on each, the first 3k pivots that
-Kcenters picks (k = 64, the reference's farthest-first rule, ParHDE.cpp:118-157, computed with the CPU
-oracle) are the positive vertices.  Features are the four the GPU kernel computes (csrc/learned.cu):
-log-degree, log of the neighbour-degree sum, hop distance from vertex 0, and the share of neighbours
-farther from vertex 0, each normalised per graph.  The 4 -> 64 -> 64 -> 1 ReLU network is trained with a
+Training data: seeded R-MAT and random geometric (2-D and 3-D) graphs.  On each, Kcenters (k = 64, the
+reference's farthest-first rule, ParHDE.cpp:118-157, computed with the CPU oracle) runs 3k passes; the
+first WARM passes are the warm start the layout runs exactly, and the pivots Kcenters picks after them are
+the positive vertices.  Features are the four the GPU kernel computes (csrc/learned.cu): log-degree, log of
+the neighbour-degree sum, the warm start's minimum distance to its pivots, and the share of neighbours
+with a larger minimum distance, each normalised per graph.  The 4 -> 64 -> 64 -> 1 ReLU network is trained with a
 class-weighted logistic loss under BF16 autocast; the FP32 weights are written to
 csrc/pivot_mlp_weights.h (compiled into the library) and a summary to pivot_mlp_train.json.
 
@@ -25,8 +26,11 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 
 
+WARM = 8  # PHDE_LEARNED_WARM in include/parhde.h
+
+
 def features(g, d0: np.ndarray) -> np.ndarray:
-    """The four per-vertex features of csrc/learned.cu (float32, shape (n, 4))."""
+    """The four per-vertex features of csrc/learned.cu (float32, shape (n, 4)); d0 = warm-start min distance."""
     off = g.offsets.astype(np.int64)
     adj = g.adj.astype(np.int64)
     n = g.n
@@ -75,10 +79,10 @@ def main(argv=None):
     X, Y, sizes = [], [], []
     t0 = time.time()
     for gi, g in enumerate(training_graphs(args.graphs, args.max_n, args.seed)):
-        d0 = orc.bfs(g, 0, parallel=True).astype(np.int64)
-        _, piv = orc.kcenters(g, min(P, g.n - 1), 0, parallel=True)
+        D, piv = orc.kcenters(g, min(P, g.n - 1), 0, parallel=True)
+        d0 = D[:, :WARM].min(axis=1).astype(np.int64)
         y = np.zeros(g.n, dtype=np.float32)
-        y[piv] = 1.0
+        y[piv[WARM:]] = 1.0
         X.append(features(g, d0))
         Y.append(y)
         sizes.append((g.name, g.n, g.nnz))
@@ -132,6 +136,7 @@ def main(argv=None):
             f.write("    " + ", ".join("%.9ef" % v for v in flat[i:i + 8]) + ",\n")
         f.write("};\n")
     summary = {"graphs": len(sizes), "vertices": int(len(Y)), "positives": int(pos), "k": args.k, "P": P,
+               "warm": WARM,
                "epochs": args.epochs, "loss": history, "mean_kcenters_pivots_in_top256": float(np.mean(hits)),
                "max_n": args.max_n, "seed": args.seed, "train_seconds": time.time() - t0,
                "training_graphs": [f"{a} n={b} nnz={c}" for a, b, c in sizes]}

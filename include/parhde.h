@@ -54,6 +54,7 @@ extern "C" {
  * serial Kcenters passes (ParHDE only). */
 #define PHDE_STRAT_LEARNED 3
 #define PHDE_LEARNED_CANDIDATES 256
+#define PHDE_LEARNED_WARM 8 /* exact Kcenters passes before the learned candidates are scored */
 /* precision of the dense stages (distances are always exact integers) */
 #define PHDE_PREC_FP64 0  /* every dense stage in FP64, the reference's arithmetic            */
 #define PHDE_PREC_MIXED 1 /* FP32 storage/SpMM, compensated Gram products; FP64 k x k solves  */

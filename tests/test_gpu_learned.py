@@ -1,7 +1,11 @@
 """Learned pivots (PHDE_STRAT_LEARNED): MLP-proposed candidates, one multi-source BFS, farthest-point order.
-Acceptance criterion: the layout's Rayleigh quotient -- the sum over its coordinates of x'Lx / x'x, the
-energy the eigensolve minimises -- within 2% of the Kcenters layout's.  Single coordinates may trade places
-(a lower second axis for a higher third), so they are reported, not gated."""
+
+Acceptance criterion: the layout's Rayleigh quotients (x'Lx / x'x per coordinate, summed over the
+coordinates -- the energy the eigensolve minimises) within 2% of the Kcenters layout's, averaged over the
+graph and seven relabelled copies of it.  The average matters: Kcenters starts at vertex 0 and breaks ties
+by the lowest index, and on an R-MAT graph of 2^16 vertices with k = 20 its own summed quotient moves by up
+to 1.48x (single coordinates by up to 2.2x) between relabellings of the same graph, so one pair of runs says
+nothing at the 2% level."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -29,14 +33,19 @@ GRAPHS = {
 @pytest.mark.parametrize("name", sorted(GRAPHS))
 def test_learned_pivots_rayleigh_within_2_percent(gpu_ctx, name):
     g = GRAPHS[name]()
-    gpu_ctx.upload(g)
+    rng = np.random.default_rng(5)
     k, c = 20, 3
-    kc = gpu_ctx.layout("ParHDE", "Kcenters", k, c, eig="exact")
-    lp = gpu_ctx.layout("ParHDE", "Learned", k, c, eig="exact")
-    assert len(lp.sources) == 3 * k and len(set(lp.sources.tolist())) == 3 * k
-    assert lp.stats["naccepted"] == k
-    rq_kc, rq_lp = rayleigh(g, kc.coords), rayleigh(g, lp.coords)
-    assert rq_lp.sum() <= 1.02 * rq_kc.sum(), (rq_lp, rq_kc)
+    tot_kc, tot_lp = [], []
+    for t in range(8):
+        gg = g if t == 0 else graphs.relabel(g, rng.permutation(g.n))
+        gpu_ctx.upload(gg)
+        kc = gpu_ctx.layout("ParHDE", "Kcenters", k, c, eig="exact")
+        lp = gpu_ctx.layout("ParHDE", "Learned", k, c, eig="exact")
+        assert len(lp.sources) == 3 * k and len(set(lp.sources.tolist())) == 3 * k
+        assert lp.stats["naccepted"] == k
+        tot_kc.append(rayleigh(gg, kc.coords).sum())
+        tot_lp.append(rayleigh(gg, lp.coords).sum())
+    assert np.mean(tot_lp) <= 1.02 * np.mean(tot_kc), (tot_lp, tot_kc)
 
 
 def test_learned_pivot_columns_are_exact(gpu_ctx):

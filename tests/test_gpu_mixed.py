@@ -52,3 +52,36 @@ def test_mixed_rejected_for_other_algorithms(gpu_ctx):
     with pytest.raises(ParHDEError) as e:
         gpu_ctx.layout("PivotMDS", "Kcenters", 5, 2, precision="mixed")
     assert e.value.status == -1
+
+
+def test_blocked_cgs2_matches_column_cgs2(monkeypatch):
+    """The blocked CGS2 (32 candidates per block, coefficient-space accept/discard loop) against the
+    column-at-a-time CGS2: same accept/discard decisions, same layout to FP32 accuracy."""
+    from icpp_2020_parhde_gb300 import Context
+    g = graphs.rmat(15, seed=4)
+    k, c = 40, 3
+    cb = Context(0)
+    cb.upload(g)
+    rb = cb.layout("ParHDE", "Kcenters", k, c, precision="mixed", eig="exact")
+    monkeypatch.setenv("PHDE_CGS2", "column")
+    cc = Context(0)
+    cc.upload(g)
+    rc = cc.layout("ParHDE", "Kcenters", k, c, precision="mixed", eig="exact")
+    for key in ("naccepted", "ndiscarded"):
+        assert rb.stats[key] == rc.stats[key]
+    np.testing.assert_allclose(rayleigh(g, rb.coords), rayleigh(g, rc.coords), rtol=1e-4)
+    assert principal_cosines(rb.coords, rc.coords).min() > 1 - 1e-5
+
+
+def test_blocked_cgs2_discards_like_the_oracle(gpu_ctx):
+    """A path graph: the column of the far end is the near end's reversed (a combination of the constant and
+    the first column), so the reference discards it; the blocked loop must take the same decisions."""
+    g = graphs.path_graph(3000)
+    k, c = 10, 2
+    gpu_ctx.upload(g)
+    r = gpu_ctx.layout("ParHDE", "Kcenters", k, c, precision="mixed", eig="exact")
+    L = orc.layout(g, "ParHDE", "Kcenters", k, c, eig="exact", nthreads=4)
+    assert L.stats.ndiscarded > 0
+    assert r.stats["ndiscarded"] == L.stats.ndiscarded
+    assert r.stats["naccepted"] == L.stats.naccepted == k
+    np.testing.assert_allclose(rayleigh(g, r.coords), rayleigh(g, L.coords), rtol=1e-3)

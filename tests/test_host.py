@@ -101,3 +101,16 @@ def test_nxyz_writer_matches_reference_embed(tmp_path):
                    stdout=subprocess.DEVNULL)
     ref_text = open(p + "_hde.nxyz").read()
     assert csr_io.format_nxyz(rec["PivotMDS_k10_c2_coords"]) == ref_text
+
+
+def test_relabel_is_isomorphic():
+    g = graphs.rmat(10, seed=3)
+    perm = np.random.default_rng(1).permutation(g.n)
+    h = graphs.relabel(g, perm)
+    assert h.n == g.n and h.nnz == g.nnz
+    deg_g = np.diff(g.offsets.astype(np.int64))
+    deg_h = np.diff(h.offsets.astype(np.int64))
+    assert np.array_equal(deg_h[perm], deg_g)
+    for v in (0, 5, g.n - 1):
+        nb = np.sort(perm[g.adj[g.offsets[v]:g.offsets[v + 1]].astype(np.int64)])
+        assert np.array_equal(h.adj[h.offsets[perm[v]]:h.offsets[perm[v] + 1]].astype(np.int64), nb)
