@@ -50,8 +50,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=3)
-    ap.add_argument("--no-mixed", action="store_true")
-    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the two Kcenters control pipelines")
+    ap.add_argument("--no-accept", action="store_true", help="skip the learned-pivot acceptance check")
+    ap.add_argument("--relabellings", type=int, default=4)
     return ap.parse_args()
 
 
@@ -211,11 +212,26 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+PIPELINES = {
+    # the GB300 pipeline: learned pivots (one multi-source BFS), FP32 n-sized stages with FP64 sums, blocked
+    # CGS2, FP64 k x k Jacobi eigensolve
+    "learned_mixed": dict(strategy="Learned", precision="mixed", eig="exact"),
+    # the reference pipeline on the GPU: Kcenters (3k serial BFS passes), FP64 throughout, power iteration
+    "plain": dict(strategy="Kcenters", precision="fp64", eig="power"),
+    # isolates the pivot choice (same precision and eigensolver as the headline)
+    "kcenters_mixed": dict(strategy="Kcenters", precision="mixed", eig="exact"),
+    # isolates the precision (same pivots and eigensolver as kcenters_mixed)
+    "kcenters_fp64_exact": dict(strategy="Kcenters", precision="fp64", eig="exact"),
+}
+PHASES = ("ms_dist", "ms_orth", "ms_mmult", "ms_eig", "ms_coords", "ms_total")
+
+
 def run_gb300(args):
     ws, rank, local = dist_init()
     import torch
     torch.cuda.set_device(local)
-    from icpp_2020_parhde_gb300 import Context, _lib
+    from icpp_2020_parhde_gb300 import Context, graphs
+    from icpp_2020_parhde_gb300.csr_io import CSRGraph
     g, gen_s = make_graph(args)
     ctx = Context(local)
     n, nnz, k, c = g.n, g.nnz, args.k, args.c
@@ -223,7 +239,6 @@ def run_gb300(args):
     off_h = torch.from_numpy(g.offsets.astype(np.uint32)).pin_memory()
     adj_h = torch.from_numpy(g.adj.astype(np.uint32)).pin_memory()
     xy_h = torch.empty(n * c, dtype=torch.float64).pin_memory()
-    from icpp_2020_parhde_gb300.csr_io import CSRGraph
     gp = CSRGraph(off_h.numpy(), adj_h.numpy(), None)
     ctx.upload(gp)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
@@ -232,132 +247,145 @@ def run_gb300(args):
         flush.fill_(1.0)
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        ctx.layout("ParHDE", "Kcenters", k, c, coords_out=xy_h.numpy())
-    # ---- device-resident timed region ----
-    flush_l2()
-    barrier(ws)
-    torch.cuda.synchronize()
-    stats = []
-    launches0 = ctx.launch_count
-    with ClockSampler(local) as clk:
+    def run(name):
+        return ctx.layout("ParHDE", k=k, c=c, coords_out=xy_h.numpy(), **PIPELINES[name])
+
+    def coords():
+        return xy_h.numpy().reshape(c, n).T.copy()
+
+    def timed(name, steps, sampler=None):
+        for _ in range(args.warmup):
+            run(name)
+        flush_l2()
+        barrier(ws)
+        torch.cuda.synchronize()
+        stats = []
+        l0 = ctx.launch_count
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush_l2()
-            r = ctx.layout("ParHDE", "Kcenters", k, c, coords_out=xy_h.numpy())
-            stats.append(r.stats)
+            stats.append(run(name).stats)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-    barrier(ws)
-    launches = ctx.launch_count - launches0
-    ms_steps = [s["ms_total"] for s in stats]
-    ms_mean = float(np.mean(ms_steps))
-    ms_max = allmax(ws, ms_mean)
-    value = ws * k * nnz / (ms_max * 1e-3)
-    # ---- end to end through the C ABI with host buffers ----
+        barrier(ws)
+        ms = allmax(ws, float(np.mean([s["ms_total"] for s in stats])))
+        return {"ms": ms, "stats": stats, "launches": ctx.launch_count - l0, "wall": wall,
+                "phases_ms": {p: float(np.mean([s[p] for s in stats])) for p in PHASES}}
+
+    # ---- headline: device-resident timed region, clocks sampled ----
+    with ClockSampler(local) as clk:
+        head = timed("learned_mixed", args.steps)
+    xy_head = coords()
+    # ---- end to end through the C ABI: pinned host CSR -> phde_graph_upload -> phde_layout -> host coords ----
     e2e_t = []
-    for i in range(args.steps):
+    for _ in range(args.steps):
         flush_l2()
         barrier(ws)
         t1 = time.perf_counter()
         ctx.upload(gp)
-        r = ctx.layout("ParHDE", "Kcenters", k, c, coords_out=xy_h.numpy())
+        run("learned_mixed")
         e2e_t.append(time.perf_counter() - t1)
     e2e_s = allmax(ws, float(np.mean(e2e_t)))
     h2d = 4 * (n + 1) + 4 * nnz
     d2h = 8 * n * c + 8 * 3 * k
-    # ---- roofline of the dominant kernel: the persistent Kcenters BFS (3k passes per launch) ----
-    P = 3 * k
-    bytes_per_pass = 8 * (n + 1) + 4 * nnz + 4 * n + 12 * n  # CSR read once, column write, Kcenters fold
-    kern_ms = float(np.mean([s["ms_dist_kernel"] for s in stats]))
-    achieved = P * bytes_per_pass / (kern_ms * 1e-3) / 1e9
+    # ---- the reference pipeline on the GPU, and the two controls ----
+    plain = timed("plain", args.steps)
+    rq_plain = rayleigh_quotients(g, coords())
+    ctl = {}
+    if not args.no_extra:
+        for name in ("kcenters_mixed", "kcenters_fp64_exact"):
+            ctl[name] = timed(name, max(1, args.steps // 2))
+            ctl[name]["rq"] = rayleigh_quotients(g, coords())
+    rq_head = rayleigh_quotients(g, xy_head)
+    # ---- acceptance of the learned pivots: summed Rayleigh quotient vs Kcenters (same precision and
+    #      eigensolver), averaged over the graph and relabelled copies (Kcenters starts at vertex 0 and breaks
+    #      ties by the lowest index; its own quotient moves by tens of percent between relabellings) ----
+    acc = {"relabellings": [], "criterion": "mean summed RQ(learned) <= 1.02 * mean summed RQ(Kcenters)"}
+    if not args.no_accept:
+        rng = np.random.default_rng(11)
+        tot_l, tot_k = [], []
+        for t in range(args.relabellings):
+            gg = g if t == 0 else graphs.relabel(g, rng.permutation(n))
+            ctx.upload(gg)
+            ctx.layout("ParHDE", k=k, c=c, coords_out=xy_h.numpy(), **PIPELINES["learned_mixed"])
+            ql = rayleigh_quotients(gg, coords())
+            ctx.layout("ParHDE", k=k, c=c, coords_out=xy_h.numpy(), **PIPELINES["kcenters_mixed"])
+            qk = rayleigh_quotients(gg, coords())
+            tot_l.append(float(ql.sum()))
+            tot_k.append(float(qk.sum()))
+            acc["relabellings"].append({"learned": ql.tolist(), "kcenters": qk.tolist()})
+        acc["ratio_of_means"] = float(np.mean(tot_l) / np.mean(tot_k))
+        acc["accepted"] = bool(acc["ratio_of_means"] <= 1.02)
+        ctx.upload(gp)
+    else:
+        acc["accepted"] = None
+    # learned pivots rejected -> plain Kcenters is the fallback, and the headline is its number
+    fallback = acc["accepted"] is False
+    hl = plain if fallback else head
+    value = ws * k * nnz / (hl["ms"] * 1e-3)
+    # ---- roofline of the headline's dominant kernel: the multi-source BFS sweep ----
     peak, peak_kind = peaks()
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "kcenters_bfs_rmat20_traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get("bytes_per_launch")
-        except Exception:
-            traffic = None
-    mixed = None
-    if not args.no_mixed:
-        # mixed precision (FP32 basis / CGS2 / SpMM, FP64 k x k solve): same workload, stated error vs FP64
-        xy64 = xy_h.numpy().reshape(c, n).T.copy()
-        ms_mixed = []
-        for _ in range(args.warmup):
-            ctx.layout("ParHDE", "Kcenters", k, c, precision="mixed", coords_out=xy_h.numpy())
-        for _ in range(args.steps):
-            flush_l2()
-            rm = ctx.layout("ParHDE", "Kcenters", k, c, precision="mixed", coords_out=xy_h.numpy())
-            ms_mixed.append(rm.stats["ms_total"])
-        xym = xy_h.numpy().reshape(c, n).T.copy()
-        rq64, rqm = rayleigh_quotients(g, xy64), rayleigh_quotients(g, xym)
-        msm = allmax(ws, float(np.mean(ms_mixed)))
-        mixed = {"value": ws * k * nnz / (msm * 1e-3), "unit": UNIT, "ms_per_graph": msm, "dtype": "f32+f64",
-                 "phases_ms": {kk: rm.stats[kk] for kk in ("ms_dist", "ms_orth", "ms_mmult", "ms_eig", "ms_coords")},
-                 "rayleigh_fp64": rq64.tolist(), "rayleigh_mixed": rqm.tolist(),
-                 "rayleigh_rel_err_max": float(np.max(np.abs(rqm - rq64) / np.abs(rq64))),
-                 "eig_iters": rm.stats["eig_iters"], "naccepted": rm.stats["naccepted"]}
-    learned = None
-    if not args.no_learned:
-        # learned pivots (one multi-source BFS instead of 3k serial passes), same workload and precision;
-        # accepted when the layout's Rayleigh quotient (sum over coordinates of x'Lx / x'x) is within 2% of
-        # the plain Kcenters layout's
-        xy64 = None
-        r64 = ctx.layout("ParHDE", "Kcenters", k, c, coords_out=xy_h.numpy())
-        xy64 = xy_h.numpy().reshape(c, n).T.copy()
-        for _ in range(args.warmup):
-            ctx.layout("ParHDE", "Learned", k, c, coords_out=xy_h.numpy())
-        ms_l = []
-        for _ in range(args.steps):
-            flush_l2()
-            rl = ctx.layout("ParHDE", "Learned", k, c, coords_out=xy_h.numpy())
-            ms_l.append(rl.stats["ms_total"])
-        xyl = xy_h.numpy().reshape(c, n).T.copy()
-        ms_lm = []
-        for _ in range(args.steps):
-            flush_l2()
-            rlm = ctx.layout("ParHDE", "Learned", k, c, precision="mixed", coords_out=xy_h.numpy())
-            ms_lm.append(rlm.stats["ms_total"])
-        xylm = xy_h.numpy().reshape(c, n).T.copy()
-        rq_p, rq_l, rq_lm = rayleigh_quotients(g, xy64), rayleigh_quotients(g, xyl), rayleigh_quotients(g, xylm)
-        msl, mslm = allmax(ws, float(np.mean(ms_l))), allmax(ws, float(np.mean(ms_lm)))
-        learned = {"value": ws * k * nnz / (msl * 1e-3), "unit": UNIT, "ms_per_graph": msl, "dtype": "f64",
-                   "speedup_vs_plain": ms_max / msl,
-                   "phases_ms": {kk: rl.stats[kk] for kk in ("ms_dist", "ms_orth", "ms_mmult", "ms_eig", "ms_coords")},
-                   "rayleigh_plain": rq_p.tolist(), "rayleigh_learned": rq_l.tolist(),
-                   "rayleigh_total_ratio": float(rq_l.sum() / rq_p.sum()),
-                   "accepted_within_2pct": bool(rq_l.sum() <= 1.02 * rq_p.sum()),
-                   "mixed": {"value": ws * k * nnz / (mslm * 1e-3), "ms_per_graph": mslm, "dtype": "f32+f64",
-                             "speedup_vs_plain": ms_max / mslm, "rayleigh": rq_lm.tolist(),
-                             "rayleigh_total_ratio": float(rq_lm.sum() / rq_p.sum()),
-                             "accepted_within_2pct": bool(rq_lm.sum() <= 1.02 * rq_p.sum())}}
+    roof = None
+    last = head["stats"][-1]
+    if not fallback and last.get("ms_msbfs_kernel", 0) > 0:
+        lv = last["msbfs_levels"]
+        per_level = 8 * (n + 1) + 4 * nnz + 2 * n * 32  # offsets + adjacency + frontier words in and out
+        bytes_launch = lv * per_level
+        kern_ms = float(np.mean([s["ms_msbfs_kernel"] for s in head["stats"]]))
+        achieved = bytes_launch / (kern_ms * 1e-3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "msbfs_rmat20_traffic.json")
+        if os.path.exists(tp):
+            try:
+                traffic = json.load(open(tp)).get("bytes_per_launch")
+            except Exception:
+                traffic = None
+        roof = {"kernel": "msbfs_kernel<4>", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": ("measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"),
+                "algorithmic_bytes_per_launch": bytes_launch, "levels": lv, "kernel_ms": kern_ms}
     if rank != 0:
         return
+
+    def summary(t, rq=None, ref_ms=None):
+        d = {"value": ws * k * nnz / (t["ms"] * 1e-3), "unit": UNIT, "ms_per_graph": t["ms"],
+             "phases_ms": t["phases_ms"], "gpu_launches_per_step": t["launches"] / max(1, len(t["stats"]))}
+        if rq is not None:
+            d["rayleigh"] = [float(x) for x in rq]
+        if ref_ms is not None:
+            d["speedup_vs_plain"] = ref_ms / t["ms"]
+        return d
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "ms_per_step": hl["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32 distances, f32 n-sized stages with f64 sums, f64 k x k" if not fallback else "f64",
         "data": "synthetic",
-        "config": {"workload": "ParHDE Kcenters layout, R-MAT scale %d ef16 (a=.57,b=.19,c=.19) LCC, k=%d, c=%d, FP64"
-                               % (args.rmat_scale, k, c),
+        "config": {"workload": "ParHDE layout of an R-MAT scale-%d graph (edgefactor 16, a=.57 b=.19 c=.19, "
+                               "symmetrised, LCC), k=%d pivots, %d coordinates" % (args.rmat_scale, k, c),
+                   "pipeline": "plain Kcenters fallback" if fallback else "learned pivots + mixed precision + exact eigensolve",
                    "n": n, "nnz": nnz, "k": k, "c": c, "parallelism": "replicas%d" % ws if ws > 1 else "single",
                    "l2": "flushed between timed steps (256 MB write)", "graph_gen_s": round(gen_s, 1)},
-        "ms_per_graph": ms_max,
-        "phases_ms": {kk: float(np.mean([s[kk] for s in stats])) for kk in
-                      ("ms_dist", "ms_orth", "ms_mmult", "ms_eig", "ms_coords", "ms_dist_kernel")},
-        "wall_s_timed_region": wall,
+        "ms_per_graph": hl["ms"],
+        "phases_ms": hl["phases_ms"],
+        "speedup_vs_plain": plain["ms"] / hl["ms"],
         "e2e": {"value": ws * k * nnz / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_graph": e2e_s * 1e3},
-        "gpu_launches": launches,
-        "roofline": {"kernel": "kcenters_bfs_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                     "algorithmic_bytes_per_launch": P * bytes_per_pass, "kernel_ms": kern_ms},
+                "ms_per_graph": e2e_s * 1e3, "path": "phde_graph_upload + phde_layout, pinned host buffers"},
+        "gpu_launches": hl["launches"],
+        "roofline": roof,
         "clocks": clk.summary(),
-        "stats_last": stats[-1],
-        "mixed_precision": mixed,
-        "learned_pivots": learned,
+        "headline_stats_last": hl["stats"][-1],
+        "learned_acceptance": acc,
+        "pipelines": {
+            "learned_mixed": summary(head, rq_head, plain["ms"]),
+            "plain": summary(plain, rq_plain),
+            **{kk: summary(v, v["rq"], plain["ms"]) for kk, v in ctl.items()},
+        },
     }
+    if "kcenters_mixed" in ctl and "kcenters_fp64_exact" in ctl:
+        a, b = ctl["kcenters_mixed"]["rq"], ctl["kcenters_fp64_exact"]["rq"]
+        line["mixed_precision_error"] = {"rayleigh_rel_err_max": float(np.max(np.abs(a - b) / np.abs(b))),
+                                         "vs": "Kcenters FP64 with the same pivots and eigensolver"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g, args, args.cpu_reps)
     print(json.dumps(line), flush=True)

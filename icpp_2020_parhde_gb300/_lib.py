@@ -40,7 +40,7 @@ class LayoutStats(C.Structure):
                 ("eig_iters", C.c_int), ("gpu_launches", C.c_int), ("ms_dist", C.c_double), ("ms_orth", C.c_double),
                 ("ms_mmult", C.c_double), ("ms_eig", C.c_double), ("ms_coords", C.c_double),
                 ("ms_total", C.c_double), ("edges_examined", C.c_int64), ("ms_dist_kernel", C.c_double),
-                ("dist_kernel_launches", C.c_int)]
+                ("dist_kernel_launches", C.c_int), ("ms_msbfs_kernel", C.c_double), ("msbfs_levels", C.c_int)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

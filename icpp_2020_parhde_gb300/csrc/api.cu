@@ -293,6 +293,8 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   const long long launches0 = ctx->launches;
   ctx->kernel_ms = 0;
   ctx->kernel_launches = 0;
+  ctx->msbfs_ms = 0;
+  ctx->msbfs_levels = 0;
   ctx->kev_pending = false;
   tm.mark(0);
   double *deg = (double *)phde_buf(ctx, "deg", sizeof(double) * n);
@@ -549,6 +551,8 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     st->gpu_launches = (int)(ctx->launches - launches0);
     st->ms_dist_kernel = ctx->kernel_ms;
     st->dist_kernel_launches = ctx->kernel_launches;
+    st->ms_msbfs_kernel = ctx->msbfs_ms;
+    st->msbfs_levels = ctx->msbfs_levels;
   }
   return PHDE_OK;
 }
@@ -594,15 +598,22 @@ int phde_distances(phde_ctx *ctx, const int64_t *sources, int nsrc, int32_t *out
   PHDE_CK(ctx, cudaMemcpyAsync(d_src, sources, sizeof(int64_t) * nsrc, cudaMemcpyHostToDevice, ctx->stream));
   int rc;
   if (!ctx->weighted) {
-    int32_t *D = (int32_t *)phde_buf(ctx, "dist.D", sizeof(int32_t) * n * nsrc);
+    // sources in groups of 256: one bitset sweep per level for each group (single BFS passes below 4)
+    const int G = std::min(nsrc, 256);
+    int32_t *D = (int32_t *)phde_buf(ctx, "dist.D", sizeof(int32_t) * n * G);
     if (!D) return PHDE_ERR_OOM;
-    if (nsrc >= 4)  // several sources: one bitset sweep per level for all of them
-      rc = phde_msbfs(ctx, d_src, nsrc, D, nullptr, nullptr);
-    else
-      rc = phde_run_bfs_passes(ctx, nsrc, 1, d_src, D, d_src2, sumsq, nullptr, 0);
-    if (rc) return rc;
-    PHDE_CK(ctx, cudaMemcpyAsync(out, D, sizeof(int32_t) * n * nsrc, cudaMemcpyDeviceToHost, ctx->stream));
-    return phde_check_device_err(ctx, "BFS");
+    for (int s0 = 0; s0 < nsrc; s0 += G) {
+      const int ns = std::min(G, nsrc - s0);
+      if (ns >= 4)
+        rc = phde_msbfs(ctx, d_src + s0, ns, D, nullptr, nullptr);
+      else
+        rc = phde_run_bfs_passes(ctx, ns, 1, d_src + s0, D, d_src2, sumsq, nullptr, 0);
+      if (rc) return rc;
+      PHDE_CK(ctx, cudaMemcpyAsync(out + (int64_t)s0 * n, D, sizeof(int32_t) * n * ns, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+      if ((rc = phde_check_device_err(ctx, "BFS"))) return rc;
+    }
+    return PHDE_OK;
   }
   int32_t *col = (int32_t *)phde_buf(ctx, "dist.col", sizeof(int32_t) * n);
   if (!col) return PHDE_ERR_OOM;

@@ -158,45 +158,80 @@ __global__ void __launch_bounds__(GT) bcgs_update_kernel(const float *S, int lda
   }
 }
 
-// The block's accept/discard loop in coefficient space (one warp, FP64; lane m holds component m).
+// The block's accept/discard loop in coefficient space (one warp, FP64).  Gd, G2 and the accepted vectors
+// r_a (with U_a = Gd r_a) sit in shared memory; every step is a 32 x 32 matrix-vector product with one
+// lane per output entry (no reductions across lanes):
+//   classical pass:  c = (U^T t) ./ dd  (lane a),  then  t -= R c  (lane m), twice;
+//   norm^2 = t^T G2 t;  discard below 1e-3, else r = t / norm, U = Gd r, dd = r^T U.
 // st: [0] accepted so far (j), [1] discarded, [2] candidates consumed, [3] accepted in this block.
 __global__ void bcgs_block_gs_kernel(const double *Gd, const double *G2, int bc, int k, int rc0, int *st,
                                      double *dlog, float *R) {
-  __shared__ double Rm[BB][BB];  // Rm[a][m]: accepted vector a
-  __shared__ double Um[BB][BB];  // Um[a][m] = (Gd r_a)[m]
-  __shared__ double dd[BB];
+  __shared__ double sGd[BB][BB + 1], sG2[BB][BB + 1];
+  __shared__ double Rm[BB][BB + 1];  // Rm[a][m]: accepted vector a
+  __shared__ double Um[BB][BB + 1];  // Um[a][m] = (Gd r_a)[m]
+  __shared__ double dd[BB], tv[BB], cv[BB];
   const int m = threadIdx.x;
+  for (int l = 0; l < BB; l++) {
+    sGd[l][m] = Gd[l * BB + m];
+    sG2[l][m] = G2[l * BB + m];
+  }
   const int j0 = st[0];
   int nacc = 0, ndisc = 0, ncons = 0;
+  __syncwarp();
   for (int i = 0; i < bc; i++) {
     if (j0 + nacc >= k) break;
     ncons++;
     double t = m == i ? 1.0 : 0.0;
-    for (int pass = 0; pass < 2; pass++) {
-      double sub = 0;
-      for (int a = 0; a < nacc; a++) {
-        const double c = warp_sum(t * Um[a][m]) / dd[a];  // classical: all c_a from the same t
-        sub += c * Rm[a][m];
+    for (int pass = 0; pass < 2 && nacc > 0; pass++) {
+      tv[m] = t;
+      __syncwarp();
+      if (m < nacc) {  // c_a = <t, U_a> / dd_a, all from the same t (classical)
+        double c0 = 0, c1 = 0;
+        for (int l = 0; l < BB; l += 2) {
+          c0 = fma(Um[m][l], tv[l], c0);
+          c1 = fma(Um[m][l + 1], tv[l + 1], c1);
+        }
+        cv[m] = (c0 + c1) / dd[m];
       }
-      t -= sub;
+      __syncwarp();
+      double s0 = 0, s1 = 0;
+      int a = 0;
+      for (; a + 1 < nacc; a += 2) {
+        s0 = fma(cv[a], Rm[a][m], s0);
+        s1 = fma(cv[a + 1], Rm[a + 1][m], s1);
+      }
+      if (a < nacc) s0 = fma(cv[a], Rm[a][m], s0);
+      t -= s0 + s1;
+      __syncwarp();
     }
-    double g2t = 0;
-    for (int l = 0; l < BB; l++) g2t += G2[m * BB + l] * __shfl_sync(PHDE_FULL_MASK, t, l);
-    const double nrm = sqrt(fmax(warp_sum(t * g2t), 0.0));
+    tv[m] = t;
+    __syncwarp();
+    double g0 = 0, g1 = 0;
+    for (int l = 0; l < BB; l += 2) {
+      g0 = fma(sG2[m][l], tv[l], g0);
+      g1 = fma(sG2[m][l + 1], tv[l + 1], g1);
+    }
+    const double nrm = sqrt(fmax(warp_sum(t * (g0 + g1)), 0.0));
     if (nrm < 0.001) {
       ndisc++;
       if (m == 0) dlog[rc0 + i] = nrm;
     } else {
       const double r = t / nrm;
-      double u = 0;
-      for (int l = 0; l < BB; l++) u += Gd[m * BB + l] * __shfl_sync(PHDE_FULL_MASK, r, l);
+      tv[m] = r;
+      __syncwarp();
+      double u0 = 0, u1 = 0;
+      for (int l = 0; l < BB; l += 2) {
+        u0 = fma(sGd[m][l], tv[l], u0);
+        u1 = fma(sGd[m][l + 1], tv[l + 1], u1);
+      }
+      const double u = u0 + u1;
       const double d = warp_sum(r * u);
       Rm[nacc][m] = r;
       Um[nacc][m] = u;
       if (m == 0) dd[nacc] = d;
-      __syncwarp();
       nacc++;
     }
+    __syncwarp();
   }
   for (int a = 0; a < BB; a++) R[m * BB + a] = a < nacc ? (float)Rm[a][m] : 0.f;
   if (m == 0) {

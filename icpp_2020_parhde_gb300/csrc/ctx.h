@@ -42,6 +42,8 @@ struct phde_ctx {
   cudaEvent_t kev[2] = {};
   bool kev_pending = false;
   double kernel_ms = 0;  // accumulated by phde_collect_kernel_time()
+  double msbfs_ms = 0;   // of which multi-source BFS sweeps
+  int msbfs_levels = 0;
   int kernel_launches = 0;
 };
 

@@ -445,6 +445,220 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(const double *Kin, 
   }
 }
 
+// ---- shared-memory Jacobi for N <= JS_MAX_N: FP32 sweeps, FP64 re-orthonormalisation, FP64 sweeps ----
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate, and a cyclic Jacobi solve of a k x k matrix is about ten
+// sweeps of N-1 rounds.  Here the sweeps that only shrink the off-diagonal run in FP32 (A32, V32); the FP32
+// eigenbasis V is then made orthonormal in FP64 (classical Gram-Schmidt, exact enough for a basis that is
+// orthogonal to FP32 rounding), A is replaced by the exactly similar V^T A V computed in FP64, and FP64
+// sweeps (quadratically convergent from an off-diagonal of FP32 rounding size) finish with the same
+// convergence test as the global-memory kernel.  Everything lives in shared memory.
+constexpr int JS_MAX_N = 96;  // 24 N^2 bytes of shared memory: A64, V64 and one work matrix
+
+template <typename T>
+__device__ void js_offnorm(const T *A, int N, double *red, double &off, double &tot) {
+  double o = 0, t = 0;
+  for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    const double a = (double)A[idx];
+    t += a * a;
+    if (i != j) o += a * a;
+  }
+  off = block_sum(o, red);
+  tot = block_sum(t, red);
+}
+
+// One cyclic sweep (M-1 rounds of M/2 disjoint rotations, circle-method pairing) on A and V.
+template <typename T>
+__device__ void js_sweep(T *A, T *V, int N, int M, int *s_order, double *s_cs, double *s_sn, int *s_p, int *s_q) {
+  const int tid = threadIdx.x;
+  for (int round = 0; round < M - 1; round++) {
+    for (int m = tid; m < M / 2; m += blockDim.x) {
+      int p = s_order[m], q = s_order[M - 1 - m];
+      if (p > q) {
+        const int t = p;
+        p = q;
+        q = t;
+      }
+      T cs = (T)1, sn = (T)0;
+      if (q < N) {
+        const T apq = A[p + q * N];
+        if (apq != (T)0) {
+          const T app = A[p + p * N], aqq = A[q + q * N];
+          const T theta = (aqq - app) / ((T)2 * apq);
+          const T t = (theta >= (T)0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt(theta * theta + (T)1));
+          cs = (T)1 / sqrt(t * t + (T)1);
+          sn = t * cs;
+        }
+      }
+      s_p[m] = p;
+      s_q[m] = q;
+      s_cs[m] = (double)cs;
+      s_sn[m] = (double)sn;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
+      const int m = idx / N, row = idx % N;
+      const int p = s_p[m], q = s_q[m];
+      if (q >= N || s_sn[m] == 0.0) continue;
+      const T cs = (T)s_cs[m], sn = (T)s_sn[m];
+      const T akp = A[row + p * N], akq = A[row + q * N];
+      A[row + p * N] = cs * akp - sn * akq;
+      A[row + q * N] = sn * akp + cs * akq;
+      const T vkp = V[row + p * N], vkq = V[row + q * N];
+      V[row + p * N] = cs * vkp - sn * vkq;
+      V[row + q * N] = sn * vkp + cs * vkq;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
+      const int m = idx / N, col = idx % N;
+      const int p = s_p[m], q = s_q[m];
+      if (q >= N || s_sn[m] == 0.0) continue;
+      const T cs = (T)s_cs[m], sn = (T)s_sn[m];
+      const T apk = A[p + col * N], aqk = A[q + col * N];
+      A[p + col * N] = cs * apk - sn * aqk;
+      A[q + col * N] = sn * apk + cs * aqk;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const int last = s_order[M - 1];
+      for (int i = M - 1; i > 1; i--) s_order[i] = s_order[i - 1];
+      s_order[1] = last;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *Kin, int N, double *K, double *evals,
+                                                                  int *sweeps, int *status, int max_sweeps) {
+  extern __shared__ double js[];
+  double *A = js, *V = js + N * N, *W = js + 2 * N * N;
+  float *A32 = (float *)W, *V32 = (float *)W + N * N;
+  __shared__ double red[32];
+  __shared__ double s_cs[JS_MAX_N / 2 + 1], s_sn[JS_MAX_N / 2 + 1], s_d[JS_MAX_N];
+  __shared__ int s_p[JS_MAX_N / 2 + 1], s_q[JS_MAX_N / 2 + 1];
+  __shared__ int s_order[JS_MAX_N + 1];
+  __shared__ int s_done;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int M = (N + 1) & ~1;
+  for (int idx = tid; idx < N * N; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    const double a = 0.5 * (Kin[i + j * N] + Kin[j + i * N]);
+    A[idx] = a;
+    A32[idx] = (float)a;
+    V32[idx] = i == j ? 1.f : 0.f;
+  }
+  for (int i = tid; i < M; i += blockDim.x) s_order[i] = i;
+  __syncthreads();
+  // ---- FP32 sweeps: until FP32 rounding dominates the off-diagonal ----
+  int sw32 = 0;
+  double off = 0, tot = 0;
+  for (; sw32 < 16; sw32++) {
+    js_offnorm(A32, N, red, off, tot);
+    if (tid == 0) s_done = off <= 1e-11 * tot;
+    __syncthreads();
+    if (s_done) break;
+    js_sweep<float>(A32, V32, N, M, s_order, s_cs, s_sn, s_p, s_q);
+  }
+  // ---- V = FP64 orthonormalisation of V32 (classical Gram-Schmidt, column order) ----
+  for (int idx = tid; idx < N * N; idx += blockDim.x) V[idx] = (double)V32[idx];
+  __syncthreads();
+  for (int j = 0; j < N; j++) {
+    for (int i = warp; i < j; i += nw) {  // s_d[i] = <V_i, V_j>
+      double d = 0;
+      for (int r = lane; r < N; r += 32) d = fma(V[r + i * N], V[r + j * N], d);
+      d = warp_sum(d);
+      if (lane == 0) s_d[i] = d;
+    }
+    __syncthreads();
+    for (int r = tid; r < N; r += blockDim.x) {
+      double v = V[r + j * N];
+      for (int i = 0; i < j; i++) v = fma(-s_d[i], V[r + i * N], v);
+      V[r + j * N] = v;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double d = 0;
+      for (int r = lane; r < N; r += 32) d = fma(V[r + j * N], V[r + j * N], d);
+      d = warp_sum(d);
+      if (lane == 0) s_d[j] = 1.0 / sqrt(d);
+    }
+    __syncthreads();
+    for (int r = tid; r < N; r += blockDim.x) V[r + j * N] *= s_d[j];
+    __syncthreads();
+  }
+  // ---- A <- V^T A V in FP64 (W = A V, then A = V^T W, symmetrised) ----
+  for (int idx = tid; idx < N * N; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    double s = 0;
+    for (int l = 0; l < N; l++) s = fma(A[i + l * N], V[l + j * N], s);
+    W[idx] = s;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < N * N; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    if (i > j) continue;
+    double s = 0, t = 0;
+    for (int l = 0; l < N; l++) {
+      s = fma(V[l + i * N], W[l + j * N], s);
+      t = fma(V[l + j * N], W[l + i * N], t);
+    }
+    s = 0.5 * (s + t);
+    // A is read by the W pass only, which finished at the barrier above
+    A[i + j * N] = s;
+    A[j + i * N] = s;
+  }
+  for (int i = tid; i < M; i += blockDim.x) s_order[i] = i;
+  __syncthreads();
+  // ---- FP64 sweeps ----
+  int sw64 = 0;
+  for (; sw64 < max_sweeps; sw64++) {
+    js_offnorm(A, N, red, off, tot);
+    if (tid == 0) s_done = (off <= 1e-28 * tot) || off == 0.0;
+    __syncthreads();
+    if (s_done) break;
+    js_sweep<double>(A, V, N, M, s_order, s_cs, s_sn, s_p, s_q);
+  }
+  if (sw64 == max_sweeps) js_offnorm(A, N, red, off, tot);
+  if (tid == 0) {
+    for (int i = 0; i < N; i++) s_order[i] = i;
+    for (int i = 0; i < N; i++) {
+      int b = i;
+      for (int j = i + 1; j < N; j++)
+        if (A[s_order[j] + s_order[j] * N] < A[s_order[b] + s_order[b] * N]) b = j;
+      const int t = s_order[i];
+      s_order[i] = s_order[b];
+      s_order[b] = t;
+    }
+    for (int c = 0; c < N; c++) evals[c] = A[s_order[c] + s_order[c] * N];
+    *sweeps = sw32 + sw64;
+    *status = (sw64 < max_sweeps || off <= 1e-20 * tot) ? PHDE_OK : PHDE_ERR_NOCONVERGE;
+  }
+  __syncthreads();
+  for (int c = warp; c < N; c += nw) {
+    const int src = s_order[c];
+    double best = -1.0;
+    int arg = 0;
+    for (int i = lane; i < N; i += 32) {
+      const double a = fabs(V[i + src * N]);
+      if (a > best) {
+        best = a;
+        arg = i;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double b2 = __shfl_xor_sync(PHDE_FULL_MASK, best, o);
+      const int a2 = __shfl_xor_sync(PHDE_FULL_MASK, arg, o);
+      if (b2 > best || (b2 == best && a2 < arg)) {
+        best = b2;
+        arg = a2;
+      }
+    }
+    const double sg = V[arg + src * N] < 0 ? -1.0 : 1.0;
+    for (int i = lane; i < N; i += 32) K[i + c * N] = sg * V[i + src * N];
+  }
+}
+
 __global__ void pick_kernel(const double *K, int N, int c, int largest, double *Y) {
   for (int idx = threadIdx.x; idx < N * c; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
@@ -466,7 +680,13 @@ int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest,
   if (!w1 || !w2 || !dd || !st) return PHDE_ERR_OOM;
   PHDE_CK(ctx, cudaMemsetAsync(st, 0, sizeof(int) * 2, ctx->stream));
   if (eig == PHDE_EIG_EXACT) {
-    jacobi_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, w1, w2, d_K, d_evals, st, st + 1, 100);
+    if (N <= JS_MAX_N && !getenv("PHDE_JACOBI_GLOBAL")) {
+      const size_t jsmem = sizeof(double) * 3 * (size_t)N * N;
+      PHDE_CK(ctx, cudaFuncSetAttribute(jacobi_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
+      jacobi_smem_kernel<<<1, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, st, st + 1, 100);
+    } else {
+      jacobi_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, w1, w2, d_K, d_evals, st, st + 1, 100);
+    }
   } else {
     const int NO = (N + PW_CL - 1) / PW_CL;
     const size_t csmem = sizeof(double) * ((size_t)N * N + 2 * (size_t)NO * N + 2 * NO + 1);

@@ -11,8 +11,10 @@
 //                    R-MAT-20 basis is 129 MB and stays largely in the 129 MB L2), same heavy-row plan.
 //   gram32_kernel    S^T LS with FP32 products accumulated in FP32 over 16-row slabs and in FP64 across
 //                    slabs and blocks.
-//   coords32_kernel  X = S*Y with the FP64 eigenvectors, FP64 accumulation.
+//   coords32_kernel  X = S*Y: FP32 products and row sums (S is FP32), FP64 column norms.
 // The k x k eigensolve stays FP64 (eigen.cu).
+#include <algorithm>
+
 #include "ctx.h"
 #include "spmm_plan.cuh"
 
@@ -20,6 +22,7 @@ namespace {
 
 constexpr int C2_THREADS = 256;
 constexpr int MAXQ = 8;  // columns per lane: k <= 256
+constexpr int COORD_MAXC = 4;  // coordinates per FP32 coords pass
 
 __device__ __forceinline__ double partials_sum(const double *part, double *red) {
   double s = 0;
@@ -365,22 +368,41 @@ __global__ void sum_parts32_kernel(const double *part, int splits, int64_t len, 
 
 // X[i + t*n] = sum_q S[i,q] * Y[q + t*k] (FP32 basis, FP64 eigenvectors and accumulation)
 __global__ void coords32_kernel(const float *S, const double *Y, int64_t n, int k, int c, double *X, double *part) {
-  extern __shared__ double smc[];
+  extern __shared__ double smc[];  // [nw * c] column sums of squares, then FP32 Y
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float *Ys = (float *)(smc + nw * c);  // Ys[q * c + t]
+  for (int idx = threadIdx.x; idx < k * c; idx += blockDim.x) {
+    const int q = idx / c, t = idx % c;
+    Ys[idx] = (float)Y[q + (int64_t)t * k];
+  }
+  __syncthreads();
   const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
-  for (int t = 0; t < c; t++) {
-    double ss = 0;
-    for (int64_t i = gw; i < n; i += gws) {
-      double s = 0;
-      for (int q = lane; q < k; q += 32) s = fma((double)S[i * k + q], Y[q + (int64_t)t * k], s);
-      s = warp_sum(s);
+  double ss[COORD_MAXC];
+#pragma unroll
+  for (int t = 0; t < COORD_MAXC; t++) ss[t] = 0;
+  // a warp per row: FP32 products and sums over the row's k entries, all c coordinates in one read of S
+  for (int64_t i = gw; i < n; i += gws) {
+    float acc[COORD_MAXC];
+#pragma unroll
+    for (int t = 0; t < COORD_MAXC; t++) acc[t] = 0.f;
+    for (int q = lane; q < k; q += 32) {
+      const float sv = S[i * k + q];
+#pragma unroll
+      for (int t = 0; t < COORD_MAXC; t++)
+        if (t < c) acc[t] = fmaf(sv, Ys[q * c + t], acc[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < COORD_MAXC; t++) {
+      if (t >= c) break;
+      const float v = warp_sum(acc[t]);
       if (lane == 0) {
-        X[i + (int64_t)t * n] = s;
-        ss = fma(s, s, ss);
+        X[i + (int64_t)t * n] = (double)v;
+        ss[t] = fma((double)v, (double)v, ss[t]);
       }
     }
-    if (lane == 0) smc[warp * c + t] = ss;
   }
+  if (lane == 0)
+    for (int t = 0; t < c; t++) smc[warp * c + t] = ss[t];
   __syncthreads();
   for (int t = threadIdx.x; t < c; t += blockDim.x) {
     double s = 0;
@@ -497,12 +519,18 @@ int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double
 
 int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X) {
   const int threads = 256;
-  const int grid = grid_of(ctx, ctx->n * 32, threads, 4);
-  double *part = (double *)phde_buf(ctx, "coords32.part", sizeof(double) * grid * (size_t)c);
+  const int grid = grid_of(ctx, ctx->n * 32, threads, 8);
+  double *part = (double *)phde_buf(ctx, "coords32.part", sizeof(double) * grid * (size_t)COORD_MAXC);
   if (!part) return PHDE_ERR_OOM;
-  coords32_kernel<<<grid, threads, sizeof(double) * (threads / 32) * c, ctx->stream>>>(S, Y, ctx->n, k, c, X, part);
-  PHDE_LAUNCHED(ctx);
-  scale32_kernel<<<grid_of(ctx, ctx->n * c, 256, 8), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid);
-  PHDE_LAUNCHED(ctx);
+  for (int t0 = 0; t0 < c; t0 += COORD_MAXC) {  // coordinates in groups of COORD_MAXC
+    const int cg = std::min(COORD_MAXC, c - t0);
+    const size_t smem = sizeof(double) * (threads / 32) * cg + sizeof(float) * (size_t)k * cg;
+    coords32_kernel<<<grid, threads, smem, ctx->stream>>>(S, Y + (int64_t)t0 * k, ctx->n, k, cg, X + (int64_t)t0 * ctx->n,
+                                                          part);
+    PHDE_LAUNCHED(ctx);
+    scale32_kernel<<<grid_of(ctx, ctx->n * cg, 256, 8), 256, 0, ctx->stream>>>(X + (int64_t)t0 * ctx->n, ctx->n, cg,
+                                                                               part, grid);
+    PHDE_LAUNCHED(ctx);
+  }
   return PHDE_OK;
 }

@@ -25,6 +25,7 @@ constexpr int MS_MAXW = 4;
 constexpr int64_t MS_HEAVY = 256;  // rows above this are cut into chunks (one warp per chunk)
 constexpr int64_t MS_CHUNK = 256;
 constexpr int MS_GROUP = 8;        // lanes per light row
+constexpr int GATHER_SMEM_COLS = 1024;  // columns whose sums of squares are kept per CTA
 
 struct MsArgs {
   const int64_t *off;
@@ -293,7 +294,9 @@ __global__ void ms_heavy_plan_kernel(const int64_t *off, int64_t n, int64_t *hea
 __global__ void gather_columns_kernel(const uint16_t *R, int64_t n, int RW, const int *cols, int ncols, int32_t *D,
                                       ull *sumsq, int *unreached) {
   extern __shared__ uint16_t tile[];  // [32][RW]
+  __shared__ ull s_ssq[GATHER_SMEM_COLS];  // per-CTA column sums; column p is always summed by warp p % nw
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int p = threadIdx.x; p < GATHER_SMEM_COLS; p += blockDim.x) s_ssq[p] = 0ull;
   int bad = 0;
   for (int64_t v0 = (int64_t)blockIdx.x * 32; v0 < n; v0 += (int64_t)gridDim.x * 32) {
     const int rows = n - v0 < 32 ? (int)(n - v0) : 32;
@@ -311,9 +314,17 @@ __global__ void gather_columns_kernel(const uint16_t *R, int64_t n, int RW, cons
       }
       const ull sq = d > 0 ? (ull)d * (ull)d : 0ull;
       const ull tot = warp_sum(sq);
-      if (lane == 0 && tot) atomicAdd(sumsq + p, tot);
+      if (lane == 0 && tot) {
+        if (p < GATHER_SMEM_COLS)
+          s_ssq[p] += tot;
+        else
+          atomicAdd(sumsq + p, tot);
+      }
     }
   }
+  __syncthreads();
+  for (int p = threadIdx.x; p < ncols && p < GATHER_SMEM_COLS; p += blockDim.x)
+    if (s_ssq[p]) atomicAdd(sumsq + p, s_ssq[p]);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(unreached, 1);
 }
 
@@ -417,12 +428,18 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.err = ctx->d_err;
     a.timeout_ns = ctx->timeout_ns;
     void *args[] = {&a};
+    const double before = ctx->kernel_ms;
     cudaEventRecord(ctx->kev[0], ctx->stream);
     PHDE_CK(ctx, cudaLaunchCooperativeKernel(fn, dim3(ctx->nsm * per_sm), dim3(MS_THREADS), args, 0, ctx->stream));
     PHDE_LAUNCHED(ctx);
     cudaEventRecord(ctx->kev[1], ctx->stream);
     ctx->kev_pending = true;
-    if ((rc = phde_check_device_err(ctx, "multi-source BFS"))) return rc;
+    if ((rc = phde_check_device_err(ctx, "multi-source BFS"))) return rc;  // synchronises, collects the time
+    ctx->msbfs_ms += ctx->kernel_ms - before;
+    int nlev = 0;
+    PHDE_CK(ctx, cudaMemcpyAsync(&nlev, levels, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->msbfs_levels += nlev;
     if (trace) {
       int nl = 0;
       std::vector<ull> h(2 * trace_cap);

@@ -93,6 +93,8 @@ typedef struct {
   int64_t edges_examined; /* adjacency entries read by the distance passes                          */
   double ms_dist_kernel;  /* device time of the distance kernel launches alone (events around each launch) */
   int dist_kernel_launches; /* number of distance kernel launches (1 for the Kcenters BFS)           */
+  double ms_msbfs_kernel;   /* of which multi-source BFS sweeps (learned and random strategies)          */
+  int msbfs_levels;         /* levels of those sweeps, summed                                           */
 } phde_layout_stats;
 
 /* optional extra outputs of phde_layout (any member may be NULL) */
