@@ -54,7 +54,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--graph", default="rmat", choices=["rmat", "rgg3d"])
     ap.add_argument("--rmat-scale", type=int, default=20)
+    ap.add_argument("--rgg-n", type=int, default=8_000_000, help="vertices of the 3-D random geometric graph")
     ap.add_argument("--k", type=int, default=50)
     ap.add_argument("--c", type=int, default=3)
     ap.add_argument("--seed", type=int, default=1)
@@ -146,8 +148,17 @@ def profiled_traffic(name):
 def make_graph(args):
     from icpp_2020_parhde_gb300 import graphs
     t = time.time()
-    g = graphs.rmat(args.rmat_scale, 16, 0.57, 0.19, 0.19, seed=args.seed)
+    if args.graph == "rgg3d":
+        g = graphs.rgg(args.rgg_n, dim=3, avg_degree=12, seed=args.seed)
+    else:
+        g = graphs.rmat(args.rmat_scale, 16, 0.57, 0.19, 0.19, seed=args.seed)
     return g, time.time() - t
+
+
+def graph_desc(args):
+    if args.graph == "rgg3d":
+        return "a 3-D random geometric graph (%d points in the unit cube, radius for mean degree 12, LCC)" % args.rgg_n
+    return ("an R-MAT scale-%d graph (edgefactor 16, a=.57 b=.19 c=.19, symmetrised, LCC)" % args.rmat_scale)
 
 
 def dist_init():
@@ -223,8 +234,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "ParHDE Kcenters layout, R-MAT scale %d ef16 LCC (n=%d, nnz=%d), k=%d, c=%d"
-                                   % (args.rmat_scale, g.n, g.nnz, args.k, args.c),
+            "config": {"workload": "ParHDE Kcenters layout of %s (n=%d, nnz=%d), k=%d, c=%d"
+                                   % (graph_desc(args), g.n, g.nnz, args.k, args.c),
                        "n": g.n, "nnz": g.nnz, "k": args.k, "c": args.c},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
                              "sample": "%d full layouts after %d warm-up, OpenMP oracle port of the reference algorithm"
@@ -356,7 +367,7 @@ def run_gb300(args):
         bytes_launch = lv * per_level
         kern_ms = float(np.mean([s["ms_msbfs_kernel"] for s in head["stats"]]))
         achieved = bytes_launch / (kern_ms * 1e-3) / 1e9
-        traffic = profiled_traffic("msbfs_kernel_rmat20.md") if args.rmat_scale == 20 else None
+        traffic = profiled_traffic("msbfs_kernel_rmat20.md") if (args.graph, args.rmat_scale, k) == ("rmat", 20, 50) else None
         roof = {"kernel": "msbfs_kernel<4>", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": ("measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"),
@@ -389,8 +400,7 @@ def run_gb300(args):
         "ms_per_step": hl["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32 distances, f32 n-sized stages with f64 sums, f64 k x k" if not fallback else "f64",
         "data": "synthetic",
-        "config": {"workload": "ParHDE layout of an R-MAT scale-%d graph (edgefactor 16, a=.57 b=.19 c=.19, "
-                               "symmetrised, LCC), k=%d pivots, %d coordinates" % (args.rmat_scale, k, c),
+        "config": {"workload": "ParHDE layout of %s, k=%d pivots, %d coordinates" % (graph_desc(args), k, c),
                    "pipeline": "plain Kcenters fallback" if fallback else "learned pivots + mixed precision + exact eigensolve",
                    "n": n, "nnz": nnz, "k": k, "c": c, "parallelism": "replicas%d" % ws if ws > 1 else "single",
                    "l2": "flushed between timed steps (256 MB write)", "graph_gen_s": round(gen_s, 1)},

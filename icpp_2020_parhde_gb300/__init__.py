@@ -132,6 +132,34 @@ class Context:
         self._check(self._L.phde_kcenters(self._h, passes, variant, _ptr(D, C.c_int32), _ptr(src, C.c_int64)))
         return (D.reshape(passes, self.n).T if D is not None else None), src
 
+    def upload_batch(self, graphs) -> None:
+        """Upload many graphs as one batch (phde_batch_upload); they keep their own local vertex ids."""
+        keep, descs = [], []
+        wide = any(np.asarray(g.offsets).dtype in (np.int64, np.uint64) for g in graphs)
+        for g in graphs:
+            off = np.ascontiguousarray(g.offsets, dtype=np.int64 if wide else np.uint32)
+            adj = np.ascontiguousarray(g.adj, dtype=np.uint32)
+            keep += [off, adj]
+            descs.append(_lib.GraphDesc(off.ctypes.data, 8 if wide else 4, adj.ctypes.data, g.n, g.nnz))
+        arr = (_lib.GraphDesc * len(descs))(*descs)
+        self._check(self._L.phde_batch_upload(self._h, arr, len(descs)))
+        self.batch_sizes = [g.n for g in graphs]
+        self.n, self.nnz, self.weighted = sum(self.batch_sizes), sum(g.nnz for g in graphs), False
+
+    def layout_batched(self, k: int = 10, c: int = 2, coords_out: np.ndarray | None = None):
+        """phde_layout_batched: (list of per-graph (n_b, c) coordinate arrays, stats dict)."""
+        o = _lib.LayoutOpts(_lib.ALGOS["ParHDE"], _lib.STRATEGIES["Kcenters"], k, c, _lib.PRECISIONS["mixed"],
+                            _lib.EIGS["exact"], 1, 0)
+        total = sum(self.batch_sizes)
+        out = coords_out if coords_out is not None else np.empty(total * c, dtype=np.float64)
+        st = _lib.LayoutStats()
+        self._check(self._L.phde_layout_batched(self._h, C.byref(o), _ptr(out, C.c_double), C.byref(st)))
+        res, base = [], 0
+        for nb in self.batch_sizes:
+            res.append(out[c * base: c * (base + nb)].reshape(c, nb).T)
+            base += nb
+        return res, st.as_dict()
+
     def selftest_barrier_timeout(self, timeout_ms: int = 50) -> int:
         return int(self._L.phde_selftest_barrier_timeout(self._h, timeout_ms))
 

@@ -26,7 +26,7 @@ EXPORTS = [
     "phde_create", "phde_destroy", "phde_last_error", "phde_status_string", "phde_version", "phde_graph_upload",
     "phde_graph_n", "phde_graph_nnz", "phde_layout", "phde_distances", "phde_kcenters", "phde_DOBFS",
     "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
-    "phde_set_pivot_model",
+    "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched",
 ]
 
 
@@ -35,12 +35,18 @@ class LayoutOpts(C.Structure):
                 ("eig", C.c_int), ("seed", C.c_uint64), ("verbose", C.c_int)]
 
 
+class GraphDesc(C.Structure):
+    _fields_ = [("offsets", C.c_void_p), ("offset_bytes", C.c_int), ("adj", C.c_void_p), ("n", C.c_int64),
+                ("nnz", C.c_int64)]
+
+
 class LayoutStats(C.Structure):
     _fields_ = [("status", C.c_int), ("npasses", C.c_int), ("naccepted", C.c_int), ("ndiscarded", C.c_int),
                 ("eig_iters", C.c_int), ("gpu_launches", C.c_int), ("ms_dist", C.c_double), ("ms_orth", C.c_double),
                 ("ms_mmult", C.c_double), ("ms_eig", C.c_double), ("ms_coords", C.c_double),
                 ("ms_total", C.c_double), ("edges_examined", C.c_int64), ("ms_dist_kernel", C.c_double),
-                ("dist_kernel_launches", C.c_int), ("ms_msbfs_kernel", C.c_double), ("msbfs_levels", C.c_int)]
+                ("dist_kernel_launches", C.c_int), ("ms_msbfs_kernel", C.c_double), ("msbfs_levels", C.c_int),
+                ("batch_graph_replay", C.c_int), ("batch_seg_rows", C.c_int), ("ms_batch_tune", C.c_double)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -91,5 +97,7 @@ def load(path: str | None = None):
     L.phde_launch_count.restype = i64
     L.phde_bfs_noalloc.argtypes = [vp, vp, i64, i64, i64, vp, vp]
     L.phde_set_pivot_model.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
+    L.phde_batch_upload.argtypes = [vp, C.POINTER(GraphDesc), C.c_int]
+    L.phde_layout_batched.argtypes = [vp, C.POINTER(LayoutOpts), f64p, C.POINTER(LayoutStats)]
     _lib = L
     return L

@@ -111,6 +111,7 @@ void *phde_buf(phde_ctx *ctx, const char *name, size_t bytes) {
     ctx->ws.erase(it);
   }
   void *p = nullptr;
+  ctx->ws_epoch++;
   if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
     cudaGetLastError();
     ctx->err = std::string("device allocation of ") + std::to_string(bytes) + " bytes for " + name + " failed";
@@ -212,6 +213,9 @@ void phde_destroy(phde_ctx *c) {
   cudaFree(c->d_w);
   cudaFree(c->d_sync);
   cudaFree(c->d_err);
+  cudaFree(c->d_vbase);
+  cudaFree(c->d_gid);
+  if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (auto &e : c->ev) cudaEventDestroy(e);
   for (auto &e : c->kev) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
@@ -247,6 +251,7 @@ int phde_graph_upload(phde_ctx *ctx, const void *offsets, int offset_bytes, cons
   ctx->n = n;
   ctx->nnz = nnz;
   ctx->graph_epoch++;
+  ctx->batch_B = 0;
   if (offset_bytes == 8) {
     PHDE_CK(ctx, cudaMemcpyAsync(ctx->d_off, offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
   } else {

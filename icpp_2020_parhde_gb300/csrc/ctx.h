@@ -17,7 +17,22 @@ struct phde_ctx {
   std::string err;
   long long launches = 0;
   uint64_t timeout_ns = 5000000000ull;  // bounded device waits: 5 s per wait
-  bool column_cgs2 = false;             // mixed path: column-at-a-time CGS2 (PHDE_CGS2=column) instead of blocked
+  bool column_cgs2 = false;
+  // uploaded batch (phde_batch_upload): the device CSR is the disjoint union of batch_B graphs
+  int batch_B = 0;
+  std::vector<int64_t> batch_vbase, batch_ebase;  // host copies, batch_B + 1 entries
+  int64_t *d_vbase = nullptr;                      // [batch_B + 1]
+  int32_t *d_gid = nullptr;                        // [n]: graph of each vertex
+  int64_t batch_tuned_epoch = -1;                  // autotuned segment length for this graph epoch and k
+  int batch_tuned_k = 0;
+  int64_t batch_seg_rows = 8192;
+  float batch_tune_ms = 0;
+  cudaGraphExec_t batch_graph = nullptr;           // the captured batched pipeline
+  int batch_graph_c = 0;
+  int64_t batch_graph_ws = -1;
+  int64_t batch_graph_launches = 0;
+  bool batch_no_graph = false;                     // capture failed once: launch directly
+  int64_t ws_epoch = 0;                            // bumped whenever a workspace buffer is (re)allocated             // mixed path: column-at-a-time CGS2 (PHDE_CGS2=column) instead of blocked
 
   // uploaded graph (offsets widened to int64)
   int64_t n = 0, nnz = 0;

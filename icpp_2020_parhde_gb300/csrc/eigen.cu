@@ -532,6 +532,12 @@ __device__ void js_sweep(T *A, T *V, int N, int M, int *s_order, double *s_cs, d
 __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *Kin, int N, double *K, double *evals,
                                                                   int *sweeps, int *status, int max_sweeps) {
   extern __shared__ double js[];
+  // a batch of problems: block b solves matrix b (N*N apart), with its own evals, sweeps and status
+  Kin += (int64_t)blockIdx.x * N * N;
+  K += (int64_t)blockIdx.x * N * N;
+  evals += (int64_t)blockIdx.x * N;
+  sweeps += blockIdx.x;
+  status += blockIdx.x;
   double *A = js, *V = js + N * N, *W = js + 2 * N * N;
   float *A32 = (float *)W, *V32 = (float *)W + N * N;
   __shared__ double red[32];
@@ -660,6 +666,8 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
 }
 
 __global__ void pick_kernel(const double *K, int N, int c, int largest, double *Y) {
+  K += (int64_t)blockIdx.x * N * N;  // batch: block b picks from matrix b
+  Y += (int64_t)blockIdx.x * N * c;
   for (int idx = threadIdx.x; idx < N * c; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
     const int col = largest ? N - 1 - j : j;
@@ -710,5 +718,20 @@ int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest,
   if (h[1] != PHDE_OK)
     return phde_fail(ctx, h[1], eig == PHDE_EIG_EXACT ? "Jacobi eigensolver did not converge"
                                                       : "power iteration did not converge (iteration cap reached)");
+  return PHDE_OK;
+}
+
+// Batched exact solve: `count` k x k problems (column-major, N*N apart) in one launch, one CTA each
+// (shared-memory Jacobi; N <= JS_MAX_N).  d_st holds 2*count ints (sweeps, status).  No synchronisation:
+// the caller reads d_st when it next synchronises.
+int phde_eigensolve_batched(phde_ctx *ctx, const double *d_M, int N, int c, int count, double *d_K,
+                            double *d_evals, double *d_Y, int *d_st) {
+  if (N > JS_MAX_N) return phde_fail(ctx, PHDE_ERR_INVALID, "batched eigensolve: k above the shared-memory limit");
+  const size_t jsmem = sizeof(double) * 3 * (size_t)N * N;
+  PHDE_CK(ctx, cudaFuncSetAttribute(jacobi_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
+  jacobi_smem_kernel<<<count, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, d_st, d_st + count, 100);
+  PHDE_LAUNCHED(ctx);
+  pick_kernel<<<count, 256, 0, ctx->stream>>>(d_K, N, c, 0, d_Y);
+  PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

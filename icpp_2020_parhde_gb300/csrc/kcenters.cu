@@ -60,7 +60,32 @@ struct KcArgs {
   int *err;
   uint64_t timeout_ns;
   int alpha, beta;
+  // batched layouts: the graph is the disjoint union of B graphs (vertex ranges vbase[b]..vbase[b+1]);
+  // every pass runs one BFS per graph, all from the same launch, and the selection is per graph.  Then
+  // sources, keys and sumsq are indexed [p * B + b], and gid[v] is v's graph.
+  int B;
+  const int64_t *vbase;
+  const int32_t *gid;
+  ull *qinit;       // [1] level-0 queue counter of the pass (count << 32 | edges)
 };
+
+// Per-graph fold of a batched pass: the max of `key` and the sum of `ssq` over the lanes of one graph
+// (a warp covers consecutive vertices, so almost always one graph), one atomic per graph per warp.
+__device__ __forceinline__ void batch_fold(ull *keys, ull *sumsq, int g, ull key, ull ssq, bool valid) {
+  const int lane = threadIdx.x & 31;
+  const int g0 = __shfl_sync(PHDE_FULL_MASK, g, 0);
+  if (__all_sync(PHDE_FULL_MASK, valid && g == g0)) {
+    const ull km = warp_max_u64(key);
+    const ull ss = warp_sum(ssq);
+    if (lane == 0) {
+      atomicMax(keys + g0, km);
+      if (ss) atomicAdd(sumsq + g0, ss);
+    }
+  } else if (valid) {
+    atomicMax(keys + g, key);
+    if (ssq) atomicAdd(sumsq + g, ssq);
+  }
+}
 
 __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
   __shared__ PushScratch psc;
@@ -77,17 +102,48 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
 
   for (int p = 0; p < a.P; p++) {
     int32_t *Dp = a.D + (int64_t)p * n;
-    if (tid == 0) {
-      Dp[src] = 0;
-      // the level-0 frontier bitmap holds only the source (the previous pass left it empty)
-      atomicOr(a.bm[step % 3] + (src >> 5), 1u << (src & 31));
-      if (blockIdx.x == 0) a.sources[p] = src;
+    int64_t s_off = 0;
+    uint32_t sdeg = 0;
+    uint32_t f_cnt = 1, f_edges = 0;
+    if (a.B == 0) {
+      if (tid == 0) {
+        Dp[src] = 0;
+        // the level-0 frontier bitmap holds only the source (the previous pass left it empty)
+        atomicOr(a.bm[step % 3] + (src >> 5), 1u << (src & 31));
+        if (blockIdx.x == 0) a.sources[p] = src;
+      }
+      __syncthreads();
+      s_off = a.off[src];
+      sdeg = (uint32_t)(a.off[src + 1] - s_off);
+      f_edges = sdeg;
+    } else {
+      // batched: block 0 queues every graph's source (vertex 0 of the graph, then the previous pass's
+      // farthest vertex) as the level-0 frontier, in graph order
+      if (blockIdx.x == 0) {
+        if (tid == 0) *a.qinit = 0ull;
+        __syncthreads();
+        uint32_t *q0v = (step & 1) ? a.qv1 : a.qv0;
+        uint32_t *q0e = (step & 1) ? a.qe1 : a.qe0;
+        for (int b0 = 0; b0 < a.B; b0 += blockDim.x) {
+          const int b = b0 + tid;
+          uint32_t v = 0, dv = 0;
+          if (b < a.B) {
+            v = p == 0 ? (uint32_t)a.vbase[b]
+                       : 0xffffffffu - (uint32_t)(__ldcg(a.keys + (int64_t)(p - 1) * a.B + b) & 0xffffffffull);
+            dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+            Dp[v] = 0;
+            atomicOr(a.bm[step % 3] + (v >> 5), 1u << (v & 31));
+            a.sources[(int64_t)p * a.B + b] = v;
+          }
+          block_push(b < a.B, v, dv, q0v, q0e, a.qinit, &psc);
+        }
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      const ull q = __ldcg(a.qinit);
+      f_cnt = (uint32_t)(q >> 32);
+      f_edges = (uint32_t)(q & 0xffffffffull);
     }
-    __syncthreads();
-    const int64_t s_off = a.off[src];
-    const uint32_t sdeg = (uint32_t)(a.off[src + 1] - s_off);
-    uint32_t f_cnt = 1, f_edges = sdeg;
-    int64_t edges_to_check = a.nnz, scout = sdeg;
+    int64_t edges_to_check = a.nnz, scout = f_edges;
     bool in_bu = false;
     int64_t awake = 0, old_awake = 0;
     int32_t L = 0;
@@ -123,7 +179,7 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
           uint32_t v = 0, dv = 0;
           if (e < E) {
             int64_t j;
-            if (L == 0) {
+            if (L == 0 && a.B == 0) {
               j = s_off + e;
             } else {
               const uint32_t s = owner_slot(qin_e, f_cnt, (uint32_t)e);
@@ -199,6 +255,37 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
     // ---- fold the finished column: min distance, farthest vertex, sum of squares ----
     ull kbest = 0, ssq = 0;
     int bad = 0;
+    if (a.B > 0) {  // batched: per-graph keys and sums; the grid-stride loop keeps warps together
+      for (int64_t base = gbase; base < n; base += gstride) {
+        const int64_t v = base + tid;
+        ull key = 0, sq = 0;
+        int g = -1;
+        const bool valid = v < n;
+        if (valid) {
+          const int32_t d = Dp[v];
+          g = a.gid[v];
+          if (d < 0) {
+            bad = 1;
+          } else {
+            sq = (ull)d * (ull)d;
+            int32_t m = a.min_d[v];
+            if (d < m) {
+              m = d;
+              a.min_d[v] = m;
+            }
+            key = ((ull)(uint32_t)m << 32) | (ull)(0xffffffffu - (uint32_t)v);
+          }
+        }
+        batch_fold(a.keys + (int64_t)p * a.B, a.sumsq + (int64_t)p * a.B, g, key, sq, valid);
+      }
+      if (__syncthreads_or(bad)) {
+        if (tid == 0) atomicCAS(a.err, 0, PHDE_ERR_DISCONNECTED);
+        return;
+      }
+      if (p + 1 == a.P) break;
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      continue;
+    }
     for (int64_t v = gbase + tid; v < n; v += gstride) {
       const int32_t d = Dp[v];
       if (d < 0) {
@@ -281,9 +368,14 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   const int64_t n = ctx->n;
   if (ctx->nnz >= (int64_t)0xffffffffll || n >= (int64_t)0xffffffffll)
     return phde_fail(ctx, PHDE_ERR_INVALID, "graphs with 2^32 or more vertices or adjacency entries are not supported");
+  // variant 3: batched ParHDE Kcenters over the uploaded batch (per-graph sources, keys and sums)
+  const int B = variant == 3 ? ctx->batch_B : 0;
+  if (variant == 3 && B < 1) return phde_fail(ctx, PHDE_ERR_INVALID, "no batch uploaded");
+  const int64_t PB = (int64_t)P * (B ? B : 1);
   int32_t *min_d = (int32_t *)phde_buf(ctx, "kc.min_d", sizeof(int32_t) * n);
-  ull *keys = (ull *)phde_buf(ctx, "kc.keys", sizeof(ull) * P);
+  ull *keys = (ull *)phde_buf(ctx, "kc.keys", sizeof(ull) * PB);
   ull *fixkey = (ull *)phde_buf(ctx, "kc.fixkey", sizeof(ull) * P);
+  ull *qinit = (ull *)phde_buf(ctx, "kc.qinit", sizeof(ull));
   uint32_t *qv0 = (uint32_t *)phde_buf(ctx, "q.v0", sizeof(uint32_t) * n);
   uint32_t *qv1 = (uint32_t *)phde_buf(ctx, "q.v1", sizeof(uint32_t) * n);
   uint32_t *qe0 = (uint32_t *)phde_buf(ctx, "q.e0", sizeof(uint32_t) * n);
@@ -293,13 +385,13 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   uint32_t *bms = (uint32_t *)phde_buf(ctx, "kc.bitmaps", sizeof(uint32_t) * 3 * W);
   if (!bms) return PHDE_ERR_OOM;
   PHDE_CK(ctx, cudaMemsetAsync(bms, 0, sizeof(uint32_t) * 3 * W, ctx->stream));
-  if (!min_d || !keys || !fixkey || !qv0 || !qv1 || !qe0 || !qe1 || !ctr) return PHDE_ERR_OOM;
+  if (!min_d || !keys || !fixkey || !qinit || !qv0 || !qv1 || !qe0 || !qe1 || !ctr) return PHDE_ERR_OOM;
 
   PHDE_CK(ctx, cudaMemsetAsync(d_D, 0xff, sizeof(int32_t) * (size_t)n * (size_t)P, ctx->stream));
-  PHDE_CK(ctx, cudaMemsetAsync(keys, 0, sizeof(ull) * P, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(keys, 0, sizeof(ull) * PB, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(fixkey, 0, sizeof(ull) * P, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(ctr, 0, sizeof(ull) * 4, ctx->stream));
-  PHDE_CK(ctx, cudaMemsetAsync(d_sumsq, 0, sizeof(ull) * P, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(d_sumsq, 0, sizeof(ull) * PB, ctx->stream));
   int rc = phde_fill_i32(ctx, min_d, n, 0x7fffffff);
   if (rc) return rc;
   if ((rc = phde_reset_sync(ctx))) return rc;
@@ -321,7 +413,11 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   a.nnz = ctx->nnz;
   a.D = d_D;
   a.P = P;
-  a.variant = variant;
+  a.variant = variant == 3 ? 0 : variant;
+  a.B = B;
+  a.vbase = ctx->d_vbase;
+  a.gid = ctx->d_gid;
+  a.qinit = qinit;
   a.require_all = require_all || variant != 1;
   a.fixed_src = d_fixed_src;
   a.sources = d_sources;

@@ -95,6 +95,9 @@ typedef struct {
   int dist_kernel_launches; /* number of distance kernel launches (1 for the Kcenters BFS)           */
   double ms_msbfs_kernel;   /* of which multi-source BFS sweeps (learned and random strategies)          */
   int msbfs_levels;         /* levels of those sweeps, summed                                           */
+  int batch_graph_replay;   /* phde_layout_batched: 1 when the pipeline ran as one CUDA graph launch     */
+  int batch_seg_rows;       /* phde_layout_batched: rows per segment CTA picked by the autotuner         */
+  double ms_batch_tune;     /* phde_layout_batched: the autotuner's best whole-batch time (first call)   */
 } phde_layout_stats;
 
 /* optional extra outputs of phde_layout (any member may be NULL) */
@@ -128,6 +131,24 @@ int64_t phde_graph_nnz(const phde_ctx *ctx);
  * extra (optional): intermediate matrices.  stats (optional). */
 int phde_layout(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out, int64_t *sources_out,
                 phde_layout_extra *extra, phde_layout_stats *stats);
+
+/* ---- batched layouts: many independent graphs in one call ----
+ * Replaces a caller's loop of DrawingBase::run() + getCoordinates() over separate graphs
+ * (variants/DrawingBase.h:41-60; spectralDrawing.cpp:186-197 per graph).  phde_batch_upload copies the
+ * graphs (each its own CSR, local vertex ids; all with the same offset width) as one disjoint union;
+ * phde_layout_batched lays every graph out: ParHDE with Kcenters pivots, opts->precision PHDE_PREC_MIXED,
+ * opts->eig PHDE_EIG_EXACT, 2 <= k <= 32, c <= 4, every graph connected with more than 3k vertices.
+ * coords_out holds sum(n_b) * c doubles: graph b's coordinates, column-major (coordinate j of its local
+ * vertex i at i + j * n_b), start at c * (n_0 + ... + n_{b-1}).  The first call on a batch autotunes and
+ * captures the pipeline into a CUDA graph; later calls replay it. */
+typedef struct {
+  const void *offsets; /* n + 1 entries */
+  int offset_bytes;    /* 4 (uint32) or 8 (int64) */
+  const uint32_t *adj; /* nnz neighbour ids in 0..n-1 */
+  int64_t n, nnz;
+} phde_graph_desc;
+int phde_batch_upload(phde_ctx *ctx, const phde_graph_desc *graphs, int count);
+int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out, phde_layout_stats *stats);
 
 /* Exact distance columns from the given sources on the uploaded graph: hop counts (unweighted graph)
  * or weighted shortest-path lengths (weighted graph).  out: n*nsrc int32, column-major; unreachable

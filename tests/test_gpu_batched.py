@@ -1,0 +1,77 @@
+"""Batched layouts (phde_batch_upload + phde_layout_batched): many graphs in one call, against the same
+graphs laid out one at a time with the same options (Kcenters pivots, mixed precision, Jacobi)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from icpp_2020_parhde_gb300 import Context, ParHDEError, graphs
+from icpp_2020_parhde_gb300.csr_io import CSRGraph
+
+pytestmark = pytest.mark.gpu
+
+
+def rayleigh(g, X):
+    A = sp.csr_matrix((np.ones(g.nnz), g.adj.astype(np.int64), g.offsets.astype(np.int64)), shape=(g.n, g.n))
+    d = np.asarray(A.sum(axis=1)).ravel()
+    return np.einsum("ij,ij->j", X, d[:, None] * X - A @ X) / np.einsum("ij,ij->j", X, X)
+
+
+def principal_cosines(X, Y):
+    qx, _ = np.linalg.qr(X)
+    qy, _ = np.linalg.qr(Y)
+    return np.linalg.svd(qx.T @ qy, compute_uv=False)
+
+
+def batch_graphs():
+    return [graphs.rgg(3000, dim=2, avg_degree=8, seed=1), graphs.rgg(12000, dim=2, avg_degree=8, seed=2),
+            graphs.mesh(60, 50, seed=3), graphs.rgg(1500, dim=2, avg_degree=8, seed=4), graphs.rmat(12, seed=5),
+            graphs.rgg(25000, dim=2, avg_degree=8, seed=6), graphs.rgg(8000, dim=3, avg_degree=12, seed=7)]
+
+
+@pytest.mark.parametrize("k,c", [(10, 2), (20, 3)])
+def test_batched_matches_single_layouts(k, c):
+    gs = batch_graphs()
+    cb = Context(0)
+    cb.upload_batch(gs)
+    xs, st = cb.layout_batched(k, c)
+    assert st["naccepted"] == k and st["npasses"] == 3 * k
+    cs = Context(0)
+    for g, xb in zip(gs, xs):
+        cs.upload(g)
+        r = cs.layout("ParHDE", "Kcenters", k, c, precision="mixed", eig="exact")
+        np.testing.assert_allclose(np.linalg.norm(xb, axis=0), 1.0, rtol=1e-9)
+        np.testing.assert_allclose(rayleigh(g, xb), rayleigh(g, r.coords), rtol=1e-4)
+        assert principal_cosines(xb, r.coords).min() > 1 - 1e-5
+
+
+def test_batched_replay_is_deterministic():
+    gs = batch_graphs()[:4]
+    cb = Context(0)
+    cb.upload_batch(gs)
+    x1, s1 = cb.layout_batched(10, 2)
+    x2, s2 = cb.layout_batched(10, 2)
+    x3, s3 = cb.layout_batched(10, 2)
+    assert s1["batch_seg_rows"] == s2["batch_seg_rows"] > 0
+    assert s1["ms_batch_tune"] > 0 and s2["ms_batch_tune"] == 0  # tuned once per batch
+    for a, b, c in zip(x1, x2, x3):
+        assert np.array_equal(a, b) and np.array_equal(b, c)
+    # distances stay exact for the batch: a batched upload is an ordinary (disconnected) graph
+    d = cb.distances([0, gs[0].n])
+    assert (d[: gs[0].n, 0] >= 0).all() and (d[gs[0].n:, 0] == -1).all()
+
+
+def test_batched_rejects_bad_input():
+    good = graphs.rgg(2000, dim=2, avg_degree=8, seed=8)
+    cb = Context(0)
+    adj = good.adj.copy()
+    adj[5] = good.n  # a neighbour outside its own graph
+    bad = CSRGraph(good.offsets, adj, None)
+    with pytest.raises(ParHDEError) as e:
+        cb.upload_batch([good, bad])
+    assert e.value.status == -2  # PHDE_ERR_CSR
+    tiny = graphs.path_graph(20)
+    cb.upload_batch([good, tiny])
+    with pytest.raises(ParHDEError) as e:
+        cb.layout_batched(10, 2)  # 20 vertices <= 3k pivots
+    with pytest.raises(ParHDEError):
+        cb.layout_batched(40, 2)  # k above 32
