@@ -236,15 +236,19 @@ int phde_graph_upload(phde_ctx *ctx, const void *offsets, int offset_bytes, cons
     return phde_fail(ctx, PHDE_ERR_INVALID, "phde_graph_upload: n and nnz must be below 2^32");
   PHDE_CK(ctx, cudaSetDevice(ctx->device));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  if (n + 1 > (ctx->n ? ctx->n + 1 : 0) || !ctx->d_off) {
+  if (n + 1 > ctx->off_cap || !ctx->d_off) {
     cudaFree(ctx->d_off);
     ctx->d_off = nullptr;
+    ctx->off_cap = 0;
     PHDE_CK(ctx, cudaMalloc(&ctx->d_off, sizeof(int64_t) * (n + 1)));
+    ctx->off_cap = n + 1;
   }
-  if (nnz > ctx->nnz || !ctx->d_adj) {
+  if (nnz > ctx->adj_cap || !ctx->d_adj) {
     cudaFree(ctx->d_adj);
     ctx->d_adj = nullptr;
+    ctx->adj_cap = 0;
     PHDE_CK(ctx, cudaMalloc(&ctx->d_adj, sizeof(uint32_t) * std::max<int64_t>(nnz, 1)));
+    ctx->adj_cap = std::max<int64_t>(nnz, 1);
     cudaFree(ctx->d_w);
     ctx->d_w = nullptr;
   }
@@ -266,7 +270,7 @@ int phde_graph_upload(phde_ctx *ctx, const void *offsets, int offset_bytes, cons
     PHDE_CK(ctx, cudaMemcpyAsync(ctx->d_adj, adj, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, ctx->stream));
   ctx->weighted = weights != nullptr;
   if (weights) {
-    if (!ctx->d_w) PHDE_CK(ctx, cudaMalloc(&ctx->d_w, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+    if (!ctx->d_w) PHDE_CK(ctx, cudaMalloc(&ctx->d_w, sizeof(int32_t) * ctx->adj_cap));
     if (nnz > 0)
       PHDE_CK(ctx, cudaMemcpyAsync(ctx->d_w, weights, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, ctx->stream));
   }

@@ -394,20 +394,32 @@ extern "C" int phde_batch_upload(phde_ctx *ctx, const phde_graph_desc *graphs, i
   PHDE_CK(ctx, cudaSetDevice(ctx->device));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
   // device CSR of the union (grow-only, as phde_graph_upload)
-  cudaFree(ctx->d_off);
-  ctx->d_off = nullptr;
-  PHDE_CK(ctx, cudaMalloc(&ctx->d_off, sizeof(int64_t) * (N + 1)));
-  cudaFree(ctx->d_adj);
-  ctx->d_adj = nullptr;
-  PHDE_CK(ctx, cudaMalloc(&ctx->d_adj, sizeof(uint32_t) * std::max<int64_t>(E, 1)));
-  cudaFree(ctx->d_w);
-  ctx->d_w = nullptr;
+  if (N + 1 > ctx->off_cap || !ctx->d_off) {
+    cudaFree(ctx->d_off);
+    ctx->d_off = nullptr;
+    ctx->off_cap = 0;
+    PHDE_CK(ctx, cudaMalloc(&ctx->d_off, sizeof(int64_t) * (N + 1)));
+    ctx->off_cap = N + 1;
+  }
+  if (E > ctx->adj_cap || !ctx->d_adj) {
+    cudaFree(ctx->d_adj);
+    ctx->d_adj = nullptr;
+    ctx->adj_cap = 0;
+    PHDE_CK(ctx, cudaMalloc(&ctx->d_adj, sizeof(uint32_t) * std::max<int64_t>(E, 1)));
+    ctx->adj_cap = std::max<int64_t>(E, 1);
+    cudaFree(ctx->d_w);
+    ctx->d_w = nullptr;
+  }
+  if (N > ctx->gid_cap || !ctx->d_gid) {
+    cudaFree(ctx->d_gid);
+    ctx->d_gid = nullptr;
+    ctx->gid_cap = 0;
+    PHDE_CK(ctx, cudaMalloc(&ctx->d_gid, sizeof(int32_t) * N));
+    ctx->gid_cap = N;
+  }
   cudaFree(ctx->d_vbase);
   ctx->d_vbase = nullptr;
   PHDE_CK(ctx, cudaMalloc(&ctx->d_vbase, sizeof(int64_t) * 2 * (count + 1)));
-  cudaFree(ctx->d_gid);
-  ctx->d_gid = nullptr;
-  PHDE_CK(ctx, cudaMalloc(&ctx->d_gid, sizeof(int32_t) * N));
   const size_t ow = wide ? 8 : 4;
   unsigned char *staged = (unsigned char *)phde_buf(ctx, "batch.staged_off", ow * (size_t)(N + count));
   int *bad = (int *)phde_buf(ctx, "upload.bad", sizeof(int));
@@ -614,7 +626,14 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
     return PHDE_OK;
   };
   int rc;
-  const bool tune = ctx->batch_tuned_epoch != ctx->graph_epoch || ctx->batch_tuned_k != k;
+  // the tuned length is kept for batches of the same shape (count, vertices, entries, k); the captured
+  // graph is rebuilt after every upload (the device CSR may have moved)
+  const int64_t shape = ((int64_t)B * 1000003 + N) * 1000003 + ctx->nnz;
+  const bool tune = ctx->batch_tuned_shape != shape || ctx->batch_tuned_k != k;
+  if (ctx->batch_graph && ctx->batch_graph_epoch != ctx->graph_epoch) {
+    cudaGraphExecDestroy(ctx->batch_graph);
+    ctx->batch_graph = nullptr;
+  }
   if (tune) {
     static const int64_t kCandidates[] = {2048, 4096, 8192, 16384, 32768};
     float best = 1e30f;
@@ -633,7 +652,7 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
       }
     }
     ctx->batch_seg_rows = best_rows;
-    ctx->batch_tuned_epoch = ctx->graph_epoch;
+    ctx->batch_tuned_shape = shape;
     ctx->batch_tuned_k = k;
     ctx->batch_tune_ms = best;
     if (ctx->batch_graph) {
@@ -666,6 +685,7 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
       if (prc == PHDE_OK && ce == cudaSuccess && graph && ctx->ws_epoch == ws0 &&
           cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
         ctx->batch_graph = exec;
+        ctx->batch_graph_epoch = ctx->graph_epoch;
         ctx->batch_graph_c = key_c;
         ctx->batch_graph_ws = ctx->ws_epoch;
         ctx->batch_graph_launches = ctx->launches - l0;

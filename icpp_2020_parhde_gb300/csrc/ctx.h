@@ -20,14 +20,16 @@ struct phde_ctx {
   bool column_cgs2 = false;
   // uploaded batch (phde_batch_upload): the device CSR is the disjoint union of batch_B graphs
   int batch_B = 0;
+  int64_t off_cap = 0, adj_cap = 0, gid_cap = 0;   // allocated entries of d_off, d_adj (and d_w), d_gid
   std::vector<int64_t> batch_vbase, batch_ebase;  // host copies, batch_B + 1 entries
   int64_t *d_vbase = nullptr;                      // [batch_B + 1]
   int32_t *d_gid = nullptr;                        // [n]: graph of each vertex
-  int64_t batch_tuned_epoch = -1;                  // autotuned segment length for this graph epoch and k
+  int64_t batch_tuned_shape = -1;                  // autotuned segment length for this batch shape and k
   int batch_tuned_k = 0;
   int64_t batch_seg_rows = 8192;
   float batch_tune_ms = 0;
   cudaGraphExec_t batch_graph = nullptr;           // the captured batched pipeline
+  int64_t batch_graph_epoch = -1;
   int batch_graph_c = 0;
   int64_t batch_graph_ws = -1;
   int64_t batch_graph_launches = 0;

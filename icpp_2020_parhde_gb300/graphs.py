@@ -248,3 +248,12 @@ def relabel(g: CSRGraph, perm: np.ndarray) -> CSRGraph:
     w = g.weights[order] if g.weights is not None else None
     return CSRGraph(off.astype(np.uint32) if off[-1] < 2**32 else off, dst[order].astype(np.uint32), w,
                     g.name + "_relabelled")
+
+
+def rgg_batch(count: int = 512, nmin: int = 1000, nmax: int = 200_000, avg_degree: float = 8.0, seed: int = 1):
+    """`count` random geometric 2-D graphs with vertex counts log-uniform in [nmin, nmax], connection radius
+    for mean degree `avg_degree`, largest connected component kept (the batched-layout workload)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(nmin), math.log(nmax), size=count)).astype(np.int64)
+    seeds = rng.integers(1, 1 << 31, size=count)
+    return [rgg(int(n), dim=2, avg_degree=avg_degree, seed=int(s)) for n, s in zip(sizes, seeds)]
