@@ -129,21 +129,33 @@ __global__ void __launch_bounds__(GT) batch_gram_kernel(Seg sg, const float *A, 
   float acc[8];
 #pragma unroll
   for (int m = 0; m < 8; m++) acc[m] = 0.f;
+  // staging as in bcgs.cu: one column per thread, the next tile prefetched into registers
+  const int q = threadIdx.x % QCH, r1 = threadIdx.x / QCH;
+  const float cst = (q == nq && ones) ? 1.f : 0.f;
+  const int xi = threadIdx.x % BB, r2 = threadIdx.x / BB;
+  constexpr int NA = RT / (GT / QCH), NX = RT / (GT / BB);
+  float pa[NA], px[NX];
+  auto fetch = [&](int64_t r0) {
+#pragma unroll
+    for (int t = 0; t < NA; t++) {
+      const int64_t row = r0 + r1 + t * (GT / QCH);
+      pa[t] = row < re ? (q < nq ? A[row * lda + q] : cst) : 0.f;
+    }
+#pragma unroll
+    for (int t = 0; t < NX; t++) {
+      const int64_t row = r0 + r2 + t * (GT / BB);
+      px[t] = (row < re && xi < nb) ? Bm[row * ldb + xi] * (w ? (float)w[row] : 1.f) : 0.f;
+    }
+  };
+  if (rb < re) fetch(rb);
   for (int64_t r0 = rb; r0 < re; r0 += RT) {
     __syncthreads();
-    for (int idx = threadIdx.x; idx < RT * QCH; idx += GT) {
-      const int r = idx / QCH, q = idx % QCH;
-      const int64_t row = r0 + r;
-      float v = 0.f;
-      if (row < re) v = q < nq ? A[row * lda + q] : ((q == nq && ones) ? 1.f : 0.f);
-      At[r][q] = v;
-    }
-    for (int idx = threadIdx.x; idx < RT * BB; idx += GT) {
-      const int r = idx / BB, i = idx % BB;
-      const int64_t row = r0 + r;
-      Xt[r][i] = (row < re && i < nb) ? Bm[row * ldb + i] * (w ? (float)w[row] : 1.f) : 0.f;
-    }
+#pragma unroll
+    for (int t = 0; t < NA; t++) At[r1 + t * (GT / QCH)][q] = pa[t];
+#pragma unroll
+    for (int t = 0; t < NX; t++) Xt[r2 + t * (GT / BB)][xi] = px[t];
     __syncthreads();
+    if (r0 + RT < re) fetch(r0 + RT);
 #pragma unroll 4
     for (int rr = 0; rr < RT; rr++) {
       const float x = Xt[rr][lane];
@@ -200,6 +212,38 @@ __global__ void __launch_bounds__(GT) batch_update_kernel(Seg sg, const float *S
   }
 }
 
+// 32-term FP64 dot product with eight independent chains (GB300's FP64 pipe is narrow: dependent FMAs
+// serialise on its latency).
+__device__ __forceinline__ double dot32(const double *r, const double *v) {
+  double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0, a7 = 0;
+#pragma unroll
+  for (int l = 0; l < 32; l += 8) {
+    a0 = fma(r[l], v[l], a0);
+    a1 = fma(r[l + 1], v[l + 1], a1);
+    a2 = fma(r[l + 2], v[l + 2], a2);
+    a3 = fma(r[l + 3], v[l + 3], a3);
+    a4 = fma(r[l + 4], v[l + 4], a4);
+    a5 = fma(r[l + 5], v[l + 5], a5);
+    a6 = fma(r[l + 6], v[l + 6], a6);
+    a7 = fma(r[l + 7], v[l + 7], a7);
+  }
+  return ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+}
+
+// sum_{a < na} c[a] * R[a][m] with four chains.
+__device__ __forceinline__ double comb(const double *c, const double (*R)[33], int na, int m) {
+  double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  int a = 0;
+  for (; a + 3 < na; a += 4) {
+    s0 = fma(c[a], R[a][m], s0);
+    s1 = fma(c[a + 1], R[a + 1][m], s1);
+    s2 = fma(c[a + 2], R[a + 2][m], s2);
+    s3 = fma(c[a + 3], R[a + 3][m], s3);
+  }
+  for (; a < na; a++) s0 = fma(c[a], R[a][m], s0);
+  return (s0 + s1) + (s2 + s3);
+}
+
 // Per graph (one warp each): the coefficient-space accept/discard loop of bcgs.cu.
 // st[4b..]: [0] accepted so far, [1] discarded, [2] candidates consumed, [3] accepted in this block.
 __global__ void batch_block_gs_kernel(const double *Gall, int bc, int k, int rc0, int P, int *stall, double *dlog,
@@ -225,22 +269,14 @@ __global__ void batch_block_gs_kernel(const double *Gall, int bc, int k, int rc0
     for (int pass = 0; pass < 2 && nacc > 0; pass++) {
       tv[m] = t;
       __syncwarp();
-      if (m < nacc) {
-        double c0 = 0;
-        for (int l = 0; l < BB; l++) c0 = fma(Um[m][l], tv[l], c0);
-        cv[m] = c0 / dd[m];
-      }
+      if (m < nacc) cv[m] = dot32(Um[m], tv) / dd[m];
       __syncwarp();
-      double s0 = 0;
-      for (int a = 0; a < nacc; a++) s0 = fma(cv[a], Rm[a][m], s0);
-      t -= s0;
+      t -= comb(cv, Rm, nacc, m);
       __syncwarp();
     }
     tv[m] = t;
     __syncwarp();
-    double g = 0;
-    for (int l = 0; l < BB; l++) g = fma(sG2[m][l], tv[l], g);
-    const double nrm = sqrt(fmax(warp_sum(t * g), 0.0));
+    const double nrm = sqrt(fmax(warp_sum(t * dot32(sG2[m], tv)), 0.0));
     if (nrm < 0.001) {
       ndisc++;
       if (m == 0) dlog[(int64_t)b * P + rc0 + i] = nrm;
@@ -248,8 +284,7 @@ __global__ void batch_block_gs_kernel(const double *Gall, int bc, int k, int rc0
       const double r = t / nrm;
       tv[m] = r;
       __syncwarp();
-      double u = 0;
-      for (int l = 0; l < BB; l++) u = fma(sGd[m][l], tv[l], u);
+      const double u = dot32(sGd[m], tv);
       const double d = warp_sum(r * u);
       Rm[nacc][m] = r;
       Um[nacc][m] = u;

@@ -30,7 +30,8 @@ constexpr int BB = 32;       // candidates per block
 constexpr int GT = 256;      // threads of the Gram / update kernels
 constexpr int QCH = 64;      // Gram rows (basis columns) per CTA along grid.y
 constexpr int RT = 32;       // rows per staged tile
-constexpr int ST_LD = 36;    // row stride of the transposed S tile: 16-byte aligned, 4-way staging conflicts
+constexpr int ST_LD = 36;
+constexpr int RED_THREADS = 1024;  // cross-CTA reductions    // row stride of the transposed S tile: 16-byte aligned, 4-way staging conflicts
 
 // D[:, rc0 + c] / ||D[:, rc0 + c]|| into X[:, c] (row-major n x 32; columns >= bc are zero).
 __global__ void bcgs_load_kernel(const int32_t *D, int64_t n, int rc0, int bc, const ull *sumsq, float *X) {
@@ -66,21 +67,34 @@ __global__ void __launch_bounds__(GT) bcgs_gram_kernel(const float *A, int lda, 
   float acc[8];
 #pragma unroll
   for (int m = 0; m < 8; m++) acc[m] = 0.f;
+  // staging: thread -> one column of the tile, every GT/QCH-th row (coalesced, no index division); the next
+  // tile's values are loaded into registers while the current one is multiplied
+  const int q = threadIdx.x % QCH, r1 = threadIdx.x / QCH, qq = qbase + q;
+  const float cst = (qq == nq && ones) ? 1.f : 0.f;
+  const int xi = threadIdx.x % BB, r2 = threadIdx.x / BB;
+  constexpr int NA = RT / (GT / QCH), NX = RT / (GT / BB);
+  float pa[NA], px[NX];
+  auto fetch = [&](int64_t r0) {
+#pragma unroll
+    for (int t = 0; t < NA; t++) {
+      const int64_t row = r0 + r1 + t * (GT / QCH);
+      pa[t] = row < re ? (qq < nq ? A[row * lda + qq] : cst) : 0.f;
+    }
+#pragma unroll
+    for (int t = 0; t < NX; t++) {
+      const int64_t row = r0 + r2 + t * (GT / BB);
+      px[t] = row < re ? X[row * BB + xi] * (w ? (float)w[row] : 1.f) : 0.f;
+    }
+  };
+  if (rb < re) fetch(rb);
   for (int64_t r0 = rb; r0 < re; r0 += RT) {
     __syncthreads();
-    for (int idx = threadIdx.x; idx < RT * QCH; idx += GT) {
-      const int r = idx / QCH, q = idx % QCH, qq = qbase + q;
-      const int64_t row = r0 + r;
-      float v = 0.f;
-      if (row < re) v = qq < nq ? A[row * lda + qq] : ((qq == nq && ones) ? 1.f : 0.f);
-      At[r][q] = v;
-    }
-    for (int idx = threadIdx.x; idx < RT * BB; idx += GT) {
-      const int r = idx / BB, i = idx % BB;
-      const int64_t row = r0 + r;
-      Xt[r][i] = row < re ? X[row * BB + i] * (w ? (float)w[row] : 1.f) : 0.f;
-    }
+#pragma unroll
+    for (int t = 0; t < NA; t++) At[r1 + t * (GT / QCH)][q] = pa[t];
+#pragma unroll
+    for (int t = 0; t < NX; t++) Xt[r2 + t * (GT / BB)][xi] = px[t];
     __syncthreads();
+    if (r0 + RT < re) fetch(r0 + RT);
 #pragma unroll 4
     for (int rr = 0; rr < RT; rr++) {
       const float x = Xt[rr][lane];
@@ -105,13 +119,25 @@ __global__ void __launch_bounds__(GT) bcgs_gram_kernel(const float *A, int lda, 
 //   mode 0 (projection): C[q][i] = sum / <q, D q> for q < nq, sum / (n * den0) for q == nq (the constant
 //                        column's coefficient times its entry 1/sqrt(n)); FP32 out.
 //   mode 1 (block Gram): G[q][i] = sum, FP64 out.
-__global__ void bcgs_reduce_kernel(const float *part, int ncta, int nq, int mode, const double *dden, double n_den0,
-                                   float *C, double *G) {
-  __shared__ double red[GT / 32][BB];
+__global__ void __launch_bounds__(RED_THREADS) bcgs_reduce_kernel(const float *part, int ncta, int nq, int mode,
+                                                                  const double *dden, double n_den0, float *C,
+                                                                  double *G) {
+  __shared__ double red[RED_THREADS / 32][BB];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int q = blockIdx.x, y = q / QCH, qq = q % QCH;
-  double s = 0;
-  for (int c = warp; c < ncta; c += nw) s += (double)__ldcg(part + ((int64_t)(y * ncta + c) * QCH + qq) * BB + lane);
+  // four independent sums per thread (the partials come from L2: hide its latency), combined in order
+  const float *base = part + ((int64_t)y * ncta * QCH + qq) * BB + lane;
+  const int64_t cs = (int64_t)QCH * BB;
+  double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  int c = warp;
+  for (; c + 3 * nw < ncta; c += 4 * nw) {
+    s0 += (double)__ldcg(base + c * cs);
+    s1 += (double)__ldcg(base + (c + nw) * cs);
+    s2 += (double)__ldcg(base + (c + 2 * nw) * cs);
+    s3 += (double)__ldcg(base + (c + 3 * nw) * cs);
+  }
+  for (; c < ncta; c += nw) s0 += (double)__ldcg(base + c * cs);
+  const double s = (s0 + s1) + (s2 + s3);
   red[warp][lane] = s;
   __syncthreads();
   if (warp == 0) {
@@ -158,6 +184,38 @@ __global__ void __launch_bounds__(GT) bcgs_update_kernel(const float *S, int lda
   }
 }
 
+// 32-term FP64 dot product with eight independent chains (GB300's FP64 pipe is narrow: dependent FMAs
+// serialise on its latency).
+__device__ __forceinline__ double dot32(const double *r, const double *v) {
+  double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0, a7 = 0;
+#pragma unroll
+  for (int l = 0; l < 32; l += 8) {
+    a0 = fma(r[l], v[l], a0);
+    a1 = fma(r[l + 1], v[l + 1], a1);
+    a2 = fma(r[l + 2], v[l + 2], a2);
+    a3 = fma(r[l + 3], v[l + 3], a3);
+    a4 = fma(r[l + 4], v[l + 4], a4);
+    a5 = fma(r[l + 5], v[l + 5], a5);
+    a6 = fma(r[l + 6], v[l + 6], a6);
+    a7 = fma(r[l + 7], v[l + 7], a7);
+  }
+  return ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+}
+
+// sum_{a < na} c[a] * R[a][m] with four chains.
+__device__ __forceinline__ double comb(const double *c, const double (*R)[33], int na, int m) {
+  double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  int a = 0;
+  for (; a + 3 < na; a += 4) {
+    s0 = fma(c[a], R[a][m], s0);
+    s1 = fma(c[a + 1], R[a + 1][m], s1);
+    s2 = fma(c[a + 2], R[a + 2][m], s2);
+    s3 = fma(c[a + 3], R[a + 3][m], s3);
+  }
+  for (; a < na; a++) s0 = fma(c[a], R[a][m], s0);
+  return (s0 + s1) + (s2 + s3);
+}
+
 // The block's accept/discard loop in coefficient space (one warp, FP64).  Gd, G2 and the accepted vectors
 // r_a (with U_a = Gd r_a) sit in shared memory; every step is a 32 x 32 matrix-vector product with one
 // lane per output entry (no reductions across lanes):
@@ -185,33 +243,14 @@ __global__ void bcgs_block_gs_kernel(const double *Gd, const double *G2, int bc,
     for (int pass = 0; pass < 2 && nacc > 0; pass++) {
       tv[m] = t;
       __syncwarp();
-      if (m < nacc) {  // c_a = <t, U_a> / dd_a, all from the same t (classical)
-        double c0 = 0, c1 = 0;
-        for (int l = 0; l < BB; l += 2) {
-          c0 = fma(Um[m][l], tv[l], c0);
-          c1 = fma(Um[m][l + 1], tv[l + 1], c1);
-        }
-        cv[m] = (c0 + c1) / dd[m];
-      }
+      if (m < nacc) cv[m] = dot32(Um[m], tv) / dd[m];  // c_a = <t, U_a> / dd_a, all from the same t (classical)
       __syncwarp();
-      double s0 = 0, s1 = 0;
-      int a = 0;
-      for (; a + 1 < nacc; a += 2) {
-        s0 = fma(cv[a], Rm[a][m], s0);
-        s1 = fma(cv[a + 1], Rm[a + 1][m], s1);
-      }
-      if (a < nacc) s0 = fma(cv[a], Rm[a][m], s0);
-      t -= s0 + s1;
+      t -= comb(cv, Rm, nacc, m);
       __syncwarp();
     }
     tv[m] = t;
     __syncwarp();
-    double g0 = 0, g1 = 0;
-    for (int l = 0; l < BB; l += 2) {
-      g0 = fma(sG2[m][l], tv[l], g0);
-      g1 = fma(sG2[m][l + 1], tv[l + 1], g1);
-    }
-    const double nrm = sqrt(fmax(warp_sum(t * (g0 + g1)), 0.0));
+    const double nrm = sqrt(fmax(warp_sum(t * dot32(sG2[m], tv)), 0.0));
     if (nrm < 0.001) {
       ndisc++;
       if (m == 0) dlog[rc0 + i] = nrm;
@@ -219,12 +258,7 @@ __global__ void bcgs_block_gs_kernel(const double *Gd, const double *G2, int bc,
       const double r = t / nrm;
       tv[m] = r;
       __syncwarp();
-      double u0 = 0, u1 = 0;
-      for (int l = 0; l < BB; l += 2) {
-        u0 = fma(sGd[m][l], tv[l], u0);
-        u1 = fma(sGd[m][l + 1], tv[l + 1], u1);
-      }
-      const double u = u0 + u1;
+      const double u = dot32(sGd[m], tv);
       const double d = warp_sum(r * u);
       Rm[nacc][m] = r;
       Um[nacc][m] = u;
@@ -270,12 +304,21 @@ __global__ void __launch_bounds__(GT) bcgs_form_kernel(const float *X, const flo
   }
 }
 
-// <q, D q> of the block's new columns from the form kernel's partials (fixed order).
-__global__ void bcgs_dd_kernel(const double *part, int ncta, int nacc, int j0, double *dden) {
-  const int lane = threadIdx.x;
+// <q, D q> of the block's new columns from the form kernel's partials (fixed order: warp w sums CTAs
+// w, w + 32, ..., then the warps' sums are added in warp order).
+__global__ void __launch_bounds__(RED_THREADS) bcgs_dd_kernel(const double *part, int ncta, int nacc, int j0,
+                                                              double *dden) {
+  __shared__ double red[RED_THREADS / 32][BB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double t = 0;
-  for (int c = 0; c < ncta; c++) t += part[(int64_t)c * BB + lane];
-  if (lane < nacc) dden[j0 + lane] = t;
+  for (int c = warp; c < ncta; c += nw) t += part[(int64_t)c * BB + lane];
+  red[warp][lane] = t;
+  __syncthreads();
+  if (warp == 0) {
+    double u = 0;
+    for (int w = 0; w < nw; w++) u += red[w][lane];
+    if (lane < nacc) dden[j0 + lane] = u;
+  }
 }
 
 }  // namespace
@@ -313,7 +356,7 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
     for (int pass = 0; pass < 2; pass++) {
       bcgs_gram_kernel<<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
       PHDE_LAUNCHED(ctx);
-      bcgs_reduce_kernel<<<nqt, GT, 0, ctx->stream>>>(part, ncta, j, 0, dden, n_den0, C, nullptr);
+      bcgs_reduce_kernel<<<nqt, RED_THREADS, 0, ctx->stream>>>(part, ncta, j, 0, dden, n_den0, C, nullptr);
       PHDE_LAUNCHED(ctx);
       const size_t smem = sizeof(float) * ((size_t)nqt * BB + (size_t)j * ST_LD);
       bcgs_update_kernel<<<g_rows, GT, smem, ctx->stream>>>(S, k, j, C, X, n);
@@ -322,7 +365,7 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
     for (int wsel = 0; wsel < 2; wsel++) {
       bcgs_gram_kernel<<<dim3(ncta, 1), GT, 0, ctx->stream>>>(X, BB, BB, 0, X, wsel == 0 ? deg : nullptr, n, part);
       PHDE_LAUNCHED(ctx);
-      bcgs_reduce_kernel<<<BB, GT, 0, ctx->stream>>>(part, ncta, BB, 1, nullptr, 0.0, nullptr, G + wsel * BB * BB);
+      bcgs_reduce_kernel<<<BB, RED_THREADS, 0, ctx->stream>>>(part, ncta, BB, 1, nullptr, 0.0, nullptr, G + wsel * BB * BB);
       PHDE_LAUNCHED(ctx);
     }
     bcgs_block_gs_kernel<<<1, BB, 0, ctx->stream>>>(G, G + BB * BB, bc, k, rc0, st, dlog, R);
@@ -333,7 +376,7 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
     if (nacc > 0) {
       bcgs_form_kernel<<<ncta, GT, 0, ctx->stream>>>(X, R, nacc, S, k, j, deg, n, fpart);
       PHDE_LAUNCHED(ctx);
-      bcgs_dd_kernel<<<1, BB, 0, ctx->stream>>>(fpart, ncta, nacc, j, dden);
+      bcgs_dd_kernel<<<1, RED_THREADS, 0, ctx->stream>>>(fpart, ncta, nacc, j, dden);
       PHDE_LAUNCHED(ctx);
     }
     j = hst[0];

@@ -12,7 +12,9 @@
 //   part with the round-robin pairing, N/2 disjoint rotations per step; eigenvalues ascending; every
 //   eigenvector signed so that its largest-magnitude entry (lowest index on ties) is positive.
 // pick_kernel: eigenVectors columns for First (0..c-1) or Largest (N-1-j), DrawingBase.cpp:51-108.
+#include <algorithm>
 #include <cooperative_groups.h>
+#include <cstdio>
 #include <cstdlib>
 
 #include "ctx.h"
@@ -453,14 +455,14 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(const double *Kin, 
 // orthogonal to FP32 rounding), A is replaced by the exactly similar V^T A V computed in FP64, and FP64
 // sweeps (quadratically convergent from an off-diagonal of FP32 rounding size) finish with the same
 // convergence test as the global-memory kernel.  Everything lives in shared memory.
-constexpr int JS_MAX_N = 96;  // 24 N^2 bytes of shared memory: A64, V64 and one work matrix
+constexpr int JS_MAX_N = 96;  // 24 N (N|1) bytes of shared memory: A64, V64 and one work matrix
 
 template <typename T>
-__device__ void js_offnorm(const T *A, int N, double *red, double &off, double &tot) {
+__device__ void js_offnorm(const T *A, int N, int LD, double *red, double &off, double &tot) {
   double o = 0, t = 0;
   for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
-    const double a = (double)A[idx];
+    const double a = (double)A[i + j * LD];
     t += a * a;
     if (i != j) o += a * a;
   }
@@ -468,13 +470,35 @@ __device__ void js_offnorm(const T *A, int N, double *red, double &off, double &
   tot = block_sum(t, red);
 }
 
-// One cyclic sweep (M-1 rounds of M/2 disjoint rotations, circle-method pairing) on A and V.
+// Square root and absolute value in T's own precision (the float overloads must not widen to double).
+__device__ __forceinline__ float js_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double js_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float js_abs(float x) { return fabsf(x); }
+__device__ __forceinline__ double js_abs(double x) { return fabs(x); }
+
+// Slot i of the circle method after r rounds: slot 0 holds element 0; slots 1..M-1 hold a rotation of
+// elements 1..M-1 (one step per round), so after r rounds slot i holds ((i - 1 - r) mod (M-1)) + 1.
+__device__ __forceinline__ int js_slot(int i, int r, int M) {
+  if (i == 0) return 0;
+  const int x = (i - 1 - r) % (M - 1);
+  return (x < 0 ? x + (M - 1) : x) + 1;
+}
+
+// One cyclic sweep (M-1 rounds of M/2 disjoint rotations, circle-method pairing) on A and V.  The pairs
+// of round r are (slot m, slot M-1-m); the pairing is the global kernel's, computed in closed form.
 template <typename T>
-__device__ void js_sweep(T *A, T *V, int N, int M, int *s_order, double *s_cs, double *s_sn, int *s_p, int *s_q) {
+__device__ void js_sweep(T *A, T *V, int N, int LD, int M, int *s_order, double *s_cs_d, double *s_sn_d, int *s_p,
+                         int *s_q) {
   const int tid = threadIdx.x;
+  (void)s_order;
+  // the rotation parameters stay in T: a double <-> float conversion per element would run on the FP64 pipe
+  T *s_cs = (T *)s_cs_d, *s_sn = (T *)s_sn_d;
   for (int round = 0; round < M - 1; round++) {
-    for (int m = tid; m < M / 2; m += blockDim.x) {
-      int p = s_order[m], q = s_order[M - 1 - m];
+    // pair m's parameters on warp m % 4 (spreads the FP64 square roots and divisions over the SM's
+    // four schedulers)
+    const int m = (tid & 31) * 4 + (tid >> 5);
+    if (tid < 128 && m < M / 2) {
+      int p = js_slot(m, round, M), q = js_slot(M - 1 - m, round, M);
       if (p > q) {
         const int t = p;
         p = q;
@@ -482,55 +506,54 @@ __device__ void js_sweep(T *A, T *V, int N, int M, int *s_order, double *s_cs, d
       }
       T cs = (T)1, sn = (T)0;
       if (q < N) {
-        const T apq = A[p + q * N];
+        const T apq = A[p + q * LD];
         if (apq != (T)0) {
-          const T app = A[p + p * N], aqq = A[q + q * N];
+          const T app = A[p + p * LD], aqq = A[q + q * LD];
           const T theta = (aqq - app) / ((T)2 * apq);
-          const T t = (theta >= (T)0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt(theta * theta + (T)1));
-          cs = (T)1 / sqrt(t * t + (T)1);
+          const T t = (theta >= (T)0 ? (T)1 : (T)-1) / (js_abs(theta) + js_sqrt(theta * theta + (T)1));
+          cs = (T)1 / js_sqrt(t * t + (T)1);
           sn = t * cs;
         }
       }
       s_p[m] = p;
       s_q[m] = q;
-      s_cs[m] = (double)cs;
-      s_sn[m] = (double)sn;
+      s_cs[m] = cs;
+      s_sn[m] = sn;
     }
     __syncthreads();
     for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
-      const int m = idx / N, row = idx % N;
-      const int p = s_p[m], q = s_q[m];
-      if (q >= N || s_sn[m] == 0.0) continue;
-      const T cs = (T)s_cs[m], sn = (T)s_sn[m];
-      const T akp = A[row + p * N], akq = A[row + q * N];
-      A[row + p * N] = cs * akp - sn * akq;
-      A[row + q * N] = sn * akp + cs * akq;
-      const T vkp = V[row + p * N], vkq = V[row + q * N];
-      V[row + p * N] = cs * vkp - sn * vkq;
-      V[row + q * N] = sn * vkp + cs * vkq;
+      const int mm = idx / N, row = idx % N;
+      const int p = s_p[mm], q = s_q[mm];
+      const T cs = s_cs[mm], sn = s_sn[mm];
+      if (q >= N || sn == (T)0) continue;
+      const T akp = A[row + p * LD], akq = A[row + q * LD];
+      A[row + p * LD] = cs * akp - sn * akq;
+      A[row + q * LD] = sn * akp + cs * akq;
+      const T vkp = V[row + p * LD], vkq = V[row + q * LD];
+      V[row + p * LD] = cs * vkp - sn * vkq;
+      V[row + q * LD] = sn * vkp + cs * vkq;
     }
     __syncthreads();
     for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
-      const int m = idx / N, col = idx % N;
-      const int p = s_p[m], q = s_q[m];
-      if (q >= N || s_sn[m] == 0.0) continue;
-      const T cs = (T)s_cs[m], sn = (T)s_sn[m];
-      const T apk = A[p + col * N], aqk = A[q + col * N];
-      A[p + col * N] = cs * apk - sn * aqk;
-      A[q + col * N] = sn * apk + cs * aqk;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      const int last = s_order[M - 1];
-      for (int i = M - 1; i > 1; i--) s_order[i] = s_order[i - 1];
-      s_order[1] = last;
+      const int mm = idx / N, col = idx % N;
+      const int p = s_p[mm], q = s_q[mm];
+      const T cs = s_cs[mm], sn = s_sn[mm];
+      if (q >= N || sn == (T)0) continue;
+      const T apk = A[p + col * LD], aqk = A[q + col * LD];
+      A[p + col * LD] = cs * apk - sn * aqk;
+      A[q + col * LD] = sn * apk + cs * aqk;
     }
     __syncthreads();
   }
 }
 
 __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *Kin, int N, double *K, double *evals,
-                                                                  int *sweeps, int *status, int max_sweeps) {
+                                                                  int *sweeps, int *status, int max_sweeps,
+                                                                  unsigned long long *trace, int c_target,
+                                                                  int largest) {
+#define JS_MARK(i)                                              \
+  if (trace && blockIdx.x == 0 && threadIdx.x == 0) trace[i] = global_timer_ns();
+  JS_MARK(0)
   extern __shared__ double js[];
   // a batch of problems: block b solves matrix b (N*N apart), with its own evals, sweeps and status
   Kin += (int64_t)blockIdx.x * N * N;
@@ -538,8 +561,10 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   evals += (int64_t)blockIdx.x * N;
   sweeps += blockIdx.x;
   status += blockIdx.x;
-  double *A = js, *V = js + N * N, *W = js + 2 * N * N;
-  float *A32 = (float *)W, *V32 = (float *)W + N * N;
+  // leading dimension LD = N | 1 (odd): the transposed accesses of a rotation's rows spread over all banks
+  const int LD = N | 1;
+  double *A = js, *V = js + N * LD, *W = js + 2 * N * LD;
+  float *A32 = (float *)W, *V32 = (float *)W + N * LD;
   __shared__ double red[32];
   __shared__ double s_cs[JS_MAX_N / 2 + 1], s_sn[JS_MAX_N / 2 + 1], s_d[JS_MAX_N];
   __shared__ int s_p[JS_MAX_N / 2 + 1], s_q[JS_MAX_N / 2 + 1];
@@ -550,9 +575,9 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   for (int idx = tid; idx < N * N; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
     const double a = 0.5 * (Kin[i + j * N] + Kin[j + i * N]);
-    A[idx] = a;
-    A32[idx] = (float)a;
-    V32[idx] = i == j ? 1.f : 0.f;
+    A[i + j * LD] = a;
+    A32[i + j * LD] = (float)a;
+    V32[i + j * LD] = i == j ? 1.f : 0.f;
   }
   for (int i = tid; i < M; i += blockDim.x) s_order[i] = i;
   __syncthreads();
@@ -560,83 +585,226 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   int sw32 = 0;
   double off = 0, tot = 0;
   for (; sw32 < 16; sw32++) {
-    js_offnorm(A32, N, red, off, tot);
+    js_offnorm(A32, N, LD, red, off, tot);
     if (tid == 0) s_done = off <= 1e-11 * tot;
     __syncthreads();
     if (s_done) break;
-    js_sweep<float>(A32, V32, N, M, s_order, s_cs, s_sn, s_p, s_q);
+    js_sweep<float>(A32, V32, N, LD, M, s_order, s_cs, s_sn, s_p, s_q);
   }
-  // ---- V = FP64 orthonormalisation of V32 (classical Gram-Schmidt, column order) ----
-  for (int idx = tid; idx < N * N; idx += blockDim.x) V[idx] = (double)V32[idx];
+  JS_MARK(1)
+  // ---- V = FP64 orthonormalisation of V32: V (V^T V)^(-1/2) to first order, V (I - E/2) with
+  //      E = V^T V - I (|E| ~ FP32 rounding, so the neglected 3/8 E^2 is ~1e-14): two parallel products ----
+  for (int idx = tid; idx < N * N; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    V[i + j * LD] = (double)V32[i + j * LD];
+  }
   __syncthreads();
-  for (int j = 0; j < N; j++) {
-    for (int i = warp; i < j; i += nw) {  // s_d[i] = <V_i, V_j>
-      double d = 0;
-      for (int r = lane; r < N; r += 32) d = fma(V[r + i * N], V[r + j * N], d);
-      d = warp_sum(d);
-      if (lane == 0) s_d[i] = d;
+  for (int idx = tid; idx < N * N; idx += blockDim.x) {  // W = E
+    const int i = idx % N, j = idx / N;
+    double e0 = 0, e1 = 0;
+    int r = 0;
+    for (; r + 1 < N; r += 2) {
+      e0 = fma(V[r + i * LD], V[r + j * LD], e0);
+      e1 = fma(V[r + 1 + i * LD], V[r + 1 + j * LD], e1);
     }
-    __syncthreads();
-    for (int r = tid; r < N; r += blockDim.x) {
-      double v = V[r + j * N];
-      for (int i = 0; i < j; i++) v = fma(-s_d[i], V[r + i * N], v);
-      V[r + j * N] = v;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      double d = 0;
-      for (int r = lane; r < N; r += 32) d = fma(V[r + j * N], V[r + j * N], d);
-      d = warp_sum(d);
-      if (lane == 0) s_d[j] = 1.0 / sqrt(d);
-    }
-    __syncthreads();
-    for (int r = tid; r < N; r += blockDim.x) V[r + j * N] *= s_d[j];
-    __syncthreads();
+    if (r < N) e0 = fma(V[r + i * LD], V[r + j * LD], e0);
+    W[i + j * LD] = (e0 + e1) - (i == j ? 1.0 : 0.0);
   }
+  __syncthreads();
+  {
+    constexpr int PER = (JS_MAX_N * JS_MAX_N + EIG_THREADS - 1) / EIG_THREADS;
+    double nv[PER];
+    int cnt = 0;
+    for (int idx = tid; idx < N * N; idx += blockDim.x, cnt++) {  // V(I - E/2), held until every read is done
+      const int r = idx % N, j = idx / N;
+      double s0 = 0, s1 = 0;
+      int l = 0;
+      for (; l + 1 < N; l += 2) {
+        s0 = fma(V[r + l * LD], W[l + j * LD], s0);
+        s1 = fma(V[r + (l + 1) * LD], W[l + 1 + j * LD], s1);
+      }
+      if (l < N) s0 = fma(V[r + l * LD], W[l + j * LD], s0);
+      nv[cnt] = V[r + j * LD] - 0.5 * (s0 + s1);
+    }
+    __syncthreads();
+    cnt = 0;
+    for (int idx = tid; idx < N * N; idx += blockDim.x, cnt++) V[idx % N + (idx / N) * LD] = nv[cnt];
+  }
+  __syncthreads();
+  JS_MARK(2)
   // ---- A <- V^T A V in FP64 (W = A V, then A = V^T W, symmetrised) ----
   for (int idx = tid; idx < N * N; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
-    double s = 0;
-    for (int l = 0; l < N; l++) s = fma(A[i + l * N], V[l + j * N], s);
-    W[idx] = s;
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int l = 0;
+    for (; l + 3 < N; l += 4) {
+      s0 = fma(A[i + l * LD], V[l + j * LD], s0);
+      s1 = fma(A[i + (l + 1) * LD], V[l + 1 + j * LD], s1);
+      s2 = fma(A[i + (l + 2) * LD], V[l + 2 + j * LD], s2);
+      s3 = fma(A[i + (l + 3) * LD], V[l + 3 + j * LD], s3);
+    }
+    for (; l < N; l++) s0 = fma(A[i + l * LD], V[l + j * LD], s0);
+    W[i + j * LD] = (s0 + s1) + (s2 + s3);
   }
   __syncthreads();
   for (int idx = tid; idx < N * N; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
     if (i > j) continue;
-    double s = 0, t = 0;
-    for (int l = 0; l < N; l++) {
-      s = fma(V[l + i * N], W[l + j * N], s);
-      t = fma(V[l + j * N], W[l + i * N], t);
+    double s0 = 0, s1 = 0, t0 = 0, t1 = 0;
+    int l = 0;
+    for (; l + 1 < N; l += 2) {
+      s0 = fma(V[l + i * LD], W[l + j * LD], s0);
+      s1 = fma(V[l + 1 + i * LD], W[l + 1 + j * LD], s1);
+      t0 = fma(V[l + j * LD], W[l + i * LD], t0);
+      t1 = fma(V[l + 1 + j * LD], W[l + 1 + i * LD], t1);
     }
-    s = 0.5 * (s + t);
+    if (l < N) {
+      s0 = fma(V[l + i * LD], W[l + j * LD], s0);
+      t0 = fma(V[l + j * LD], W[l + i * LD], t0);
+    }
+    const double s = 0.5 * ((s0 + s1) + (t0 + t1));
     // A is read by the W pass only, which finished at the barrier above
-    A[i + j * N] = s;
-    A[j + i * N] = s;
+    A[i + j * LD] = s;
+    A[j + i * LD] = s;
   }
   for (int i = tid; i < M; i += blockDim.x) s_order[i] = i;
   __syncthreads();
-  // ---- FP64 sweeps ----
-  int sw64 = 0;
-  for (; sw64 < max_sweeps; sw64++) {
-    js_offnorm(A, N, red, off, tot);
-    if (tid == 0) s_done = (off <= 1e-28 * tot) || off == 0.0;
-    __syncthreads();
-    if (s_done) break;
-    js_sweep<double>(A, V, N, M, s_order, s_cs, s_sn, s_p, s_q);
+  JS_MARK(3)
+  // ---- FP64 refinement.  A = V^T A V is exactly similar and off-diagonal to FP32 rounding.  When every
+  //      pair is well separated (|a_ij| <= 1e-3 |a_ii - a_jj|), perturbation theory finishes the job:
+  //      eigenvalues a_ii + sum_j a_ij^2 / (a_ii - a_jj) (error ~ off^3 / gap^2), eigenvectors e_i +
+  //      sum_j a_ji / (lambda_i - a_jj) e_j, and for the c wanted ones two more fixed-point steps of
+  //      (A - lambda_i) y = 0 with y_i = 1 (each gains a factor ~ off / gap).  Otherwise FP64 Jacobi
+  //      sweeps. ----
+  __shared__ double s_lam[JS_MAX_N];
+  __shared__ int s_bad;
+  if (tid == 0) s_bad = c_target * N > EIG_THREADS;  // one refined entry per thread at most
+  __syncthreads();
+  for (int idx = tid; idx < N * N; idx += blockDim.x) {
+    const int i = idx % N, j = idx / N;
+    if (i < j && !(fabs(A[i + j * LD]) <= 1e-3 * fabs(A[i + i * LD] - A[j + j * LD]))) s_bad = 1;
   }
-  if (sw64 == max_sweeps) js_offnorm(A, N, red, off, tot);
-  if (tid == 0) {
-    for (int i = 0; i < N; i++) s_order[i] = i;
-    for (int i = 0; i < N; i++) {
-      int b = i;
-      for (int j = i + 1; j < N; j++)
-        if (A[s_order[j] + s_order[j] * N] < A[s_order[b] + s_order[b] * N]) b = j;
-      const int t = s_order[i];
-      s_order[i] = s_order[b];
-      s_order[b] = t;
+  __syncthreads();
+  int sw64 = 0;
+  const double *Vout = V;  // eigenvector columns (unsorted), V itself after sweeps
+  if (!s_bad) {
+    for (int i = tid; i < N; i += blockDim.x) {
+      const double aii = A[i + i * LD];
+      double l0 = 0, l1 = 0;
+      for (int j = 0; j < N; j++) {
+        if (j == i) continue;
+        const double aij = A[i + j * LD];
+        const double t = aij * aij / (aii - A[j + j * LD]);
+        if (j & 1) l1 += t; else l0 += t;
+      }
+      s_lam[i] = aii + (l0 + l1);
     }
-    for (int c = 0; c < N; c++) evals[c] = A[s_order[c] + s_order[c] * N];
+    __syncthreads();
+    for (int idx = tid; idx < N * N; idx += blockDim.x) {  // W[:, i] = y_i to first order
+      const int j = idx % N, i = idx / N;
+      W[j + i * LD] = j == i ? 1.0 : A[j + i * LD] / (s_lam[i] - A[j + j * LD]);
+    }
+    __syncthreads();
+    // ranks of the eigenvalues: the wanted columns are the c smallest (or largest)
+    for (int i = tid; i < N; i += blockDim.x) {
+      const double li = s_lam[i];
+      int rank = 0;
+      for (int j = 0; j < N; j++) {
+        const double lj = s_lam[j];
+        rank += (lj < li) || (lj == li && j < i);
+      }
+      s_order[rank] = i;
+    }
+    __syncthreads();
+    for (int it = 0; it < 2; it++) {
+      // new y_j for j != i from the current y (computed into registers, written after a barrier)
+      double ny[(JS_MAX_N * 4 + EIG_THREADS - 1) / EIG_THREADS];
+      int cnt = 0;
+      for (int idx = tid; idx < N * c_target; idx += blockDim.x, cnt++) {
+        const int j = idx % N, ti = idx / N;
+        const int i = s_order[largest ? N - 1 - ti : ti];
+        double v = 1.0;
+        if (j != i) {
+          double s0 = 0, s1 = 0;
+          for (int l = 0; l < N; l++) {
+            if (l == j) continue;
+            const double t = A[j + l * LD] * W[l + i * LD];
+            if (l & 1) s1 += t; else s0 += t;
+          }
+          v = -(s0 + s1) / (A[j + j * LD] - s_lam[i]);
+        }
+        ny[cnt] = v;
+      }
+      __syncthreads();
+      cnt = 0;
+      for (int idx = tid; idx < N * c_target; idx += blockDim.x, cnt++) {
+        const int j = idx % N, ti = idx / N;
+        const int i = s_order[largest ? N - 1 - ti : ti];
+        W[j + i * LD] = ny[cnt];
+      }
+      __syncthreads();
+      for (int ti = tid; ti < c_target; ti += blockDim.x) {  // lambda_i = a_ii + sum_{l != i} a_il y_l
+        const int i = s_order[largest ? N - 1 - ti : ti];
+        double s0 = 0;
+        for (int l = 0; l < N; l++)
+          if (l != i) s0 = fma(A[i + l * LD], W[l + i * LD], s0);
+        s_lam[i] = A[i + i * LD] + s0;
+      }
+      __syncthreads();
+    }
+    // eigenvectors of the original matrix: V y_i, normalised (A is no longer needed: it takes them)
+    for (int idx = tid; idx < N * N; idx += blockDim.x) {
+      const int r = idx % N, i = idx / N;
+      double s0 = 0, s1 = 0;
+      int l = 0;
+      for (; l + 1 < N; l += 2) {
+        s0 = fma(V[r + l * LD], W[l + i * LD], s0);
+        s1 = fma(V[r + (l + 1) * LD], W[l + 1 + i * LD], s1);
+      }
+      if (l < N) s0 = fma(V[r + l * LD], W[l + i * LD], s0);
+      A[r + i * LD] = s0 + s1;
+    }
+    __syncthreads();
+    for (int i = warp; i < N; i += nw) {
+      double d = 0;
+      for (int r = lane; r < N; r += 32) d = fma(A[r + i * LD], A[r + i * LD], d);
+      d = warp_sum(d);
+      const double inv = 1.0 / sqrt(d);
+      for (int r = lane; r < N; r += 32) A[r + i * LD] *= inv;
+    }
+    __syncthreads();
+    Vout = A;
+    off = 0;
+    tot = 1;
+  } else {
+    for (; sw64 < max_sweeps; sw64++) {
+      js_offnorm(A, N, LD, red, off, tot);
+      if (tid == 0) s_done = (off <= 1e-24 * tot) || off == 0.0;
+      __syncthreads();
+      if (s_done) break;
+      js_sweep<double>(A, V, N, LD, M, s_order, s_cs, s_sn, s_p, s_q);
+    }
+    if (sw64 == max_sweeps) js_offnorm(A, N, LD, red, off, tot);
+    for (int i = tid; i < N; i += blockDim.x) s_lam[i] = A[i + i * LD];
+    __syncthreads();
+  }
+  JS_MARK(4)
+  if (trace && blockIdx.x == 0 && threadIdx.x == 0) {
+    trace[6] = sw32;
+    trace[7] = s_bad ? sw64 : 1000;  // 1000: refined by perturbation
+  }
+  // ascending order of the eigenvalues, ties by index (the stable order): rank of each entry, in parallel
+  for (int i = tid; i < N; i += blockDim.x) {
+    const double li = s_lam[i];
+    int rank = 0;
+    for (int j = 0; j < N; j++) {
+      const double lj = s_lam[j];
+      rank += (lj < li) || (lj == li && j < i);
+    }
+    s_order[rank] = i;
+    evals[rank] = li;
+  }
+  if (tid == 0) {
     *sweeps = sw32 + sw64;
     *status = (sw64 < max_sweeps || off <= 1e-20 * tot) ? PHDE_OK : PHDE_ERR_NOCONVERGE;
   }
@@ -646,7 +814,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
     double best = -1.0;
     int arg = 0;
     for (int i = lane; i < N; i += 32) {
-      const double a = fabs(V[i + src * N]);
+      const double a = fabs(Vout[i + src * LD]);
       if (a > best) {
         best = a;
         arg = i;
@@ -660,9 +828,12 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
         arg = a2;
       }
     }
-    const double sg = V[arg + src * N] < 0 ? -1.0 : 1.0;
-    for (int i = lane; i < N; i += 32) K[i + c * N] = sg * V[i + src * N];
+    const double sg = Vout[arg + src * LD] < 0 ? -1.0 : 1.0;
+    for (int i = lane; i < N; i += 32) K[i + c * N] = sg * Vout[i + src * LD];
   }
+  __syncthreads();
+  JS_MARK(5)
+#undef JS_MARK
 }
 
 __global__ void pick_kernel(const double *K, int N, int c, int largest, double *Y) {
@@ -689,9 +860,21 @@ int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest,
   PHDE_CK(ctx, cudaMemsetAsync(st, 0, sizeof(int) * 2, ctx->stream));
   if (eig == PHDE_EIG_EXACT) {
     if (N <= JS_MAX_N && !getenv("PHDE_JACOBI_GLOBAL")) {
-      const size_t jsmem = sizeof(double) * 3 * (size_t)N * N;
+      const size_t jsmem = sizeof(double) * 3 * (size_t)N * (N | 1);
       PHDE_CK(ctx, cudaFuncSetAttribute(jacobi_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
-      jacobi_smem_kernel<<<1, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, st, st + 1, 100);
+      // PHDE_EIG_TRACE=1: print the kernel's phase timeline (FP32 sweeps, orthonormalisation, similarity,
+      // FP64 sweeps, sort) after the solve
+      unsigned long long *tr = getenv("PHDE_EIG_TRACE") ? (unsigned long long *)phde_buf(ctx, "eig.trace", 64) : nullptr;
+      jacobi_smem_kernel<<<1, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, st, st + 1, 100, tr,
+                                                                  c, largest);
+      if (tr) {
+        unsigned long long h[8];
+        PHDE_CK(ctx, cudaMemcpyAsync(h, tr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+        PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        fprintf(stderr, "jacobi N=%d: fp32 sweeps %llu: %.1f us, orthonormalise %.1f us, similarity %.1f us, "
+                        "fp64 sweeps %llu: %.1f us, sort/sign %.1f us\n", N, h[6], (h[1] - h[0]) * 1e-3,
+                (h[2] - h[1]) * 1e-3, (h[3] - h[2]) * 1e-3, h[7], (h[4] - h[3]) * 1e-3, (h[5] - h[4]) * 1e-3);
+      }
     } else {
       jacobi_kernel<<<1, EIG_THREADS, 0, ctx->stream>>>(d_M, N, w1, w2, d_K, d_evals, st, st + 1, 100);
     }
@@ -727,9 +910,10 @@ int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest,
 int phde_eigensolve_batched(phde_ctx *ctx, const double *d_M, int N, int c, int count, double *d_K,
                             double *d_evals, double *d_Y, int *d_st) {
   if (N > JS_MAX_N) return phde_fail(ctx, PHDE_ERR_INVALID, "batched eigensolve: k above the shared-memory limit");
-  const size_t jsmem = sizeof(double) * 3 * (size_t)N * N;
+  const size_t jsmem = sizeof(double) * 3 * (size_t)N * (N | 1);
   PHDE_CK(ctx, cudaFuncSetAttribute(jacobi_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
-  jacobi_smem_kernel<<<count, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, d_st, d_st + count, 100);
+  jacobi_smem_kernel<<<count, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, d_st, d_st + count, 100,
+                                                                  nullptr, c, 0);
   PHDE_LAUNCHED(ctx);
   pick_kernel<<<count, 256, 0, ctx->stream>>>(d_K, N, c, 0, d_Y);
   PHDE_LAUNCHED(ctx);

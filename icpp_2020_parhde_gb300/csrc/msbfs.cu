@@ -48,6 +48,10 @@ struct MsArgs {
   int *levels_out;
   ull *trace;                 // optional [2*trace_cap]: per level end time (ns) and vertices given new bits
   int trace_cap;
+  uint32_t *done;             // [n/32] bitmap: saturated with both frontier words zero (or a hub row): skipped
+  uint32_t *touched;          // [n/32] bitmap of level 1's candidates (neighbours of the sources), zeroed
+  uint32_t *tlist;            // [n] those candidates, in claim order
+  unsigned *tcount;           // [1]
   GridSync *gs;
   int *err;
   uint64_t timeout_ns;
@@ -132,12 +136,73 @@ __device__ __forceinline__ bool ms_thread_finalise(const MsArgs &a, int64_t v, c
   return any;
 }
 
+// One vertex v pulled by its MS_GROUP-lane group (gl = lane in group): OR of the neighbours' frontier words,
+// new bits finalised.  Every lane of the warp must call it (the group shuffles are warp-wide); lanes whose
+// group has no vertex pass act = false.  Returns through `newbits` whether v got new bits (group leader).
+template <int W>
+__device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full)[W], const ull *fcur, ull *fnext,
+                                               int32_t L, int64_t v, bool act, int gl, bool mark_done,
+                                               bool &newbits) {
+  newbits = false;
+  int64_t e0 = 0, e1 = 0;
+  if (act) {
+    e0 = a.off[v];
+    e1 = a.off[v + 1];
+    if (e1 - e0 > MS_HEAVY) act = false;  // hub rows go by chunks
+  }
+  ull s[W];
+  bool sat = true;
+#pragma unroll
+  for (int w = 0; w < W; w++) s[w] = 0ull;
+  if (act) {
+    ld_words<W>(a.seen + v * W, s);
+#pragma unroll
+    for (int w = 0; w < W; w++) sat &= (s[w] == full[w]);
+  }
+  ull acc[W];
+#pragma unroll
+  for (int w = 0; w < W; w++) acc[w] = 0ull;
+  if (act && !sat)
+    for (int64_t e = e0 + gl; e < e1; e += 2 * MS_GROUP) {
+      const int64_t e2 = e + MS_GROUP;
+      const uint32_t u0 = __ldg(a.adj + e);
+      const uint32_t u1 = e2 < e1 ? __ldg(a.adj + e2) : u0;
+      ull x0[W], x1[W];
+      ld_words<W>(fcur + (int64_t)u0 * W, x0);
+      ld_words<W>(fcur + (int64_t)u1 * W, x1);
+#pragma unroll
+      for (int w = 0; w < W; w++) acc[w] |= x0[w] | x1[w];
+    }
+#pragma unroll
+  for (int w = 0; w < W; w++)
+#pragma unroll
+    for (int o = MS_GROUP / 2; o > 0; o >>= 1) acc[w] |= __shfl_xor_sync(PHDE_FULL_MASK, acc[w], o, MS_GROUP);
+  // every lane of the group read `seen` above, before the shuffles; the writes come after them
+  if (act) {
+    if (sat) {
+      // saturated: clear this level's output word; once the current word is empty too, the vertex is
+      // finished for the rest of the sweep
+      ull cur[W];
+      ld_words<W>(fcur + v * W, cur);
+      bool empty = true;
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        if (w == gl) fnext[v * W + w] = 0ull;
+        empty &= cur[w] == 0ull;
+      }
+      if (mark_done && empty && gl == 0) atomicOr(a.done + (v >> 5), 1u << (v & 31));
+    } else if (ms_group_finalise<W>(a, v, acc, s, fnext, L, gl) && gl == 0) {
+      newbits = true;
+    }
+  }
+}
+
 template <int W>
 __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
   __shared__ unsigned s_cnt;
   const int64_t n = a.n;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, gl = lane & (MS_GROUP - 1), grp = lane / MS_GROUP;
   const int64_t gw = gt >> 5, gws = gts >> 5;
   // full mask of the valid source bits per word
   ull full[W];
@@ -146,7 +211,7 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
     const int bits = a.nsrc - 64 * w;
     full[w] = bits >= 64 ? ~0ull : (bits <= 0 ? 0ull : ((1ull << bits) - 1ull));
   }
-  // level 0: every source sees itself
+  // level 0: every source sees itself; hub rows never enter the light pull (their bit in `done`)
   if (gt == 0)
     for (int b = 0; b < a.nsrc; b++) {
       const int64_t s = a.src[b];
@@ -154,6 +219,29 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
       atomicOr(a.front[0] + s * W + (b >> 6), 1ull << (b & 63));
       a.R[s * a.RW + a.col0 + b] = 1;  // level 0
     }
+  for (int64_t h = gt; h < a.nheavy; h += gts) {
+    const int64_t v = a.heavy_rows[h];
+    atomicOr(a.done + (v >> 5), 1u << (v & 31));
+  }
+  // level 1's candidates: the sources' neighbours, each claimed once through the touched bitmap
+  for (int64_t b = gw; b < a.nsrc; b += gws) {
+    const int64_t s = a.src[b], e0 = a.off[s], e1 = a.off[s + 1];
+    for (int64_t base = e0; base < e1; base += 32) {
+      const int64_t e = base + lane;
+      bool mine = false;
+      uint32_t u = 0;
+      if (e < e1) {
+        u = __ldg(a.adj + e);
+        const uint32_t bit = 1u << (u & 31);
+        mine = (atomicOr(a.touched + (u >> 5), bit) & bit) == 0u;
+      }
+      const unsigned bal = __ballot_sync(PHDE_FULL_MASK, mine);
+      unsigned slot0 = 0;
+      if (lane == 0 && bal) slot0 = atomicAdd(a.tcount, (unsigned)__popc(bal));
+      slot0 = __shfl_sync(PHDE_FULL_MASK, slot0, 0);
+      if (mine) a.tlist[slot0 + __popc(bal & ((1u << lane) - 1u))] = u;
+    }
+  }
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
   int32_t L = 0;
   for (;; L++) {
@@ -167,64 +255,44 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
     if (gt == 0) a.active[(L + 1) % 3] = 0u;
     if (threadIdx.x == 0) s_cnt = 0u;
     unsigned cnt = 0;
-    // light rows: a group of MS_GROUP lanes per vertex, neighbours strided across the group, two neighbour
-    // loads in flight per lane.  A warp holds 32/MS_GROUP groups with consecutive ids; the loop runs over
-    // the warp's first group id so its trip count is warp-uniform and every lane reaches the shuffles.
-    {
-      const int gl = lane & (MS_GROUP - 1);
-      const int64_t gstr = gts / MS_GROUP;                 // groups in the grid
-      const int64_t wfirst = (gt >> 5) * (32 / MS_GROUP);  // this warp's first group id
-      for (int64_t i0 = wfirst; i0 < n; i0 += gstr) {
-        const int64_t v = i0 + (lane / MS_GROUP);
-        bool act = v < n;
-        int64_t e0 = 0, e1 = 0;
-        if (act) {
-          e0 = a.off[v];
-          e1 = a.off[v + 1];
-          if (e1 - e0 > MS_HEAVY) act = false;
-        }
-        ull s[W];
-        bool sat = true;
-#pragma unroll
-        for (int w = 0; w < W; w++) s[w] = 0ull;
-        if (act) {
-          ld_words<W>(a.seen + v * W, s);
-#pragma unroll
-          for (int w = 0; w < W; w++) sat &= (s[w] == full[w]);
-        }
-        ull acc[W];
-#pragma unroll
-        for (int w = 0; w < W; w++) acc[w] = 0ull;
-        if (act && !sat)
-          for (int64_t e = e0 + gl; e < e1; e += 2 * MS_GROUP) {
-            const int64_t e2 = e + MS_GROUP;
-            const uint32_t u0 = __ldg(a.adj + e);
-            const uint32_t u1 = e2 < e1 ? __ldg(a.adj + e2) : u0;
-            ull x0[W], x1[W];
-            ld_words<W>(fcur + (int64_t)u0 * W, x0);
-            ld_words<W>(fcur + (int64_t)u1 * W, x1);
-#pragma unroll
-            for (int w = 0; w < W; w++) acc[w] |= x0[w] | x1[w];
-          }
-#pragma unroll
-        for (int w = 0; w < W; w++)
-#pragma unroll
-          for (int o = MS_GROUP / 2; o > 0; o >>= 1) acc[w] |= __shfl_xor_sync(PHDE_FULL_MASK, acc[w], o, MS_GROUP);
-        // every lane of the group read `seen` above, before the shuffles; the writes come after them
-        if (act) {
-          if (sat) {
-#pragma unroll
-            for (int w = 0; w < W; w++)
-              if (w == gl) fnext[v * W + w] = 0ull;
-          } else if (ms_group_finalise<W>(a, v, acc, s, fnext, L, gl) && gl == 0) {
-            cnt++;
-          }
+    if (L == 0) {
+      // level 1 has new bits only next to a source: pull the claimed candidates (fnext starts zeroed)
+      const unsigned nt = __ldcg(a.tcount);
+      for (int64_t i0 = gw * (32 / MS_GROUP); i0 < nt; i0 += gws * (32 / MS_GROUP)) {
+        const int64_t i = i0 + grp;
+        const bool act = i < nt;
+        const int64_t v = act ? (int64_t)a.tlist[i] : 0;
+        bool nb;
+        ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, false, nb);
+        cnt += nb;
+      }
+    } else {
+      // light rows, 32-vertex tiles per warp: one load of the done bitmap skips finished vertices; the
+      // unfinished ones go to the warp's four 8-lane groups in turn
+      const int64_t ntiles = (n + 31) / 32;
+      for (int64_t t = gw; t < ntiles; t += gws) {
+        const int64_t v0 = t * 32;
+        const unsigned valid = n - v0 >= 32 ? 0xffffffffu : ((1u << (n - v0)) - 1u);
+        // one read of the tile's word, broadcast: the warp sets bits of it below
+        unsigned todo = __shfl_sync(PHDE_FULL_MASK, lane == 0 ? __ldcg(a.done + t) : 0u, 0);
+        todo = ~todo & valid;
+        while (todo) {
+          // the grp-th set bit of todo (none: act = false)
+          unsigned rest = todo;
+          for (int j = 0; j < grp && rest; j++) rest &= rest - 1u;
+          const bool act = rest != 0u;
+          const int64_t v = v0 + (act ? __ffs(rest) - 1 : 0);
+          bool nb;
+          ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, true, nb);
+          cnt += nb;
+          for (int j = 0; j < 32 / MS_GROUP && todo; j++) todo &= todo - 1u;
         }
       }
     }
     // heavy-row chunks: one warp per chunk, OR-reduced, combined with atomicOr
     for (int64_t c = gw; c < a.nchunks; c += gws) {
       const int64_t v = a.chunk_row[c], e0 = a.chunk_e0[c], e1 = min(a.off[v + 1], e0 + MS_CHUNK);
+      if (L == 0 && !((__ldcg(a.touched + (v >> 5)) >> (v & 31)) & 1u)) continue;  // not next to a source
       ull acc[W];
       ld_words<W>(a.seen + v * W, acc);  // seen changes only in the finalisation after the barrier
       bool sat = true;
@@ -293,22 +361,27 @@ __global__ void ms_heavy_plan_kernel(const int64_t *off, int64_t n, int64_t *hea
 // per-column exact sums of squares and an unreached flag on the way.
 __global__ void gather_columns_kernel(const uint16_t *R, int64_t n, int RW, const int *cols, int ncols, int32_t *D,
                                       ull *sumsq, int *unreached) {
-  extern __shared__ uint16_t tile[];  // [32][RW]
+  extern __shared__ uint16_t tile[];  // [32][RW + 2]: the padded row stride puts consecutive rows in
+                                      // consecutive banks (a plain 512-byte stride maps every lane to one bank)
   __shared__ ull s_ssq[GATHER_SMEM_COLS];  // per-CTA column sums; column p is always summed by warp p % nw
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int TLD = RW + 2, hw = RW / 2;  // row stride in 16-bit entries; 32-bit words per row
   for (int p = threadIdx.x; p < GATHER_SMEM_COLS; p += blockDim.x) s_ssq[p] = 0ull;
   int bad = 0;
   for (int64_t v0 = (int64_t)blockIdx.x * 32; v0 < n; v0 += (int64_t)gridDim.x * 32) {
     const int rows = n - v0 < 32 ? (int)(n - v0) : 32;
     __syncthreads();
-    const ull *src = (const ull *)(R + v0 * RW);
-    ull *dst = (ull *)tile;
-    for (int i = threadIdx.x; i < rows * RW / 4; i += blockDim.x) dst[i] = src[i];
+    const uint32_t *src = (const uint32_t *)(R + v0 * RW);
+    uint32_t *dst = (uint32_t *)tile;
+    for (int i = threadIdx.x; i < rows * hw; i += blockDim.x) {
+      const int r = i / hw, c = i - r * hw;
+      dst[r * (TLD / 2) + c] = src[i];
+    }
     __syncthreads();
     for (int p = warp; p < ncols; p += nw) {
       int d = -1;
       if (lane < rows) {
-        d = (int)tile[lane * RW + cols[p]] - 1;
+        d = (int)tile[lane * TLD + cols[p]] - 1;
         D[(int64_t)p * n + v0 + lane] = d;
         bad |= d < 0;
       }
@@ -372,9 +445,12 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
   ull *f0 = (ull *)phde_buf(ctx, "ms.f0", sizeof(ull) * n * Wmax);
   ull *f1 = (ull *)phde_buf(ctx, "ms.f1", sizeof(ull) * n * Wmax);
   ull *hacc = (ull *)phde_buf(ctx, "ms.hacc", sizeof(ull) * n * Wmax);
-  unsigned *active = (unsigned *)phde_buf(ctx, "ms.active", sizeof(unsigned) * 3);
+  unsigned *active = (unsigned *)phde_buf(ctx, "ms.active", sizeof(unsigned) * 4);
   int *levels = (int *)phde_buf(ctx, "ms.levels", sizeof(int));
-  if (!R || !seen || !f0 || !f1 || !hacc || !active || !levels) return PHDE_ERR_OOM;
+  const int64_t nw32 = (n + 31) / 32;
+  uint32_t *bms = (uint32_t *)phde_buf(ctx, "ms.bitmaps", sizeof(uint32_t) * 2 * nw32);  // done, touched
+  uint32_t *tlist = (uint32_t *)phde_buf(ctx, "ms.tlist", sizeof(uint32_t) * n);
+  if (!R || !seen || !f0 || !f1 || !hacc || !active || !levels || !bms || !tlist) return PHDE_ERR_OOM;
   const int64_t *crow, *ce0;
   int64_t nch, chunk;
   int rc0 = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
@@ -399,7 +475,9 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     per_sm = std::min(per_sm, 4);
     PHDE_CK(ctx, cudaMemsetAsync(seen, 0, sizeof(ull) * n * W, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(f0, 0, sizeof(ull) * n * W, ctx->stream));
-    PHDE_CK(ctx, cudaMemsetAsync(active, 0, sizeof(unsigned) * 3, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(f1, 0, sizeof(ull) * n * W, ctx->stream));  // level 1 writes candidates only
+    PHDE_CK(ctx, cudaMemsetAsync(active, 0, sizeof(unsigned) * 4, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(bms, 0, sizeof(uint32_t) * 2 * nw32, ctx->stream));
     int rc = phde_reset_sync(ctx);
     if (rc) return rc;
     MsArgs a;
@@ -424,6 +502,10 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.levels_out = levels;
     a.trace = trace;
     a.trace_cap = trace_cap;
+    a.done = bms;
+    a.touched = bms + nw32;
+    a.tlist = tlist;
+    a.tcount = active + 3;
     a.gs = ctx->d_sync;
     a.err = ctx->d_err;
     a.timeout_ns = ctx->timeout_ns;
@@ -472,7 +554,7 @@ int phde_record_columns(phde_ctx *ctx, const uint16_t *R, int RW, const int *h_c
   PHDE_CK(ctx, cudaMemcpyAsync(dcols, h_cols, sizeof(int) * ncols, cudaMemcpyHostToDevice, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(ssq, 0, sizeof(ull) * ncols, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(unr, 0, sizeof(int), ctx->stream));
-  const size_t smem = sizeof(uint16_t) * 32 * (size_t)RW;
+  const size_t smem = sizeof(uint16_t) * 32 * (size_t)(RW + 2);
   PHDE_CK(ctx, cudaFuncSetAttribute(gather_columns_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 31) / 32, (int64_t)ctx->nsm * 4));
   gather_columns_kernel<<<g, 512, smem, ctx->stream>>>(R, n, RW, dcols, ncols, D, ssq, unr);
