@@ -22,6 +22,7 @@
 #include <cstring>
 #include <vector>
 
+#include "bcgs_gs.cuh"
 #include "ctx.h"
 
 int phde_degrees(phde_ctx *ctx, double *deg);
@@ -212,93 +213,24 @@ __global__ void __launch_bounds__(GT) batch_update_kernel(Seg sg, const float *S
   }
 }
 
-// 32-term FP64 dot product with eight independent chains (GB300's FP64 pipe is narrow: dependent FMAs
-// serialise on its latency).
-__device__ __forceinline__ double dot32(const double *r, const double *v) {
-  double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0, a7 = 0;
-#pragma unroll
-  for (int l = 0; l < 32; l += 8) {
-    a0 = fma(r[l], v[l], a0);
-    a1 = fma(r[l + 1], v[l + 1], a1);
-    a2 = fma(r[l + 2], v[l + 2], a2);
-    a3 = fma(r[l + 3], v[l + 3], a3);
-    a4 = fma(r[l + 4], v[l + 4], a4);
-    a5 = fma(r[l + 5], v[l + 5], a5);
-    a6 = fma(r[l + 6], v[l + 6], a6);
-    a7 = fma(r[l + 7], v[l + 7], a7);
-  }
-  return ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
-}
-
-// sum_{a < na} c[a] * R[a][m] with four chains.
-__device__ __forceinline__ double comb(const double *c, const double (*R)[33], int na, int m) {
-  double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-  int a = 0;
-  for (; a + 3 < na; a += 4) {
-    s0 = fma(c[a], R[a][m], s0);
-    s1 = fma(c[a + 1], R[a + 1][m], s1);
-    s2 = fma(c[a + 2], R[a + 2][m], s2);
-    s3 = fma(c[a + 3], R[a + 3][m], s3);
-  }
-  for (; a < na; a++) s0 = fma(c[a], R[a][m], s0);
-  return (s0 + s1) + (s2 + s3);
-}
-
-// Per graph (one warp each): the coefficient-space accept/discard loop of bcgs.cu.
+// Per graph (one CTA of four warps each): the accept/discard loop of bcgs_gs.cuh.
 // st[4b..]: [0] accepted so far, [1] discarded, [2] candidates consumed, [3] accepted in this block.
-__global__ void batch_block_gs_kernel(const double *Gall, int bc, int k, int rc0, int P, int *stall, double *dlog,
-                                      float *Rall) {
-  __shared__ double sGd[BB][BB + 1], sG2[BB][BB + 1];
-  __shared__ double Rm[BB][BB + 1], Um[BB][BB + 1];
-  __shared__ double dd[BB], tv[BB], cv[BB];
-  const int b = blockIdx.x, m = threadIdx.x;
+__global__ void __launch_bounds__(bcgs_gs::NW * 32) batch_block_gs_kernel(const double *Gall, int bc, int k, int rc0,
+                                                                          int P, int *stall, double *dlog,
+                                                                          float *Rall) {
+  __shared__ bcgs_gs::Smem S;
+  __shared__ int res[3];
+  const int b = blockIdx.x;
   const double *Gd = Gall + (int64_t)b * 2 * BB * BB, *G2 = Gd + BB * BB;
   int *st = stall + 4 * b;
-  float *R = Rall + (int64_t)b * BB * BB;
-  for (int l = 0; l < BB; l++) {
-    sGd[l][m] = Gd[l * BB + m];
-    sG2[l][m] = G2[l * BB + m];
-  }
   const int j0 = st[0];
-  int nacc = 0, ndisc = 0, ncons = 0;
-  __syncwarp();
-  for (int i = 0; i < bc; i++) {
-    if (j0 + nacc >= k) break;
-    ncons++;
-    double t = m == i ? 1.0 : 0.0;
-    for (int pass = 0; pass < 2 && nacc > 0; pass++) {
-      tv[m] = t;
-      __syncwarp();
-      if (m < nacc) cv[m] = dot32(Um[m], tv) / dd[m];
-      __syncwarp();
-      t -= comb(cv, Rm, nacc, m);
-      __syncwarp();
-    }
-    tv[m] = t;
-    __syncwarp();
-    const double nrm = sqrt(fmax(warp_sum(t * dot32(sG2[m], tv)), 0.0));
-    if (nrm < 0.001) {
-      ndisc++;
-      if (m == 0) dlog[(int64_t)b * P + rc0 + i] = nrm;
-    } else {
-      const double r = t / nrm;
-      tv[m] = r;
-      __syncwarp();
-      const double u = dot32(sGd[m], tv);
-      const double d = warp_sum(r * u);
-      Rm[nacc][m] = r;
-      Um[nacc][m] = u;
-      if (m == 0) dd[nacc] = d;
-      nacc++;
-    }
-    __syncwarp();
-  }
-  for (int a = 0; a < BB; a++) R[m * BB + a] = a < nacc ? (float)Rm[a][m] : 0.f;
-  if (m == 0) {
-    st[0] = j0 + nacc;
-    st[1] += ndisc;
-    st[2] += ncons;
-    st[3] = nacc;
+  bcgs_gs::run(S, Gd, G2, bc, k, j0, dlog + (int64_t)b * P + rc0, Rall + (int64_t)b * BB * BB, res, res + 1, res + 2);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    st[0] = j0 + res[0];
+    st[1] += res[1];
+    st[2] += res[2];
+    st[3] = res[0];
   }
 }
 
@@ -542,7 +474,7 @@ int batch_pipeline(phde_ctx *ctx, const BatchBufs &q, int k, int c) {
                                                                q.G + wsel * BB * BB);
       PHDE_LAUNCHED(ctx);
     }
-    batch_block_gs_kernel<<<B, BB, 0, ctx->stream>>>(q.G, bc, k, rc0, P, q.st, q.dlog, q.R);
+    batch_block_gs_kernel<<<B, bcgs_gs::NW * 32, 0, ctx->stream>>>(q.G, bc, k, rc0, P, q.st, q.dlog, q.R);
     PHDE_LAUNCHED(ctx);
     batch_form_kernel<<<ns, GT, 0, ctx->stream>>>(q.sg, q.X, q.R, q.st, q.S, k, q.deg, q.fpart);
     PHDE_LAUNCHED(ctx);

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <vector>
 
+#include "bcgs_gs.cuh"
 #include "ctx.h"
 
 namespace {
@@ -184,95 +185,21 @@ __global__ void __launch_bounds__(GT) bcgs_update_kernel(const float *S, int lda
   }
 }
 
-// 32-term FP64 dot product with eight independent chains (GB300's FP64 pipe is narrow: dependent FMAs
-// serialise on its latency).
-__device__ __forceinline__ double dot32(const double *r, const double *v) {
-  double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0, a7 = 0;
-#pragma unroll
-  for (int l = 0; l < 32; l += 8) {
-    a0 = fma(r[l], v[l], a0);
-    a1 = fma(r[l + 1], v[l + 1], a1);
-    a2 = fma(r[l + 2], v[l + 2], a2);
-    a3 = fma(r[l + 3], v[l + 3], a3);
-    a4 = fma(r[l + 4], v[l + 4], a4);
-    a5 = fma(r[l + 5], v[l + 5], a5);
-    a6 = fma(r[l + 6], v[l + 6], a6);
-    a7 = fma(r[l + 7], v[l + 7], a7);
-  }
-  return ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
-}
-
-// sum_{a < na} c[a] * R[a][m] with four chains.
-__device__ __forceinline__ double comb(const double *c, const double (*R)[33], int na, int m) {
-  double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-  int a = 0;
-  for (; a + 3 < na; a += 4) {
-    s0 = fma(c[a], R[a][m], s0);
-    s1 = fma(c[a + 1], R[a + 1][m], s1);
-    s2 = fma(c[a + 2], R[a + 2][m], s2);
-    s3 = fma(c[a + 3], R[a + 3][m], s3);
-  }
-  for (; a < na; a++) s0 = fma(c[a], R[a][m], s0);
-  return (s0 + s1) + (s2 + s3);
-}
-
-// The block's accept/discard loop in coefficient space (one warp, FP64).  Gd, G2 and the accepted vectors
-// r_a (with U_a = Gd r_a) sit in shared memory; every step is a 32 x 32 matrix-vector product with one
-// lane per output entry (no reductions across lanes):
-//   classical pass:  c = (U^T t) ./ dd  (lane a),  then  t -= R c  (lane m), twice;
-//   norm^2 = t^T G2 t;  discard below 1e-3, else r = t / norm, U = Gd r, dd = r^T U.
+// The block's accept/discard loop (bcgs_gs.cuh), one CTA of four warps.
 // st: [0] accepted so far (j), [1] discarded, [2] candidates consumed, [3] accepted in this block.
-__global__ void bcgs_block_gs_kernel(const double *Gd, const double *G2, int bc, int k, int rc0, int *st,
-                                     double *dlog, float *R) {
-  __shared__ double sGd[BB][BB + 1], sG2[BB][BB + 1];
-  __shared__ double Rm[BB][BB + 1];  // Rm[a][m]: accepted vector a
-  __shared__ double Um[BB][BB + 1];  // Um[a][m] = (Gd r_a)[m]
-  __shared__ double dd[BB], tv[BB], cv[BB];
-  const int m = threadIdx.x;
-  for (int l = 0; l < BB; l++) {
-    sGd[l][m] = Gd[l * BB + m];
-    sG2[l][m] = G2[l * BB + m];
-  }
+__global__ void __launch_bounds__(bcgs_gs::NW * 32) bcgs_block_gs_kernel(const double *Gd, const double *G2, int bc,
+                                                                         int k, int rc0, int *st, double *dlog,
+                                                                         float *R) {
+  __shared__ bcgs_gs::Smem S;
+  __shared__ int res[3];
   const int j0 = st[0];
-  int nacc = 0, ndisc = 0, ncons = 0;
-  __syncwarp();
-  for (int i = 0; i < bc; i++) {
-    if (j0 + nacc >= k) break;
-    ncons++;
-    double t = m == i ? 1.0 : 0.0;
-    for (int pass = 0; pass < 2 && nacc > 0; pass++) {
-      tv[m] = t;
-      __syncwarp();
-      if (m < nacc) cv[m] = dot32(Um[m], tv) / dd[m];  // c_a = <t, U_a> / dd_a, all from the same t (classical)
-      __syncwarp();
-      t -= comb(cv, Rm, nacc, m);
-      __syncwarp();
-    }
-    tv[m] = t;
-    __syncwarp();
-    const double nrm = sqrt(fmax(warp_sum(t * dot32(sG2[m], tv)), 0.0));
-    if (nrm < 0.001) {
-      ndisc++;
-      if (m == 0) dlog[rc0 + i] = nrm;
-    } else {
-      const double r = t / nrm;
-      tv[m] = r;
-      __syncwarp();
-      const double u = dot32(sGd[m], tv);
-      const double d = warp_sum(r * u);
-      Rm[nacc][m] = r;
-      Um[nacc][m] = u;
-      if (m == 0) dd[nacc] = d;
-      nacc++;
-    }
-    __syncwarp();
-  }
-  for (int a = 0; a < BB; a++) R[m * BB + a] = a < nacc ? (float)Rm[a][m] : 0.f;
-  if (m == 0) {
-    st[0] = j0 + nacc;
-    st[1] += ndisc;
-    st[2] += ncons;
-    st[3] = nacc;
+  bcgs_gs::run(S, Gd, G2, bc, k, j0, dlog + rc0, R, res, res + 1, res + 2);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    st[0] = j0 + res[0];
+    st[1] += res[1];
+    st[2] += res[2];
+    st[3] = res[0];
   }
 }
 
@@ -368,7 +295,7 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
       bcgs_reduce_kernel<<<BB, RED_THREADS, 0, ctx->stream>>>(part, ncta, BB, 1, nullptr, 0.0, nullptr, G + wsel * BB * BB);
       PHDE_LAUNCHED(ctx);
     }
-    bcgs_block_gs_kernel<<<1, BB, 0, ctx->stream>>>(G, G + BB * BB, bc, k, rc0, st, dlog, R);
+    bcgs_block_gs_kernel<<<1, bcgs_gs::NW * 32, 0, ctx->stream>>>(G, G + BB * BB, bc, k, rc0, st, dlog, R);
     PHDE_LAUNCHED(ctx);
     PHDE_CK(ctx, cudaMemcpyAsync(hst, st, sizeof(hst), cudaMemcpyDeviceToHost, ctx->stream));
     PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
