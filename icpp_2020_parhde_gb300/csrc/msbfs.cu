@@ -1,12 +1,20 @@
 // msbfs.cu -- multi-source breadth-first search with per-vertex source bitsets (one persistent launch).
 //
 // Up to 64*W sources (W <= 4 words) are searched together.  Every vertex keeps a `seen` bitset (bit b:
-// source b has reached it) and the frontier bitset of the current level.  One level is a pull sweep:
-// an unsaturated vertex ORs the frontier words of its neighbours, keeps the bits it has not seen,
-// records hop distance L+1 for each of them and publishes them as its next-level frontier.  The
-// adjacency is read once per level for all sources, and a vertex every source has reached drops out.
-// Rows above MS_HEAVY neighbours (R-MAT hubs) are cut into chunks whose partial ORs are combined with
-// atomicOr before the same finalisation; OR is order-free, so the result is deterministic.
+// source b has reached it) and the frontier bitset of the current level.  A level computes, for each
+// vertex that can gain bits, the OR of its neighbours' frontier words, keeps the bits it has not seen,
+// records hop distance L+1 for each of them (16-bit record, row per vertex) and publishes them as its
+// next-level frontier word.  Two ways to pick the vertices of a level:
+//   dense  -- every vertex not yet finished, in 32-vertex tiles: a `done` bitmap (saturated, both frontier
+//             words zero) lets a warp skip 32 finished vertices with one load;
+//   sparse -- when the frontier's out-edges are few (below nnz / 16): only the frontier's neighbours can
+//             gain bits, so they are claimed once (a per-vertex level stamp), listed, and pulled; the
+//             stale output words of two levels back are cleared from their list.  The frontier of a
+//             sparse level is a (vertex, edge prefix) list that the previous level built (or that is
+//             rebuilt by one scan of the frontier words after a dense level), walked edge-balanced.
+// Light rows are pulled by groups of 8 lanes; rows above MS_HEAVY neighbours (R-MAT hubs) are cut into
+// chunks whose partial ORs are combined with atomicOr before the same finalisation.  OR is order-free, so
+// the result is deterministic.
 //
 // Used where all sources are known up front -- random pivot strategies, learned pivots, and
 // phde_distances -- so the reference's one-BFS-per-pivot loop (ParHDE.cpp:158-175,
@@ -44,14 +52,20 @@ struct MsArgs {
   const int64_t *chunk_row;   // heavy-row chunks: row and first edge
   const int64_t *chunk_e0;
   int64_t nchunks;
-  unsigned *active;           // [3] vertices given new bits: level L adds to slot L%3 and clears slot (L+1)%3
+  // vertices given new bits at level L, with edge prefixes (count << 32 | edges in lctr): slot L % 4; the
+  // sources are slot 3 (level -1).  Level L reads its frontier from slot (L-1) % 4, clears the stale
+  // output words of slot (L-2) % 4 when it runs sparse, and resets slot (L+1) % 4.
+  uint32_t *qv[4], *qe[4];
+  ull *lctr;                  // [4] list positions (count << 32 | edges) of the lists built by sparse levels
+  ull *lstat;                 // [4] the same totals for every level (dense levels count without a list)
+  int32_t *stamp;             // [n] claim stamps of sparse levels (L + 1), zeroed
+  uint32_t *cand;             // [n] candidates of a sparse level
+  unsigned *ccount;           // [2] candidate counters, by level parity
+  int64_t sparse_edges;       // a level runs sparse when its frontier has fewer out-edges
   int *levels_out;
   ull *trace;                 // optional [2*trace_cap]: per level end time (ns) and vertices given new bits
   int trace_cap;
   uint32_t *done;             // [n/32] bitmap: saturated with both frontier words zero (or a hub row): skipped
-  uint32_t *touched;          // [n/32] bitmap of level 1's candidates (neighbours of the sources), zeroed
-  uint32_t *tlist;            // [n] those candidates, in claim order
-  unsigned *tcount;           // [1]
   GridSync *gs;
   int *err;
   uint64_t timeout_ns;
@@ -142,12 +156,14 @@ __device__ __forceinline__ bool ms_thread_finalise(const MsArgs &a, int64_t v, c
 template <int W>
 __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full)[W], const ull *fcur, ull *fnext,
                                                int32_t L, int64_t v, bool act, int gl, bool mark_done,
-                                               bool &newbits) {
+                                               bool &newbits, uint32_t &deg) {
   newbits = false;
   int64_t e0 = 0, e1 = 0;
+  deg = 0;
   if (act) {
     e0 = a.off[v];
     e1 = a.off[v + 1];
+    deg = (uint32_t)(e1 - e0);
     if (e1 - e0 > MS_HEAVY) act = false;  // hub rows go by chunks
   }
   ull s[W];
@@ -198,8 +214,7 @@ __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full
 }
 
 template <int W>
-__global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
-  __shared__ unsigned s_cnt;
+__global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
   const int64_t n = a.n;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31, gl = lane & (MS_GROUP - 1), grp = lane / MS_GROUP;
@@ -223,25 +238,20 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
     const int64_t v = a.heavy_rows[h];
     atomicOr(a.done + (v >> 5), 1u << (v & 31));
   }
-  // level 1's candidates: the sources' neighbours, each claimed once through the touched bitmap
-  for (int64_t b = gw; b < a.nsrc; b += gws) {
-    const int64_t s = a.src[b], e0 = a.off[s], e1 = a.off[s + 1];
-    for (int64_t base = e0; base < e1; base += 32) {
-      const int64_t e = base + lane;
-      bool mine = false;
-      uint32_t u = 0;
-      if (e < e1) {
-        u = __ldg(a.adj + e);
-        const uint32_t bit = 1u << (u & 31);
-        mine = (atomicOr(a.touched + (u >> 5), bit) & bit) == 0u;
-      }
-      const unsigned bal = __ballot_sync(PHDE_FULL_MASK, mine);
-      unsigned slot0 = 0;
-      if (lane == 0 && bal) slot0 = atomicAdd(a.tcount, (unsigned)__popc(bal));
-      slot0 = __shfl_sync(PHDE_FULL_MASK, slot0, 0);
-      if (mine) a.tlist[slot0 + __popc(bal & ((1u << lane) - 1u))] = u;
+  // the sources are the frontier of level 0 (list slot 3)
+  if (gt == 0) {
+    ull run = 0;
+    for (int b = 0; b < a.nsrc; b++) {
+      const int64_t s = a.src[b];
+      a.qv[3][b] = (uint32_t)s;
+      a.qe[3][b] = (uint32_t)run;
+      run += (ull)(a.off[s + 1] - a.off[s]);
     }
+    a.lctr[3] = a.lstat[3] = ((ull)a.nsrc << 32) | run;
   }
+  __shared__ PushScratch psc;
+  __shared__ ull s_stat;
+  bool built_f = true, built_z = true;  // lists of levels L-1 and L-2 exist (sparse levels build them)
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
   int32_t L = 0;
   for (;; L++) {
@@ -251,20 +261,82 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
     }
     const ull *fcur = a.front[L & 1];
     ull *fnext = a.front[(L + 1) & 1];
-    // slot (L+1)%3 was last read after level L-2's final barrier, which every block has passed
-    if (gt == 0) a.active[(L + 1) % 3] = 0u;
-    if (threadIdx.x == 0) s_cnt = 0u;
-    unsigned cnt = 0;
-    if (L == 0) {
-      // level 1 has new bits only next to a source: pull the claimed candidates (fnext starts zeroed)
-      const unsigned nt = __ldcg(a.tcount);
-      for (int64_t i0 = gw * (32 / MS_GROUP); i0 < nt; i0 += gws * (32 / MS_GROUP)) {
-        const int64_t i = i0 + grp;
-        const bool act = i < nt;
-        const int64_t v = act ? (int64_t)a.tlist[i] : 0;
+    const int so = L & 3, sf = (L + 3) & 3, sz = (L + 2) & 3;
+    // slot (L+1)%4 and the other candidate counter were last used by level L-1, finished at its barrier
+    if (gt == 0) {
+      a.lctr[(L + 1) & 3] = 0ull;
+      a.lstat[(L + 1) & 3] = 0ull;
+      a.ccount[(L + 1) & 1] = 0u;
+    }
+    if (threadIdx.x == 0) s_stat = 0ull;
+    ull my_stat = 0;  // dense: this thread's (count << 32 | edges) of vertices given new bits
+    // the frontier's totals: its list counter if the previous level built one, else its count
+    const ull fstat = built_f ? __ldcg(a.lctr + sf) : __ldcg(a.lstat + sf);
+    const uint32_t fedges = (uint32_t)(fstat & 0xffffffffull);
+    const bool sparse = (int64_t)fedges < a.sparse_edges;
+    if (sparse) {
+      if (!built_f) {
+        // the previous level ran dense: list its frontier (the vertices with a nonzero current word)
+        for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += gts) {
+          const int64_t v = base + threadIdx.x;
+          bool nz = false;
+          uint32_t dv = 0;
+          if (v < n) {
+            ull x[W];
+            ld_words<W>(fcur + v * W, x);
+#pragma unroll
+            for (int w = 0; w < W; w++) nz |= x[w] != 0ull;
+            if (nz) dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+          }
+          block_push(nz, (uint32_t)v, dv, a.qv[sf], a.qe[sf], a.lctr + sf, &psc);
+        }
+      }
+      // stale output words (the vertices given bits at level L-2) go to zero: from its list, or all
+      if (built_z) {
+        const uint32_t zcnt = (uint32_t)(__ldcg(a.lctr + sz) >> 32);
+        for (int64_t i = gt; i < zcnt; i += gts) {
+          const int64_t v = a.qv[sz][i];
+#pragma unroll
+          for (int w = 0; w < W; w++) fnext[v * W + w] = 0ull;
+        }
+      } else {
+        for (int64_t i = gt; i < n * W; i += gts) fnext[i] = 0ull;
+      }
+      if (!built_f && !grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      // new bits can only appear next to the frontier: claim those neighbours once (stamp L+1),
+      // edge-balanced over the frontier's edges
+      const ull fctr = __ldcg(a.lctr + sf);
+      const uint32_t fcnt = (uint32_t)(fctr >> 32), fe = (uint32_t)(fctr & 0xffffffffull);
+      const uint32_t *fqv = a.qv[sf], *fqe = a.qe[sf];
+      unsigned *cc = a.ccount + (L & 1);
+      for (int64_t base = gw * 32; base < fe; base += gws * 32) {
+        const int64_t e = base + lane;
+        bool mine = false;
+        uint32_t v = 0;
+        if (e < fe) {
+          const uint32_t slot = owner_slot(fqe, fcnt, (uint32_t)e);
+          const uint32_t u = fqv[slot];
+          v = __ldg(a.adj + a.off[u] + (e - (int64_t)fqe[slot]));
+          mine = atomicMax(a.stamp + v, L + 1) < L + 1;
+        }
+        const unsigned bal = __ballot_sync(PHDE_FULL_MASK, mine);
+        unsigned slot0 = 0;
+        if (lane == 0 && bal) slot0 = atomicAdd(cc, (unsigned)__popc(bal));
+        slot0 = __shfl_sync(PHDE_FULL_MASK, slot0, 0);
+        if (mine) a.cand[slot0 + __popc(bal & ((1u << lane) - 1u))] = v;
+      }
+      if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+      // pull the candidates; the block-uniform loop lets block_push list the vertices given new bits
+      const unsigned nc = __ldcg(cc);
+      const int gpb = blockDim.x / MS_GROUP;  // groups per block
+      for (int64_t i0 = (int64_t)blockIdx.x * gpb; i0 < nc; i0 += (int64_t)gridDim.x * gpb) {
+        const int64_t i = i0 + threadIdx.x / MS_GROUP;
+        const bool act = i < nc;
+        const int64_t v = act ? (int64_t)a.cand[i] : 0;
         bool nb;
-        ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, false, nb);
-        cnt += nb;
+        uint32_t dv;
+        ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, true, nb, dv);
+        block_push(nb, (uint32_t)v, dv, a.qv[so], a.qe[so], a.lctr + so, &psc);
       }
     } else {
       // light rows, 32-vertex tiles per warp: one load of the done bitmap skips finished vertices; the
@@ -283,8 +355,9 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
           const bool act = rest != 0u;
           const int64_t v = v0 + (act ? __ffs(rest) - 1 : 0);
           bool nb;
-          ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, true, nb);
-          cnt += nb;
+          uint32_t dv;
+          ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, true, nb, dv);
+          if (nb) my_stat += (1ull << 32) | (ull)dv;
           for (int j = 0; j < 32 / MS_GROUP && todo; j++) todo &= todo - 1u;
         }
       }
@@ -292,7 +365,7 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
     // heavy-row chunks: one warp per chunk, OR-reduced, combined with atomicOr
     for (int64_t c = gw; c < a.nchunks; c += gws) {
       const int64_t v = a.chunk_row[c], e0 = a.chunk_e0[c], e1 = min(a.off[v + 1], e0 + MS_CHUNK);
-      if (L == 0 && !((__ldcg(a.touched + (v >> 5)) >> (v & 31)) & 1u)) continue;  // not next to a source
+      if (sparse && __ldcg(a.stamp + v) != L + 1) continue;  // a sparse level pulls its candidates only
       ull acc[W];
       ld_words<W>(a.seen + v * W, acc);  // seen changes only in the finalisation after the barrier
       bool sat = true;
@@ -325,14 +398,29 @@ __global__ void __launch_bounds__(MS_THREADS) msbfs_kernel(MsArgs a) {
         acc[w] = __ldcg(a.hacc + v * W + w);
         a.hacc[v * W + w] = 0ull;
       }
-      if (ms_thread_finalise<W>(a, v, acc, fnext, L)) cnt++;
+      if (ms_thread_finalise<W>(a, v, acc, fnext, L)) {
+        const uint32_t dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+        if (sparse) {
+          const ull pos = atomicAdd(a.lctr + so, (1ull << 32) | (ull)dv);
+          a.qv[so][(uint32_t)(pos >> 32)] = (uint32_t)v;
+          a.qe[so][(uint32_t)(pos >> 32)] = (uint32_t)(pos & 0xffffffffull);
+        } else {
+          my_stat += (1ull << 32) | (ull)dv;
+        }
+      }
     }
-    cnt = warp_sum(cnt);
-    if (lane == 0 && cnt) atomicAdd(&s_cnt, cnt);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_cnt) atomicAdd(a.active + (L % 3), s_cnt);
+    // this level's totals: the list counter (sparse) or one atomic per block (dense)
+    if (!sparse) {
+      my_stat = warp_sum(my_stat);
+      if (lane == 0 && my_stat) atomicAdd(&s_stat, my_stat);
+      __syncthreads();
+      if (threadIdx.x == 0 && s_stat) atomicAdd(a.lstat + so, s_stat);
+    }
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-    const unsigned tot = __ldcg(a.active + (L % 3));
+    built_z = built_f;
+    built_f = sparse;
+    const ull ostat = sparse ? __ldcg(a.lctr + so) : __ldcg(a.lstat + so);
+    const unsigned tot = (unsigned)(ostat >> 32);
     if (a.trace && gt == 0 && L < a.trace_cap) {
       a.trace[2 * L] = global_timer_ns();
       a.trace[2 * L + 1] = tot;
@@ -445,12 +533,14 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
   ull *f0 = (ull *)phde_buf(ctx, "ms.f0", sizeof(ull) * n * Wmax);
   ull *f1 = (ull *)phde_buf(ctx, "ms.f1", sizeof(ull) * n * Wmax);
   ull *hacc = (ull *)phde_buf(ctx, "ms.hacc", sizeof(ull) * n * Wmax);
-  unsigned *active = (unsigned *)phde_buf(ctx, "ms.active", sizeof(unsigned) * 4);
   int *levels = (int *)phde_buf(ctx, "ms.levels", sizeof(int));
-  const int64_t nw32 = (n + 31) / 32;
-  uint32_t *bms = (uint32_t *)phde_buf(ctx, "ms.bitmaps", sizeof(uint32_t) * 2 * nw32);  // done, touched
-  uint32_t *tlist = (uint32_t *)phde_buf(ctx, "ms.tlist", sizeof(uint32_t) * n);
-  if (!R || !seen || !f0 || !f1 || !hacc || !active || !levels || !bms || !tlist) return PHDE_ERR_OOM;
+  const int64_t nw32 = (n + 31) / 32, lcap = n + 256;  // a level list holds each vertex once; the sources' may repeat
+  uint32_t *bms = (uint32_t *)phde_buf(ctx, "ms.done", sizeof(uint32_t) * nw32);
+  uint32_t *lists = (uint32_t *)phde_buf(ctx, "ms.lists", sizeof(uint32_t) * 8 * lcap);  // qv[4], qe[4]
+  uint32_t *cand = (uint32_t *)phde_buf(ctx, "ms.cand", sizeof(uint32_t) * n);
+  int32_t *stamp = (int32_t *)phde_buf(ctx, "ms.stamp", sizeof(int32_t) * n);
+  ull *lctr = (ull *)phde_buf(ctx, "ms.lctr", sizeof(ull) * 8 + sizeof(unsigned) * 2);  // lctr[4], lstat[4], ccount[2]
+  if (!R || !seen || !f0 || !f1 || !hacc || !levels || !bms || !lists || !cand || !stamp || !lctr) return PHDE_ERR_OOM;
   const int64_t *crow, *ce0;
   int64_t nch, chunk;
   int rc0 = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
@@ -476,8 +566,9 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     PHDE_CK(ctx, cudaMemsetAsync(seen, 0, sizeof(ull) * n * W, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(f0, 0, sizeof(ull) * n * W, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(f1, 0, sizeof(ull) * n * W, ctx->stream));  // level 1 writes candidates only
-    PHDE_CK(ctx, cudaMemsetAsync(active, 0, sizeof(unsigned) * 4, ctx->stream));
-    PHDE_CK(ctx, cudaMemsetAsync(bms, 0, sizeof(uint32_t) * 2 * nw32, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(lctr, 0, sizeof(ull) * 8 + sizeof(unsigned) * 2, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(bms, 0, sizeof(uint32_t) * nw32, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(stamp, 0, sizeof(int32_t) * n, ctx->stream));
     int rc = phde_reset_sync(ctx);
     if (rc) return rc;
     MsArgs a;
@@ -498,14 +589,20 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.chunk_row = crow;
     a.chunk_e0 = ce0;
     a.nchunks = nch;
-    a.active = active;
+    for (int i = 0; i < 4; i++) {
+      a.qv[i] = lists + (int64_t)i * lcap;
+      a.qe[i] = lists + (int64_t)(4 + i) * lcap;
+    }
+    a.lctr = lctr;
+    a.lstat = lctr + 4;
+    a.ccount = (unsigned *)(lctr + 8);
+    a.stamp = stamp;
+    a.cand = cand;
+    a.sparse_edges = std::max<int64_t>(ctx->nnz / 16, 1);
     a.levels_out = levels;
     a.trace = trace;
     a.trace_cap = trace_cap;
     a.done = bms;
-    a.touched = bms + nw32;
-    a.tlist = tlist;
-    a.tcount = active + 3;
     a.gs = ctx->d_sync;
     a.err = ctx->d_err;
     a.timeout_ns = ctx->timeout_ns;
