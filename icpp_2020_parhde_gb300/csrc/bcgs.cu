@@ -53,67 +53,99 @@ __global__ void bcgs_load_kernel(const int32_t *D, int64_t n, int rc0, int bc, c
   }
 }
 
-// Partial Gram products over each CTA's row slab: part[(y * gridDim.x + x) * QCH + qq][i] =
-//   sum_r A[r][q] * w[r] * X[r][i],   q = y * QCH + qq,
-// where A[r][q] is the basis (row-major, leading dimension lda) for q < nq, 1 for q == nq when `ones`
-// (the constant column), 0 beyond.  w = deg (FP64, integral) or 1.  FP32 products, FP32 slab sums.
+// Partial Gram products over each CTA's row slab (QC Gram rows per CTA along grid.y):
+//   part[((y * gridDim.x + x) * R + qq) * 32 + i] = sum_r A[r][q] * w[r] * X[r][i],   q = y * QC + qq,
+// where A[r][q] is the basis (row-major, leading dimension lda) for q < nq, 1 for q == nq when `ones` (the
+// constant column), 0 beyond; R = QC.  SELF (A = X, QC = 32): both X^T D X (rows 0..31) and X^T X (rows
+// 32..63) from one read of X, R = 64.  FP32 products, FP32 slab sums; staging of the next 32-row tile is
+// prefetched into registers while the current one is multiplied.
+template <int QC, bool SELF>
 __global__ void __launch_bounds__(GT) bcgs_gram_kernel(const float *A, int lda, int nq, int ones, const float *X,
                                                        const double *w, int64_t n, float *part) {
-  __shared__ __align__(16) float At[RT][QCH];
+  constexpr int QPW = QC / 8;  // Gram rows per warp (eight warps)
+  constexpr int NR = SELF ? 2 * QC : QC;
+  __shared__ __align__(16) float At[RT][QC];
   __shared__ float Xt[RT][BB];
+  __shared__ float Xw[SELF ? RT : 1][BB];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int qbase = blockIdx.y * QCH;
+  const int qbase = blockIdx.y * QC;
   const int64_t per = ((n + gridDim.x - 1) / gridDim.x + RT - 1) / RT * RT;
   const int64_t rb = (int64_t)blockIdx.x * per, re = min(n, rb + per);
-  float acc[8];
+  float acc[QPW], acc2[SELF ? QPW : 1];
 #pragma unroll
-  for (int m = 0; m < 8; m++) acc[m] = 0.f;
-  // staging: thread -> one column of the tile, every GT/QCH-th row (coalesced, no index division); the next
-  // tile's values are loaded into registers while the current one is multiplied
-  const int q = threadIdx.x % QCH, r1 = threadIdx.x / QCH, qq = qbase + q;
+  for (int m = 0; m < QPW; m++) acc[m] = 0.f;
+#pragma unroll
+  for (int m = 0; m < (SELF ? QPW : 1); m++) acc2[m] = 0.f;
+  const int q = threadIdx.x % QC, r1 = threadIdx.x / QC, qq = qbase + q;
   const float cst = (qq == nq && ones) ? 1.f : 0.f;
   const int xi = threadIdx.x % BB, r2 = threadIdx.x / BB;
-  constexpr int NA = RT / (GT / QCH), NX = RT / (GT / BB);
-  float pa[NA], px[NX];
+  constexpr int NA = RT / (GT / QC), NX = RT / (GT / BB);
+  float pa[NA], px[NX], pw[NX];
   auto fetch = [&](int64_t r0) {
 #pragma unroll
     for (int t = 0; t < NA; t++) {
-      const int64_t row = r0 + r1 + t * (GT / QCH);
+      const int64_t row = r0 + r1 + t * (GT / QC);
       pa[t] = row < re ? (qq < nq ? A[row * lda + qq] : cst) : 0.f;
     }
 #pragma unroll
     for (int t = 0; t < NX; t++) {
       const int64_t row = r0 + r2 + t * (GT / BB);
-      px[t] = row < re ? X[row * BB + xi] * (w ? (float)w[row] : 1.f) : 0.f;
+      const float x = row < re ? X[row * BB + xi] : 0.f;
+      const float wf = (w && row < re) ? (float)w[row] : 1.f;
+      px[t] = SELF ? x : x * wf;
+      pw[t] = x * wf;
     }
   };
   if (rb < re) fetch(rb);
   for (int64_t r0 = rb; r0 < re; r0 += RT) {
     __syncthreads();
 #pragma unroll
-    for (int t = 0; t < NA; t++) At[r1 + t * (GT / QCH)][q] = pa[t];
+    for (int t = 0; t < NA; t++) At[r1 + t * (GT / QC)][q] = pa[t];
 #pragma unroll
-    for (int t = 0; t < NX; t++) Xt[r2 + t * (GT / BB)][xi] = px[t];
+    for (int t = 0; t < NX; t++) {
+      Xt[r2 + t * (GT / BB)][xi] = px[t];
+      if (SELF) Xw[r2 + t * (GT / BB)][xi] = pw[t];
+    }
     __syncthreads();
     if (r0 + RT < re) fetch(r0 + RT);
 #pragma unroll 4
     for (int rr = 0; rr < RT; rr++) {
       const float x = Xt[rr][lane];
-      const float4 a0 = *(const float4 *)&At[rr][warp * 8];
-      const float4 a1 = *(const float4 *)&At[rr][warp * 8 + 4];
-      acc[0] = fmaf(a0.x, x, acc[0]);
-      acc[1] = fmaf(a0.y, x, acc[1]);
-      acc[2] = fmaf(a0.z, x, acc[2]);
-      acc[3] = fmaf(a0.w, x, acc[3]);
-      acc[4] = fmaf(a1.x, x, acc[4]);
-      acc[5] = fmaf(a1.y, x, acc[5]);
-      acc[6] = fmaf(a1.z, x, acc[6]);
-      acc[7] = fmaf(a1.w, x, acc[7]);
+      float av[QPW];
+      if constexpr (QPW % 4 == 0) {
+#pragma unroll
+        for (int m = 0; m < QPW; m += 4) {
+          const float4 a4 = *(const float4 *)&At[rr][warp * QPW + m];
+          av[m] = a4.x;
+          av[m + 1] = a4.y;
+          av[m + 2] = a4.z;
+          av[m + 3] = a4.w;
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < QPW; m++) av[m] = At[rr][warp * QPW + m];
+      }
+#pragma unroll
+      for (int m = 0; m < QPW; m++) acc[m] = fmaf(av[m], x, acc[m]);
+      if constexpr (SELF) {
+        const float xw = Xw[rr][lane];
+#pragma unroll
+        for (int m = 0; m < QPW; m++) acc2[m] = fmaf(av[m], xw, acc2[m]);
+      }
     }
   }
-  float *dst = part + ((int64_t)(blockIdx.y * gridDim.x + blockIdx.x) * QCH + warp * 8) * BB + lane;
+  float *dst = part + ((int64_t)(blockIdx.y * gridDim.x + blockIdx.x) * NR + warp * QPW) * BB + lane;
+  if constexpr (SELF) {
+    // rows 0..QC-1: X^T D X (weighted), rows QC..2QC-1: X^T X
 #pragma unroll
-  for (int m = 0; m < 8; m++) dst[m * BB] = acc[m];
+    for (int m = 0; m < QPW; m++) {
+      dst[m * BB] = acc2[m];
+      dst[(QC + m) * BB] = acc[m];
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < QPW; m++) dst[m * BB] = acc[m];
+  }
 }
 
 // Sum the partials of Gram row q (one CTA per row, fixed order: deterministic) in FP64.
@@ -122,13 +154,14 @@ __global__ void __launch_bounds__(GT) bcgs_gram_kernel(const float *A, int lda, 
 //   mode 1 (block Gram): G[q][i] = sum, FP64 out.
 __global__ void __launch_bounds__(RED_THREADS) bcgs_reduce_kernel(const float *part, int ncta, int nq, int mode,
                                                                   const double *dden, double n_den0, float *C,
-                                                                  double *G) {
+                                                                  double *G, int rows) {
   __shared__ double red[RED_THREADS / 32][BB];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int q = blockIdx.x, y = q / QCH, qq = q % QCH;
+  // Gram row q; `rows` partial rows per CTA (the kernel's QC, 2 QC for the block Grams)
+  const int q = blockIdx.x, y = mode == 0 ? q / rows : 0, qq = mode == 0 ? q % rows : q;
   // four independent sums per thread (the partials come from L2: hide its latency), combined in order
-  const float *base = part + ((int64_t)y * ncta * QCH + qq) * BB + lane;
-  const int64_t cs = (int64_t)QCH * BB;
+  const float *base = part + ((int64_t)y * ncta * rows + qq) * BB + lane;
+  const int64_t cs = (int64_t)rows * BB;
   double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
   int c = warp;
   for (; c + 3 * nw < ncta; c += 4 * nw) {
@@ -279,22 +312,27 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
     const int bc = std::min(BB, P - rc0);
     bcgs_load_kernel<<<g_rows, GT, 0, ctx->stream>>>(D, n, rc0, bc, sumsq, X);
     PHDE_LAUNCHED(ctx);
-    const int nqt = j + 1, nqc = (nqt + QCH - 1) / QCH;
+    const int nqt = j + 1;
+    const int qc = nqt <= 8 ? 8 : (nqt <= 32 ? 32 : 64), nqc = (nqt + qc - 1) / qc;
     for (int pass = 0; pass < 2; pass++) {
-      bcgs_gram_kernel<<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
+      if (qc == 8)
+        bcgs_gram_kernel<8, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
+      else if (qc == 32)
+        bcgs_gram_kernel<32, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
+      else
+        bcgs_gram_kernel<64, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
       PHDE_LAUNCHED(ctx);
-      bcgs_reduce_kernel<<<nqt, RED_THREADS, 0, ctx->stream>>>(part, ncta, j, 0, dden, n_den0, C, nullptr);
+      bcgs_reduce_kernel<<<nqt, RED_THREADS, 0, ctx->stream>>>(part, ncta, j, 0, dden, n_den0, C, nullptr, qc);
       PHDE_LAUNCHED(ctx);
       const size_t smem = sizeof(float) * ((size_t)nqt * BB + (size_t)j * ST_LD);
       bcgs_update_kernel<<<g_rows, GT, smem, ctx->stream>>>(S, k, j, C, X, n);
       PHDE_LAUNCHED(ctx);
     }
-    for (int wsel = 0; wsel < 2; wsel++) {
-      bcgs_gram_kernel<<<dim3(ncta, 1), GT, 0, ctx->stream>>>(X, BB, BB, 0, X, wsel == 0 ? deg : nullptr, n, part);
-      PHDE_LAUNCHED(ctx);
-      bcgs_reduce_kernel<<<BB, RED_THREADS, 0, ctx->stream>>>(part, ncta, BB, 1, nullptr, 0.0, nullptr, G + wsel * BB * BB);
-      PHDE_LAUNCHED(ctx);
-    }
+    // block Grams X^T D X and X^T X in one pass; G holds them one after the other (64 rows of 32)
+    bcgs_gram_kernel<32, true><<<dim3(ncta, 1), GT, 0, ctx->stream>>>(X, BB, BB, 0, X, deg, n, part);
+    PHDE_LAUNCHED(ctx);
+    bcgs_reduce_kernel<<<2 * BB, RED_THREADS, 0, ctx->stream>>>(part, ncta, BB, 1, nullptr, 0.0, nullptr, G, 2 * BB);
+    PHDE_LAUNCHED(ctx);
     bcgs_block_gs_kernel<<<1, bcgs_gs::NW * 32, 0, ctx->stream>>>(G, G + BB * BB, bc, k, rc0, st, dlog, R);
     PHDE_LAUNCHED(ctx);
     PHDE_CK(ctx, cudaMemcpyAsync(hst, st, sizeof(hst), cudaMemcpyDeviceToHost, ctx->stream));

@@ -9,8 +9,8 @@
 //                    (||x|| < 1e-3 discards, ParHDE.cpp:267) and the same acceptance order.
 //   spmm32 kernels   LS = D*S - A*S with an FP32 basis (half the bytes of every neighbour gather; the
 //                    R-MAT-20 basis is 129 MB and stays largely in the 129 MB L2), same heavy-row plan.
-//   gram32_kernel    S^T LS with FP32 products accumulated in FP32 over 16-row slabs and in FP64 across
-//                    slabs and blocks.
+//   gram32_kernel    S^T LS with FP32 products accumulated in FP32 over 128-row spans and in FP64 across
+//                    spans and blocks.
 //   coords32_kernel  X = S*Y: FP32 products and row sums (S is FP32), FP64 column norms.
 // The k x k eigensolve stays FP64 (eigen.cu).
 #include <algorithm>
@@ -222,6 +222,89 @@ __global__ void __launch_bounds__(C2_THREADS) cgs2_kernel(Cgs2Args a) {
 }
 
 // ---- FP32 Laplacian SpMM ----
+// A warp per row (light rows) or per chunk of a heavy row.  Lane l owns columns 2l, 2l+1 of every 64-column
+// tile (float2 gathers: one 8-byte load per lane and neighbour row; k even), KT tiles (k <= 64 KT); the
+// neighbour loop keeps four rows in flight.  Odd k uses the scalar variant (lane l: columns l + 32t).
+template <int KT>
+__device__ __forceinline__ void spmm32_acc2(const uint32_t *adj, const float *S, int k, int lane, int64_t e0,
+                                            int64_t e1, float2 (&acc)[KT]) {
+  int64_t e = e0;
+  for (; e + 4 <= e1; e += 4) {
+    const int64_t v0 = __ldg(adj + e), v1 = __ldg(adj + e + 1), v2 = __ldg(adj + e + 2), v3 = __ldg(adj + e + 3);
+#pragma unroll
+    for (int t = 0; t < KT; t++) {
+      const int q = 2 * lane + 64 * t;
+      if (q < k) {
+        const float2 a0 = *(const float2 *)(S + v0 * k + q), a1 = *(const float2 *)(S + v1 * k + q);
+        const float2 a2 = *(const float2 *)(S + v2 * k + q), a3 = *(const float2 *)(S + v3 * k + q);
+        acc[t].x -= (a0.x + a1.x) + (a2.x + a3.x);
+        acc[t].y -= (a0.y + a1.y) + (a2.y + a3.y);
+      }
+    }
+  }
+  for (; e < e1; e++) {
+    const int64_t v = __ldg(adj + e);
+#pragma unroll
+    for (int t = 0; t < KT; t++) {
+      const int q = 2 * lane + 64 * t;
+      if (q < k) {
+        const float2 a = *(const float2 *)(S + v * k + q);
+        acc[t].x -= a.x;
+        acc[t].y -= a.y;
+      }
+    }
+  }
+}
+
+template <int KT>
+__global__ void spmm32_light2_kernel(const int64_t *off, const uint32_t *adj, const double *deg, const float *S,
+                                     float *LS, int64_t n, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < n; i += gws) {
+    const int64_t e0 = off[i], e1 = off[i + 1];
+    if (e1 - e0 > SPMM_HEAVY) continue;
+    const float di = (float)(e1 - e0);  // unweighted: the degree is the row length
+    float2 acc[KT];
+#pragma unroll
+    for (int t = 0; t < KT; t++) {
+      const int q = 2 * lane + 64 * t;
+      acc[t] = make_float2(0.f, 0.f);
+      if (q < k) {
+        const float2 si = *(const float2 *)(S + i * k + q);
+        acc[t] = make_float2(di * si.x, di * si.y);
+      }
+    }
+    spmm32_acc2<KT>(adj, S, k, lane, e0, e1, acc);
+#pragma unroll
+    for (int t = 0; t < KT; t++) {
+      const int q = 2 * lane + 64 * t;
+      if (q < k) *(float2 *)(LS + i * k + q) = acc[t];
+    }
+  }
+}
+
+template <int KT>
+__global__ void spmm32_chunk2_kernel(const uint32_t *adj, const float *S, const Chunk *chunks, int64_t nchunks,
+                                     float *part, int k) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = gw; c < nchunks; c += gws) {
+    float2 acc[KT];
+#pragma unroll
+    for (int t = 0; t < KT; t++) acc[t] = make_float2(0.f, 0.f);
+    const Chunk ch = chunks[c];
+    spmm32_acc2<KT>(adj, S, k, lane, ch.e0, ch.e1, acc);
+#pragma unroll
+    for (int t = 0; t < KT; t++) {
+      const int q = 2 * lane + 64 * t;
+      if (q < k) *(float2 *)(part + c * k + q) = acc[t];
+    }
+  }
+}
+
 __device__ __forceinline__ void spmm32_acc(const uint32_t *adj, const float *S, int k, int lane, int64_t e0,
                                            int64_t e1, float (&acc)[MAXQ]) {
   int64_t e = e0;
@@ -307,7 +390,7 @@ __global__ void spmm32_fix_kernel(const HeavyRow *heavy, int64_t nheavy, const d
   }
 }
 
-// ---- Gram A^T B with FP32 inputs: 64x64 tile per block, FP32 over 16-row slabs, FP64 across slabs ----
+// ---- Gram A^T B with FP32 inputs: 64x64 tile per block, 16-row staged slabs, FP32 over 128 rows, FP64 beyond ----
 constexpr int GT = 64, GR = 16;
 __global__ void __launch_bounds__(256) gram32_kernel(const float *A, const float *B, int64_t n, int k, double *part) {
   __shared__ float sA[GR][GT + 1];
@@ -320,7 +403,9 @@ __global__ void __launch_bounds__(256) gram32_kernel(const float *A, const float
   const int64_t r0 = (int64_t)blockIdx.y * rows_per;
   const int64_t r1 = min(n, r0 + rows_per);
   double accd[4][4] = {};
-  for (int64_t rb = r0; rb < r1; rb += GR) {
+  float acc[4][4] = {};
+  int slab = 0;
+  for (int64_t rb = r0; rb < r1; rb += GR, slab++) {
     for (int idx = threadIdx.x; idx < GR * GT; idx += 256) {
       const int rr = idx / GT, cc = idx % GT;
       const int64_t r = rb + rr;
@@ -328,7 +413,6 @@ __global__ void __launch_bounds__(256) gram32_kernel(const float *A, const float
       sB[rr][cc] = (r < r1 && q0 + cc < k) ? B[r * k + q0 + cc] : 0.f;
     }
     __syncthreads();
-    float acc[4][4] = {};
 #pragma unroll 4
     for (int rr = 0; rr < GR; rr++) {
       float av[4], bv[4];
@@ -342,10 +426,16 @@ __global__ void __launch_bounds__(256) gram32_kernel(const float *A, const float
 #pragma unroll
         for (int v = 0; v < 4; v++) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
     }
+    // FP32 sums over 128 rows, then into FP64: GB300's FP64 adds are 1/64-rate, so not after every slab
+    if ((slab & 7) == 7 || rb + GR >= r1) {
 #pragma unroll
-    for (int u = 0; u < 4; u++)
+      for (int u = 0; u < 4; u++)
 #pragma unroll
-      for (int v = 0; v < 4; v++) accd[u][v] += (double)acc[u][v];
+        for (int v = 0; v < 4; v++) {
+          accd[u][v] += (double)acc[u][v];
+          acc[u][v] = 0.f;
+        }
+    }
     __syncthreads();
   }
   double *out = part + (int64_t)blockIdx.y * k * k;
@@ -358,11 +448,27 @@ __global__ void __launch_bounds__(256) gram32_kernel(const float *A, const float
     }
 }
 
-__global__ void sum_parts32_kernel(const double *part, int splits, int64_t len, double *out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0;
-    for (int b = 0; b < splits; b++) s += part[(int64_t)b * len + i];
-    out[i] = s;
+// out[i] = sum over splits of part[b][i]: a block per 32 outputs, its 8 warps over interleaved splits (two
+// chains each), combined in warp order -- deterministic, and short FP64 dependency chains.
+__global__ void __launch_bounds__(256) sum_parts32_kernel(const double *part, int splits, int64_t len, double *out) {
+  __shared__ double red[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 32 + lane;
+  double s0 = 0, s1 = 0;
+  if (i < len) {
+    int b = warp;
+    for (; b + 8 < splits; b += 16) {
+      s0 += part[(int64_t)b * len + i];
+      s1 += part[(int64_t)(b + 8) * len + i];
+    }
+    if (b < splits) s0 += part[(int64_t)b * len + i];
+  }
+  red[warp][lane] = s0 + s1;
+  __syncthreads();
+  if (warp == 0 && i < len) {
+    double t = 0;
+    for (int w = 0; w < 8; w++) t += red[w][lane];
+    out[i] = t;
   }
 }
 
@@ -488,14 +594,36 @@ int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float 
   int rc = phde_spmm_plan(ctx, &heavy, &chunks, &nheavy, &nchunks);
   if (rc) return rc;
   const int threads = 256;
-  spmm32_light_kernel<<<grid_of(ctx, ctx->n * 32, threads, 8), threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, deg,
-                                                                                          S, LS, ctx->n, k);
+  // float2 gathers for even k on unweighted graphs (the degree is the row length), else the scalar kernels
+  const int KT = (k + 63) / 64;
+  const bool v2 = k % 2 == 0 && !ctx->weighted && KT <= 4;
+  const int gl = grid_of(ctx, ctx->n * 32, threads, 8);
+#define PHDE_SPMM_LIGHT(T) \
+  spmm32_light2_kernel<T><<<gl, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, deg, S, LS, ctx->n, k)
+  if (v2) {
+    if (KT == 1) PHDE_SPMM_LIGHT(1);
+    else if (KT == 2) PHDE_SPMM_LIGHT(2);
+    else if (KT == 3) PHDE_SPMM_LIGHT(3);
+    else PHDE_SPMM_LIGHT(4);
+  } else {
+    spmm32_light_kernel<<<gl, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, deg, S, LS, ctx->n, k);
+  }
+#undef PHDE_SPMM_LIGHT
   PHDE_LAUNCHED(ctx);
   if (nheavy > 0) {
     float *part = (float *)phde_buf(ctx, "spmm32.part", sizeof(float) * nchunks * k);
     if (!part) return PHDE_ERR_OOM;
-    spmm32_chunk_kernel<<<grid_of(ctx, nchunks * 32, threads, 8), threads, 0, ctx->stream>>>(ctx->d_adj, S, chunks,
-                                                                                             nchunks, part, k);
+    const int gc = grid_of(ctx, nchunks * 32, threads, 8);
+#define PHDE_SPMM_CHUNK(T) spmm32_chunk2_kernel<T><<<gc, threads, 0, ctx->stream>>>(ctx->d_adj, S, chunks, nchunks, part, k)
+    if (v2) {
+      if (KT == 1) PHDE_SPMM_CHUNK(1);
+      else if (KT == 2) PHDE_SPMM_CHUNK(2);
+      else if (KT == 3) PHDE_SPMM_CHUNK(3);
+      else PHDE_SPMM_CHUNK(4);
+    } else {
+      spmm32_chunk_kernel<<<gc, threads, 0, ctx->stream>>>(ctx->d_adj, S, chunks, nchunks, part, k);
+    }
+#undef PHDE_SPMM_CHUNK
     PHDE_LAUNCHED(ctx);
     spmm32_fix_kernel<<<grid_of(ctx, nheavy * 32, threads, 8), threads, 0, ctx->stream>>>(heavy, nheavy, deg, S, part,
                                                                                           LS, k);
@@ -512,7 +640,7 @@ int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double
   if (!part) return PHDE_ERR_OOM;
   gram32_kernel<<<dim3(tiles * tiles, splits), 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
   PHDE_LAUNCHED(ctx);
-  sum_parts32_kernel<<<grid_of(ctx, (int64_t)k * k, 256, 8), 256, 0, ctx->stream>>>(part, splits, (int64_t)k * k, M);
+  sum_parts32_kernel<<<(int)(((int64_t)k * k + 31) / 32), 256, 0, ctx->stream>>>(part, splits, (int64_t)k * k, M);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }
