@@ -455,6 +455,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(const double *Kin, 
 // orthogonal to FP32 rounding), A is replaced by the exactly similar V^T A V computed in FP64, and FP64
 // sweeps (quadratically convergent from an off-diagonal of FP32 rounding size) finish with the same
 // convergence test as the global-memory kernel.  Everything lives in shared memory.
+constexpr int JS_MIN_THREADS = 256;  // the shared-memory solver runs with 256..1024 threads
 constexpr int JS_MAX_N = 96;  // 24 N (N|1) bytes of shared memory: A64, V64 and one work matrix
 
 template <typename T>
@@ -612,7 +613,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   }
   __syncthreads();
   {
-    constexpr int PER = (JS_MAX_N * JS_MAX_N + EIG_THREADS - 1) / EIG_THREADS;
+    constexpr int PER = (JS_MAX_N * JS_MAX_N + JS_MIN_THREADS - 1) / JS_MIN_THREADS;
     double nv[PER];
     int cnt = 0;
     for (int idx = tid; idx < N * N; idx += blockDim.x, cnt++) {  // V(I - E/2), held until every read is done
@@ -678,7 +679,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   //      sweeps. ----
   __shared__ double s_lam[JS_MAX_N];
   __shared__ int s_bad;
-  if (tid == 0) s_bad = c_target * N > EIG_THREADS;  // one refined entry per thread at most
+  if (tid == 0) s_bad = c_target * N > 2 * (int)blockDim.x;  // two refined entries per thread at most
   __syncthreads();
   for (int idx = tid; idx < N * N; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
@@ -718,7 +719,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
     __syncthreads();
     for (int it = 0; it < 2; it++) {
       // new y_j for j != i from the current y (computed into registers, written after a barrier)
-      double ny[(JS_MAX_N * 4 + EIG_THREADS - 1) / EIG_THREADS];
+      double ny[2];  // N * c_target <= 2 * blockDim.x (checked above)
       int cnt = 0;
       for (int idx = tid; idx < N * c_target; idx += blockDim.x, cnt++) {
         const int j = idx % N, ti = idx / N;
@@ -846,6 +847,16 @@ __global__ void pick_kernel(const double *K, int N, int c, int largest, double *
   }
 }
 
+// Threads of the shared-memory solver: its rounds are barrier bound, so the fewest that still cover a
+// round's work (measured on GB300: 256 up to N = 16, 512 above).  PHDE_JACOBI_THREADS overrides.
+int js_threads(int N) {
+  if (const char *e = getenv("PHDE_JACOBI_THREADS")) {
+    const int t = atoi(e);
+    if (t == 256 || t == 512 || t == 1024) return t;
+  }
+  return N <= 16 ? 256 : 512;
+}
+
 }  // namespace
 
 // Solve the k x k problem in d_M (column-major).  On success d_K holds the eigenvector matrix,
@@ -865,8 +876,8 @@ int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest,
       // PHDE_EIG_TRACE=1: print the kernel's phase timeline (FP32 sweeps, orthonormalisation, similarity,
       // FP64 sweeps, sort) after the solve
       unsigned long long *tr = getenv("PHDE_EIG_TRACE") ? (unsigned long long *)phde_buf(ctx, "eig.trace", 64) : nullptr;
-      jacobi_smem_kernel<<<1, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, st, st + 1, 100, tr,
-                                                                  c, largest);
+      jacobi_smem_kernel<<<1, js_threads(N), jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, st, st + 1, 100, tr, c,
+                                                                    largest);
       if (tr) {
         unsigned long long h[8];
         PHDE_CK(ctx, cudaMemcpyAsync(h, tr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
@@ -912,8 +923,8 @@ int phde_eigensolve_batched(phde_ctx *ctx, const double *d_M, int N, int c, int 
   if (N > JS_MAX_N) return phde_fail(ctx, PHDE_ERR_INVALID, "batched eigensolve: k above the shared-memory limit");
   const size_t jsmem = sizeof(double) * 3 * (size_t)N * (N | 1);
   PHDE_CK(ctx, cudaFuncSetAttribute(jacobi_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
-  jacobi_smem_kernel<<<count, EIG_THREADS, jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, d_st, d_st + count, 100,
-                                                                  nullptr, c, 0);
+  jacobi_smem_kernel<<<count, js_threads(N), jsmem, ctx->stream>>>(d_M, N, d_K, d_evals, d_st, d_st + count, 100,
+                                                                    nullptr, c, 0);
   PHDE_LAUNCHED(ctx);
   pick_kernel<<<count, 256, 0, ctx->stream>>>(d_K, N, c, 0, d_Y);
   PHDE_LAUNCHED(ctx);
