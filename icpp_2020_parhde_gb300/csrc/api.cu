@@ -215,6 +215,7 @@ void phde_destroy(phde_ctx *c) {
   cudaFree(c->d_err);
   cudaFree(c->d_vbase);
   cudaFree(c->d_gid);
+  cudaFree(c->d_order);
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (auto &e : c->ev) cudaEventDestroy(e);
   for (auto &e : c->kev) cudaEventDestroy(e);

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "bcgs_gs.cuh"
@@ -29,6 +30,8 @@ int phde_degrees(phde_ctx *ctx, double *deg);
 int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float *LS, int k);
 int phde_eigensolve_batched(phde_ctx *ctx, const double *d_M, int N, int c, int count, double *d_K,
                             double *d_evals, double *d_Y, int *d_st);
+int phde_run_bfs_batched_blocks(phde_ctx *ctx, int P, const int32_t *d_order, int32_t *d_D, int64_t *d_sources,
+                                unsigned long long *d_sumsq, unsigned long long *d_edges);
 
 namespace {
 
@@ -421,6 +424,17 @@ extern "C" int phde_batch_upload(phde_ctx *ctx, const phde_graph_desc *graphs, i
   ctx->batch_B = count;
   ctx->batch_vbase = vb;
   ctx->batch_ebase = eb;
+  // graphs largest first (the one-CTA-per-graph Kcenters takes them in this order)
+  std::vector<int32_t> order(count);
+  for (int b = 0; b < count; b++) order[b] = b;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t x, int32_t y) { return vb[x + 1] - vb[x] > vb[y + 1] - vb[y]; });
+  cudaFree(ctx->d_order);
+  ctx->d_order = nullptr;
+  PHDE_CK(ctx, cudaMalloc(&ctx->d_order, sizeof(int32_t) * count));
+  PHDE_CK(ctx, cudaMemcpy(ctx->d_order, order.data(), sizeof(int32_t) * count, cudaMemcpyHostToDevice));
+  const char *mode = getenv("PHDE_BATCH_BFS");
+  ctx->batch_blocks = mode ? std::string(mode) == "blocks" : count >= ctx->nsm / 2;
   return PHDE_OK;
 }
 
@@ -447,7 +461,13 @@ int batch_pipeline(phde_ctx *ctx, const BatchBufs &q, int k, int c) {
   int rc;
   const int64_t *d_eb = ctx->d_vbase + (B + 1);
   if ((rc = phde_degrees(ctx, q.deg))) return rc;
-  if ((rc = phde_run_bfs_passes(ctx, P, 3, nullptr, q.D, q.src, q.sumsq, q.edges, 1))) return rc;
+  // Kcenters: one CTA per graph when the batch has enough graphs to fill the GPU (block barriers only),
+  // else the whole-grid batched variant (every pass one BFS of the union)
+  if (ctx->batch_blocks)
+    rc = phde_run_bfs_batched_blocks(ctx, P, ctx->d_order, q.D, q.src, q.sumsq, q.edges);
+  else
+    rc = phde_run_bfs_passes(ctx, P, 3, nullptr, q.D, q.src, q.sumsq, q.edges, 1);
+  if (rc) return rc;
   batch_inv_norms_kernel<<<(P * B + 255) / 256, 256, 0, ctx->stream>>>(q.sumsq, P * B, q.inv);
   PHDE_LAUNCHED(ctx);
   PHDE_CK(ctx, cudaMemsetAsync(q.st, 0, sizeof(int) * 4 * B, ctx->stream));

@@ -24,6 +24,8 @@ struct phde_ctx {
   std::vector<int64_t> batch_vbase, batch_ebase;  // host copies, batch_B + 1 entries
   int64_t *d_vbase = nullptr;                      // [batch_B + 1]
   int32_t *d_gid = nullptr;                        // [n]: graph of each vertex
+  int32_t *d_order = nullptr;                      // [batch_B]: graphs, largest first
+  bool batch_blocks = false;                       // Kcenters with one CTA per graph
   int64_t batch_tuned_shape = -1;                  // autotuned segment length for this batch shape and k
   int batch_tuned_k = 0;
   int64_t batch_seg_rows = 8192;

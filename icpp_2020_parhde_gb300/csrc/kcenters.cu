@@ -349,6 +349,133 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
   if (tid == 0 && a.edges) atomicAdd(a.edges, etot);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Batched Kcenters with one CTA per graph (batches of small graphs).  A grid-wide level barrier costs
+// more than a small graph's whole level, and every grid-wide level waits for the deepest graph of the
+// batch; here each CTA takes whole graphs from a work list (largest first) and runs their 3k passes with
+// block barriers only.  Per pass: a level-synchronous top-down BFS from the pass's source over queues in
+// the graph's own slice of the union's queue arrays -- a thread per frontier vertex, its neighbours' loads
+// issued in batches of eight before the claims (atomicCAS on the distance entry; appends through a
+// shared-memory counter) --, then the Kcenters fold over the graph's vertices (min distance,
+// farthest vertex with the lowest index on ties -- the key (min_d << 32) | ~v --, exact sum of squares).
+// Same outputs as the batched variant of kcenters_bfs_kernel: D columns over the union, sources, keys and
+// sums indexed [p * B + b].
+struct KbArgs {
+  const int64_t *off;
+  const uint32_t *adj;
+  int64_t N;
+  int32_t *D;
+  int P, B;
+  const int64_t *vbase;
+  const int32_t *order;  // graphs, largest first
+  unsigned *next;        // work-list counter (zeroed)
+  int64_t *sources;
+  int32_t *min_d;
+  ull *sumsq;
+  uint32_t *q0, *q1;     // [N] each: frontier vertices
+  ull *edges;
+  int *err;
+};
+
+constexpr int KB_THREADS = 1024;
+
+__global__ void __launch_bounds__(KB_THREADS) kcenters_block_kernel(KbArgs a) {
+  __shared__ int s_graph;
+  // level L appends through s_c[L % 3]; after the level every thread reads it, and
+  // thread 0 clears s_c[(L + 2) % 3] -- last read before this level's final barrier, next used two levels on
+  __shared__ ull s_c[3];
+  __shared__ ull red[32];
+  __shared__ int64_t s_src;
+  const int tid = threadIdx.x;
+  ull edges_local = 0;
+  for (;;) {
+    if (tid == 0) s_graph = (int)atomicAdd(a.next, 1u);
+    __syncthreads();
+    const int gi = s_graph;
+    __syncthreads();
+    if (gi >= a.B) break;
+    const int b = a.order[gi];
+    const int64_t vb = a.vbase[b], nb = a.vbase[b + 1] - vb;
+    int64_t src = vb;  // Kcenters starts at the graph's vertex 0
+    for (int p = 0; p < a.P; p++) {
+      int32_t *Dp = a.D + (int64_t)p * a.N;
+      if (tid == 0) {
+        Dp[src] = 0;
+        a.q0[vb] = (uint32_t)src;
+        s_c[0] = 0ull;
+        s_c[1] = 0ull;
+      }
+      uint32_t cnt = 1;
+      const uint32_t *qin = a.q0 + vb;
+      uint32_t *qout = a.q1 + vb;
+      int32_t L = 0;
+      __syncthreads();
+      while (cnt > 0) {
+        unsigned *c = (unsigned *)(s_c + (L % 3));
+        // a thread per frontier vertex; its neighbours in batches of 8 with every load of a batch in flight
+        // before the claims (a level's critical path is its chain of memory round trips)
+        for (uint32_t i = tid; i < cnt; i += blockDim.x) {
+          const uint32_t u = qin[i];
+          const int64_t e1 = a.off[u + 1];
+          for (int64_t e0 = a.off[u]; e0 < e1; e0 += 8) {
+            uint32_t vv[8];
+#pragma unroll
+            for (int t = 0; t < 8; t++) vv[t] = e0 + t < e1 ? __ldg(a.adj + e0 + t) : 0xffffffffu;
+            int old[8];  // all eight claims issued before any result is used
+#pragma unroll
+            for (int t = 0; t < 8; t++) old[t] = vv[t] != 0xffffffffu ? atomicCAS(Dp + vv[t], -1, L + 1) : 0;
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+              if (vv[t] == 0xffffffffu) continue;
+              edges_local++;
+              if (old[t] == -1) qout[atomicAdd(c, 1u)] = vv[t];
+            }
+          }
+        }
+        __syncthreads();
+        cnt = *c;
+        if (tid == 0) s_c[(L + 2) % 3] = 0ull;
+        const uint32_t *tq = qin;
+        qin = qout;
+        qout = (uint32_t *)tq;
+        L++;
+      }
+      // fold: min distance, farthest vertex (lowest index on ties), exact sum of squares
+      ull kbest = 0, ssq = 0;
+      int bad = 0;
+      for (int64_t v = vb + tid; v < vb + nb; v += blockDim.x) {
+        const int32_t d = __ldcg(Dp + v);
+        if (d < 0) {
+          bad = 1;
+          continue;
+        }
+        ssq += (ull)d * (ull)d;
+        int32_t m = a.min_d[v];
+        if (d < m) {
+          m = d;
+          a.min_d[v] = m;
+        }
+        const ull key = ((ull)(uint32_t)m << 32) | (ull)(0xffffffffu - (uint32_t)v);
+        kbest = key > kbest ? key : kbest;
+      }
+      bad = __syncthreads_or(bad);
+      ssq = block_sum(ssq, red);
+      kbest = block_max_u64(kbest, red);
+      if (tid == 0) {
+        a.sumsq[(int64_t)p * a.B + b] = ssq;
+        a.sources[(int64_t)p * a.B + b] = src;
+        if (bad) atomicCAS(a.err, 0, PHDE_ERR_DISCONNECTED);
+        s_src = (int64_t)(0xffffffffu - (uint32_t)(kbest & 0xffffffffull));
+      }
+      __syncthreads();
+      src = s_src;
+      if (bad) break;
+    }
+  }
+  const ull etot = block_sum(edges_local, red);
+  if (tid == 0 && a.edges) atomicAdd(a.edges, etot);
+}
+
 __global__ void fill_i32_kernel(int32_t *p, int64_t n, int32_t v) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -472,5 +599,44 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
       fclose(f);
     }
   }
+  return PHDE_OK;
+}
+
+// Batched Kcenters, one CTA per graph (see kcenters_block_kernel).  d_order lists the graphs largest first.
+int phde_run_bfs_batched_blocks(phde_ctx *ctx, int P, const int32_t *d_order, int32_t *d_D, int64_t *d_sources,
+                                unsigned long long *d_sumsq, unsigned long long *d_edges) {
+  const int64_t N = ctx->n;
+  const int B = ctx->batch_B;
+  int32_t *min_d = (int32_t *)phde_buf(ctx, "kc.min_d", sizeof(int32_t) * N);
+  uint32_t *q0 = (uint32_t *)phde_buf(ctx, "q.v0", sizeof(uint32_t) * N);
+  uint32_t *q1 = (uint32_t *)phde_buf(ctx, "q.v1", sizeof(uint32_t) * N);
+  unsigned *next = (unsigned *)phde_buf(ctx, "kb.next", sizeof(unsigned));
+  if (!min_d || !q0 || !q1 || !next) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(d_D, 0xff, sizeof(int32_t) * (size_t)N * (size_t)P, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(next, 0, sizeof(unsigned), ctx->stream));
+  int rc = phde_fill_i32(ctx, min_d, N, 0x7fffffff);
+  if (rc) return rc;
+  KbArgs a;
+  a.off = ctx->d_off;
+  a.adj = ctx->d_adj;
+  a.N = N;
+  a.D = d_D;
+  a.P = P;
+  a.B = B;
+  a.vbase = ctx->d_vbase;
+  a.order = d_order;
+  a.next = next;
+  a.sources = d_sources;
+  a.min_d = min_d;
+  a.sumsq = d_sumsq;
+  a.q0 = q0;
+  a.q1 = q1;
+  a.edges = d_edges;
+  a.err = ctx->d_err;
+  int per_sm = 0;
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kcenters_block_kernel, KB_THREADS, 0));
+  const int grid = std::max(1, std::min(B, ctx->nsm * std::max(per_sm, 1)));
+  kcenters_block_kernel<<<grid, KB_THREADS, 0, ctx->stream>>>(a);
+  PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

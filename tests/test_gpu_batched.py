@@ -75,3 +75,19 @@ def test_batched_rejects_bad_input():
         cb.layout_batched(10, 2)  # 20 vertices <= 3k pivots
     with pytest.raises(ParHDEError):
         cb.layout_batched(40, 2)  # k above 32
+
+
+def test_block_per_graph_kcenters_matches_union(monkeypatch):
+    """The one-CTA-per-graph Kcenters (large batches) and the whole-grid batched Kcenters give the same
+    distance columns and pivots, so the same layouts bit for bit."""
+    gs = batch_graphs()
+    out = {}
+    for mode in ("union", "blocks"):
+        monkeypatch.setenv("PHDE_BATCH_BFS", mode)
+        cb = Context(0)
+        cb.upload_batch(gs)
+        xs, st = cb.layout_batched(10, 2)
+        out[mode] = [x.copy() for x in xs]
+        cb.close()
+    for a, b in zip(out["union"], out["blocks"]):
+        assert np.array_equal(a, b)
