@@ -164,6 +164,17 @@ class Context:
         return int(self._L.phde_selftest_barrier_timeout(self._h, timeout_ms))
 
 
+def write_nxyz_fast(path: str, coords: np.ndarray, nthreads: int = 0) -> None:
+    """phde_write_nxyz: the .nxyz file of an (n, c) coordinate array, formatted by host threads in the
+    library -- byte-identical to ``csr_io.write_nxyz`` and the reference's writeCoords."""
+    X = np.asarray(coords, dtype=np.float64)
+    n, c = X.shape
+    colmajor = np.ascontiguousarray(X.T).ravel()
+    rc = _lib.load().phde_write_nxyz(path.encode(), _ptr(colmajor, C.c_double), n, c, nthreads)
+    if rc != 0:
+        raise ParHDEError(rc, "phde_write_nxyz failed for " + path)
+
+
 # ---------------------------------------------------------------------------------------------
 # The reference's class interface (variants/DrawingBase.h:41-47, ParHDE.h, WParHDE.h, PivotMDS.h, PHDE.h).
 

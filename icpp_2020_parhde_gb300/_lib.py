@@ -26,7 +26,7 @@ EXPORTS = [
     "phde_create", "phde_destroy", "phde_last_error", "phde_status_string", "phde_version", "phde_graph_upload",
     "phde_graph_n", "phde_graph_nnz", "phde_layout", "phde_distances", "phde_kcenters", "phde_DOBFS",
     "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
-    "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched",
+    "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched", "phde_write_nxyz",
 ]
 
 
@@ -99,5 +99,6 @@ def load(path: str | None = None):
     L.phde_set_pivot_model.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
     L.phde_batch_upload.argtypes = [vp, C.POINTER(GraphDesc), C.c_int]
     L.phde_layout_batched.argtypes = [vp, C.POINTER(LayoutOpts), f64p, C.POINTER(LayoutStats)]
+    L.phde_write_nxyz.argtypes = [C.c_char_p, f64p, i64, C.c_int, C.c_int]
     _lib = L
     return L

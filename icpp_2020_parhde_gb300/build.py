@@ -1,8 +1,8 @@
 """Build the GB300 layout library in-tree.
 
 ``libparhde_gb300.so``  every ``csrc/*.cu`` compiled for sm_103a (``-gencode arch=compute_103a,code=sm_103a``)
-                        plus the C++ reference-interface classes (``csrc/drawing.cpp``), C ABI in
-                        ``include/parhde.h``.
+                        plus the library's host C++ (the reference-interface classes ``csrc/drawing.cpp``,
+                        the parallel ``.nxyz`` writer ``csrc/nxyz.cpp``), C ABI in ``include/parhde.h``.
 ``embed``               the drop-in driver (``csrc/embed.cpp``), linked against the library.
 
 Translation units are compiled in parallel and only when a source or header is newer than its object.
@@ -72,18 +72,20 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)
-    cpp = os.path.join(CSRC, "drawing.cpp")
-    if os.path.exists(cpp):
-        obj = os.path.join(OBJ_DIR, "drawing.cpp.o")
+    # host C++ of the library (the reference-interface classes, the .nxyz writer); embed.cpp is the driver
+    for cpp in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
+        if os.path.basename(cpp) == "embed.cpp":
+            continue
+        obj = os.path.join(OBJ_DIR, os.path.basename(cpp) + ".o")
         objs.append(obj)
         if force or _stale(obj, [cpp] + hdrs):
-            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-I" + INCLUDE, "-c", cpp, "-o", obj])
+            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-pthread", "-I" + INCLUDE, "-c", cpp, "-o", obj])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB_PATH, objs):
         tmp = LIB_PATH + ".tmp"
-        _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
         os.replace(tmp, LIB_PATH)
     emb = os.path.join(CSRC, "embed.cpp")
     if os.path.exists(emb) and (force or _stale(EMBED_PATH, [emb, LIB_PATH] + hdrs)):

@@ -21,13 +21,8 @@ static void write_coords(long n, const double *xy, int c, const char *input) {
   std::string name(input);
   name += "_hde.nxyz";
   std::cout << "Writing coordinates to file " << name << std::endl;
-  std::ofstream out(name);
-  for (long i = 0; i < n; i++) {
-    for (int j = 0; j < c; j++) {
-      out << xy[i + (long)j * n];
-      out << (j + 1 < c ? "," : "\n");
-    }
-  }
+  // the library's parallel writer: the reference's ostream formatting, byte for byte
+  if (phde_write_nxyz(name.c_str(), xy, n, c, 0) != PHDE_OK) std::cerr << "cannot write " << name << std::endl;
 }
 
 int main(int argc, char **argv) {

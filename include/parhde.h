@@ -147,6 +147,12 @@ typedef struct {
   const uint32_t *adj; /* nnz neighbour ids in 0..n-1 */
   int64_t n, nnz;
 } phde_graph_desc;
+/* Write coordinates (column-major n x c, the layout phde_layout returns) as a .nxyz text file: one line
+ * per vertex, "x0,x1[,x2...]", each value formatted like std::ostream's default (%g, 6 significant digits)
+ * -- byte-identical to the reference's writeCoords (spectralDrawing.cpp:42-65), formatted by `nthreads`
+ * host threads (0: all cores).  Host only; needs no context. */
+int phde_write_nxyz(const char *path, const double *coords, int64_t n, int c, int nthreads);
+
 int phde_batch_upload(phde_ctx *ctx, const phde_graph_desc *graphs, int count);
 int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out, phde_layout_stats *stats);
 

@@ -114,3 +114,19 @@ def test_relabel_is_isomorphic():
     for v in (0, 5, g.n - 1):
         nb = np.sort(perm[g.adj[g.offsets[v]:g.offsets[v + 1]].astype(np.int64)])
         assert np.array_equal(h.adj[h.offsets[perm[v]]:h.offsets[perm[v] + 1]].astype(np.int64), nb)
+
+
+def test_fast_nxyz_writer_is_byte_identical(tmp_path):
+    """phde_write_nxyz (parallel host formatter in the library) against the %g formatting of the
+    reference's writeCoords, on values that exercise every %g branch."""
+    from icpp_2020_parhde_gb300 import write_nxyz_fast
+    rng = np.random.default_rng(3)
+    n = 20000
+    X = rng.standard_normal((n, 3)) * np.logspace(-12, 12, n)[:, None]
+    X[:8, 0] = [0.0, -0.0, 1e-5, 1e-4, 123456.5, 1234567.0, 0.1 + 0.2, -9.999995e-7]
+    X[:4, 1] = [np.inf, -np.inf, 1e300, -1e-300]
+    for c, nth in ((2, 1), (3, 0), (3, 7)):
+        p1, p2 = tmp_path / "a.nxyz", tmp_path / "b.nxyz"
+        csr_io.write_nxyz(str(p1), X[:, :c])
+        write_nxyz_fast(str(p2), X[:, :c], nthreads=nth)
+        assert p1.read_bytes() == p2.read_bytes()
