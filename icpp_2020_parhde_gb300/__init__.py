@@ -132,6 +132,28 @@ class Context:
         self._check(self._L.phde_kcenters(self._h, passes, variant, _ptr(D, C.c_int32), _ptr(src, C.c_int64)))
         return (D.reshape(passes, self.n).T if D is not None else None), src
 
+    def graph_from_entries(self, u, v, w, n1: int, n2: int, symmetric: bool) -> dict:
+        """phde_graph_from_entries: Matrix Market entries (1-indexed) -> the uploaded graph, on the GPU (the
+        reference's mtx2csr).  Returns the conversion counts."""
+        u = np.ascontiguousarray(u, dtype=np.uint32)
+        v = np.ascontiguousarray(v, dtype=np.uint32)
+        wa = None if w is None else np.ascontiguousarray(w, dtype=np.int32)
+        info = _lib.CsrInfo()
+        self._check(self._L.phde_graph_from_entries(self._h, _ptr(u, C.c_uint32), _ptr(v, C.c_uint32),
+                                                    _ptr(wa, C.c_int32), u.shape[0], n1, n2, 1 if symmetric else 0,
+                                                    C.byref(info)))
+        self.n, self.nnz, self.weighted = info.n, info.nnz, wa is not None
+        return {f: getattr(info, f) for f, _ in info._fields_}
+
+    def download(self) -> CSRGraph:
+        """phde_graph_download: the uploaded graph as host arrays (uint32 offsets)."""
+        off = np.empty(self.n + 1, dtype=np.uint32)
+        adj = np.empty(max(self.nnz, 1), dtype=np.uint32)
+        w = np.empty(max(self.nnz, 1), dtype=np.int32) if self.weighted else None
+        self._check(self._L.phde_graph_download(self._h, _ptr(off, C.c_uint32), _ptr(adj, C.c_uint32),
+                                                _ptr(w, C.c_int32)))
+        return CSRGraph(off, adj[: self.nnz], None if w is None else w[: self.nnz])
+
     def upload_batch(self, graphs) -> None:
         """Upload many graphs as one batch (phde_batch_upload); they keep their own local vertex ids."""
         keep, descs = [], []

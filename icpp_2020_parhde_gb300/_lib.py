@@ -27,12 +27,18 @@ EXPORTS = [
     "phde_graph_n", "phde_graph_nnz", "phde_layout", "phde_distances", "phde_kcenters", "phde_DOBFS",
     "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
     "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched", "phde_write_nxyz",
+    "phde_graph_from_entries", "phde_graph_download",
 ]
 
 
 class LayoutOpts(C.Structure):
     _fields_ = [("algo", C.c_int), ("strategy", C.c_int), ("k", C.c_int), ("c", C.c_int), ("precision", C.c_int),
                 ("eig", C.c_int), ("seed", C.c_uint64), ("verbose", C.c_int)]
+
+
+class CsrInfo(C.Structure):
+    _fields_ = [("n_in", C.c_int64), ("nnz_dedup", C.c_int64), ("ncomponents", C.c_int64), ("n", C.c_int64),
+                ("nnz", C.c_int64)]
 
 
 class GraphDesc(C.Structure):
@@ -100,5 +106,7 @@ def load(path: str | None = None):
     L.phde_batch_upload.argtypes = [vp, C.POINTER(GraphDesc), C.c_int]
     L.phde_layout_batched.argtypes = [vp, C.POINTER(LayoutOpts), f64p, C.POINTER(LayoutStats)]
     L.phde_write_nxyz.argtypes = [C.c_char_p, f64p, i64, C.c_int, C.c_int]
+    L.phde_graph_from_entries.argtypes = [vp, u32p, u32p, i32p, i64, i64, i64, C.c_int, C.POINTER(CsrInfo)]
+    L.phde_graph_download.argtypes = [vp, u32p, u32p, i32p]
     _lib = L
     return L

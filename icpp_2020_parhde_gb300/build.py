@@ -3,7 +3,7 @@
 ``libparhde_gb300.so``  every ``csrc/*.cu`` compiled for sm_103a (``-gencode arch=compute_103a,code=sm_103a``)
                         plus the library's host C++ (the reference-interface classes ``csrc/drawing.cpp``,
                         the parallel ``.nxyz`` writer ``csrc/nxyz.cpp``), C ABI in ``include/parhde.h``.
-``embed``               the drop-in driver (``csrc/embed.cpp``), linked against the library.
+``embed``, ``mtx2csr``    the drop-in drivers (``csrc/embed.cpp``, ``csrc/mtx2csr.cpp``), linked against the library.
 
 Translation units are compiled in parallel and only when a source or header is newer than its object.
 """
@@ -24,6 +24,8 @@ OBJ_DIR = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libparhde_gb300.so")
 EMBED_PATH = os.path.join(LIB_DIR, "embed")
+MTX2CSR_PATH = os.path.join(LIB_DIR, "mtx2csr")
+DRIVERS = ("embed.cpp", "mtx2csr.cpp")  # sources with a main(): built as executables, not into the library
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -74,7 +76,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             jobs.append(cmd)
     # host C++ of the library (the reference-interface classes, the .nxyz writer); embed.cpp is the driver
     for cpp in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
-        if os.path.basename(cpp) == "embed.cpp":
+        if os.path.basename(cpp) in DRIVERS:
             continue
         obj = os.path.join(OBJ_DIR, os.path.basename(cpp) + ".o")
         objs.append(obj)
@@ -87,10 +89,12 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         tmp = LIB_PATH + ".tmp"
         _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
         os.replace(tmp, LIB_PATH)
-    emb = os.path.join(CSRC, "embed.cpp")
-    if os.path.exists(emb) and (force or _stale(EMBED_PATH, [emb, LIB_PATH] + hdrs)):
-        _run(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, emb, "-o", EMBED_PATH, "-L" + LIB_DIR, "-lparhde_gb300",
-              "-Wl,-rpath,$ORIGIN"])
+    for drv in DRIVERS:  # command-line drop-ins, linked against the library
+        src = os.path.join(CSRC, drv)
+        exe = os.path.join(LIB_DIR, os.path.splitext(drv)[0])
+        if os.path.exists(src) and (force or _stale(exe, [src, LIB_PATH] + hdrs)):
+            _run(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, src, "-o", exe, "-L" + LIB_DIR, "-lparhde_gb300",
+                  "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("built", LIB_PATH)
     return LIB_PATH

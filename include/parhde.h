@@ -147,6 +147,26 @@ typedef struct {
   const uint32_t *adj; /* nnz neighbour ids in 0..n-1 */
   int64_t n, nnz;
 } phde_graph_desc;
+/* ---- input conversion: Matrix Market entries to the layout's CSR (the reference's mtx2csr tool,
+ * mtx2csr.cpp:117-296), on the GPU.  The result becomes the context's uploaded graph. ---- */
+typedef struct {
+  int64_t n_in;         /* vertices of the matrix graph (n1, or n1 + n2 for a bipartite reading) */
+  int64_t nnz_dedup;    /* directed entries after self-loop removal and deduplication */
+  int64_t ncomponents;  /* connected components */
+  int64_t n;            /* vertices of the largest component (the graph kept) */
+  int64_t nnz;          /* its directed entries */
+} phde_csr_info;
+/* u, v: 1-indexed row and column of each of `count` entries; w: their integer weights or NULL.
+ * symmetric != 0: an n1 x n1 matrix read as an undirected graph (each entry both directions, self loops
+ * dropped); symmetric == 0: an n1 x n2 matrix read as a bipartite graph (rows become vertices n2 .. n2+n1-1).
+ * Parallel entries keep the smallest weight; the largest connected component (the one holding the smallest
+ * vertex on ties) is kept and renumbered in increasing order, as the reference does. */
+int phde_graph_from_entries(phde_ctx *ctx, const uint32_t *u, const uint32_t *v, const int32_t *w, int64_t count,
+                            int64_t n1, int64_t n2, int symmetric, phde_csr_info *info);
+/* Copy the uploaded graph to host memory: offsets as uint32 (n + 1), adjacency (nnz), weights (nnz, or NULL).
+ * Sizes from phde_graph_n / phde_graph_nnz. */
+int phde_graph_download(phde_ctx *ctx, uint32_t *offsets, uint32_t *adj, int32_t *weights);
+
 /* Write coordinates (column-major n x c, the layout phde_layout returns) as a .nxyz text file: one line
  * per vertex, "x0,x1[,x2...]", each value formatted like std::ostream's default (%g, 6 significant digits)
  * -- byte-identical to the reference's writeCoords (spectralDrawing.cpp:42-65), formatted by `nthreads`

@@ -1,7 +1,8 @@
 #!/bin/sh
 # Builds the reference ParHDE sources, read in place from the ParHDE tree (never copied), into
 # oracle/_ref/: libparhde_ref.so (reference classes + ref_harness.cpp, for golden generation and
-# oracle pinning) and embed (the reference driver, for .nxyz comparisons and CPU timing).
+# oracle pinning), embed (the reference driver, for .nxyz comparisons and CPU timing) and mtx2csr (the
+# reference's Matrix Market converter, for the converter's golden files).
 # Test infrastructure only.  Usage: oracle/build_ref.sh [path-to-ParHDE-tree]
 set -e
 REF=${1:-${PARHDE_REF_SRC:-/root/reference}}
@@ -30,4 +31,5 @@ wait
 VAR="DrawingBase.o ParallelComponents.o PivotMDS.o PHDE.o WParHDE.o ParHDE.o"
 $CXX -shared -fopenmp -o libparhde_ref.so bfs_h.o sssp_h.o $VAR ref_harness.o
 $CXX $FLAGS $INC "$REF/spectralDrawing.cpp" bfs.o sssp.o $VAR -o embed -lm
-echo "built $OUT/libparhde_ref.so and $OUT/embed"
+$CXX -O2 -std=c++11 -w "$REF/mtx2csr.cpp" -o mtx2csr
+echo "built $OUT/libparhde_ref.so, $OUT/embed and $OUT/mtx2csr"

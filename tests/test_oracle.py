@@ -2,6 +2,7 @@
 reference itself, and against the live reference build when it is present (this container only)."""
 import ctypes
 import ctypes.util
+import os
 
 import numpy as np
 import pytest
@@ -94,3 +95,15 @@ def test_oracle_matches_live_reference_rgg(algo, k, c):
     assert L.status == 0
     assert np.array_equal(L.sources, src)
     np.testing.assert_allclose(L.coords, xy, rtol=0, atol=1e-12)
+
+
+def test_mtx_oracle_matches_reference_converter():
+    """The converter's oracle reproduces the reference mtx2csr's binary CSR byte for byte on every fixture
+    (tests/golden/mtx, written by tests/golden/make_mtx_golden.py with the reference build)."""
+    import glob
+    from oracle import mtx_oracle
+    paths = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "mtx", "*.mtx")))
+    assert len(paths) >= 5
+    for p in paths:
+        with open(p[:-4] + ".csr", "rb") as f:
+            assert mtx_oracle.mtx2csr_bytes(p) == f.read(), p
