@@ -182,6 +182,29 @@ class Context:
             base += nb
         return res, st.as_dict()
 
+    def draw(self, x, y) -> dict:
+        """phde_draw: rasterise the uploaded graph at vertex positions (x, y) on the GPU (the reference's draw
+        tool).  Returns the image geometry and timings; the image stays on the device."""
+        xa = np.ascontiguousarray(x, dtype=np.float64)
+        ya = np.ascontiguousarray(y, dtype=np.float64)
+        if xa.shape != (self.n,) or ya.shape != (self.n,):
+            raise ValueError("x and y need one value per vertex (%d)" % self.n)
+        info = _lib.DrawInfo()
+        self._check(self._L.phde_draw(self._h, _ptr(xa, C.c_double), _ptr(ya, C.c_double), C.byref(info)))
+        self.draw_size = (int(info.width), int(info.height))
+        return info.as_dict()
+
+    def draw_image(self, out: np.ndarray | None = None) -> np.ndarray:
+        """phde_draw_download: the drawn image as an (height, width, 4) RGBA uint8 array."""
+        W, H = self.draw_size
+        img = out if out is not None else np.empty((H, W, 4), dtype=np.uint8)
+        self._check(self._L.phde_draw_download(self._h, img.ctypes.data_as(C.POINTER(C.c_uint8)), img.nbytes))
+        return img
+
+    def draw_png(self, path: str, nthreads: int = 0) -> None:
+        """phde_draw_write_png: the drawn image as a PNG file."""
+        self._check(self._L.phde_draw_write_png(self._h, path.encode(), nthreads))
+
     def selftest_barrier_timeout(self, timeout_ms: int = 50) -> int:
         return int(self._L.phde_selftest_barrier_timeout(self._h, timeout_ms))
 
@@ -195,6 +218,18 @@ def write_nxyz_fast(path: str, coords: np.ndarray, nthreads: int = 0) -> None:
     rc = _lib.load().phde_write_nxyz(path.encode(), _ptr(colmajor, C.c_double), n, c, nthreads)
     if rc != 0:
         raise ParHDEError(rc, "phde_write_nxyz failed for " + path)
+
+
+def write_png(path: str, rgba: np.ndarray, nthreads: int = 0) -> None:
+    """phde_write_png: an (height, width, 4) RGBA uint8 image as a PNG file (palette when it has at most 256
+    colours), deflated by host threads in the library."""
+    img = np.ascontiguousarray(rgba, dtype=np.uint8)
+    if img.ndim != 3 or img.shape[2] != 4:
+        raise ValueError("rgba must be (height, width, 4)")
+    H, W = img.shape[:2]
+    rc = _lib.load().phde_write_png(path.encode(), img.ctypes.data_as(C.POINTER(C.c_uint8)), W, H, nthreads)
+    if rc != 0:
+        raise ParHDEError(rc, "phde_write_png failed for " + path)
 
 
 # ---------------------------------------------------------------------------------------------

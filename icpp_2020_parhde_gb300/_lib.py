@@ -27,7 +27,8 @@ EXPORTS = [
     "phde_graph_n", "phde_graph_nnz", "phde_layout", "phde_distances", "phde_kcenters", "phde_DOBFS",
     "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
     "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched", "phde_write_nxyz",
-    "phde_graph_from_entries", "phde_graph_download",
+    "phde_graph_from_entries", "phde_graph_download", "phde_draw", "phde_draw_download", "phde_draw_write_png",
+    "phde_write_png",
 ]
 
 
@@ -53,6 +54,17 @@ class LayoutStats(C.Structure):
                 ("ms_total", C.c_double), ("edges_examined", C.c_int64), ("ms_dist_kernel", C.c_double),
                 ("dist_kernel_launches", C.c_int), ("ms_msbfs_kernel", C.c_double), ("msbfs_levels", C.c_int),
                 ("batch_graph_replay", C.c_int), ("batch_seg_rows", C.c_int), ("ms_batch_tune", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class DrawInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("width_computed", C.c_uint32),
+                ("height_computed", C.c_uint32), ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double),
+                ("ymax", C.c_double), ("aspect", C.c_double), ("max_edge_length", C.c_float),
+                ("gpu_launches", C.c_int), ("pixels", C.c_int64), ("ms_device", C.c_double),
+                ("ms_raster", C.c_double), ("ms_total", C.c_double)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -108,5 +120,9 @@ def load(path: str | None = None):
     L.phde_write_nxyz.argtypes = [C.c_char_p, f64p, i64, C.c_int, C.c_int]
     L.phde_graph_from_entries.argtypes = [vp, u32p, u32p, i32p, i64, i64, i64, C.c_int, C.POINTER(CsrInfo)]
     L.phde_graph_download.argtypes = [vp, u32p, u32p, i32p]
+    L.phde_draw.argtypes = [vp, f64p, f64p, C.POINTER(DrawInfo)]
+    L.phde_draw_download.argtypes = [vp, C.POINTER(C.c_uint8), C.c_size_t]
+    L.phde_draw_write_png.argtypes = [vp, C.c_char_p, C.c_int]
+    L.phde_write_png.argtypes = [C.c_char_p, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint32, C.c_int]
     _lib = L
     return L

@@ -2,8 +2,10 @@
 
 ``libparhde_gb300.so``  every ``csrc/*.cu`` compiled for sm_103a (``-gencode arch=compute_103a,code=sm_103a``)
                         plus the library's host C++ (the reference-interface classes ``csrc/drawing.cpp``,
-                        the parallel ``.nxyz`` writer ``csrc/nxyz.cpp``), C ABI in ``include/parhde.h``.
-``embed``, ``mtx2csr``    the drop-in drivers (``csrc/embed.cpp``, ``csrc/mtx2csr.cpp``), linked against the library.
+                        the parallel ``.nxyz`` writer ``csrc/nxyz.cpp``, the PNG writer ``csrc/png.cpp``),
+                        C ABI in ``include/parhde.h``.
+``embed``, ``mtx2csr``, ``draw``  the drop-in drivers (``csrc/embed.cpp``, ``csrc/mtx2csr.cpp``,
+                        ``csrc/draw.cpp``), linked against the library.
 
 Translation units are compiled in parallel and only when a source or header is newer than its object.
 """
@@ -25,7 +27,8 @@ LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libparhde_gb300.so")
 EMBED_PATH = os.path.join(LIB_DIR, "embed")
 MTX2CSR_PATH = os.path.join(LIB_DIR, "mtx2csr")
-DRIVERS = ("embed.cpp", "mtx2csr.cpp")  # sources with a main(): built as executables, not into the library
+DRAW_PATH = os.path.join(LIB_DIR, "draw")
+DRIVERS = ("embed.cpp", "mtx2csr.cpp", "draw.cpp")  # sources with a main(): built as executables, not into the library
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -93,8 +96,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         src = os.path.join(CSRC, drv)
         exe = os.path.join(LIB_DIR, os.path.splitext(drv)[0])
         if os.path.exists(src) and (force or _stale(exe, [src, LIB_PATH] + hdrs)):
-            _run(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, src, "-o", exe, "-L" + LIB_DIR, "-lparhde_gb300",
-                  "-Wl,-rpath,$ORIGIN"])
+            _run(["g++", "-std=c++17", "-O2", "-pthread", "-I" + INCLUDE, src, "-o", exe, "-L" + LIB_DIR,
+                  "-lparhde_gb300", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("built", LIB_PATH)
     return LIB_PATH

@@ -17,7 +17,7 @@ struct phde_ctx {
   std::string err;
   long long launches = 0;
   uint64_t timeout_ns = 5000000000ull;  // bounded device waits: 5 s per wait
-  bool column_cgs2 = false;
+  bool column_cgs2 = false;  // mixed path: column-at-a-time CGS2 (PHDE_CGS2=column) instead of blocked
   // uploaded batch (phde_batch_upload): the device CSR is the disjoint union of batch_B graphs
   int batch_B = 0;
   int64_t off_cap = 0, adj_cap = 0, gid_cap = 0;   // allocated entries of d_off, d_adj (and d_w), d_gid
@@ -36,7 +36,12 @@ struct phde_ctx {
   int64_t batch_graph_ws = -1;
   int64_t batch_graph_launches = 0;
   bool batch_no_graph = false;                     // capture failed once: launch directly
-  int64_t ws_epoch = 0;                            // bumped whenever a workspace buffer is (re)allocated             // mixed path: column-at-a-time CGS2 (PHDE_CGS2=column) instead of blocked
+  int64_t ws_epoch = 0;                            // bumped whenever a workspace buffer is (re)allocated
+  // drawing (draw.cu): the entry-row array's graph, and the size of the last image drawn
+  long long draw_rows_epoch = -1;
+  void *draw_rows_buf = nullptr;
+  unsigned draw_W = 0, draw_H = 0;
+  long long draw_epoch = -1;
 
   // uploaded graph (offsets widened to int64)
   int64_t n = 0, nnz = 0;
@@ -96,6 +101,10 @@ void *phde_buf(phde_ctx *ctx, const char *name, size_t bytes);
 int phde_reset_sync(phde_ctx *ctx);
 // Read the device error word after the stream drained; returns PHDE_OK or the recorded status.
 int phde_check_device_err(phde_ctx *ctx, const char *what);
+
+// ---- drawing (draw.cu) ----
+// The last drawn image's 4-bit palette scanlines (H rows of 1 + ceil(W / 2) bytes) copied to the host.
+int phde_draw_scanlines(phde_ctx *ctx, std::vector<uint8_t> &out, unsigned &W, unsigned &H);
 
 // ---- kernels (kcenters.cu) ----
 // Kcenters / fixed-source BFS passes into D (n * P int32, column-major).  variant: 0 ParHDE history

@@ -173,6 +173,35 @@ int phde_graph_download(phde_ctx *ctx, uint32_t *offsets, uint32_t *adj, int32_t
  * host threads (0: all cores).  Host only; needs no context. */
 int phde_write_nxyz(const char *path, const double *coords, int64_t n, int c, int nthreads);
 
+/* ---- drawing: the reference's draw tool (draw_graph.c:135-351), on the GPU ----
+ * phde_draw rasterises the uploaded graph at the vertex positions (x[i], y[i]) (host arrays of n doubles: the
+ * two coordinate columns the draw command line selects) into an image held by the context: the image size from
+ * the coordinate bounds (draw_graph.c:201-249), one Bresenham line per CSR entry u -> v in CSR order, later lines
+ * over earlier ones, coloured by length bin and draw_line's counters (draw_graph.c:49-128, 282-326), on the
+ * (4, 4, 4) background.  The pixels are those of the reference run with one thread.  Coordinates that are not
+ * finite, or a degenerate coordinate range (an image side that is not a positive 32-bit number), return
+ * PHDE_ERR_INVALID; images above 2^20 pixels a side or 2^32 pixels return PHDE_ERR_TOO_LARGE.
+ * phde_draw_download copies the image as RGBA bytes (width * height * 4, row-major, y down the rows as the
+ * reference indexes it); phde_draw_write_png writes it as a PNG file (lodepng_encode32_file's role,
+ * draw_graph.c:331) deflated by nthreads host threads (0: all cores).  phde_write_png writes any RGBA image
+ * the same way (host only; needs no context). */
+typedef struct {
+  uint32_t width, height;                   /* image size, after the reference's size correction       */
+  uint32_t width_computed, height_computed; /* sqrt(100 n / aspect) and aspect * width, before it      */
+  double xmin, xmax, ymin, ymax;            /* coordinate bounds (starting from 1 and -1)               */
+  double aspect;                            /* (xmax - xmin) / (ymax - ymin)                            */
+  float max_edge_length;                    /* longest CSR entry, in pixels                             */
+  int gpu_launches;                         /* kernels this call launched                               */
+  int64_t pixels;                           /* pixel writes of all lines                                */
+  double ms_device;                         /* device time: coordinate copy, bounds, raster, colours    */
+  double ms_raster;                         /* of which the line rasteriser                             */
+  double ms_total;                          /* the whole call, host clock                               */
+} phde_draw_info;
+int phde_draw(phde_ctx *ctx, const double *x, const double *y, phde_draw_info *info);
+int phde_draw_download(phde_ctx *ctx, uint8_t *rgba, size_t bytes);
+int phde_draw_write_png(phde_ctx *ctx, const char *path, int nthreads);
+int phde_write_png(const char *path, const uint8_t *rgba, uint32_t width, uint32_t height, int nthreads);
+
 int phde_batch_upload(phde_ctx *ctx, const phde_graph_desc *graphs, int count);
 int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out, phde_layout_stats *stats);
 

@@ -1,8 +1,9 @@
 #!/bin/sh
 # Builds the reference ParHDE sources, read in place from the ParHDE tree (never copied), into
 # oracle/_ref/: libparhde_ref.so (reference classes + ref_harness.cpp, for golden generation and
-# oracle pinning), embed (the reference driver, for .nxyz comparisons and CPU timing) and mtx2csr (the
-# reference's Matrix Market converter, for the converter's golden files).
+# oracle pinning), embed (the reference driver, for .nxyz comparisons and CPU timing), mtx2csr (the
+# reference's Matrix Market converter, for the converter's golden files) and draw (the reference's
+# edge-image tool, for the rasteriser's golden images).
 # Test infrastructure only.  Usage: oracle/build_ref.sh [path-to-ParHDE-tree]
 set -e
 REF=${1:-${PARHDE_REF_SRC:-/root/reference}}
@@ -32,4 +33,6 @@ VAR="DrawingBase.o ParallelComponents.o PivotMDS.o PHDE.o WParHDE.o ParHDE.o"
 $CXX -shared -fopenmp -o libparhde_ref.so bfs_h.o sssp_h.o $VAR ref_harness.o
 $CXX $FLAGS $INC "$REF/spectralDrawing.cpp" bfs.o sssp.o $VAR -o embed -lm
 $CXX -O2 -std=c++11 -w "$REF/mtx2csr.cpp" -o mtx2csr
-echo "built $OUT/libparhde_ref.so, $OUT/embed and $OUT/mtx2csr"
+# the reference's draw tool with its own flags (Makefile:6,37-38); run with OMP_NUM_THREADS=1 for its serial order
+${CC:-gcc} -std=c99 -O2 -fopenmp -w "$REF/draw_graph.c" "$REF/lodepng.c" -o draw -lm
+echo "built $OUT/libparhde_ref.so, $OUT/embed, $OUT/mtx2csr and $OUT/draw"

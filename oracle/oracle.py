@@ -27,12 +27,12 @@ SSSP_INF = (2**31 - 1) // 2
 def build_oracle(force: bool = False) -> str:
     """Compile parhde_oracle.c with the reference's optimisation level (-O2) and OpenMP.  No FMA contraction:
     the reference is built in ISO C++ mode, where gcc keeps a*b+c as two roundings on every architecture."""
-    src = os.path.join(HERE, "parhde_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("parhde_oracle.c", "draw_oracle.c")]
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, srcs)):
         tmp = LIB_PATH + ".tmp"
-        subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", src, "-o",
-                               tmp, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", *srcs,
+                               "-o", tmp, "-lm"])
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -84,6 +84,9 @@ def lib():
                                    i64p]
         L.orc_glibc_rand.argtypes = [C.c_uint32, C.c_int, i32p]
         L.orc_check_csr.argtypes = [u32p, u32p, C.c_int64, C.c_int64]
+        L.orc_draw_geometry.argtypes = [f64p, f64p, C.c_long, f64p, C.POINTER(C.c_uint)]
+        L.orc_draw.argtypes = [u32p, u32p, C.c_long, C.c_long, f64p, f64p, C.POINTER(C.c_ubyte), C.c_uint, C.c_uint,
+                               C.POINTER(C.c_float)]
         _lib = L
     return _lib
 
@@ -228,3 +231,52 @@ def ref_layout(g, algo: str = "ParHDE", strategy: str = "Kcenters", k: int = 10,
     if nc < 0:
         raise RuntimeError("ref_layout failed")
     return coords[: g.n * nc].reshape(nc, g.n).T.copy(), srcs[: ns.value].copy()
+
+
+# ----------------------------------------------------------------------------- the draw tool (draw_oracle.c)
+
+REF_DRAW_PATH = os.path.join(REF_DIR, "draw")
+
+
+def draw_geometry(x, y):
+    """Bounds and image size of draw_graph.c:201-249: (bounds (xmin, xmax, ymin, ymax, aspect),
+    (width, height) as computed, (width, height) as corrected); None when the size is not a positive 32-bit number."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    b = np.zeros(5, dtype=np.float64)
+    d = np.zeros(4, dtype=np.uint32)
+    rc = lib().orc_draw_geometry(_p(x, C.c_double), _p(y, C.c_double), len(x), _p(b, C.c_double),
+                                 d.ctypes.data_as(C.POINTER(C.c_uint)))
+    if rc != 0:
+        return None
+    return tuple(b), (int(d[0]), int(d[1])), (int(d[2]), int(d[3]))
+
+
+def draw(g, x, y):
+    """The reference's edge image for graph g at vertex positions (x, y): (rgba (H, W, 4) uint8, max edge length)."""
+    geo = draw_geometry(x, y)
+    if geo is None:
+        raise ValueError("image size is not a positive 32-bit number")
+    W, H = geo[2]
+    off, adj, _ = _csr_args(g)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    img = np.zeros((H, W, 4), dtype=np.uint8)
+    ml = C.c_float(0)
+    rc = lib().orc_draw(_p(off, C.c_uint32), _p(adj, C.c_uint32), g.n, g.nnz, _p(x, C.c_double), _p(y, C.c_double),
+                        img.ctypes.data_as(C.POINTER(C.c_ubyte)), W, H, C.byref(ml))
+    if rc != 0:
+        raise RuntimeError("orc_draw failed")
+    return img, float(ml.value)
+
+
+def ref_draw_available() -> bool:
+    return os.access(REF_DRAW_PATH, os.X_OK)
+
+
+def ref_draw(csr_path: str, coords_path: str, png_path: str, ncoords: int, first: int, second: int) -> str:
+    """Run the reference's draw binary (one OpenMP thread: its serial order) and return its standard output."""
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([REF_DRAW_PATH, csr_path, coords_path, png_path, str(ncoords), str(first), str(second)],
+                       env=env, capture_output=True, text=True, check=True)
+    return r.stdout + r.stderr

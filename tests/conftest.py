@@ -57,3 +57,26 @@ def gpu_ctx():
     ctx = Context(0)
     yield ctx
     ctx.close()
+
+
+# ---- draw fixtures (tests/golden/draw, made by tests/golden/make_draw_golden.py) ----
+DRAW_DIR = os.path.join(GOLDEN_DIR, "draw")
+
+
+def draw_case_names():
+    import json
+    path = os.path.join(DRAW_DIR, "cases.json")
+    return sorted(json.load(open(path))) if os.path.exists(path) else []
+
+
+def load_draw_case(name: str):
+    """(graph, x, y, meta, reference png path): the coordinate columns the case's command line selects,
+    parsed from the .nxyz text as the reference's fscanf("%lf") reads them."""
+    import json
+    from icpp_2020_parhde_gb300.csr_io import read_csr
+    meta = json.load(open(os.path.join(DRAW_DIR, "cases.json")))[name]
+    base = os.path.join(DRAW_DIR, name)
+    g = read_csr(base + ".csr")
+    with open(base + ".nxyz") as f:
+        rows = np.array([[float(t) for t in line.split(",")] for line in f if line.strip()], dtype=np.float64)
+    return g, rows[:, meta["first"] - 1].copy(), rows[:, meta["second"] - 1].copy(), meta, base + ".png"

@@ -130,3 +130,27 @@ def test_fast_nxyz_writer_is_byte_identical(tmp_path):
         csr_io.write_nxyz(str(p1), X[:, :c])
         write_nxyz_fast(str(p2), X[:, :c], nthreads=nth)
         assert p1.read_bytes() == p2.read_bytes()
+
+
+def test_png_writer_round_trip(tmp_path):
+    """phde_write_png (host code of the library): palette images of 1, 2, 4 and 8 bits, and RGBA, decode to the
+    same pixels."""
+    import pngdecode
+    from icpp_2020_parhde_gb300 import write_png
+    rng = np.random.default_rng(7)
+    for (H, W, ncol) in [(7, 5, 2), (40, 33, 4), (33, 257, 9), (64, 64, 200), (50, 70, 300), (1, 1, 1), (3, 1000, 17)]:
+        cols = rng.integers(0, 256, (ncol, 4), dtype=np.uint8)
+        idx = rng.integers(0, ncol, (H, W))
+        idx[:, : W // 2] = 0  # long runs
+        img = cols[idx]
+        path = str(tmp_path / ("t%d_%d_%d.png" % (H, W, ncol)))
+        write_png(path, img, nthreads=3)
+        assert np.array_equal(pngdecode.read(path), img)
+    # a larger image spread over many deflate ranges
+    img = np.zeros((1500, 1200, 4), np.uint8)
+    img[..., 3] = 255
+    img[::7, :, 0] = 200
+    img[:, ::13, 1] = 100
+    path = str(tmp_path / "big.png")
+    write_png(path, img, nthreads=8)
+    assert np.array_equal(pngdecode.read(path), img)

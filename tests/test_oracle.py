@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_NAMES, golden_runs, load_golden
+from conftest import GOLDEN_NAMES, draw_case_names, golden_runs, load_draw_case, load_golden
 from oracle import oracle as orc
 
 
@@ -107,3 +107,24 @@ def test_mtx_oracle_matches_reference_converter():
     for p in paths:
         with open(p[:-4] + ".csr", "rb") as f:
             assert mtx_oracle.mtx2csr_bytes(p) == f.read(), p
+
+
+# ---------------------------------------------------------------------------------------------- draw
+@pytest.mark.parametrize("name", draw_case_names())
+def test_draw_oracle_matches_reference_png(name):
+    """The draw restatement reproduces the reference draw tool's image (its PNG decoded) pixel for pixel."""
+    import pngdecode
+    g, x, y, meta, png = load_draw_case(name)
+    img, _ = orc.draw(g, x, y)
+    ref = pngdecode.read(png)
+    assert img.shape == ref.shape
+    assert np.array_equal(img, ref)
+
+
+def test_draw_oracle_geometry_degenerate():
+    # equal x: zero range, no image size
+    assert orc.draw_geometry(np.full(10, 0.25), np.linspace(-3, 3, 10)) is None
+    # equal y = 2: the bounds start at 1 and -1, so the y range is [1, 2] and the image exists
+    (xmin, xmax, ymin, ymax, aspect), (w0, h0), (W, H) = orc.draw_geometry(np.linspace(0, 5, 10), np.full(10, 2.0))
+    assert (xmin, xmax, ymin, ymax, aspect) == (0.0, 5.0, 1.0, 2.0, 5.0)
+    assert (w0, h0, W, H) == (14, 70, 14, 70)
