@@ -182,6 +182,20 @@ class Context:
             base += nb
         return res, st.as_dict()
 
+    def gram_f32(self, A, B, w=None, nsplit: int = 0) -> np.ndarray:
+        """phde_gram_f32: A^T diag(w) B (FP64 result) on the tensor cores, for FP32 row-major A (n, p), B (n, q)."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        B = np.ascontiguousarray(B, dtype=np.float32)
+        n, p = A.shape
+        q = B.shape[1]
+        if B.shape[0] != n:
+            raise ValueError("A and B need the same rows")
+        wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+        G = np.empty((p, q), dtype=np.float64)
+        self._check(self._L.phde_gram_f32(self._h, _ptr(A, C.c_float), p, p, _ptr(B, C.c_float), q, q,
+                                          _ptr(wa, C.c_double), n, nsplit, _ptr(G, C.c_double)))
+        return G
+
     def draw(self, x, y) -> dict:
         """phde_draw: rasterise the uploaded graph at vertex positions (x, y) on the GPU (the reference's draw
         tool).  Returns the image geometry and timings; the image stays on the device."""

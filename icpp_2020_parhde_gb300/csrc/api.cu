@@ -199,6 +199,10 @@ int phde_create(phde_ctx **out, int device) {
   for (auto &e : c->kev) cudaEventCreate(&e);
   if (const char *t = getenv("PHDE_WAIT_LIMIT_MS")) c->timeout_ns = (uint64_t)atoll(t) * 1000000ull;
   if (const char *t = getenv("PHDE_CGS2")) c->column_cgs2 = std::string(t) == "column";
+  if (const char *t = getenv("PHDE_TC_GRAM")) {
+    c->tc_gram = std::string(t) != "0";
+    c->tc_gram_cgs2 = std::string(t) == "all";
+  }
   *out = c;
   return PHDE_OK;
 }

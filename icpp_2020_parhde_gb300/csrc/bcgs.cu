@@ -288,6 +288,8 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
   const int64_t n = ctx->n;
   if (ctx->weighted) return phde_fail(ctx, PHDE_ERR_INVALID, "blocked CGS2 takes unweighted graphs");
   const int ncta = ctx->nsm * 6;  // Gram row slabs (several CTAs per SM hide the staging latency)
+  const int ncta_tc = ctx->nsm * 2;  // tensor-core Gram: two CTAs per SM (88 KB of stages each)
+  const int ncta_g = ctx->tc_gram_cgs2 ? ncta_tc : ncta;
   const int nqc_max = (k + 1 + QCH - 1) / QCH;
   float *X = (float *)phde_buf(ctx, "bcgs.X", sizeof(float) * n * BB);
   float *part = (float *)phde_buf(ctx, "bcgs.part", sizeof(float) * (size_t)nqc_max * ncta * QCH * BB);
@@ -313,25 +315,33 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
     bcgs_load_kernel<<<g_rows, GT, 0, ctx->stream>>>(D, n, rc0, bc, sumsq, X);
     PHDE_LAUNCHED(ctx);
     const int nqt = j + 1;
-    const int qc = nqt <= 8 ? 8 : (nqt <= 32 ? 32 : 64), nqc = (nqt + qc - 1) / qc;
+    const int qc = ctx->tc_gram_cgs2 ? QCH : nqt <= 8 ? 8 : (nqt <= 32 ? 32 : 64), nqc = (nqt + qc - 1) / qc;
     for (int pass = 0; pass < 2; pass++) {
-      if (qc == 8)
+      if (ctx->tc_gram_cgs2) {
+        const int rc = phde_tc_gram32(ctx, S, k, j, 1, X, deg, n, ncta_tc, nqc, 0, part);
+        if (rc) return rc;
+      } else if (qc == 8)
         bcgs_gram_kernel<8, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
       else if (qc == 32)
         bcgs_gram_kernel<32, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
       else
         bcgs_gram_kernel<64, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
-      PHDE_LAUNCHED(ctx);
-      bcgs_reduce_kernel<<<nqt, RED_THREADS, 0, ctx->stream>>>(part, ncta, j, 0, dden, n_den0, C, nullptr, qc);
+      if (!ctx->tc_gram_cgs2) PHDE_LAUNCHED(ctx);
+      bcgs_reduce_kernel<<<nqt, RED_THREADS, 0, ctx->stream>>>(part, ncta_g, j, 0, dden, n_den0, C, nullptr, qc);
       PHDE_LAUNCHED(ctx);
       const size_t smem = sizeof(float) * ((size_t)nqt * BB + (size_t)j * ST_LD);
       bcgs_update_kernel<<<g_rows, GT, smem, ctx->stream>>>(S, k, j, C, X, n);
       PHDE_LAUNCHED(ctx);
     }
     // block Grams X^T D X and X^T X in one pass; G holds them one after the other (64 rows of 32)
-    bcgs_gram_kernel<32, true><<<dim3(ncta, 1), GT, 0, ctx->stream>>>(X, BB, BB, 0, X, deg, n, part);
-    PHDE_LAUNCHED(ctx);
-    bcgs_reduce_kernel<<<2 * BB, RED_THREADS, 0, ctx->stream>>>(part, ncta, BB, 1, nullptr, 0.0, nullptr, G, 2 * BB);
+    if (ctx->tc_gram_cgs2) {
+      const int rc = phde_tc_gram32(ctx, nullptr, 0, 0, 0, X, deg, n, ncta_tc, 1, 1, part);
+      if (rc) return rc;
+    } else {
+      bcgs_gram_kernel<32, true><<<dim3(ncta, 1), GT, 0, ctx->stream>>>(X, BB, BB, 0, X, deg, n, part);
+      PHDE_LAUNCHED(ctx);
+    }
+    bcgs_reduce_kernel<<<2 * BB, RED_THREADS, 0, ctx->stream>>>(part, ncta_g, BB, 1, nullptr, 0.0, nullptr, G, 2 * BB);
     PHDE_LAUNCHED(ctx);
     bcgs_block_gs_kernel<<<1, bcgs_gs::NW * 32, 0, ctx->stream>>>(G, G + BB * BB, bc, k, rc0, st, dlog, R);
     PHDE_LAUNCHED(ctx);

@@ -18,6 +18,11 @@ struct phde_ctx {
   long long launches = 0;
   uint64_t timeout_ns = 5000000000ull;  // bounded device waits: 5 s per wait
   bool column_cgs2 = false;  // mixed path: column-at-a-time CGS2 (PHDE_CGS2=column) instead of blocked
+  // mixed path: S^T (L S) on the tensor cores (PHDE_TC_GRAM=0: FP32 CUDA cores); the CGS2 Grams on them too
+  // with PHDE_TC_GRAM=all (slower there: those Grams are 32 columns wide and stream at the memory roofline
+  // on the CUDA cores)
+  bool tc_gram = true;
+  bool tc_gram_cgs2 = false;
   // uploaded batch (phde_batch_upload): the device CSR is the disjoint union of batch_B graphs
   int batch_B = 0;
   int64_t off_cap = 0, adj_cap = 0, gid_cap = 0;   // allocated entries of d_off, d_adj (and d_w), d_gid
@@ -101,6 +106,15 @@ void *phde_buf(phde_ctx *ctx, const char *name, size_t bytes);
 int phde_reset_sync(phde_ctx *ctx);
 // Read the device error word after the stream drained; returns PHDE_OK or the recorded status.
 int phde_check_device_err(phde_ctx *ctx, const char *what);
+
+// ---- tensor-core Gram products (tcgram.cu) ----
+// FP64 partials [nsplit][acols x bcols] of A^T diag(w) B (w may be null).
+int phde_tc_gram64(phde_ctx *ctx, const float *A, int lda, int acols, const float *B, int ldb, int bcols,
+                   const double *w, int64_t n, int nsplit, double *out64);
+// FP32 partials in the blocked-CGS2 layout (bcgs.cu): self == 0 projection [S u0]^T D X over nqc chunks of 64
+// Gram rows, self == 1 block Grams (X^T D X, X^T X).
+int phde_tc_gram32(phde_ctx *ctx, const float *A, int lda, int nq, int ones, const float *X, const double *w,
+                   int64_t n, int ncta, int nqc, int self, float *part);
 
 // ---- drawing (draw.cu) ----
 // The last drawn image's 4-bit palette scanlines (H rows of 1 + ceil(W / 2) bytes) copied to the host.

@@ -634,6 +634,17 @@ int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float 
 
 int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double *M) {
   const int tiles = (k + GT - 1) / GT;
+  if (ctx->tc_gram) {  // tensor cores (tcgram.cu): 2 CTAs per SM, rows split evenly
+    const int splits =
+        (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * 2 / (tiles * tiles), (ctx->n + 1023) / 1024));
+    double *part = (double *)phde_buf(ctx, "gram32.part", sizeof(double) * (size_t)splits * k * k);
+    if (!part) return PHDE_ERR_OOM;
+    int rc = phde_tc_gram64(ctx, A, k, k, B, k, k, nullptr, ctx->n, splits, part);
+    if (rc) return rc;
+    sum_parts32_kernel<<<(int)(((int64_t)k * k + 31) / 32), 256, 0, ctx->stream>>>(part, splits, (int64_t)k * k, M);
+    PHDE_LAUNCHED(ctx);
+    return PHDE_OK;
+  }
   const int splits =
       (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * 8 / (tiles * tiles), (ctx->n + 255) / 256));
   double *part = (double *)phde_buf(ctx, "gram32.part", sizeof(double) * (size_t)splits * k * k);

@@ -231,6 +231,13 @@ int phde_DeltaStep(const uint32_t *row, const uint32_t *col, const int32_t *weig
  * Returns PHDE_ERR_TIMEOUT when the bounded wait gave up as designed. */
 int phde_selftest_barrier_timeout(phde_ctx *ctx, int timeout_ms);
 
+/* Diagnostics used by the tests: G = A^T diag(w) B through the tensor-core Gram kernel of the mixed path
+ * (FP32 inputs split into three BF16 parts, FP32 accumulation in TMEM, FP64 across row blocks).  A: n rows of
+ * acols FP32 (leading dimension lda), B: n rows of bcols (ldb), w: n doubles or NULL, all host arrays; G: acols
+ * x bcols FP64 row-major.  nsplit: row blocks per output tile (0: one per 4096 rows). */
+int phde_gram_f32(phde_ctx *ctx, const float *A, int lda, int acols, const float *B, int ldb, int bcols,
+                  const double *w, int64_t n, int nsplit, double *G);
+
 /* Replace the pivot-scoring MLP used by PHDE_STRAT_LEARNED (4 -> 64 -> 64 -> 1, ReLU): `count` floats,
  * W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3[1] (row-major).  The library starts with the
  * weights trained by icpp_2020_parhde_gb300/train_pivot_mlp.py.  No counterpart in the reference. */
