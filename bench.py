@@ -24,6 +24,9 @@ Reported:
               launch / its event-timed duration, against the measured HBM copy bandwidth; traffic from the
               committed ncu capture; roofline_plain does the same for the plain pipeline's Kcenters BFS
   cpu_baseline  the oracle port of the reference algorithm (OpenMP, all host threads) on the same graph
+  batched     512 random geometric graphs laid out in one phde_layout_batched call, against one call each
+  draw        the draw tool on the headline layout: Bresenham pixel writes per second of device time, the
+              end-to-end path to a PNG file, and the one-thread oracle's rate on an R-MAT-16 sample
 
 N > 1 GPUs: replicas only -- every rank lays out its own copy of the graph; value = all ranks' graphs /
 max-over-ranks time (weak scaling).  --impl reference times the reference algorithm on the host cores.
@@ -66,6 +69,7 @@ def parse():
     ap.add_argument("--no-accept", action="store_true", help="skip the learned-pivot acceptance check")
     ap.add_argument("--relabellings", type=int, default=4)
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-graph batched layout measurement")
+    ap.add_argument("--no-draw", action="store_true", help="skip the draw-tool measurement")
     ap.add_argument("--batch-count", type=int, default=512)
     return ap.parse_args()
 
@@ -429,10 +433,68 @@ def run_gb300(args):
                                          "vs": "Kcenters FP64 with the same pivots and eigensolver"}
     if not args.no_batched:
         line["batched"] = run_batched(args, local, flush_l2)
+    if not args.no_draw:
+        line["draw"] = run_draw(args, ctx, gp, xy_head, flush_l2)
+        ctx.upload(gp)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(g, args, args.cpu_reps)
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def run_draw(args, ctx, g, xy, flush_l2):
+    """The draw tool on the headline layout: its first two coordinates rasterised (phde_draw: bounds, scaling,
+    Bresenham lines of every CSR entry, colour counters, palette scanlines).  value = Bresenham pixel writes per
+    second of device time; e2e = host coordinates -> PNG file through the C ABI (phde_draw + phde_draw_write_png,
+    deflate on the host threads).  The CPU baseline is the one-thread oracle (the reference's serial order) on a
+    bounded sample: an R-MAT scale-16 layout from the same pipeline."""
+    import tempfile
+    from icpp_2020_parhde_gb300 import graphs
+    x, y = np.ascontiguousarray(xy[:, 0]), np.ascontiguousarray(xy[:, 1])
+    ctx.upload(g)
+    for _ in range(args.warmup):
+        info = ctx.draw(x, y)
+    dev, ras = [], []
+    steps = max(3, args.steps // 6)
+    for _ in range(steps):
+        flush_l2()
+        info = ctx.draw(x, y)
+        dev.append(info["ms_device"])
+        ras.append(info["ms_raster"])
+    path = os.path.join(tempfile.mkdtemp(), "draw.png")
+    e2e = []
+    for _ in range(steps):
+        flush_l2()
+        t1 = time.perf_counter()
+        ctx.draw(x, y)
+        ctx.draw_png(path, 0)
+        e2e.append(time.perf_counter() - t1)
+    png_bytes = os.path.getsize(path)
+    px = info["pixels"]
+    out = {"workload": "draw of the headline layout (coordinates 1 and 2) of %s: %d x %d image, %d CSR entries"
+                       % (graph_desc(args), info["width"], info["height"], g.nnz),
+           "value": px / (np.mean(dev) * 1e-3), "unit": "pixel writes/s", "pixels_per_step": px,
+           "ms_device": float(np.mean(dev)), "ms_raster": float(np.mean(ras)),
+           "e2e": {"value": px / float(np.mean(e2e)), "unit": "pixel writes/s", "ms": float(np.mean(e2e)) * 1e3,
+                   "path": "phde_draw + phde_draw_write_png (host coordinates to PNG file)",
+                   "h2d_bytes_per_step": 16 * g.n, "png_bytes": png_bytes},
+           "gpu_launches": info["gpu_launches"]}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        gs = graphs.rmat(16, 16, seed=args.seed)
+        ctx.upload(gs)
+        xs = ctx.layout("ParHDE", k=args.k, c=2, **PIPELINES["learned_mixed"]).coords
+        sx, sy = np.ascontiguousarray(xs[:, 0]), np.ascontiguousarray(xs[:, 1])
+        info_s = ctx.draw(sx, sy)
+        t1 = time.perf_counter()
+        ref, _ = orc.draw(gs, sx, sy)
+        t_cpu = time.perf_counter() - t1
+        same = bool(np.array_equal(ref, ctx.draw_image()))
+        out["cpu_baseline"] = {"value": info_s["pixels"] / t_cpu, "unit": "pixel writes/s", "cores": 1, "kind": "port",
+                               "sample": "R-MAT scale 16 layout (n = %d, %d entries, %d pixel writes) drawn by the "
+                                         "one-thread oracle in %.2f s; identical image on the GPU: %s"
+                                         % (gs.n, gs.nnz, info_s["pixels"], t_cpu, same)}
+    return out
 
 
 def run_batched(args, local, flush_l2):
