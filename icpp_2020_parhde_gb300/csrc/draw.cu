@@ -14,7 +14,8 @@
 //      line of major extent M and minor extent m the minor coordinate after i major steps is
 //      floor((i m + M - floor(M / 2) - 1) / M) -- so a thread can start anywhere on any line.  Every pixel
 //      gets atomicMax(owner, entry + 1): the last entry in CSR order covering a pixel owns it, as the
-//      reference's overwrite order decides;
+//      reference's overwrite order decides.  Tiles run from the last to the first, and an owner that a
+//      cached read already shows to be later needs no atomic (owners only grow);
 //   4. the counters only grow and each grants its colour to the first entries that reach it, so the
 //      entries given each counted colour are exactly those before a cut position.  One CTA finds the four
 //      cuts from the tile counts: entries of bin 0 past the first counter's limit reach the second counter,
@@ -36,8 +37,14 @@ namespace {
 constexpr int RT = 2048;          // CSR entries per raster tile
 constexpr int RT_THREADS = 512;   // threads per raster CTA
 constexpr int RCHUNK = 32;        // pixels per raster chunk
+constexpr int RGROUP = 8;         // pixels whose owner reads a thread issues together
 constexpr int SEL_THREADS = 1024; // the cut-selection CTA
 constexpr uint32_t BG_INDEX = 8;  // palette index of the background
+// The owner image is stored in 8 x 8-pixel tiles (256 bytes, tiles in row-major order): a line of any
+// direction stays inside one tile for about eight steps, so more of its owner reads hit L1.
+__host__ __device__ __forceinline__ size_t tile_index(unsigned x, unsigned y, unsigned tiles_w) {
+  return (((size_t)(y >> 3) * tiles_w + (x >> 3)) << 6) + ((y & 7u) << 3) + (x & 7u);
+}
 constexpr uint32_t MAX_SIDE = 1u << 20;
 
 // colour codes 0..7 (draw_line's colours, draw_graph.c:57-102) and 8 (the background, draw_graph.c:273-277),
@@ -286,6 +293,7 @@ __global__ void __launch_bounds__(RT_THREADS) draw_raster_kernel(const uint32_t 
   const uint32_t P = s_pre[RT];
   if (tid == 0) atomicAdd(pixels, (ull)P);
   const uint32_t nch = (P + RCHUNK - 1) / RCHUNK;
+  const unsigned tiles_w = (W + 7) >> 3;
   for (uint32_t c = tid; c < nch; c += RT_THREADS) {
     const uint32_t p0 = c * RCHUNK, pend = min(p0 + RCHUNK, P);
     int lo = 0, hi = cnt;  // s_pre[lo] <= p0 < s_pre[hi]
@@ -300,21 +308,37 @@ __global__ void __launch_bounds__(RT_THREADS) draw_raster_kernel(const uint32_t 
     Line L;
     line_at(L, s_a[i], s_b[i], k);
     uint32_t tag = (uint32_t)(e0 + i + 1);
-    for (uint32_t p = p0; p < pend; p++) {
-      if ((unsigned)L.cx < W && (unsigned)L.cy < H) {
-        uint32_t *o = &owner[(size_t)L.cy * W + (unsigned)L.cx];
-        if (!SKIP || __ldca(o) < tag) atomicMax(o, tag);
-      }
-      if (--left == 0) {
-        if (p + 1 < pend) {
-          i++;
-          left = s_pre[i + 1] - s_pre[i];
-          line_at(L, s_a[i], s_b[i], 0);
-          tag++;
+    // RGROUP pixels at a time: their positions first, then all their owner reads, then the atomics, so a
+    // thread has RGROUP independent reads in flight instead of one read-compare-atomic chain per pixel
+    for (uint32_t p = p0; p < pend; p += RGROUP) {
+      size_t at[RGROUP];
+      uint32_t tg[RGROUP];
+#pragma unroll
+      for (int q = 0; q < RGROUP; q++) {
+        tg[q] = 0;  // 0: no pixel (past the chunk, or outside the image)
+        if (p + q < pend) {
+          if ((unsigned)L.cx < W && (unsigned)L.cy < H) {
+            at[q] = tile_index((unsigned)L.cx, (unsigned)L.cy, tiles_w);
+            tg[q] = tag;
+          }
+          if (--left == 0) {
+            if (p + q + 1 < pend) {
+              i++;
+              left = s_pre[i + 1] - s_pre[i];
+              line_at(L, s_a[i], s_b[i], 0);
+              tag++;
+            }
+          } else {
+            line_step(L);
+          }
         }
-      } else {
-        line_step(L);
       }
+      uint32_t cur[RGROUP];
+#pragma unroll
+      for (int q = 0; q < RGROUP; q++) cur[q] = (SKIP && tg[q]) ? __ldca(&owner[at[q]]) : 0u;
+#pragma unroll
+      for (int q = 0; q < RGROUP; q++)
+        if (tg[q] && cur[q] < tg[q]) atomicMax(&owner[at[q]], tg[q]);
     }
   }
 }
@@ -470,17 +494,18 @@ __device__ __forceinline__ uint32_t pixel_code(uint32_t o, const uint8_t *bin, i
 __global__ void draw_pack_kernel(const uint32_t *owner, const uint8_t *bin, const int64_t *cuts, unsigned W,
                                  unsigned H, size_t S, uint8_t *packed) {
   const int64_t cut0 = cuts[0], cut2 = cuts[1], cut6 = cuts[2], cut5 = cuts[3];
+  const unsigned tiles_w = (W + 7) >> 3;
   for (unsigned y = blockIdx.x; y < H; y += gridDim.x) {
-    const uint32_t *row = owner + (size_t)y * W;
     uint8_t *out = packed + (size_t)y * S;
     for (size_t j = threadIdx.x; j < S; j += blockDim.x) {
       if (j == 0) {
         out[0] = 0;
         continue;
       }
-      const size_t x = 2 * (j - 1);
-      const uint32_t hi = pixel_code(row[x], bin, cut0, cut2, cut6, cut5);
-      const uint32_t lo = x + 1 < W ? pixel_code(row[x + 1], bin, cut0, cut2, cut6, cut5) : 0u;
+      const unsigned x = 2 * (unsigned)(j - 1);  // even: x and x + 1 share a tile row
+      const size_t t = tile_index(x, y, tiles_w);
+      const uint32_t hi = pixel_code(owner[t], bin, cut0, cut2, cut6, cut5);
+      const uint32_t lo = x + 1 < W ? pixel_code(owner[t + 1], bin, cut0, cut2, cut6, cut5) : 0u;
       out[j] = (uint8_t)((hi << 4) | lo);
     }
   }
@@ -569,9 +594,10 @@ extern "C" int phde_draw(phde_ctx *ctx, const double *x, const double *y, phde_d
     return phde_fail(ctx, PHDE_ERR_TOO_LARGE, "phde_draw: the image exceeds 2^20 pixels a side or 2^32 pixels");
   const double xri = 1.0 / (xmax - xmin), yri = 1.0 / (ymax - ymin);
 
-  const size_t npix = (size_t)W * H, S = 1 + ((size_t)W + 1) / 2;
+  const size_t S = 1 + ((size_t)W + 1) / 2;
+  const size_t npix_tiled = (size_t)((W + 7) >> 3) * ((H + 7) >> 3) * 64;  // >= W * H
   const int64_t ntiles = (nnz + RT - 1) / RT;
-  uint32_t *owner = (uint32_t *)phde_buf(ctx, "draw.owner", sizeof(uint32_t) * npix);
+  uint32_t *owner = (uint32_t *)phde_buf(ctx, "draw.owner", sizeof(uint32_t) * npix_tiled);
   uint8_t *packed = (uint8_t *)phde_buf(ctx, "draw.packed", S * H);
   uint32_t *erow = (uint32_t *)phde_buf(ctx, "draw.erow", sizeof(uint32_t) * std::max<int64_t>(nnz, 1));
   uint8_t *bin = (uint8_t *)phde_buf(ctx, "draw.bin", std::max<int64_t>(nnz, 1));
@@ -593,7 +619,7 @@ extern "C" int phde_draw(phde_ctx *ctx, const double *x, const double *y, phde_d
   draw_scale_kernel<<<grid_of(ctx, n, 256), 256, 0, ctx->stream>>>(d_x, d_y, n, xmin, ymin, xri, yri, W, H, pix);
   PHDE_LAUNCHED(ctx);
   PHDE_CK(ctx, cudaMemsetAsync(misc, 0, sizeof(ull) * 8, ctx->stream));
-  PHDE_CK(ctx, cudaMemsetAsync(owner, 0, sizeof(uint32_t) * npix, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(owner, 0, sizeof(uint32_t) * npix_tiled, ctx->stream));
   if (nnz > 0) {
     draw_maxlen_kernel<<<grid_of(ctx, nnz, 256), 256, 0, ctx->stream>>>(erow, ctx->d_adj, pix, nnz, maxbits);
     PHDE_LAUNCHED(ctx);
