@@ -42,8 +42,8 @@ constexpr int SEL_THREADS = 1024; // the cut-selection CTA
 constexpr uint32_t BG_INDEX = 8;  // palette index of the background
 // The owner image is stored in 8 x 8-pixel tiles (256 bytes, tiles in row-major order): a line of any
 // direction stays inside one tile for about eight steps, so more of its owner reads hit L1.
-__host__ __device__ __forceinline__ size_t tile_index(unsigned x, unsigned y, unsigned tiles_w) {
-  return (((size_t)(y >> 3) * tiles_w + (x >> 3)) << 6) + ((y & 7u) << 3) + (x & 7u);
+__host__ __device__ __forceinline__ uint32_t tile_index(unsigned x, unsigned y, unsigned tiles_w) {
+  return (((y >> 3) * tiles_w + (x >> 3)) << 6) + ((y & 7u) << 3) + (x & 7u);  // < 2^31: the size cap
 }
 constexpr uint32_t MAX_SIDE = 1u << 20;
 
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(RT_THREADS) draw_raster_kernel(const uint32_t 
     // RGROUP pixels at a time: their positions first, then all their owner reads, then the atomics, so a
     // thread has RGROUP independent reads in flight instead of one read-compare-atomic chain per pixel
     for (uint32_t p = p0; p < pend; p += RGROUP) {
-      size_t at[RGROUP];
+      uint32_t at[RGROUP];
       uint32_t tg[RGROUP];
 #pragma unroll
       for (int q = 0; q < RGROUP; q++) {
@@ -503,7 +503,7 @@ __global__ void draw_pack_kernel(const uint32_t *owner, const uint8_t *bin, cons
         continue;
       }
       const unsigned x = 2 * (unsigned)(j - 1);  // even: x and x + 1 share a tile row
-      const size_t t = tile_index(x, y, tiles_w);
+      const uint32_t t = tile_index(x, y, tiles_w);
       const uint32_t hi = pixel_code(owner[t], bin, cut0, cut2, cut6, cut5);
       const uint32_t lo = x + 1 < W ? pixel_code(owner[t + 1], bin, cut0, cut2, cut6, cut5) : 0u;
       out[j] = (uint8_t)((hi << 4) | lo);
@@ -590,8 +590,8 @@ extern "C" int phde_draw(phde_ctx *ctx, const double *x, const double *y, phde_d
     H /= 5;
   }
   if (W == 0 || H == 0) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_draw: the corrected image size is 0");
-  if (W > MAX_SIDE || H > MAX_SIDE || (uint64_t)W * H > (1ull << 32))
-    return phde_fail(ctx, PHDE_ERR_TOO_LARGE, "phde_draw: the image exceeds 2^20 pixels a side or 2^32 pixels");
+  if (W > MAX_SIDE || H > MAX_SIDE || (uint64_t)((W + 7) >> 3) * ((H + 7) >> 3) * 64 > (1ull << 31))
+    return phde_fail(ctx, PHDE_ERR_TOO_LARGE, "phde_draw: the image exceeds 2^20 pixels a side or 2^31 pixels");
   const double xri = 1.0 / (xmax - xmin), yri = 1.0 / (ymax - ymin);
 
   const size_t S = 1 + ((size_t)W + 1) / 2;

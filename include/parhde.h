@@ -180,7 +180,7 @@ int phde_write_nxyz(const char *path, const double *coords, int64_t n, int c, in
  * over earlier ones, coloured by length bin and draw_line's counters (draw_graph.c:49-128, 282-326), on the
  * (4, 4, 4) background.  The pixels are those of the reference run with one thread.  Coordinates that are not
  * finite, or a degenerate coordinate range (an image side that is not a positive 32-bit number), return
- * PHDE_ERR_INVALID; images above 2^20 pixels a side or 2^32 pixels return PHDE_ERR_TOO_LARGE.
+ * PHDE_ERR_INVALID; images above 2^20 pixels a side or 2^31 pixels return PHDE_ERR_TOO_LARGE.
  * phde_draw_download copies the image as RGBA bytes (width * height * 4, row-major, y down the rows as the
  * reference indexes it); phde_draw_write_png writes it as a PNG file (lodepng_encode32_file's role,
  * draw_graph.c:331) deflated by nthreads host threads (0: all cores).  phde_write_png writes any RGBA image
