@@ -8,7 +8,8 @@
 //
 // GB300 issues FP64 at 1/64 of its FP32 rate, so the cost is the number of FP64 warp instructions: every
 // 32-term product is split over the four warps of the CTA (one per SM sub-partition), eight terms each,
-// and the partial sums meet in shared memory.  Lane m of every warp holds component m of t.
+// and the partial sums meet in shared memory.  Lane m of every warp holds component m of t.  The first
+// projection pass starts from t = e_i, where <t, Gd r_a> is the stored (Gd r_a)[i]: no product at all.
 #pragma once
 #include "common.cuh"
 
@@ -58,12 +59,17 @@ __device__ __forceinline__ void run(Smem &S, const double *Gd, const double *G2,
     ncons++;
     double t = m == i ? 1.0 : 0.0;  // every warp keeps the same t
     for (int pass = 0; pass < 2 && nacc > 0; pass++) {
-      if (w == 0) S.tv[m] = t;
-      __syncthreads();
-      // c_a = <t, U_a> / dd_a (lane a), each warp a quarter of the terms
-      S.part[w][m] = m < nacc ? quarter_dot(S.U, m, S.tv, w) : 0.0;
-      __syncthreads();
-      if (w == 0 && m < nacc) S.cv[m] = ((S.part[0][m] + S.part[1][m]) + (S.part[2][m] + S.part[3][m])) / S.dd[m];
+      if (pass == 0) {
+        // t = e_i: <t, U_a> is U_a[i] exactly, no dot product needed
+        if (w == 0 && m < nacc) S.cv[m] = S.U[m][i] / S.dd[m];
+      } else {
+        if (w == 0) S.tv[m] = t;
+        __syncthreads();
+        // c_a = <t, U_a> / dd_a (lane a), each warp a quarter of the terms
+        S.part[w][m] = m < nacc ? quarter_dot(S.U, m, S.tv, w) : 0.0;
+        __syncthreads();
+        if (w == 0 && m < nacc) S.cv[m] = ((S.part[0][m] + S.part[1][m]) + (S.part[2][m] + S.part[3][m])) / S.dd[m];
+      }
       __syncthreads();
       // t -= sum_a c_a R[a][m], warp w takes a = w, w + 4, ...
       double s = 0;
