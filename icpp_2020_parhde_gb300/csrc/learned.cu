@@ -101,48 +101,117 @@ __global__ void feature_max_kernel(const int64_t *off, const int32_t *d0, const 
   }
 }
 
-__global__ void mlp_score_kernel(const int64_t *off, const int32_t *d0, const ull *hop2, const uint32_t *outw,
-                                 const ull *maxes, int64_t n, const float *weights, float *score,
-                                 unsigned *hist, int nbins) {
-  __shared__ float w[MLP_WEIGHTS];
-  extern __shared__ unsigned s_hist[];  // [nbins] per-block histogram, merged at the end
-  for (int i = threadIdx.x; i < MLP_WEIGHTS; i += blockDim.x) w[i] = weights[i];
-  for (int i = threadIdx.x; i < nbins; i += blockDim.x) s_hist[i] = 0u;
-  __syncthreads();
-  const float *W1 = w, *b1 = W1 + MLP_H * MLP_IN, *W2 = b1 + MLP_H, *b2 = W2 + MLP_H * MLP_H, *w3 = b2 + MLP_H,
-              *b3 = w3 + MLP_H;
+// Scores of 128 vertices per tile and 256 threads: features -> F[128][4]; layer 1 (4 -> 64, ReLU) -> H[64][128]
+// (hidden unit major); layer 2 (64 -> 64, ReLU) as a register-tiled product, thread (vg, og) computing
+// vertices 8 vg .. 8 vg + 7 times hidden units 4 og .. 4 og + 3 (32 FMAs per 12 shared-memory words); the
+// output unit's dot product over the 64 hidden units summed across the 16 threads of a vertex group with
+// shuffles; then the sigmoid and the score histogram.
+constexpr int MLP_TILE = 128;
+__global__ void __launch_bounds__(256) mlp_score_kernel(const int64_t *off, const int32_t *d0, const ull *hop2,
+                                                        const uint32_t *outw, const ull *maxes, int64_t n,
+                                                        const float *weights, float *score, unsigned *hist,
+                                                        int nbins) {
+  __shared__ float W1[MLP_H][MLP_IN], b1[MLP_H], b2[MLP_H], w3[MLP_H];
+  __shared__ __align__(16) float W2t[MLP_H][MLP_H];  // W2t[i][o] = W2[o][i]
+  __shared__ float F[MLP_TILE][MLP_IN + 1];
+  __shared__ float s_b3;
+  // dynamic: H[i][v] (layer-1 output i of tile vertex v), then the per-block score histogram [nbins]
+  extern __shared__ __align__(16) float s_dyn[];
+  float(*H)[MLP_TILE] = (float(*)[MLP_TILE])s_dyn;
+  unsigned *s_hist = (unsigned *)(s_dyn + MLP_H * MLP_TILE);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < MLP_H * MLP_IN; i += blockDim.x) W1[i / MLP_IN][i % MLP_IN] = weights[i];
+  const float *gb1 = weights + MLP_H * MLP_IN, *gW2 = gb1 + MLP_H, *gb2 = gW2 + MLP_H * MLP_H, *gw3 = gb2 + MLP_H;
+  for (int i = tid; i < MLP_H; i += blockDim.x) {
+    b1[i] = gb1[i];
+    b2[i] = gb2[i];
+    w3[i] = gw3[i];
+  }
+  for (int i = tid; i < MLP_H * MLP_H; i += blockDim.x) W2t[i % MLP_H][i / MLP_H] = gW2[i];
+  if (tid == 0) s_b3 = gw3[MLP_H];
+  for (int i = tid; i < nbins; i += blockDim.x) s_hist[i] = 0u;
   const float ldeg = logf(1.f + (float)maxes[0]), lhop = logf(1.f + (float)maxes[1]);
   const float md0 = maxes[2] ? (float)maxes[2] : 1.f;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const float deg = (float)(off[v + 1] - off[v]);
-    float f[MLP_IN];
-    f[0] = ldeg > 0.f ? logf(1.f + deg) / ldeg : 0.f;
-    f[1] = lhop > 0.f ? logf(1.f + (float)hop2[v]) / lhop : 0.f;
-    f[2] = (float)(d0[v] < 0 ? 0 : d0[v]) / md0;
-    f[3] = deg > 0.f ? (float)outw[v] / deg : 0.f;
-    float h1[MLP_H];
-#pragma unroll
-    for (int o = 0; o < MLP_H; o++) {
-      float a = b1[o];
-#pragma unroll
-      for (int i = 0; i < MLP_IN; i++) a = fmaf(W1[o * MLP_IN + i], f[i], a);
-      h1[o] = a > 0.f ? a : 0.f;
+  const int og = tid & 15, vg = tid >> 4;  // hidden units 4 og .. 4 og + 3, tile vertices 8 vg .. 8 vg + 7
+  for (int64_t t0 = (int64_t)blockIdx.x * MLP_TILE; t0 < n; t0 += (int64_t)gridDim.x * MLP_TILE) {
+    __syncthreads();  // the weights (first tile) or the previous tile's H and F are no longer read
+    if (tid < MLP_TILE) {
+      const int64_t v = t0 + tid;
+      float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+      if (v < n) {
+        const float deg = (float)(off[v + 1] - off[v]);
+        f0 = ldeg > 0.f ? logf(1.f + deg) / ldeg : 0.f;
+        f1 = lhop > 0.f ? logf(1.f + (float)hop2[v]) / lhop : 0.f;
+        f2 = (float)(d0[v] < 0 ? 0 : d0[v]) / md0;
+        f3 = deg > 0.f ? (float)outw[v] / deg : 0.f;
+      }
+      F[tid][0] = f0;
+      F[tid][1] = f1;
+      F[tid][2] = f2;
+      F[tid][3] = f3;
     }
-    float out = b3[0];
-    for (int o = 0; o < MLP_H; o++) {
-      float a = b2[o];
+    __syncthreads();
+    // layer 1: thread (vg, og) fills H[4 og .. 4 og + 3][8 vg .. 8 vg + 7]
 #pragma unroll
-      for (int i = 0; i < MLP_H; i++) a = fmaf(W2[o * MLP_H + i], h1[i], a);
-      out = fmaf(w3[o], a > 0.f ? a : 0.f, out);
+    for (int j = 0; j < 8; j++) {
+      const int v = vg * 8 + j;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int o = og * 4 + u;
+        float a = b1[o];
+#pragma unroll
+        for (int i = 0; i < MLP_IN; i++) a = fmaf(W1[o][i], F[v][i], a);
+        H[o][v] = a > 0.f ? a : 0.f;
+      }
     }
-    const float p = 1.f / (1.f + expf(-out));
-    score[v] = p;
-    int bin = (int)(p * nbins);
-    bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
-    atomicAdd(s_hist + bin, 1u);
+    __syncthreads();
+    // layer 2 tile: acc[j][u] for vertex 8 vg + j and hidden unit 4 og + u
+    float acc[8][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const float b = b2[og * 4 + u];
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[j][u] = b;
+    }
+#pragma unroll 4
+    for (int i = 0; i < MLP_H; i++) {
+      const float4 ha = *(const float4 *)&H[i][vg * 8], hb = *(const float4 *)&H[i][vg * 8 + 4];
+      const float4 w = *(const float4 *)&W2t[i][og * 4];
+      const float hv[8] = {ha.x, ha.y, ha.z, ha.w, hb.x, hb.y, hb.z, hb.w};
+      const float wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+#pragma unroll
+        for (int u = 0; u < 4; u++) acc[j][u] = fmaf(wv[u], hv[j], acc[j][u]);
+    }
+    // output unit: sum over hidden units of w3 * ReLU(layer 2), the 16 threads of a vertex group combined
+    float part[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      float p = 0.f;
+#pragma unroll
+      for (int u = 0; u < 4; u++) p = fmaf(w3[og * 4 + u], acc[j][u] > 0.f ? acc[j][u] : 0.f, p);
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) p += __shfl_xor_sync(PHDE_FULL_MASK, p, o);
+      part[j] = p;
+    }
+    if (og < 8) {  // lane og of the group finishes vertex 8 vg + og
+      float outv = part[0];
+#pragma unroll
+      for (int j = 1; j < 8; j++)
+        if (og == j) outv = part[j];
+      const int64_t v = t0 + vg * 8 + og;
+      if (v < n) {
+        const float pr = 1.f / (1.f + expf(-(s_b3 + outv)));
+        score[v] = pr;
+        int bin = (int)(pr * nbins);
+        bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+        atomicAdd(s_hist + bin, 1u);
+      }
+    }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+  for (int i = tid; i < nbins; i += blockDim.x)
     if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
 }
 
@@ -215,8 +284,11 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
   PHDE_LAUNCHED(ctx);
   feature_max_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, n, maxes);
   PHDE_LAUNCHED(ctx);
-  mlp_score_kernel<<<g, 256, sizeof(unsigned) * nbins, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts,
-                                                                      score, hist, nbins);
+  const int gm = (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * 4));
+  const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE + sizeof(unsigned) * nbins;
+  PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
+  mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts, score, hist,
+                                                       nbins);
   PHDE_LAUNCHED(ctx);
   std::vector<unsigned> hh(nbins);
   PHDE_CK(ctx, cudaMemcpyAsync(hh.data(), hist, sizeof(unsigned) * nbins, cudaMemcpyDeviceToHost, ctx->stream));
