@@ -195,7 +195,10 @@ __global__ void __launch_bounds__(256) mlp_score_kernel(const int64_t *off, cons
       for (int o = 8; o > 0; o >>= 1) p += __shfl_xor_sync(PHDE_FULL_MASK, p, o);
       part[j] = p;
     }
-    if (og < 8) {  // lane og of the group finishes vertex 8 vg + og
+    // lane og < 8 of the group finishes vertex 8 vg + og; the histogram count is aggregated over the warp's
+    // lanes with the same bin (scores crowd into few bins, so per-vertex atomics would serialise)
+    int bin = -1;
+    if (og < 8) {
       float outv = part[0];
 #pragma unroll
       for (int j = 1; j < 8; j++)
@@ -204,11 +207,12 @@ __global__ void __launch_bounds__(256) mlp_score_kernel(const int64_t *off, cons
       if (v < n) {
         const float pr = 1.f / (1.f + expf(-(s_b3 + outv)));
         score[v] = pr;
-        int bin = (int)(pr * nbins);
+        bin = (int)(pr * nbins);
         bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
-        atomicAdd(s_hist + bin, 1u);
       }
     }
+    const unsigned same = __match_any_sync(PHDE_FULL_MASK, bin);
+    if (bin >= 0 && (tid & 31) == __ffs(same) - 1) atomicAdd(s_hist + bin, (unsigned)__popc(same));
   }
   __syncthreads();
   for (int i = tid; i < nbins; i += blockDim.x)

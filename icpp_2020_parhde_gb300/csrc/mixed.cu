@@ -473,56 +473,63 @@ __global__ void __launch_bounds__(256) sum_parts32_kernel(const double *part, in
 }
 
 // X[i + t*n] = sum_q S[i,q] * Y[q + t*k] (FP32 basis, FP64 eigenvectors and accumulation)
-__global__ void coords32_kernel(const float *S, const double *Y, int64_t n, int k, int c, double *X, double *part) {
-  extern __shared__ double smc[];  // [nw * c] column sums of squares, then FP32 Y
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  float *Ys = (float *)(smc + nw * c);  // Ys[q * c + t]
+// X[:, t] = S Y[:, t] for c <= COORD_MAXC coordinates: a block stages COORD_ROWS consecutive rows of S (one
+// contiguous range of memory, read coalesced) into shared memory, then a thread per row forms its c FP32 dot
+// products over the row's k entries; per-block FP64 sums of squares for the column norms.
+constexpr int COORD_ROWS = 128;
+__global__ void __launch_bounds__(COORD_ROWS) coords32_kernel(const float *S, const double *Y, int64_t n, int k, int c,
+                                                              double *X, double *part) {
+  extern __shared__ float smc[];  // [COORD_ROWS * k] rows of S, then Ys[q * c + t]
+  __shared__ double red[32];
+  float *rows = smc, *Ys = smc + COORD_ROWS * k;
   for (int idx = threadIdx.x; idx < k * c; idx += blockDim.x) {
     const int q = idx / c, t = idx % c;
     Ys[idx] = (float)Y[q + (int64_t)t * k];
   }
-  __syncthreads();
-  const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
   double ss[COORD_MAXC];
 #pragma unroll
   for (int t = 0; t < COORD_MAXC; t++) ss[t] = 0;
-  // a warp per row: FP32 products and sums over the row's k entries, all c coordinates in one read of S
-  for (int64_t i = gw; i < n; i += gws) {
-    float acc[COORD_MAXC];
+  for (int64_t i0 = (int64_t)blockIdx.x * COORD_ROWS; i0 < n; i0 += (int64_t)gridDim.x * COORD_ROWS) {
+    const int nr = (int)min((int64_t)COORD_ROWS, n - i0);
+    __syncthreads();  // Ys written (first tile), or the previous tile's rows read
+    const float *src = S + i0 * k;
+    for (int e = threadIdx.x; e < nr * k; e += blockDim.x) rows[e] = src[e];
+    __syncthreads();
+    if ((int)threadIdx.x < nr) {
+      float acc[COORD_MAXC];
 #pragma unroll
-    for (int t = 0; t < COORD_MAXC; t++) acc[t] = 0.f;
-    for (int q = lane; q < k; q += 32) {
-      const float sv = S[i * k + q];
+      for (int t = 0; t < COORD_MAXC; t++) acc[t] = 0.f;
+      const float *row = rows + threadIdx.x * k;
+      for (int q = 0; q < k; q++) {
+        const float sv = row[q];
 #pragma unroll
-      for (int t = 0; t < COORD_MAXC; t++)
-        if (t < c) acc[t] = fmaf(sv, Ys[q * c + t], acc[t]);
-    }
+        for (int t = 0; t < COORD_MAXC; t++)
+          if (t < c) acc[t] = fmaf(sv, Ys[q * c + t], acc[t]);
+      }
 #pragma unroll
-    for (int t = 0; t < COORD_MAXC; t++) {
-      if (t >= c) break;
-      const float v = warp_sum(acc[t]);
-      if (lane == 0) {
-        X[i + (int64_t)t * n] = (double)v;
-        ss[t] = fma((double)v, (double)v, ss[t]);
+      for (int t = 0; t < COORD_MAXC; t++) {
+        if (t >= c) break;
+        X[i0 + threadIdx.x + (int64_t)t * n] = (double)acc[t];
+        ss[t] = fma((double)acc[t], (double)acc[t], ss[t]);
       }
     }
   }
-  if (lane == 0)
-    for (int t = 0; t < c; t++) smc[warp * c + t] = ss[t];
-  __syncthreads();
-  for (int t = threadIdx.x; t < c; t += blockDim.x) {
-    double s = 0;
-    for (int w = 0; w < nw; w++) s += smc[w * c + t];
-    part[(int64_t)blockIdx.x * c + t] = s;
+  for (int t = 0; t < c; t++) {  // c is uniform: every thread takes part in each block sum
+    const double s = block_sum(ss[t], red);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * c + t] = s;
   }
 }
 
+// X[:, t] /= ||X[:, t]||: each block sums the per-block partials itself (a block-wide reduction, the same
+// fixed order in every block), then scales its share.
 __global__ void scale32_kernel(double *X, int64_t n, int c, const double *part, int nparts) {
-  __shared__ double inv[PHDE_MAX_K];
-  for (int t = threadIdx.x; t < c; t += blockDim.x) {
+  __shared__ double inv[COORD_MAXC];
+  __shared__ double red[32];
+  for (int t = 0; t < c; t++) {
     double s = 0;
-    for (int b = 0; b < nparts; b++) s += part[(int64_t)b * c + t];
-    inv[t] = 1.0 / sqrt(s);
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += part[(int64_t)b * c + t];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) inv[t] = 1.0 / sqrt(s);
   }
   __syncthreads();
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * c;
@@ -657,15 +664,17 @@ int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double
 }
 
 int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X) {
-  const int threads = 256;
-  const int grid = grid_of(ctx, ctx->n * 32, threads, 8);
+  const int grid = grid_of(ctx, ctx->n, COORD_ROWS, 8);
   double *part = (double *)phde_buf(ctx, "coords32.part", sizeof(double) * grid * (size_t)COORD_MAXC);
   if (!part) return PHDE_ERR_OOM;
+  const size_t smem_max = sizeof(float) * ((size_t)COORD_ROWS * k + (size_t)k * COORD_MAXC);
+  PHDE_CK(ctx, cudaFuncSetAttribute(coords32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)std::max<size_t>(smem_max, 48 * 1024)));
   for (int t0 = 0; t0 < c; t0 += COORD_MAXC) {  // coordinates in groups of COORD_MAXC
     const int cg = std::min(COORD_MAXC, c - t0);
-    const size_t smem = sizeof(double) * (threads / 32) * cg + sizeof(float) * (size_t)k * cg;
-    coords32_kernel<<<grid, threads, smem, ctx->stream>>>(S, Y + (int64_t)t0 * k, ctx->n, k, cg, X + (int64_t)t0 * ctx->n,
-                                                          part);
+    const size_t smem = sizeof(float) * ((size_t)COORD_ROWS * k + (size_t)k * cg);
+    coords32_kernel<<<grid, COORD_ROWS, smem, ctx->stream>>>(S, Y + (int64_t)t0 * k, ctx->n, k, cg,
+                                                             X + (int64_t)t0 * ctx->n, part);
     PHDE_LAUNCHED(ctx);
     scale32_kernel<<<grid_of(ctx, ctx->n * cg, 256, 8), 256, 0, ctx->stream>>>(X + (int64_t)t0 * ctx->n, ctx->n, cg,
                                                                                part, grid);
