@@ -244,7 +244,11 @@ __global__ void __launch_bounds__(GT) bcgs_form_kernel(const float *X, const flo
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int idx = threadIdx.x; idx < BB * BB; idx += GT) Rs[idx / BB][idx % BB] = R[idx];
   __syncthreads();
+  // deg * v^2 in FP32, summed in FP32 over 16 rows and in FP64 beyond (GB300's FP64 rate is 1/64 of FP32,
+  // and three FP64 operations per element would bound the kernel)
   double dsum = 0;
+  float fsum = 0.f;
+  int cnt = 0;
   for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < n; r += (int64_t)gridDim.x * nw) {
     const float x = X[r * BB + lane];
     float v = 0.f;
@@ -252,9 +256,15 @@ __global__ void __launch_bounds__(GT) bcgs_form_kernel(const float *X, const flo
     for (int i = 0; i < BB; i++) v = fmaf(__shfl_sync(PHDE_FULL_MASK, x, i), Rs[i][lane], v);
     if (lane < nacc) {
       S[r * lda + j0 + lane] = v;
-      dsum += (double)v * (double)v * deg[r];
+      fsum = fmaf(v * v, (float)deg[r], fsum);
+    }
+    if (++cnt == 16) {
+      dsum += (double)fsum;
+      fsum = 0.f;
+      cnt = 0;
     }
   }
+  dsum += (double)fsum;
   red[warp][lane] = dsum;
   __syncthreads();
   if (warp == 0) {

@@ -473,8 +473,11 @@ __global__ void gather_columns_kernel(const uint16_t *R, int64_t n, int RW, cons
         D[(int64_t)p * n + v0 + lane] = d;
         bad |= d < 0;
       }
-      const ull sq = d > 0 ? (ull)d * (ull)d : 0ull;
-      const ull tot = warp_sum(sq);
+      // d < 2^16, so d * d < 2^32: the warp sums its high and low 16-bit halves with one 32-bit reduction
+      // each (no overflow: 32 * 2^16 fits), instead of a 64-bit shuffle tree
+      const uint32_t sq = d > 0 ? (uint32_t)d * (uint32_t)d : 0u;
+      const ull tot = ((ull)__reduce_add_sync(PHDE_FULL_MASK, sq >> 16) << 16) +
+                      (ull)__reduce_add_sync(PHDE_FULL_MASK, sq & 0xffffu);
       if (lane == 0 && tot) {
         if (p < GATHER_SMEM_COLS)
           s_ssq[p] += tot;
