@@ -30,7 +30,18 @@ constexpr int MLP_WEIGHTS = MLP_H * MLP_IN + MLP_H + MLP_H * MLP_H + MLP_H + MLP
 // per vertex; heavier rows (R-MAT hubs): one warp per chunk of the multi-source BFS plan, integer
 // atomicAdd (exact, order-free).  hop2/outw are zeroed before the launch.
 constexpr int64_t FEAT_HEAVY = 256;
-__global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, const int32_t *d0, int64_t n,
+// pk[v] = degree(v) << 32 | (uint32) d0[v]: what the feature pass gathers per neighbour, in one 8-byte load
+__global__ void feature_pack_kernel(const int64_t *off, const int32_t *d0, int64_t n, ull *pk) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+    pk[v] = ((ull)(off[v + 1] - off[v]) << 32) | (ull)(uint32_t)d0[v];
+}
+
+__device__ __forceinline__ void feature_edge(ull pku, int32_t dv, ull &h, unsigned &o) {
+  h += pku >> 32;
+  o += (int32_t)(uint32_t)pku > dv ? 1u : 0u;
+}
+
+__global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, const int32_t *d0, const ull *pk, int64_t n,
                                    const int64_t *chunk_row, const int64_t *chunk_e0, int64_t nchunks, int64_t chunk,
                                    ull *hop2, uint32_t *outw) {
   const int lane = threadIdx.x & 31, gl = lane & 7;
@@ -47,11 +58,7 @@ __global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, cons
         act = false;
       } else {
         const int32_t dv = d0[v];
-        for (int64_t e = e0 + gl; e < e1; e += 8) {
-          const int64_t u = __ldg(adj + e);
-          h += (ull)(off[u + 1] - off[u]);
-          o += d0[u] > dv ? 1u : 0u;
-        }
+        for (int64_t e = e0 + gl; e < e1; e += 8) feature_edge(__ldg(pk + __ldg(adj + e)), dv, h, o);
       }
     }
     for (int s = 4; s > 0; s >>= 1) {
@@ -69,11 +76,7 @@ __global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, cons
     const int32_t dv = d0[v];
     ull h = 0;
     unsigned o = 0;
-    for (int64_t e = e0 + lane; e < e1; e += 32) {
-      const int64_t u = __ldg(adj + e);
-      h += (ull)(off[u + 1] - off[u]);
-      o += d0[u] > dv ? 1u : 0u;
-    }
+    for (int64_t e = e0 + lane; e < e1; e += 32) feature_edge(__ldg(pk + __ldg(adj + e)), dv, h, o);
     h = warp_sum(h);
     o = warp_sum(o);
     if (lane == 0) {
@@ -266,6 +269,7 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
   ull *hop2 = (ull *)phde_buf(ctx, "lp.hop2", sizeof(ull) * n);
   uint32_t *outw = (uint32_t *)phde_buf(ctx, "lp.outw", sizeof(uint32_t) * n);
   ull *maxes = (ull *)phde_buf(ctx, "lp.max", sizeof(ull) * 3);
+  ull *pk = (ull *)phde_buf(ctx, "lp.pack", sizeof(ull) * n);
   float *score = (float *)phde_buf(ctx, "lp.score", sizeof(float) * n);
   unsigned *hist = (unsigned *)phde_buf(ctx, "lp.hist", sizeof(unsigned) * nbins);
   float *wts = (float *)phde_buf(ctx, "lp.w", sizeof(float) * MLP_WEIGHTS);
@@ -273,7 +277,7 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
   int64_t *cand = (int64_t *)phde_buf(ctx, "lp.cand", sizeof(int64_t) * cap);
   float *cscore = (float *)phde_buf(ctx, "lp.cscore", sizeof(float) * cap);
   unsigned *count = (unsigned *)phde_buf(ctx, "lp.count", sizeof(unsigned));
-  if (!hop2 || !outw || !maxes || !score || !hist || !wts || !cand || !cscore || !count) return PHDE_ERR_OOM;
+  if (!hop2 || !outw || !maxes || !pk || !score || !hist || !wts || !cand || !cscore || !count) return PHDE_ERR_OOM;
   PHDE_CK(ctx, cudaMemsetAsync(maxes, 0, sizeof(ull) * 3, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(hist, 0, sizeof(unsigned) * nbins, ctx->stream));
   PHDE_CK(ctx, cudaMemcpyAsync(wts, h_weights, sizeof(float) * MLP_WEIGHTS, cudaMemcpyHostToDevice, ctx->stream));
@@ -284,7 +288,10 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
   if (rc) return rc;
   PHDE_CK(ctx, cudaMemsetAsync(hop2, 0, sizeof(ull) * n, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(outw, 0, sizeof(uint32_t) * n, ctx->stream));
-  feature_raw_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, d_d0, n, crow, ce0, nch, chunk, hop2, outw);
+  feature_pack_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, n, pk);
+  PHDE_LAUNCHED(ctx);
+  feature_raw_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, d_d0, pk, n, crow, ce0, nch, chunk, hop2,
+                                                 outw);
   PHDE_LAUNCHED(ctx);
   feature_max_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, n, maxes);
   PHDE_LAUNCHED(ctx);
