@@ -152,3 +152,13 @@ def _csr(n, pairs):
     np.add.at(off, d[:, 0] + 1, 1)
     from icpp_2020_parhde_gb300.csr_io import CSRGraph
     return CSRGraph(np.cumsum(off).astype(np.uint32), d[:, 1].astype(np.uint32), None, "draw")
+
+
+def test_draw_plain_raster_variant_matches(monkeypatch):
+    """PHDE_DRAW_RASTER=plain (an atomic for every pixel write, tiles in order) draws the same image."""
+    from icpp_2020_parhde_gb300 import Context
+    g, x, y, meta, png = load_draw_case("random_spread")
+    monkeypatch.setenv("PHDE_DRAW_RASTER", "plain")
+    with Context(0) as ctx:
+        img, _ = gpu_image(ctx, g, x, y)
+    assert np.array_equal(img, pngdecode.read(png))

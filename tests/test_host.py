@@ -154,3 +154,11 @@ def test_png_writer_round_trip(tmp_path):
     path = str(tmp_path / "big.png")
     write_png(path, img, nthreads=8)
     assert np.array_equal(pngdecode.read(path), img)
+
+
+def test_draw_driver_usage_without_gpu():
+    """lib/draw keeps the reference's command line: a wrong argument count prints the usage line and fails."""
+    pbuild.build()
+    r = subprocess.run([pbuild.DRAW_PATH], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert "Usage:" in r.stderr and "<first coord> <second coord>" in r.stderr
