@@ -522,27 +522,53 @@ __device__ void js_sweep(T *A, T *V, int N, int LD, int M, int *s_order, double 
       s_sn[m] = sn;
     }
     __syncthreads();
-    for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
-      const int mm = idx / N, row = idx % N;
-      const int p = s_p[mm], q = s_q[mm];
-      const T cs = s_cs[mm], sn = s_sn[mm];
+    // A <- J^T A J in one step: every 2 x 2 block (rows of pair m1, columns of pair m2) takes its column
+    // rotation and then its row rotation, the same operations in the same order as rotating all columns
+    // first and all rows after, without a barrier in between (the pairs partition the indices, so blocks
+    // are disjoint); V <- V J beside it.  A pair whose second index is the padding index N (odd N) or whose
+    // sine is 0 is the identity.
+    const int P = M / 2;
+    for (int it = tid; it < P * P; it += blockDim.x) {
+      const int m1 = it / P, m2 = it - m1 * P;
+      const int p1 = s_p[m1], q1 = s_q[m1];
+      const T c1 = s_cs[m1], s1 = s_sn[m1];
+      const bool q1ok = q1 < N;
+      {
+        const int p2 = s_p[m2], q2 = s_q[m2];
+        const T c2 = s_cs[m2], s2 = s_sn[m2];
+        const bool q2ok = q2 < N;
+        const T a = A[p1 + p2 * LD];
+        const T b = q2ok ? A[p1 + q2 * LD] : (T)0;
+        const T d = q1ok ? A[q1 + p2 * LD] : (T)0;
+        const T e = (q1ok && q2ok) ? A[q1 + q2 * LD] : (T)0;
+        T a1 = a, b1 = b, d1 = d, e1 = e;
+        if (q2ok && s2 != (T)0) {  // columns p2, q2
+          a1 = c2 * a - s2 * b;
+          b1 = s2 * a + c2 * b;
+          d1 = c2 * d - s2 * e;
+          e1 = s2 * d + c2 * e;
+        }
+        T a2 = a1, b2 = b1, d2 = d1, e2 = e1;
+        if (q1ok && s1 != (T)0) {  // rows p1, q1
+          a2 = c1 * a1 - s1 * d1;
+          d2 = s1 * a1 + c1 * d1;
+          b2 = c1 * b1 - s1 * e1;
+          e2 = s1 * b1 + c1 * e1;
+        }
+        A[p1 + p2 * LD] = a2;
+        if (q2ok) A[p1 + q2 * LD] = b2;
+        if (q1ok) A[q1 + p2 * LD] = d2;
+        if (q1ok && q2ok) A[q1 + q2 * LD] = e2;
+      }
+    }
+    for (int idx = tid; idx < P * N; idx += blockDim.x) {
+      const int m2 = idx / N, row = idx - m2 * N;
+      const int p = s_p[m2], q = s_q[m2];
+      const T cs = s_cs[m2], sn = s_sn[m2];
       if (q >= N || sn == (T)0) continue;
-      const T akp = A[row + p * LD], akq = A[row + q * LD];
-      A[row + p * LD] = cs * akp - sn * akq;
-      A[row + q * LD] = sn * akp + cs * akq;
       const T vkp = V[row + p * LD], vkq = V[row + q * LD];
       V[row + p * LD] = cs * vkp - sn * vkq;
       V[row + q * LD] = sn * vkp + cs * vkq;
-    }
-    __syncthreads();
-    for (int idx = tid; idx < (M / 2) * N; idx += blockDim.x) {
-      const int mm = idx / N, col = idx % N;
-      const int p = s_p[mm], q = s_q[mm];
-      const T cs = s_cs[mm], sn = s_sn[mm];
-      if (q >= N || sn == (T)0) continue;
-      const T apk = A[p + col * LD], aqk = A[q + col * LD];
-      A[p + col * LD] = cs * apk - sn * aqk;
-      A[q + col * LD] = sn * apk + cs * aqk;
     }
     __syncthreads();
   }
@@ -567,7 +593,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   double *A = js, *V = js + N * LD, *W = js + 2 * N * LD;
   float *A32 = (float *)W, *V32 = (float *)W + N * LD;
   __shared__ double red[32];
-  __shared__ double s_cs[JS_MAX_N / 2 + 1], s_sn[JS_MAX_N / 2 + 1], s_d[JS_MAX_N];
+  __shared__ double s_cs[JS_MAX_N / 2 + 1], s_sn[JS_MAX_N / 2 + 1];
   __shared__ int s_p[JS_MAX_N / 2 + 1], s_q[JS_MAX_N / 2 + 1];
   __shared__ int s_order[JS_MAX_N + 1];
   __shared__ int s_done;
