@@ -148,6 +148,23 @@ __global__ void __launch_bounds__(GT) bcgs_gram_kernel(const float *A, int lda, 
   }
 }
 
+// The projection Gram of the first block, when only the constant column is accepted: per-CTA sums of
+// w_r X[r][i] (the constant column's Gram row), in the layout bcgs_reduce_kernel reads with one row per CTA.
+__global__ void __launch_bounds__(GT) bcgs_u0_kernel(const float *X, const double *w, int64_t n, float *part) {
+  __shared__ float red[GT / 32][BB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float acc = 0.f;
+  for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < n; r += (int64_t)gridDim.x * nw)
+    acc = fmaf(X[r * BB + lane], (float)w[r], acc);
+  red[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    float t = 0.f;
+    for (int i = 0; i < nw; i++) t += red[i][lane];
+    part[(int64_t)blockIdx.x * BB + lane] = t;
+  }
+}
+
 // Sum the partials of Gram row q (one CTA per row, fixed order: deterministic) in FP64.
 //   mode 0 (projection): C[q][i] = sum / <q, D q> for q < nq, sum / (n * den0) for q == nq (the constant
 //                        column's coefficient times its entry 1/sqrt(n)); FP32 out.
@@ -327,7 +344,9 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
     const int nqt = j + 1;
     const int qc = ctx->tc_gram_cgs2 ? QCH : nqt <= 8 ? 8 : (nqt <= 32 ? 32 : 64), nqc = (nqt + qc - 1) / qc;
     for (int pass = 0; pass < 2; pass++) {
-      if (ctx->tc_gram_cgs2) {
+      if (j == 0) {
+        bcgs_u0_kernel<<<ncta, GT, 0, ctx->stream>>>(X, deg, n, part);
+      } else if (ctx->tc_gram_cgs2) {
         const int rc = phde_tc_gram32(ctx, S, k, j, 1, X, deg, n, ncta_tc, nqc, 0, part);
         if (rc) return rc;
       } else if (qc == 8)
@@ -336,8 +355,11 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
         bcgs_gram_kernel<32, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
       else
         bcgs_gram_kernel<64, false><<<dim3(ncta, nqc), GT, 0, ctx->stream>>>(S, k, j, 1, X, deg, n, part);
-      if (!ctx->tc_gram_cgs2) PHDE_LAUNCHED(ctx);
-      bcgs_reduce_kernel<<<nqt, RED_THREADS, 0, ctx->stream>>>(part, ncta_g, j, 0, dden, n_den0, C, nullptr, qc);
+      if (j == 0 || !ctx->tc_gram_cgs2) PHDE_LAUNCHED(ctx);
+      if (j == 0)  // one Gram row (the constant column) per CTA
+        bcgs_reduce_kernel<<<1, RED_THREADS, 0, ctx->stream>>>(part, ncta, 0, 0, dden, n_den0, C, nullptr, 1);
+      else
+        bcgs_reduce_kernel<<<nqt, RED_THREADS, 0, ctx->stream>>>(part, ncta_g, j, 0, dden, n_den0, C, nullptr, qc);
       PHDE_LAUNCHED(ctx);
       const size_t smem = sizeof(float) * ((size_t)nqt * BB + (size_t)j * ST_LD);
       bcgs_update_kernel<<<g_rows, GT, smem, ctx->stream>>>(S, k, j, C, X, n);
