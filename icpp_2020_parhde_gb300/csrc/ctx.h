@@ -42,6 +42,9 @@ struct phde_ctx {
   int64_t batch_graph_launches = 0;
   bool batch_no_graph = false;                     // capture failed once: launch directly
   int64_t ws_epoch = 0;                            // bumped whenever a workspace buffer is (re)allocated
+  // SSSP band width: the mean edge weight of the uploaded graph (sssp.cu)
+  double w_mean = 1.0;
+  long long w_mean_epoch = -1;
   // drawing (draw.cu): the entry-row array's graph, and the size of the last image drawn
   long long draw_rows_epoch = -1;
   void *draw_rows_buf = nullptr;

@@ -325,9 +325,9 @@ __global__ void spmm_plan_kernel(const int64_t *off, int64_t n, HeavyRow *heavy,
   }
 }
 
-template <bool W>
+template <bool W, int KT>
 __device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32_t *w, const double *S, int k,
-                                                int lane, int64_t e0, int64_t e1, double (&acc)[MAXQ]) {
+                                                int lane, int64_t e0, int64_t e1, double (&acc)[KT]) {
   int64_t e = e0;
   for (; e + 4 <= e1; e += 4) {
     const int64_t v0 = __ldg(adj + e), v1 = __ldg(adj + e + 1), v2 = __ldg(adj + e + 2), v3 = __ldg(adj + e + 3);
@@ -339,7 +339,7 @@ __device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32
       w3 = (double)__ldg(w + e + 3);
     }
 #pragma unroll
-    for (int t = 0; t < MAXQ; t++) {
+    for (int t = 0; t < KT; t++) {
       const int q = lane + 32 * t;
       if (q < k) {
         const double s0 = S[v0 * k + q], s1 = S[v1 * k + q], s2 = S[v2 * k + q], s3 = S[v3 * k + q];
@@ -358,7 +358,7 @@ __device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32
     const int64_t v = __ldg(adj + e);
     const double we = W ? (double)__ldg(w + e) : 1.0;
 #pragma unroll
-    for (int t = 0; t < MAXQ; t++) {
+    for (int t = 0; t < KT; t++) {
       const int q = lane + 32 * t;
       if (q < k) acc[t] = W ? __dsub_rn(acc[t], __dmul_rn(we, S[v * k + q])) : __dsub_rn(acc[t], S[v * k + q]);
     }
@@ -366,7 +366,7 @@ __device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32
 }
 
 // Light rows: LS[i,q] = d_i*S[i,q] - sum_e w_e*S[adj_e,q].  Heavy rows are skipped here.
-template <bool W>
+template <bool W, int KT>
 __global__ void spmm_light_kernel(const int64_t *off, const uint32_t *adj, const int32_t *w, const double *deg,
                                   const double *S, double *LS, int64_t n, int k) {
   const int lane = threadIdx.x & 31;
@@ -376,15 +376,15 @@ __global__ void spmm_light_kernel(const int64_t *off, const uint32_t *adj, const
     const int64_t e0 = off[i], e1 = off[i + 1];
     if (e1 - e0 > SPMM_HEAVY) continue;
     const double di = deg[i];
-    double acc[MAXQ];
+    double acc[KT];
 #pragma unroll
-    for (int t = 0; t < MAXQ; t++) {
+    for (int t = 0; t < KT; t++) {
       const int q = lane + 32 * t;
       acc[t] = q < k ? __dmul_rn(di, S[i * k + q]) : 0.0;
     }
-    spmm_accumulate<W>(adj, w, S, k, lane, e0, e1, acc);
+    spmm_accumulate<W, KT>(adj, w, S, k, lane, e0, e1, acc);
 #pragma unroll
-    for (int t = 0; t < MAXQ; t++) {
+    for (int t = 0; t < KT; t++) {
       const int q = lane + 32 * t;
       if (q < k) LS[i * k + q] = acc[t];
     }
@@ -392,20 +392,20 @@ __global__ void spmm_light_kernel(const int64_t *off, const uint32_t *adj, const
 }
 
 // Heavy-row chunks: part[c, q] = sum over the chunk of w_e*S[adj_e,q].
-template <bool W>
+template <bool W, int KT>
 __global__ void spmm_chunk_kernel(const uint32_t *adj, const int32_t *w, const double *S, const Chunk *chunks,
                                   int64_t nchunks, double *part, int k) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t gws = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t c = gw; c < nchunks; c += gws) {
-    double acc[MAXQ];
+    double acc[KT];
 #pragma unroll
-    for (int t = 0; t < MAXQ; t++) acc[t] = 0.0;
+    for (int t = 0; t < KT; t++) acc[t] = 0.0;
     const Chunk ch = chunks[c];
-    spmm_accumulate<W>(adj, w, S, k, lane, ch.e0, ch.e1, acc);  // accumulates -sum
+    spmm_accumulate<W, KT>(adj, w, S, k, lane, ch.e0, ch.e1, acc);  // accumulates -sum
 #pragma unroll
-    for (int t = 0; t < MAXQ; t++) {
+    for (int t = 0; t < KT; t++) {
       const int q = lane + 32 * t;
       if (q < k) part[c * k + q] = acc[t];
     }
@@ -437,21 +437,26 @@ __global__ void spmm_heavy_fix_kernel(const HeavyRow *heavy, int64_t nheavy, con
 // grid = (tiles_p * tiles_q, splits).  part: [splits][k*k] column-major (entry (p,q) at q + p*k, the
 // reference's C[k + i*mdim] layout).
 constexpr int GT = 64, GR = 16;
+// U x U accumulators per thread (16 x 16 threads): tiles of 16 U.  The host picks the smallest tile that
+// covers k (FP64 runs at 1/64 of the FP32 rate on GB300, so a 64-wide tile for k = 20 would waste 90% of
+// the FMAs); every output sums its rows in the same order whatever the tile.
+template <int U>
 __global__ void __launch_bounds__(256) gram_kernel(const double *A, const double *B, int64_t n, int k,
                                                    double *part) {
-  __shared__ double sA[GR][GT + 1];
-  __shared__ double sB[GR][GT + 1];
-  const int tiles = (k + GT - 1) / GT;
+  constexpr int TS = 16 * U;
+  __shared__ double sA[GR][TS + 1];
+  __shared__ double sB[GR][TS + 1];
+  const int tiles = (k + TS - 1) / TS;
   const int tp = blockIdx.x / tiles, tq = blockIdx.x % tiles;
-  const int p0 = tp * GT, q0 = tq * GT;
+  const int p0 = tp * TS, q0 = tq * TS;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t rows_per = (n + gridDim.y - 1) / gridDim.y;
   const int64_t r0 = (int64_t)blockIdx.y * rows_per;
   const int64_t r1 = min(n, r0 + rows_per);
-  double acc[4][4] = {};
+  double acc[U][U] = {};
   for (int64_t rb = r0; rb < r1; rb += GR) {
-    for (int idx = threadIdx.x; idx < GR * GT; idx += 256) {
-      const int rr = idx / GT, cc = idx % GT;
+    for (int idx = threadIdx.x; idx < GR * TS; idx += 256) {
+      const int rr = idx / TS, cc = idx % TS;
       const int64_t r = rb + rr;
       sA[rr][cc] = (r < r1 && p0 + cc < k) ? A[r * k + p0 + cc] : 0.0;
       sB[rr][cc] = (r < r1 && q0 + cc < k) ? B[r * k + q0 + cc] : 0.0;
@@ -459,24 +464,24 @@ __global__ void __launch_bounds__(256) gram_kernel(const double *A, const double
     __syncthreads();
 #pragma unroll 4
     for (int rr = 0; rr < GR; rr++) {
-      double av[4], bv[4];
+      double av[U], bv[U];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
+      for (int u = 0; u < U; u++) {
         av[u] = sA[rr][ty + 16 * u];
         bv[u] = sB[rr][tx + 16 * u];
       }
 #pragma unroll
-      for (int u = 0; u < 4; u++)
+      for (int u = 0; u < U; u++)
 #pragma unroll
-        for (int v = 0; v < 4; v++) acc[u][v] = fma(av[u], bv[v], acc[u][v]);
+        for (int v = 0; v < U; v++) acc[u][v] = fma(av[u], bv[v], acc[u][v]);
     }
     __syncthreads();
   }
   double *out = part + (int64_t)blockIdx.y * k * k;
 #pragma unroll
-  for (int u = 0; u < 4; u++)
+  for (int u = 0; u < U; u++)
 #pragma unroll
-    for (int v = 0; v < 4; v++) {
+    for (int v = 0; v < U; v++) {
       const int p = p0 + ty + 16 * u, q = q0 + tx + 16 * v;
       if (p < k && q < k) out[q + (int64_t)p * k] = acc[u][v];
     }
@@ -760,19 +765,44 @@ int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS,
   const int threads = 256;
   const int32_t *w = ctx->weighted ? ctx->d_w : nullptr;
   const int grid = grid_for(ctx, ctx->n * 32, threads, 8);
+  // column tiles of 32 per lane, a compile-time count (1, 2, 4 or 8): the FP64 instructions of empty tiles
+  // are not issued at all
+  const int kt = k <= 32 ? 1 : (k <= 64 ? 2 : (k <= 128 ? 4 : 8));
+#define PHDE_SPMM64(WW, T) \
+  spmm_light_kernel<WW, T><<<grid, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, w, deg, S, LS, ctx->n, k)
+#define PHDE_SPMM64_KT(WW) \
+  do {                    \
+    if (kt == 1) PHDE_SPMM64(WW, 1); \
+    else if (kt == 2) PHDE_SPMM64(WW, 2); \
+    else if (kt == 4) PHDE_SPMM64(WW, 4); \
+    else PHDE_SPMM64(WW, 8); \
+  } while (0)
   if (w)
-    spmm_light_kernel<true><<<grid, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, w, deg, S, LS, ctx->n, k);
+    PHDE_SPMM64_KT(true);
   else
-    spmm_light_kernel<false><<<grid, threads, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, w, deg, S, LS, ctx->n, k);
+    PHDE_SPMM64_KT(false);
+#undef PHDE_SPMM64_KT
+#undef PHDE_SPMM64
   PHDE_LAUNCHED(ctx);
   if (nheavy > 0) {
     double *part = (double *)phde_buf(ctx, "spmm.part", sizeof(double) * nchunks * k);
     if (!part) return PHDE_ERR_OOM;
     const int g2 = grid_for(ctx, nchunks * 32, threads, 8);
+#define PHDE_CHUNK64(WW, T) \
+  spmm_chunk_kernel<WW, T><<<g2, threads, 0, ctx->stream>>>(ctx->d_adj, w, S, chunks, nchunks, part, k)
+#define PHDE_CHUNK64_KT(WW) \
+  do {                     \
+    if (kt == 1) PHDE_CHUNK64(WW, 1); \
+    else if (kt == 2) PHDE_CHUNK64(WW, 2); \
+    else if (kt == 4) PHDE_CHUNK64(WW, 4); \
+    else PHDE_CHUNK64(WW, 8); \
+  } while (0)
     if (w)
-      spmm_chunk_kernel<true><<<g2, threads, 0, ctx->stream>>>(ctx->d_adj, w, S, chunks, nchunks, part, k);
+      PHDE_CHUNK64_KT(true);
     else
-      spmm_chunk_kernel<false><<<g2, threads, 0, ctx->stream>>>(ctx->d_adj, w, S, chunks, nchunks, part, k);
+      PHDE_CHUNK64_KT(false);
+#undef PHDE_CHUNK64_KT
+#undef PHDE_CHUNK64
     PHDE_LAUNCHED(ctx);
     spmm_heavy_fix_kernel<<<grid_for(ctx, nheavy * 32, threads, 8), threads, 0, ctx->stream>>>(heavy, nheavy, deg, S,
                                                                                               part, LS, k);
@@ -783,11 +813,18 @@ int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS,
 
 // M (k x k, column-major as the reference stores it) = A^T B.
 int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M) {
-  const int tiles = (k + GT - 1) / GT;
+  const int ts = k <= 16 ? 16 : (k <= 32 ? 32 : GT);
+  const int tiles = (k + ts - 1) / ts;
   int splits = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * 4 / (tiles * tiles), (ctx->n + 255) / 256));
   double *part = (double *)phde_buf(ctx, "gram.part", sizeof(double) * (size_t)splits * k * k);
   if (!part) return PHDE_ERR_OOM;
-  gram_kernel<<<dim3(tiles * tiles, splits), 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+  const dim3 grid(tiles * tiles, splits);
+  if (ts == 16)
+    gram_kernel<1><<<grid, 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+  else if (ts == 32)
+    gram_kernel<2><<<grid, 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+  else
+    gram_kernel<4><<<grid, 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
   PHDE_LAUNCHED(ctx);
   sum_parts_kernel<<<grid_for(ctx, (int64_t)k * k, 256), 256, 0, ctx->stream>>>(part, splits, (int64_t)k * k, M);
   PHDE_LAUNCHED(ctx);
