@@ -586,38 +586,53 @@ __global__ void centre_kernel(const int32_t *D, int64_t n, int k, const ull *col
 }
 
 // X[i + t*n] = sum_q M[i,q] * Y[q + t*k]; per-block partial sums of squares per coordinate.
-__global__ void coords_kernel(const double *M, const double *Y, int64_t n, int k, int c, double *X,
-                              double *part) {
-  extern __shared__ double sm[];  // [nwarps][c]
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int64_t gw = (int64_t)blockIdx.x * nw + warp, gws = (int64_t)gridDim.x * nw;
-  for (int t = 0; t < c; t++) {
-    double ss = 0;
-    for (int64_t i = gw; i < n; i += gws) {
-      double s = 0;
-      for (int q = lane; q < k; q += 32) s += __dmul_rn(M[i * k + q], Y[q + (int64_t)t * k]);
-      s = warp_sum(s);
-      if (lane == 0) {
-        X[i + (int64_t)t * n] = s;
-        ss += __dmul_rn(s, s);
-      }
-    }
-    if (lane == 0) sm[warp * c + t] = ss;
-  }
+// X[:, t] = S Y[:, t], FP64: a thread per row forms all c coordinates, each as the sequential sum over the row's
+// k entries (the reference's order), with Y in shared memory; per-block sums of squares for the norms.
+constexpr int CO_MAXC = 8;  // coordinates per pass (more run in groups)
+__global__ void coords_kernel(const double *M, const double *Y, int64_t n, int k, int c, double *X, double *part) {
+  extern __shared__ double Ys[];  // [k * c]: Ys[q + t * k] = Y[q + t * k]
+  __shared__ double red[32];
+  for (int i = threadIdx.x; i < k * c; i += blockDim.x) Ys[i] = Y[i];
   __syncthreads();
-  for (int t = threadIdx.x; t < c; t += blockDim.x) {
-    double s = 0;
-    for (int w = 0; w < nw; w++) s += sm[w * c + t];
-    part[(int64_t)blockIdx.x * c + t] = s;
+  for (int t0 = 0; t0 < c; t0 += CO_MAXC) {
+    const int cg = min(CO_MAXC, c - t0);
+    double ss[CO_MAXC];
+#pragma unroll
+    for (int t = 0; t < CO_MAXC; t++) ss[t] = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      double s[CO_MAXC];
+#pragma unroll
+      for (int t = 0; t < CO_MAXC; t++) s[t] = 0;
+      const double *row = M + i * k;
+      for (int q = 0; q < k; q++) {
+        const double m = row[q];
+#pragma unroll
+        for (int t = 0; t < CO_MAXC; t++)
+          if (t < cg) s[t] += __dmul_rn(m, Ys[q + (t0 + t) * k]);
+      }
+#pragma unroll
+      for (int t = 0; t < CO_MAXC; t++)
+        if (t < cg) {
+          X[i + (int64_t)(t0 + t) * n] = s[t];
+          ss[t] += __dmul_rn(s[t], s[t]);
+        }
+    }
+    for (int t = 0; t < cg; t++) {  // cg is uniform: every thread takes part in each block sum
+      const double tot = block_sum(ss[t], red);
+      if (threadIdx.x == 0) part[(int64_t)blockIdx.x * c + t0 + t] = tot;
+    }
   }
 }
 
+// X[:, t] /= ||X[:, t]||: each block sums the per-block partials itself (block-wide, fixed order), then scales.
 __global__ void scale_coords_kernel(double *X, int64_t n, int c, const double *part, int nparts) {
   __shared__ double inv[PHDE_MAX_K];
-  for (int t = threadIdx.x; t < c; t += blockDim.x) {
+  __shared__ double red[32];
+  for (int t = 0; t < c; t++) {
     double s = 0;
-    for (int b = 0; b < nparts; b++) s += part[(int64_t)b * c + t];
-    inv[t] = 1.0 / sqrt(s);
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += part[(int64_t)b * c + t];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) inv[t] = 1.0 / sqrt(s);
   }
   __syncthreads();
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * c;
@@ -859,10 +874,13 @@ int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, d
     PHDE_LAUNCHED(ctx);
     return PHDE_OK;
   }
-  const int grid = grid_for(ctx, ctx->n * 32, threads, 4);
+  const int grid = grid_for(ctx, ctx->n, threads, 8);
   double *part = (double *)phde_buf(ctx, "coords.part", sizeof(double) * grid * (size_t)c);
   if (!part) return PHDE_ERR_OOM;
-  coords_kernel<<<grid, threads, sizeof(double) * (threads / 32) * c, ctx->stream>>>(M, Y, ctx->n, k, c, X, part);
+  const size_t ysmem = sizeof(double) * (size_t)k * c;
+  PHDE_CK(ctx, cudaFuncSetAttribute(coords_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)std::max<size_t>(ysmem, 48 * 1024)));
+  coords_kernel<<<grid, threads, ysmem, ctx->stream>>>(M, Y, ctx->n, k, c, X, part);
   PHDE_LAUNCHED(ctx);
   scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid);
   PHDE_LAUNCHED(ctx);
