@@ -233,13 +233,15 @@ __global__ void mgs_step_kernel(double *U, int64_t n, int xcol, int q, int jcoun
   __shared__ double red[32];
   __shared__ double s_num, s_dinv;
   double *x = U + (int64_t)xcol * n;
-  if (q > 0) {
+  if (q > 0) {  // the previous step's partials, summed by the whole block (the same fixed order in every block)
+    double num = 0, den = 0;
+    for (int b = threadIdx.x; b < nparts_in; b += blockDim.x) {
+      den += part_in[2 * b];
+      num += part_in[2 * b + 1];
+    }
+    den = block_sum(den, red);
+    num = block_sum(num, red);
     if (threadIdx.x == 0) {
-      double num = 0, den = 0;
-      for (int b = 0; b < nparts_in; b++) {
-        den += part_in[2 * b];
-        num += part_in[2 * b + 1];
-      }
       s_num = num;
       s_dinv = 1.0 / den;
     }
@@ -255,12 +257,12 @@ __global__ void mgs_step_kernel(double *U, int64_t n, int xcol, int q, int jcoun
       xi = __dsub_rn(xi, __dmul_rn(__dmul_rn(num, yp[i]), dinv));
       x[i] = xi;
     }
-    if (q < jcount) {
+    if (q < jcount) {  // the dot products with fused multiply-adds (GB300 runs FP64 at 1/64 of FP32)
       const double dy = __dmul_rn(y[i], deg[i]);
-      a0 += __dmul_rn(y[i], dy);
-      a1 += __dmul_rn(xi, dy);
+      a0 = fma(y[i], dy, a0);
+      a1 = fma(xi, dy, a1);
     } else {
-      a0 += __dmul_rn(xi, xi);
+      a0 = fma(xi, xi, a0);
     }
   }
   a0 = block_sum(a0, red);
