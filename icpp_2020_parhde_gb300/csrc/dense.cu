@@ -439,9 +439,9 @@ __global__ void spmm_heavy_fix_kernel(const HeavyRow *heavy, int64_t nheavy, con
 // grid = (tiles_p * tiles_q, splits).  part: [splits][k*k] column-major (entry (p,q) at q + p*k, the
 // reference's C[k + i*mdim] layout).
 constexpr int GT = 64, GR = 16;
-// U x U accumulators per thread (16 x 16 threads): tiles of 16 U.  The host picks the smallest tile that
-// covers k (FP64 runs at 1/64 of the FP32 rate on GB300, so a 64-wide tile for k = 20 would waste 90% of
-// the FMAs); every output sums its rows in the same order whatever the tile.
+// U x U accumulators per thread (16 x 16 threads): tiles of 16 U, used with U = 4 for k > 32 (smaller k go to
+// gram_small_kernel: FP64 runs at 1/64 of the FP32 rate on GB300, so padding k = 20 to a 64-wide tile would
+// waste 90% of the FMAs); every output sums its rows in the same order whatever the kernel.
 template <int U>
 __global__ void __launch_bounds__(256) gram_kernel(const double *A, const double *B, int64_t n, int k,
                                                    double *part) {
@@ -487,6 +487,47 @@ __global__ void __launch_bounds__(256) gram_kernel(const double *A, const double
       const int p = p0 + ty + 16 * u, q = q0 + tx + 16 * v;
       if (p < k && q < k) out[q + (int64_t)p * k] = acc[u][v];
     }
+}
+
+// k <= 32: thread t owns outputs t, t + 256, ... of the k x k result (no padding to a tile), each summed over the
+// rows in the same order as gram_kernel, from row slabs staged in shared memory.
+constexpr int GS_MAXO = 4;  // outputs per thread: k * k <= 1024
+__global__ void __launch_bounds__(256) gram_small_kernel(const double *A, const double *B, int64_t n, int k,
+                                                         double *part) {
+  __shared__ double sA[GR][33];
+  __shared__ double sB[GR][33];
+  const int64_t rows_per = (n + gridDim.y - 1) / gridDim.y;
+  const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+  const int64_t r1 = min(n, r0 + rows_per);
+  const int nout = k * k;
+  int op[GS_MAXO], oq[GS_MAXO];
+#pragma unroll
+  for (int u = 0; u < GS_MAXO; u++) {
+    const int o = threadIdx.x + 256 * u;
+    op[u] = o < nout ? o / k : 0;
+    oq[u] = o < nout ? o % k : 0;
+  }
+  double acc[GS_MAXO] = {};
+  for (int64_t rb = r0; rb < r1; rb += GR) {
+    for (int idx = threadIdx.x; idx < GR * k; idx += 256) {
+      const int rr = idx / k, cc = idx % k;
+      const int64_t r = rb + rr;
+      sA[rr][cc] = r < r1 ? A[r * k + cc] : 0.0;
+      sB[rr][cc] = r < r1 ? B[r * k + cc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < GR; rr++)
+#pragma unroll
+      for (int u = 0; u < GS_MAXO; u++) acc[u] = fma(sA[rr][op[u]], sB[rr][oq[u]], acc[u]);
+    __syncthreads();
+  }
+  double *out = part + (int64_t)blockIdx.y * k * k;
+#pragma unroll
+  for (int u = 0; u < GS_MAXO; u++) {
+    const int o = threadIdx.x + 256 * u;
+    if (o < nout) out[oq[u] + (int64_t)op[u] * k] = acc[u];
+  }
 }
 
 __global__ void sum_parts_kernel(const double *part, int splits, int64_t len, double *out) {
@@ -836,10 +877,8 @@ int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M)
   double *part = (double *)phde_buf(ctx, "gram.part", sizeof(double) * (size_t)splits * k * k);
   if (!part) return PHDE_ERR_OOM;
   const dim3 grid(tiles * tiles, splits);
-  if (ts == 16)
-    gram_kernel<1><<<grid, 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
-  else if (ts == 32)
-    gram_kernel<2><<<grid, 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+  if (k <= 32)
+    gram_small_kernel<<<dim3(1, splits), 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
   else
     gram_kernel<4><<<grid, 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
   PHDE_LAUNCHED(ctx);
