@@ -3,7 +3,8 @@
 Workload (one step = one full layout of one graph): ParHDE, k = 50, c = 3, on a seeded synthetic R-MAT graph
 of scale 20, edgefactor 16, (a, b, c) = (0.57, 0.19, 0.19), symmetrised, self-loops and duplicates removed,
 largest connected component kept (n = 646,362, nnz = 31,403,988 for seed 1).  --rmat-scale/--k/--c select
-other sizes (scale 22 with k = 64 is the learned-pivot target size).
+other sizes (scale 22 with k = 64 is the learned-pivot target size); --graph grid3d --k 20 --c 2 times the
+weighted configuration (WParHDE with delta-stepping SSSP, FP64) on a 256^3 grid with weights in [1, 255].
 
 Pipelines timed (each from the CSR resident in device memory to the n x c coordinates in host memory, by the
 library's CUDA events on its stream; L2 flushed between steps):
@@ -57,7 +58,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--graph", default="rmat", choices=["rmat", "rgg3d"])
+    ap.add_argument("--graph", default="rmat", choices=["rmat", "rgg3d", "grid3d"],
+                    help="grid3d: the weighted configuration (WParHDE, delta-stepping SSSP, FP64) on an L^3 grid")
+    ap.add_argument("--grid-l", type=int, default=256, help="side of the weighted 3-D grid")
     ap.add_argument("--rmat-scale", type=int, default=20)
     ap.add_argument("--rgg-n", type=int, default=8_000_000, help="vertices of the 3-D random geometric graph")
     ap.add_argument("--k", type=int, default=50)
@@ -156,12 +159,16 @@ def make_graph(args):
     t = time.time()
     if args.graph == "rgg3d":
         g = graphs.rgg(args.rgg_n, dim=3, avg_degree=12, seed=args.seed)
+    elif args.graph == "grid3d":
+        g = graphs.grid3d(args.grid_l, seed=args.seed, weighted=True)
     else:
         g = graphs.rmat(args.rmat_scale, 16, 0.57, 0.19, 0.19, seed=args.seed)
     return g, time.time() - t
 
 
 def graph_desc(args):
+    if args.graph == "grid3d":
+        return "a %d^3 6-neighbour grid with int32 weights uniform in [1, 255]" % args.grid_l
     if args.graph == "rgg3d":
         return "a 3-D random geometric graph (%d points in the unit cube, radius for mean degree 12, LCC)" % args.rgg_n
     return ("an R-MAT scale-%d graph (edgefactor 16, a=.57 b=.19 c=.19, symmetrised, LCC)" % args.rmat_scale)
@@ -555,10 +562,77 @@ def run_batched(args, local, flush_l2):
             "rayleigh_rel_err_vs_single_max": max(rq_err) if rq_err else None, "graph_gen_s": round(gen_s, 1)}
 
 
+def run_weighted(args):
+    """The weighted configuration: WParHDE (Kcenters pivots by delta-stepping SSSP, coupled MGS, FP64 as the
+    reference) with k pivots and c coordinates on a weighted 3-D grid; same timing rules as the headline."""
+    ws, rank, local = dist_init()
+    import torch
+    torch.cuda.set_device(local)
+    from icpp_2020_parhde_gb300 import Context, graphs
+    g, gen_s = make_graph(args)
+    ctx = Context(local)
+    n, nnz, k, c = g.n, g.nnz, args.k, args.c
+    ctx.upload(g)
+    xy_h = torch.empty(n * c, dtype=torch.float64).pin_memory()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def run():
+        return ctx.layout("wParHDE", "Kcenters", k=k, c=c, precision="fp64", eig="power", coords_out=xy_h.numpy())
+
+    for _ in range(args.warmup):
+        run()
+    clk = ClockSampler(local).__enter__()
+    barrier(ws)
+    torch.cuda.synchronize()
+    stats = []
+    l0 = ctx.launch_count
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        stats.append(run().stats)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = allmax(ws, float(np.mean([st["ms_total"] for st in stats])))
+    launches = ctx.launch_count - l0
+    e2e_t = []
+    for _ in range(max(1, args.steps // 4)):
+        t1 = time.perf_counter()
+        ctx.upload(g)
+        run()
+        e2e_t.append(time.perf_counter() - t1)
+    clk.__exit__(None, None, None)
+    e2e_s = allmax(ws, float(np.mean(e2e_t)))
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": ws * k * nnz / (ms * 1e-3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32 distances, f64", "data": "synthetic",
+            "config": {"workload": "WParHDE layout of %s, k=%d pivots, %d coordinates" % (graph_desc(args), k, c),
+                       "n": n, "nnz": nnz, "k": k, "c": c, "l2": "flushed between timed steps (256 MB write)",
+                       "graph_gen_s": round(gen_s, 1)},
+            "phases_ms": {p: float(np.mean([st[p] for st in stats])) for p in PHASES},
+            "e2e": {"value": ws * k * nnz / e2e_s, "unit": UNIT, "ms_per_graph": e2e_s * 1e3,
+                    "h2d_bytes_per_step": 4 * (n + 1) + 8 * nnz, "d2h_bytes_per_step": 8 * n * c},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        gs = graphs.grid3d(64, seed=args.seed, weighted=True)
+        t1 = time.perf_counter()
+        orc.layout(gs, "wParHDE", "Kcenters", k, c, nthreads=os.cpu_count() or 1, want_S=False)
+        t_cpu = time.perf_counter() - t1
+        line["cpu_baseline"] = {"value": k * gs.nnz / t_cpu, "unit": UNIT, "cores": os.cpu_count() or 1,
+                                "kind": "port", "sample": "one layout of a 64^3 weighted grid (nnz = %d) in %.2f s"
+                                                          % (gs.nnz, t_cpu)}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.graph == "grid3d":
+        run_weighted(args)
     else:
         run_gb300(args)
 
