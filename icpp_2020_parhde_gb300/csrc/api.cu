@@ -18,10 +18,11 @@ int phde_fill_i32(phde_ctx *ctx, int32_t *p, int64_t n, int32_t v);
 int phde_degrees(phde_ctx *ctx, double *deg);
 int phde_cgs(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, double *S, int k,
              int *h_state, double *h_dlog);
-int phde_mgs_pass(phde_ctx *ctx, const int32_t *col, const ull *sumsq, double *U, int xcol, int jcount,
+int phde_mgs_pass(phde_ctx *ctx, const int32_t *col, const ull *sumsq, double *U, int j, int g, int k,
                   const double *deg, double *h_nrm2);
 int phde_const_col(phde_ctx *ctx, double *U);
-int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale, double *S, int k, int scol);
+int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale);
+int phde_basis_rows(phde_ctx *ctx, const double *U, int k, double *S);
 int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS, int k);
 int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M);
 int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C);
@@ -351,7 +352,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     if ((rc = phde_fill_i32(ctx, min_d, n, 0x7fffffff))) return rc;
     PHDE_CK(ctx, cudaMemsetAsync(cur, 0, sizeof(int64_t) * 2, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(sumsq, 0, sizeof(ull) * P, ctx->stream));
-    int correct = 1;
+    int correct = 1, gram_cols = 0;  // columns of U whose D-Gram entries the MGS kernels hold
     for (int r = 0; r < P; r++) {
       if (correct > k) break;
       tm.mark(6);
@@ -362,7 +363,9 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       PHDE_CK(ctx, cudaMemcpyAsync(cur, cur + 1, sizeof(int64_t), cudaMemcpyDeviceToDevice, ctx->stream));
       tm.mark(7);
       double nrm2 = 0;
-      if ((rc = phde_mgs_pass(ctx, col, sumsq + r, U, correct, correct, deg, &nrm2))) return rc;
+      const int g = gram_cols < correct ? correct - 1 : -1;
+      if ((rc = phde_mgs_pass(ctx, col, sumsq + r, U, correct, g, k, deg, &nrm2))) return rc;
+      gram_cols = correct;
       if ((rc = phde_check_device_err(ctx, "WParHDE distance pass"))) return rc;
       npasses++;
       ms_dist += tm.ms(6, 7);
@@ -371,7 +374,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
         ndiscarded++;
         if (o->verbose) printf("discarding vec %d, normdist %g\n", correct, nrm);
       } else {
-        if ((rc = phde_accept_col(ctx, U, correct, 1.0 / nrm, Sbuf, k, correct - 1))) return rc;
+        if ((rc = phde_accept_col(ctx, U, correct, 1.0 / nrm))) return rc;
         correct++;
       }
       tm.mark(6);
@@ -383,7 +386,11 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       return phde_fail(ctx, PHDE_ERR_TOO_FEW_PIVOTS,
                        "Number of Pivots obtained: " + std::to_string(naccepted) + " inadequate, increase the Pivots Limits: " +
                            std::to_string(P));
+    tm.mark(7);
+    if ((rc = phde_basis_rows(ctx, U, k, Sbuf))) return rc;  // U's accepted columns -> row-major S
     tm.mark(2);
+    PHDE_CK(ctx, cudaEventSynchronize(ctx->ev[2]));
+    ms_orth += tm.ms(7, 2);
   } else {
     // ---- distance phase: Kcenters (or random) BFS passes into D ----
     int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);

@@ -178,6 +178,115 @@ __device__ __forceinline__ uint32_t owner_slot(const uint32_t *qe, uint32_t f, u
   return lo;
 }
 
+// Owners of the 32 consecutive edges e0 + lane (lane = 0..31) of a warp, found by the whole warp (every
+// lane calls it with the same e0 < total edges).  The warp's first owner comes from a 32-ary search (one
+// probe per lane and step: about log32(f) dependent loads instead of log2(f)); the others from one window
+// load qe[s0 .. s0+31]: the slot starting at edge e0 + t is written to position t of a per-warp scratch
+// (the largest such slot, for slots of zero out-degree), and a prefix maximum over the lanes gives each
+// lane the last slot starting at or before its edge.  A lane whose edge lies beyond the window (only
+// possible with zero-degree frontier entries) falls back to the binary search.  `win` is 32 words of
+// shared memory private to the warp; `start` receives qe[owner].
+__device__ __forceinline__ uint32_t warp_owner_slots(const uint32_t *qe, uint32_t f, uint32_t e0, uint32_t *win,
+                                                     uint32_t &start) {
+  const int lane = threadIdx.x & 31;
+  uint32_t lo = 0, hi = f;  // invariant: qe[lo] <= e0, answer in [lo, hi)
+  while (hi - lo > 32) {
+    const uint32_t step = (hi - lo + 31) >> 5;
+    const uint32_t pos = lo + (uint32_t)lane * step;
+    const unsigned m = __ballot_sync(PHDE_FULL_MASK, pos < hi && qe[pos] <= e0);  // bit 0 always set
+    lo += (uint32_t)(31 - __clz(m)) * step;
+    hi = min(hi, lo + step);
+  }
+  {
+    const uint32_t pos = lo + lane;
+    const unsigned m = __ballot_sync(PHDE_FULL_MASK, pos < hi && qe[pos] <= e0);
+    lo += (uint32_t)(31 - __clz(m));
+  }
+  const uint32_t s0 = lo, sl = s0 + lane;
+  const uint32_t q = sl < f ? qe[sl] : 0xffffffffu;
+  const uint32_t qx = s0 + 32 < f ? qe[s0 + 32] : 0xffffffffu;
+  win[lane] = 0;
+  __syncwarp();
+  if (q != 0xffffffffu && q >= e0 && q - e0 < 32u) atomicMax(win + (q - e0), (uint32_t)lane);
+  __syncwarp();
+  uint32_t off = win[lane];
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(PHDE_FULL_MASK, off, o);
+    if (lane >= o) off = max(off, y);
+  }
+  __syncwarp();  // win is reused by the next call
+  const uint32_t e = e0 + lane;
+  start = __shfl_sync(PHDE_FULL_MASK, q, (int)off);  // qe of the owner, from the window
+  if (e >= qx) {
+    const uint32_t s = owner_slot(qe, f, e);
+    start = qe[s];
+    return s;
+  }
+  return s0 + off;
+}
+
+// block_push for two queues at once: the near frontier (vertex + start-edge prefix, as block_push) and a
+// plain vertex list (the far pile), one scan and one barrier pair for both, the two counter atomics
+// issued by two lanes together.
+struct Push2Scratch {
+  ull warp_tot[32];
+  unsigned warp_far[32];
+  ull base;
+  unsigned base_far;
+};
+
+__device__ __forceinline__ void block_push2(bool to_near, uint32_t v, uint32_t dv, uint32_t *qv, uint32_t *qe,
+                                            ull *ctr, bool to_far, uint32_t *far, unsigned *far_ctr,
+                                            Push2Scratch *sc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const ull mine = to_near ? ((1ull << 32) | (ull)dv) : 0ull;
+  ull x = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    ull y = __shfl_up_sync(PHDE_FULL_MASK, x, o);
+    if (lane >= o) x += y;
+  }
+  const unsigned fb = __ballot_sync(PHDE_FULL_MASK, to_far);
+  if (lane == 31) {
+    sc->warp_tot[warp] = x;
+    sc->warp_far[warp] = __popc(fb);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const ull w = lane < nw ? sc->warp_tot[lane] : 0ull;
+    const unsigned wf = lane < nw ? sc->warp_far[lane] : 0u;
+    ull incl = w;
+    unsigned inclf = wf;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const ull y = __shfl_up_sync(PHDE_FULL_MASK, incl, o);
+      const unsigned yf = __shfl_up_sync(PHDE_FULL_MASK, inclf, o);
+      if (lane >= o) {
+        incl += y;
+        inclf += yf;
+      }
+    }
+    const ull total = __shfl_sync(PHDE_FULL_MASK, incl, 31);
+    const unsigned totf = __shfl_sync(PHDE_FULL_MASK, inclf, 31);
+    if (lane < nw) {
+      sc->warp_tot[lane] = incl - w;
+      sc->warp_far[lane] = inclf - wf;
+    }
+    if (lane == 0) sc->base = total ? atomicAdd(ctr, total) : 0ull;
+    if (lane == 1) sc->base_far = totf ? atomicAdd(far_ctr, totf) : 0u;
+  }
+  __syncthreads();
+  if (to_near) {
+    const ull pos = sc->base + sc->warp_tot[warp] + (x - mine);
+    const uint32_t slot = (uint32_t)(pos >> 32);
+    qv[slot] = v;
+    qe[slot] = (uint32_t)(pos & 0xffffffffull);
+  }
+  if (to_far) far[sc->base_far + sc->warp_far[warp] + __popc(fb & ((1u << lane) - 1u))] = v;
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------------------------
 // Host-side helpers.
 struct LaunchCounter {

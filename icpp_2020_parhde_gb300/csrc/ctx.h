@@ -59,6 +59,8 @@ struct phde_ctx {
   int32_t *d_w = nullptr;
   long long graph_epoch = 0;  // bumped by every upload; caches keyed on it (the SpMM chunk plan)
   long long spmm_plan_epoch = -1;
+  long long w64_epoch = -1;  // FP64 copy of the edge weights for the Laplacian SpMM
+  void *w64_buf = nullptr;
   int64_t spmm_nheavy = 0, spmm_nchunks = 0;
   std::vector<float> pivot_model;  // MLP weights of the learned pivot strategy
   long long ms_plan_epoch = -1;  // multi-source BFS heavy-row plan

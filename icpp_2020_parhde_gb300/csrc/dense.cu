@@ -3,14 +3,13 @@
 //   cgs_kernel        ParHDE D-orthogonalisation (ParHDE.cpp:190-285): one persistent cooperative launch
 //                     runs the whole candidate loop -- coefficient dots, projection update, norm test and
 //                     acceptance -- with device-side control, so no host round trip per candidate.
-//   mgs_step_kernel   WParHDE modified Gram-Schmidt step (WParHDE.cpp:167-190), fused: apply step q-1's
-//                     projection and accumulate step q's dot products in the same sweep.
-//   lap_spmm_kernel   LS = D*S - A*S (ParHDE.cpp:288-300, WParHDE.cpp:229-241): one warp per row, lanes
-//                     across the k columns of a row-major S, neighbours in CSR order with separate
-//                     multiply/subtract roundings -- the reference's exact operation sequence.
-//   gram_kernel       C = A^T B for row-major n x k operands (matrixTransMultiplication,
-//                     DrawingBase.cpp:221-244): 64x64 output tiles, split over row ranges, partials summed
-//                     in a fixed order.
+//   mgs kernels       WParHDE modified Gram-Schmidt (WParHDE.cpp:164-213) in its one-reduction form: a dot
+//                     sweep, a one-warp coefficient solve and an update sweep per distance column.
+//   spmm kernels      LS = D*S - A*S (ParHDE.cpp:288-300, WParHDE.cpp:229-241): one warp per row, lanes
+//                     across the k columns of a row-major S, neighbours in CSR order.
+//   gram kernels      C = A^T B for row-major n x k operands (matrixTransMultiplication,
+//                     DrawingBase.cpp:221-244), C symmetric: the upper triangle, split over row ranges,
+//                     partials summed in a fixed order and mirrored.
 //   centring kernels  PivotMDS double centring (PivotMDS.cpp:30-66) and PHDE column centring
 //                     (PHDE.cpp:30-47) from exact integer sums.
 //   coords kernels    X = M * Y (DrawingBase.cpp:207-219) and the unit-norm scaling of getCoordinates
@@ -224,70 +223,138 @@ __global__ void __launch_bounds__(CGS_THREADS) cgs_kernel(CgsArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------------
-// WParHDE MGS step q over column-major U (n x (k+1)).  If q > 0 the block first sums step q-1's partials
-// (fixed order) and applies x -= (num * y_{q-1}) * (1/den) (WParHDE.cpp:184-188).  If q < jcount it then
-// accumulates step q's partials den = sum y_q*(y_q*d), num = sum x*(y_q*d) (WParHDE.cpp:176-181); at
-// q == jcount it accumulates sum x^2 instead (the norm test, WParHDE.cpp:195-197).
-__global__ void mgs_step_kernel(double *U, int64_t n, int xcol, int q, int jcount, const double *deg,
-                                const double *part_in, double *part_out, int nparts_in) {
-  __shared__ double red[32];
-  __shared__ double s_num, s_dinv;
-  double *x = U + (int64_t)xcol * n;
-  if (q > 0) {  // the previous step's partials, summed by the whole block (the same fixed order in every block)
-    double num = 0, den = 0;
-    for (int b = threadIdx.x; b < nparts_in; b += blockDim.x) {
-      den += part_in[2 * b];
-      num += part_in[2 * b + 1];
-    }
-    den = block_sum(den, red);
-    num = block_sum(num, red);
-    if (threadIdx.x == 0) {
-      s_num = num;
-      s_dinv = 1.0 / den;
-    }
-    __syncthreads();
-  }
-  const double num = q > 0 ? s_num : 0.0, dinv = q > 0 ? s_dinv : 0.0;
-  const double *yp = q > 0 ? U + (int64_t)(q - 1) * n : U;
-  const double *y = U + (int64_t)q * n;
-  double a0 = 0, a1 = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double xi = x[i];
-    if (q > 0) {
-      xi = __dsub_rn(xi, __dmul_rn(__dmul_rn(num, yp[i]), dinv));
-      x[i] = xi;
-    }
-    if (q < jcount) {  // the dot products with fused multiply-adds (GB300 runs FP64 at 1/64 of FP32)
-      const double dy = __dmul_rn(y[i], deg[i]);
-      a0 = fma(y[i], dy, a0);
-      a1 = fma(xi, dy, a1);
-    } else {
-      a0 = fma(xi, xi, a0);
-    }
-  }
-  a0 = block_sum(a0, red);
-  a1 = block_sum(a1, red);
-  if (threadIdx.x == 0) {
-    part_out[2 * blockIdx.x] = a0;
-    part_out[2 * blockIdx.x + 1] = a1;
-  }
-}
+// WParHDE coupled D-orthogonalisation (WParHDE.cpp:164-213): the new distance column x0 (normalised) is
+// projected against the accepted columns y_0 .. y_{j-1} of U (column-major n x (k+1), y_0 the constant
+// column) by modified Gram-Schmidt: c_q = <x_q, D y_q> / <y_q, D y_q>, x_{q+1} = x_q - c_q y_q.  MGS's j
+// sweeps over memory are replaced by two, with the same coefficients in exact arithmetic:
+//   <x_q, D y_q> = <x0, D y_q> - sum_{p<q} c_p <y_p, D y_q>,
+// so one sweep forms r_q = <x0, D y_q> for every q (and, once per accepted column g, the Gram entries
+// G[p][g] = <y_p, D y_g>, p <= g), a one-warp kernel solves the recurrence for the c_q, and a second sweep
+// forms x = x0 - sum_q c_q y_q with its squared L2 norm (the discard test, WParHDE.cpp:194-204).  This is
+// the one-reduction form of MGS (Swirydowicz, Langou, Ananthan, Yang and Thomas, "Low synchronization
+// Gram-Schmidt and GMRES algorithms", 2020), whose loss of orthogonality is MGS's; GB300 runs FP64 at 1/64
+// of the FP32 rate, and it needs about half of MGS's FP64 instructions and a fifth of its memory traffic.
+constexpr int MGS_TP = 8;  // columns per thread in the dot sweep
 
-// x = col * (1/sqrt(sumsq)) into U column xcol (WParHDE.cpp:154-162)
-__global__ void normalise_col_kernel(const int32_t *col, const ull *sumsq, double *U, int64_t n, int xcol) {
+// Column p of U (p < j) gives r_p = sum_i y_p[i] * (x0[i] * d[i]) (product p) and, when g >= 0 (then g = j - 1),
+// G[p][g] = sum_i y_p[i] * (y_g[i] * d[i]) (product j + p), from one load of y_p[i].  x0 = col * (1/sqrt(sumsq))
+// as WParHDE.cpp:154-162.  blockIdx.y picks MGS_TP columns; part[blockIdx.x * np + product] = the block's sum.
+__global__ void __launch_bounds__(256) mgs_dots_kernel(const int32_t *col, const ull *sumsq, const double *U,
+                                                       const double *deg, int64_t n, int j, int g, double *part) {
+  __shared__ double red[8][2 * MGS_TP];
+  const bool gr = g >= 0;
+  const int np = j + (gr ? j : 0);
+  const int p0 = blockIdx.y * MGS_TP;
   const double inv = 1.0 / sqrt((double)*sumsq);
-  double *x = U + (int64_t)xcol * n;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] = __dmul_rn((double)col[i], inv);
+  const double *yg = U + (int64_t)(gr ? g : 0) * n;
+  double ar[MGS_TP], ag[MGS_TP];
+#pragma unroll
+  for (int t = 0; t < MGS_TP; t++) ar[t] = ag[t] = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = deg[i];
+    const double z0 = __dmul_rn(__dmul_rn((double)col[i], inv), d);
+    const double z1 = gr ? __dmul_rn(yg[i], d) : 0.0;
+#pragma unroll
+    for (int t = 0; t < MGS_TP; t++)
+      if (p0 + t < j) {
+        const double y = U[(int64_t)(p0 + t) * n + i];
+        ar[t] = fma(y, z0, ar[t]);
+        if (gr) ag[t] = fma(y, z1, ag[t]);
+      }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < MGS_TP; t++) {
+    const double vr = warp_sum(ar[t]);
+    const double vg = warp_sum(ag[t]);
+    if (lane == 0) {
+      red[warp][t] = vr;
+      red[warp][MGS_TP + t] = vg;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * MGS_TP) {
+    const int t = threadIdx.x % MGS_TP, p = p0 + t;
+    const bool isg = threadIdx.x >= MGS_TP;
+    if (p < j && (!isg || gr)) {
+      double v = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w][threadIdx.x];
+      part[(int64_t)blockIdx.x * np + (isg ? j + p : p)] = v;
+    }
+  }
 }
 
-// Accept: x *= 1/nrm, copy into row-major S column j-1 (WParHDE.cpp:205-213).
-__global__ void accept_col_kernel(double *U, int64_t n, int xcol, double scale, double *S, int k, int scol) {
-  double *x = U + (int64_t)xcol * n;
+// One warp: sums the dot sweep's partials (block order), stores the new Gram entries G[p][g] (row-major
+// (k+1) x (k+1), p <= g), then solves c_q = (r_q - sum_{p<q} c_p G[p][q]) / G[q][q] for q = 0 .. j-1.
+__global__ void mgs_solve_kernel(const double *part, int nparts, int j, int g, int ldg, double *G, double *coef) {
+  __shared__ double r[PHDE_MAX_K + 1], c[PHDE_MAX_K + 1];
+  const int lane = threadIdx.x;
+  const int np = j + (g >= 0 ? g + 1 : 0);
+  for (int p = lane; p < np; p += 32) {
+    double v = 0;
+    for (int b = 0; b < nparts; b++) v += part[(int64_t)b * np + p];
+    if (p < j)
+      r[p] = v;
+    else
+      G[(int64_t)(p - j) * ldg + g] = v;
+  }
+  __threadfence_block();
+  __syncwarp();
+  for (int q = 0; q < j; q++) {
+    double s = 0;
+    for (int p = lane; p < q; p += 32) s = fma(c[p], G[(int64_t)p * ldg + q], s);
+    s = warp_sum(s);
+    if (lane == 0) c[q] = __dmul_rn(r[q] - s, 1.0 / G[(int64_t)q * ldg + q]);
+    __syncwarp();
+  }
+  for (int q = lane; q < j; q += 32) coef[q] = c[q];
+}
+
+// x = x0 - sum_q c_q y_q into U column j; part[block] = the block's sum of x^2.
+__global__ void __launch_bounds__(256) mgs_apply_kernel(const int32_t *col, const ull *sumsq, double *U, int64_t n,
+                                                        int j, const double *coef, double *part) {
+  __shared__ double cs[PHDE_MAX_K + 1];
+  __shared__ double red[32];
+  for (int q = threadIdx.x; q < j; q += blockDim.x) cs[q] = coef[q];
+  __syncthreads();
+  const double inv = 1.0 / sqrt((double)*sumsq);
+  double *x = U + (int64_t)j * n;
+  double ss = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double v = __dmul_rn(x[i], scale);
-    x[i] = v;
-    S[i * k + scol] = v;
+    double xi = __dmul_rn((double)col[i], inv);
+#pragma unroll 4
+    for (int q = 0; q < j; q++) xi = fma(-cs[q], U[(int64_t)q * n + i], xi);
+    x[i] = xi;
+    ss = fma(xi, xi, ss);
+  }
+  ss = block_sum(ss, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = ss;
+}
+
+// Accept: x *= 1/nrm in place (WParHDE.cpp:205-208).
+__global__ void scale_col_kernel(double *x, int64_t n, double scale) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = __dmul_rn(x[i], scale);
+}
+
+// S (row-major n x k) from U's accepted columns 1 .. k (the distMatrix copy, WParHDE.cpp:210-213): a block
+// transposes 32 rows x k columns through shared memory.
+__global__ void __launch_bounds__(256) basis_rows_kernel(const double *U, int64_t n, int k, double *S) {
+  __shared__ double t[32][33];
+  for (int64_t i0 = (int64_t)blockIdx.x * 32; i0 < n; i0 += (int64_t)gridDim.x * 32) {
+    for (int q0 = 0; q0 < k; q0 += 32) {
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      for (int qq = w; qq < 32; qq += 8) {
+        const int q = q0 + qq;
+        if (q < k && i0 + lane < n) t[qq][lane] = U[(int64_t)(q + 1) * n + i0 + lane];
+      }
+      __syncthreads();
+      for (int rr = w; rr < 32; rr += 8) {
+        const int q = q0 + lane;
+        if (q < k && i0 + rr < n) S[(i0 + rr) * k + q] = t[lane][rr];
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -312,9 +379,16 @@ __global__ void degrees_kernel(const int64_t *off, const int32_t *w, int64_t n, 
 
 // ---- Laplacian SpMM, load balanced ----
 // Rows of degree <= SPMM_HEAVY are done by one warp each, neighbours in CSR order (the reference's
-// exact subtraction sequence, ParHDE.cpp:293-298), four neighbour rows in flight.  Heavier rows (R-MAT
+// subtraction sequence, ParHDE.cpp:293-298), four neighbour rows in flight.  Weighted rows subtract
+// w*S[j] with one fused multiply-add, the weights read as FP64 (converted once per uploaded graph): GB300
+// runs FP64 at 1/64 of the FP32 rate, so one FP64 instruction per edge and column instead of three.  Heavier rows (R-MAT
 // hubs) are cut into chunks of SPMM_CHUNK neighbours; one warp sums each chunk, and a fix-up pass forms
 // LS = d*S - (sum of the chunk partials in chunk order), so the result is deterministic.
+__global__ void widen_weights_kernel(const int32_t *w, int64_t nnz, double *w64) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+    w64[e] = (double)w[e];
+}
+
 __global__ void spmm_plan_kernel(const int64_t *off, int64_t n, HeavyRow *heavy, Chunk *chunks, ull *counts) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e0 = off[i], e1 = off[i + 1], deg = e1 - e0;
@@ -328,17 +402,17 @@ __global__ void spmm_plan_kernel(const int64_t *off, int64_t n, HeavyRow *heavy,
 }
 
 template <bool W, int KT>
-__device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32_t *w, const double *S, int k,
+__device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const double *w, const double *S, int k,
                                                 int lane, int64_t e0, int64_t e1, double (&acc)[KT]) {
   int64_t e = e0;
   for (; e + 4 <= e1; e += 4) {
     const int64_t v0 = __ldg(adj + e), v1 = __ldg(adj + e + 1), v2 = __ldg(adj + e + 2), v3 = __ldg(adj + e + 3);
     double w0 = 1, w1 = 1, w2 = 1, w3 = 1;
     if (W) {
-      w0 = (double)__ldg(w + e);
-      w1 = (double)__ldg(w + e + 1);
-      w2 = (double)__ldg(w + e + 2);
-      w3 = (double)__ldg(w + e + 3);
+      w0 = __ldg(w + e);
+      w1 = __ldg(w + e + 1);
+      w2 = __ldg(w + e + 2);
+      w3 = __ldg(w + e + 3);
     }
 #pragma unroll
     for (int t = 0; t < KT; t++) {
@@ -346,10 +420,10 @@ __device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32
       if (q < k) {
         const double s0 = S[v0 * k + q], s1 = S[v1 * k + q], s2 = S[v2 * k + q], s3 = S[v3 * k + q];
         if (W) {
-          acc[t] = __dsub_rn(acc[t], __dmul_rn(w0, s0));
-          acc[t] = __dsub_rn(acc[t], __dmul_rn(w1, s1));
-          acc[t] = __dsub_rn(acc[t], __dmul_rn(w2, s2));
-          acc[t] = __dsub_rn(acc[t], __dmul_rn(w3, s3));
+          acc[t] = fma(-w0, s0, acc[t]);
+          acc[t] = fma(-w1, s1, acc[t]);
+          acc[t] = fma(-w2, s2, acc[t]);
+          acc[t] = fma(-w3, s3, acc[t]);
         } else {
           acc[t] = __dsub_rn(__dsub_rn(__dsub_rn(__dsub_rn(acc[t], s0), s1), s2), s3);
         }
@@ -358,18 +432,18 @@ __device__ __forceinline__ void spmm_accumulate(const uint32_t *adj, const int32
   }
   for (; e < e1; e++) {
     const int64_t v = __ldg(adj + e);
-    const double we = W ? (double)__ldg(w + e) : 1.0;
+    const double we = W ? __ldg(w + e) : 1.0;
 #pragma unroll
     for (int t = 0; t < KT; t++) {
       const int q = lane + 32 * t;
-      if (q < k) acc[t] = W ? __dsub_rn(acc[t], __dmul_rn(we, S[v * k + q])) : __dsub_rn(acc[t], S[v * k + q]);
+      if (q < k) acc[t] = W ? fma(-we, S[v * k + q], acc[t]) : __dsub_rn(acc[t], S[v * k + q]);
     }
   }
 }
 
 // Light rows: LS[i,q] = d_i*S[i,q] - sum_e w_e*S[adj_e,q].  Heavy rows are skipped here.
 template <bool W, int KT>
-__global__ void spmm_light_kernel(const int64_t *off, const uint32_t *adj, const int32_t *w, const double *deg,
+__global__ void spmm_light_kernel(const int64_t *off, const uint32_t *adj, const double *w, const double *deg,
                                   const double *S, double *LS, int64_t n, int k) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -395,7 +469,7 @@ __global__ void spmm_light_kernel(const int64_t *off, const uint32_t *adj, const
 
 // Heavy-row chunks: part[c, q] = sum over the chunk of w_e*S[adj_e,q].
 template <bool W, int KT>
-__global__ void spmm_chunk_kernel(const uint32_t *adj, const int32_t *w, const double *S, const Chunk *chunks,
+__global__ void spmm_chunk_kernel(const uint32_t *adj, const double *w, const double *S, const Chunk *chunks,
                                   int64_t nchunks, double *part, int k) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -435,13 +509,15 @@ __global__ void spmm_heavy_fix_kernel(const HeavyRow *heavy, int64_t nheavy, con
   }
 }
 
-// Partial C = A^T B over one row range.  Block (16,16) computes a 64x64 output tile (4x4 per thread).
-// grid = (tiles_p * tiles_q, splits).  part: [splits][k*k] column-major (entry (p,q) at q + p*k, the
-// reference's C[k + i*mdim] layout).
+// Partial C = A^T B over one row range, for C symmetric (A^T B = S^T L S with L symmetric): only the
+// entries p <= q are summed, the rest are mirrored when the partials are added (sum_parts_sym_kernel).
+// part: [splits][k*k] column-major (entry (p,q) at q + p*k, the reference's C[k + i*mdim] layout).
+//
+// gram_list_kernel (k(k+1)/2 <= 8192): thread t of the block owns upper-triangle outputs t, t + T, ... (NO
+// of them, T threads), each summed over the block's rows in order from row slabs staged in shared memory.
+// FP64 runs at 1/64 of the FP32 rate on GB300, so no FMA is spent on padding or on the lower triangle.
+// gram_kernel (larger k): 16 x 16 threads, U x U accumulators each, on the tiles at or above the diagonal.
 constexpr int GT = 64, GR = 16;
-// U x U accumulators per thread (16 x 16 threads): tiles of 16 U, used with U = 4 for k > 32 (smaller k go to
-// gram_small_kernel: FP64 runs at 1/64 of the FP32 rate on GB300, so padding k = 20 to a 64-wide tile would
-// waste 90% of the FMAs); every output sums its rows in the same order whatever the kernel.
 template <int U>
 __global__ void __launch_bounds__(256) gram_kernel(const double *A, const double *B, int64_t n, int k,
                                                    double *part) {
@@ -449,7 +525,12 @@ __global__ void __launch_bounds__(256) gram_kernel(const double *A, const double
   __shared__ double sA[GR][TS + 1];
   __shared__ double sB[GR][TS + 1];
   const int tiles = (k + TS - 1) / TS;
-  const int tp = blockIdx.x / tiles, tq = blockIdx.x % tiles;
+  int tp = 0, rest = blockIdx.x;  // blockIdx.x enumerates the tile pairs tp <= tq row by row
+  while (rest >= tiles - tp) {
+    rest -= tiles - tp;
+    tp++;
+  }
+  const int tq = tp + rest;
   const int p0 = tp * TS, q0 = tq * TS;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t rows_per = (n + gridDim.y - 1) / gridDim.y;
@@ -485,55 +566,62 @@ __global__ void __launch_bounds__(256) gram_kernel(const double *A, const double
 #pragma unroll
     for (int v = 0; v < U; v++) {
       const int p = p0 + ty + 16 * u, q = q0 + tx + 16 * v;
-      if (p < k && q < k) out[q + (int64_t)p * k] = acc[u][v];
+      if (p <= q && q < k) out[q + (int64_t)p * k] = acc[u][v];
     }
 }
 
-// k <= 32: thread t owns outputs t, t + 256, ... of the k x k result (no padding to a tile), each summed over the
-// rows in the same order as gram_kernel, from row slabs staged in shared memory.
-constexpr int GS_MAXO = 4;  // outputs per thread: k * k <= 1024
-__global__ void __launch_bounds__(256) gram_small_kernel(const double *A, const double *B, int64_t n, int k,
+template <int NO>
+__global__ void __launch_bounds__(1024) gram_list_kernel(const double *A, const double *B, int64_t n, int k,
                                                          double *part) {
-  __shared__ double sA[GR][33];
-  __shared__ double sB[GR][33];
+  extern __shared__ double gsm[];  // sA[GR][k + 1], sB[GR][k + 1]
+  double *sA = gsm, *sB = gsm + GR * (k + 1);
+  const int kp = k + 1;
   const int64_t rows_per = (n + gridDim.y - 1) / gridDim.y;
   const int64_t r0 = (int64_t)blockIdx.y * rows_per;
   const int64_t r1 = min(n, r0 + rows_per);
-  const int nout = k * k;
-  int op[GS_MAXO], oq[GS_MAXO];
+  const int nout = k * (k + 1) / 2;
+  int op[NO], oq[NO];
 #pragma unroll
-  for (int u = 0; u < GS_MAXO; u++) {
-    const int o = threadIdx.x + 256 * u;
-    op[u] = o < nout ? o / k : 0;
-    oq[u] = o < nout ? o % k : 0;
+  for (int u = 0; u < NO; u++) {
+    int o = threadIdx.x + (int)blockDim.x * u, p = 0;
+    if (o >= nout) o = 0;  // a spare slot repeats output 0 and is not stored
+    while (o >= k - p) {   // row p of the upper triangle holds k - p outputs
+      o -= k - p;
+      p++;
+    }
+    op[u] = p;
+    oq[u] = p + o;
   }
-  double acc[GS_MAXO] = {};
+  double acc[NO] = {};
   for (int64_t rb = r0; rb < r1; rb += GR) {
-    for (int idx = threadIdx.x; idx < GR * k; idx += 256) {
+    for (int idx = threadIdx.x; idx < GR * k; idx += blockDim.x) {
       const int rr = idx / k, cc = idx % k;
       const int64_t r = rb + rr;
-      sA[rr][cc] = r < r1 ? A[r * k + cc] : 0.0;
-      sB[rr][cc] = r < r1 ? B[r * k + cc] : 0.0;
+      sA[rr * kp + cc] = r < r1 ? A[r * k + cc] : 0.0;
+      sB[rr * kp + cc] = r < r1 ? B[r * k + cc] : 0.0;
     }
     __syncthreads();
 #pragma unroll 4
     for (int rr = 0; rr < GR; rr++)
 #pragma unroll
-      for (int u = 0; u < GS_MAXO; u++) acc[u] = fma(sA[rr][op[u]], sB[rr][oq[u]], acc[u]);
+      for (int u = 0; u < NO; u++) acc[u] = fma(sA[rr * kp + op[u]], sB[rr * kp + oq[u]], acc[u]);
     __syncthreads();
   }
   double *out = part + (int64_t)blockIdx.y * k * k;
 #pragma unroll
-  for (int u = 0; u < GS_MAXO; u++) {
-    const int o = threadIdx.x + 256 * u;
-    if (o < nout) out[oq[u] + (int64_t)op[u] * k] = acc[u];
-  }
+  for (int u = 0; u < NO; u++)
+    if (threadIdx.x + (int)blockDim.x * u < nout) out[oq[u] + (int64_t)op[u] * k] = acc[u];
 }
 
-__global__ void sum_parts_kernel(const double *part, int splits, int64_t len, double *out) {
+// M[i] = sum over splits of the partials, in split order; for a symmetric product the entries below the
+// diagonal take the partials of their mirror.
+__global__ void sum_parts_sym_kernel(const double *part, int splits, int k, double *out) {
+  const int64_t len = (int64_t)k * k;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i / k), q = (int)(i % k);
+    const int64_t src = p <= q ? i : (int64_t)p + (int64_t)q * k;
     double s = 0;
-    for (int b = 0; b < splits; b++) s += part[(int64_t)b * len + i];
+    for (int b = 0; b < splits; b++) s += part[(int64_t)b * len + src];
     out[i] = s;
   }
 }
@@ -629,36 +717,47 @@ __global__ void centre_kernel(const int32_t *D, int64_t n, int k, const ull *col
 }
 
 // X[i + t*n] = sum_q M[i,q] * Y[q + t*k]; per-block partial sums of squares per coordinate.
-// X[:, t] = S Y[:, t], FP64: a thread per row forms all c coordinates, each as the sequential sum over the row's
-// k entries (the reference's order), with Y in shared memory; per-block sums of squares for the norms.
-constexpr int CO_MAXC = 8;  // coordinates per pass (more run in groups)
-__global__ void coords_kernel(const double *M, const double *Y, int64_t n, int k, int c, double *X, double *part) {
-  extern __shared__ double Ys[];  // [k * c]: Ys[q + t * k] = Y[q + t * k]
+// X[:, t] = S Y[:, t], FP64: a block stages blockDim.x consecutive rows of S (one contiguous range, read
+// coalesced) into shared memory at a padded stride, then a thread per row forms up to CO_MAXC coordinates,
+// each summed over the row's k entries in order with fused multiply-adds (more coordinates run in groups).
+constexpr int CO_MAXC = 8;
+__global__ void __launch_bounds__(128) coords_kernel(const double *M, const double *Y, int64_t n, int k, int c,
+                                                     double *X, double *part) {
+  extern __shared__ double csm[];  // the group's Ys[q + t * k], then the row tile [blockDim.x][k + 1]
   __shared__ double red[32];
-  for (int i = threadIdx.x; i < k * c; i += blockDim.x) Ys[i] = Y[i];
-  __syncthreads();
+  const int rows = blockDim.x, kp = k + 1;
+  double *Ys = csm, *tile = csm + (size_t)k * CO_MAXC;
   for (int t0 = 0; t0 < c; t0 += CO_MAXC) {
     const int cg = min(CO_MAXC, c - t0);
+    __syncthreads();  // the previous group's last tile read
+    for (int i = threadIdx.x; i < k * cg; i += blockDim.x) Ys[i] = Y[(int64_t)t0 * k + i];
     double ss[CO_MAXC];
 #pragma unroll
     for (int t = 0; t < CO_MAXC; t++) ss[t] = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-      double s[CO_MAXC];
+    for (int64_t i0 = (int64_t)blockIdx.x * rows; i0 < n; i0 += (int64_t)gridDim.x * rows) {
+      const int nr = (int)min((int64_t)rows, n - i0);
+      __syncthreads();  // Ys written (first tile), or the previous tile read
+      const double *src = M + i0 * k;
+      for (int e = threadIdx.x; e < nr * k; e += blockDim.x) tile[(e / k) * kp + e % k] = src[e];
+      __syncthreads();
+      if ((int)threadIdx.x < nr) {
+        const double *row = tile + threadIdx.x * kp;
+        double sv[CO_MAXC];
 #pragma unroll
-      for (int t = 0; t < CO_MAXC; t++) s[t] = 0;
-      const double *row = M + i * k;
-      for (int q = 0; q < k; q++) {
-        const double m = row[q];
+        for (int t = 0; t < CO_MAXC; t++) sv[t] = 0;
+        for (int q = 0; q < k; q++) {
+          const double m = row[q];
+#pragma unroll
+          for (int t = 0; t < CO_MAXC; t++)
+            if (t < cg) sv[t] = fma(m, Ys[q + t * k], sv[t]);
+        }
 #pragma unroll
         for (int t = 0; t < CO_MAXC; t++)
-          if (t < cg) s[t] += __dmul_rn(m, Ys[q + (t0 + t) * k]);
+          if (t < cg) {
+            X[i0 + threadIdx.x + (int64_t)(t0 + t) * n] = sv[t];
+            ss[t] = fma(sv[t], sv[t], ss[t]);
+          }
       }
-#pragma unroll
-      for (int t = 0; t < CO_MAXC; t++)
-        if (t < cg) {
-          X[i + (int64_t)(t0 + t) * n] = s[t];
-          ss[t] += __dmul_rn(s[t], s[t]);
-        }
     }
     for (int t = 0; t < cg; t++) {  // cg is uniform: every thread takes part in each block sum
       const double tot = block_sum(ss[t], red);
@@ -752,29 +851,33 @@ int phde_cgs(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const dou
   return PHDE_OK;
 }
 
-// WParHDE: normalise the new distance column into U column xcol and run MGS against columns
-// 0..jcount-1; returns the squared norm of the projected vector in *h_nrm2 (synchronises).
-int phde_mgs_pass(phde_ctx *ctx, const int32_t *col, const ull *sumsq, double *U, int xcol, int jcount,
+// WParHDE: project the new distance column (normalised) against U's columns 0 .. j-1 into column j; g >= 0
+// names the column accepted since the last call, whose Gram entries the dot sweep adds.  Returns the
+// squared norm of the projected vector in *h_nrm2 (synchronises).
+int phde_mgs_pass(phde_ctx *ctx, const int32_t *col, const ull *sumsq, double *U, int j, int g, int k,
                   const double *deg, double *h_nrm2) {
   const int64_t n = ctx->n;
-  const int threads = 512;
-  const int grid = grid_for(ctx, n, threads, 2);
-  double *pa = (double *)phde_buf(ctx, "mgs.pa", sizeof(double) * 2 * grid);
-  double *pb = (double *)phde_buf(ctx, "mgs.pb", sizeof(double) * 2 * grid);
-  if (!pa || !pb) return PHDE_ERR_OOM;
-  normalise_col_kernel<<<grid, threads, 0, ctx->stream>>>(col, sumsq, U, n, xcol);
+  const int threads = 256;
+  const int np = j + (g >= 0 ? g + 1 : 0);
+  const int ty = (j + MGS_TP - 1) / MGS_TP;
+  const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, (int64_t)ctx->nsm * 8 / ty));
+  const int ga = grid_for(ctx, n, threads, 8);
+  double *part = (double *)phde_buf(ctx, "mgs.part", sizeof(double) * (size_t)gx * (2 * PHDE_MAX_K + 2));
+  double *G = (double *)phde_buf(ctx, "mgs.G", sizeof(double) * (size_t)(PHDE_MAX_K + 1) * (PHDE_MAX_K + 1));
+  double *coef = (double *)phde_buf(ctx, "mgs.coef", sizeof(double) * (PHDE_MAX_K + 1));
+  double *pn = (double *)phde_buf(ctx, "mgs.norm", sizeof(double) * ga);
+  if (!part || !G || !coef || !pn) return PHDE_ERR_OOM;
+  mgs_dots_kernel<<<dim3(gx, ty), threads, 0, ctx->stream>>>(col, sumsq, U, deg, n, j, g, part);
   PHDE_LAUNCHED(ctx);
-  for (int q = 0; q <= jcount; q++) {
-    double *pin = (q & 1) ? pa : pb, *pout = (q & 1) ? pb : pa;
-    mgs_step_kernel<<<grid, threads, 0, ctx->stream>>>(U, n, xcol, q, jcount, deg, pin, pout, grid);
-    PHDE_LAUNCHED(ctx);
-  }
-  double *pfinal = (jcount & 1) ? pb : pa;
-  std::vector<double> h(2 * grid);
-  PHDE_CK(ctx, cudaMemcpyAsync(h.data(), pfinal, sizeof(double) * 2 * grid, cudaMemcpyDeviceToHost, ctx->stream));
+  mgs_solve_kernel<<<1, 32, 0, ctx->stream>>>(part, gx, j, g, k + 1, G, coef);
+  PHDE_LAUNCHED(ctx);
+  mgs_apply_kernel<<<ga, threads, 0, ctx->stream>>>(col, sumsq, U, n, j, coef, pn);
+  PHDE_LAUNCHED(ctx);
+  std::vector<double> h(ga);
+  PHDE_CK(ctx, cudaMemcpyAsync(h.data(), pn, sizeof(double) * ga, cudaMemcpyDeviceToHost, ctx->stream));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
   double s = 0;
-  for (int b = 0; b < grid; b++) s += h[2 * b];
+  for (int b = 0; b < ga; b++) s += h[b];
   *h_nrm2 = s;
   return PHDE_OK;
 }
@@ -785,8 +888,14 @@ int phde_const_col(phde_ctx *ctx, double *U) {
   return PHDE_OK;
 }
 
-int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale, double *S, int k, int scol) {
-  accept_col_kernel<<<grid_for(ctx, ctx->n, 256), 256, 0, ctx->stream>>>(U, ctx->n, xcol, scale, S, k, scol);
+int phde_accept_col(phde_ctx *ctx, double *U, int xcol, double scale) {
+  scale_col_kernel<<<grid_for(ctx, ctx->n, 256), 256, 0, ctx->stream>>>(U + (int64_t)xcol * ctx->n, ctx->n, scale);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+int phde_basis_rows(phde_ctx *ctx, const double *U, int k, double *S) {
+  basis_rows_kernel<<<grid_for(ctx, (ctx->n + 31) / 32 * 256, 256, 4), 256, 0, ctx->stream>>>(U, ctx->n, k, S);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }
@@ -821,7 +930,18 @@ int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS,
   int rc = phde_spmm_plan(ctx, &heavy, &chunks, &nheavy, &nchunks);
   if (rc) return rc;
   const int threads = 256;
-  const int32_t *w = ctx->weighted ? ctx->d_w : nullptr;
+  const double *w = nullptr;
+  if (ctx->weighted) {
+    double *w64 = (double *)phde_buf(ctx, "spmm.w64", sizeof(double) * ctx->nnz);
+    if (!w64) return PHDE_ERR_OOM;
+    if (ctx->w64_epoch != ctx->graph_epoch || ctx->w64_buf != w64) {
+      widen_weights_kernel<<<grid_for(ctx, ctx->nnz, 256), 256, 0, ctx->stream>>>(ctx->d_w, ctx->nnz, w64);
+      PHDE_LAUNCHED(ctx);
+      ctx->w64_epoch = ctx->graph_epoch;
+      ctx->w64_buf = w64;
+    }
+    w = w64;
+  }
   const int grid = grid_for(ctx, ctx->n * 32, threads, 8);
   // column tiles of 32 per lane, a compile-time count (1, 2, 4 or 8): the FP64 instructions of empty tiles
   // are not issued at all
@@ -871,18 +991,38 @@ int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS,
 
 // M (k x k, column-major as the reference stores it) = A^T B.
 int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M) {
-  const int ts = k <= 16 ? 16 : (k <= 32 ? 32 : GT);
-  const int tiles = (k + ts - 1) / ts;
-  int splits = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * 4 / (tiles * tiles), (ctx->n + 255) / 256));
+  // C = S^T L S is symmetric: the entries p <= q are summed and mirrored
+  const int nout = k * (k + 1) / 2;
+  const int no = nout <= 1024 ? 1 : (nout <= 2048 ? 2 : (nout <= 4096 ? 4 : (nout <= 8192 ? 8 : 0)));
+  int blocks_x, threads, splits;
+  size_t smem = 0;
+  if (no) {
+    threads = (int)(((nout + no - 1) / no + 31) / 32 * 32);
+    blocks_x = 1;
+    smem = sizeof(double) * 2 * GR * (k + 1);
+    const int per_sm = std::max(1, 2048 / threads);
+    splits = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm, (ctx->n + 255) / 256));
+  } else {
+    const int tiles = (k + GT - 1) / GT;
+    threads = 256;
+    blocks_x = tiles * (tiles + 1) / 2;
+    splits = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * 4 / blocks_x, (ctx->n + 255) / 256));
+  }
   double *part = (double *)phde_buf(ctx, "gram.part", sizeof(double) * (size_t)splits * k * k);
   if (!part) return PHDE_ERR_OOM;
-  const dim3 grid(tiles * tiles, splits);
-  if (k <= 32)
-    gram_small_kernel<<<dim3(1, splits), 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+  const dim3 grid(blocks_x, splits);
+  if (no == 1)
+    gram_list_kernel<1><<<grid, threads, smem, ctx->stream>>>(A, B, ctx->n, k, part);
+  else if (no == 2)
+    gram_list_kernel<2><<<grid, threads, smem, ctx->stream>>>(A, B, ctx->n, k, part);
+  else if (no == 4)
+    gram_list_kernel<4><<<grid, threads, smem, ctx->stream>>>(A, B, ctx->n, k, part);
+  else if (no == 8)
+    gram_list_kernel<8><<<grid, threads, smem, ctx->stream>>>(A, B, ctx->n, k, part);
   else
-    gram_kernel<4><<<grid, 256, 0, ctx->stream>>>(A, B, ctx->n, k, part);
+    gram_kernel<4><<<grid, threads, 0, ctx->stream>>>(A, B, ctx->n, k, part);
   PHDE_LAUNCHED(ctx);
-  sum_parts_kernel<<<grid_for(ctx, (int64_t)k * k, 256), 256, 0, ctx->stream>>>(part, splits, (int64_t)k * k, M);
+  sum_parts_sym_kernel<<<grid_for(ctx, (int64_t)k * k, 256), 256, 0, ctx->stream>>>(part, splits, k, M);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }
@@ -915,13 +1055,15 @@ int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, d
     PHDE_LAUNCHED(ctx);
     return PHDE_OK;
   }
-  const int grid = grid_for(ctx, ctx->n, threads, 8);
+  // row tiles of 128 rows (64 for k > 100): at most (256 * 8 + 64 * 257) * 8 bytes of shared memory
+  const int rows = k <= 100 ? 128 : 64;
+  const int grid = grid_for(ctx, ctx->n, rows, 8);
   double *part = (double *)phde_buf(ctx, "coords.part", sizeof(double) * grid * (size_t)c);
   if (!part) return PHDE_ERR_OOM;
-  const size_t ysmem = sizeof(double) * (size_t)k * c;
+  const size_t smem = sizeof(double) * ((size_t)k * CO_MAXC + (size_t)rows * (k + 1));
   PHDE_CK(ctx, cudaFuncSetAttribute(coords_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)std::max<size_t>(ysmem, 48 * 1024)));
-  coords_kernel<<<grid, threads, ysmem, ctx->stream>>>(M, Y, ctx->n, k, c, X, part);
+                                    (int)std::max<size_t>(smem, 48 * 1024)));
+  coords_kernel<<<grid, rows, smem, ctx->stream>>>(M, Y, ctx->n, k, c, X, part);
   PHDE_LAUNCHED(ctx);
   scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid);
   PHDE_LAUNCHED(ctx);

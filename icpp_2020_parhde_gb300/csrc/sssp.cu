@@ -42,31 +42,9 @@ struct SsArgs {
   uint64_t timeout_ns;
 };
 
-__device__ __forceinline__ void block_append(bool flag, uint32_t v, uint32_t *arr, unsigned *ctr, unsigned *s_base,
-                                             unsigned *s_warp) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  const unsigned bal = __ballot_sync(PHDE_FULL_MASK, flag);
-  const unsigned before = __popc(bal & ((1u << lane) - 1u));
-  if (lane == 0) s_warp[warp] = __popc(bal);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned tot = 0;
-    for (int i = 0; i < nw; i++) {
-      unsigned c = s_warp[i];
-      s_warp[i] = tot;
-      tot += c;
-    }
-    *s_base = tot ? atomicAdd(ctr, tot) : 0u;
-  }
-  __syncthreads();
-  if (flag) arr[*s_base + s_warp[warp] + before] = v;
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(SS_THREADS) sssp_nearfar_kernel(SsArgs a) {
-  __shared__ PushScratch psc;
-  __shared__ unsigned s_warp[32];
-  __shared__ unsigned s_base;
+__global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
+  __shared__ Push2Scratch psc;
+  __shared__ uint32_t s_win[SS_THREADS / 32][32];
   __shared__ ull red[32];
   const int tid = threadIdx.x;
   const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
@@ -99,33 +77,36 @@ __global__ void __launch_bounds__(SS_THREADS) sssp_nearfar_kernel(SsArgs a) {
       if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 1) & 3] = 0ull;
       const int64_t E = f_edges;
       for (int64_t base = gbase; base < E; base += gstride) {
-        const int64_t e = base + tid;
+        const int64_t e = base + tid, e0w = base + (tid & ~31);
         bool to_near = false, to_far = false;
         uint32_t v = 0, dv = 0;
-        if (e < E) {
-          const uint32_t s = owner_slot(qin_e, f_cnt, (uint32_t)e);
-          const uint32_t u = qin_v[s];
-          const int64_t j = a.off[u] + (e - (int64_t)qin_e[s]);
-          v = __ldg(a.adj + j);
-          edges_local++;
-          const int32_t du = __ldcg(a.dist + u);
-          const int32_t nd = du + __ldg(a.w + j);
-          if (nd < __ldcg(a.dist + v)) {
-            const int32_t old = atomicMin(a.dist + v, nd);
-            if (nd < old) {
-              if (nd < T) {
-                if (atomicExch(a.stamp_near + v, it + 1) != it + 1) {
-                  to_near = true;
-                  dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+        if (e0w < E) {  // warp-uniform
+          uint32_t es;
+          const uint32_t s = warp_owner_slots(qin_e, f_cnt, (uint32_t)e0w, s_win[tid >> 5], es);
+          if (e < E) {
+            const uint32_t u = qin_v[s];
+            const int64_t j = a.off[u] + (e - (int64_t)es);
+            v = __ldg(a.adj + j);
+            edges_local++;
+            const int32_t du = __ldcg(a.dist + u);
+            const int32_t nd = du + __ldg(a.w + j);
+            if (nd < __ldcg(a.dist + v)) {
+              const int64_t ov0 = __ldg(a.off + v), ov1 = __ldg(a.off + v + 1);  // in flight with the atomic
+              const int32_t old = atomicMin(a.dist + v, nd);
+              if (nd < old) {
+                if (nd < T) {
+                  if (atomicExch(a.stamp_near + v, it + 1) != it + 1) {
+                    to_near = true;
+                    dv = (uint32_t)(ov1 - ov0);
+                  }
+                } else if (atomicExch(a.stamp_far + v, phase) != phase) {
+                  to_far = true;
                 }
-              } else if (atomicExch(a.stamp_far + v, phase) != phase) {
-                to_far = true;
               }
             }
           }
         }
-        block_push(to_near, v, dv, qout_v, qout_e, octr, &psc);
-        block_append(to_far, v, far_in, fctr, &s_base, s_warp);
+        block_push2(to_near, v, dv, qout_v, qout_e, octr, to_far, far_in, fctr, &psc);
       }
       if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
       const ull out = __ldcg(octr);
@@ -177,8 +158,7 @@ __global__ void __launch_bounds__(SS_THREADS) sssp_nearfar_kernel(SsArgs a) {
           keep = atomicExch(a.stamp_far + v, phase + 1) != phase + 1;
         }
       }
-      block_push(to_near, v, dv, qout_v, qout_e, octr, &psc);
-      block_append(keep, v, far_out, fout_ctr, &s_base, s_warp);
+      block_push2(to_near, v, dv, qout_v, qout_e, octr, keep, far_out, fout_ctr, &psc);
     }
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
     const ull out = __ldcg(octr);
