@@ -53,7 +53,8 @@ class LayoutStats(C.Structure):
                 ("ms_mmult", C.c_double), ("ms_eig", C.c_double), ("ms_coords", C.c_double),
                 ("ms_total", C.c_double), ("edges_examined", C.c_int64), ("ms_dist_kernel", C.c_double),
                 ("dist_kernel_launches", C.c_int), ("ms_msbfs_kernel", C.c_double), ("msbfs_levels", C.c_int),
-                ("batch_graph_replay", C.c_int), ("batch_seg_rows", C.c_int), ("ms_batch_tune", C.c_double)]
+                ("batch_graph_replay", C.c_int), ("batch_seg_rows", C.c_int), ("ms_batch_tune", C.c_double),
+                ("sssp_rounds", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

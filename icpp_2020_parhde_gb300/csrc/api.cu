@@ -313,9 +313,9 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   ctx->kev_pending = false;
   tm.mark(0);
   double *deg = (double *)phde_buf(ctx, "deg", sizeof(double) * n);
-  ull *edges = (ull *)phde_buf(ctx, "edges", sizeof(ull));
+  ull *edges = (ull *)phde_buf(ctx, "edges", 2 * sizeof(ull));  // [0] edges examined, [1] SSSP rounds
   if (!deg || !edges) return PHDE_ERR_OOM;
-  PHDE_CK(ctx, cudaMemsetAsync(edges, 0, sizeof(ull), ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(edges, 0, 2 * sizeof(ull), ctx->stream));
   int rc = phde_degrees(ctx, deg);
   if (rc) return rc;
 
@@ -535,8 +535,8 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   tm.mark(5);
   if (sources_out && npasses > 0)
     PHDE_CK(ctx, cudaMemcpyAsync(sources_out, d_src, sizeof(int64_t) * npasses, cudaMemcpyDeviceToHost, ctx->stream));
-  ull h_edges = 0;
-  PHDE_CK(ctx, cudaMemcpyAsync(&h_edges, edges, sizeof(ull), cudaMemcpyDeviceToHost, ctx->stream));
+  ull h_edges[2] = {0, 0};
+  PHDE_CK(ctx, cudaMemcpyAsync(h_edges, edges, 2 * sizeof(ull), cudaMemcpyDeviceToHost, ctx->stream));
   if (extra && extra->evecs)
     PHDE_CK(ctx, cudaMemcpyAsync(extra->evecs, K, sizeof(double) * k * k, cudaMemcpyDeviceToHost, ctx->stream));
   if (extra && extra->evals)
@@ -568,7 +568,8 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     st->ms_eig = tm.ms(3, 4);
     st->ms_coords = tm.ms(4, 5);
     st->ms_total = tm.ms(0, 5);
-    st->edges_examined = (int64_t)h_edges;
+    st->edges_examined = (int64_t)h_edges[0];
+    st->sssp_rounds = (int64_t)h_edges[1];
     st->gpu_launches = (int)(ctx->launches - launches0);
     st->ms_dist_kernel = ctx->kernel_ms;
     st->dist_kernel_launches = ctx->kernel_launches;

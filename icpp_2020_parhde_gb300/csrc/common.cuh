@@ -178,30 +178,37 @@ __device__ __forceinline__ uint32_t owner_slot(const uint32_t *qe, uint32_t f, u
   return lo;
 }
 
+// Largest s in [0, f) with qe[s] <= e (qe non-decreasing, qe[0] == 0, every lane passes the same e): a
+// 32-ary search by the whole warp, one probe per lane and step, about log32(f) dependent loads instead of
+// the log2(f) of owner_slot.
+//
 // Owners of the 32 consecutive edges e0 + lane (lane = 0..31) of a warp, found by the whole warp (every
-// lane calls it with the same e0 < total edges).  The warp's first owner comes from a 32-ary search (one
-// probe per lane and step: about log32(f) dependent loads instead of log2(f)); the others from one window
+// lane calls it with the same e0 < total edges).  The warp's first owner comes from the 32-ary search;
+// the others from one window
 // load qe[s0 .. s0+31]: the slot starting at edge e0 + t is written to position t of a per-warp scratch
 // (the largest such slot, for slots of zero out-degree), and a prefix maximum over the lanes gives each
 // lane the last slot starting at or before its edge.  A lane whose edge lies beyond the window (only
 // possible with zero-degree frontier entries) falls back to the binary search.  `win` is 32 words of
 // shared memory private to the warp; `start` receives qe[owner].
-__device__ __forceinline__ uint32_t warp_owner_slots(const uint32_t *qe, uint32_t f, uint32_t e0, uint32_t *win,
-                                                     uint32_t &start) {
+__device__ __forceinline__ uint32_t warp_search_slot(const uint32_t *qe, uint32_t f, uint32_t e) {
   const int lane = threadIdx.x & 31;
-  uint32_t lo = 0, hi = f;  // invariant: qe[lo] <= e0, answer in [lo, hi)
+  uint32_t lo = 0, hi = f;  // invariant: qe[lo] <= e, answer in [lo, hi)
   while (hi - lo > 32) {
     const uint32_t step = (hi - lo + 31) >> 5;
     const uint32_t pos = lo + (uint32_t)lane * step;
-    const unsigned m = __ballot_sync(PHDE_FULL_MASK, pos < hi && qe[pos] <= e0);  // bit 0 always set
+    const unsigned m = __ballot_sync(PHDE_FULL_MASK, pos < hi && qe[pos] <= e);  // bit 0 always set
     lo += (uint32_t)(31 - __clz(m)) * step;
     hi = min(hi, lo + step);
   }
-  {
-    const uint32_t pos = lo + lane;
-    const unsigned m = __ballot_sync(PHDE_FULL_MASK, pos < hi && qe[pos] <= e0);
-    lo += (uint32_t)(31 - __clz(m));
-  }
+  const uint32_t pos = lo + lane;
+  const unsigned m = __ballot_sync(PHDE_FULL_MASK, pos < hi && qe[pos] <= e);
+  return lo + (uint32_t)(31 - __clz(m));
+}
+
+__device__ __forceinline__ uint32_t warp_owner_slots(const uint32_t *qe, uint32_t f, uint32_t e0, uint32_t *win,
+                                                     uint32_t &start) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lo = warp_search_slot(qe, f, e0);
   const uint32_t s0 = lo, sl = s0 + lane;
   const uint32_t q = sl < f ? qe[sl] : 0xffffffffu;
   const uint32_t qx = s0 + 32 < f ? qe[s0 + 32] : 0xffffffffu;
@@ -226,9 +233,9 @@ __device__ __forceinline__ uint32_t warp_owner_slots(const uint32_t *qe, uint32_
   return s0 + off;
 }
 
-// block_push for two queues at once: the near frontier (vertex + start-edge prefix, as block_push) and a
-// plain vertex list (the far pile), one scan and one barrier pair for both, the two counter atomics
-// issued by two lanes together.
+// block_push for two queues at once: the near frontier (vertex + start-edge prefix, as block_push, and
+// optionally a third per-slot word o) and a plain vertex list (the far pile), one scan and one barrier pair
+// for both, the two counter atomics issued by two lanes together.
 struct Push2Scratch {
   ull warp_tot[32];
   unsigned warp_far[32];
@@ -238,7 +245,7 @@ struct Push2Scratch {
 
 __device__ __forceinline__ void block_push2(bool to_near, uint32_t v, uint32_t dv, uint32_t *qv, uint32_t *qe,
                                             ull *ctr, bool to_far, uint32_t *far, unsigned *far_ctr,
-                                            Push2Scratch *sc) {
+                                            Push2Scratch *sc, uint32_t *qo = nullptr, uint32_t o = 0) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   const ull mine = to_near ? ((1ull << 32) | (ull)dv) : 0ull;
   ull x = mine;
@@ -282,6 +289,7 @@ __device__ __forceinline__ void block_push2(bool to_near, uint32_t v, uint32_t d
     const uint32_t slot = (uint32_t)(pos >> 32);
     qv[slot] = v;
     qe[slot] = (uint32_t)(pos & 0xffffffffull);
+    if (qo) qo[slot] = o;
   }
   if (to_far) far[sc->base_far + sc->warp_far[warp] + __popc(fb & ((1u << lane) - 1u))] = v;
   __syncthreads();

@@ -31,18 +31,20 @@ struct SsArgs {
   int32_t *dist;  // [n], SSSP_INF initially
   int32_t delta;
   uint32_t *qv0, *qv1, *qe0, *qe1;  // near frontier (vertex, start-edge prefix)
+  uint32_t *qo0, *qo1;              // near frontier: the vertex's first adjacency index
   uint32_t *far0, *far1;            // far pile
   int32_t *stamp_near, *stamp_far;  // [n], -1 initially
   ull *ctr;                         // [4] near ring
   unsigned *farctr;                 // [2]
   ull *minfar;                      // [2], alternating by phase
-  ull *edges;
+  ull *edges;  // [0] += adjacency entries read, [1] += rounds; may be null
   GridSync *gs;
   int *err;
   uint64_t timeout_ns;
 };
 
-__global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
+template <int MINB>
+__global__ void __launch_bounds__(SS_THREADS, MINB) sssp_nearfar_kernel(SsArgs a) {
   __shared__ Push2Scratch psc;
   __shared__ uint32_t s_win[SS_THREADS / 32][32];
   __shared__ ull red[32];
@@ -54,6 +56,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
     a.dist[src] = 0;
     a.qv0[0] = (uint32_t)src;
     a.qe0[0] = 0;
+    a.qo0[0] = (uint32_t)a.off[src];
     a.stamp_near[src] = 0;
   }
   ull edges_local = 0;
@@ -69,8 +72,10 @@ __global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
     while (f_cnt > 0) {
       const uint32_t *qin_v = (step & 1) ? a.qv1 : a.qv0;
       const uint32_t *qin_e = (step & 1) ? a.qe1 : a.qe0;
+      const uint32_t *qin_o = (step & 1) ? a.qo1 : a.qo0;
       uint32_t *qout_v = (step & 1) ? a.qv0 : a.qv1;
       uint32_t *qout_e = (step & 1) ? a.qe0 : a.qe1;
+      uint32_t *qout_o = (step & 1) ? a.qo0 : a.qo1;
       ull *octr = a.ctr + (step & 3);
       uint32_t *far_in = (phase & 1) ? a.far1 : a.far0;
       unsigned *fctr = a.farctr + (phase & 1);
@@ -79,13 +84,13 @@ __global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
       for (int64_t base = gbase; base < E; base += gstride) {
         const int64_t e = base + tid, e0w = base + (tid & ~31);
         bool to_near = false, to_far = false;
-        uint32_t v = 0, dv = 0;
+        uint32_t v = 0, dv = 0, ov = 0;
         if (e0w < E) {  // warp-uniform
           uint32_t es;
           const uint32_t s = warp_owner_slots(qin_e, f_cnt, (uint32_t)e0w, s_win[tid >> 5], es);
           if (e < E) {
             const uint32_t u = qin_v[s];
-            const int64_t j = a.off[u] + (e - (int64_t)es);
+            const int64_t j = (int64_t)qin_o[s] + (e - (int64_t)es);  // qin_o[s] = off[u], loaded with u
             v = __ldg(a.adj + j);
             edges_local++;
             const int32_t du = __ldcg(a.dist + u);
@@ -98,6 +103,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
                   if (atomicExch(a.stamp_near + v, it + 1) != it + 1) {
                     to_near = true;
                     dv = (uint32_t)(ov1 - ov0);
+                    ov = (uint32_t)ov0;
                   }
                 } else if (atomicExch(a.stamp_far + v, phase) != phase) {
                   to_far = true;
@@ -106,7 +112,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
             }
           }
         }
-        block_push2(to_near, v, dv, qout_v, qout_e, octr, to_far, far_in, fctr, &psc);
+        block_push2(to_near, v, dv, qout_v, qout_e, octr, to_far, far_in, fctr, &psc, qout_o, ov);
       }
       if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
       const ull out = __ldcg(octr);
@@ -140,25 +146,27 @@ __global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
     // split the pile: this is a step of its own, writing the next round's input queue
     uint32_t *qout_v = (step & 1) ? a.qv0 : a.qv1;
     uint32_t *qout_e = (step & 1) ? a.qe0 : a.qe1;
+    uint32_t *qout_o = (step & 1) ? a.qo0 : a.qo1;
     ull *octr = a.ctr + (step & 3);
     if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 1) & 3] = 0ull;
     for (int64_t base = gbase; base < (int64_t)far_cnt; base += gstride) {
       const int64_t i = base + tid;
       bool to_near = false, keep = false;
-      uint32_t v = 0, dv = 0;
+      uint32_t v = 0, dv = 0, ov = 0;
       if (i < far_cnt) {
         v = far_in[i];
         const int32_t d = __ldcg(a.dist + v);
         if (d >= T_old && d < T) {
           if (atomicExch(a.stamp_near + v, it + 1) != it + 1) {
             to_near = true;
-            dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+            ov = (uint32_t)a.off[v];
+            dv = (uint32_t)(a.off[v + 1] - ov);
           }
         } else if (d >= T) {
           keep = atomicExch(a.stamp_far + v, phase + 1) != phase + 1;
         }
       }
-      block_push2(to_near, v, dv, qout_v, qout_e, octr, keep, far_out, fout_ctr, &psc);
+      block_push2(to_near, v, dv, qout_v, qout_e, octr, keep, far_out, fout_ctr, &psc, qout_o, ov);
     }
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
     const ull out = __ldcg(octr);
@@ -171,6 +179,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) sssp_nearfar_kernel(SsArgs a) {
   }
   ull etot = block_sum(edges_local, red);
   if (tid == 0 && a.edges) atomicAdd(a.edges, etot);
+  if (blockIdx.x == 0 && tid == 0 && a.edges) atomicAdd(a.edges + 1, (ull)it);  // rounds (relaxation + split)
 }
 
 // Fold one finished distance column into the Kcenters state (WParHDE.cpp:117-136).
@@ -284,6 +293,8 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   uint32_t *qv1 = (uint32_t *)phde_buf(ctx, "q.v1", sizeof(uint32_t) * n);
   uint32_t *qe0 = (uint32_t *)phde_buf(ctx, "q.e0", sizeof(uint32_t) * n);
   uint32_t *qe1 = (uint32_t *)phde_buf(ctx, "q.e1", sizeof(uint32_t) * n);
+  uint32_t *qo0 = (uint32_t *)phde_buf(ctx, "ss.qo0", sizeof(uint32_t) * n);
+  uint32_t *qo1 = (uint32_t *)phde_buf(ctx, "ss.qo1", sizeof(uint32_t) * n);
   uint32_t *far0 = (uint32_t *)phde_buf(ctx, "ss.far0", sizeof(uint32_t) * n);
   uint32_t *far1 = (uint32_t *)phde_buf(ctx, "ss.far1", sizeof(uint32_t) * n);
   int32_t *stn = (int32_t *)phde_buf(ctx, "ss.stamp_near", sizeof(int32_t) * n);
@@ -291,7 +302,7 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   ull *ctr = (ull *)phde_buf(ctx, "q.ctr", sizeof(ull) * 4);
   unsigned *farctr = (unsigned *)phde_buf(ctx, "ss.farctr", sizeof(unsigned) * 2);
   ull *minfar = (ull *)phde_buf(ctx, "ss.minfar", sizeof(ull) * 2);
-  if (!qv0 || !qv1 || !qe0 || !qe1 || !far0 || !far1 || !stn || !stf || !ctr || !farctr || !minfar) return PHDE_ERR_OOM;
+  if (!qv0 || !qv1 || !qe0 || !qe1 || !qo0 || !qo1 || !far0 || !far1 || !stn || !stf || !ctr || !farctr || !minfar) return PHDE_ERR_OOM;
   int rc;
   if ((rc = phde_fill_i32(ctx, d_col, n, SSSP_INF))) return rc;
   PHDE_CK(ctx, cudaMemsetAsync(stn, 0xff, sizeof(int32_t) * n, ctx->stream));
@@ -300,10 +311,16 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   PHDE_CK(ctx, cudaMemsetAsync(farctr, 0, sizeof(unsigned) * 2, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(minfar, 0xff, sizeof(ull) * 2, ctx->stream));
   if ((rc = phde_reset_sync(ctx))) return rc;
+  // Resident CTAs per SM: one (with the registers it wants) below 2^20 vertices, where rounds are short and
+  // latency-bound (a 64^3 grid: 1.5 ms per pass against 2.1 ms with two), two (registers capped at 32) on
+  // larger graphs (a 256^3 grid: 14.3 ms against 16.1 ms with one); PHDE_SSSP_CTAS=1 or 2 picks outright.
+  const char *ce = getenv("PHDE_SSSP_CTAS");
+  const int want = ce ? (atoi(ce) == 1 ? 1 : 2) : (n < ((int64_t)1 << 20) ? 1 : 2);
+  const void *kfn = want == 1 ? (const void *)sssp_nearfar_kernel<1> : (const void *)sssp_nearfar_kernel<2>;
   int per_sm = 0;
-  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_nearfar_kernel, SS_THREADS, 0));
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, SS_THREADS, 0));
   if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "sssp kernel cannot be resident");
-  per_sm = std::min(per_sm, 2);
+  per_sm = std::min(per_sm, want);
   SsArgs a;
   a.off = ctx->d_off;
   a.adj = ctx->d_adj;
@@ -316,6 +333,8 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   a.qv1 = qv1;
   a.qe0 = qe0;
   a.qe1 = qe1;
+  a.qo0 = qo0;
+  a.qo1 = qo1;
   a.far0 = far0;
   a.far1 = far1;
   a.stamp_near = stn;
@@ -329,7 +348,7 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   a.timeout_ns = ctx->timeout_ns;
   void *args[] = {&a};
   cudaEventRecord(ctx->kev[0], ctx->stream);
-  PHDE_CK(ctx, cudaLaunchCooperativeKernel((const void *)sssp_nearfar_kernel, dim3(ctx->nsm * per_sm),
+  PHDE_CK(ctx, cudaLaunchCooperativeKernel(kfn, dim3(ctx->nsm * per_sm),
                                            dim3(SS_THREADS), args, 0, ctx->stream));
   PHDE_LAUNCHED(ctx);
   cudaEventRecord(ctx->kev[1], ctx->stream);

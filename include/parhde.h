@@ -98,6 +98,7 @@ typedef struct {
   int batch_graph_replay;   /* phde_layout_batched: 1 when the pipeline ran as one CUDA graph launch     */
   int batch_seg_rows;       /* phde_layout_batched: rows per segment CTA picked by the autotuner         */
   double ms_batch_tune;     /* phde_layout_batched: the autotuner's best whole-batch time (first call)   */
+  int64_t sssp_rounds;      /* WParHDE: synchronised relaxation rounds of the SSSP passes, summed        */
 } phde_layout_stats;
 
 /* optional extra outputs of phde_layout (any member may be NULL) */
