@@ -30,6 +30,7 @@ struct SsArgs {
   const int64_t *src;
   int32_t *dist;  // [n], SSSP_INF initially
   int32_t delta;
+  int lmax;                         // block-local relaxation rounds per grid round
   uint32_t *qv0, *qv1, *qe0, *qe1;  // near frontier (vertex, start-edge prefix)
   uint32_t *qo0, *qo1;              // near frontier: the vertex's first adjacency index
   uint32_t *far0, *far1;            // far pile
@@ -43,11 +44,69 @@ struct SsArgs {
   uint64_t timeout_ns;
 };
 
+constexpr int SS_LQ = SS_THREADS;  // block-local queue capacity (one entry per thread for its prefix scan)
+
+// The block-local queue: vertices a block improved below the band limit, relaxed again by the same block
+// before the grid barrier.
+struct LocalQ {
+  uint32_t v[2][SS_LQ], deg[2][SS_LQ], first[2][SS_LQ], off[2][SS_LQ];  // first: exclusive prefix of deg
+  uint32_t cnt[2];  // entries claimed (may exceed SS_LQ: the excess went to the grid queue)
+  uint32_t total;   // edges of the buffer being relaxed
+  uint32_t warp_sum[32];
+};
+
+// One edge u -> v (index j).  Returns the flags of what the improvement asks for: near (below the band
+// limit T) or far; atomicMin has already lowered dist[v].  ov/dv: v's adjacency start and out-degree.
+__device__ __forceinline__ void relax_edge(const SsArgs &a, uint32_t u, int64_t j, int64_t T, uint32_t &v, bool &near,
+                                           bool &far, uint32_t &ov, uint32_t &dv) {
+  v = __ldg(a.adj + j);
+  const int32_t du = __ldcg(a.dist + u);
+  const int32_t nd = du + __ldg(a.w + j);
+  if (nd < __ldcg(a.dist + v)) {
+    const int64_t ov0 = __ldg(a.off + v), ov1 = __ldg(a.off + v + 1);  // in flight with the atomic
+    const int32_t old = atomicMin(a.dist + v, nd);
+    if (nd < old) {
+      near = nd < T;
+      far = !near;
+      ov = (uint32_t)ov0;
+      dv = (uint32_t)(ov1 - ov0);
+    }
+  }
+}
+
+// Offers near improvements to local buffer b (warp-aggregated slot claims in shared memory); those that do
+// not fit fall back to the grid queue, de-duplicated by the round's stamp.  Far improvements are
+// de-duplicated by the phase's stamp.  On return to_near / to_far are the grid-queue and far-pile flags.
+__device__ __forceinline__ void place(const SsArgs &a, LocalQ &lq, int b, bool local_ok, uint32_t v, uint32_t dv,
+                                      uint32_t ov, int32_t it, int32_t phase, bool &to_near, bool &to_far) {
+  const int lane = threadIdx.x & 31;
+  bool want = local_ok && to_near;
+  const unsigned m = __ballot_sync(PHDE_FULL_MASK, want);
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    uint32_t wb = 0;
+    if (lane == leader) wb = atomicAdd(&lq.cnt[b], (uint32_t)__popc(m));
+    wb = __shfl_sync(PHDE_FULL_MASK, wb, leader);
+    if (want) {
+      const uint32_t slot = wb + __popc(m & ((1u << lane) - 1u));
+      if (slot < SS_LQ) {
+        lq.v[b][slot] = v;
+        lq.deg[b][slot] = dv;
+        lq.off[b][slot] = ov;
+        to_near = false;  // handled locally
+      }
+    }
+  }
+  if (to_near) to_near = atomicExch(a.stamp_near + v, it + 1) != it + 1;
+  if (to_far) to_far = atomicExch(a.stamp_far + v, phase) != phase;
+}
+
 template <int MINB>
 __global__ void __launch_bounds__(SS_THREADS, MINB) sssp_nearfar_kernel(SsArgs a) {
   __shared__ Push2Scratch psc;
   __shared__ uint32_t s_win[SS_THREADS / 32][32];
   __shared__ ull red[32];
+  __shared__ LocalQ lq;
   const int tid = threadIdx.x;
   const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
   const int64_t gbase = (int64_t)blockIdx.x * blockDim.x;
@@ -81,6 +140,9 @@ __global__ void __launch_bounds__(SS_THREADS, MINB) sssp_nearfar_kernel(SsArgs a
       unsigned *fctr = a.farctr + (phase & 1);
       if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 1) & 3] = 0ull;
       const int64_t E = f_edges;
+      const bool local_on = a.lmax > 0;
+      if (tid == 0) lq.cnt[0] = lq.cnt[1] = 0;
+      __syncthreads();
       for (int64_t base = gbase; base < E; base += gstride) {
         const int64_t e = base + tid, e0w = base + (tid & ~31);
         bool to_near = false, to_far = false;
@@ -91,28 +153,70 @@ __global__ void __launch_bounds__(SS_THREADS, MINB) sssp_nearfar_kernel(SsArgs a
           if (e < E) {
             const uint32_t u = qin_v[s];
             const int64_t j = (int64_t)qin_o[s] + (e - (int64_t)es);  // qin_o[s] = off[u], loaded with u
-            v = __ldg(a.adj + j);
             edges_local++;
-            const int32_t du = __ldcg(a.dist + u);
-            const int32_t nd = du + __ldg(a.w + j);
-            if (nd < __ldcg(a.dist + v)) {
-              const int64_t ov0 = __ldg(a.off + v), ov1 = __ldg(a.off + v + 1);  // in flight with the atomic
-              const int32_t old = atomicMin(a.dist + v, nd);
-              if (nd < old) {
-                if (nd < T) {
-                  if (atomicExch(a.stamp_near + v, it + 1) != it + 1) {
-                    to_near = true;
-                    dv = (uint32_t)(ov1 - ov0);
-                    ov = (uint32_t)ov0;
-                  }
-                } else if (atomicExch(a.stamp_far + v, phase) != phase) {
-                  to_far = true;
-                }
-              }
-            }
+            relax_edge(a, u, j, T, v, to_near, to_far, ov, dv);
           }
         }
+        place(a, lq, 0, local_on, v, dv, ov, it, phase, to_near, to_far);
         block_push2(to_near, v, dv, qout_v, qout_e, octr, to_far, far_in, fctr, &psc, qout_o, ov);
+      }
+      // ---- block-local rounds: relax what this block improved, without a grid barrier; the last local
+      // round (and any overflow of the local queue) sends its improvements to the grid queue ----
+      int cur = 0;
+      for (int li = 0; li < a.lmax; li++) {
+        __syncthreads();  // the buffer's entries are written
+        const uint32_t cnt = min(lq.cnt[cur], (uint32_t)SS_LQ);
+        if (cnt == 0) break;
+        {  // exclusive prefix of the out-degrees, one entry per thread
+          const int lane = tid & 31, w = tid >> 5;
+          const uint32_t d = (uint32_t)tid < cnt ? lq.deg[cur][tid] : 0u;
+          uint32_t x = d;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(PHDE_FULL_MASK, x, o);
+            if (lane >= o) x += y;
+          }
+          if (lane == 31) lq.warp_sum[w] = x;
+          __syncthreads();
+          if (w == 0) {
+            const uint32_t ws_ = lane < (int)(blockDim.x >> 5) ? lq.warp_sum[lane] : 0u;
+            uint32_t y = ws_;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const uint32_t z = __shfl_up_sync(PHDE_FULL_MASK, y, o);
+              if (lane >= o) y += z;
+            }
+            lq.warp_sum[lane] = y - ws_;
+            if (lane == 31) lq.total = y;
+          }
+          __syncthreads();
+          if ((uint32_t)tid < cnt) lq.first[cur][tid] = lq.warp_sum[w] + x - d;
+          if (tid == 0) lq.cnt[cur ^ 1] = 0;
+          __syncthreads();
+        }
+        const uint32_t total = lq.total;
+        for (uint32_t eb = 0; eb < total; eb += blockDim.x) {
+          const uint32_t e = eb + tid;
+          bool to_near = false, to_far = false;
+          uint32_t v = 0, dv = 0, ov = 0;
+          if (e < total) {
+            uint32_t lo = 0, hi = cnt;  // the entry owning local edge e
+            while (hi - lo > 1) {
+              const uint32_t mid = (lo + hi) >> 1;
+              if (lq.first[cur][mid] <= e)
+                lo = mid;
+              else
+                hi = mid;
+            }
+            const uint32_t u = lq.v[cur][lo];
+            const int64_t j = (int64_t)lq.off[cur][lo] + (e - lq.first[cur][lo]);
+            edges_local++;
+            relax_edge(a, u, j, T, v, to_near, to_far, ov, dv);
+          }
+          place(a, lq, cur ^ 1, li + 1 < a.lmax, v, dv, ov, it, phase, to_near, to_far);
+          block_push2(to_near, v, dv, qout_v, qout_e, octr, to_far, far_in, fctr, &psc, qout_o, ov);
+        }
+        cur ^= 1;
       }
       if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
       const ull out = __ldcg(octr);
@@ -329,6 +433,10 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   a.src = d_src;
   a.dist = d_col;
   a.delta = delta;
+  // block-local rounds per grid round: each block keeps relaxing the vertices it improved below the band
+  // limit (up to SS_LQ of them) this many times before the grid barrier; PHDE_SSSP_LOCAL sets the count
+  const char *le = getenv("PHDE_SSSP_LOCAL");
+  a.lmax = le ? std::max(0, atoi(le)) : 4;
   a.qv0 = qv0;
   a.qv1 = qv1;
   a.qe0 = qe0;

@@ -64,6 +64,24 @@ def test_sssp_exact_vs_oracle(gpu_ctx, L, seed):
         assert np.array_equal(d[:, i], orc.sssp(g, s))
 
 
+@pytest.mark.parametrize("local,ctas,delta", [("0", "2", None), ("1", "1", None), ("4", "2", "40"), ("16", "1", "7")])
+def test_sssp_round_shapes_exact(gpu_ctx, monkeypatch, local, ctas, delta):
+    """The block-local round count, resident CTAs per SM and band width change the work, never the
+    distances: a weighted grid and a weighted R-MAT (hubs: several chunks per block) under each shape."""
+    monkeypatch.setenv("PHDE_SSSP_LOCAL", local)
+    monkeypatch.setenv("PHDE_SSSP_CTAS", ctas)
+    if delta is None:
+        monkeypatch.delenv("PHDE_SSSP_DELTA", raising=False)
+    else:
+        monkeypatch.setenv("PHDE_SSSP_DELTA", delta)
+    for g in (graphs.grid3d(24, seed=4), graphs.with_random_weights(graphs.rmat(13, seed=5), seed=6, wmin=1, wmax=300)):
+        gpu_ctx.upload(g)
+        src = [0, g.n - 1, g.n // 3]
+        d = gpu_ctx.distances(src)
+        for i, s in enumerate(src):
+            assert np.array_equal(d[:, i], orc.sssp(g, s))
+
+
 def test_sssp_exact_on_weighted_rmat(gpu_ctx):
     g = graphs.with_random_weights(graphs.rmat(14, seed=9), seed=3, wmin=1, wmax=1000)
     gpu_ctx.upload(g)
