@@ -569,10 +569,16 @@ def run_weighted(args):
     import torch
     torch.cuda.set_device(local)
     from icpp_2020_parhde_gb300 import Context, graphs
+    from icpp_2020_parhde_gb300.csr_io import CSRGraph
     g, gen_s = make_graph(args)
     ctx = Context(local)
     n, nnz, k, c = g.n, g.nnz, args.k, args.c
-    ctx.upload(g)
+    # pinned host copies of the inputs (end-to-end path) and of the output
+    off_h = torch.from_numpy(g.offsets.astype(np.uint32)).pin_memory()
+    adj_h = torch.from_numpy(g.adj.astype(np.uint32)).pin_memory()
+    w_h = torch.from_numpy(g.weights.astype(np.int32)).pin_memory()
+    gp = CSRGraph(off_h.numpy(), adj_h.numpy(), w_h.numpy())
+    ctx.upload(gp)
     xy_h = torch.empty(n * c, dtype=torch.float64).pin_memory()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -597,7 +603,7 @@ def run_weighted(args):
     e2e_t = []
     for _ in range(args.steps):
         t1 = time.perf_counter()
-        ctx.upload(g)
+        ctx.upload(gp)
         run()
         e2e_t.append(time.perf_counter() - t1)
     clk.__exit__(None, None, None)
@@ -613,7 +619,8 @@ def run_weighted(args):
             "phases_ms": {p: float(np.mean([st[p] for st in stats])) for p in PHASES},
             "e2e": {"value": ws * k * nnz / e2e_s, "unit": UNIT, "ms_per_graph": e2e_s * 1e3,
                     "h2d_bytes_per_step": 4 * (n + 1) + 8 * nnz, "d2h_bytes_per_step": 8 * n * c,
-                    "timing": "mean of %d host-timed upload + layout calls" % len(e2e_t), "ms_each": [round(x * 1e3, 1) for x in e2e_t]},
+                    "timing": "mean of %d host-timed calls: upload from pinned host CSR + layout + coordinates to "
+                              "pinned host memory" % len(e2e_t), "ms_each": [round(x * 1e3, 1) for x in e2e_t]},
             "gpu_launches": launches, "clocks": clk.summary()}
     if not args.no_cpu_baseline:
         from oracle import oracle as orc
