@@ -43,6 +43,50 @@ def test_layout_matches_reference_goldens(case):
         np.testing.assert_allclose(L.coords, ref_xy, rtol=0, atol=1e-12)
 
 
+def _one_reduction_mgs(g, sources, k):
+    """WParHDE's coupled D-orthogonalisation in the one-reduction form the GPU kernels use (mgs_dots_kernel,
+    mgs_solve_kernel, mgs_apply_kernel): per distance column one sweep for r_q = <x0, D y_q> (and the Gram
+    row of the newest accepted column), the recurrence c_q G_qq = r_q - sum_{p<q} c_p G_pq, one sweep for
+    x = x0 - sum c_q y_q; discard below 1e-3 as WParHDE.cpp:194-204."""
+    n = g.n
+    off = g.offsets.astype(np.int64)
+    d = np.array([float(g.weights[off[i]:off[i + 1]].astype(np.float64).sum()) for i in range(n)])
+    Y = [np.full(n, 1.0 / np.sqrt(n))]
+    G = np.zeros((k + 1, k + 1))
+    gram_cols = 0
+    for s in sources:
+        if len(Y) > k:
+            break
+        col = orc.sssp(g, int(s)).astype(np.float64)
+        x0 = col * (1.0 / np.sqrt(float(np.sum(col.astype(np.int64) ** 2))))
+        j = len(Y)
+        if gram_cols < j:
+            yg = Y[j - 1] * d
+            for p in range(j):
+                G[p, j - 1] = Y[p] @ yg
+            gram_cols = j
+        r = np.array([Y[q] @ (x0 * d) for q in range(j)])
+        c = np.zeros(j)
+        for q in range(j):
+            c[q] = (r[q] - c[:q] @ G[:q, q]) * (1.0 / G[q, q])
+        x = x0 - sum(c[q] * Y[q] for q in range(j))
+        nrm = np.sqrt(x @ x)
+        if nrm >= 0.001:
+            Y.append(x * (1.0 / nrm))
+    return np.stack(Y[1:k + 1], axis=1)
+
+
+def test_one_reduction_mgs_matches_reference_mgs():
+    """The reorganised MGS equals the reference's sweep-per-column MGS (the oracle follows WParHDE.cpp's
+    operation order) to rounding, on the golden weighted grid and on a larger one."""
+    from icpp_2020_parhde_gb300 import graphs
+    for g, k in ((load_golden("grid12w")[0], 10), (graphs.grid3d(16, seed=3), 16)):
+        L = orc.layout(g, "wParHDE", "Kcenters", k, 2, nthreads=1, dist_algo="serial")
+        assert L.status == 0
+        S = _one_reduction_mgs(g, L.sources, k)
+        np.testing.assert_allclose(S, L.S, rtol=0, atol=1e-10)
+
+
 def test_kcenters_variants_agree_on_connected_graph():
     g, _ = load_golden("rmat13")
     d0, s0 = orc.kcenters(g, 30, 0)
