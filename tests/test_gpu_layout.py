@@ -72,6 +72,38 @@ def test_exact_eigensolver_vs_numpy(gpu_ctx, algo, k, c):
     np.testing.assert_allclose(sign_align(r.coords, L.coords), L.coords, rtol=0, atol=1e-7)
 
 
+@pytest.mark.parametrize("algo,k,make", [
+    ("ParHDE", 64, lambda: graphs.mesh(150, 80, seed=31)),
+    ("ParHDE", 130, lambda: graphs.mesh(150, 80, seed=32)),
+    ("wParHDE", 40, lambda: graphs.grid3d(20, seed=33)),
+], ids=["parhde-k64", "parhde-k130", "wparhde-k40"])
+def test_fp64_large_k_vs_oracle(gpu_ctx, algo, k, make):
+    """Large k takes the other FP64 kernel shapes: the Gram with 4 or more outputs per thread or on upper
+    tiles, coordinate row tiles of 64 rows, MGS dot sweeps over several column tiles."""
+    sp = pytest.importorskip("scipy.sparse")
+    g = make()
+    gpu_ctx.upload(g)
+    r = gpu_ctx.layout(algo, "Kcenters", k, 3, eig="exact", extra=True)
+    L = orc.layout(g, algo, "Kcenters", k, 3, eig="exact", nthreads=4)
+    assert np.array_equal(r.sources, L.sources)
+    np.testing.assert_allclose(r.basis, L.S, rtol=0, atol=1e-9)
+    # SpMM + Gram against S^T L S formed in numpy from the GPU's own basis (tight: the kernels alone) ...
+    w = np.ones(g.nnz) if g.weights is None else g.weights.astype(np.float64)
+    A = sp.csr_matrix((w, g.adj.astype(np.int64), g.offsets.astype(np.int64)), shape=(g.n, g.n))
+    Lap = sp.diags(np.asarray(A.sum(axis=1)).ravel()) - A
+    Mb = r.basis.T @ (Lap @ r.basis)
+    np.testing.assert_allclose(r.gram, Mb, rtol=0, atol=1e-11 * np.abs(Mb).max())
+    # ... and against the oracle's, where the late basis columns' conditioning (up to k = 130 nearly
+    # collinear distance columns) amplifies the orthogonalisation's rounding differences
+    np.testing.assert_allclose(r.gram, L.M, rtol=0, atol=1e-6 * np.abs(L.M).max())
+    # the coordinates against the GPU's own basis and Gram (a rectangular mesh: the first four eigenvalues
+    # are apart by 2.7e-5 relative or more, so the eigenvectors are well defined)
+    w, V = np.linalg.eigh(0.5 * (r.gram + r.gram.T))
+    X = r.basis @ V[:, :3]
+    X /= np.linalg.norm(X, axis=0)
+    np.testing.assert_allclose(sign_align(r.coords, X), X, rtol=0, atol=1e-8)
+
+
 def test_wparhde_on_larger_grid_vs_oracle(gpu_ctx):
     g = graphs.grid3d(24, seed=8)
     gpu_ctx.upload(g)
