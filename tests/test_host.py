@@ -72,6 +72,34 @@ def test_library_exports_every_declared_symbol():
         assert re.search(r"\bT %s$" % f, out, re.M), f
 
 
+def test_ctypes_mirrors_match_the_c_abi(tmp_path):
+    """Every ctypes structure of the Python binding has the size and field offsets of its C declaration in
+    include/parhde.h (compiled here with the host compiler)."""
+    from icpp_2020_parhde_gb300 import _lib
+    structs = {"phde_layout_opts": _lib.LayoutOpts, "phde_layout_stats": _lib.LayoutStats,
+               "phde_layout_extra": _lib.LayoutExtra, "phde_graph_desc": _lib.GraphDesc,
+               "phde_csr_info": _lib.CsrInfo, "phde_draw_info": _lib.DrawInfo}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "parhde.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "abi.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "abi"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n"):
+        if ln:
+            a, b, v = ln.split()
+            got[(a, b)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
 def test_status_strings_without_gpu():
     lib = ctypes.CDLL(pbuild.build())
     lib.phde_status_string.restype = ctypes.c_char_p
