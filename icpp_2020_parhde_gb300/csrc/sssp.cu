@@ -433,10 +433,14 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   a.src = d_src;
   a.dist = d_col;
   a.delta = delta;
-  // block-local rounds per grid round: each block keeps relaxing the vertices it improved below the band
-  // limit (up to SS_LQ of them) this many times before the grid barrier; PHDE_SSSP_LOCAL sets the count
+  // block-local rounds per grid round (PHDE_SSSP_LOCAL, none by default): each block keeps relaxing the
+  // vertices it improved below the band limit (up to SS_LQ of them) this many times before the grid
+  // barrier.  On a 256^3 grid four local rounds took 10-12.5 ms per pass on some runs and 43-50 ms on
+  // others (same inputs, band 1024; band 512 stayed near 13 ms), against 14.6 ms without: the blocks that
+  // run ahead inside the band relax with distances other blocks later lower, and how much of that is
+  // wasted depends on timing.  Off until that is bounded.
   const char *le = getenv("PHDE_SSSP_LOCAL");
-  a.lmax = le ? std::max(0, atoi(le)) : 4;
+  a.lmax = le ? std::max(0, atoi(le)) : 0;
   a.qv0 = qv0;
   a.qv1 = qv1;
   a.qe0 = qe0;
