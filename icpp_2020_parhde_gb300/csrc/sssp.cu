@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(SS_THREADS, MINB) sssp_nearfar_kernel(SsArgs a
   __shared__ Push2Scratch psc;
   __shared__ uint32_t s_win[SS_THREADS / 32][32];
   __shared__ ull red[32];
-  __shared__ LocalQ lq;
+  extern __shared__ __align__(16) unsigned char ss_dyn[];  // the LocalQ, present only when a.lmax > 0
+  LocalQ &lq = *reinterpret_cast<LocalQ *>(ss_dyn);
   const int tid = threadIdx.x;
   const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
   const int64_t gbase = (int64_t)blockIdx.x * blockDim.x;
@@ -141,8 +142,10 @@ __global__ void __launch_bounds__(SS_THREADS, MINB) sssp_nearfar_kernel(SsArgs a
       if (blockIdx.x == 0 && tid == 0) a.ctr[(step + 1) & 3] = 0ull;
       const int64_t E = f_edges;
       const bool local_on = a.lmax > 0;
-      if (tid == 0) lq.cnt[0] = lq.cnt[1] = 0;
-      __syncthreads();
+      if (local_on) {
+        if (tid == 0) lq.cnt[0] = lq.cnt[1] = 0;
+        __syncthreads();
+      }
       for (int64_t base = gbase; base < E; base += gstride) {
         const int64_t e = base + tid, e0w = base + (tid & ~31);
         bool to_near = false, to_far = false;
@@ -421,8 +424,17 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   const char *ce = getenv("PHDE_SSSP_CTAS");
   const int want = ce ? (atoi(ce) == 1 ? 1 : 2) : (n < ((int64_t)1 << 20) ? 1 : 2);
   const void *kfn = want == 1 ? (const void *)sssp_nearfar_kernel<1> : (const void *)sssp_nearfar_kernel<2>;
+  // block-local rounds per grid round (PHDE_SSSP_LOCAL, none by default): each block keeps relaxing the
+  // vertices it improved below the band limit (up to SS_LQ of them) this many times before the grid
+  // barrier.  On a 256^3 grid four local rounds took 10-12.5 ms per pass on some runs and 43-50 ms on
+  // others (same inputs, band 1024; band 512 stayed near 13 ms), against 14.6 ms without: the blocks that
+  // run ahead inside the band relax with distances other blocks later lower, and how much of that is
+  // wasted depends on timing.  Off until that is bounded.
+  const char *le = getenv("PHDE_SSSP_LOCAL");
+  const int lmax = le ? std::max(0, atoi(le)) : 0;
+  const size_t dyn = lmax > 0 ? sizeof(LocalQ) : 0;  // the queue's shared memory, below the 48 KB default
   int per_sm = 0;
-  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, SS_THREADS, 0));
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, SS_THREADS, dyn));
   if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "sssp kernel cannot be resident");
   per_sm = std::min(per_sm, want);
   SsArgs a;
@@ -433,14 +445,7 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   a.src = d_src;
   a.dist = d_col;
   a.delta = delta;
-  // block-local rounds per grid round (PHDE_SSSP_LOCAL, none by default): each block keeps relaxing the
-  // vertices it improved below the band limit (up to SS_LQ of them) this many times before the grid
-  // barrier.  On a 256^3 grid four local rounds took 10-12.5 ms per pass on some runs and 43-50 ms on
-  // others (same inputs, band 1024; band 512 stayed near 13 ms), against 14.6 ms without: the blocks that
-  // run ahead inside the band relax with distances other blocks later lower, and how much of that is
-  // wasted depends on timing.  Off until that is bounded.
-  const char *le = getenv("PHDE_SSSP_LOCAL");
-  a.lmax = le ? std::max(0, atoi(le)) : 0;
+  a.lmax = lmax;
   a.qv0 = qv0;
   a.qv1 = qv1;
   a.qe0 = qe0;
@@ -461,7 +466,7 @@ int phde_run_sssp(phde_ctx *ctx, const int64_t *d_src, int32_t *d_col, int32_t d
   void *args[] = {&a};
   cudaEventRecord(ctx->kev[0], ctx->stream);
   PHDE_CK(ctx, cudaLaunchCooperativeKernel(kfn, dim3(ctx->nsm * per_sm),
-                                           dim3(SS_THREADS), args, 0, ctx->stream));
+                                           dim3(SS_THREADS), args, dyn, ctx->stream));
   PHDE_LAUNCHED(ctx);
   cudaEventRecord(ctx->kev[1], ctx->stream);
   ctx->kev_pending = true;
