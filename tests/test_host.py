@@ -100,6 +100,26 @@ def test_ctypes_mirrors_match_the_c_abi(tmp_path):
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
 
 
+@pytest.mark.parametrize("extra,algo", [(["--rmat-scale", "12"], "ParHDE"),
+                                        (["--graph", "grid3d", "--grid-l", "20"], "wParHDE")])
+def test_bench_reference_arm_contract(extra, algo):
+    """`bench.py --impl reference` (the reference algorithm on the host cores) prints one JSON line with the
+    contract's keys; the weighted configuration runs WParHDE."""
+    import json
+    r = subprocess.run(["python", os.path.join(ROOT, "bench.py"), "--impl", "reference", "--k", "8", "--c", "2",
+                        "--steps", "1", "--warmup", "0"] + extra, capture_output=True, text=True, timeout=300,
+                       cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["value"] > 0 and d["config"]["workload"].startswith(algo + " ")
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] in ("port", "reference")
+
+
 def test_status_strings_without_gpu():
     lib = ctypes.CDLL(pbuild.build())
     lib.phde_status_string.restype = ctypes.c_char_p
