@@ -622,7 +622,10 @@ def run_weighted(args):
                     "h2d_bytes_per_step": 4 * (n + 1) + 8 * nnz, "d2h_bytes_per_step": 8 * n * c,
                     "timing": "mean of %d host-timed calls: upload from pinned host CSR + layout + coordinates to "
                               "pinned host memory" % len(e2e_t), "ms_each": [round(x * 1e3, 1) for x in e2e_t]},
-            "gpu_launches": launches, "clocks": clk.summary()}
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "sssp": {"grid_rounds_per_layout": float(np.mean([st["sssp_rounds"] for st in stats])),
+                     "edges_relaxed_per_layout": float(np.mean([st["edges_examined"] for st in stats])),
+                     "passes_per_layout": float(np.mean([st["npasses"] for st in stats]))}}
     if not args.no_cpu_baseline:
         from oracle import oracle as orc
         gs = graphs.grid3d(64, seed=args.seed, weighted=True)
