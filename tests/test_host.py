@@ -204,6 +204,24 @@ def test_png_writer_round_trip(tmp_path):
     assert np.array_equal(pngdecode.read(path), img)
 
 
+def test_embed_driver_command_line_without_gpu(tmp_path):
+    """lib/embed keeps the reference's command line (spectralDrawing.cpp:67-115): no argument prints the
+    usage line, -h the option list, an unknown algorithm or strategy aborts with the reference's message,
+    and a missing input file is reported before any device work."""
+    pbuild.build()
+    r = subprocess.run([pbuild.EMBED_PATH], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Usage:" in r.stderr
+    r = subprocess.run([pbuild.EMBED_PATH, "x.csr", "-h"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "-r <value> : Number of pivots (default=10)" in r.stdout
+    r = subprocess.run([pbuild.EMBED_PATH, "x.csr", "-a", "Spring"], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "Unrecognized algorithm" in r.stderr
+    r = subprocess.run([pbuild.EMBED_PATH, "x.csr", "-p", "Median"], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "Unrecognized Strategy" in r.stderr
+    r = subprocess.run([pbuild.EMBED_PATH, str(tmp_path / "missing.csr")], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 1 and "Could not open input file" in r.stdout
+
+
 def test_draw_driver_usage_without_gpu():
     """lib/draw keeps the reference's command line: a wrong argument count prints the usage line and fails."""
     pbuild.build()
