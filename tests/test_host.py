@@ -222,6 +222,19 @@ def test_embed_driver_command_line_without_gpu(tmp_path):
     assert r.returncode == 1 and "Could not open input file" in r.stdout
 
 
+def test_mtx2csr_driver_command_line_without_gpu(tmp_path):
+    """lib/mtx2csr keeps the reference converter's command line: a wrong argument count prints the usage line,
+    an unreadable input is reported before any device work."""
+    pbuild.build()
+    exe = os.path.join(os.path.dirname(pbuild.EMBED_PATH), "mtx2csr")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Usage:" in r.stdout and "<MM filename> <binary CSR filename>" in r.stdout
+    r = subprocess.run([exe, str(tmp_path / "missing.mtx"), str(tmp_path / "out.csr")], capture_output=True,
+                       text=True, timeout=60)
+    assert r.returncode == 1 and "could not open input file" in r.stdout
+    assert not (tmp_path / "out.csr").exists()
+
+
 def test_draw_driver_usage_without_gpu():
     """lib/draw keeps the reference's command line: a wrong argument count prints the usage line and fails."""
     pbuild.build()
