@@ -18,7 +18,7 @@ STATUS = {
 NOALLOC_MAX_VERTICES = 1048576
 ALGOS = {"PivotMDS": 0, "PHDE": 1, "wParHDE": 2, "WParHDE": 2, "ParHDE": 3}
 STRATEGIES = {"RandCoarse": 0, "RandFine": 1, "Kcenters": 2, "Learned": 3}
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "exact": 2}
 EIGS = {"power": 0, "exact": 1}
 
 # every symbol include/parhde.h declares

@@ -329,6 +329,8 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   double *Y = (double *)phde_buf(ctx, "layout.Y", sizeof(double) * k * c);
   if (!d_src || !sumsq || !Sbuf || !M || !K || !ev || !Y) return PHDE_ERR_OOM;
   const bool mixed = o->precision == PHDE_PREC_MIXED;
+  bool exact = o->precision == PHDE_PREC_EXACT;  // cleared when the inputs are out of the exact path's range
+  ExactBasis eb;
   float *S32 = nullptr;
   if (mixed) {
     S32 = (float *)phde_buf(ctx, "layout.S32", sizeof(float) * n * k);
@@ -471,7 +473,13 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     if (hde) {
       int state[4] = {0, 0, 0, 0};
       std::vector<double> dlog(P);
-      if (mixed && !ctx->column_cgs2)
+      if (exact) {
+        rc = phde_exact_orth(ctx, D, P_used, k, &eb, state, dlog.data());
+        if (rc == PHDE_ERR_TOO_LARGE) {  // distances or degrees beyond the exact sums: the FP64 vector kernels
+          exact = false;
+          rc = phde_cgs(ctx, D, P_used, sumsq, deg, Sbuf, k, state, dlog.data());
+        }
+      } else if (mixed && !ctx->column_cgs2)
         rc = phde_bcgs2_mixed(ctx, D, P_used, sumsq, deg, S32, k, state, dlog.data());
       else if (mixed)
         rc = phde_cgs2_mixed(ctx, D, P_used, sumsq, deg, S32, k, state, dlog.data());
@@ -505,7 +513,11 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   }
 
   // ---- Laplacian SpMM + Gram (HDE) or C^T C (MDS) ----
-  if (hde && mixed) {
+  if (hde && exact) {
+    int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);
+    if (!D) return PHDE_ERR_OOM;
+    if ((rc = phde_exact_lap(ctx, D, k, &eb, M))) return rc;
+  } else if (hde && mixed) {
     float *LS32 = (float *)phde_buf(ctx, "layout.LS32", sizeof(float) * n * k);
     if (!LS32) return PHDE_ERR_OOM;
     if ((rc = phde_lap_spmm_mixed(ctx, deg, S32, LS32, k))) return rc;
@@ -526,7 +538,9 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   tm.mark(4);
   double *X = (double *)phde_buf(ctx, "layout.X", sizeof(double) * n * c);
   if (!X) return PHDE_ERR_OOM;
-  if (mixed)
+  if (exact)
+    rc = phde_exact_coords(ctx, Y, k, c, &eb, X);
+  else if (mixed)
     rc = phde_coords_mixed(ctx, S32, Y, k, c, X);
   else
     rc = phde_coords(ctx, Sbuf, Y, k, c, X, !hde);
@@ -544,6 +558,11 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   std::vector<double> Srow;
   std::vector<float> Srow32;
   if (extra && extra->basis) {
+    if (exact) {
+      int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);
+      if (!D) return PHDE_ERR_OOM;
+      if ((rc = phde_exact_basis(ctx, D, k, &eb, Sbuf))) return rc;
+    }
     if (mixed) {
       Srow32.resize((size_t)n * k);
       PHDE_CK(ctx, cudaMemcpyAsync(Srow32.data(), S32, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->stream));
@@ -589,7 +608,7 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, in
   if (o->strategy == PHDE_STRAT_LEARNED && o->algo != PHDE_ALGO_PARHDE)
     return phde_fail(ctx, PHDE_ERR_INVALID, "learned pivots are implemented for ParHDE");
   if (o->eig != PHDE_EIG_POWER && o->eig != PHDE_EIG_EXACT) return phde_fail(ctx, PHDE_ERR_INVALID, "unknown eigensolver");
-  if (o->precision != PHDE_PREC_FP64 && o->precision != PHDE_PREC_MIXED)
+  if (o->precision != PHDE_PREC_FP64 && o->precision != PHDE_PREC_MIXED && o->precision != PHDE_PREC_EXACT)
     return phde_fail(ctx, PHDE_ERR_INVALID, "unknown precision");
   if (o->k < 1 || o->k > PHDE_MAX_K || o->k >= ctx->n || o->c < 1 || o->c > o->k)
     return phde_fail(ctx, PHDE_ERR_K_RANGE, "need 1 <= k <= 256, k < n and 1 <= c <= k");
@@ -599,6 +618,8 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, in
     return phde_fail(ctx, PHDE_ERR_WEIGHTS, "ParHDE code doesn't requires the weighted edges");
   if (o->precision == PHDE_PREC_MIXED && o->algo != PHDE_ALGO_PARHDE)
     return phde_fail(ctx, PHDE_ERR_INVALID, "mixed precision is implemented for ParHDE; use PHDE_PREC_FP64");
+  if (o->precision == PHDE_PREC_EXACT && o->algo != PHDE_ALGO_PARHDE)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "the exact-Gram path is implemented for ParHDE; use PHDE_PREC_FP64");
   cudaSetDevice(ctx->device);
   int rc = layout_impl(ctx, o, coords_out, sources_out, extra, st);
   if (st) st->status = rc;

@@ -121,6 +121,22 @@ int phde_tc_gram64(phde_ctx *ctx, const float *A, int lda, int acols, const floa
 int phde_tc_gram32(phde_ctx *ctx, const float *A, int lda, int nq, int ones, const float *X, const double *w,
                    int64_t n, int ncta, int nqc, int self, float *part);
 
+// ---- exact-Gram dense stages (exact.cu, PHDE_PREC_EXACT) ----
+// The accepted basis as coefficients over the integer columns Z = [1, D columns]: S_q = Z A[q][*].
+struct ExactBasis {
+  double *A = nullptr;   // [k][ld]
+  int *acc_idx = nullptr;  // [k] Z index of each accepted column (D column + 1)
+  int ld = 0;
+  unsigned maxz = 0, maxdeg = 0;
+  void *Z = nullptr;     // accepted columns, row-major n x kp, uint8 (maxz <= 255) or uint16
+  bool z16 = false;
+  int kp = 0;
+};
+int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog);
+int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, double *M);
+int phde_exact_coords(phde_ctx *ctx, const double *Y, int k, int c, ExactBasis *eb, double *X);
+int phde_exact_basis(phde_ctx *ctx, const int32_t *D, int k, const ExactBasis *eb, double *S);
+
 // ---- drawing (draw.cu) ----
 // The last drawn image's 4-bit palette scanlines (H rows of 1 + ceil(W / 2) bytes) copied to the host.
 int phde_draw_scanlines(phde_ctx *ctx, std::vector<uint8_t> &out, unsigned &W, unsigned &H);

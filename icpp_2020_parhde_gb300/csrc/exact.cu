@@ -1,0 +1,934 @@
+// exact.cu -- ParHDE's dense stages from exact integer Gram matrices of the distance columns
+//             (PHDE_PREC_EXACT).
+//
+// The reference turns the integer BFS columns into FP64 vectors and works on those vectors: it normalises
+// them, D-orthogonalises them by classical Gram-Schmidt (ParHDE.cpp:176-285), forms LS = D S - A S
+// (ParHDE.cpp:288-300) and S^T LS (DrawingBase.cpp:221-244), and finally X = S Y (DrawingBase.cpp:207-219).
+// Every vector it builds is a linear combination of the integer columns Z = [1, d_1, ..., d_P] (1 = the
+// constant column before its 1/sqrt(n) scaling).  So S = Z A for a small coefficient matrix A, and every
+// n-sized product the reference needs is a small integer matrix of Z:
+//     <x, D q>, <q, D q>   from  G_D = Z^T D Z         ||x - sum c q||_2   from  G_I = Z^T Z
+//     S^T L S = A^T (Z_acc^T L Z_acc) A_acc            X = Z (A Y)
+// Here those integer matrices are formed EXACTLY (64-bit sums of integer products of distances and
+// degrees, order-free), and the reference's candidate loop -- the same coefficients, the same ||x|| < 1e-3
+// discard rule, the same acceptance order -- runs in FP64 on (P+1)-dimensional coefficient vectors.
+// GB300 issues FP64 at 1/64 of its FP32 rate; this path keeps FP64 out of every n-sized loop, and the
+// n-sized sums themselves carry no rounding at all.
+//
+//   zgram_kernel     G_I, G_D for a block of candidate columns (upper triangle, 4x4 register tiles,
+//                    32-bit partial sums flushed to 64-bit atomics under a per-row magnitude bound)
+//   coef_kernel      the candidate loop in coefficient space (one CTA, FP64)
+//   pack_kernel      the accepted columns as a row-major uint8 / uint16 matrix Z_acc (n x kp)
+//   lgram_kernel     Z_acc^T L Z_acc: per row (or heavy-row chunk) r = deg z_i - sum_j z_j gathered by a
+//                    warp (16-bit lanes packed two to a register for uint8 rows), then the outer product
+//                    z_i (x) r accumulated in register tiles -- the Laplacian product never reaches memory
+//   mgram_kernel     M = A_acc^T (Z_acc^T L Z_acc) A_acc (FP64, k x k)
+//   coords kernels   X = Z (A Y) in fixed point: A Y scaled to 62-bit integers per coordinate, exact
+//                    integer row sums, one rounding to FP64; then the unit-norm scaling of getCoordinates
+//                    (DrawingBase.cpp:196-205)
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ctx.h"
+
+namespace {
+
+constexpr int ZG_THREADS = 256;
+constexpr int ZG_ROWS = 32;   // rows per staged slab
+constexpr int LG_THREADS = 256;
+constexpr int LG_ITEMS = 64;  // rows / chunks per slab
+constexpr int CF_THREADS = 256;
+constexpr uint64_t B32 = 1ull << 32;
+constexpr uint64_t B31 = 1ull << 31;
+
+// Upper-triangle tile (pb, qb), pb <= qb, qb in [qb0, qb1): tiles are numbered qb-major.
+__device__ __forceinline__ void tile_of(int t, int qb0, int qb1, int &pb, int &qb) {
+  pb = -1;
+  qb = -1;
+  for (int b = qb0; b < qb1; b++) {
+    if (t <= b) {
+      pb = t;
+      qb = b;
+      return;
+    }
+    t -= b + 1;
+  }
+}
+
+__device__ __forceinline__ double gsym(const ull *G, int ld, int p, int q) {
+  return (double)(long long)(p <= q ? G[(int64_t)p * ld + q] : G[(int64_t)q * ld + p]);
+}
+
+// ------------------------------------------------------------------------------------------------
+// G_I = Z^T Z and G_D = Z^T D Z for the Z columns p in [0, c1), q in [c0, c1), p <= q.
+struct ZgArgs {
+  const int32_t *D;  // n x P column-major; Z column t >= 1 is D column t - 1, Z column 0 is all ones
+  const int64_t *off;
+  int64_t n;
+  int P;
+  int c0, c1;        // multiples of 4
+  int ntiles;        // tiles of the block, CTA y takes [y * ZG_THREADS, ...)
+  ull *GI, *GD;
+  int ld;
+  unsigned *maxz;    // [0] largest distance, [1] largest degree
+};
+
+__global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
+  extern __shared__ int zsm[];  // [ZG_ROWS][S]
+  __shared__ unsigned s_deg[ZG_ROWS];
+  __shared__ ull red[32];
+  const int S = a.c1 + 4;
+  const int t = blockIdx.y * ZG_THREADS + threadIdx.x;
+  int pb, qb;
+  tile_of(t, a.c0 / 4, a.c1 / 4, pb, qb);
+  const bool active = t < a.ntiles && pb >= 0;
+  uint32_t aI[4][4], aD[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) aI[i][j] = aD[i][j] = 0;
+  auto flush = [&]() {
+    if (!active) return;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int p = 4 * pb + i, q = 4 * qb + j;
+        if (p <= q && q < a.c1) {
+          if (aI[i][j]) atomicAdd(a.GI + (int64_t)p * a.ld + q, (ull)aI[i][j]);
+          if (aD[i][j]) atomicAdd(a.GD + (int64_t)p * a.ld + q, (ull)aD[i][j]);
+        }
+        aI[i][j] = aD[i][j] = 0;
+      }
+  };
+  const int64_t per = ((a.n + gridDim.x - 1) / gridDim.x + ZG_ROWS - 1) / ZG_ROWS * ZG_ROWS;
+  const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(a.n, r0 + per);
+  ull run = 0;  // bound on every partial sum since the last flush (uniform across the block)
+  for (int64_t i0 = r0; i0 < r1; i0 += ZG_ROWS) {
+    const int rows = (int)min((int64_t)ZG_ROWS, r1 - i0);
+    __syncthreads();  // previous slab consumed
+    unsigned mz = 0, md = 0;
+    for (int e = threadIdx.x; e < ZG_ROWS * a.c1; e += ZG_THREADS) {
+      const int col = e / ZG_ROWS, r = e - col * ZG_ROWS;
+      int v = 0;
+      if (r < rows) v = col == 0 ? 1 : (col - 1 < a.P ? a.D[(int64_t)(col - 1) * a.n + i0 + r] : 0);
+      zsm[r * S + col] = v;
+      mz = max(mz, (unsigned)v);
+    }
+    if (threadIdx.x < ZG_ROWS) {
+      const int r = threadIdx.x;
+      const unsigned d = r < rows ? (unsigned)(a.off[i0 + r + 1] - a.off[i0 + r]) : 0u;
+      s_deg[r] = d;
+      md = d;
+    }
+    const ull mzs = block_max_u64((ull)mz, red);
+    const ull mds = block_max_u64((ull)md, red);
+    if (threadIdx.x == 0) {
+      atomicMax(a.maxz, (unsigned)mzs);
+      atomicMax(a.maxz + 1, (unsigned)mds);
+    }
+    const ull mz2 = mzs * mzs;
+    for (int r = 0; r < rows; r++) {
+      const unsigned d = s_deg[r];
+      const ull b = (ull)max(d, 1u) * mz2;  // every product of this row is at most b
+      const int *zr = zsm + r * S;
+      if (b >= B32) {  // a row whose products may not fit 32 bits: 64-bit atomics directly (rare hubs)
+        if (active) {
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int p = 4 * pb + i, q = 4 * qb + j;
+              if (p <= q && q < a.c1) {
+                const ull zz = (ull)(unsigned)zr[p] * (ull)(unsigned)zr[q];
+                if (zz) {
+                  atomicAdd(a.GI + (int64_t)p * a.ld + q, zz);
+                  atomicAdd(a.GD + (int64_t)p * a.ld + q, zz * d);
+                }
+              }
+            }
+        }
+        continue;
+      }
+      if (run + b >= B32) {
+        flush();
+        run = 0;
+      }
+      run += b;
+      if (active) {
+        const int4 zp = *(const int4 *)(zr + 4 * pb);
+        const int4 zq = *(const int4 *)(zr + 4 * qb);
+        const uint32_t p4[4] = {(uint32_t)zp.x, (uint32_t)zp.y, (uint32_t)zp.z, (uint32_t)zp.w};
+        const uint32_t q4[4] = {(uint32_t)zq.x, (uint32_t)zq.y, (uint32_t)zq.z, (uint32_t)zq.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint32_t y = p4[i] * d;
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            aI[i][j] += p4[i] * q4[j];
+            aD[i][j] += y * q4[j];
+          }
+        }
+      }
+    }
+  }
+  flush();
+}
+
+// ------------------------------------------------------------------------------------------------
+// The reference's candidate loop (ParHDE.cpp:190-285) on coefficient vectors over Z.  Accepted vector q
+// is S_q = Z A[q][*] (A[q][i] = 0 for i > acc_idx[q]); the candidate with Z index r is x = d_r / ||d_r||,
+// i.e. the vector inv * e_r with inv = 1 / sqrt(G_I[r][r]).  Per candidate:
+//   num_q = <x, D S_q> = inv * sum_i G_D[r][i] A[q][i],   den_q = <S_q, D S_q> (kept from acceptance)
+//   c_q = num_q * (1 / den_q); the constant column u0 = e_0 / sqrt(n) likewise
+//   t = inv e_r - sum c_q A[q] - c_0 e_0 / sqrt(n),   ||x - sum c q||^2 = t^T G_I t
+//   discard when the norm is below 1e-3, else A[nacc] = t * (1 / norm).
+struct CoefArgs {
+  const ull *GI, *GD;
+  int ld;
+  int64_t n;
+  int r_end;      // examine Z indices [state[3], r_end)
+  int k;
+  double *A;      // [k][ld]
+  double *den;    // [k]
+  int *acc_idx;   // [k]
+  int *state;     // [0] accepted, [1] discarded, [2] examined, [3] next Z index
+  double *dlog;   // [P]: norm of each discarded candidate (by candidate index = Z index - 1); NaN otherwise
+};
+
+__global__ void __launch_bounds__(CF_THREADS) coef_kernel(CoefArgs a) {
+  extern __shared__ double cs[];  // rr[ld], gdr[ld], cq[k]
+  __shared__ double red[32];
+  __shared__ int s_idx[PHDE_MAX_K];
+  double *rr = cs, *gdr = cs + a.ld, *cq = cs + 2 * a.ld;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = CF_THREADS / 32;
+  int nacc = a.state[0], ndisc = a.state[1], nexam = a.state[2];
+  for (int q = threadIdx.x; q < nacc; q += CF_THREADS) s_idx[q] = a.acc_idx[q];
+  const double rsn = 1.0 / sqrt((double)a.n);
+  const double den0 = gsym(a.GD, a.ld, 0, 0) * rsn * rsn;  // <u0, D u0> = nnz / n
+  int r = a.state[3];
+  for (; r < a.r_end && nacc < a.k; r++) {
+    __syncthreads();
+    for (int i = threadIdx.x; i <= r; i += CF_THREADS) gdr[i] = gsym(a.GD, a.ld, i, r);
+    const double inv = 1.0 / sqrt(gsym(a.GI, a.ld, r, r));
+    __syncthreads();
+    for (int q = warp; q < nacc; q += nw) {
+      const int top = s_idx[q];
+      const double *Aq = a.A + (int64_t)q * a.ld;
+      double s = 0;
+      for (int i = lane; i <= top; i += 32) s = fma(gdr[i], Aq[i], s);
+      s = warp_sum(s);
+      if (lane == 0) cq[q] = (inv * s) * (1.0 / a.den[q]);
+    }
+    const double c0 = (inv * gdr[0] * rsn) * (1.0 / den0);
+    __syncthreads();
+    for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
+      double v = i == r ? inv : 0.0;
+      if (i == 0) v -= c0 * rsn;
+      for (int q = 0; q < nacc; q++)
+        if (s_idx[q] >= i) v -= cq[q] * a.A[(int64_t)q * a.ld + i];
+      rr[i] = v;
+    }
+    __syncthreads();
+    double s = 0;
+    for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
+      double ti = 0;
+      for (int j = 0; j <= r; j++) ti = fma(gsym(a.GI, a.ld, i, j), rr[j], ti);
+      s = fma(rr[i], ti, s);
+    }
+    const double nrm = sqrt(fmax(block_sum(s, red), 0.0));
+    nexam++;
+    if (nrm < 0.001) {
+      if (threadIdx.x == 0) a.dlog[r - 1] = nrm;
+      ndisc++;
+      continue;
+    }
+    const double sc = 1.0 / nrm;
+    double *An = a.A + (int64_t)nacc * a.ld;
+    for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
+      const double v = rr[i] * sc;
+      rr[i] = v;
+      An[i] = v;
+    }
+    __syncthreads();
+    double dsum = 0;
+    for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
+      double ti = 0;
+      for (int j = 0; j <= r; j++) ti = fma(gsym(a.GD, a.ld, i, j), rr[j], ti);
+      dsum = fma(rr[i], ti, dsum);
+    }
+    dsum = block_sum(dsum, red);
+    if (threadIdx.x == 0) {
+      a.den[nacc] = dsum;
+      a.acc_idx[nacc] = r;
+    }
+    s_idx[nacc] = r;  // every thread writes the same value
+    nacc++;
+  }
+  if (threadIdx.x == 0) {
+    a.state[0] = nacc;
+    a.state[1] = ndisc;
+    a.state[2] = nexam;
+    a.state[3] = r;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Z_acc[i][t] = D[acc_idx[t] - 1][i] for t < k, 0 for k <= t < kp; 16 bytes per store.
+template <typename T>
+__global__ void pack_kernel(const int32_t *D, int64_t n, const int *acc_idx, int k, int kp, T *Z) {
+  __shared__ int s_col[PHDE_MAX_K];
+  for (int t = threadIdx.x; t < kp; t += blockDim.x) s_col[t] = t < k ? acc_idx[t] - 1 : -1;
+  __syncthreads();
+  constexpr int V = 16 / sizeof(T);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int t0 = 0; t0 < kp; t0 += V) {
+      union {
+        uint4 u;
+        T v[V];
+      } w;
+#pragma unroll
+      for (int j = 0; j < V; j++) {
+        const int col = s_col[t0 + j];
+        w.v[j] = col >= 0 ? (T)D[(int64_t)col * n + i] : (T)0;
+      }
+      *(uint4 *)(Z + i * kp + t0) = w.u;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Z_acc^T L Z_acc.  Items: rows 0..n-1 (rows of degree > heavy contribute nothing as rows) and the
+// heavy rows' chunks of at most `chunk` (<= 256) edges.  Item u of row i has z = Z_acc[i] and
+// r = (deg_i z if the item holds the row's diagonal term) - sum over its edges of Z_acc[j]; the items'
+// z (x) r sum to Z^T (D Z - A Z) = Z^T L Z.
+template <typename T, int CPL>
+struct RowLoad;  // lane l's CPL columns of a row: l*CPL .. l*CPL+CPL-1
+template <>
+struct RowLoad<uint8_t, 2> {
+  typedef uint16_t V;
+};
+template <>
+struct RowLoad<uint8_t, 4> {
+  typedef uint32_t V;
+};
+template <>
+struct RowLoad<uint8_t, 8> {
+  typedef uint2 V;
+};
+template <>
+struct RowLoad<uint16_t, 2> {
+  typedef uint32_t V;
+};
+template <>
+struct RowLoad<uint16_t, 4> {
+  typedef uint2 V;
+};
+template <>
+struct RowLoad<uint16_t, 8> {
+  typedef uint4 V;
+};
+
+// the 32-bit words of a loaded vector (a 16-bit load is zero-extended into one word)
+__device__ __forceinline__ void words_of(const uint16_t &v, uint32_t (&w)[1]) { w[0] = v; }
+__device__ __forceinline__ void words_of(const uint32_t &v, uint32_t (&w)[1]) { w[0] = v; }
+__device__ __forceinline__ void words_of(const uint2 &v, uint32_t (&w)[2]) {
+  w[0] = v.x;
+  w[1] = v.y;
+}
+__device__ __forceinline__ void words_of(const uint4 &v, uint32_t (&w)[4]) {
+  w[0] = v.x;
+  w[1] = v.y;
+  w[2] = v.z;
+  w[3] = v.w;
+}
+template <typename T, int CPL>
+struct NWords {
+  static constexpr int value = (CPL * (int)sizeof(T) + 3) / 4;
+};
+
+// unpack a loaded vector into CPL ints
+template <typename T, int CPL>
+__device__ __forceinline__ void unpack(const typename RowLoad<T, CPL>::V &v, int (&o)[CPL]) {
+  uint32_t w[NWords<T, CPL>::value];
+  words_of(v, w);
+  if (sizeof(T) == 1) {
+#pragma unroll
+    for (int c = 0; c < CPL; c++) o[c] = (int)((w[c / 4] >> (8 * (c % 4))) & 0xffu);
+  } else {
+#pragma unroll
+    for (int c = 0; c < CPL; c++) o[c] = (int)((w[c / 2] >> (16 * (c % 2))) & 0xffffu);
+  }
+}
+
+// neighbour sums: for uint8 rows two columns share a 32-bit register as 16-bit halves (bytes moved apart
+// by one byte permute; at most 256 neighbours of at most 255 keep each half below 2^16, so plain adds never
+// carry across); uint16 rows sum each column in its own register
+template <typename T, int CPL>
+struct NbSum {
+  static constexpr int NW = sizeof(T) == 1 ? CPL / 2 : CPL;
+  uint32_t s[NW];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < NW; i++) s[i] = 0;
+  }
+  __device__ __forceinline__ void add(const typename RowLoad<T, CPL>::V &v) {
+    uint32_t w[NWords<T, CPL>::value];
+    words_of(v, w);
+    if (sizeof(T) == 1) {
+#pragma unroll
+      for (int i = 0; i < NW; i++) s[i] += __byte_perm(w[i / 2], 0u, (i % 2) ? 0x4342 : 0x4140);
+    } else {
+#pragma unroll
+      for (int i = 0; i < NW; i++) s[i] += (w[i / 2] >> (16 * (i % 2))) & 0xffffu;
+    }
+  }
+  __device__ __forceinline__ int get(int c) const {
+    if (sizeof(T) == 1) return (int)((s[c / 2] >> (16 * (c % 2))) & 0xffffu);
+    return (int)s[c];
+  }
+};
+
+struct LgArgs {
+  const int64_t *off;
+  const uint32_t *adj;
+  int64_t n;
+  const void *Z;  // row-major n x kp
+  int kp;
+  int64_t heavy;  // rows of degree > heavy are done as chunks
+  const int64_t *chunk_row, *chunk_e0;
+  int64_t nchunks, chunk;
+  ull *GL;        // [kp x kp], p <= q at p * kp + q, two's complement
+  int ntiles;
+};
+
+template <typename T, int CPL, int TS>
+__global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
+  typedef typename RowLoad<T, CPL>::V V;
+  extern __shared__ int lsm[];  // zs[LG_ITEMS][SL], rs[LG_ITEMS][SL]
+  __shared__ ull s_bnd[LG_ITEMS];
+  const int kp = a.kp, SL = kp + 4;
+  int *zs = lsm, *rs = lsm + LG_ITEMS * SL;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = LG_THREADS / 32;
+  const T *Z = (const T *)a.Z;
+  const int t = blockIdx.y * LG_THREADS + threadIdx.x;
+  int pb, qb;
+  tile_of(t, 0, kp / TS, pb, qb);
+  const bool active = t < a.ntiles && pb >= 0;
+  int acc[TS][TS];
+#pragma unroll
+  for (int i = 0; i < TS; i++)
+#pragma unroll
+    for (int j = 0; j < TS; j++) acc[i][j] = 0;
+  auto flush = [&]() {
+    if (!active) return;
+#pragma unroll
+    for (int i = 0; i < TS; i++)
+#pragma unroll
+      for (int j = 0; j < TS; j++) {
+        const int p = TS * pb + i, q = TS * qb + j;
+        if (p <= q && acc[i][j]) atomicAdd(a.GL + (int64_t)p * kp + q, (ull)(long long)acc[i][j]);
+        acc[i][j] = 0;
+      }
+  };
+  const int64_t items = a.n + a.nchunks;
+  const int64_t nslab = (items + LG_ITEMS - 1) / LG_ITEMS;
+  ull run = 0;
+  for (int64_t s = blockIdx.x; s < nslab; s += gridDim.x) {
+    const int64_t u0 = s * LG_ITEMS;
+    __syncthreads();  // previous slab consumed
+    for (int slot = warp; slot < LG_ITEMS; slot += nw) {
+      const int64_t u = u0 + slot;
+      int64_t row = -1, e0 = 0, e1 = 0;
+      bool diag = false;
+      if (u < a.n) {
+        e0 = a.off[u];
+        e1 = a.off[u + 1];
+        if (e1 - e0 <= a.heavy) {
+          row = u;
+          diag = true;
+        }
+      } else if (u < items) {
+        const int64_t c = u - a.n;
+        row = a.chunk_row[c];
+        e0 = a.chunk_e0[c];
+        const int64_t re0 = a.off[row], re1 = a.off[row + 1];
+        e1 = min(e0 + a.chunk, re1);
+        diag = e0 == re0;
+      }
+      int zi[CPL], r[CPL];
+      if (row >= 0) {
+        const V own = *(const V *)(Z + row * kp + lane * CPL);
+        unpack<T, CPL>(own, zi);
+        NbSum<T, CPL> nb;
+        nb.zero();
+        int64_t e = e0;
+        for (; e + 4 <= e1; e += 4) {
+          const int64_t v0 = __ldg(a.adj + e), v1 = __ldg(a.adj + e + 1), v2 = __ldg(a.adj + e + 2),
+                        v3 = __ldg(a.adj + e + 3);
+          const V x0 = *(const V *)(Z + v0 * kp + lane * CPL), x1 = *(const V *)(Z + v1 * kp + lane * CPL);
+          const V x2 = *(const V *)(Z + v2 * kp + lane * CPL), x3 = *(const V *)(Z + v3 * kp + lane * CPL);
+          nb.add(x0);
+          nb.add(x1);
+          nb.add(x2);
+          nb.add(x3);
+        }
+        for (; e < e1; e++) {
+          const int64_t v = __ldg(a.adj + e);
+          nb.add(*(const V *)(Z + v * kp + lane * CPL));
+        }
+        const int deg = diag ? (int)(a.off[row + 1] - a.off[row]) : 0;
+#pragma unroll
+        for (int c = 0; c < CPL; c++) r[c] = deg * zi[c] - nb.get(c);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPL; c++) zi[c] = r[c] = 0;
+      }
+      unsigned zm = 0, rm = 0;
+#pragma unroll
+      for (int c = 0; c < CPL; c++) {
+        zs[slot * SL + lane * CPL + c] = zi[c];
+        rs[slot * SL + lane * CPL + c] = r[c];
+        zm = max(zm, (unsigned)zi[c]);
+        rm = max(rm, (unsigned)abs(r[c]));
+      }
+      zm = __reduce_max_sync(PHDE_FULL_MASK, zm);
+      rm = __reduce_max_sync(PHDE_FULL_MASK, rm);
+      if (lane == 0) s_bnd[slot] = (ull)zm * (ull)rm;
+    }
+    __syncthreads();
+    const int nit = (int)min((int64_t)LG_ITEMS, items - u0);
+    for (int slot = 0; slot < nit; slot++) {
+      const ull b = s_bnd[slot];
+      if (b == 0) continue;
+      const int *zr = zs + slot * SL, *rr = rs + slot * SL;
+      if (b >= B31) {  // products of this item may not fit 32 bits: 64-bit atomics directly
+        if (active) {
+#pragma unroll
+          for (int i = 0; i < TS; i++)
+#pragma unroll
+            for (int j = 0; j < TS; j++) {
+              const int p = TS * pb + i, q = TS * qb + j;
+              const long long v = (long long)zr[p] * (long long)rr[q];
+              if (p <= q && v) atomicAdd(a.GL + (int64_t)p * kp + q, (ull)v);
+            }
+        }
+        continue;
+      }
+      if (run + b >= B31) {
+        flush();
+        run = 0;
+      }
+      run += b;
+      if (active) {
+        int zp[TS], rq[TS];
+#pragma unroll
+        for (int i = 0; i < TS; i += 4) {
+          const int4 x = *(const int4 *)(zr + TS * pb + i);
+          const int4 y = *(const int4 *)(rr + TS * qb + i);
+          zp[i] = x.x, zp[i + 1] = x.y, zp[i + 2] = x.z, zp[i + 3] = x.w;
+          rq[i] = y.x, rq[i + 1] = y.y, rq[i + 2] = y.z, rq[i + 3] = y.w;
+        }
+#pragma unroll
+        for (int i = 0; i < TS; i++)
+#pragma unroll
+          for (int j = 0; j < TS; j++) acc[i][j] += zp[i] * rq[j];
+      }
+    }
+  }
+  flush();
+}
+
+// ------------------------------------------------------------------------------------------------
+// M = A_acc^T G_L A_acc, A_acc[t][q] = A[q][acc_idx[t]] (zero for t > q).  CTA q forms B = G_L A_acc[:, q]
+// and the entries M[p][q] = M[q][p], p <= q (each written once: M is exactly symmetric).
+__global__ void __launch_bounds__(256) mgram_kernel(const ull *GL, int kp, const double *A, int ld, const int *acc_idx,
+                                                     int k, double *M) {
+  __shared__ double aq[PHDE_MAX_K], bq[PHDE_MAX_K];
+  __shared__ int idx[PHDE_MAX_K];
+  const int q = blockIdx.x;
+  for (int t = threadIdx.x; t < k; t += blockDim.x) {
+    idx[t] = acc_idx[t];
+    aq[t] = A[(int64_t)q * ld + acc_idx[t]];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < k; t += blockDim.x) {
+    double s = 0;
+    for (int u = 0; u <= q; u++) s = fma(gsym(GL, kp, t, u), aq[u], s);
+    bq[t] = s;
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p <= q; p += blockDim.x) {
+    const double *Ap = A + (int64_t)p * ld;
+    double s = 0;
+    for (int t = 0; t <= p; t++) s = fma(Ap[idx[t]], bq[t], s);
+    M[p + (int64_t)q * k] = s;
+    M[q + (int64_t)p * k] = s;
+  }
+}
+
+// S (row-major n x k) = Z A^T restricted to the accepted columns, for callers that ask for the basis.
+__global__ void basis_kernel(const int32_t *D, int64_t n, const double *A, int ld, const int *acc_idx, int k,
+                             double *S) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / k;
+    const int q = (int)(e - i * k);
+    const double *Aq = A + (int64_t)q * ld;
+    double s = Aq[0];
+    for (int t = 0; t <= q; t++) s = fma(Aq[acc_idx[t]], (double)D[(int64_t)(acc_idx[t] - 1) * n + i], s);
+    S[e] = s;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Coordinates X = Z W, W = A Y (W[0] on the constant column, W[1 + t] on accepted column t).  Per
+// coordinate, W is scaled by 2^s to 62-bit integers (s the largest with |W_0| + maxz sum |W_t| < 2^61 / 2^s),
+// stored as signed high and unsigned low 32-bit words; a row's sum is then exact in 64-bit integers and
+// rounded once to FP64.  The scaling error is below 2^-62 of the row's largest possible magnitude.
+__global__ void coords_prep_kernel(const double *A, int ld, const int *acc_idx, int k, const double *Y, int c,
+                                   unsigned maxz, int kp, int32_t *whi, uint32_t *wlo, long long *w0fix,
+                                   double *sinv) {
+  __shared__ double W[PHDE_MAX_K + 1];
+  __shared__ double red[32];
+  for (int j = 0; j < c; j++) {
+    __syncthreads();
+    for (int t = threadIdx.x; t <= k; t += blockDim.x) {
+      // t == 0: the constant column; t >= 1: accepted column t - 1
+      double s = 0;
+      for (int q = 0; q < k; q++) {
+        const double aqt = t == 0 ? A[(int64_t)q * ld] : (q >= t - 1 ? A[(int64_t)q * ld + acc_idx[t - 1]] : 0.0);
+        s = fma(aqt, Y[q + (int64_t)j * k], s);
+      }
+      W[t] = s;
+    }
+    __syncthreads();
+    double b = 0;
+    for (int t = threadIdx.x; t <= k; t += blockDim.x) b += fabs(W[t]) * (t == 0 ? 1.0 : (double)maxz);
+    b = block_sum(b, red);
+    int e = 0;
+    frexp(b, &e);  // b < 2^e
+    const int sh = b > 0 ? 61 - e : 0;
+    for (int t = threadIdx.x; t < kp + 1; t += blockDim.x) {
+      const long long f = t <= k ? llrint(ldexp(W[t], sh)) : 0ll;
+      if (t == 0) {
+        w0fix[j] = f;
+      } else {
+        whi[(int64_t)j * kp + t - 1] = (int32_t)(f >> 32);
+        wlo[(int64_t)j * kp + t - 1] = (uint32_t)(f & 0xffffffffll);
+      }
+    }
+    if (threadIdx.x == 0) sinv[j] = ldexp(1.0, -sh);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) coords_fix_kernel(const T *Z, int64_t n, int kp, int c, const int32_t *whi,
+                                                         const uint32_t *wlo, const long long *w0fix,
+                                                         const double *sinv, double *X, double *part) {
+  extern __shared__ uint32_t wsm[];  // per coordinate: hi[kp], lo[kp]
+  __shared__ double red[32];
+  for (int e = threadIdx.x; e < c * kp; e += blockDim.x) {
+    wsm[2 * e] = (uint32_t)whi[e];
+    wsm[2 * e + 1] = wlo[e];
+  }
+  __syncthreads();
+  constexpr int V = 16 / sizeof(T);
+  double ss[4] = {0, 0, 0, 0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int j0 = 0; j0 < c; j0 += 4) {
+      long long hi[4];
+      ull lo[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        hi[j] = 0;
+        lo[j] = 0;
+      }
+      for (int t0 = 0; t0 < kp; t0 += V) {
+        union {
+          uint4 u;
+          T v[V];
+        } w;
+        w.u = *(const uint4 *)(Z + i * kp + t0);
+#pragma unroll
+        for (int x = 0; x < V; x++) {
+          const uint32_t z = (uint32_t)w.v[x];
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            if (j0 + j < c) {
+              const uint32_t *wp = wsm + 2 * ((int64_t)(j0 + j) * kp + t0 + x);
+              hi[j] += (long long)(int32_t)wp[0] * (long long)z;
+              lo[j] += (ull)wp[1] * (ull)z;
+            }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (j0 + j < c) {
+          const long long tot = (long long)((ull)hi[j] << 32) + (long long)lo[j] + w0fix[j0 + j];
+          const double x = (double)tot * sinv[j0 + j];
+          X[i + (int64_t)(j0 + j) * n] = x;
+          if (j0 + j < 4) ss[j] = fma(x, x, ss[j]);
+        }
+    }
+  }
+  // column sums of squares for the first four coordinates here; more coordinates use norm_part_kernel
+  for (int j = 0; j < 4 && j < c; j++) {
+    const double tot = block_sum(ss[j], red);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * c + j] = tot;
+  }
+}
+
+__global__ void norm_part_kernel(const double *X, int64_t n, int c, int j0, double *part) {
+  __shared__ double red[32];
+  for (int j = j0; j < c; j++) {
+    double s = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+      s = fma(X[i + (int64_t)j * n], X[i + (int64_t)j * n], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * c + j] = s;
+  }
+}
+
+// X[:, j] *= 1 / ||X[:, j]|| (getCoordinates, DrawingBase.cpp:196-205): each block sums the per-block
+// partials itself in a fixed order, then scales its share.
+__global__ void unit_scale_kernel(double *X, int64_t n, int c, const double *part, int nparts) {
+  __shared__ double inv[PHDE_MAX_K];
+  __shared__ double red[32];
+  for (int j = 0; j < c; j++) {
+    double s = 0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += part[(int64_t)b * c + j];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) inv[j] = 1.0 / sqrt(s);
+  }
+  __syncthreads();
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * c; e += (int64_t)gridDim.x * blockDim.x)
+    X[e] = X[e] * inv[e / n];
+}
+
+int grid_n(phde_ctx *ctx, int64_t work, int threads, int per_sm) {
+  int64_t b = (work + threads - 1) / threads;
+  b = std::min<int64_t>(b, (int64_t)ctx->nsm * per_sm);
+  return (int)std::max<int64_t>(b, 1);
+}
+
+}  // namespace
+
+// ==================================================================================================
+// host side
+
+// G_I, G_D for Z columns p < c1, q in [c0, c1).
+static int exact_zgram(phde_ctx *ctx, const int32_t *D, int P, int c0, int c1, ull *GI, ull *GD, int ld,
+                       unsigned *maxz) {
+  const int nq = (c1 - c0) / 4;
+  const int ntiles = nq * (c0 / 4) + nq * (nq + 1) / 2;
+  const int gy = (ntiles + ZG_THREADS - 1) / ZG_THREADS;
+  const size_t smem = sizeof(int) * ZG_ROWS * (size_t)(c1 + 4);
+  PHDE_CK(ctx, cudaFuncSetAttribute(zgram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zgram_kernel, ZG_THREADS, smem));
+  per_sm = std::max(1, std::min(per_sm, 4));
+  const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm / gy + 1,
+                                                              (ctx->n + ZG_ROWS - 1) / ZG_ROWS));
+  ZgArgs a;
+  a.D = D;
+  a.off = ctx->d_off;
+  a.n = ctx->n;
+  a.P = P;
+  a.c0 = c0;
+  a.c1 = c1;
+  a.ntiles = ntiles;
+  a.GI = GI;
+  a.GD = GD;
+  a.ld = ld;
+  a.maxz = maxz;
+  zgram_kernel<<<dim3(gx, gy), ZG_THREADS, smem, ctx->stream>>>(a);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// The D-orthogonalisation of the P candidate columns of D (ParHDE.cpp:190-285) in coefficient space.
+// Candidates go in blocks: the first block holds k + max(4, k/8) of them (discards are rare), later blocks
+// 16; each block adds its rows and columns to G_I and G_D and runs the candidate loop until k are accepted.
+// h_state: accepted, discarded, examined; h_dlog[i]: norm of discarded candidate i (NaN otherwise).
+// Returns PHDE_ERR_TOO_LARGE when the distances or degrees are too large for exact 64-bit sums that
+// convert exactly to FP64 (the caller then takes the FP64 vector path).
+int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog) {
+  const int64_t n = ctx->n;
+  const int ld = ((P + 1) + 3) / 4 * 4;
+  ull *GI = (ull *)phde_buf(ctx, "ex.GI", sizeof(ull) * ld * ld);
+  ull *GD = (ull *)phde_buf(ctx, "ex.GD", sizeof(ull) * ld * ld);
+  double *A = (double *)phde_buf(ctx, "ex.A", sizeof(double) * (size_t)k * ld);
+  double *den = (double *)phde_buf(ctx, "ex.den", sizeof(double) * k);
+  int *acc_idx = (int *)phde_buf(ctx, "ex.acc", sizeof(int) * k);
+  int *state = (int *)phde_buf(ctx, "ex.state", sizeof(int) * 4);
+  unsigned *maxz = (unsigned *)phde_buf(ctx, "ex.maxz", sizeof(unsigned) * 2);
+  double *dlog = (double *)phde_buf(ctx, "ex.dlog", sizeof(double) * P);
+  if (!GI || !GD || !A || !den || !acc_idx || !state || !maxz || !dlog) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(GI, 0, sizeof(ull) * ld * ld, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(GD, 0, sizeof(ull) * ld * ld, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(A, 0, sizeof(double) * (size_t)k * ld, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(dlog, 0xff, sizeof(double) * P, ctx->stream));  // NaN: not discarded
+  PHDE_CK(ctx, cudaMemsetAsync(maxz, 0, sizeof(unsigned) * 2, ctx->stream));
+  const int st0[4] = {0, 0, 0, 1};
+  PHDE_CK(ctx, cudaMemcpyAsync(state, st0, sizeof(st0), cudaMemcpyHostToDevice, ctx->stream));
+  const size_t csmem = sizeof(double) * (2 * (size_t)ld + k);
+  PHDE_CK(ctx, cudaFuncSetAttribute(coef_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)std::max<size_t>(csmem, 48 * 1024)));
+  int c0 = 0, c1 = std::min(ld, (1 + std::min(P, k + std::max(4, k / 8)) + 3) / 4 * 4);
+  int hs[4] = {0, 0, 0, 1};
+  unsigned hm[2] = {0, 0};
+  for (;;) {
+    int rc = exact_zgram(ctx, D, P, c0, c1, GI, GD, ld, maxz);
+    if (rc) return rc;
+    PHDE_CK(ctx, cudaMemcpyAsync(hm, maxz, sizeof(hm), cudaMemcpyDeviceToHost, ctx->stream));
+    PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    // G_I, G_D, Z^T L Z entries are at most nnz * maxz^2 (and n * maxz^2): exact in FP64 below 2^53; the
+    // Laplacian rows r = deg z - sum z stay in 32 bits; distances fit 16 bits
+    const double mz = (double)hm[0];
+    if (hm[0] > 65535u || (double)std::max<int64_t>(ctx->nnz, n) * mz * mz >= 9007199254740992.0 ||
+        (double)hm[1] * mz >= 2147483647.0)
+      return phde_fail(ctx, PHDE_ERR_TOO_LARGE, "exact path: distances or degrees too large");
+    CoefArgs ca;
+    ca.GI = GI;
+    ca.GD = GD;
+    ca.ld = ld;
+    ca.n = n;
+    ca.r_end = std::min(c1, P + 1);
+    ca.k = k;
+    ca.A = A;
+    ca.den = den;
+    ca.acc_idx = acc_idx;
+    ca.state = state;
+    ca.dlog = dlog;
+    coef_kernel<<<1, CF_THREADS, csmem, ctx->stream>>>(ca);
+    PHDE_LAUNCHED(ctx);
+    PHDE_CK(ctx, cudaMemcpyAsync(hs, state, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+    PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hs[0] >= k || c1 >= P + 1) break;
+    c0 = c1;
+    c1 = std::min(ld, c1 + 16);
+  }
+  h_state[0] = hs[0];
+  h_state[1] = hs[1];
+  h_state[2] = hs[2];
+  PHDE_CK(ctx, cudaMemcpyAsync(h_dlog, dlog, sizeof(double) * P, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  eb->A = A;
+  eb->acc_idx = acc_idx;
+  eb->ld = ld;
+  eb->maxz = hm[0];
+  eb->maxdeg = hm[1];
+  eb->Z = nullptr;
+  return PHDE_OK;
+}
+
+// Pack the accepted columns, form Z_acc^T L Z_acc exactly and M = A_acc^T (Z_acc^T L Z_acc) A_acc.
+int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, double *M) {
+  const int64_t n = ctx->n;
+  const bool z16 = eb->maxz > 255u;
+  const int kp = k <= 64 ? 64 : k <= 128 ? 128 : 256;
+  void *Z = phde_buf(ctx, "ex.Z", (size_t)n * kp * (z16 ? 2 : 1));
+  ull *GL = (ull *)phde_buf(ctx, "ex.GL", sizeof(ull) * kp * kp);
+  if (!Z || !GL) return PHDE_ERR_OOM;
+  const int gp = grid_n(ctx, n, 256, 8);
+  if (z16)
+    pack_kernel<uint16_t><<<gp, 256, 0, ctx->stream>>>(D, n, eb->acc_idx, k, kp, (uint16_t *)Z);
+  else
+    pack_kernel<uint8_t><<<gp, 256, 0, ctx->stream>>>(D, n, eb->acc_idx, k, kp, (uint8_t *)Z);
+  PHDE_LAUNCHED(ctx);
+  eb->Z = Z;
+  eb->z16 = z16;
+  eb->kp = kp;
+  const int64_t *crow, *ce0;
+  int64_t nch, chunk;
+  int rc = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
+  if (rc) return rc;
+  PHDE_CK(ctx, cudaMemsetAsync(GL, 0, sizeof(ull) * kp * kp, ctx->stream));
+  LgArgs a;
+  a.off = ctx->d_off;
+  a.adj = ctx->d_adj;
+  a.n = n;
+  a.Z = Z;
+  a.kp = kp;
+  a.heavy = chunk;  // rows above the chunk length are the ones the plan cut into chunks
+  a.chunk_row = crow;
+  a.chunk_e0 = ce0;
+  a.nchunks = nch;
+  a.chunk = chunk;
+  a.GL = GL;
+  const int TS = kp <= 64 ? 4 : 8;
+  const int nb = kp / TS;
+  a.ntiles = nb * (nb + 1) / 2;
+  const int gy = (a.ntiles + LG_THREADS - 1) / LG_THREADS;
+  const size_t smem = sizeof(int) * 2 * LG_ITEMS * (size_t)(kp + 4);
+  const int64_t nslab = (n + nch + LG_ITEMS - 1) / LG_ITEMS;
+  auto launch = [&](auto kern) -> int {
+    PHDE_CK(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LG_THREADS, smem));
+    per_sm = std::max(1, per_sm);
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm / gy, nslab));
+    kern<<<dim3(gx, gy), LG_THREADS, smem, ctx->stream>>>(a);
+    PHDE_LAUNCHED(ctx);
+    return PHDE_OK;
+  };
+  if (z16) {
+    if (kp == 64) rc = launch(lgram_kernel<uint16_t, 2, 4>);
+    else if (kp == 128) rc = launch(lgram_kernel<uint16_t, 4, 8>);
+    else if (kp == 256) rc = launch(lgram_kernel<uint16_t, 8, 8>);
+    else rc = phde_fail(ctx, PHDE_ERR_INVALID, "exact path: unsupported column count");
+  } else {
+    if (kp == 64) rc = launch(lgram_kernel<uint8_t, 2, 4>);
+    else if (kp == 128) rc = launch(lgram_kernel<uint8_t, 4, 8>);
+    else if (kp == 256) rc = launch(lgram_kernel<uint8_t, 8, 8>);
+    else rc = phde_fail(ctx, PHDE_ERR_INVALID, "exact path: unsupported column count");
+  }
+  if (rc) return rc;
+  mgram_kernel<<<k, 256, 0, ctx->stream>>>(GL, kp, eb->A, eb->ld, eb->acc_idx, k, M);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// X (column-major n x c, unit columns) = Z (A Y).
+int phde_exact_coords(phde_ctx *ctx, const double *Y, int k, int c, ExactBasis *eb, double *X) {
+  const int64_t n = ctx->n;
+  const int kp = eb->kp;
+  int32_t *whi = (int32_t *)phde_buf(ctx, "ex.whi", sizeof(int32_t) * (size_t)c * kp);
+  uint32_t *wlo = (uint32_t *)phde_buf(ctx, "ex.wlo", sizeof(uint32_t) * (size_t)c * kp);
+  long long *w0 = (long long *)phde_buf(ctx, "ex.w0", sizeof(long long) * c);
+  double *sinv = (double *)phde_buf(ctx, "ex.sinv", sizeof(double) * c);
+  const int grid = grid_n(ctx, n, 128, 8);
+  double *part = (double *)phde_buf(ctx, "ex.part", sizeof(double) * (size_t)grid * c);
+  if (!whi || !wlo || !w0 || !sinv || !part) return PHDE_ERR_OOM;
+  coords_prep_kernel<<<1, 256, 0, ctx->stream>>>(eb->A, eb->ld, eb->acc_idx, k, Y, c, eb->maxz, kp, whi, wlo, w0,
+                                                 sinv);
+  PHDE_LAUNCHED(ctx);
+  const size_t smem = sizeof(uint32_t) * 2 * (size_t)c * kp;
+  if (eb->z16) {
+    PHDE_CK(ctx, cudaFuncSetAttribute(coords_fix_kernel<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 48 * 1024)));
+    coords_fix_kernel<uint16_t><<<grid, 128, smem, ctx->stream>>>((const uint16_t *)eb->Z, n, kp, c, whi, wlo, w0,
+                                                                  sinv, X, part);
+  } else {
+    PHDE_CK(ctx, cudaFuncSetAttribute(coords_fix_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(smem, 48 * 1024)));
+    coords_fix_kernel<uint8_t><<<grid, 128, smem, ctx->stream>>>((const uint8_t *)eb->Z, n, kp, c, whi, wlo, w0,
+                                                                 sinv, X, part);
+  }
+  PHDE_LAUNCHED(ctx);
+  if (c > 4) {
+    norm_part_kernel<<<grid, 128, 0, ctx->stream>>>(X, n, c, 4, part);
+    PHDE_LAUNCHED(ctx);
+  }
+  unit_scale_kernel<<<grid_n(ctx, n * c, 256, 8), 256, 0, ctx->stream>>>(X, n, c, part, grid);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// The basis S = Z A (row-major n x k FP64), only for callers that ask for it.
+int phde_exact_basis(phde_ctx *ctx, const int32_t *D, int k, const ExactBasis *eb, double *S) {
+  basis_kernel<<<grid_n(ctx, ctx->n * k, 256, 8), 256, 0, ctx->stream>>>(D, ctx->n, eb->A, eb->ld, eb->acc_idx, k, S);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}

@@ -58,6 +58,12 @@ extern "C" {
 /* precision of the dense stages (distances are always exact integers) */
 #define PHDE_PREC_FP64 0  /* every dense stage in FP64, the reference's arithmetic            */
 #define PHDE_PREC_MIXED 1 /* FP32 storage/SpMM, compensated Gram products; FP64 k x k solves  */
+/* ParHDE only: every n-sized product the reference forms in FP64 (the D-orthogonalisation's dot products
+ * and norms, L*S, S^T L S, S*Y) taken instead from exact integer Gram matrices of the distance columns
+ * (int64 sums, no rounding); the Gram-Schmidt loop runs on FP64 coefficient vectors, k x k stages in FP64.
+ * At least the reference's FP64 accuracy.  Distances above 65535, or degree * distance >= 2^31, take the
+ * PHDE_PREC_FP64 kernels instead. */
+#define PHDE_PREC_EXACT 2
 /* eigensolver of the k x k problem */
 #define PHDE_EIG_POWER 0  /* subspace power iteration, ParallelComponents.cpp:48-158 (non-MKL build) */
 #define PHDE_EIG_EXACT 1  /* exact symmetric eigensolve, the LAPACKE_dsyev role (MKL build)          */

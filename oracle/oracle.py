@@ -280,3 +280,43 @@ def ref_draw(csr_path: str, coords_path: str, png_path: str, ncoords: int, first
     r = subprocess.run([REF_DRAW_PATH, csr_path, coords_path, png_path, str(ncoords), str(first), str(second)],
                        env=env, capture_output=True, text=True, check=True)
     return r.stdout + r.stderr
+
+
+# ----------------------------------------------------------------------------- dense stages for given pivots
+
+def hde_from_sources(g, sources, k: int, c: int):
+    """ParHDE's dense stages (ParHDE.cpp:176-308, DrawingBase.cpp:196-244) in numpy FP64 for a given pivot
+    sequence: the BFS column of every source (the C oracle's serial BFS), L2 normalisation, classical
+    Gram-Schmidt in the D inner product against the constant column and the accepted columns with the
+    reference's 1e-3 discard rule, LS = D S - A S, M = S^T LS, the c eigenvectors of the smallest eigenvalues
+    (numpy eigh, the exact eigensolver) and the unit-norm coordinates.  For pivot strategies the C oracle does
+    not restate (learned pivots): it checks the dense stages on the GPU's own pivot sequence.
+    Returns (coords (n, c), S (n, k), M (k, k), naccepted, ndiscarded)."""
+    import scipy.sparse as sp
+    n = g.n
+    off = g.offsets.astype(np.int64)
+    deg = np.diff(off).astype(np.float64)
+    A = sp.csr_matrix((np.ones(g.nnz), g.adj.astype(np.int64), off), shape=(n, n))
+    u0 = np.full(n, 1.0 / np.sqrt(n))
+    Q = []
+    nd = 0
+    for s in sources:
+        if len(Q) >= k:
+            break
+        x = bfs(g, int(s)).astype(np.float64)
+        x = x * (1.0 / np.sqrt(x @ x))
+        coef = [(x @ (deg * q)) * (1.0 / (q @ (deg * q))) for q in Q]
+        c0 = (x @ (deg * u0)) * (1.0 / (u0 @ (deg * u0)))
+        r = x - sum((cq * q for cq, q in zip(coef, Q)), np.zeros(n)) - c0 * u0
+        nrm = np.sqrt(r @ r)
+        if nrm < 0.001:
+            nd += 1
+            continue
+        Q.append(r * (1.0 / nrm))
+    S = np.stack(Q, axis=1)
+    LS = deg[:, None] * S - A @ S
+    M = S.T @ LS
+    w, V = np.linalg.eigh(0.5 * (M + M.T))
+    X = S @ V[:, :c]
+    X /= np.linalg.norm(X, axis=0)
+    return X, S, M, len(Q), nd
