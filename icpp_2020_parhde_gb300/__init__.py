@@ -120,6 +120,16 @@ class Context:
             res.evals = bufs["evals"]
         return res
 
+    def set_pivot_model(self, weights) -> None:
+        """phde_set_pivot_model: replace the learned strategy's MLP weights (4 -> 64 -> 64 -> 1, ReLU)."""
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        self._check(self._L.phde_set_pivot_model(self._h, _ptr(w, C.c_float), w.size))
+
+    def set_pivot_check(self, rule: str = "sum", tolerance: float = 0.02) -> None:
+        """phde_set_pivot_check: the acceptance rule of the "LearnedChecked" strategy ("sum" of the quotients,
+        or "each" coordinate) and its tolerance."""
+        self._check(self._L.phde_set_pivot_check(self._h, {"sum": 0, "each": 1}[rule], float(tolerance)))
+
     def distances(self, sources) -> np.ndarray:
         src = np.ascontiguousarray(np.atleast_1d(sources), dtype=np.int64)
         out = np.empty(self.n * src.shape[0], dtype=np.int32)

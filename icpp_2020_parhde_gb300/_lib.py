@@ -17,7 +17,8 @@ STATUS = {
 }
 NOALLOC_MAX_VERTICES = 1048576
 ALGOS = {"PivotMDS": 0, "PHDE": 1, "wParHDE": 2, "WParHDE": 2, "ParHDE": 3}
-STRATEGIES = {"RandCoarse": 0, "RandFine": 1, "Kcenters": 2, "Learned": 3}
+STRATEGIES = {"RandCoarse": 0, "RandFine": 1, "Kcenters": 2, "Learned": 3, "LearnedChecked": 4}
+OUTCOMES = {0: "reference strategy", 1: "learned", 2: "rejected: Kcenters", 3: "failed: Kcenters"}
 PRECISIONS = {"fp64": 0, "mixed": 1, "exact": 2}
 EIGS = {"power": 0, "exact": 1}
 
@@ -28,7 +29,7 @@ EXPORTS = [
     "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
     "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched", "phde_write_nxyz",
     "phde_graph_from_entries", "phde_graph_download", "phde_draw", "phde_draw_download", "phde_draw_write_png",
-    "phde_write_png", "phde_gram_f32",
+    "phde_write_png", "phde_gram_f32", "phde_set_pivot_check",
 ]
 
 
@@ -54,10 +55,14 @@ class LayoutStats(C.Structure):
                 ("ms_total", C.c_double), ("edges_examined", C.c_int64), ("ms_dist_kernel", C.c_double),
                 ("dist_kernel_launches", C.c_int), ("ms_msbfs_kernel", C.c_double), ("msbfs_levels", C.c_int),
                 ("batch_graph_replay", C.c_int), ("batch_seg_rows", C.c_int), ("ms_batch_tune", C.c_double),
-                ("sssp_rounds", C.c_int64)]
+                ("sssp_rounds", C.c_int64), ("pivot_outcome", C.c_int), ("rayleigh", C.c_double * 8),
+                ("rayleigh_kcenters", C.c_double * 8), ("ms_check", C.c_double), ("ms_lap_kernel", C.c_double)]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        for f in ("rayleigh", "rayleigh_kcenters"):
+            d[f] = list(d[f])
+        return d
 
 
 class DrawInfo(C.Structure):
@@ -116,6 +121,7 @@ def load(path: str | None = None):
     L.phde_launch_count.restype = i64
     L.phde_bfs_noalloc.argtypes = [vp, vp, i64, i64, i64, vp, vp]
     L.phde_set_pivot_model.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
+    L.phde_set_pivot_check.argtypes = [vp, C.c_int, C.c_double]
     L.phde_batch_upload.argtypes = [vp, C.POINTER(GraphDesc), C.c_int]
     L.phde_layout_batched.argtypes = [vp, C.POINTER(LayoutOpts), f64p, C.POINTER(LayoutStats)]
     L.phde_write_nxyz.argtypes = [C.c_char_p, f64p, i64, C.c_int, C.c_int]

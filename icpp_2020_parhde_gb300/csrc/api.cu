@@ -198,6 +198,7 @@ int phde_create(phde_ctx **out, int device) {
   }
   for (auto &e : c->ev) cudaEventCreate(&e);
   for (auto &e : c->kev) cudaEventCreate(&e);
+  for (auto &e : c->lev) cudaEventCreate(&e);
   if (const char *t = getenv("PHDE_WAIT_LIMIT_MS")) c->timeout_ns = (uint64_t)atoll(t) * 1000000ull;
   if (const char *t = getenv("PHDE_CGS2")) c->column_cgs2 = std::string(t) == "column";
   if (const char *t = getenv("PHDE_TC_GRAM")) {
@@ -224,6 +225,7 @@ void phde_destroy(phde_ctx *c) {
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (auto &e : c->ev) cudaEventDestroy(e);
   for (auto &e : c->kev) cudaEventDestroy(e);
+  for (auto &e : c->lev) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -311,6 +313,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   ctx->msbfs_ms = 0;
   ctx->msbfs_levels = 0;
   ctx->kev_pending = false;
+  ctx->lev_pending = false;
   tm.mark(0);
   double *deg = (double *)phde_buf(ctx, "deg", sizeof(double) * n);
   ull *edges = (ull *)phde_buf(ctx, "edges", 2 * sizeof(ull));  // [0] edges examined, [1] SSSP rounds
@@ -538,19 +541,26 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   tm.mark(4);
   double *X = (double *)phde_buf(ctx, "layout.X", sizeof(double) * n * c);
   if (!X) return PHDE_ERR_OOM;
+  double *rqd = (double *)phde_buf(ctx, "layout.rq", sizeof(double) * PHDE_RQ_MAX);
+  if (!rqd) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(rqd, 0, sizeof(double) * PHDE_RQ_MAX, ctx->stream));
+  const bool want_rq = ctx->want_rq || o->strategy == PHDE_STRAT_LEARNED;
   if (exact)
-    rc = phde_exact_coords(ctx, Y, k, c, &eb, X);
+    rc = phde_exact_coords(ctx, M, Y, k, c, &eb, X, rqd);  // the quotients come with it, from k x k products
   else if (mixed)
     rc = phde_coords_mixed(ctx, S32, Y, k, c, X);
   else
     rc = phde_coords(ctx, Sbuf, Y, k, c, X, !hde);
   if (rc) return rc;
+  if (want_rq && !exact && hde && (rc = phde_rayleigh(ctx, X, c, rqd))) return rc;
   PHDE_CK(ctx, cudaMemcpyAsync(coords_out, X, sizeof(double) * n * c, cudaMemcpyDeviceToHost, ctx->stream));
   tm.mark(5);
   if (sources_out && npasses > 0)
     PHDE_CK(ctx, cudaMemcpyAsync(sources_out, d_src, sizeof(int64_t) * npasses, cudaMemcpyDeviceToHost, ctx->stream));
   ull h_edges[2] = {0, 0};
   PHDE_CK(ctx, cudaMemcpyAsync(h_edges, edges, 2 * sizeof(ull), cudaMemcpyDeviceToHost, ctx->stream));
+  double h_rq[PHDE_RQ_MAX];
+  PHDE_CK(ctx, cudaMemcpyAsync(h_rq, rqd, sizeof(h_rq), cudaMemcpyDeviceToHost, ctx->stream));
   if (extra && extra->evecs)
     PHDE_CK(ctx, cudaMemcpyAsync(extra->evecs, K, sizeof(double) * k * k, cudaMemcpyDeviceToHost, ctx->stream));
   if (extra && extra->evals)
@@ -594,6 +604,88 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
     st->dist_kernel_launches = ctx->kernel_launches;
     st->ms_msbfs_kernel = ctx->msbfs_ms;
     st->msbfs_levels = ctx->msbfs_levels;
+    if (exact || (want_rq && hde))
+      for (int j = 0; j < PHDE_RQ_MAX; j++) st->rayleigh[j] = j < c ? h_rq[j] : 0.0;
+    if (ctx->lev_pending) {
+      float t = 0;
+      if (cudaEventElapsedTime(&t, ctx->lev[0], ctx->lev[1]) == cudaSuccess) st->ms_lap_kernel = t;
+      cudaGetLastError();
+    }
+  }
+  return PHDE_OK;
+}
+
+// The learned strategies: PHDE_STRAT_LEARNED falls back to Kcenters when the proposal gives no layout;
+// PHDE_STRAT_LEARNED_CHECKED also lays the graph out with Kcenters and returns the learned layout only when its
+// Rayleigh quotients pass the acceptance rule against Kcenters'.
+static bool pivots_accepted(const phde_ctx *ctx, const double *rl, const double *rk, int c) {
+  const int cc = std::min(c, PHDE_RQ_MAX);
+  const double f = 1.0 + ctx->pivot_check_tol;
+  if (ctx->pivot_check_rule == PHDE_CHECK_EACH) {
+    for (int j = 0; j < cc; j++)
+      if (!(rl[j] <= f * rk[j])) return false;
+    return true;
+  }
+  double sl = 0, sk = 0;
+  for (int j = 0; j < cc; j++) {
+    sl += rl[j];
+    sk += rk[j];
+  }
+  return sl <= f * sk;  // false for NaN quotients
+}
+
+static int layout_learned(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, int64_t *sources_out,
+                          phde_layout_extra *extra, phde_layout_stats *st) {
+  const bool checked = o->strategy == PHDE_STRAT_LEARNED_CHECKED;
+  phde_layout_opts ol = *o, ok = *o;
+  ol.strategy = PHDE_STRAT_LEARNED;
+  ok.strategy = PHDE_STRAT_KCENTERS;
+  phde_layout_stats sl, sk;
+  memset(&sl, 0, sizeof(sl));
+  memset(&sk, 0, sizeof(sk));
+  const int64_t n = ctx->n;
+  std::vector<double> xk;
+  std::vector<int64_t> srck;
+  int rc;
+  if (checked) {  // the Kcenters reference layout first, kept on the host
+    xk.resize((size_t)n * o->c);
+    srck.resize((size_t)3 * o->k);
+    ctx->want_rq = true;
+    rc = layout_impl(ctx, &ok, xk.data(), srck.data(), nullptr, &sk);
+    ctx->want_rq = false;
+    if (rc) return rc;
+  }
+  rc = layout_impl(ctx, &ol, coords_out, sources_out, extra, &sl);
+  int outcome = PHDE_OUTCOME_LEARNED;
+  if (rc == PHDE_ERR_TOO_LARGE || rc == PHDE_ERR_TOO_FEW_PIVOTS) {
+    cudaStreamSynchronize(ctx->stream);
+    outcome = PHDE_OUTCOME_FAILED;
+  } else if (rc) {
+    return rc;
+  } else if (checked && !pivots_accepted(ctx, sl.rayleigh, sk.rayleigh, o->c)) {
+    outcome = PHDE_OUTCOME_REJECTED;
+  }
+  if (outcome != PHDE_OUTCOME_LEARNED) {
+    if (checked && !(extra && (extra->basis || extra->gram || extra->evecs || extra->evals))) {
+      memcpy(coords_out, xk.data(), sizeof(double) * xk.size());
+      if (sources_out) memcpy(sources_out, srck.data(), sizeof(int64_t) * sk.npasses);
+    } else {
+      const double check_ms = sk.ms_total;
+      ctx->want_rq = true;
+      rc = layout_impl(ctx, &ok, coords_out, sources_out, extra, &sk);
+      ctx->want_rq = false;
+      if (rc) return rc;
+      sk.ms_total += check_ms;
+    }
+  }
+  if (st) {
+    const phde_layout_stats &ret = outcome == PHDE_OUTCOME_LEARNED ? sl : sk;
+    *st = ret;
+    st->pivot_outcome = outcome;
+    memcpy(st->rayleigh, sl.rayleigh, sizeof(st->rayleigh));
+    memcpy(st->rayleigh_kcenters, sk.rayleigh, sizeof(st->rayleigh_kcenters));
+    st->ms_check = checked ? sk.ms_total : 0.0;
+    st->ms_total = sl.ms_total + sk.ms_total;  // every layout this call computed
   }
   return PHDE_OK;
 }
@@ -604,8 +696,8 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, in
   if (!ctx || !o || !coords_out) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout: null argument");
   if (ctx->n <= 0) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_layout: no graph uploaded");
   if (o->algo < 0 || o->algo > 3) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized algorithm");
-  if (o->strategy < 0 || o->strategy > 3) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized Strategy");
-  if (o->strategy == PHDE_STRAT_LEARNED && o->algo != PHDE_ALGO_PARHDE)
+  if (o->strategy < 0 || o->strategy > 4) return phde_fail(ctx, PHDE_ERR_INVALID, "Unrecognized Strategy");
+  if ((o->strategy == PHDE_STRAT_LEARNED || o->strategy == PHDE_STRAT_LEARNED_CHECKED) && o->algo != PHDE_ALGO_PARHDE)
     return phde_fail(ctx, PHDE_ERR_INVALID, "learned pivots are implemented for ParHDE");
   if (o->eig != PHDE_EIG_POWER && o->eig != PHDE_EIG_EXACT) return phde_fail(ctx, PHDE_ERR_INVALID, "unknown eigensolver");
   if (o->precision != PHDE_PREC_FP64 && o->precision != PHDE_PREC_MIXED && o->precision != PHDE_PREC_EXACT)
@@ -621,7 +713,9 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, in
   if (o->precision == PHDE_PREC_EXACT && o->algo != PHDE_ALGO_PARHDE)
     return phde_fail(ctx, PHDE_ERR_INVALID, "the exact-Gram path is implemented for ParHDE; use PHDE_PREC_FP64");
   cudaSetDevice(ctx->device);
-  int rc = layout_impl(ctx, o, coords_out, sources_out, extra, st);
+  const bool learned = o->strategy == PHDE_STRAT_LEARNED || o->strategy == PHDE_STRAT_LEARNED_CHECKED;
+  int rc = learned ? layout_learned(ctx, o, coords_out, sources_out, extra, st)
+                   : layout_impl(ctx, o, coords_out, sources_out, extra, st);
   if (st) st->status = rc;
   if (rc != PHDE_OK) cudaStreamSynchronize(ctx->stream);
   return rc;
@@ -746,6 +840,14 @@ int phde_DeltaStep(const uint32_t *row, const uint32_t *col, const int32_t *weig
   int64_t s = source;
   if ((rc = phde_distances(ctx, &s, 1, d.data()))) return rc;
   for (long v = 0; v < numNodes; v++) dist[v] = (double)d[v];  // every entry, kDistInf when unreached (sssp.cc:137-139)
+  return PHDE_OK;
+}
+
+int phde_set_pivot_check(phde_ctx *ctx, int rule, double tolerance) {
+  if (!ctx || (rule != PHDE_CHECK_SUM && rule != PHDE_CHECK_EACH) || !(tolerance >= 0.0 && tolerance < 10.0))
+    return phde_fail(ctx, PHDE_ERR_INVALID, "pivot check: rule PHDE_CHECK_SUM or PHDE_CHECK_EACH, tolerance in [0, 10)");
+  ctx->pivot_check_rule = rule;
+  ctx->pivot_check_tol = tolerance;
   return PHDE_OK;
 }
 

@@ -63,6 +63,9 @@ struct phde_ctx {
   void *w64_buf = nullptr;
   int64_t spmm_nheavy = 0, spmm_nchunks = 0;
   std::vector<float> pivot_model;  // MLP weights of the learned pivot strategy
+  int pivot_check_rule = PHDE_CHECK_SUM;  // PHDE_STRAT_LEARNED_CHECKED's acceptance rule and tolerance
+  double pivot_check_tol = 0.02;
+  bool want_rq = false;            // compute the Rayleigh quotients of every layout (the checked strategy's reference)
   long long ms_plan_epoch = -1;  // multi-source BFS heavy-row plan
   int64_t ms_nheavy = 0, ms_nchunks = 0;
 
@@ -74,6 +77,8 @@ struct phde_ctx {
   cudaEvent_t ev[8] = {};
   // events bracketing each distance-kernel launch; kev_pending says a pair was recorded
   cudaEvent_t kev[2] = {};
+  cudaEvent_t lev[2] = {};  // around the exact path's Laplacian Gram kernel; lev_pending says they were recorded
+  bool lev_pending = false;
   bool kev_pending = false;
   double kernel_ms = 0;  // accumulated by phde_collect_kernel_time()
   double msbfs_ms = 0;   // of which multi-source BFS sweeps
@@ -125,6 +130,7 @@ int phde_tc_gram32(phde_ctx *ctx, const float *A, int lda, int nq, int ones, con
 // The accepted basis as coefficients over the integer columns Z = [1, D columns]: S_q = Z A[q][*].
 struct ExactBasis {
   double *A = nullptr;   // [k][ld]
+  const ull *GI = nullptr;  // [ld][ld] Z^T Z (upper triangle)
   int *acc_idx = nullptr;  // [k] Z index of each accepted column (D column + 1)
   int ld = 0;
   unsigned maxz = 0, maxdeg = 0;
@@ -134,7 +140,10 @@ struct ExactBasis {
 };
 int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog);
 int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, double *M);
-int phde_exact_coords(phde_ctx *ctx, const double *Y, int k, int c, ExactBasis *eb, double *X);
+int phde_exact_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, ExactBasis *eb, double *X,
+                      double *rq);
+// Rayleigh quotients of the first min(c, PHDE_RQ_MAX) coordinate columns of X (device) into rq (device).
+int phde_rayleigh(phde_ctx *ctx, const double *X, int c, double *rq);
 int phde_exact_basis(phde_ctx *ctx, const int32_t *D, int k, const ExactBasis *eb, double *S);
 
 // ---- drawing (draw.cu) ----

@@ -586,9 +586,11 @@ __global__ void basis_kernel(const int32_t *D, int64_t n, const double *A, int l
 // coordinate, W is scaled by 2^s to 62-bit integers (s the largest with |W_0| + maxz sum |W_t| < 2^61 / 2^s),
 // stored as signed high and unsigned low 32-bit words; a row's sum is then exact in 64-bit integers and
 // rounded once to FP64.  The scaling error is below 2^-62 of the row's largest possible magnitude.
+// Also the Rayleigh quotient of each coordinate: x = Z w is S y, so x^T L x = y^T M y (M = S^T L S, the
+// matrix handed to the eigensolver) and x^T x = w^T G_I w over the constant and accepted columns.
 __global__ void coords_prep_kernel(const double *A, int ld, const int *acc_idx, int k, const double *Y, int c,
                                    unsigned maxz, int kp, int32_t *whi, uint32_t *wlo, long long *w0fix,
-                                   double *sinv) {
+                                   double *sinv, const double *M, const ull *GI, double *rq) {
   __shared__ double W[PHDE_MAX_K + 1];
   __shared__ double red[32];
   for (int j = 0; j < c; j++) {
@@ -619,6 +621,23 @@ __global__ void coords_prep_kernel(const double *A, int ld, const int *acc_idx, 
       }
     }
     if (threadIdx.x == 0) sinv[j] = ldexp(1.0, -sh);
+    if (j < PHDE_RQ_MAX) {
+      double num = 0, den = 0;
+      for (int p = threadIdx.x; p < k; p += blockDim.x) {
+        double t = 0;
+        for (int q = 0; q < k; q++) t = fma(M[p + (int64_t)q * k], Y[q + (int64_t)j * k], t);
+        num = fma(Y[p + (int64_t)j * k], t, num);
+      }
+      for (int s = threadIdx.x; s <= k; s += blockDim.x) {
+        const int is = s == 0 ? 0 : acc_idx[s - 1];
+        double t = 0;
+        for (int u = 0; u <= k; u++) t = fma(gsym(GI, ld, is, u == 0 ? 0 : acc_idx[u - 1]), W[u], t);
+        den = fma(W[s], t, den);
+      }
+      num = block_sum(num, red);
+      den = block_sum(den, red);
+      if (threadIdx.x == 0) rq[j] = num / den;
+    }
   }
 }
 
@@ -704,6 +723,67 @@ __global__ void unit_scale_kernel(double *X, int64_t n, int c, const double *par
   __syncthreads();
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * c; e += (int64_t)gridDim.x * blockDim.x)
     X[e] = X[e] * inv[e / n];
+}
+
+// Rayleigh quotients of the coordinate columns X (column-major n x c, c <= PHDE_RQ_MAX) on the uploaded graph:
+// per block, sum_i x_i (d_i x_i - sum_j x_j) and sum_i x_i^2 for each column, a warp per row.
+__global__ void __launch_bounds__(256) rq_rows_kernel(const int64_t *off, const uint32_t *adj, const int32_t *w,
+                                                      const double *X, int64_t n, int c, double *part) {
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31;
+  double num[PHDE_RQ_MAX], den[PHDE_RQ_MAX];
+#pragma unroll
+  for (int j = 0; j < PHDE_RQ_MAX; j++) num[j] = den[j] = 0;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = gw; i < n; i += nwarp) {
+    const int64_t e0 = off[i], e1 = off[i + 1];
+    double s[PHDE_RQ_MAX], dsum = 0;
+#pragma unroll
+    for (int j = 0; j < PHDE_RQ_MAX; j++) s[j] = 0;
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
+      const int64_t v = adj[e];
+      const double we = w ? (double)w[e] : 1.0;
+      dsum += we;
+#pragma unroll
+      for (int j = 0; j < PHDE_RQ_MAX; j++)
+        if (j < c) s[j] = fma(we, X[v + (int64_t)j * n], s[j]);
+    }
+    dsum = warp_sum(dsum);
+#pragma unroll
+    for (int j = 0; j < PHDE_RQ_MAX; j++)
+      if (j < c) {
+        const double t = warp_sum(s[j]);
+        if (lane == 0) {
+          const double xi = X[i + (int64_t)j * n];
+          num[j] = fma(xi, dsum * xi - t, num[j]);
+          den[j] = fma(xi, xi, den[j]);
+        }
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < PHDE_RQ_MAX; j++)
+    if (j < c) {
+      const double a = block_sum(num[j], red);
+      const double b = block_sum(den[j], red);
+      if (threadIdx.x == 0) {
+        part[(int64_t)blockIdx.x * 2 * PHDE_RQ_MAX + j] = a;
+        part[(int64_t)blockIdx.x * 2 * PHDE_RQ_MAX + PHDE_RQ_MAX + j] = b;
+      }
+    }
+}
+
+__global__ void rq_finish_kernel(const double *part, int nparts, int c, double *rq) {
+  __shared__ double red[32];
+  for (int j = 0; j < c; j++) {
+    double a = 0, b = 0;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
+      a += part[(int64_t)p * 2 * PHDE_RQ_MAX + j];
+      b += part[(int64_t)p * 2 * PHDE_RQ_MAX + PHDE_RQ_MAX + j];
+    }
+    a = block_sum(a, red);
+    b = block_sum(b, red);
+    if (threadIdx.x == 0) rq[j] = a / b;
+  }
 }
 
 int grid_n(phde_ctx *ctx, int64_t work, int threads, int per_sm) {
@@ -815,6 +895,7 @@ int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *e
   PHDE_CK(ctx, cudaMemcpyAsync(h_dlog, dlog, sizeof(double) * P, cudaMemcpyDeviceToHost, ctx->stream));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
   eb->A = A;
+  eb->GI = GI;
   eb->acc_idx = acc_idx;
   eb->ld = ld;
   eb->maxz = hm[0];
@@ -869,8 +950,11 @@ int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, doubl
     PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LG_THREADS, smem));
     per_sm = std::max(1, per_sm);
     const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm / gy, nslab));
+    cudaEventRecord(ctx->lev[0], ctx->stream);
     kern<<<dim3(gx, gy), LG_THREADS, smem, ctx->stream>>>(a);
     PHDE_LAUNCHED(ctx);
+    cudaEventRecord(ctx->lev[1], ctx->stream);
+    ctx->lev_pending = true;
     return PHDE_OK;
   };
   if (z16) {
@@ -891,7 +975,8 @@ int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, doubl
 }
 
 // X (column-major n x c, unit columns) = Z (A Y).
-int phde_exact_coords(phde_ctx *ctx, const double *Y, int k, int c, ExactBasis *eb, double *X) {
+int phde_exact_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, ExactBasis *eb, double *X,
+                      double *rq) {
   const int64_t n = ctx->n;
   const int kp = eb->kp;
   int32_t *whi = (int32_t *)phde_buf(ctx, "ex.whi", sizeof(int32_t) * (size_t)c * kp);
@@ -902,7 +987,7 @@ int phde_exact_coords(phde_ctx *ctx, const double *Y, int k, int c, ExactBasis *
   double *part = (double *)phde_buf(ctx, "ex.part", sizeof(double) * (size_t)grid * c);
   if (!whi || !wlo || !w0 || !sinv || !part) return PHDE_ERR_OOM;
   coords_prep_kernel<<<1, 256, 0, ctx->stream>>>(eb->A, eb->ld, eb->acc_idx, k, Y, c, eb->maxz, kp, whi, wlo, w0,
-                                                 sinv);
+                                                 sinv, M, eb->GI, rq);
   PHDE_LAUNCHED(ctx);
   const size_t smem = sizeof(uint32_t) * 2 * (size_t)c * kp;
   if (eb->z16) {
@@ -929,6 +1014,21 @@ int phde_exact_coords(phde_ctx *ctx, const double *Y, int k, int c, ExactBasis *
 // The basis S = Z A (row-major n x k FP64), only for callers that ask for it.
 int phde_exact_basis(phde_ctx *ctx, const int32_t *D, int k, const ExactBasis *eb, double *S) {
   basis_kernel<<<grid_n(ctx, ctx->n * k, 256, 8), 256, 0, ctx->stream>>>(D, ctx->n, eb->A, eb->ld, eb->acc_idx, k, S);
+  PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// Rayleigh quotients x_j^T L x_j / x_j^T x_j of the first min(c, PHDE_RQ_MAX) columns of X (device), into rq
+// (device, PHDE_RQ_MAX doubles).
+int phde_rayleigh(phde_ctx *ctx, const double *X, int c, double *rq) {
+  const int cc = std::min(c, PHDE_RQ_MAX);
+  const int grid = grid_n(ctx, ctx->n * 32, 256, 4);
+  double *part = (double *)phde_buf(ctx, "rq.part", sizeof(double) * (size_t)grid * 2 * PHDE_RQ_MAX);
+  if (!part) return PHDE_ERR_OOM;
+  rq_rows_kernel<<<grid, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, ctx->weighted ? ctx->d_w : nullptr, X, ctx->n,
+                                                cc, part);
+  PHDE_LAUNCHED(ctx);
+  rq_finish_kernel<<<1, 256, 0, ctx->stream>>>(part, grid, cc, rq);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

@@ -53,6 +53,14 @@ extern "C" {
  * farthest-point selection on their exact pairwise distances; one multi-source BFS replaces the 3k
  * serial Kcenters passes (ParHDE only). */
 #define PHDE_STRAT_LEARNED 3
+/* PHDE_STRAT_LEARNED with its acceptance test in the same call: the Kcenters layout (same precision and
+ * eigensolver) is computed too, and the learned layout is returned only when its Rayleigh quotients
+ * x_i^T L x_i / x_i^T x_i are within the tolerance of the Kcenters layout's (phde_set_pivot_check: their sum,
+ * by default, or every coordinate); otherwise the Kcenters layout is returned.  Costs one Kcenters layout more
+ * than PHDE_STRAT_LEARNED.  Both learned strategies fall back to Kcenters by themselves when the proposal
+ * cannot give a layout (the multi-source BFS's level limit, fewer than k vectors surviving the
+ * D-orthogonalisation); phde_layout_stats.pivot_outcome says which layout came back. */
+#define PHDE_STRAT_LEARNED_CHECKED 4
 #define PHDE_LEARNED_CANDIDATES 256
 #define PHDE_LEARNED_WARM 8 /* exact Kcenters passes before the learned candidates are scored */
 /* precision of the dense stages (distances are always exact integers) */
@@ -105,7 +113,21 @@ typedef struct {
   int batch_seg_rows;       /* phde_layout_batched: rows per segment CTA picked by the autotuner         */
   double ms_batch_tune;     /* phde_layout_batched: the autotuner's best whole-batch time (first call)   */
   int64_t sssp_rounds;      /* WParHDE: synchronised relaxation rounds of the SSSP passes, summed        */
+  /* learned strategies: PHDE_OUTCOME_*; 0 for the reference's strategies */
+  int pivot_outcome;
+  /* Rayleigh quotients x_i^T L x_i / x_i^T x_i of the first PHDE_RQ_MAX returned coordinates (learned
+   * strategies and PHDE_PREC_EXACT; 0 otherwise), and for PHDE_STRAT_LEARNED_CHECKED the Kcenters layout's */
+  double rayleigh[8];
+  double rayleigh_kcenters[8];
+  double ms_check;          /* PHDE_STRAT_LEARNED_CHECKED: the Kcenters layout's time (part of ms_total)  */
+  double ms_lap_kernel;     /* PHDE_PREC_EXACT: device time of the fused Laplacian Gram kernel (Z^T L Z)   */
 } phde_layout_stats;
+#define PHDE_RQ_MAX 8
+#define PHDE_OUTCOME_LEARNED 1        /* the learned proposal's layout                                      */
+#define PHDE_OUTCOME_REJECTED 2       /* learned layout outside the Rayleigh tolerance: Kcenters layout      */
+#define PHDE_OUTCOME_FAILED 3         /* learned proposal gave no layout (level limit, too few pivots): Kcenters */
+#define PHDE_CHECK_SUM 0              /* sum of the c quotients within the tolerance of Kcenters' sum        */
+#define PHDE_CHECK_EACH 1             /* every coordinate's quotient within the tolerance of Kcenters'       */
 
 /* optional extra outputs of phde_layout (any member may be NULL) */
 typedef struct {
@@ -249,6 +271,11 @@ int phde_gram_f32(phde_ctx *ctx, const float *A, int lda, int acols, const float
  * W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3[1] (row-major).  The library starts with the
  * weights trained by icpp_2020_parhde_gb300/train_pivot_mlp.py.  No counterpart in the reference. */
 int phde_set_pivot_model(phde_ctx *ctx, const float *weights, int count);
+
+/* The acceptance rule of PHDE_STRAT_LEARNED_CHECKED: rule PHDE_CHECK_SUM (default) or PHDE_CHECK_EACH, and
+ * the tolerance (default 0.02: learned quotients at most 1.02 times Kcenters').  No counterpart in the
+ * reference. */
+int phde_set_pivot_check(phde_ctx *ctx, int rule, double tolerance);
 
 /* Kernel launches issued through this context since it was created. */
 int64_t phde_launch_count(const phde_ctx *ctx);

@@ -63,3 +63,89 @@ def test_learned_only_for_parhde(gpu_ctx):
     gpu_ctx.upload(g)
     with pytest.raises(ParHDEError):
         gpu_ctx.layout("PivotMDS", "Learned", 5, 2)
+
+
+# ---- acceptance in the library: PHDE_STRAT_LEARNED_CHECKED and the structural fallback ----
+
+def _model_size():
+    return 64 * 4 + 64 + 64 * 64 + 64 + 64 + 1
+
+
+def _clustering_model():
+    """A pivot model that prefers the vertices closest to the warm-start pivots (score = sigmoid(-10 f2), f2 the
+    warm start's normalised minimum distance): every proposed candidate sits next to a pivot already taken."""
+    w = np.zeros(_model_size(), np.float32)
+    w[0 * 4 + 2] = 1.0                       # W1[0][2]: hidden unit 0 = f2
+    w[64 * 4 + 64 + 0] = 1.0                 # W2[0][0]: second layer passes it on
+    w[64 * 4 + 64 + 64 * 64 + 64 + 0] = -10  # w3[0]: the farther, the lower the score
+    return w
+
+
+@pytest.mark.parametrize("precision", ["exact", "mixed", "fp64"])
+def test_rayleigh_quotients_in_stats(gpu_ctx, precision):
+    g = graphs.rmat(14, seed=41)
+    gpu_ctx.upload(g)
+    r = gpu_ctx.layout("ParHDE", "Learned", 12, 3, precision=precision, eig="exact")
+    assert r.stats["pivot_outcome"] == 1
+    np.testing.assert_allclose(r.stats["rayleigh"][:3], rayleigh(g, r.coords), rtol=1e-9)
+    assert r.stats["rayleigh"][3:] == [0.0] * 5
+
+
+def test_learned_checked_rejects_a_clustering_model():
+    """A model whose candidates all crowd around the warm-start pivots gives a much worse layout: the checked
+    strategy must reject it and return the Kcenters layout itself (same coordinates, same pivots)."""
+    from icpp_2020_parhde_gb300 import Context
+    g = graphs.rgg(40000, dim=2, avg_degree=8, seed=42)
+    k, c = 20, 2
+    with Context(0) as ctx:
+        ctx.upload(g)
+        kc = ctx.layout("ParHDE", "Kcenters", k, c, precision="exact", eig="exact")
+        ctx.set_pivot_model(_clustering_model())
+        bad = ctx.layout("ParHDE", "Learned", k, c, precision="exact", eig="exact")
+        r = ctx.layout("ParHDE", "LearnedChecked", k, c, precision="exact", eig="exact")
+    assert sum(rayleigh(g, bad.coords)) > 1.02 * sum(rayleigh(g, kc.coords))
+    assert r.stats["pivot_outcome"] == 2
+    assert np.array_equal(r.coords, kc.coords) and np.array_equal(r.sources, kc.sources)
+    np.testing.assert_allclose(r.stats["rayleigh_kcenters"][:c], rayleigh(g, kc.coords), rtol=1e-9)
+    np.testing.assert_allclose(r.stats["rayleigh"][:c], rayleigh(g, bad.coords), rtol=1e-9)
+    assert r.stats["ms_check"] > 0 and r.stats["ms_total"] > r.stats["ms_check"]
+
+
+def test_learned_checked_with_a_zero_model():
+    """All-zero weights score every vertex alike.  Whatever the rule decides, the checked strategy returns either
+    the learned layout (the same as PHDE_STRAT_LEARNED's) or the Kcenters layout, and says which."""
+    from icpp_2020_parhde_gb300 import Context
+    g = graphs.rmat(15, seed=43)
+    k, c = 16, 3
+    with Context(0) as ctx:
+        ctx.upload(g)
+        ctx.set_pivot_model(np.zeros(_model_size(), np.float32))
+        kc = ctx.layout("ParHDE", "Kcenters", k, c, precision="exact", eig="exact")
+        lp = ctx.layout("ParHDE", "Learned", k, c, precision="exact", eig="exact")
+        for rule in ("sum", "each"):
+            ctx.set_pivot_check(rule, 0.02)
+            r = ctx.layout("ParHDE", "LearnedChecked", k, c, precision="exact", eig="exact")
+            ql, qk = rayleigh(g, lp.coords), rayleigh(g, kc.coords)
+            ok = ql.sum() <= 1.02 * qk.sum() if rule == "sum" else bool(np.all(ql <= 1.02 * qk))
+            assert r.stats["pivot_outcome"] == (1 if ok else 2), (rule, ql, qk)
+            want = lp if ok else kc
+            assert np.array_equal(r.coords, want.coords) and np.array_equal(r.sources, want.sources)
+
+
+def test_learned_falls_back_when_the_search_is_too_deep(gpu_ctx):
+    """A 70000-vertex path: the multi-source BFS's 16-bit level record overflows, so the learned proposal gives
+    no layout; PHDE_STRAT_LEARNED returns the Kcenters layout and says so."""
+    g = graphs.path_graph(70000)
+    gpu_ctx.upload(g)
+    r = gpu_ctx.layout("ParHDE", "Learned", 6, 2, precision="exact", eig="exact")
+    kc = gpu_ctx.layout("ParHDE", "Kcenters", 6, 2, precision="exact", eig="exact")
+    assert r.stats["pivot_outcome"] == 3
+    assert np.array_equal(r.coords, kc.coords) and np.array_equal(r.sources, kc.sources)
+
+
+def test_pivot_check_arguments(gpu_ctx):
+    with pytest.raises(ParHDEError):
+        gpu_ctx._check(gpu_ctx._L.phde_set_pivot_check(gpu_ctx._h, 7, 0.02))
+    with pytest.raises(ParHDEError):
+        gpu_ctx.set_pivot_check("sum", -1.0)
+    gpu_ctx.set_pivot_check("sum", 0.02)
