@@ -291,15 +291,33 @@ class Runner:
         return {"ms": ms, "stats": stats, "launches": (self.ctx.launch_count - l0) / max(1, steps), "phases": ph}
 
     def e2e(self, p, steps):
-        ts = []
+        ts, tu = [], []
         for _ in range(steps):
             self.flush_l2()
             barrier(self.ws)
             t1 = time.perf_counter()
             self.ctx.upload(self.gp)
+            t2 = time.perf_counter()
             self.run(p)
             ts.append(time.perf_counter() - t1)
+            tu.append(t2 - t1)
+        self.upload_ms = float(np.mean(tu)) * 1e3
         return allmax(self.ws, float(np.mean(ts))) * 1e3
+
+    def h2d_probe(self):
+        """Host-to-device bandwidth of the pinned adjacency array alone (one plain copy, no kernels)."""
+        import torch
+        src = self.gp._pinned[1]
+        dst = torch.empty_like(src, device="cuda")
+        for _ in range(2):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t1) / 3
+        return {"bytes": int(src.numel() * 4), "ms": t * 1e3, "gbs": src.numel() * 4 / t / 1e9}
 
     def h2d(self):
         g = self.g
@@ -410,6 +428,7 @@ def run_gb300(args):
     xy_head = R.coords()
     st_head = head["stats"][-1]
     e2e_head = R.e2e(P_LEARNED, args.steps)
+    upload_head = R.upload_ms
     # ---- the reference pipeline on the GPU, the pivot control, the checked strategy, mixed precision ----
     sub_steps = max(3, args.steps // 4)
     controls = [x for x in args.controls.split(",") if x]
@@ -494,7 +513,8 @@ def run_gb300(args):
         "ms_per_graph": head["ms"],
         "phases_ms": head["phases"],
         "e2e": {"value": ws * k * nnz / (e2e_head * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_graph": e2e_head,
+                "d2h_bytes_per_step": d2h, "ms_per_graph": e2e_head, "upload_ms": upload_head,
+                "h2d_copy_probe": R.h2d_probe(),
                 "path": "phde_graph_upload from pinned host CSR + phde_layout (coordinates to pinned host memory)"},
         "gpu_launches": int(round(head["launches"] * args.steps)),
         "roofline": roof,
