@@ -125,6 +125,16 @@ class Context:
         w = np.ascontiguousarray(weights, dtype=np.float32)
         self._check(self._L.phde_set_pivot_model(self._h, _ptr(w, C.c_float), w.size))
 
+    def pivot_scores(self, ncand: int = 256):
+        """phde_pivot_scores: the learned strategy's proposal step alone -- (scores (n,), warm-start minimum
+        distances (n,), the ncand candidates it takes)."""
+        sc = np.empty(self.n, dtype=np.float32)
+        d0 = np.empty(self.n, dtype=np.int32)
+        cand = np.empty(ncand, dtype=np.int64)
+        self._check(self._L.phde_pivot_scores(self._h, _ptr(sc, C.c_float), _ptr(d0, C.c_int32),
+                                              _ptr(cand, C.c_int64), ncand))
+        return sc, d0, cand
+
     def set_pivot_check(self, rule: str = "sum", tolerance: float = 0.02) -> None:
         """phde_set_pivot_check: the acceptance rule of the "LearnedChecked" strategy ("sum" of the quotients,
         or "each" coordinate) and its tolerance."""

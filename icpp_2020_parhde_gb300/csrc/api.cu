@@ -334,6 +334,8 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   const bool mixed = o->precision == PHDE_PREC_MIXED;
   bool exact = o->precision == PHDE_PREC_EXACT;  // cleared when the inputs are out of the exact path's range
   ExactBasis eb;
+  ZSrc zsrc;                   // where the exact path reads the candidate columns
+  std::vector<int> rec_order;  // learned pivots: the record columns of candidates P0.. (exact path)
   float *S32 = nullptr;
   if (mixed) {
     S32 = (float *)phde_buf(ctx, "layout.S32", sizeof(float) * n * k);
@@ -445,10 +447,25 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
         for (int i = 0; i < Mc; i++) mind[i] = std::min(mind[i], csub[(size_t)i * Mc + best]);
       }
       const int Pn = (int)order.size();
-      int unreached = 0;
-      if ((rc = phde_record_columns(ctx, R, RW, order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0, &unreached)))
-        return rc;
-      if (unreached) return phde_fail(ctx, PHDE_ERR_DISCONNECTED, "distance passes: the graph is not connected");
+      if (exact && hde) {
+        // the exact path reads the candidates' columns from the record where they are (no gather); the warm
+        // start's first pass already required every vertex to be reached
+        int *rmap = (int *)phde_buf(ctx, "lp.rmap", sizeof(int) * std::max(Pn, 1));
+        if (!rmap) return PHDE_ERR_OOM;
+        if (Pn > 0)
+          PHDE_CK(ctx, cudaMemcpyAsync(rmap, order.data(), sizeof(int) * Pn, cudaMemcpyHostToDevice, ctx->stream));
+        zsrc.D = D;
+        zsrc.P0 = P0;
+        zsrc.R = R;
+        zsrc.RW = RW;
+        zsrc.rmap = rmap;
+        rec_order = order;
+      } else {
+        int unreached = 0;
+        if ((rc = phde_record_columns(ctx, R, RW, order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0, &unreached)))
+          return rc;
+        if (unreached) return phde_fail(ctx, PHDE_ERR_DISCONNECTED, "distance passes: the graph is not connected");
+      }
       std::vector<int64_t> srcs(Pn);
       for (int p = 0; p < Pn; p++) srcs[p] = cand[order[p]];
       if (Pn > 0)
@@ -477,9 +494,20 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       int state[4] = {0, 0, 0, 0};
       std::vector<double> dlog(P);
       if (exact) {
-        rc = phde_exact_orth(ctx, D, P_used, k, &eb, state, dlog.data());
+        if (!zsrc.R) {
+          zsrc.D = D;
+          zsrc.P0 = P_used;
+        }
+        rc = phde_exact_orth(ctx, zsrc, P_used, k, &eb, state, dlog.data());
         if (rc == PHDE_ERR_TOO_LARGE) {  // distances or degrees beyond the exact sums: the FP64 vector kernels
           exact = false;
+          if (zsrc.R) {  // they need the learned candidates' columns in D, with their sums of squares
+            int unreached = 0;
+            const int P0 = zsrc.P0, Pn = (int)rec_order.size();
+            if ((rc = phde_record_columns(ctx, zsrc.R, zsrc.RW, rec_order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0,
+                                          &unreached)))
+              return rc;
+          }
           rc = phde_cgs(ctx, D, P_used, sumsq, deg, Sbuf, k, state, dlog.data());
         }
       } else if (mixed && !ctx->column_cgs2)
@@ -517,9 +545,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
 
   // ---- Laplacian SpMM + Gram (HDE) or C^T C (MDS) ----
   if (hde && exact) {
-    int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);
-    if (!D) return PHDE_ERR_OOM;
-    if ((rc = phde_exact_lap(ctx, D, k, &eb, M))) return rc;
+    if ((rc = phde_exact_lap(ctx, zsrc, k, &eb, M))) return rc;
   } else if (hde && mixed) {
     float *LS32 = (float *)phde_buf(ctx, "layout.LS32", sizeof(float) * n * k);
     if (!LS32) return PHDE_ERR_OOM;
@@ -568,11 +594,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   std::vector<double> Srow;
   std::vector<float> Srow32;
   if (extra && extra->basis) {
-    if (exact) {
-      int32_t *D = (int32_t *)phde_buf(ctx, "layout.D", sizeof(int32_t) * n * P);
-      if (!D) return PHDE_ERR_OOM;
-      if ((rc = phde_exact_basis(ctx, D, k, &eb, Sbuf))) return rc;
-    }
+    if (exact && (rc = phde_exact_basis(ctx, zsrc, k, &eb, Sbuf))) return rc;
     if (mixed) {
       Srow32.resize((size_t)n * k);
       PHDE_CK(ctx, cudaMemcpyAsync(Srow32.data(), S32, sizeof(float) * n * k, cudaMemcpyDeviceToHost, ctx->stream));
@@ -840,6 +862,40 @@ int phde_DeltaStep(const uint32_t *row, const uint32_t *col, const int32_t *weig
   int64_t s = source;
   if ((rc = phde_distances(ctx, &s, 1, d.data()))) return rc;
   for (long v = 0; v < numNodes; v++) dist[v] = (double)d[v];  // every entry, kDistInf when unreached (sssp.cc:137-139)
+  return PHDE_OK;
+}
+
+int phde_pivot_scores(phde_ctx *ctx, float *scores, int32_t *warm_dist, int64_t *candidates, int ncand) {
+  if (!ctx || ncand < 0 || ncand > PHDE_LEARNED_CANDIDATES) return phde_fail(ctx, PHDE_ERR_INVALID, "pivot scores: bad arguments");
+  if (ctx->n <= 0) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "pivot scores: no graph uploaded");
+  if (ctx->weighted) return phde_fail(ctx, PHDE_ERR_WEIGHTS, "learned pivots are implemented for unweighted graphs");
+  cudaSetDevice(ctx->device);
+  const int64_t n = ctx->n;
+  const int P0 = (int)std::min<int64_t>(PHDE_LEARNED_WARM, n);
+  int32_t *D = (int32_t *)phde_buf(ctx, "ps.D", sizeof(int32_t) * n * P0);
+  int64_t *d_src = (int64_t *)phde_buf(ctx, "ps.src", sizeof(int64_t) * (P0 + 2));
+  ull *sumsq = (ull *)phde_buf(ctx, "ps.sumsq", sizeof(ull) * P0);
+  if (!D || !d_src || !sumsq) return PHDE_ERR_OOM;
+  if (ctx->pivot_model.empty()) {
+    const float *w0;
+    int cnt;
+    if (phde_default_pivot_model(&w0, &cnt)) return phde_fail(ctx, PHDE_ERR_INVALID, "built-in pivot model has the wrong size");
+    ctx->pivot_model.assign(w0, w0 + cnt);
+  }
+  int rc = phde_run_bfs_passes(ctx, P0, 0, nullptr, D, d_src, sumsq, nullptr, 1);
+  if (rc || (rc = phde_check_device_err(ctx, "pivot scores: warm start"))) return rc;
+  const int32_t *mind0 = (const int32_t *)phde_buf(ctx, "kc.min_d", sizeof(int32_t) * n);
+  if (!mind0) return PHDE_ERR_OOM;
+  std::vector<int64_t> cand;
+  std::vector<float> cscore;
+  if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), std::max(ncand, 1), mind0, cand, cscore))) return rc;
+  const float *score = (const float *)phde_buf(ctx, "lp.score", sizeof(float) * n);
+  if (!score) return PHDE_ERR_OOM;
+  if (scores) PHDE_CK(ctx, cudaMemcpyAsync(scores, score, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  if (warm_dist) PHDE_CK(ctx, cudaMemcpyAsync(warm_dist, mind0, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (candidates)
+    for (int i = 0; i < ncand; i++) candidates[i] = i < (int)cand.size() ? cand[i] : -1;
   return PHDE_OK;
 }
 

@@ -127,6 +127,16 @@ int phde_tc_gram32(phde_ctx *ctx, const float *A, int lda, int nq, int ones, con
                    int64_t n, int ncta, int nqc, int self, float *part);
 
 // ---- exact-Gram dense stages (exact.cu, PHDE_PREC_EXACT) ----
+// Where the candidate distance columns live: Z column t (1 <= t <= P) is int32 column t - 1 of D (column-major,
+// n rows) for t <= P0, else column rmap[t - 1 - P0] of the multi-source BFS record R (row-major n x RW uint16,
+// level + 1).  Kcenters and random pivots have every column in D (P0 = P).
+struct ZSrc {
+  const int32_t *D = nullptr;
+  int P0 = 0;
+  const uint16_t *R = nullptr;
+  int RW = 0;
+  const int *rmap = nullptr;  // device array
+};
 // The accepted basis as coefficients over the integer columns Z = [1, D columns]: S_q = Z A[q][*].
 struct ExactBasis {
   double *A = nullptr;   // [k][ld]
@@ -138,13 +148,13 @@ struct ExactBasis {
   bool z16 = false;
   int kp = 0;
 };
-int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog);
-int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, double *M);
+int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog);
+int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double *M);
 int phde_exact_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, ExactBasis *eb, double *X,
                       double *rq);
 // Rayleigh quotients of the first min(c, PHDE_RQ_MAX) coordinate columns of X (device) into rq (device).
 int phde_rayleigh(phde_ctx *ctx, const double *X, int c, double *rq);
-int phde_exact_basis(phde_ctx *ctx, const int32_t *D, int k, const ExactBasis *eb, double *S);
+int phde_exact_basis(phde_ctx *ctx, const ZSrc &src, int k, const ExactBasis *eb, double *S);
 
 // ---- drawing (draw.cu) ----
 // The last drawn image's 4-bit palette scanlines (H rows of 1 + ceil(W / 2) bytes) copied to the host.

@@ -63,7 +63,7 @@ __device__ __forceinline__ double gsym(const ull *G, int ld, int p, int q) {
 // ------------------------------------------------------------------------------------------------
 // G_I = Z^T Z and G_D = Z^T D Z for the Z columns p in [0, c1), q in [c0, c1), p <= q.
 struct ZgArgs {
-  const int32_t *D;  // n x P column-major; Z column t >= 1 is D column t - 1, Z column 0 is all ones
+  ZSrc src;          // Z column 0 is all ones, columns 1..P the candidates (ZSrc)
   const int64_t *off;
   int64_t n;
   int P;
@@ -75,10 +75,15 @@ struct ZgArgs {
 };
 
 __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
-  extern __shared__ int zsm[];  // [ZG_ROWS][S]
+  extern __shared__ int zsm[];  // [ZG_ROWS][S], then the record column of each Z column of the block
   __shared__ unsigned s_deg[ZG_ROWS];
   __shared__ ull red[32];
   const int S = a.c1 + 4;
+  int *s_rmap = zsm + ZG_ROWS * S;
+  const int P0 = a.src.P0;
+  // Z columns [0, nd) are the ones column and D columns; [nd, c1) record columns (or padding beyond P)
+  const int nd = min(a.c1, P0 + 1), nr = a.c1 - nd;
+  for (int j = threadIdx.x; j < nr; j += ZG_THREADS) s_rmap[j] = nd + j <= a.P ? a.src.rmap[nd + j - 1 - P0] : -1;
   const int t = blockIdx.y * ZG_THREADS + threadIdx.x;
   int pb, qb;
   tile_of(t, a.c0 / 4, a.c1 / 4, pb, qb);
@@ -109,11 +114,18 @@ __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
     const int rows = (int)min((int64_t)ZG_ROWS, r1 - i0);
     __syncthreads();  // previous slab consumed
     unsigned mz = 0, md = 0;
-    for (int e = threadIdx.x; e < ZG_ROWS * a.c1; e += ZG_THREADS) {
+    for (int e = threadIdx.x; e < ZG_ROWS * nd; e += ZG_THREADS) {  // consecutive threads: rows of a column
       const int col = e / ZG_ROWS, r = e - col * ZG_ROWS;
       int v = 0;
-      if (r < rows) v = col == 0 ? 1 : (col - 1 < a.P ? a.D[(int64_t)(col - 1) * a.n + i0 + r] : 0);
+      if (r < rows) v = col == 0 ? 1 : (col - 1 < a.P ? a.src.D[(int64_t)(col - 1) * a.n + i0 + r] : 0);
       zsm[r * S + col] = v;
+      mz = max(mz, (unsigned)v);
+    }
+    for (int e = threadIdx.x; e < ZG_ROWS * nr; e += ZG_THREADS) {  // consecutive threads: columns of a row
+      const int r = e / nr, j = e - r * nr;
+      const int rc = s_rmap[j];
+      const int v = r < rows && rc >= 0 ? (int)a.src.R[(i0 + r) * a.src.RW + rc] - 1 : 0;
+      zsm[r * S + nd + j] = v;
       mz = max(mz, (unsigned)v);
     }
     if (threadIdx.x < ZG_ROWS) {
@@ -187,6 +199,7 @@ __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
 struct CoefArgs {
   const ull *GI, *GD;
   int ld;
+  int nc;         // > 0: the leading nc x nc blocks of G_I and G_D are staged in shared memory as FP64
   int64_t n;
   int r_end;      // examine Z indices [state[3], r_end)
   int k;
@@ -198,10 +211,21 @@ struct CoefArgs {
 };
 
 __global__ void __launch_bounds__(CF_THREADS) coef_kernel(CoefArgs a) {
-  extern __shared__ double cs[];  // rr[ld], gdr[ld], cq[k]
+  extern __shared__ double cs[];  // rr[ld], gdr[ld], cq[k], then (nc > 0) GIs[nc][nc], GDs[nc][nc]
   __shared__ double red[32];
   __shared__ int s_idx[PHDE_MAX_K];
   double *rr = cs, *gdr = cs + a.ld, *cq = cs + 2 * a.ld;
+  double *GIs = cq + a.k, *GDs = GIs + (size_t)a.nc * a.nc;
+  const int nc = a.nc;
+  for (int e = threadIdx.x; e < nc * nc; e += CF_THREADS) {
+    const int i = e / nc, j = e - i * nc;
+    GIs[e] = gsym(a.GI, a.ld, i, j);
+    GDs[e] = gsym(a.GD, a.ld, i, j);
+  }
+  __syncthreads();
+  // G_I / G_D entry (i, j): from shared memory when staged (every index the loop reads is below r_end <= nc)
+  auto gi = [&](int i, int j) { return nc ? GIs[i * nc + j] : gsym(a.GI, a.ld, i, j); };
+  auto gd = [&](int i, int j) { return nc ? GDs[i * nc + j] : gsym(a.GD, a.ld, i, j); };
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = CF_THREADS / 32;
   int nacc = a.state[0], ndisc = a.state[1], nexam = a.state[2];
   for (int q = threadIdx.x; q < nacc; q += CF_THREADS) s_idx[q] = a.acc_idx[q];
@@ -210,8 +234,8 @@ __global__ void __launch_bounds__(CF_THREADS) coef_kernel(CoefArgs a) {
   int r = a.state[3];
   for (; r < a.r_end && nacc < a.k; r++) {
     __syncthreads();
-    for (int i = threadIdx.x; i <= r; i += CF_THREADS) gdr[i] = gsym(a.GD, a.ld, i, r);
-    const double inv = 1.0 / sqrt(gsym(a.GI, a.ld, r, r));
+    for (int i = threadIdx.x; i <= r; i += CF_THREADS) gdr[i] = gd(i, r);
+    const double inv = 1.0 / sqrt(gi(r, r));
     __syncthreads();
     for (int q = warp; q < nacc; q += nw) {
       const int top = s_idx[q];
@@ -234,7 +258,7 @@ __global__ void __launch_bounds__(CF_THREADS) coef_kernel(CoefArgs a) {
     double s = 0;
     for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
       double ti = 0;
-      for (int j = 0; j <= r; j++) ti = fma(gsym(a.GI, a.ld, i, j), rr[j], ti);
+      for (int j = 0; j <= r; j++) ti = fma(gi(i, j), rr[j], ti);
       s = fma(rr[i], ti, s);
     }
     const double nrm = sqrt(fmax(block_sum(s, red), 0.0));
@@ -255,7 +279,7 @@ __global__ void __launch_bounds__(CF_THREADS) coef_kernel(CoefArgs a) {
     double dsum = 0;
     for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
       double ti = 0;
-      for (int j = 0; j <= r; j++) ti = fma(gsym(a.GD, a.ld, i, j), rr[j], ti);
+      for (int j = 0; j <= r; j++) ti = fma(gd(i, j), rr[j], ti);
       dsum = fma(rr[i], ti, dsum);
     }
     dsum = block_sum(dsum, red);
@@ -277,9 +301,14 @@ __global__ void __launch_bounds__(CF_THREADS) coef_kernel(CoefArgs a) {
 // ------------------------------------------------------------------------------------------------
 // Z_acc[i][t] = D[acc_idx[t] - 1][i] for t < k, 0 for k <= t < kp; 16 bytes per store.
 template <typename T>
-__global__ void pack_kernel(const int32_t *D, int64_t n, const int *acc_idx, int k, int kp, T *Z) {
+__global__ void pack_kernel(ZSrc src, int64_t n, const int *acc_idx, int k, int kp, T *Z) {
   __shared__ int s_col[PHDE_MAX_K];
-  for (int t = threadIdx.x; t < kp; t += blockDim.x) s_col[t] = t < k ? acc_idx[t] - 1 : -1;
+  __shared__ bool s_rec[PHDE_MAX_K];
+  for (int t = threadIdx.x; t < kp; t += blockDim.x) {
+    const int z = t < k ? acc_idx[t] : 0;  // Z index of accepted column t
+    s_rec[t] = z > src.P0;
+    s_col[t] = t >= k ? -1 : (z > src.P0 ? src.rmap[z - 1 - src.P0] : z - 1);
+  }
   __syncthreads();
   constexpr int V = 16 / sizeof(T);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -291,7 +320,7 @@ __global__ void pack_kernel(const int32_t *D, int64_t n, const int *acc_idx, int
 #pragma unroll
       for (int j = 0; j < V; j++) {
         const int col = s_col[t0 + j];
-        w.v[j] = col >= 0 ? (T)D[(int64_t)col * n + i] : (T)0;
+        w.v[j] = col < 0 ? (T)0 : s_rec[t0 + j] ? (T)(src.R[i * src.RW + col] - 1) : (T)src.D[(int64_t)col * n + i];
       }
       *(uint4 *)(Z + i * kp + t0) = w.u;
     }
@@ -303,92 +332,48 @@ __global__ void pack_kernel(const int32_t *D, int64_t n, const int *acc_idx, int
 // heavy rows' chunks of at most `chunk` (<= 256) edges.  Item u of row i has z = Z_acc[i] and
 // r = (deg_i z if the item holds the row's diagonal term) - sum over its edges of Z_acc[j]; the items'
 // z (x) r sum to Z^T (D Z - A Z) = Z^T L Z.
-template <typename T, int CPL>
-struct RowLoad;  // lane l's CPL columns of a row: l*CPL .. l*CPL+CPL-1
-template <>
-struct RowLoad<uint8_t, 2> {
-  typedef uint16_t V;
-};
-template <>
-struct RowLoad<uint8_t, 4> {
-  typedef uint32_t V;
-};
-template <>
-struct RowLoad<uint8_t, 8> {
-  typedef uint2 V;
-};
-template <>
-struct RowLoad<uint16_t, 2> {
-  typedef uint32_t V;
-};
-template <>
-struct RowLoad<uint16_t, 4> {
-  typedef uint2 V;
-};
-template <>
-struct RowLoad<uint16_t, 8> {
-  typedef uint4 V;
-};
-
-// the 32-bit words of a loaded vector (a 16-bit load is zero-extended into one word)
-__device__ __forceinline__ void words_of(const uint16_t &v, uint32_t (&w)[1]) { w[0] = v; }
-__device__ __forceinline__ void words_of(const uint32_t &v, uint32_t (&w)[1]) { w[0] = v; }
-__device__ __forceinline__ void words_of(const uint2 &v, uint32_t (&w)[2]) {
-  w[0] = v.x;
-  w[1] = v.y;
-}
-__device__ __forceinline__ void words_of(const uint4 &v, uint32_t (&w)[4]) {
-  w[0] = v.x;
-  w[1] = v.y;
-  w[2] = v.z;
-  w[3] = v.w;
-}
-template <typename T, int CPL>
-struct NWords {
-  static constexpr int value = (CPL * (int)sizeof(T) + 3) / 4;
-};
-
-// unpack a loaded vector into CPL ints
-template <typename T, int CPL>
-__device__ __forceinline__ void unpack(const typename RowLoad<T, CPL>::V &v, int (&o)[CPL]) {
-  uint32_t w[NWords<T, CPL>::value];
-  words_of(v, w);
-  if (sizeof(T) == 1) {
-#pragma unroll
-    for (int c = 0; c < CPL; c++) o[c] = (int)((w[c / 4] >> (8 * (c % 4))) & 0xffu);
-  } else {
-#pragma unroll
-    for (int c = 0; c < CPL; c++) o[c] = (int)((w[c / 2] >> (16 * (c % 2))) & 0xffffu);
-  }
-}
-
-// neighbour sums: for uint8 rows two columns share a 32-bit register as 16-bit halves (bytes moved apart
-// by one byte permute; at most 256 neighbours of at most 255 keep each half below 2^16, so plain adds never
-// carry across); uint16 rows sum each column in its own register
-template <typename T, int CPL>
-struct NbSum {
-  static constexpr int NW = sizeof(T) == 1 ? CPL / 2 : CPL;
-  uint32_t s[NW];
+//
+// Gathers: a row of Z_acc is KP values; LPR lanes read it with one 16-byte load each, so a warp is
+// G = 32 / LPR lane groups, each on its own neighbour, and one load instruction fetches G neighbour rows.
+// Sums: for uint8 rows two columns share a 32-bit register as 16-bit halves (bytes moved apart by one byte
+// permute; an item has at most 256 neighbours of at most 255, so no half ever carries into the next, also
+// after the groups are added together); uint16 rows sum each column in its own register.
+template <typename T>
+struct Sum16 {  // the sums of one 16-byte slice of a row: 16 uint8 or 8 uint16 columns, in 8 registers
+  uint32_t s[8];
   __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int i = 0; i < NW; i++) s[i] = 0;
+    for (int i = 0; i < 8; i++) s[i] = 0;
   }
-  __device__ __forceinline__ void add(const typename RowLoad<T, CPL>::V &v) {
-    uint32_t w[NWords<T, CPL>::value];
-    words_of(v, w);
-    if (sizeof(T) == 1) {
+  __device__ __forceinline__ void add(const uint4 &v) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-      for (int i = 0; i < NW; i++) s[i] += __byte_perm(w[i / 2], 0u, (i % 2) ? 0x4342 : 0x4140);
-    } else {
-#pragma unroll
-      for (int i = 0; i < NW; i++) s[i] += (w[i / 2] >> (16 * (i % 2))) & 0xffffu;
+    for (int i = 0; i < 4; i++) {
+      if (sizeof(T) == 1) {
+        s[2 * i] += __byte_perm(w[i], 0u, 0x4140);
+        s[2 * i + 1] += __byte_perm(w[i], 0u, 0x4342);
+      } else {
+        s[2 * i] += w[i] & 0xffffu;
+        s[2 * i + 1] += w[i] >> 16;
+      }
     }
   }
-  __device__ __forceinline__ int get(int c) const {
+  __device__ __forceinline__ void add_from(int lane_mask) {  // add the sums of lane ^ lane_mask
+#pragma unroll
+    for (int i = 0; i < 8; i++) s[i] += __shfl_xor_sync(PHDE_FULL_MASK, s[i], lane_mask);
+  }
+  __device__ __forceinline__ int get(int c) const {  // column c of the slice
     if (sizeof(T) == 1) return (int)((s[c / 2] >> (16 * (c % 2))) & 0xffffu);
     return (int)s[c];
   }
 };
+
+template <typename T>
+__device__ __forceinline__ int slice_val(const uint4 &v, int c) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  if (sizeof(T) == 1) return (int)((w[c / 4] >> (8 * (c % 4))) & 0xffu);
+  return (int)((w[c / 2] >> (16 * (c % 2))) & 0xffffu);
+}
 
 struct LgArgs {
   const int64_t *off;
@@ -403,18 +388,22 @@ struct LgArgs {
   int ntiles;
 };
 
-template <typename T, int CPL, int TS>
+template <typename T, int KP, int TS>
 __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
-  typedef typename RowLoad<T, CPL>::V V;
+  constexpr int V = 16 / (int)sizeof(T);  // columns per 16-byte slice
+  constexpr int LPR = KP / V;             // lanes per row
+  constexpr int G = 32 / LPR;             // neighbour rows per load instruction
+  constexpr int SL = KP + 4;
   extern __shared__ int lsm[];  // zs[LG_ITEMS][SL], rs[LG_ITEMS][SL]
   __shared__ ull s_bnd[LG_ITEMS];
-  const int kp = a.kp, SL = kp + 4;
+  __shared__ int s_next;
   int *zs = lsm, *rs = lsm + LG_ITEMS * SL;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = LG_THREADS / 32;
+  const int lane = threadIdx.x & 31;
+  const int gi = lane / LPR, pi = lane % LPR;  // lane group (neighbour) and slice within the row
   const T *Z = (const T *)a.Z;
   const int t = blockIdx.y * LG_THREADS + threadIdx.x;
   int pb, qb;
-  tile_of(t, 0, kp / TS, pb, qb);
+  tile_of(t, 0, KP / TS, pb, qb);
   const bool active = t < a.ntiles && pb >= 0;
   int acc[TS][TS];
 #pragma unroll
@@ -428,7 +417,7 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
 #pragma unroll
       for (int j = 0; j < TS; j++) {
         const int p = TS * pb + i, q = TS * qb + j;
-        if (p <= q && acc[i][j]) atomicAdd(a.GL + (int64_t)p * kp + q, (ull)(long long)acc[i][j]);
+        if (p <= q && acc[i][j]) atomicAdd(a.GL + (int64_t)p * KP + q, (ull)(long long)acc[i][j]);
         acc[i][j] = 0;
       }
   };
@@ -438,7 +427,13 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
   for (int64_t s = blockIdx.x; s < nslab; s += gridDim.x) {
     const int64_t u0 = s * LG_ITEMS;
     __syncthreads();  // previous slab consumed
-    for (int slot = warp; slot < LG_ITEMS; slot += nw) {
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    for (;;) {  // the warps take the slab's items one at a time
+      int slot = 0;
+      if (lane == 0) slot = atomicAdd(&s_next, 1);
+      slot = __shfl_sync(PHDE_FULL_MASK, slot, 0);
+      if (slot >= LG_ITEMS) break;
       const int64_t u = u0 + slot;
       int64_t row = -1, e0 = 0, e1 = 0;
       bool diag = false;
@@ -457,41 +452,37 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
         e1 = min(e0 + a.chunk, re1);
         diag = e0 == re0;
       }
-      int zi[CPL], r[CPL];
+      unsigned zm = 0, rm = 0;
       if (row >= 0) {
-        const V own = *(const V *)(Z + row * kp + lane * CPL);
-        unpack<T, CPL>(own, zi);
-        NbSum<T, CPL> nb;
+        Sum16<T> nb;
         nb.zero();
-        int64_t e = e0;
-        for (; e + 4 <= e1; e += 4) {
-          const int64_t v0 = __ldg(a.adj + e), v1 = __ldg(a.adj + e + 1), v2 = __ldg(a.adj + e + 2),
-                        v3 = __ldg(a.adj + e + 3);
-          const V x0 = *(const V *)(Z + v0 * kp + lane * CPL), x1 = *(const V *)(Z + v1 * kp + lane * CPL);
-          const V x2 = *(const V *)(Z + v2 * kp + lane * CPL), x3 = *(const V *)(Z + v3 * kp + lane * CPL);
+        int64_t e = e0 + gi;
+        for (; e + G < e1; e += 2 * G) {
+          const int64_t v0 = __ldg(a.adj + e), v1 = __ldg(a.adj + e + G);
+          const uint4 x0 = __ldg((const uint4 *)(Z + v0 * KP) + pi);
+          const uint4 x1 = __ldg((const uint4 *)(Z + v1 * KP) + pi);
           nb.add(x0);
           nb.add(x1);
-          nb.add(x2);
-          nb.add(x3);
         }
-        for (; e < e1; e++) {
-          const int64_t v = __ldg(a.adj + e);
-          nb.add(*(const V *)(Z + v * kp + lane * CPL));
+        if (e < e1) nb.add(__ldg((const uint4 *)(Z + (int64_t)__ldg(a.adj + e) * KP) + pi));
+#pragma unroll
+        for (int m = LPR; m < 32; m <<= 1) nb.add_from(m);
+        if (gi == 0) {
+          const uint4 own = __ldg((const uint4 *)(Z + row * KP) + pi);
+          const int deg = diag ? (int)(a.off[row + 1] - a.off[row]) : 0;
+#pragma unroll
+          for (int c = 0; c < V; c++) {
+            const int zi = slice_val<T>(own, c);
+            const int r = deg * zi - nb.get(c);
+            zs[slot * SL + pi * V + c] = zi;
+            rs[slot * SL + pi * V + c] = r;
+            zm = max(zm, (unsigned)zi);
+            rm = max(rm, (unsigned)abs(r));
+          }
         }
-        const int deg = diag ? (int)(a.off[row + 1] - a.off[row]) : 0;
+      } else if (gi == 0) {
 #pragma unroll
-        for (int c = 0; c < CPL; c++) r[c] = deg * zi[c] - nb.get(c);
-      } else {
-#pragma unroll
-        for (int c = 0; c < CPL; c++) zi[c] = r[c] = 0;
-      }
-      unsigned zm = 0, rm = 0;
-#pragma unroll
-      for (int c = 0; c < CPL; c++) {
-        zs[slot * SL + lane * CPL + c] = zi[c];
-        rs[slot * SL + lane * CPL + c] = r[c];
-        zm = max(zm, (unsigned)zi[c]);
-        rm = max(rm, (unsigned)abs(r[c]));
+        for (int c = 0; c < V; c++) zs[slot * SL + pi * V + c] = rs[slot * SL + pi * V + c] = 0;
       }
       zm = __reduce_max_sync(PHDE_FULL_MASK, zm);
       rm = __reduce_max_sync(PHDE_FULL_MASK, rm);
@@ -511,7 +502,7 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
             for (int j = 0; j < TS; j++) {
               const int p = TS * pb + i, q = TS * qb + j;
               const long long v = (long long)zr[p] * (long long)rr[q];
-              if (p <= q && v) atomicAdd(a.GL + (int64_t)p * kp + q, (ull)v);
+              if (p <= q && v) atomicAdd(a.GL + (int64_t)p * KP + q, (ull)v);
             }
         }
         continue;
@@ -569,14 +560,18 @@ __global__ void __launch_bounds__(256) mgram_kernel(const ull *GL, int kp, const
 }
 
 // S (row-major n x k) = Z A^T restricted to the accepted columns, for callers that ask for the basis.
-__global__ void basis_kernel(const int32_t *D, int64_t n, const double *A, int ld, const int *acc_idx, int k,
+__global__ void basis_kernel(ZSrc src, int64_t n, const double *A, int ld, const int *acc_idx, int k,
                              double *S) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / k;
     const int q = (int)(e - i * k);
     const double *Aq = A + (int64_t)q * ld;
     double s = Aq[0];
-    for (int t = 0; t <= q; t++) s = fma(Aq[acc_idx[t]], (double)D[(int64_t)(acc_idx[t] - 1) * n + i], s);
+    for (int t = 0; t <= q; t++) {
+      const int z = acc_idx[t];
+      const int d = z <= src.P0 ? src.D[(int64_t)(z - 1) * n + i] : (int)src.R[i * src.RW + src.rmap[z - 1 - src.P0]] - 1;
+      s = fma(Aq[z], (double)d, s);
+    }
     S[e] = s;
   }
 }
@@ -798,12 +793,12 @@ int grid_n(phde_ctx *ctx, int64_t work, int threads, int per_sm) {
 // host side
 
 // G_I, G_D for Z columns p < c1, q in [c0, c1).
-static int exact_zgram(phde_ctx *ctx, const int32_t *D, int P, int c0, int c1, ull *GI, ull *GD, int ld,
+static int exact_zgram(phde_ctx *ctx, const ZSrc &src, int P, int c0, int c1, ull *GI, ull *GD, int ld,
                        unsigned *maxz) {
   const int nq = (c1 - c0) / 4;
   const int ntiles = nq * (c0 / 4) + nq * (nq + 1) / 2;
   const int gy = (ntiles + ZG_THREADS - 1) / ZG_THREADS;
-  const size_t smem = sizeof(int) * ZG_ROWS * (size_t)(c1 + 4);
+  const size_t smem = sizeof(int) * (ZG_ROWS * (size_t)(c1 + 4) + c1);
   PHDE_CK(ctx, cudaFuncSetAttribute(zgram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zgram_kernel, ZG_THREADS, smem));
@@ -811,7 +806,7 @@ static int exact_zgram(phde_ctx *ctx, const int32_t *D, int P, int c0, int c1, u
   const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm / gy + 1,
                                                               (ctx->n + ZG_ROWS - 1) / ZG_ROWS));
   ZgArgs a;
-  a.D = D;
+  a.src = src;
   a.off = ctx->d_off;
   a.n = ctx->n;
   a.P = P;
@@ -833,7 +828,7 @@ static int exact_zgram(phde_ctx *ctx, const int32_t *D, int P, int c0, int c1, u
 // h_state: accepted, discarded, examined; h_dlog[i]: norm of discarded candidate i (NaN otherwise).
 // Returns PHDE_ERR_TOO_LARGE when the distances or degrees are too large for exact 64-bit sums that
 // convert exactly to FP64 (the caller then takes the FP64 vector path).
-int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog) {
+int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog) {
   const int64_t n = ctx->n;
   const int ld = ((P + 1) + 3) / 4 * 4;
   ull *GI = (ull *)phde_buf(ctx, "ex.GI", sizeof(ull) * ld * ld);
@@ -852,14 +847,14 @@ int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *e
   PHDE_CK(ctx, cudaMemsetAsync(maxz, 0, sizeof(unsigned) * 2, ctx->stream));
   const int st0[4] = {0, 0, 0, 1};
   PHDE_CK(ctx, cudaMemcpyAsync(state, st0, sizeof(st0), cudaMemcpyHostToDevice, ctx->stream));
-  const size_t csmem = sizeof(double) * (2 * (size_t)ld + k);
-  PHDE_CK(ctx, cudaFuncSetAttribute(coef_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)std::max<size_t>(csmem, 48 * 1024)));
+  const size_t csmem0 = sizeof(double) * (2 * (size_t)ld + k);
+  constexpr size_t CF_SMEM_MAX = 200 * 1024;
+  PHDE_CK(ctx, cudaFuncSetAttribute(coef_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_SMEM_MAX));
   int c0 = 0, c1 = std::min(ld, (1 + std::min(P, k + std::max(4, k / 8)) + 3) / 4 * 4);
   int hs[4] = {0, 0, 0, 1};
   unsigned hm[2] = {0, 0};
   for (;;) {
-    int rc = exact_zgram(ctx, D, P, c0, c1, GI, GD, ld, maxz);
+    int rc = exact_zgram(ctx, src, P, c0, c1, GI, GD, ld, maxz);
     if (rc) return rc;
     PHDE_CK(ctx, cudaMemcpyAsync(hm, maxz, sizeof(hm), cudaMemcpyDeviceToHost, ctx->stream));
     PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -873,6 +868,10 @@ int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *e
     ca.GI = GI;
     ca.GD = GD;
     ca.ld = ld;
+    // stage the Gram blocks the loop reads when both fit next to the vectors
+    const int rend = std::min(c1, P + 1);
+    ca.nc = csmem0 + sizeof(double) * 2 * (size_t)rend * rend <= CF_SMEM_MAX ? rend : 0;
+    const size_t csmem = csmem0 + sizeof(double) * 2 * (size_t)ca.nc * ca.nc;
     ca.n = n;
     ca.r_end = std::min(c1, P + 1);
     ca.k = k;
@@ -905,7 +904,7 @@ int phde_exact_orth(phde_ctx *ctx, const int32_t *D, int P, int k, ExactBasis *e
 }
 
 // Pack the accepted columns, form Z_acc^T L Z_acc exactly and M = A_acc^T (Z_acc^T L Z_acc) A_acc.
-int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, double *M) {
+int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double *M) {
   const int64_t n = ctx->n;
   const bool z16 = eb->maxz > 255u;
   const int kp = k <= 64 ? 64 : k <= 128 ? 128 : 256;
@@ -914,9 +913,9 @@ int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, doubl
   if (!Z || !GL) return PHDE_ERR_OOM;
   const int gp = grid_n(ctx, n, 256, 8);
   if (z16)
-    pack_kernel<uint16_t><<<gp, 256, 0, ctx->stream>>>(D, n, eb->acc_idx, k, kp, (uint16_t *)Z);
+    pack_kernel<uint16_t><<<gp, 256, 0, ctx->stream>>>(src, n, eb->acc_idx, k, kp, (uint16_t *)Z);
   else
-    pack_kernel<uint8_t><<<gp, 256, 0, ctx->stream>>>(D, n, eb->acc_idx, k, kp, (uint8_t *)Z);
+    pack_kernel<uint8_t><<<gp, 256, 0, ctx->stream>>>(src, n, eb->acc_idx, k, kp, (uint8_t *)Z);
   PHDE_LAUNCHED(ctx);
   eb->Z = Z;
   eb->z16 = z16;
@@ -958,15 +957,13 @@ int phde_exact_lap(phde_ctx *ctx, const int32_t *D, int k, ExactBasis *eb, doubl
     return PHDE_OK;
   };
   if (z16) {
-    if (kp == 64) rc = launch(lgram_kernel<uint16_t, 2, 4>);
-    else if (kp == 128) rc = launch(lgram_kernel<uint16_t, 4, 8>);
-    else if (kp == 256) rc = launch(lgram_kernel<uint16_t, 8, 8>);
-    else rc = phde_fail(ctx, PHDE_ERR_INVALID, "exact path: unsupported column count");
+    if (kp == 64) rc = launch(lgram_kernel<uint16_t, 64, 4>);
+    else if (kp == 128) rc = launch(lgram_kernel<uint16_t, 128, 8>);
+    else rc = launch(lgram_kernel<uint16_t, 256, 8>);
   } else {
-    if (kp == 64) rc = launch(lgram_kernel<uint8_t, 2, 4>);
-    else if (kp == 128) rc = launch(lgram_kernel<uint8_t, 4, 8>);
-    else if (kp == 256) rc = launch(lgram_kernel<uint8_t, 8, 8>);
-    else rc = phde_fail(ctx, PHDE_ERR_INVALID, "exact path: unsupported column count");
+    if (kp == 64) rc = launch(lgram_kernel<uint8_t, 64, 4>);
+    else if (kp == 128) rc = launch(lgram_kernel<uint8_t, 128, 8>);
+    else rc = launch(lgram_kernel<uint8_t, 256, 8>);
   }
   if (rc) return rc;
   mgram_kernel<<<k, 256, 0, ctx->stream>>>(GL, kp, eb->A, eb->ld, eb->acc_idx, k, M);
@@ -1012,8 +1009,8 @@ int phde_exact_coords(phde_ctx *ctx, const double *M, const double *Y, int k, in
 }
 
 // The basis S = Z A (row-major n x k FP64), only for callers that ask for it.
-int phde_exact_basis(phde_ctx *ctx, const int32_t *D, int k, const ExactBasis *eb, double *S) {
-  basis_kernel<<<grid_n(ctx, ctx->n * k, 256, 8), 256, 0, ctx->stream>>>(D, ctx->n, eb->A, eb->ld, eb->acc_idx, k, S);
+int phde_exact_basis(phde_ctx *ctx, const ZSrc &src, int k, const ExactBasis *eb, double *S) {
+  basis_kernel<<<grid_n(ctx, ctx->n * k, 256, 8), 256, 0, ctx->stream>>>(src, ctx->n, eb->A, eb->ld, eb->acc_idx, k, S);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

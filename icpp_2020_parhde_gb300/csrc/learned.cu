@@ -10,7 +10,7 @@
 //     f2 = d0(v) / max d0
 //     f3 = |{u in N(v): d0(u) > d0(v)}| / deg v   (share of neighbours farther from the pivots)
 //   score = MLP(f): 4 -> 64 -> 64 -> 1, ReLU, FP32 (weights trained on the pivots Kcenters picks after
-//           the warm start, icpp_2020_parhde_gb300/train_pivot_mlp.py, compiled in from pivot_mlp_weights.h)
+//           the warm start, train/train_pivot_mlp.py, compiled in from pivot_mlp_weights.h)
 // The host takes the M best-scored vertices as candidates, runs ONE multi-source BFS from all of them,
 // and picks the remaining pivots among them by farthest-point selection on exact distances, seeded with
 // the warm-start pivots.

@@ -33,6 +33,7 @@ constexpr int MS_MAXW = 4;
 constexpr int64_t MS_HEAVY = 256;  // rows above this are cut into chunks (one warp per chunk)
 constexpr int64_t MS_CHUNK = 256;
 constexpr int MS_GROUP = 8;        // lanes per light row
+constexpr int MS_TILE_CHUNK = 4;   // dense levels: 32-vertex tiles a warp takes from the level counter at once
 constexpr int GATHER_SMEM_COLS = 1024;  // columns whose sums of squares are kept per CTA
 
 struct MsArgs {
@@ -61,6 +62,7 @@ struct MsArgs {
   int32_t *stamp;             // [n] claim stamps of sparse levels (L + 1), zeroed
   uint32_t *cand;             // [n] candidates of a sparse level
   unsigned *ccount;           // [2] candidate counters, by level parity
+  unsigned *tctr;             // [4] dense levels: next 32-vertex tile to hand out, slot L % 4 (reset one level ahead)
   int64_t sparse_edges;       // a level runs sparse when its frontier has fewer out-edges
   int *levels_out;
   ull *trace;                 // optional [2*trace_cap]: per level end time (ns) and vertices given new bits
@@ -267,6 +269,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       a.lctr[(L + 1) & 3] = 0ull;
       a.lstat[(L + 1) & 3] = 0ull;
       a.ccount[(L + 1) & 1] = 0u;
+      a.tctr[(L + 1) & 3] = 0u;
     }
     if (threadIdx.x == 0) s_stat = 0ull;
     ull my_stat = 0;  // dense: this thread's (count << 32 | edges) of vertices given new bits
@@ -340,9 +343,19 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       }
     } else {
       // light rows, 32-vertex tiles per warp: one load of the done bitmap skips finished vertices; the
-      // unfinished ones go to the warp's four 8-lane groups in turn
+      // unfinished ones go to the warp's four 8-lane groups in turn.  Warps take MS_TILE_CHUNK tiles at a time
+      // from a level counter, so warps that meet heavy neighbourhoods do not hold the level's end back.
       const int64_t ntiles = (n + 31) / 32;
-      for (int64_t t = gw; t < ntiles; t += gws) {
+      unsigned *tc = a.tctr + (L & 3);
+      int64_t t = 0, tend = 0;
+      for (;; t++) {
+        if (t >= tend) {
+          unsigned tb = 0;
+          if (lane == 0) tb = atomicAdd(tc, (unsigned)MS_TILE_CHUNK);
+          t = (int64_t)__shfl_sync(PHDE_FULL_MASK, tb, 0);
+          if (t >= ntiles) break;
+          tend = min(t + MS_TILE_CHUNK, ntiles);
+        }
         const int64_t v0 = t * 32;
         const unsigned valid = n - v0 >= 32 ? 0xffffffffu : ((1u << (n - v0)) - 1u);
         // one read of the tile's word, broadcast: the warp sets bits of it below
@@ -542,7 +555,9 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
   uint32_t *lists = (uint32_t *)phde_buf(ctx, "ms.lists", sizeof(uint32_t) * 8 * lcap);  // qv[4], qe[4]
   uint32_t *cand = (uint32_t *)phde_buf(ctx, "ms.cand", sizeof(uint32_t) * n);
   int32_t *stamp = (int32_t *)phde_buf(ctx, "ms.stamp", sizeof(int32_t) * n);
-  ull *lctr = (ull *)phde_buf(ctx, "ms.lctr", sizeof(ull) * 8 + sizeof(unsigned) * 2);  // lctr[4], lstat[4], ccount[2]
+  // lctr[4], lstat[4], ccount[2], tctr[4]
+  const size_t ctr_bytes = sizeof(ull) * 8 + sizeof(unsigned) * 6;
+  ull *lctr = (ull *)phde_buf(ctx, "ms.lctr", ctr_bytes);
   if (!R || !seen || !f0 || !f1 || !hacc || !levels || !bms || !lists || !cand || !stamp || !lctr) return PHDE_ERR_OOM;
   const int64_t *crow, *ce0;
   int64_t nch, chunk;
@@ -569,7 +584,7 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     PHDE_CK(ctx, cudaMemsetAsync(seen, 0, sizeof(ull) * n * W, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(f0, 0, sizeof(ull) * n * W, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(f1, 0, sizeof(ull) * n * W, ctx->stream));  // level 1 writes candidates only
-    PHDE_CK(ctx, cudaMemsetAsync(lctr, 0, sizeof(ull) * 8 + sizeof(unsigned) * 2, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(lctr, 0, ctr_bytes, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(bms, 0, sizeof(uint32_t) * nw32, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(stamp, 0, sizeof(int32_t) * n, ctx->stream));
     int rc = phde_reset_sync(ctx);
@@ -599,6 +614,7 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.lctr = lctr;
     a.lstat = lctr + 4;
     a.ccount = (unsigned *)(lctr + 8);
+    a.tctr = a.ccount + 2;
     a.stamp = stamp;
     a.cand = cand;
     a.sparse_edges = std::max<int64_t>(ctx->nnz / 16, 1);

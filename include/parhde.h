@@ -269,8 +269,15 @@ int phde_gram_f32(phde_ctx *ctx, const float *A, int lda, int acols, const float
 
 /* Replace the pivot-scoring MLP used by PHDE_STRAT_LEARNED (4 -> 64 -> 64 -> 1, ReLU): `count` floats,
  * W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3[1] (row-major).  The library starts with the
- * weights trained by icpp_2020_parhde_gb300/train_pivot_mlp.py.  No counterpart in the reference. */
+ * weights trained by train/train_pivot_mlp.py.  No counterpart in the reference. */
 int phde_set_pivot_model(phde_ctx *ctx, const float *weights, int count);
+
+/* Diagnostics used by the tests: the learned strategy's proposal step alone on the uploaded graph -- the
+ * PHDE_LEARNED_WARM exact Kcenters passes, the per-vertex features and the pivot-scoring MLP -- returning
+ * every vertex's score (scores: n floats), the warm start's minimum distance to its pivots (warm_dist: n int32)
+ * and the `ncand` best-scored vertices the strategy takes as candidates (score descending, index ascending on
+ * ties).  Any output may be NULL.  No counterpart in the reference. */
+int phde_pivot_scores(phde_ctx *ctx, float *scores, int32_t *warm_dist, int64_t *candidates, int ncand);
 
 /* The acceptance rule of PHDE_STRAT_LEARNED_CHECKED: rule PHDE_CHECK_SUM (default) or PHDE_CHECK_EACH, and
  * the tolerance (default 0.02: learned quotients at most 1.02 times Kcenters').  No counterpart in the

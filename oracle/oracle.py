@@ -37,11 +37,16 @@ def build_oracle(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_reference(ref_tree: str = "/root/reference") -> str | None:
-    """Build oracle/_ref from the reference sources when the tree is present (never on the GPU machine)."""
-    if not os.path.isfile(os.path.join(ref_tree, "variants", "ParHDE.cpp")):
+def build_reference(ref_tree: str | None = None) -> str | None:
+    """Build oracle/_ref from the reference sources when the tree is present.  The tree is `ref_tree`, else the
+    recipe's own choice (build_ref.sh: $PARHDE_REF_SRC, else its default location); None when there is no tree
+    (the recipe exits 2), as on a machine that only has this repository."""
+    r = subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")] + ([ref_tree] if ref_tree else []),
+                       stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+    if r.returncode == 2:
         return None
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), ref_tree], stdout=subprocess.DEVNULL)
+    if r.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + r.stderr[-2000:])
     return REF_LIB_PATH
 
 

@@ -7,9 +7,10 @@ the positive vertices.  Features are the four the GPU kernel computes (csrc/lear
 the neighbour-degree sum, the warm start's minimum distance to its pivots, and the share of neighbours
 with a larger minimum distance, each normalised per graph.  The 4 -> 64 -> 64 -> 1 ReLU network is trained with a
 class-weighted logistic loss under BF16 autocast; the FP32 weights are written to
-csrc/pivot_mlp_weights.h (compiled into the library) and a summary to pivot_mlp_train.json.
+icpp_2020_parhde_gb300/csrc/pivot_mlp_weights.h (compiled into the library) and a summary to
+train/pivot_mlp_train.json.  An offline tool: the library never imports it.
 
-    python -m icpp_2020_parhde_gb300.train_pivot_mlp [--graphs 200] [--max-n 100000]
+    python train/train_pivot_mlp.py [--graphs 200] [--max-n 100000]
 """
 from __future__ import annotations
 
@@ -22,28 +23,12 @@ import time
 
 import numpy as np
 
-PKG = os.path.dirname(os.path.abspath(__file__))
-ROOT = os.path.dirname(PKG)
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+PKG = os.path.join(ROOT, "icpp_2020_parhde_gb300")
+sys.path.insert(0, ROOT)
 
-
-WARM = 8  # PHDE_LEARNED_WARM in include/parhde.h
-
-
-def features(g, d0: np.ndarray) -> np.ndarray:
-    """The four per-vertex features of csrc/learned.cu (float32, shape (n, 4)); d0 = warm-start min distance."""
-    off = g.offsets.astype(np.int64)
-    adj = g.adj.astype(np.int64)
-    n = g.n
-    deg = np.diff(off).astype(np.float64)
-    src = np.repeat(np.arange(n), np.diff(off))
-    hop2 = np.bincount(src, weights=deg[adj], minlength=n)
-    outw = np.bincount(src, weights=(d0[adj] > d0[src]).astype(np.float64), minlength=n)
-    f = np.zeros((n, 4), dtype=np.float64)
-    f[:, 0] = np.log1p(deg) / max(np.log1p(deg.max()), 1e-30)
-    f[:, 1] = np.log1p(hop2) / max(np.log1p(hop2.max()), 1e-30)
-    f[:, 2] = np.maximum(d0, 0) / max(d0.max(), 1)
-    f[:, 3] = np.where(deg > 0, outw / np.maximum(deg, 1), 0.0)
-    return f.astype(np.float32)
+from oracle.pivot_oracle import WARM, features  # noqa: E402  (the numpy restatement of the GPU features)
 
 
 def training_graphs(count: int, max_n: int, seed: int):
@@ -70,7 +55,6 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=6)
     ap.add_argument("--seed", type=int, default=2020)
     args = ap.parse_args(argv)
-    sys.path.insert(0, ROOT)
     import torch
     from oracle import oracle as orc  # the CPU oracle computes the Kcenters labels
 
@@ -129,7 +113,7 @@ def main(argv=None):
     flat = np.concatenate([W1.ravel(), b1, W2.ravel(), b2, w3, b3]).astype(np.float32)
     hdr = os.path.join(PKG, "csrc", "pivot_mlp_weights.h")
     with open(hdr, "w") as f:
-        f.write("// Generated by icpp_2020_parhde_gb300/train_pivot_mlp.py -- do not edit.\n")
+        f.write("// Generated by train/train_pivot_mlp.py -- do not edit.\n")
         f.write("// Pivot-scoring MLP 4 -> 64 -> 64 -> 1 (ReLU): W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3.\n")
         f.write("#pragma once\nstatic const float kPivotMlpWeights[%d] = {\n" % flat.size)
         for i in range(0, flat.size, 8):
@@ -140,7 +124,7 @@ def main(argv=None):
                "epochs": args.epochs, "loss": history, "mean_kcenters_pivots_in_top256": float(np.mean(hits)),
                "max_n": args.max_n, "seed": args.seed, "train_seconds": time.time() - t0,
                "training_graphs": [f"{a} n={b} nnz={c}" for a, b, c in sizes]}
-    with open(os.path.join(PKG, "pivot_mlp_train.json"), "w") as f:
+    with open(os.path.join(HERE, "pivot_mlp_train.json"), "w") as f:
         json.dump(summary, f, indent=1)
     print(json.dumps({k: v for k, v in summary.items() if k != "training_graphs"}, indent=1))
 
