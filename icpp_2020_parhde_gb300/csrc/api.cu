@@ -26,7 +26,8 @@ int phde_basis_rows(phde_ctx *ctx, const double *U, int k, double *S);
 int phde_lap_spmm(phde_ctx *ctx, const double *deg, const double *S, double *LS, int k);
 int phde_gram(phde_ctx *ctx, const double *A, const double *B, int k, double *M);
 int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C);
-int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X, int seq);
+int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X, int seq,
+                double *norm2 = nullptr);
 int phde_gram_seq(phde_ctx *ctx, const double *C, int k, double *M);
 int phde_cgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, const double *deg, float *S, int k,
                     int *h_state, double *h_dlog);
@@ -34,7 +35,7 @@ int phde_bcgs2_mixed(phde_ctx *ctx, const int32_t *D, int P, const ull *sumsq, c
                      int *h_state, double *h_dlog);
 int phde_lap_spmm_mixed(phde_ctx *ctx, const double *deg, const float *S, float *LS, int k);
 int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double *M);
-int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X);
+int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X, double *norm2);
 int phde_default_pivot_model(const float **w, int *count);
 int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const int32_t *d_d0,
                           std::vector<int64_t> &h_cand, std::vector<float> &h_score);
@@ -568,17 +569,18 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   double *X = (double *)phde_buf(ctx, "layout.X", sizeof(double) * n * c);
   if (!X) return PHDE_ERR_OOM;
   double *rqd = (double *)phde_buf(ctx, "layout.rq", sizeof(double) * PHDE_RQ_MAX);
-  if (!rqd) return PHDE_ERR_OOM;
+  double *norm2 = (double *)phde_buf(ctx, "layout.norm2", sizeof(double) * PHDE_MAX_K);
+  if (!rqd || !norm2) return PHDE_ERR_OOM;
   PHDE_CK(ctx, cudaMemsetAsync(rqd, 0, sizeof(double) * PHDE_RQ_MAX, ctx->stream));
   const bool want_rq = ctx->want_rq || o->strategy == PHDE_STRAT_LEARNED;
   if (exact)
     rc = phde_exact_coords(ctx, M, Y, k, c, &eb, X, rqd);  // the quotients come with it, from k x k products
   else if (mixed)
-    rc = phde_coords_mixed(ctx, S32, Y, k, c, X);
+    rc = phde_coords_mixed(ctx, S32, Y, k, c, X, want_rq ? norm2 : nullptr);
   else
-    rc = phde_coords(ctx, Sbuf, Y, k, c, X, !hde);
+    rc = phde_coords(ctx, Sbuf, Y, k, c, X, !hde, want_rq ? norm2 : nullptr);
   if (rc) return rc;
-  if (want_rq && !exact && hde && (rc = phde_rayleigh(ctx, X, c, rqd))) return rc;
+  if (want_rq && !exact && hde && (rc = phde_rayleigh(ctx, M, Y, k, c, norm2, rqd))) return rc;
   PHDE_CK(ctx, cudaMemcpyAsync(coords_out, X, sizeof(double) * n * c, cudaMemcpyDeviceToHost, ctx->stream));
   tm.mark(5);
   if (sources_out && npasses > 0)

@@ -79,6 +79,49 @@ __device__ __forceinline__ bool grid_sync(GridSync *gs, int *err, uint64_t timeo
 }
 
 // ---------------------------------------------------------------------------------------------
+// L2 eviction priorities.  A policy word from createpolicy rides on loads and reductions as a hint: data
+// gathered again and again (a search frontier) is marked evict-last, data streamed once (adjacency lists,
+// write-once records) evict-first, so the streams do not push the reused data out of L2.  Hints only: the
+// values read and written are the same with or without them.
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+// 16 bytes through L2 only (never a possibly stale L1 line: other blocks write these words between grid
+// barriers), with an L2 policy
+__device__ __forceinline__ uint4 ld_cg_hint(const void *p, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.cg.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p), "l"(pol));
+  return v;
+}
+// read-only 16 bytes with an L2 policy
+__device__ __forceinline__ uint4 ld_nc_hint16(const void *p, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p), "l"(pol));
+  return v;
+}
+// read-only 4 bytes (the adjacency) with an L2 policy
+__device__ __forceinline__ uint32_t ld_nc_hint(const uint32_t *p, uint64_t pol) {
+  uint32_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+// OR-reduction in L2 (no value returned) with an L2 policy
+__device__ __forceinline__ void red_or_hint(unsigned long long *p, unsigned long long v, uint64_t pol) {
+  asm volatile("red.global.or.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+
+// ---------------------------------------------------------------------------------------------
 // Reductions.
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {

@@ -152,8 +152,9 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
 int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double *M);
 int phde_exact_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, ExactBasis *eb, double *X,
                       double *rq);
-// Rayleigh quotients of the first min(c, PHDE_RQ_MAX) coordinate columns of X (device) into rq (device).
-int phde_rayleigh(phde_ctx *ctx, const double *X, int c, double *rq);
+// Rayleigh quotients of the first min(c, PHDE_RQ_MAX) coordinates X = S Y: y^T M y / ||S y||^2 (device arrays),
+// into rq (device).
+int phde_rayleigh(phde_ctx *ctx, const double *M, const double *Y, int k, int c, const double *norm2, double *rq);
 int phde_exact_basis(phde_ctx *ctx, const ZSrc &src, int k, const ExactBasis *eb, double *S);
 
 // ---- drawing (draw.cu) ----

@@ -766,8 +766,9 @@ __global__ void __launch_bounds__(128) coords_kernel(const double *M, const doub
   }
 }
 
-// X[:, t] /= ||X[:, t]||: each block sums the per-block partials itself (block-wide, fixed order), then scales.
-__global__ void scale_coords_kernel(double *X, int64_t n, int c, const double *part, int nparts) {
+// X[:, t] /= ||X[:, t]||: each block sums the per-block partials itself (block-wide, fixed order), then scales;
+// block 0 also reports ||X[:, t]||^2 before the scaling (norm2, optional).
+__global__ void scale_coords_kernel(double *X, int64_t n, int c, const double *part, int nparts, double *norm2) {
   __shared__ double inv[PHDE_MAX_K];
   __shared__ double red[32];
   for (int t = 0; t < c; t++) {
@@ -775,6 +776,7 @@ __global__ void scale_coords_kernel(double *X, int64_t n, int c, const double *p
     for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += part[(int64_t)b * c + t];
     s = block_sum(s, red);
     if (threadIdx.x == 0) inv[t] = 1.0 / sqrt(s);
+    if (norm2 && blockIdx.x == 0 && threadIdx.x == 0) norm2[t] = s;
   }
   __syncthreads();
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * c;
@@ -1042,7 +1044,7 @@ int phde_centre(phde_ctx *ctx, const int32_t *D, int k, int pivotmds, double *C)
   return PHDE_OK;
 }
 
-int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X, int seq) {
+int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, double *X, int seq, double *norm2) {
   const int threads = 256;
   if (seq) {
     double *part = (double *)phde_buf(ctx, "coords.part", sizeof(double) * c);
@@ -1051,7 +1053,7 @@ int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, d
     PHDE_LAUNCHED(ctx);
     colnorm_seq_kernel<<<c, 32, 0, ctx->stream>>>(X, ctx->n, part);
     PHDE_LAUNCHED(ctx);
-    scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, 1);
+    scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, 1, norm2);
     PHDE_LAUNCHED(ctx);
     return PHDE_OK;
   }
@@ -1065,7 +1067,7 @@ int phde_coords(phde_ctx *ctx, const double *M, const double *Y, int k, int c, d
                                     (int)std::max<size_t>(smem, 48 * 1024)));
   coords_kernel<<<grid, rows, smem, ctx->stream>>>(M, Y, ctx->n, k, c, X, part);
   PHDE_LAUNCHED(ctx);
-  scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid);
+  scale_coords_kernel<<<grid_for(ctx, ctx->n * c, 256), 256, 0, ctx->stream>>>(X, ctx->n, c, part, grid, norm2);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

@@ -456,15 +456,17 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
       if (row >= 0) {
         Sum16<T> nb;
         nb.zero();
+        // the packed rows are gathered again and again (evict-last in L2), the adjacency streams by once
+        const uint64_t keep = l2_policy_evict_last(), stream = l2_policy_evict_first();
         int64_t e = e0 + gi;
         for (; e + G < e1; e += 2 * G) {
-          const int64_t v0 = __ldg(a.adj + e), v1 = __ldg(a.adj + e + G);
-          const uint4 x0 = __ldg((const uint4 *)(Z + v0 * KP) + pi);
-          const uint4 x1 = __ldg((const uint4 *)(Z + v1 * KP) + pi);
+          const int64_t v0 = ld_nc_hint(a.adj + e, stream), v1 = ld_nc_hint(a.adj + e + G, stream);
+          const uint4 x0 = ld_nc_hint16((const uint4 *)(Z + v0 * KP) + pi, keep);
+          const uint4 x1 = ld_nc_hint16((const uint4 *)(Z + v1 * KP) + pi, keep);
           nb.add(x0);
           nb.add(x1);
         }
-        if (e < e1) nb.add(__ldg((const uint4 *)(Z + (int64_t)__ldg(a.adj + e) * KP) + pi));
+        if (e < e1) nb.add(ld_nc_hint16((const uint4 *)(Z + (int64_t)ld_nc_hint(a.adj + e, stream) * KP) + pi, keep));
 #pragma unroll
         for (int m = LPR; m < 32; m <<= 1) nb.add_from(m);
         if (gi == 0) {
@@ -720,64 +722,19 @@ __global__ void unit_scale_kernel(double *X, int64_t n, int c, const double *par
     X[e] = X[e] * inv[e / n];
 }
 
-// Rayleigh quotients of the coordinate columns X (column-major n x c, c <= PHDE_RQ_MAX) on the uploaded graph:
-// per block, sum_i x_i (d_i x_i - sum_j x_j) and sum_i x_i^2 for each column, a warp per row.
-__global__ void __launch_bounds__(256) rq_rows_kernel(const int64_t *off, const uint32_t *adj, const int32_t *w,
-                                                      const double *X, int64_t n, int c, double *part) {
+// Rayleigh quotients of the coordinates X = S Y (before their unit scaling): x_j^T L x_j = y_j^T M y_j with
+// M = S^T L S (the matrix handed to the eigensolver), over ||x_j||^2 (the coordinate kernels' own sum).
+__global__ void rq_gram_kernel(const double *M, const double *Y, int k, int c, const double *norm2, double *rq) {
   __shared__ double red[32];
-  const int lane = threadIdx.x & 31;
-  double num[PHDE_RQ_MAX], den[PHDE_RQ_MAX];
-#pragma unroll
-  for (int j = 0; j < PHDE_RQ_MAX; j++) num[j] = den[j] = 0;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = gw; i < n; i += nwarp) {
-    const int64_t e0 = off[i], e1 = off[i + 1];
-    double s[PHDE_RQ_MAX], dsum = 0;
-#pragma unroll
-    for (int j = 0; j < PHDE_RQ_MAX; j++) s[j] = 0;
-    for (int64_t e = e0 + lane; e < e1; e += 32) {
-      const int64_t v = adj[e];
-      const double we = w ? (double)w[e] : 1.0;
-      dsum += we;
-#pragma unroll
-      for (int j = 0; j < PHDE_RQ_MAX; j++)
-        if (j < c) s[j] = fma(we, X[v + (int64_t)j * n], s[j]);
+  for (int j = 0; j < c && j < PHDE_RQ_MAX; j++) {
+    double num = 0;
+    for (int p = threadIdx.x; p < k; p += blockDim.x) {
+      double t = 0;
+      for (int q = 0; q < k; q++) t = fma(M[p + (int64_t)q * k], Y[q + (int64_t)j * k], t);
+      num = fma(Y[p + (int64_t)j * k], t, num);
     }
-    dsum = warp_sum(dsum);
-#pragma unroll
-    for (int j = 0; j < PHDE_RQ_MAX; j++)
-      if (j < c) {
-        const double t = warp_sum(s[j]);
-        if (lane == 0) {
-          const double xi = X[i + (int64_t)j * n];
-          num[j] = fma(xi, dsum * xi - t, num[j]);
-          den[j] = fma(xi, xi, den[j]);
-        }
-      }
-  }
-#pragma unroll
-  for (int j = 0; j < PHDE_RQ_MAX; j++)
-    if (j < c) {
-      const double a = block_sum(num[j], red);
-      const double b = block_sum(den[j], red);
-      if (threadIdx.x == 0) {
-        part[(int64_t)blockIdx.x * 2 * PHDE_RQ_MAX + j] = a;
-        part[(int64_t)blockIdx.x * 2 * PHDE_RQ_MAX + PHDE_RQ_MAX + j] = b;
-      }
-    }
-}
-
-__global__ void rq_finish_kernel(const double *part, int nparts, int c, double *rq) {
-  __shared__ double red[32];
-  for (int j = 0; j < c; j++) {
-    double a = 0, b = 0;
-    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
-      a += part[(int64_t)p * 2 * PHDE_RQ_MAX + j];
-      b += part[(int64_t)p * 2 * PHDE_RQ_MAX + PHDE_RQ_MAX + j];
-    }
-    a = block_sum(a, red);
-    b = block_sum(b, red);
-    if (threadIdx.x == 0) rq[j] = a / b;
+    num = block_sum(num, red);
+    if (threadIdx.x == 0) rq[j] = num / norm2[j];
   }
 }
 
@@ -1015,17 +972,10 @@ int phde_exact_basis(phde_ctx *ctx, const ZSrc &src, int k, const ExactBasis *eb
   return PHDE_OK;
 }
 
-// Rayleigh quotients x_j^T L x_j / x_j^T x_j of the first min(c, PHDE_RQ_MAX) columns of X (device), into rq
-// (device, PHDE_RQ_MAX doubles).
-int phde_rayleigh(phde_ctx *ctx, const double *X, int c, double *rq) {
-  const int cc = std::min(c, PHDE_RQ_MAX);
-  const int grid = grid_n(ctx, ctx->n * 32, 256, 4);
-  double *part = (double *)phde_buf(ctx, "rq.part", sizeof(double) * (size_t)grid * 2 * PHDE_RQ_MAX);
-  if (!part) return PHDE_ERR_OOM;
-  rq_rows_kernel<<<grid, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, ctx->weighted ? ctx->d_w : nullptr, X, ctx->n,
-                                                cc, part);
-  PHDE_LAUNCHED(ctx);
-  rq_finish_kernel<<<1, 256, 0, ctx->stream>>>(part, grid, cc, rq);
+// Rayleigh quotients of the first min(c, PHDE_RQ_MAX) coordinates from M, Y and the pre-scaling column norms
+// (device arrays), into rq (device).
+int phde_rayleigh(phde_ctx *ctx, const double *M, const double *Y, int k, int c, const double *norm2, double *rq) {
+  rq_gram_kernel<<<1, 256, 0, ctx->stream>>>(M, Y, k, c, norm2, rq);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

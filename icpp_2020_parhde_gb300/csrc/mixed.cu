@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(COORD_ROWS) coords32_kernel(const float *S, co
 
 // X[:, t] /= ||X[:, t]||: each block sums the per-block partials itself (a block-wide reduction, the same
 // fixed order in every block), then scales its share.
-__global__ void scale32_kernel(double *X, int64_t n, int c, const double *part, int nparts) {
+__global__ void scale32_kernel(double *X, int64_t n, int c, const double *part, int nparts, double *norm2) {
   __shared__ double inv[COORD_MAXC];
   __shared__ double red[32];
   for (int t = 0; t < c; t++) {
@@ -530,6 +530,7 @@ __global__ void scale32_kernel(double *X, int64_t n, int c, const double *part, 
     for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += part[(int64_t)b * c + t];
     s = block_sum(s, red);
     if (threadIdx.x == 0) inv[t] = 1.0 / sqrt(s);
+    if (norm2 && blockIdx.x == 0 && threadIdx.x == 0) norm2[t] = s;  // ||X[:, t]||^2 before the scaling
   }
   __syncthreads();
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * c;
@@ -663,7 +664,7 @@ int phde_gram_mixed(phde_ctx *ctx, const float *A, const float *B, int k, double
   return PHDE_OK;
 }
 
-int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X) {
+int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int c, double *X, double *norm2) {
   const int grid = grid_of(ctx, ctx->n, COORD_ROWS, 8);
   double *part = (double *)phde_buf(ctx, "coords32.part", sizeof(double) * grid * (size_t)COORD_MAXC);
   if (!part) return PHDE_ERR_OOM;
@@ -677,7 +678,7 @@ int phde_coords_mixed(phde_ctx *ctx, const float *S, const double *Y, int k, int
                                                              X + (int64_t)t0 * ctx->n, part);
     PHDE_LAUNCHED(ctx);
     scale32_kernel<<<grid_of(ctx, ctx->n * cg, 256, 8), 256, 0, ctx->stream>>>(X + (int64_t)t0 * ctx->n, ctx->n, cg,
-                                                                               part, grid);
+                                                                               part, grid, norm2 ? norm2 + t0 : nullptr);
     PHDE_LAUNCHED(ctx);
   }
   return PHDE_OK;

@@ -74,6 +74,22 @@ struct MsArgs {
 };
 
 // Frontier words of one vertex through the L2 (other blocks wrote them during the previous level).
+// Frontier words of one vertex, kept in L2 (evict-last): every level gathers them from many neighbours.
+template <int W>
+__device__ __forceinline__ void ld_front(const ull *p, ull (&x)[W], uint64_t keep) {
+  if constexpr (W == 4 || W == 2) {
+#pragma unroll
+    for (int h = 0; h < W / 2; h++) {
+      const uint4 a = ld_cg_hint(p + 2 * h, keep);
+      x[2 * h] = ((ull)a.y << 32) | a.x;
+      x[2 * h + 1] = ((ull)a.w << 32) | a.z;
+    }
+  } else {
+#pragma unroll
+    for (int w = 0; w < W; w++) x[w] = __ldcg(p + w);
+  }
+}
+
 template <int W>
 __device__ __forceinline__ void ld_words(const ull *p, ull (&x)[W]) {
   if constexpr (W == 4) {
@@ -117,7 +133,7 @@ __device__ __forceinline__ bool ms_group_finalise(const MsArgs &a, int64_t v, co
   for (int i = 0; i < 2 * W; i++) {
     const int gi = gl + 8 * (i & 1);
     const unsigned nib = (unsigned)(nw[i >> 1] >> (4 * gi)) & 15u;
-    if (nib) atomicOr(row + gl + 8 * i, nibble_lanes(nib, val));  // result unused: a reduction in L2
+    if (nib) red_or_hint(row + gl + 8 * i, nibble_lanes(nib, val), l2_policy_evict_first());  // a reduction in L2
   }
 #pragma unroll
   for (int w = 0; w < W; w++)
@@ -180,14 +196,15 @@ __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full
   ull acc[W];
 #pragma unroll
   for (int w = 0; w < W; w++) acc[w] = 0ull;
+  const uint64_t stream = l2_policy_evict_first(), keep = l2_policy_evict_last();
   if (act && !sat)
     for (int64_t e = e0 + gl; e < e1; e += 2 * MS_GROUP) {
       const int64_t e2 = e + MS_GROUP;
-      const uint32_t u0 = __ldg(a.adj + e);
-      const uint32_t u1 = e2 < e1 ? __ldg(a.adj + e2) : u0;
+      const uint32_t u0 = ld_nc_hint(a.adj + e, stream);
+      const uint32_t u1 = e2 < e1 ? ld_nc_hint(a.adj + e2, stream) : u0;
       ull x0[W], x1[W];
-      ld_words<W>(fcur + (int64_t)u0 * W, x0);
-      ld_words<W>(fcur + (int64_t)u1 * W, x1);
+      ld_front<W>(fcur + (int64_t)u0 * W, x0, keep);
+      ld_front<W>(fcur + (int64_t)u1 * W, x1, keep);
 #pragma unroll
       for (int w = 0; w < W; w++) acc[w] |= x0[w] | x1[w];
     }
@@ -388,9 +405,10 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         acc[w] = 0ull;
       }
       if (sat) continue;  // the row's finalisation writes zero new bits either way
+      const uint64_t stream = l2_policy_evict_first(), keep = l2_policy_evict_last();
       for (int64_t e = e0 + lane; e < e1; e += 32) {
         ull x[W];
-        ld_words<W>(fcur + (int64_t)__ldg(a.adj + e) * W, x);
+        ld_front<W>(fcur + (int64_t)ld_nc_hint(a.adj + e, stream) * W, x, keep);
 #pragma unroll
         for (int w = 0; w < W; w++) acc[w] |= x[w];
       }

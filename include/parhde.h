@@ -298,7 +298,9 @@ int64_t phde_launch_count(const phde_ctx *ctx);
  * inputs return PHDE_ERR_TOO_LARGE with a message on stderr.  The call allocates nothing, waits for
  * its own kernel on `stream`, and returns PHDE_OK or PHDE_ERR_TIMEOUT.  All calls share the scratch:
  * calls whose kernels overlap on the GPU race and must be serialised by the caller.  The first call on
- * a device looks up the scratch address (one-time set-up); make it before any stream capture. */
+ * a device looks up the scratch address (one-time set-up); make it before any stream capture.  The address
+ * is kept for the life of the process: after a cudaDeviceReset of that device the module is loaded again
+ * elsewhere, so a process that resets a device must not call this entry point on it afterwards. */
 #define PHDE_NOALLOC_MAX_VERTICES 1048576
 int phde_bfs_noalloc(const int64_t *d_offsets, const uint32_t *d_adj, int64_t n, int64_t nnz, int64_t source,
                      int32_t *d_dist, void *stream);

@@ -91,3 +91,23 @@ def test_block_per_graph_kcenters_matches_union(monkeypatch):
         cb.close()
     for a, b in zip(out["union"], out["blocks"]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("k,c", [(10, 2), (20, 3)])
+def test_batched_vs_fp64_oracle(k, c):
+    """Every graph of a batch against the FP64 oracle (the reference algorithm with the exact eigensolver) laid
+    out on its own: the same pivots, Rayleigh quotients within the mixed path's 0.1 %, and the coordinate
+    subspace within 1e-3 (principal cosines)."""
+    from oracle import oracle as orc
+    gs = batch_graphs()
+    cb = Context(0)
+    cb.upload_batch(gs)
+    xs, st = cb.layout_batched(k, c)
+    cs = Context(0)
+    for g, xb in zip(gs, xs):
+        L = orc.layout(g, "ParHDE", "Kcenters", k, c, eig="exact", nthreads=4)
+        assert L.status == 0
+        cs.upload(g)
+        assert np.array_equal(cs.kcenters(3 * k, 0, want_dist=False)[1], L.sources[: 3 * k])
+        np.testing.assert_allclose(rayleigh(g, xb), rayleigh(g, L.coords), rtol=1e-3)
+        assert principal_cosines(xb, L.coords).min() > 1 - 1e-3

@@ -176,3 +176,22 @@ def test_cluster_power_iteration_matches_single_cta_bitwise(gpu_ctx, monkeypatch
         assert a.stats["eig_iters"] == b.stats["eig_iters"]
         assert np.array_equal(a.evecs, b.evecs) and np.array_equal(a.evals, b.evals)
         assert np.array_equal(a.coords, b.coords)
+
+
+def test_wparhde_above_2_20_vertices_vs_oracle(gpu_ctx):
+    """A weighted 104^3 grid (1,124,864 vertices): graphs of 2^20 vertices or more take the SSSP's narrow band
+    (eight times the mean weight) and two CTAs per SM.  Distances, pivots and the layout against the oracle."""
+    g = graphs.grid3d(104, seed=9)
+    assert g.n >= 1 << 20
+    gpu_ctx.upload(g)
+    r = gpu_ctx.layout("wParHDE", "Kcenters", 20, 2, extra=True)
+    L = orc.layout(g, "wParHDE", "Kcenters", 20, 2, nthreads=16)
+    assert L.status == 0
+    assert np.array_equal(r.sources, L.sources)
+    assert r.stats["naccepted"] == L.stats.naccepted and r.stats["ndiscarded"] == L.stats.ndiscarded
+    d = gpu_ctx.distances(r.sources[:3])
+    for i in range(3):
+        assert np.array_equal(d[:, i], orc.sssp(g, int(r.sources[i]), parallel=True))
+    np.testing.assert_allclose(r.gram, L.M, rtol=0, atol=1e-7 * np.abs(L.M).max())
+    if not _degenerate(L.M, 2, largest=False, rel=1e-5):
+        np.testing.assert_allclose(r.coords, L.coords, rtol=0, atol=1e-6)

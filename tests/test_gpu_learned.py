@@ -87,7 +87,10 @@ def test_rayleigh_quotients_in_stats(gpu_ctx, precision):
     gpu_ctx.upload(g)
     r = gpu_ctx.layout("ParHDE", "Learned", 12, 3, precision=precision, eig="exact")
     assert r.stats["pivot_outcome"] == 1
-    np.testing.assert_allclose(r.stats["rayleigh"][:3], rayleigh(g, r.coords), rtol=1e-9)
+    # y^T (S^T L S) y / ||S y||^2 from the pipeline's own k x k matrix: FP64-exact for the exact-Gram and FP64
+    # paths; the mixed path's S^T L S carries its FP32 products
+    tol = 1e-5 if precision == "mixed" else 1e-9
+    np.testing.assert_allclose(r.stats["rayleigh"][:3], rayleigh(g, r.coords), rtol=tol)
     assert r.stats["rayleigh"][3:] == [0.0] * 5
 
 

@@ -85,3 +85,28 @@ def test_blocked_cgs2_discards_like_the_oracle(gpu_ctx):
     assert r.stats["ndiscarded"] == L.stats.ndiscarded
     assert r.stats["naccepted"] == L.stats.naccepted == k
     np.testing.assert_allclose(rayleigh(g, r.coords), rayleigh(g, L.coords), rtol=1e-3)
+
+
+@pytest.mark.parametrize("make,k,c", [
+    (lambda: graphs.rmat(16, seed=4), 50, 3),
+    (lambda: graphs.rmat(17, seed=5), 64, 3),
+    (lambda: graphs.rgg(80000, dim=3, avg_degree=12, seed=6), 50, 3),
+    (lambda: graphs.rgg(80000, dim=3, avg_degree=12, seed=7), 64, 3),
+], ids=["rmat16-k50", "rmat17-k64", "rgg3d-k50", "rgg3d-k64"])
+def test_mixed_vs_fp64_oracle_at_benchmark_k(gpu_ctx, make, k, c):
+    """The k the benchmark runs (50 and 64): the blocked CGS2 in FP32 on up to 64 nearly collinear distance
+    columns.  Stated error against the FP64 oracle (same pivots, exact eigensolver): the accept/discard count, the
+    eigenvalues of S^T L S within 1e-3 relative, every coordinate's Rayleigh quotient within 0.1 %, and the
+    coordinate subspace within 1e-3 (principal cosines)."""
+    g = make()
+    gpu_ctx.upload(g)
+    r = gpu_ctx.layout("ParHDE", "Kcenters", k, c, precision="mixed", eig="exact", extra=True)
+    L = orc.layout(g, "ParHDE", "Kcenters", k, c, eig="exact", nthreads=8)
+    assert L.status == 0
+    assert np.array_equal(r.sources, L.sources)
+    assert r.stats["naccepted"] == L.stats.naccepted == k and r.stats["ndiscarded"] == L.stats.ndiscarded
+    w_m = np.linalg.eigvalsh(0.5 * (r.gram + r.gram.T))
+    w_o = np.linalg.eigvalsh(0.5 * (L.M + L.M.T))
+    np.testing.assert_allclose(w_m, w_o, rtol=1e-3, atol=1e-3 * np.abs(w_o).max())
+    np.testing.assert_allclose(rayleigh(g, r.coords), rayleigh(g, L.coords), rtol=1e-3)
+    assert principal_cosines(r.coords, L.coords).min() > 1 - 1e-3

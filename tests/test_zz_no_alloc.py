@@ -12,6 +12,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
+from icpp_2020_parhde_gb300 import graphs
+
 pytestmark = pytest.mark.gpu
 
 
@@ -25,6 +27,7 @@ def _setup(g):
 
 def test_noalloc_bfs_matches_existing_entry_point_twice():
     from icpp_2020_parhde_gb300 import Context, _lib, graphs
+    from oracle import oracle as orc
 
     L = _lib.load()
     g = graphs.rmat(16, seed=2)
@@ -41,8 +44,28 @@ def test_noalloc_bfs_matches_existing_entry_point_twice():
         rc = L.phde_bfs_noalloc(off.data_ptr(), adj.data_ptr(), g.n, g.nnz, s, dist.data_ptr(), stream)
         assert rc == 0
         torch.cuda.synchronize()
-        assert np.array_equal(dist.cpu().numpy(), want[:, i])
+        got = dist.cpu().numpy()
+        assert np.array_equal(got, want[:, i])
+        assert np.array_equal(got, orc.bfs(g, s))  # and the oracle's BFS, not only the library's own
     assert torch.cuda.mem_get_info()[0] == free0  # the calls allocated no device memory
+
+
+@pytest.mark.parametrize("make", [lambda: graphs.mesh(900, 40, seed=4), lambda: graphs.path_graph(5000)],
+                         ids=["long-mesh", "path"])
+def test_noalloc_bfs_matches_oracle_on_long_searches(make):
+    """Graphs with hundreds to thousands of levels, so the search switches between top-down and bottom-up
+    steps many times, against the oracle's BFS, on two calls in a row from different sources."""
+    from icpp_2020_parhde_gb300 import _lib
+    from oracle import oracle as orc
+
+    L = _lib.load()
+    g = make()
+    torch, off, adj, dist = _setup(g)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for s in (0, g.n - 1):
+        assert L.phde_bfs_noalloc(off.data_ptr(), adj.data_ptr(), g.n, g.nnz, s, dist.data_ptr(), stream) == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(dist.cpu().numpy(), orc.bfs(g, s))
 
 
 def test_noalloc_bfs_rejects_graphs_beyond_capacity():
