@@ -14,9 +14,13 @@ static int env_eig() {
   return (e && !strcmp(e, "exact")) ? PHDE_EIG_EXACT : PHDE_EIG_POWER;
 }
 
-static int env_precision() {
+// PHDE_PRECISION=mixed|exact selects the ParHDE class's dense stages; the other classes keep FP64
+static int env_precision(int algo) {
   const char *e = getenv("PHDE_PRECISION");
-  return (e && !strcmp(e, "mixed")) ? PHDE_PREC_MIXED : PHDE_PREC_FP64;
+  if (!e || algo != PHDE_ALGO_PARHDE) return PHDE_PREC_FP64;
+  if (!strcmp(e, "mixed")) return PHDE_PREC_MIXED;
+  if (!strcmp(e, "exact")) return PHDE_PREC_EXACT;
+  return PHDE_PREC_FP64;
 }
 
 DrawingBase::DrawingBase(unsigned int *rowPtrs_, unsigned int *adj_, int32_t *weights_, long n_, long m_,
@@ -53,7 +57,7 @@ int DrawingBase::runAlgorithm(int algo, int strategy, int tries) {
   o.strategy = strategy;
   o.k = numSources;
   o.c = numCoord;
-  o.precision = env_precision();
+  o.precision = env_precision(algo);
   o.eig = env_eig();
   o.seed = 1;
   o.verbose = 1;

@@ -40,6 +40,9 @@ int main(int argc, char **argv) {
         if (!strcmp(optarg, "RandFine")) doRand = 1;
         else if (!strcmp(optarg, "RandCoarse")) doRand = 0;
         else if (!strcmp(optarg, "Kcenters")) doRand = 2;
+        // beyond the reference's strategies (ParHDE only; the help text stays the reference's)
+        else if (!strcmp(optarg, "Learned")) doRand = PHDE_STRAT_LEARNED;
+        else if (!strcmp(optarg, "LearnedChecked")) doRand = PHDE_STRAT_LEARNED_CHECKED;
         else { std::cerr << "Unrecognized Strategy" << std::endl; abort(); }
         break;
       case 'a':

@@ -74,12 +74,17 @@ struct ZgArgs {
   unsigned *maxz;    // [0] largest distance, [1] largest degree
 };
 
+// A slab whose distances all fit a byte goes through byte dot products: zs4[q][col] packs rows 4q .. 4q+3 of a
+// column into one word (dp4a: four rows of Z^T Z per instruction) and ys2[h][col] packs deg * z of rows 2h, 2h+1
+// as two 16-bit halves (dp2a against the bytes of zs4: two rows of Z^T D Z per instruction).  Rows whose
+// deg * z does not fit 16 bits take the one-row 32-bit path.  Every sum is still exact.
 __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
-  extern __shared__ int zsm[];  // [ZG_ROWS][S], then the record column of each Z column of the block
+  extern __shared__ int zsm[];  // [ZG_ROWS][S], zs4[ZG_ROWS/4][S], ys2[ZG_ROWS/2][S], then the record columns
   __shared__ unsigned s_deg[ZG_ROWS];
   __shared__ ull red[32];
   const int S = a.c1 + 4;
-  int *s_rmap = zsm + ZG_ROWS * S;
+  uint32_t *zs4 = (uint32_t *)zsm + ZG_ROWS * S, *ys2 = zs4 + (ZG_ROWS / 4) * S;
+  int *s_rmap = (int *)(ys2 + (ZG_ROWS / 2) * S);
   const int P0 = a.src.P0;
   // Z columns [0, nd) are the ones column and D columns; [nd, c1) record columns (or padding beyond P)
   const int nd = min(a.c1, P0 + 1), nr = a.c1 - nd;
@@ -141,8 +146,66 @@ __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
       atomicMax(a.maxz + 1, (unsigned)mds);
     }
     const ull mz2 = mzs * mzs;
+    const bool bytes = mzs <= 255;  // uniform: the slab's distances fit a byte
+    if (bytes) {
+      // pack (rows past the end and rows for the 32-bit path pack as zeros)
+      for (int e = threadIdx.x; e < (ZG_ROWS / 4) * a.c1; e += ZG_THREADS) {
+        const int q = e / a.c1, col = e - q * a.c1;
+        uint32_t w = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int r = 4 * q + j;
+          if ((ull)max(s_deg[r], 1u) * mzs <= 65535ull) w |= (uint32_t)zsm[r * S + col] << (8 * j);
+        }
+        zs4[q * S + col] = w;
+      }
+      for (int e = threadIdx.x; e < (ZG_ROWS / 2) * a.c1; e += ZG_THREADS) {
+        const int h = e / a.c1, col = e - h * a.c1;
+        uint32_t w = 0;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+          const int r = 2 * h + j;
+          const unsigned d = s_deg[r];
+          if ((ull)max(d, 1u) * mzs <= 65535ull) w |= ((uint32_t)zsm[r * S + col] * d) << (16 * j);
+        }
+        ys2[h * S + col] = w;
+      }
+      __syncthreads();
+      for (int q = 0; q < ZG_ROWS / 4; q++) {
+        ull b = 0;  // bound of the quad's light rows
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int r = 4 * q + j;
+          const unsigned d = s_deg[r];
+          if (r < rows && (ull)max(d, 1u) * mzs <= 65535ull) b += (ull)max(d, 1u) * mz2;
+        }
+        if (b == 0) continue;
+        if (run + b >= B32) {
+          flush();
+          run = 0;
+        }
+        run += b;
+        if (active) {
+          const uint4 zp = *(const uint4 *)(zs4 + q * S + 4 * pb);
+          const uint4 zq = *(const uint4 *)(zs4 + q * S + 4 * qb);
+          const uint4 y0 = *(const uint4 *)(ys2 + (2 * q) * S + 4 * pb);
+          const uint4 y1 = *(const uint4 *)(ys2 + (2 * q + 1) * S + 4 * pb);
+          const uint32_t p4[4] = {zp.x, zp.y, zp.z, zp.w}, q4[4] = {zq.x, zq.y, zq.z, zq.w};
+          const uint32_t ya[4] = {y0.x, y0.y, y0.z, y0.w}, yb[4] = {y1.x, y1.y, y1.z, y1.w};
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              aI[i][j] = __dp4a(p4[i], q4[j], aI[i][j]);
+              aD[i][j] = __dp2a_lo(ya[i], q4[j], aD[i][j]);
+              aD[i][j] = __dp2a_hi(yb[i], q4[j], aD[i][j]);
+            }
+        }
+      }
+    }
     for (int r = 0; r < rows; r++) {
       const unsigned d = s_deg[r];
+      if (bytes && (ull)max(d, 1u) * mzs <= 65535ull) continue;  // done above
       const ull b = (ull)max(d, 1u) * mz2;  // every product of this row is at most b
       const int *zr = zsm + r * S;
       if (b >= B32) {  // a row whose products may not fit 32 bits: 64-bit atomics directly (rare hubs)
@@ -473,25 +536,32 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
           const uint4 own = __ldg((const uint4 *)(Z + row * KP) + pi);
           const int deg = diag ? (int)(a.off[row + 1] - a.off[row]) : 0;
 #pragma unroll
-          for (int c = 0; c < V; c++) {
-            const int zi = slice_val<T>(own, c);
-            const int r = deg * zi - nb.get(c);
-            zs[slot * SL + pi * V + c] = zi;
-            rs[slot * SL + pi * V + c] = r;
-            zm = max(zm, (unsigned)zi);
-            rm = max(rm, (unsigned)abs(r));
+          for (int c4 = 0; c4 < V; c4 += 4) {
+            int zi[4], r[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              zi[c] = slice_val<T>(own, c4 + c);
+              r[c] = deg * zi[c] - nb.get(c4 + c);
+              zm = max(zm, (unsigned)zi[c]);
+              rm = max(rm, (unsigned)abs(r[c]));
+            }
+            *(int4 *)(zs + slot * SL + pi * V + c4) = make_int4(zi[0], zi[1], zi[2], zi[3]);
+            *(int4 *)(rs + slot * SL + pi * V + c4) = make_int4(r[0], r[1], r[2], r[3]);
           }
         }
       } else if (gi == 0) {
 #pragma unroll
-        for (int c = 0; c < V; c++) zs[slot * SL + pi * V + c] = rs[slot * SL + pi * V + c] = 0;
+        for (int c4 = 0; c4 < V; c4 += 4) {
+          *(int4 *)(zs + slot * SL + pi * V + c4) = make_int4(0, 0, 0, 0);
+          *(int4 *)(rs + slot * SL + pi * V + c4) = make_int4(0, 0, 0, 0);
+        }
       }
       zm = __reduce_max_sync(PHDE_FULL_MASK, zm);
       rm = __reduce_max_sync(PHDE_FULL_MASK, rm);
       if (lane == 0) s_bnd[slot] = (ull)zm * (ull)rm;
     }
     __syncthreads();
-    const int nit = (int)min((int64_t)LG_ITEMS, items - u0);
+    const int nit = active ? (int)min((int64_t)LG_ITEMS, items - u0) : 0;  // threads without a tile skip it
     for (int slot = 0; slot < nit; slot++) {
       const ull b = s_bnd[slot];
       if (b == 0) continue;
@@ -755,7 +825,7 @@ static int exact_zgram(phde_ctx *ctx, const ZSrc &src, int P, int c0, int c1, ul
   const int nq = (c1 - c0) / 4;
   const int ntiles = nq * (c0 / 4) + nq * (nq + 1) / 2;
   const int gy = (ntiles + ZG_THREADS - 1) / ZG_THREADS;
-  const size_t smem = sizeof(int) * (ZG_ROWS * (size_t)(c1 + 4) + c1);
+  const size_t smem = sizeof(int) * ((ZG_ROWS + ZG_ROWS / 4 + ZG_ROWS / 2) * (size_t)(c1 + 4) + c1);
   PHDE_CK(ctx, cudaFuncSetAttribute(zgram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zgram_kernel, ZG_THREADS, smem));

@@ -68,6 +68,11 @@ struct MsArgs {
   ull *trace;                 // optional [2*trace_cap]: per level end time (ns) and vertices given new bits
   int trace_cap;
   uint32_t *done;             // [n/32] bitmap: saturated with both frontier words zero (or a hub row): skipped
+  // [3][n/32] frontier bitmaps: bit v of fbm[L % 3] <=> vertex v's frontier word of level L is nonzero.  A pull
+  // tests a neighbour's bit (one L1/L2-resident word) before gathering its 32-byte word, so levels with a
+  // small frontier skip most gathers.  Level L reads fbm[L % 3], sets fbm[(L+1) % 3] and clears fbm[(L+2) % 3]
+  // (read during level L-1, written again during level L+1).
+  uint32_t *fbm[3];
   GridSync *gs;
   int *err;
   uint64_t timeout_ns;
@@ -171,10 +176,13 @@ __device__ __forceinline__ bool ms_thread_finalise(const MsArgs &a, int64_t v, c
 // One vertex v pulled by its MS_GROUP-lane group (gl = lane in group): OR of the neighbours' frontier words,
 // new bits finalised.  Every lane of the warp must call it (the group shuffles are warp-wide); lanes whose
 // group has no vertex pass act = false.  Returns through `newbits` whether v got new bits (group leader).
+__device__ __forceinline__ bool fbit(const uint32_t *bm, uint32_t u) { return (__ldcg(bm + (u >> 5)) >> (u & 31)) & 1u; }
+
 template <int W>
 __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full)[W], const ull *fcur, ull *fnext,
-                                               int32_t L, int64_t v, bool act, int gl, bool mark_done,
-                                               bool &newbits, uint32_t &deg) {
+                                               const uint32_t *fbm_cur, uint32_t *fbm_next, bool use_bm, int32_t L,
+                                               int64_t v, bool act, int gl, bool mark_done, bool &newbits,
+                                               uint32_t &deg) {
   newbits = false;
   int64_t e0 = 0, e1 = 0;
   deg = 0;
@@ -202,11 +210,19 @@ __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full
       const int64_t e2 = e + MS_GROUP;
       const uint32_t u0 = ld_nc_hint(a.adj + e, stream);
       const uint32_t u1 = e2 < e1 ? ld_nc_hint(a.adj + e2, stream) : u0;
-      ull x0[W], x1[W];
-      ld_front<W>(fcur + (int64_t)u0 * W, x0, keep);
-      ld_front<W>(fcur + (int64_t)u1 * W, x1, keep);
+      // gather only the neighbours in this level's frontier (their bitmap bit): an empty word adds nothing
+      if (!use_bm || fbit(fbm_cur, u0)) {
+        ull x0[W];
+        ld_front<W>(fcur + (int64_t)u0 * W, x0, keep);
 #pragma unroll
-      for (int w = 0; w < W; w++) acc[w] |= x0[w] | x1[w];
+        for (int w = 0; w < W; w++) acc[w] |= x0[w];
+      }
+      if (e2 < e1 && (!use_bm || fbit(fbm_cur, u1))) {
+        ull x1[W];
+        ld_front<W>(fcur + (int64_t)u1 * W, x1, keep);
+#pragma unroll
+        for (int w = 0; w < W; w++) acc[w] |= x1[w];
+      }
     }
 #pragma unroll
   for (int w = 0; w < W; w++)
@@ -217,17 +233,13 @@ __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full
     if (sat) {
       // saturated: clear this level's output word; once the current word is empty too, the vertex is
       // finished for the rest of the sweep
-      ull cur[W];
-      ld_words<W>(fcur + v * W, cur);
-      bool empty = true;
 #pragma unroll
-      for (int w = 0; w < W; w++) {
+      for (int w = 0; w < W; w++)
         if (w == gl) fnext[v * W + w] = 0ull;
-        empty &= cur[w] == 0ull;
-      }
-      if (mark_done && empty && gl == 0) atomicOr(a.done + (v >> 5), 1u << (v & 31));
+      if (mark_done && gl == 0 && !fbit(fbm_cur, (uint32_t)v)) atomicOr(a.done + (v >> 5), 1u << (v & 31));
     } else if (ms_group_finalise<W>(a, v, acc, s, fnext, L, gl) && gl == 0) {
       newbits = true;
+      atomicOr(fbm_next + (v >> 5), 1u << (v & 31));
     }
   }
 }
@@ -251,6 +263,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       const int64_t s = a.src[b];
       atomicOr(a.seen + s * W + (b >> 6), 1ull << (b & 63));
       atomicOr(a.front[0] + s * W + (b >> 6), 1ull << (b & 63));
+      atomicOr(a.fbm[0] + (s >> 5), 1u << (s & 31));
       a.R[s * a.RW + a.col0 + b] = 1;  // level 0
     }
   for (int64_t h = gt; h < a.nheavy; h += gts) {
@@ -280,6 +293,12 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
     }
     const ull *fcur = a.front[L & 1];
     ull *fnext = a.front[(L + 1) & 1];
+    const uint32_t *fbm_cur = a.fbm[L % 3];
+    uint32_t *fbm_next = a.fbm[(L + 1) % 3];
+    {
+      uint32_t *fbm_old = a.fbm[(L + 2) % 3];
+      for (int64_t i = gt; i < (n + 31) / 32; i += gts) fbm_old[i] = 0u;
+    }
     const int so = L & 3, sf = (L + 3) & 3, sz = (L + 2) & 3;
     // slot (L+1)%4 and the other candidate counter were last used by level L-1, finished at its barrier
     if (gt == 0) {
@@ -293,6 +312,9 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
     // the frontier's totals: its list counter if the previous level built one, else its count
     const ull fstat = built_f ? __ldcg(a.lctr + sf) : __ldcg(a.lstat + sf);
     const uint32_t fedges = (uint32_t)(fstat & 0xffffffffull);
+    // test the frontier bitmap before each gather while the frontier holds at most a quarter of the vertices
+    // (above that, most neighbours are in it and the test only lengthens the dependent chain)
+    const bool use_bm = (int64_t)(fstat >> 32) <= n / 4;
     const bool sparse = (int64_t)fedges < a.sparse_edges;
     if (sparse) {
       if (!built_f) {
@@ -355,7 +377,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         const int64_t v = act ? (int64_t)a.cand[i] : 0;
         bool nb;
         uint32_t dv;
-        ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, true, nb, dv);
+        ms_pull_vertex<W>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, v, act, gl, true, nb, dv);
         block_push(nb, (uint32_t)v, dv, a.qv[so], a.qe[so], a.lctr + so, &psc);
       }
     } else {
@@ -386,7 +408,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
           const int64_t v = v0 + (act ? __ffs(rest) - 1 : 0);
           bool nb;
           uint32_t dv;
-          ms_pull_vertex<W>(a, full, fcur, fnext, L, v, act, gl, true, nb, dv);
+          ms_pull_vertex<W>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, v, act, gl, true, nb, dv);
           if (nb) my_stat += (1ull << 32) | (ull)dv;
           for (int j = 0; j < 32 / MS_GROUP && todo; j++) todo &= todo - 1u;
         }
@@ -407,8 +429,10 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       if (sat) continue;  // the row's finalisation writes zero new bits either way
       const uint64_t stream = l2_policy_evict_first(), keep = l2_policy_evict_last();
       for (int64_t e = e0 + lane; e < e1; e += 32) {
+        const uint32_t u = ld_nc_hint(a.adj + e, stream);
+        if (use_bm && !fbit(fbm_cur, u)) continue;
         ull x[W];
-        ld_front<W>(fcur + (int64_t)ld_nc_hint(a.adj + e, stream) * W, x, keep);
+        ld_front<W>(fcur + (int64_t)u * W, x, keep);
 #pragma unroll
         for (int w = 0; w < W; w++) acc[w] |= x[w];
       }
@@ -430,6 +454,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         a.hacc[v * W + w] = 0ull;
       }
       if (ms_thread_finalise<W>(a, v, acc, fnext, L)) {
+        atomicOr(fbm_next + (v >> 5), 1u << (v & 31));
         const uint32_t dv = (uint32_t)(a.off[v + 1] - a.off[v]);
         if (sparse) {
           const ull pos = atomicAdd(a.lctr + so, (1ull << 32) | (ull)dv);
@@ -570,13 +595,15 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
   int *levels = (int *)phde_buf(ctx, "ms.levels", sizeof(int));
   const int64_t nw32 = (n + 31) / 32, lcap = n + 256;  // a level list holds each vertex once; the sources' may repeat
   uint32_t *bms = (uint32_t *)phde_buf(ctx, "ms.done", sizeof(uint32_t) * nw32);
+  uint32_t *fbm = (uint32_t *)phde_buf(ctx, "ms.fbm", sizeof(uint32_t) * 3 * nw32);
   uint32_t *lists = (uint32_t *)phde_buf(ctx, "ms.lists", sizeof(uint32_t) * 8 * lcap);  // qv[4], qe[4]
   uint32_t *cand = (uint32_t *)phde_buf(ctx, "ms.cand", sizeof(uint32_t) * n);
   int32_t *stamp = (int32_t *)phde_buf(ctx, "ms.stamp", sizeof(int32_t) * n);
   // lctr[4], lstat[4], ccount[2], tctr[4]
   const size_t ctr_bytes = sizeof(ull) * 8 + sizeof(unsigned) * 6;
   ull *lctr = (ull *)phde_buf(ctx, "ms.lctr", ctr_bytes);
-  if (!R || !seen || !f0 || !f1 || !hacc || !levels || !bms || !lists || !cand || !stamp || !lctr) return PHDE_ERR_OOM;
+  if (!R || !seen || !f0 || !f1 || !hacc || !levels || !bms || !fbm || !lists || !cand || !stamp || !lctr)
+    return PHDE_ERR_OOM;
   const int64_t *crow, *ce0;
   int64_t nch, chunk;
   int rc0 = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
@@ -604,6 +631,7 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     PHDE_CK(ctx, cudaMemsetAsync(f1, 0, sizeof(ull) * n * W, ctx->stream));  // level 1 writes candidates only
     PHDE_CK(ctx, cudaMemsetAsync(lctr, 0, ctr_bytes, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(bms, 0, sizeof(uint32_t) * nw32, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(fbm, 0, sizeof(uint32_t) * 3 * nw32, ctx->stream));
     PHDE_CK(ctx, cudaMemsetAsync(stamp, 0, sizeof(int32_t) * n, ctx->stream));
     int rc = phde_reset_sync(ctx);
     if (rc) return rc;
@@ -640,6 +668,7 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.trace = trace;
     a.trace_cap = trace_cap;
     a.done = bms;
+    for (int i = 0; i < 3; i++) a.fbm[i] = fbm + (int64_t)i * nw32;
     a.gs = ctx->d_sync;
     a.err = ctx->d_err;
     a.timeout_ns = ctx->timeout_ns;

@@ -46,6 +46,21 @@ def test_exact_vs_reference_goldens(gpu_ctx, case):
     np.testing.assert_allclose(r.coords, ref_xy, rtol=0, atol=COORD_ATOL)
 
 
+def hub_mesh():
+    """A 300 x 300 mesh plus one vertex joined to every mesh vertex: the hub's row has degree 90,000, so its
+    degree times distance needs more than 16 bits and it takes the one-row 32-bit path of the Gram kernel."""
+    from icpp_2020_parhde_gb300.csr_io import CSRGraph
+    g = graphs.mesh(300, 300, seed=12)
+    n = g.n
+    A = sp.csr_matrix((np.ones(g.nnz), g.adj.astype(np.int64), g.offsets.astype(np.int64)), shape=(n, n)).tocoo()
+    hub = np.full(n, n, dtype=np.int64)
+    rows = np.concatenate([A.row, np.arange(n), hub])
+    cols = np.concatenate([A.col, hub, np.arange(n)])
+    B = sp.csr_matrix((np.ones(len(rows)), (rows, cols)), shape=(n + 1, n + 1))
+    B.sort_indices()
+    return CSRGraph(B.indptr.astype(np.uint32), B.indices.astype(np.uint32), None)
+
+
 @pytest.mark.parametrize("make,k,c", [
     (lambda: graphs.rmat(16, seed=7), 64, 3),
     (lambda: graphs.rmat(16, seed=7), 50, 3),
@@ -53,7 +68,8 @@ def test_exact_vs_reference_goldens(gpu_ctx, case):
     (lambda: graphs.mesh(150, 80, seed=31), 130, 3),
     (lambda: graphs.mesh(900, 12, seed=5), 24, 2),   # diameter above 255: 16-bit packed columns
     (lambda: graphs.rmat(14, seed=3), 20, 7),        # more than four coordinates
-], ids=["rmat16-k64", "rmat16-k50", "rgg3d-k64", "mesh-k130", "long-mesh-u16", "rmat14-c7"])
+    (hub_mesh, 20, 2),                               # a row too heavy for the byte dot products
+], ids=["rmat16-k64", "rmat16-k50", "rgg3d-k64", "mesh-k130", "long-mesh-u16", "rmat14-c7", "hub-mesh"])
 def test_exact_vs_fp64_oracle(gpu_ctx, make, k, c):
     g = make()
     gpu_ctx.upload(g)
