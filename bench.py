@@ -660,25 +660,42 @@ def run_batched(args, local, flush_l2):
     cb = Context(local)
     cb.upload_batch(gs)
     out = torch.empty(ntot * c, dtype=torch.float64).pin_memory()
-    _, st0 = cb.layout_batched(k, c, coords_out=out.numpy())  # first call: autotune + capture
-    for _ in range(3):
-        cb.layout_batched(k, c, coords_out=out.numpy())
-    ms = []
     steps = max(3, args.steps // 5)
-    for _ in range(steps):
-        flush_l2()
-        _, st = cb.layout_batched(k, c, coords_out=out.numpy())
-        ms.append(st["ms_total"])
-    xs = [x.copy() for x in cb.layout_batched(k, c, coords_out=out.numpy())[0]]
-    t_b = float(np.mean(ms))
-    e2e = []
-    for _ in range(steps):
-        flush_l2()
-        t1 = time.perf_counter()
-        cb.upload_batch(gs)
-        cb.layout_batched(k, c, coords_out=out.numpy())
-        e2e.append(time.perf_counter() - t1)
+    timing, rqs = {}, {}
+    for strat in ("Kcenters", "Learned"):
+        _, st0 = cb.layout_batched(k, c, coords_out=out.numpy(), strategy=strat)  # tunes (first) / runs uncaptured
+        for _ in range(3):
+            cb.layout_batched(k, c, coords_out=out.numpy(), strategy=strat)   # captures, then replays
+        ms = []
+        for _ in range(steps):
+            flush_l2()
+            _, st = cb.layout_batched(k, c, coords_out=out.numpy(), strategy=strat)
+            ms.append(st["ms_total"])
+        rqs[strat] = cb.batch_rayleigh()
+        if strat == "Kcenters":
+            xs = [x.copy() for x in cb.layout_batched(k, c, coords_out=out.numpy())[0]]
+            st_kc, st0_kc = st, st0
+        e2e = []
+        for _ in range(steps):
+            flush_l2()
+            t1 = time.perf_counter()
+            cb.upload_batch(gs)
+            cb.layout_batched(k, c, coords_out=out.numpy(), strategy=strat)
+            e2e.append(time.perf_counter() - t1)
+        timing[strat] = {"ms_per_batch": float(np.mean(ms)), "e2e_ms_per_batch": float(np.mean(e2e)) * 1e3,
+                         "gpu_launches_per_batch": st["gpu_launches"], "cuda_graph_replay": bool(st["batch_graph_replay"])}
     cb.close()
+    st, st0 = st_kc, st0_kc
+    t_b = timing["Kcenters"]["ms_per_batch"]
+    e2e = [timing["Kcenters"]["e2e_ms_per_batch"] * 1e-3]
+    # the learned pivots' acceptance per graph, against the batch's Kcenters layouts (same precision and solver)
+    ql, qk = rqs["Learned"], rqs["Kcenters"]
+    sum_ratio = ql.sum(axis=1) / qk.sum(axis=1)
+    learned_check = {"graphs": len(gs), "sum_ratio_mean": float(np.mean(sum_ratio)),
+                     "sum_ratio_max": float(np.max(sum_ratio)),
+                     "graphs_within_2pct_sum": int(np.sum(sum_ratio <= 1.02)),
+                     "graphs_within_2pct_each": int(np.sum(np.all(ql <= 1.02 * qk, axis=1))),
+                     "mean_sum_ratio_over_graphs_weighted": float(ql.sum() / qk.sum())}
     cs = Context(local)
     loop = {"kcenters_mixed": 0.0, "plain": 0.0}
     rq_err = []
@@ -697,6 +714,12 @@ def run_batched(args, local, flush_l2):
                       "graphs": len(gs), "n": ntot, "nnz": nnz_tot, "k": k, "c": c},
            "pipeline": "Kcenters, mixed precision, Jacobi; one persistent Kcenters launch + one CUDA graph replay",
            "value": k * nnz_tot / (t_b * 1e-3), "unit": UNIT, "ms_per_batch": t_b, "ms_per_graph": t_b / len(gs),
+           "learned": {"value": k * nnz_tot / (timing["Learned"]["ms_per_batch"] * 1e-3), "unit": UNIT,
+                       **timing["Learned"],
+                       "speedup_vs_kcenters_batched": {
+                           "device": t_b / timing["Learned"]["ms_per_batch"],
+                           "e2e": timing["Kcenters"]["e2e_ms_per_batch"] / timing["Learned"]["e2e_ms_per_batch"]},
+                       "rayleigh_check_vs_kcenters": learned_check},
            "e2e": {"value": k * nnz_tot / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_batch": e2e_ms,
                    "h2d_bytes_per_step": 4 * (ntot + len(gs)) + 4 * nnz_tot, "d2h_bytes_per_step": 8 * ntot * c},
            "loop_ms_per_batch": loop, "speedup_vs_loop": {kk: v / t_b for kk, v in loop.items()},

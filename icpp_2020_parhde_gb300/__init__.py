@@ -188,19 +188,29 @@ class Context:
         self.batch_sizes = [g.n for g in graphs]
         self.n, self.nnz, self.weighted = sum(self.batch_sizes), sum(g.nnz for g in graphs), False
 
-    def layout_batched(self, k: int = 10, c: int = 2, coords_out: np.ndarray | None = None):
-        """phde_layout_batched: (list of per-graph (n_b, c) coordinate arrays, stats dict)."""
-        o = _lib.LayoutOpts(_lib.ALGOS["ParHDE"], _lib.STRATEGIES["Kcenters"], k, c, _lib.PRECISIONS["mixed"],
+    def layout_batched(self, k: int = 10, c: int = 2, coords_out: np.ndarray | None = None,
+                       strategy: str = "Kcenters"):
+        """phde_layout_batched: (list of per-graph (n_b, c) coordinate arrays, stats dict).  strategy "Kcenters" or
+        "Learned"."""
+        o = _lib.LayoutOpts(_lib.ALGOS["ParHDE"], _lib.STRATEGIES[strategy], k, c, _lib.PRECISIONS["mixed"],
                             _lib.EIGS["exact"], 1, 0)
         total = sum(self.batch_sizes)
         out = coords_out if coords_out is not None else np.empty(total * c, dtype=np.float64)
         st = _lib.LayoutStats()
         self._check(self._L.phde_layout_batched(self._h, C.byref(o), _ptr(out, C.c_double), C.byref(st)))
+        self._last_batch_c = c
         res, base = [], 0
         for nb in self.batch_sizes:
             res.append(out[c * base: c * (base + nb)].reshape(c, nb).T)
             base += nb
         return res, st.as_dict()
+
+    def batch_rayleigh(self) -> np.ndarray:
+        """phde_batch_rayleigh: (graphs, c) Rayleigh quotients of the last batched layout."""
+        c = self._last_batch_c
+        rq = np.empty(len(self.batch_sizes) * c, dtype=np.float64)
+        self._check(self._L.phde_batch_rayleigh(self._h, _ptr(rq, C.c_double)))
+        return rq.reshape(-1, c)
 
     def gram_f32(self, A, B, w=None, nsplit: int = 0) -> np.ndarray:
         """phde_gram_f32: A^T diag(w) B (FP64 result) on the tensor cores, for FP32 row-major A (n, p), B (n, q)."""

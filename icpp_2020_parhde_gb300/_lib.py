@@ -29,7 +29,7 @@ EXPORTS = [
     "phde_DeltaStep", "phde_selftest_barrier_timeout", "phde_launch_count", "phde_bfs_noalloc",
     "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched", "phde_write_nxyz",
     "phde_graph_from_entries", "phde_graph_download", "phde_draw", "phde_draw_download", "phde_draw_write_png",
-    "phde_write_png", "phde_gram_f32", "phde_set_pivot_check", "phde_pivot_scores",
+    "phde_write_png", "phde_gram_f32", "phde_set_pivot_check", "phde_pivot_scores", "phde_batch_rayleigh",
 ]
 
 
@@ -125,6 +125,7 @@ def load(path: str | None = None):
     L.phde_pivot_scores.argtypes = [vp, C.POINTER(C.c_float), i32p, i64p, C.c_int]
     L.phde_batch_upload.argtypes = [vp, C.POINTER(GraphDesc), C.c_int]
     L.phde_layout_batched.argtypes = [vp, C.POINTER(LayoutOpts), f64p, C.POINTER(LayoutStats)]
+    L.phde_batch_rayleigh.argtypes = [vp, f64p]
     L.phde_write_nxyz.argtypes = [C.c_char_p, f64p, i64, C.c_int, C.c_int]
     L.phde_graph_from_entries.argtypes = [vp, u32p, u32p, i32p, i64, i64, i64, C.c_int, C.POINTER(CsrInfo)]
     L.phde_graph_download.argtypes = [vp, u32p, u32p, i32p]

@@ -32,6 +32,9 @@ int phde_eigensolve_batched(phde_ctx *ctx, const double *d_M, int N, int c, int 
                             double *d_evals, double *d_Y, int *d_st);
 int phde_run_bfs_batched_blocks(phde_ctx *ctx, int P, const int32_t *d_order, int32_t *d_D, int64_t *d_sources,
                                 unsigned long long *d_sumsq, unsigned long long *d_edges);
+int phde_batch_learned_pivots(phde_ctx *ctx, int P, const float *d_weights, int32_t *D, int64_t *sources,
+                              unsigned long long *sumsq, unsigned long long *edges);
+int phde_default_pivot_model(const float **w, int *count);
 
 namespace {
 
@@ -328,6 +331,23 @@ __global__ void batch_norms_kernel(Seg sg, const double *cpart, int c, int B, do
     inv[i] = 1.0 / sqrt(tot);
   }
 }
+// Rayleigh quotient of every graph's coordinates: y^T M_b y over ||X_b y||^2 = 1 / inv^2 (one warp per graph).
+__global__ void batch_rq_kernel(const double *M, const double *Y, const double *inv, int k, int c, double *rq) {
+  const int b = blockIdx.x, lane = threadIdx.x;
+  const double *Mb = M + (int64_t)b * k * k, *Yb = Y + (int64_t)b * k * c;
+  for (int t = 0; t < c; t++) {
+    double s = 0;
+    for (int p = lane; p < k; p += 32) {
+      double u = 0;
+      for (int q = 0; q < k; q++) u = fma(Mb[p + q * k], Yb[q + t * k], u);
+      s = fma(Yb[p + t * k], u, s);
+    }
+    s = warp_sum(s);
+    const double iv = inv[(int64_t)b * c + t];
+    if (lane == 0) rq[(int64_t)b * c + t] = s * iv * iv;
+  }
+}
+
 __global__ void batch_scale_kernel(const int32_t *gid, const int64_t *vbase, int64_t N, int c, const double *inv,
                                    double *out) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
@@ -422,6 +442,8 @@ extern "C" int phde_batch_upload(phde_ctx *ctx, const phde_graph_desc *graphs, i
                                         "at its nnz; its neighbours must be below its n");
   }
   ctx->batch_B = count;
+  ctx->batch_warm_key = -1;  // a new batch: its buffers are sized anew before any capture
+  ctx->batch_last_c = 0;
   ctx->batch_vbase = vb;
   ctx->batch_ebase = eb;
   // graphs largest first (the one-CTA-per-graph Kcenters takes them in this order)
@@ -452,6 +474,9 @@ struct BatchBufs {
   double *G, *dden, *fpart, *M, *K, *ev, *Y, *cpart, *cinv, *out;
   int *st, *est;
   double *dlog;
+  double *rq;              // [B][c] Rayleigh quotients
+  bool learned = false;    // learned pivots (batch_learned.cu) instead of Kcenters
+  const float *weights = nullptr;  // the pivot model on the device
   Seg sg;
 };
 
@@ -463,7 +488,9 @@ int batch_pipeline(phde_ctx *ctx, const BatchBufs &q, int k, int c) {
   if ((rc = phde_degrees(ctx, q.deg))) return rc;
   // Kcenters: one CTA per graph when the batch has enough graphs to fill the GPU (block barriers only),
   // else the whole-grid batched variant (every pass one BFS of the union)
-  if (ctx->batch_blocks)
+  if (q.learned)
+    rc = phde_batch_learned_pivots(ctx, P, q.weights, q.D, q.src, q.sumsq, q.edges);
+  else if (ctx->batch_blocks)
     rc = phde_run_bfs_batched_blocks(ctx, P, ctx->d_order, q.D, q.src, q.sumsq, q.edges);
   else
     rc = phde_run_bfs_passes(ctx, P, 3, nullptr, q.D, q.src, q.sumsq, q.edges, 1);
@@ -511,6 +538,8 @@ int batch_pipeline(phde_ctx *ctx, const BatchBufs &q, int k, int c) {
   PHDE_LAUNCHED(ctx);
   batch_norms_kernel<<<(B * c + 255) / 256, 256, 0, ctx->stream>>>(q.sg, q.cpart, c, B, q.cinv);
   PHDE_LAUNCHED(ctx);
+  batch_rq_kernel<<<B, 32, 0, ctx->stream>>>(q.M, q.Y, q.cinv, k, c, q.rq);
+  PHDE_LAUNCHED(ctx);
   batch_scale_kernel<<<grid_rows(ctx, N), 256, 0, ctx->stream>>>(ctx->d_gid, ctx->d_vbase, N, c, q.cinv, q.out);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
@@ -542,17 +571,24 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
   if (!ctx) return PHDE_ERR_INVALID;
   if (!o || !coords_out) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout_batched: bad arguments");
   if (ctx->batch_B < 1) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_layout_batched: no batch uploaded");
-  if (o->algo != PHDE_ALGO_PARHDE || o->strategy != PHDE_STRAT_KCENTERS || o->precision != PHDE_PREC_MIXED ||
-      o->eig != PHDE_EIG_EXACT)
+  if (o->algo != PHDE_ALGO_PARHDE || (o->strategy != PHDE_STRAT_KCENTERS && o->strategy != PHDE_STRAT_LEARNED) ||
+      o->precision != PHDE_PREC_MIXED || o->eig != PHDE_EIG_EXACT)
     return phde_fail(ctx, PHDE_ERR_INVALID,
-                     "phde_layout_batched: supports ParHDE with Kcenters pivots, PHDE_PREC_MIXED and PHDE_EIG_EXACT");
+                     "phde_layout_batched: supports ParHDE with Kcenters or learned pivots, PHDE_PREC_MIXED and "
+                     "PHDE_EIG_EXACT");
+  const bool learned = o->strategy == PHDE_STRAT_LEARNED;
   const int k = o->k, c = o->c, B = ctx->batch_B, P = 3 * k;
   if (k < 2 || k > BB) return phde_fail(ctx, PHDE_ERR_K_RANGE, "phde_layout_batched: k must be in 2..32");
   if (c < 1 || c > MAXC || c > k) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout_batched: c must be in 1..min(4, k)");
-  for (int b = 0; b < B; b++)
+  for (int b = 0; b < B; b++) {
     if (ctx->batch_vbase[b + 1] - ctx->batch_vbase[b] <= P)
       return phde_fail(ctx, PHDE_ERR_K_RANGE,
                        "phde_layout_batched: graph " + std::to_string(b) + " has no more vertices than 3k pivots");
+    if (learned && ctx->batch_vbase[b + 1] - ctx->batch_vbase[b] <= PHDE_LEARNED_CANDIDATES)
+      return phde_fail(ctx, PHDE_ERR_K_RANGE,
+                       "phde_layout_batched: learned pivots need more than 256 vertices per graph (graph " +
+                           std::to_string(b) + ")");
+  }
   PHDE_CK(ctx, cudaSetDevice(ctx->device));
   const int64_t N = ctx->n;
   ctx->kernel_ms = 0;
@@ -581,8 +617,23 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
   q.st = (int *)phde_buf(ctx, "batch.st", sizeof(int) * 4 * B);
   q.est = (int *)phde_buf(ctx, "batch.est", sizeof(int) * 2 * B);
   q.dlog = (double *)phde_buf(ctx, "batch.dlog", sizeof(double) * P * B);
+  q.rq = (double *)phde_buf(ctx, "batch.rq", sizeof(double) * B * c);
+  q.learned = learned;
+  if (learned) {  // the model goes to the device before the (captured) sequence, on every call
+    if (ctx->pivot_model.empty()) {
+      const float *w0;
+      int cnt;
+      if (phde_default_pivot_model(&w0, &cnt)) return phde_fail(ctx, PHDE_ERR_INVALID, "built-in pivot model has the wrong size");
+      ctx->pivot_model.assign(w0, w0 + cnt);
+    }
+    float *dw = (float *)phde_buf(ctx, "lpb.w", sizeof(float) * ctx->pivot_model.size());
+    if (!dw) return PHDE_ERR_OOM;
+    PHDE_CK(ctx, cudaMemcpyAsync(dw, ctx->pivot_model.data(), sizeof(float) * ctx->pivot_model.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    q.weights = dw;
+  }
   if (!q.deg || !q.D || !q.src || !q.sumsq || !q.edges || !q.inv || !q.X || !q.S || !q.LS || !q.C || !q.R || !q.G ||
-      !q.dden || !q.M || !q.K || !q.ev || !q.Y || !q.cinv || !q.out || !q.st || !q.est || !q.dlog)
+      !q.dden || !q.M || !q.K || !q.ev || !q.Y || !q.cinv || !q.out || !q.st || !q.est || !q.dlog || !q.rq)
     return PHDE_ERR_OOM;
   PHDE_CK(ctx, cudaMemsetAsync(q.edges, 0, sizeof(ull), ctx->stream));
 
@@ -650,14 +701,20 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
   if ((rc = set_segments(ctx->batch_seg_rows))) return rc;
   const int64_t launches0 = ctx->launches;
   // ---- run: replay the captured graph, or capture it (first call after tuning), or launch directly ----
-  const int key_c = c;
+  const int key_c = c * 8 + o->strategy;  // the captured sequence depends on c and the pivot strategy
   if (ctx->batch_graph && (ctx->batch_graph_c != key_c || ctx->batch_graph_ws != ctx->ws_epoch)) {
     cudaGraphExecDestroy(ctx->batch_graph);
     ctx->batch_graph = nullptr;
   }
   cudaEventRecord(ctx->ev[0], ctx->stream);
-  bool replayed = false;
-  if (ctx->batch_graph) {
+  bool replayed = false, ran = false;
+  if (ctx->batch_warm_key != key_c) {
+    // the first call with this sequence runs it directly (it allocates its buffers); the next one captures it
+    if ((rc = batch_pipeline(ctx, q, k, c))) return rc;
+    ran = true;
+    ctx->batch_warm_key = key_c;
+    ctx->batch_no_graph = false;
+  } else if (ctx->batch_graph) {
     PHDE_CK(ctx, cudaGraphLaunch(ctx->batch_graph, ctx->stream));
     ctx->launches += ctx->batch_graph_launches;
     replayed = true;
@@ -689,7 +746,7 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
       ctx->batch_no_graph = true;
     }
   }
-  if (!replayed && (rc = batch_pipeline(ctx, q, k, c))) return rc;
+  if (!replayed && !ran && (rc = batch_pipeline(ctx, q, k, c))) return rc;
   // the caller's buffer is not part of the captured graph: copy after it
   PHDE_CK(ctx, cudaMemcpyAsync(coords_out, q.out, sizeof(double) * N * c, cudaMemcpyDeviceToHost, ctx->stream));
   cudaEventRecord(ctx->ev[1], ctx->stream);
@@ -713,6 +770,7 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
   }
   if (naccepted_min < k)
     return phde_fail(ctx, PHDE_ERR_TOO_FEW_PIVOTS, "batched layout: a graph has fewer than k independent pivot columns");
+  ctx->batch_last_c = c;
   if (stats) {
     memset(stats, 0, sizeof(*stats));
     stats->status = PHDE_OK;
@@ -727,5 +785,18 @@ extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, dou
     stats->batch_seg_rows = (int)ctx->batch_seg_rows;
     stats->ms_batch_tune = tune ? ctx->batch_tune_ms : 0.0;
   }
+  return PHDE_OK;
+}
+
+// The last phde_layout_batched call's Rayleigh quotients, graph b's coordinate t at rq_out[b * c + t].
+extern "C" int phde_batch_rayleigh(phde_ctx *ctx, double *rq_out) {
+  if (!ctx || !rq_out) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_batch_rayleigh: bad arguments");
+  if (ctx->batch_B < 1 || ctx->batch_last_c < 1)
+    return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_batch_rayleigh: no batched layout computed");
+  const size_t cnt = (size_t)ctx->batch_B * ctx->batch_last_c;
+  const double *rq = (const double *)phde_buf(ctx, "batch.rq", sizeof(double) * cnt);
+  if (!rq) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemcpyAsync(rq_out, rq, sizeof(double) * cnt, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return PHDE_OK;
 }

@@ -38,6 +38,8 @@ struct phde_ctx {
   cudaGraphExec_t batch_graph = nullptr;           // the captured batched pipeline
   int64_t batch_graph_epoch = -1;
   int batch_graph_c = 0;
+  int batch_warm_key = -1;                         // the sequence last run uncaptured (c, strategy)
+  int batch_last_c = 0;                            // coordinates of the last batched layout
   int64_t batch_graph_ws = -1;
   int64_t batch_graph_launches = 0;
   bool batch_no_graph = false;                     // capture failed once: launch directly

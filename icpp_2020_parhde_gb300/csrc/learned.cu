@@ -86,6 +86,40 @@ __global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, cons
   }
 }
 
+// Per-graph maxima of a batch (the disjoint union, graph of each vertex in gid): maxes[3 b .. 3 b + 2].  A warp
+// whose 32 vertices lie in one graph reduces first and adds one atomic per value.
+__global__ void feature_max_batched_kernel(const int64_t *off, const int32_t *d0, const ull *hop2, const int32_t *gid,
+                                           int64_t n, ull *maxes) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n; base += stride) {
+    const int64_t v = base + lane;
+    ull mdeg = 0, mhop = 0, md0 = 0;
+    int g = -1;
+    if (v < n) {
+      mdeg = (ull)(off[v + 1] - off[v]);
+      mhop = hop2[v];
+      md0 = (ull)(d0[v] < 0 ? 0 : d0[v]);
+      g = gid[v];
+    }
+    const int g0 = __shfl_sync(PHDE_FULL_MASK, g, 0);
+    if (__all_sync(PHDE_FULL_MASK, g == g0)) {
+      mdeg = warp_max_u64(mdeg);
+      mhop = warp_max_u64(mhop);
+      md0 = warp_max_u64(md0);
+      if (lane == 0) {
+        atomicMax(maxes + 3 * g0, mdeg);
+        atomicMax(maxes + 3 * g0 + 1, mhop);
+        atomicMax(maxes + 3 * g0 + 2, md0);
+      }
+    } else if (g >= 0) {
+      atomicMax(maxes + 3 * g, mdeg);
+      atomicMax(maxes + 3 * g + 1, mhop);
+      atomicMax(maxes + 3 * g + 2, md0);
+    }
+  }
+}
+
 __global__ void feature_max_kernel(const int64_t *off, const int32_t *d0, const ull *hop2, int64_t n, ull *maxes) {
   __shared__ ull red[32];
   ull mdeg = 0, mhop = 0, md0 = 0;
@@ -110,10 +144,12 @@ __global__ void feature_max_kernel(const int64_t *off, const int32_t *d0, const 
 // output unit's dot product over the 64 hidden units summed across the 16 threads of a vertex group with
 // shuffles; then the sigmoid and the score histogram.
 constexpr int MLP_TILE = 128;
+// gid (batches): the features of vertex v are normalised by its own graph's maxima, maxes[3 gid[v] ..]; no
+// histogram when nbins is 0.
 __global__ void __launch_bounds__(256) mlp_score_kernel(const int64_t *off, const int32_t *d0, const ull *hop2,
                                                         const uint32_t *outw, const ull *maxes, int64_t n,
                                                         const float *weights, float *score, unsigned *hist,
-                                                        int nbins) {
+                                                        int nbins, const int32_t *gid) {
   __shared__ float W1[MLP_H][MLP_IN], b1[MLP_H], b2[MLP_H], w3[MLP_H];
   __shared__ __align__(16) float W2t[MLP_H][MLP_H];  // W2t[i][o] = W2[o][i]
   __shared__ float F[MLP_TILE][MLP_IN + 1];
@@ -142,10 +178,17 @@ __global__ void __launch_bounds__(256) mlp_score_kernel(const int64_t *off, cons
       const int64_t v = t0 + tid;
       float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
       if (v < n) {
+        float ld = ldeg, lh = lhop, m0 = md0;
+        if (gid) {  // this vertex's graph's maxima
+          const ull *mx = maxes + 3 * (int64_t)gid[v];
+          ld = logf(1.f + (float)mx[0]);
+          lh = logf(1.f + (float)mx[1]);
+          m0 = mx[2] ? (float)mx[2] : 1.f;
+        }
         const float deg = (float)(off[v + 1] - off[v]);
-        f0 = ldeg > 0.f ? logf(1.f + deg) / ldeg : 0.f;
-        f1 = lhop > 0.f ? logf(1.f + (float)hop2[v]) / lhop : 0.f;
-        f2 = (float)(d0[v] < 0 ? 0 : d0[v]) / md0;
+        f0 = ld > 0.f ? logf(1.f + deg) / ld : 0.f;
+        f1 = lh > 0.f ? logf(1.f + (float)hop2[v]) / lh : 0.f;
+        f2 = (float)(d0[v] < 0 ? 0 : d0[v]) / m0;
         f3 = deg > 0.f ? (float)outw[v] / deg : 0.f;
       }
       F[tid][0] = f0;
@@ -210,8 +253,10 @@ __global__ void __launch_bounds__(256) mlp_score_kernel(const int64_t *off, cons
       if (v < n) {
         const float pr = 1.f / (1.f + expf(-(s_b3 + outv)));
         score[v] = pr;
-        bin = (int)(pr * nbins);
-        bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+        if (nbins > 0) {
+          bin = (int)(pr * nbins);
+          bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+        }
       }
     }
     const unsigned same = __match_any_sync(PHDE_FULL_MASK, bin);
@@ -299,7 +344,7 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
   const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE + sizeof(unsigned) * nbins;
   PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
   mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts, score, hist,
-                                                       nbins);
+                                                       nbins, nullptr);
   PHDE_LAUNCHED(ctx);
   std::vector<unsigned> hh(nbins);
   PHDE_CK(ctx, cudaMemcpyAsync(hh.data(), hist, sizeof(unsigned) * nbins, cudaMemcpyDeviceToHost, ctx->stream));
@@ -350,5 +395,42 @@ int phde_cand_distances(phde_ctx *ctx, const int32_t *D, int P0, const uint16_t 
     PHDE_CK(ctx, cudaMemcpyAsync(h_sub.data(), sub, sizeof(int32_t) * M * P0, cudaMemcpyDeviceToHost, ctx->stream));
   PHDE_CK(ctx, cudaMemcpyAsync(h_csub.data(), csub, sizeof(int32_t) * M * M, cudaMemcpyDeviceToHost, ctx->stream));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return PHDE_OK;
+}
+
+// Scores of every vertex of an uploaded batch (features normalised per graph) into the context's "lp.score"
+// buffer; d_d0 is the warm start's minimum distance.  No synchronisation (part of the captured batched layout).
+// d_weights: the model on the device (the caller copies it before the captured sequence).
+int phde_batch_scores(phde_ctx *ctx, const float *d_weights, const int32_t *d_d0, const float **score_out) {
+  const int64_t n = ctx->n;
+  const int B = ctx->batch_B;
+  ull *hop2 = (ull *)phde_buf(ctx, "lp.hop2", sizeof(ull) * n);
+  uint32_t *outw = (uint32_t *)phde_buf(ctx, "lp.outw", sizeof(uint32_t) * n);
+  ull *maxes = (ull *)phde_buf(ctx, "lpb.max", sizeof(ull) * 3 * B);
+  ull *pk = (ull *)phde_buf(ctx, "lp.pack", sizeof(ull) * n);
+  float *score = (float *)phde_buf(ctx, "lp.score", sizeof(float) * n);
+  if (!hop2 || !outw || !maxes || !pk || !score) return PHDE_ERR_OOM;
+  const int64_t *crow, *ce0;
+  int64_t nch, chunk;
+  int rc = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
+  if (rc) return rc;
+  PHDE_CK(ctx, cudaMemsetAsync(maxes, 0, sizeof(ull) * 3 * B, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(hop2, 0, sizeof(ull) * n, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(outw, 0, sizeof(uint32_t) * n, ctx->stream));
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->nsm * 8));
+  feature_pack_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, n, pk);
+  PHDE_LAUNCHED(ctx);
+  feature_raw_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, d_d0, pk, n, crow, ce0, nch, chunk, hop2,
+                                                 outw);
+  PHDE_LAUNCHED(ctx);
+  feature_max_batched_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, ctx->d_gid, n, maxes);
+  PHDE_LAUNCHED(ctx);
+  const int gm = (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * 4));
+  const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE;
+  PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
+  mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, d_weights, score,
+                                                       nullptr, 0, ctx->d_gid);
+  PHDE_LAUNCHED(ctx);
+  *score_out = score;
   return PHDE_OK;
 }

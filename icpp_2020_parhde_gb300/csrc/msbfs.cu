@@ -42,6 +42,10 @@ struct MsArgs {
   int64_t n;
   int nsrc;        // sources this sweep (the word count W is the kernel's template argument)
   const int64_t *src;
+  // batches (period > 0): src holds nlist sources and entry i searches with bit i % period -- each graph's
+  // candidates share the bit positions, the components never meet; the level-0 frontier list is left for
+  // the first level to build (built_f false)
+  int nlist, period;
   uint16_t *R;     // row-major n x RW distance record: R[v*RW + b] = level + 1 (0 = unreached)
   int RW;          // row width (all sources of all sweeps, a multiple of 64)
   int col0;        // first source of this sweep within the row
@@ -258,7 +262,20 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
     full[w] = bits >= 64 ? ~0ull : (bits <= 0 ? 0ull : ((1ull << bits) - 1ull));
   }
   // level 0: every source sees itself; hub rows never enter the light pull (their bit in `done`)
-  if (gt == 0)
+  if (a.period > 0) {
+    ull my = 0;  // (sources << 32 | their edges) of this thread, for the level-0 frontier totals
+    for (int64_t i = gt; i < a.nlist; i += gts) {
+      const int b = (int)(i % a.period);
+      const int64_t s = a.src[i];
+      atomicOr(a.seen + s * W + (b >> 6), 1ull << (b & 63));
+      atomicOr(a.front[0] + s * W + (b >> 6), 1ull << (b & 63));
+      atomicOr(a.fbm[0] + (s >> 5), 1u << (s & 31));
+      a.R[s * a.RW + a.col0 + b] = 1;
+      my += (1ull << 32) | (ull)(a.off[s + 1] - a.off[s]);
+    }
+    my = warp_sum(my);
+    if ((threadIdx.x & 31) == 0 && my) atomicAdd(a.lstat + 3, my);
+  } else if (gt == 0)
     for (int b = 0; b < a.nsrc; b++) {
       const int64_t s = a.src[b];
       atomicOr(a.seen + s * W + (b >> 6), 1ull << (b & 63));
@@ -271,7 +288,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
     atomicOr(a.done + (v >> 5), 1u << (v & 31));
   }
   // the sources are the frontier of level 0 (list slot 3)
-  if (gt == 0) {
+  if (gt == 0 && a.period == 0) {
     ull run = 0;
     for (int b = 0; b < a.nsrc; b++) {
       const int64_t s = a.src[b];
@@ -283,7 +300,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
   }
   __shared__ PushScratch psc;
   __shared__ ull s_stat;
-  bool built_f = true, built_z = true;  // lists of levels L-1 and L-2 exist (sparse levels build them)
+  bool built_f = a.period == 0, built_z = true;  // lists of levels L-1 and L-2 exist (sparse levels build them)
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
   int32_t L = 0;
   for (;; L++) {
@@ -580,11 +597,12 @@ int phde_heavy_chunks(phde_ctx *ctx, const int64_t **chunk_row, const int64_t **
   return PHDE_OK;
 }
 
-// Multi-source BFS from `nsrc` sources (device array; sweeps of up to 256).  The result is the row-major
-// record R (n x RW uint16, RW = nsrc rounded up to 64; level + 1, 0 = unreached), returned through *R_out.
-int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **R_out, int *RW_out) {
+// The sweep: sources d_src (nlist entries; bit = entry, or entry % period for batches), optionally without
+// host synchronisation (sync false: no error read-back and no level count -- for captured sequences).
+static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, int period, bool sync, uint16_t **R_out,
+                     int *RW_out) {
   const int64_t n = ctx->n;
-  if (nsrc < 1) return PHDE_ERR_INVALID;
+  if (nsrc < 1 || (period > 0 && (nsrc != period || period > 64 * MS_MAXW))) return PHDE_ERR_INVALID;
   const int RW = (nsrc + 63) / 64 * 64;
   const int Wmax = MS_MAXW;
   uint16_t *R = (uint16_t *)phde_buf(ctx, "ms.R", sizeof(uint16_t) * n * RW);
@@ -641,6 +659,8 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     a.n = n;
     a.nsrc = ns;
     a.src = d_src + s0;
+    a.nlist = period > 0 ? nlist : ns;
+    a.period = period;
     a.R = R;
     a.RW = RW;
     a.col0 = s0;
@@ -679,6 +699,10 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
     PHDE_LAUNCHED(ctx);
     cudaEventRecord(ctx->kev[1], ctx->stream);
     ctx->kev_pending = true;
+    if (!sync) {  // captured batched layouts: no host wait; the error word is read after the whole sequence
+      ctx->kev_pending = false;
+      continue;
+    }
     if ((rc = phde_check_device_err(ctx, "multi-source BFS"))) return rc;  // synchronises, collects the time
     ctx->msbfs_ms += ctx->kernel_ms - before;
     int nlev = 0;
@@ -703,6 +727,19 @@ int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **
   *R_out = R;
   *RW_out = RW;
   return PHDE_OK;
+}
+
+// Multi-source BFS from `nsrc` sources (device array; sweeps of up to 256).  The result is the row-major
+// record R (n x RW uint16, RW = nsrc rounded up to 64; level + 1, 0 = unreached), returned through *R_out.
+int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **R_out, int *RW_out) {
+  return msbfs_run(ctx, d_src, nsrc, nsrc, 0, true, R_out, RW_out);
+}
+
+// A batch's candidates in one sweep: d_src holds nlist vertices, entry i searching with bit i % period
+// (period <= 256: every graph's candidates take bits 0 .. period-1).  No host synchronisation.
+int phde_msbfs_record_batched(phde_ctx *ctx, const int64_t *d_src, int nlist, int period, uint16_t **R_out,
+                              int *RW_out) {
+  return msbfs_run(ctx, d_src, period, nlist, period, false, R_out, RW_out);
 }
 
 // Columns `h_cols` of the record into D (n x ncols int32 column-major, -1 unreached); optional exact sums

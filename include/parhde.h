@@ -165,7 +165,8 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out,
  * Replaces a caller's loop of DrawingBase::run() + getCoordinates() over separate graphs
  * (variants/DrawingBase.h:41-60; spectralDrawing.cpp:186-197 per graph).  phde_batch_upload copies the
  * graphs (each its own CSR, local vertex ids; all with the same offset width) as one disjoint union;
- * phde_layout_batched lays every graph out: ParHDE with Kcenters pivots, opts->precision PHDE_PREC_MIXED,
+ * phde_layout_batched lays every graph out: ParHDE with Kcenters pivots or learned pivots (PHDE_STRAT_LEARNED:
+ * every graph above 256 vertices; each graph gets the pivots a single-graph learned layout picks), opts->precision PHDE_PREC_MIXED,
  * opts->eig PHDE_EIG_EXACT, 2 <= k <= 32, c <= 4, every graph connected with more than 3k vertices.
  * coords_out holds sum(n_b) * c doubles: graph b's coordinates, column-major (coordinate j of its local
  * vertex i at i + j * n_b), start at c * (n_0 + ... + n_{b-1}).  The first call on a batch autotunes and
@@ -233,6 +234,10 @@ int phde_write_png(const char *path, const uint8_t *rgba, uint32_t width, uint32
 
 int phde_batch_upload(phde_ctx *ctx, const phde_graph_desc *graphs, int count);
 int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out, phde_layout_stats *stats);
+/* The Rayleigh quotients x^T L x / x^T x of every graph's coordinates from the last phde_layout_batched call:
+ * graph b's coordinate t at rq_out[b * c + t] (count * c doubles).  No counterpart in the reference: the
+ * per-graph quality figure by which a batch's learned pivots are compared with Kcenters'. */
+int phde_batch_rayleigh(phde_ctx *ctx, double *rq_out);
 
 /* Exact distance columns from the given sources on the uploaded graph: hop counts (unweighted graph)
  * or weighted shortest-path lengths (weighted graph).  out: n*nsrc int32, column-major; unreachable

@@ -111,3 +111,51 @@ def test_batched_vs_fp64_oracle(k, c):
         assert np.array_equal(cs.kcenters(3 * k, 0, want_dist=False)[1], L.sources[: 3 * k])
         np.testing.assert_allclose(rayleigh(g, xb), rayleigh(g, L.coords), rtol=1e-3)
         assert principal_cosines(xb, L.coords).min() > 1 - 1e-3
+
+
+def learned_batch_graphs():
+    return [graphs.rgg(3000, dim=2, avg_degree=8, seed=11), graphs.rgg(12000, dim=2, avg_degree=8, seed=12),
+            graphs.mesh(60, 50, seed=13), graphs.rmat(12, seed=14), graphs.rgg(25000, dim=2, avg_degree=8, seed=15),
+            graphs.rgg(8000, dim=3, avg_degree=12, seed=16), graphs.rgg(600, dim=2, avg_degree=8, seed=17)]
+
+
+@pytest.mark.parametrize("k,c", [(10, 2), (20, 3)])
+def test_batched_learned_matches_single_learned_layouts(k, c):
+    """Learned pivots in a batch (warm start, per-graph feature normalisation and candidates, one multi-source
+    sweep for all graphs, per-graph farthest-point order) give every graph the pivots its own learned layout
+    takes: the same layout up to the mixed path's rounding, and the per-graph Rayleigh quotients the library
+    reports."""
+    gs = [g for g in learned_batch_graphs() if g.n > 256]
+    cb = Context(0)
+    cb.upload_batch(gs)
+    xs, st = cb.layout_batched(k, c, strategy="Learned")
+    xs = [x.copy() for x in xs]
+    rq_lib = cb.batch_rayleigh()
+    assert st["naccepted"] == k
+    cs = Context(0)
+    for i, (g, xb) in enumerate(zip(gs, xs)):
+        cs.upload(g)
+        r = cs.layout("ParHDE", "Learned", k, c, precision="mixed", eig="exact")
+        q = rayleigh(g, xb)
+        np.testing.assert_allclose(np.linalg.norm(xb, axis=0), 1.0, rtol=1e-9)
+        np.testing.assert_allclose(q, rayleigh(g, r.coords), rtol=1e-4)
+        assert principal_cosines(xb, r.coords).min() > 1 - 1e-5
+        np.testing.assert_allclose(rq_lib[i], q, rtol=1e-5)
+    # a replay of the captured sequence gives the same layouts bit for bit
+    xs2, st2 = cb.layout_batched(k, c, strategy="Learned")
+    xs3, st3 = cb.layout_batched(k, c, strategy="Learned")
+    assert st3["batch_graph_replay"] == 1
+    for a, b in zip(xs, xs3):
+        assert np.array_equal(a, b)
+
+
+def test_batched_learned_rejects_small_graphs():
+    gs = learned_batch_graphs()  # the last graph has 256 vertices or fewer after its LCC
+    small = [g for g in gs if g.n <= 256]
+    if not small:
+        gs.append(graphs.path_graph(200))
+    cb = Context(0)
+    cb.upload_batch(gs)
+    with pytest.raises(ParHDEError) as e:
+        cb.layout_batched(10, 2, strategy="Learned")
+    assert e.value.status == -4
