@@ -109,14 +109,14 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t = threading.Thread(target=self._read, args=(self.proc,), daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
+    def _read(self, proc):
+        for line in proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
@@ -126,6 +126,18 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            self.t.join(timeout=5)
+            self.proc = None
+
+    # A polling nvidia-smi slows host<->device copies several-fold on these machines (the adjacency upload
+    # took 13-15 ms with it running and 2.6 ms without, the same pinned buffers), so the end-to-end loops run
+    # with the sampler paused; the device-timed regions are sampled.
+    def pause(self):
+        self.__exit__(None, None, None)
+
+    def resume(self):
+        if self.proc is None:
+            self.__enter__()
 
     def summary(self):
         sm, mx, reasons = [], [], set()
@@ -261,9 +273,10 @@ def cpu_layout(g, algo, k, c, reps, desc):
 class Runner:
     """Timed layouts of one uploaded graph: device time (library events) and end to end (upload + layout)."""
 
-    def __init__(self, ctx, g, gp, algo, k, c, xy, flush_l2, ws):
+    def __init__(self, ctx, g, gp, algo, k, c, xy, flush_l2, ws, clk=None):
         self.ctx, self.g, self.gp, self.algo, self.k, self.c = ctx, g, gp, algo, k, c
         self.xy, self.flush_l2, self.ws = xy, flush_l2, ws
+        self.clk = clk  # the clock sampler, paused around the end-to-end loops
 
     def run(self, p):
         return self.ctx.layout(self.algo, k=self.k, c=self.c, coords_out=self.xy.numpy(), **p)
@@ -292,15 +305,21 @@ class Runner:
 
     def e2e(self, p, steps):
         ts, tu = [], []
-        for _ in range(steps):
-            self.flush_l2()
-            barrier(self.ws)
-            t1 = time.perf_counter()
-            self.ctx.upload(self.gp)
-            t2 = time.perf_counter()
-            self.run(p)
-            ts.append(time.perf_counter() - t1)
-            tu.append(t2 - t1)
+        if self.clk:
+            self.clk.pause()
+        try:
+            for _ in range(steps):
+                self.flush_l2()
+                barrier(self.ws)
+                t1 = time.perf_counter()
+                self.ctx.upload(self.gp)
+                t2 = time.perf_counter()
+                self.run(p)
+                ts.append(time.perf_counter() - t1)
+                tu.append(t2 - t1)
+        finally:
+            if self.clk:
+                self.clk.resume()
         self.upload_ms = float(np.mean(tu)) * 1e3
         return allmax(self.ws, float(np.mean(ts))) * 1e3
 
@@ -421,8 +440,8 @@ def run_gb300(args):
         flush.fill_(1.0)
         torch.cuda.synchronize()
 
-    R = Runner(ctx, g, gp, "ParHDE", k, c, xy, flush_l2, ws)
     clk = ClockSampler(local).__enter__()
+    R = Runner(ctx, g, gp, "ParHDE", k, c, xy, flush_l2, ws, clk)
     # ---- headline: device-resident timed region, then end to end through the C ABI ----
     head = R.timed(P_LEARNED, args.steps, args.warmup)
     xy_head = R.coords()
@@ -594,7 +613,7 @@ def run_single(args, local, kind, k, c, flush_l2):
     return out
 
 
-def run_weighted(args, local, flush_l2):
+def run_weighted(args, local, flush_l2, clk=None):
     """The weighted configuration: WParHDE (Kcenters pivots by delta-stepping SSSP, coupled MGS, FP64 as the
     reference) on the weighted 3-D grid; CPU baseline: one oracle layout of the same graph."""
     import torch
@@ -605,7 +624,7 @@ def run_weighted(args, local, flush_l2):
     gp = pinned_graph(g)
     xy = torch.empty(g.n * c, dtype=torch.float64).pin_memory()
     ctx.upload(gp)
-    R = Runner(ctx, g, gp, "wParHDE", k, c, xy, flush_l2, 1)
+    R = Runner(ctx, g, gp, "wParHDE", k, c, xy, flush_l2, 1, clk)
     p = dict(strategy="Kcenters", precision="fp64", eig="power")
     steps = max(3, args.steps // 5)
     r = R.timed(p, steps, 2)
@@ -634,7 +653,7 @@ def run_weighted_headline(args, ws, rank, local):
         torch.cuda.synchronize()
 
     clk = ClockSampler(local).__enter__()
-    out = run_weighted(args, local, flush_l2)
+    out = run_weighted(args, local, flush_l2, clk)
     clk.__exit__(None, None, None)
     if rank != 0:
         return

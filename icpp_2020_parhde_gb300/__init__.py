@@ -226,6 +226,20 @@ class Context:
                                           _ptr(wa, C.c_double), n, nsplit, _ptr(G, C.c_double)))
         return G
 
+    def symeig(self, M, c: int, largest: bool = False):
+        """phde_symeig: the layouts' exact eigensolver on a symmetric k x k matrix.  Returns (evals ascending,
+        Y (k, c): the eigenvectors of the c smallest -- or largest, largest first -- eigenvalues, sweeps)."""
+        Mf = np.asfortranarray(M, dtype=np.float64)
+        k = Mf.shape[0]
+        if Mf.shape != (k, k):
+            raise ValueError("M must be square")
+        ev = np.empty(k, dtype=np.float64)
+        Y = np.empty((c, k), dtype=np.float64)  # column-major k x c
+        it = C.c_int(0)
+        self._check(self._L.phde_symeig(self._h, Mf.ctypes.data_as(C.POINTER(C.c_double)), k, c, int(largest),
+                                        _ptr(ev, C.c_double), _ptr(Y, C.c_double), C.byref(it)))
+        return ev, Y.T.copy(), it.value
+
     def draw(self, x, y) -> dict:
         """phde_draw: rasterise the uploaded graph at vertex positions (x, y) on the GPU (the reference's draw
         tool).  Returns the image geometry and timings; the image stays on the device."""

@@ -30,6 +30,7 @@ EXPORTS = [
     "phde_set_pivot_model", "phde_batch_upload", "phde_layout_batched", "phde_write_nxyz",
     "phde_graph_from_entries", "phde_graph_download", "phde_draw", "phde_draw_download", "phde_draw_write_png",
     "phde_write_png", "phde_gram_f32", "phde_set_pivot_check", "phde_pivot_scores", "phde_batch_rayleigh",
+    "phde_symeig",
 ]
 
 
@@ -131,6 +132,7 @@ def load(path: str | None = None):
     L.phde_graph_download.argtypes = [vp, u32p, u32p, i32p]
     f32p = C.POINTER(C.c_float)
     L.phde_gram_f32.argtypes = [vp, f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, f64p, i64, C.c_int, f64p]
+    L.phde_symeig.argtypes = [vp, f64p, C.c_int, C.c_int, C.c_int, f64p, f64p, C.POINTER(C.c_int)]
     L.phde_draw.argtypes = [vp, f64p, f64p, C.POINTER(DrawInfo)]
     L.phde_draw_download.argtypes = [vp, C.POINTER(C.c_uint8), C.c_size_t]
     L.phde_draw_write_png.argtypes = [vp, C.c_char_p, C.c_int]

@@ -116,6 +116,26 @@ __device__ __forceinline__ uint32_t ld_nc_hint(const uint32_t *p, uint64_t pol) 
   asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
   return v;
 }
+// 32 bytes (four 64-bit words) in one 256-bit load through L2 only, with an L2 policy; p 32-byte aligned
+__device__ __forceinline__ void ld_cg_hint32(const void *p, uint64_t pol, unsigned long long (&x)[4]) {
+  asm volatile("ld.global.cg.L2::cache_hint.v4.u64 {%0, %1, %2, %3}, [%4], %5;"
+               : "=l"(x[0]), "=l"(x[1]), "=l"(x[2]), "=l"(x[3])
+               : "l"(p), "l"(pol));
+}
+// Asynchronous global -> shared copies (cp.async): 16 bytes through L2 only, or 8 bytes; a group per commit.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most `n` of this thread's committed groups are still in flight
+template <int n>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(n) : "memory"); }
+
 // OR-reduction in L2 (no value returned) with an L2 policy
 __device__ __forceinline__ void red_or_hint(unsigned long long *p, unsigned long long v, uint64_t pol) {
   asm volatile("red.global.or.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
@@ -138,6 +158,8 @@ __device__ __forceinline__ ull warp_max_u64(ull v) {
   }
   return v;
 }
+
+__device__ __forceinline__ unsigned warp_max_u32(unsigned v) { return __reduce_max_sync(PHDE_FULL_MASK, v); }
 
 // Block sum of one value per thread; result valid in every thread.  `scratch` holds >= 32 entries.
 template <typename T>

@@ -149,6 +149,7 @@ struct ExactBasis {
   void *Z = nullptr;     // accepted columns, row-major n x kp, uint8 (maxz <= 255) or uint16
   bool z16 = false;
   int kp = 0;
+  const uint32_t *Zq = nullptr;  // byte path: the candidate columns in the quad layout (row stride ld words)
 };
 int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb, int *h_state, double *h_dlog);
 int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double *M);
@@ -171,6 +172,14 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
                         int64_t *d_sources, unsigned long long *d_sumsq, unsigned long long *d_edges, int require_all);
 
 // ---- kernels (msbfs.cu) ----
+// The frontier words of every level of a level-mode sweep: bit b of word w of vertex v is set in level L's
+// array, lvl[(L * n + v) * W + w], exactly when source 64 w + b reaches v first at level L; levels 0 .. nlev - 1.
+struct MsLevels {
+  const ull *lvl = nullptr;
+  int nlev = 0;
+  int W = 0;
+};
+int phde_msbfs_levels(phde_ctx *ctx, const int64_t *d_src, int nsrc, int lvl_cap, MsLevels *lv);
 // Distance columns for nsrc given sources (device array) into D (n * nsrc int32, -1 unreached), up to 256
 // sources per sweep.  With sumsq: exact per-column sums of squares and *h_unreached (synchronises).
 int phde_msbfs(phde_ctx *ctx, const int64_t *d_src, int nsrc, int32_t *D, unsigned long long *sumsq,

@@ -457,6 +457,8 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_kernel(const double *Kin, 
 // convergence test as the global-memory kernel.  Everything lives in shared memory.
 constexpr int JS_MIN_THREADS = 256;  // the shared-memory solver runs with 256..1024 threads
 constexpr int JS_MAX_N = 96;  // 24 N (N|1) bytes of shared memory: A64, V64 and one work matrix
+constexpr int JS_BAD_CAP = 512;       // unseparated pairs the targeted FP64 rotations take on (more: sweeps)
+constexpr int JS_TJ_MAX_ROUNDS = 48;  // rounds of targeted rotations before falling back to sweeps
 
 template <typename T>
 __device__ void js_offnorm(const T *A, int N, int LD, double *red, double &off, double &tot) {
@@ -484,6 +486,10 @@ __device__ __forceinline__ int js_slot(int i, int r, int M) {
   const int x = (i - 1 - r) % (M - 1);
   return (x < 0 ? x + (M - 1) : x) + 1;
 }
+
+template <typename T>
+__device__ void js_apply(T *A, T *V, int N, int LD, int M, const T *s_cs, const T *s_sn, const int *s_p,
+                         const int *s_q);
 
 // One cyclic sweep (M-1 rounds of M/2 disjoint rotations, circle-method pairing) on A and V.  The pairs
 // of round r are (slot m, slot M-1-m); the pairing is the global kernel's, computed in closed form.
@@ -522,11 +528,21 @@ __device__ void js_sweep(T *A, T *V, int N, int LD, int M, int *s_order, double 
       s_sn[m] = sn;
     }
     __syncthreads();
-    // A <- J^T A J in one step: every 2 x 2 block (rows of pair m1, columns of pair m2) takes its column
-    // rotation and then its row rotation, the same operations in the same order as rotating all columns
-    // first and all rows after, without a barrier in between (the pairs partition the indices, so blocks
-    // are disjoint); V <- V J beside it.  A pair whose second index is the padding index N (odd N) or whose
-    // sine is 0 is the identity.
+    js_apply<T>(A, V, N, LD, M, s_cs, s_sn, s_p, s_q);
+  }
+}
+
+// A <- J^T A J and V <- V J for the M/2 disjoint rotations (s_p[m], s_q[m], s_cs[m], s_sn[m]) that partition the
+// indices 0..M-1, in one step: every 2 x 2 block (rows of pair m1, columns of pair m2) takes its column
+// rotation and then its row rotation, the same operations in the same order as rotating all columns first and
+// all rows after, without a barrier in between (the pairs partition the indices, so blocks are disjoint).  A
+// pair whose second index is the padding index N (odd N) or whose sine is 0 is the identity.  Ends with a
+// barrier.
+template <typename T>
+__device__ void js_apply(T *A, T *V, int N, int LD, int M, const T *s_cs, const T *s_sn, const int *s_p,
+                         const int *s_q) {
+  const int tid = threadIdx.x;
+  {
     const int P = M / 2;
     for (int it = tid; it < P * P; it += blockDim.x) {
       const int m1 = it / P, m2 = it - m1 * P;
@@ -619,8 +635,9 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
     js_sweep<float>(A32, V32, N, LD, M, s_order, s_cs, s_sn, s_p, s_q);
   }
   JS_MARK(1)
-  // ---- V = FP64 orthonormalisation of V32: V (V^T V)^(-1/2) to first order, V (I - E/2) with
-  //      E = V^T V - I (|E| ~ FP32 rounding, so the neglected 3/8 E^2 is ~1e-14): two parallel products ----
+  // ---- V = FP64 orthonormalisation of V32: V (V^T V)^(-1/2) to second order, V (I - E/2 + 3/8 E^2) with
+  //      E = V^T V - I.  |E| is the rounding the FP32 rotations accumulated (~1e-5 at k = 64), so the first-order
+  //      form would leave ~3/8 |E|^2 ~ 1e-10 in the eigenvalues; the neglected third-order term is ~1e-15 ----
   for (int idx = tid; idx < N * N; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
     V[i + j * LD] = (double)V32[i + j * LD];
@@ -642,7 +659,23 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
     constexpr int PER = (JS_MAX_N * JS_MAX_N + JS_MIN_THREADS - 1) / JS_MIN_THREADS;
     double nv[PER];
     int cnt = 0;
-    for (int idx = tid; idx < N * N; idx += blockDim.x, cnt++) {  // V(I - E/2), held until every read is done
+    for (int idx = tid; idx < N * N; idx += blockDim.x, cnt++) {  // F = E/2 - 3/8 E^2, held until E is read
+      const int i = idx % N, j = idx / N;
+      double s0 = 0, s1 = 0;
+      int l = 0;
+      for (; l + 1 < N; l += 2) {
+        s0 = fma(W[i + l * LD], W[l + j * LD], s0);
+        s1 = fma(W[i + (l + 1) * LD], W[l + 1 + j * LD], s1);
+      }
+      if (l < N) s0 = fma(W[i + l * LD], W[l + j * LD], s0);
+      nv[cnt] = 0.5 * W[i + j * LD] - 0.375 * (s0 + s1);
+    }
+    __syncthreads();
+    cnt = 0;
+    for (int idx = tid; idx < N * N; idx += blockDim.x, cnt++) W[idx % N + (idx / N) * LD] = nv[cnt];
+    __syncthreads();
+    cnt = 0;
+    for (int idx = tid; idx < N * N; idx += blockDim.x, cnt++) {  // V - V F, held until every read is done
       const int r = idx % N, j = idx / N;
       double s0 = 0, s1 = 0;
       int l = 0;
@@ -651,7 +684,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
         s1 = fma(V[r + (l + 1) * LD], W[l + 1 + j * LD], s1);
       }
       if (l < N) s0 = fma(V[r + l * LD], W[l + j * LD], s0);
-      nv[cnt] = V[r + j * LD] - 0.5 * (s0 + s1);
+      nv[cnt] = V[r + j * LD] - (s0 + s1);
     }
     __syncthreads();
     cnt = 0;
@@ -703,25 +736,142 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   //      sum_j a_ji / (lambda_i - a_jj) e_j, and for the c wanted ones two more fixed-point steps of
   //      (A - lambda_i) y = 0 with y_i = 1 (each gains a factor ~ off / gap).  Otherwise FP64 Jacobi
   //      sweeps. ----
+  //      When some pairs are not separated (close eigenvalues) but none of them involves a wanted index (the
+  //      c smallest or largest diagonal entries), FP64 rotations of just those pairs come first -- a few
+  //      rounds of disjoint rotations, each as cheap as one round of a sweep, until every coupling left is
+  //      either separated or negligible (1e-15 of the Frobenius norm) -- and the refinement then treats the
+  //      negligible couplings of unseparated pairs as zero.  The wanted eigenpairs only ever divide by the
+  //      gaps to separated eigenvalues.
   __shared__ double s_lam[JS_MAX_N];
-  __shared__ int s_bad;
-  if (tid == 0) s_bad = c_target * N > 2 * (int)blockDim.x;  // two refined entries per thread at most
+  __shared__ int s_bad, s_full, s_nbad, s_nsel;
+  __shared__ int s_cnt[JS_MAX_N + 1];
+  __shared__ unsigned char s_want[JS_MAX_N + 1];
+  __shared__ short s_bp[JS_BAD_CAP], s_bq[JS_BAD_CAP];
+  if (tid == 0) {
+    s_bad = 0;
+    s_full = c_target * N > 2 * (int)blockDim.x;  // two refined entries per thread at most
+  }
   __syncthreads();
   for (int idx = tid; idx < N * N; idx += blockDim.x) {
     const int i = idx % N, j = idx / N;
     if (i < j && !(fabs(A[i + j * LD]) <= 1e-3 * fabs(A[i + i * LD] - A[j + j * LD]))) s_bad = 1;
   }
   __syncthreads();
+  int tj_rounds = 0;
+  if (s_bad && !s_full) {
+    js_offnorm(A, N, LD, red, off, tot);
+    const double negl = 1e-15 * sqrt(tot);
+    for (int i = tid; i < N; i += blockDim.x) {
+      const double ai = A[i + i * LD];
+      int rank = 0;
+      for (int j = 0; j < N; j++) {
+        const double aj = A[j + j * LD];
+        rank += (aj < ai) || (aj == ai && j < i);
+      }
+      s_want[i] = largest ? rank >= N - c_target : rank < c_target;
+    }
+    __syncthreads();
+    // pair (i, j), i < j: 0 separated or negligible, 1 to rotate, 2 unseparated with a wanted index
+    auto pair_kind = [&](int i, int j) -> int {
+      const double aij = A[i + j * LD], gap = fabs(A[i + i * LD] - A[j + j * LD]);
+      const bool sep = fabs(aij) <= 1e-3 * gap;
+      if (s_want[i] || s_want[j]) return (sep && gap > 0.0) ? 0 : 2;
+      return (!sep && fabs(aij) > negl) ? 1 : 0;
+    };
+    for (;; tj_rounds++) {
+      for (int i = tid; i < N; i += blockDim.x) {
+        int cnt = 0;
+        bool fb = false;
+        for (int j = i + 1; j < N; j++) {
+          const int kd = pair_kind(i, j);
+          cnt += kd == 1;
+          fb |= kd == 2;
+        }
+        s_cnt[i] = cnt;
+        if (fb) s_full = 1;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int run = 0;
+        for (int i = 0; i < N; i++) {
+          const int c = s_cnt[i];
+          s_cnt[i] = run;
+          run += c;
+        }
+        s_nbad = run;
+        if (run > JS_BAD_CAP || (run > 0 && tj_rounds == JS_TJ_MAX_ROUNDS)) s_full = 1;
+      }
+      __syncthreads();
+      const int nbad = s_nbad;
+      if (s_full || nbad == 0) break;  // uniform
+      for (int i = tid; i < N; i += blockDim.x) {  // the pairs to rotate, in row order
+        int pos = s_cnt[i];
+        for (int j = i + 1; j < N; j++)
+          if (pair_kind(i, j) == 1) {
+            s_bp[pos] = (short)i;
+            s_bq[pos] = (short)j;
+            pos++;
+          }
+      }
+      __syncthreads();
+      if (tid == 0) {
+        // greedy disjoint selection in list order; every other index (and the padding index N when N is odd)
+        // goes into identity pairs, so the pairs partition 0..M-1 as js_apply expects
+        for (int i = 0; i < N; i++) s_want[i] &= 1u;  // bit 1: taken this round
+        int m = 0;
+        for (int b = 0; b < nbad; b++) {
+          const int p = s_bp[b], q = s_bq[b];
+          if ((s_want[p] | s_want[q]) & 2u) continue;
+          s_want[p] |= 2u;
+          s_want[q] |= 2u;
+          s_p[m] = p;
+          s_q[m] = q;
+          m++;
+        }
+        s_nsel = m;
+        int prev = -1;
+        for (int i = 0; i < M; i++) {
+          if (i < N && (s_want[i] & 2u)) continue;
+          if (prev < 0) {
+            prev = i;
+          } else {
+            s_p[m] = prev;
+            s_q[m] = i;
+            s_cs[m] = 1.0;
+            s_sn[m] = 0.0;
+            m++;
+            prev = -1;
+          }
+        }
+        for (int i = 0; i < N; i++) s_want[i] &= 1u;
+      }
+      __syncthreads();
+      for (int m = tid; m < s_nsel; m += blockDim.x) {
+        const int p = s_p[m], q = s_q[m];
+        const double apq = A[p + q * LD], app = A[p + p * LD], aqq = A[q + q * LD];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / sqrt(t * t + 1.0);
+        s_cs[m] = cs;
+        s_sn[m] = t * cs;
+      }
+      __syncthreads();
+      js_apply<double>(A, V, N, LD, M, s_cs, s_sn, s_p, s_q);
+    }
+  }
   int sw64 = 0;
   const double *Vout = V;  // eigenvector columns (unsorted), V itself after sweeps
-  if (!s_bad) {
+  if (!s_full) {
+    // (the separation test skips only the negligible couplings the targeted rotations left; with no
+    // unseparated pair it never fails)
     for (int i = tid; i < N; i += blockDim.x) {
       const double aii = A[i + i * LD];
       double l0 = 0, l1 = 0;
       for (int j = 0; j < N; j++) {
         if (j == i) continue;
-        const double aij = A[i + j * LD];
-        const double t = aij * aij / (aii - A[j + j * LD]);
+        const double aij = A[i + j * LD], ajj = A[j + j * LD];
+        if (aij == 0.0 || !(fabs(aij) <= 1e-3 * fabs(aii - ajj))) continue;
+        const double t = aij * aij / (aii - ajj);
         if (j & 1) l1 += t; else l0 += t;
       }
       s_lam[i] = aii + (l0 + l1);
@@ -729,7 +879,10 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
     __syncthreads();
     for (int idx = tid; idx < N * N; idx += blockDim.x) {  // W[:, i] = y_i to first order
       const int j = idx % N, i = idx / N;
-      W[j + i * LD] = j == i ? 1.0 : A[j + i * LD] / (s_lam[i] - A[j + j * LD]);
+      const double aji = A[j + i * LD], ajj = A[j + j * LD];
+      W[j + i * LD] = j == i ? 1.0
+                             : (aji != 0.0 && fabs(aji) <= 1e-3 * fabs(A[i + i * LD] - ajj) ? aji / (s_lam[i] - ajj)
+                                                                                          : 0.0);
     }
     __syncthreads();
     // ranks of the eigenvalues: the wanted columns are the c smallest (or largest)
@@ -818,7 +971,7 @@ __global__ void __launch_bounds__(EIG_THREADS) jacobi_smem_kernel(const double *
   JS_MARK(4)
   if (trace && blockIdx.x == 0 && threadIdx.x == 0) {
     trace[6] = sw32;
-    trace[7] = s_bad ? sw64 : 1000;  // 1000: refined by perturbation
+    trace[7] = s_full ? sw64 : 1000 + tj_rounds;  // 1000 + r: refined by perturbation after r targeted rounds
   }
   // ascending order of the eigenvalues, ties by index (the stable order): rank of each entry, in parallel
   for (int i = tid; i < N; i += blockDim.x) {
@@ -909,7 +1062,7 @@ int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest,
         PHDE_CK(ctx, cudaMemcpyAsync(h, tr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
         PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
         fprintf(stderr, "jacobi N=%d: fp32 sweeps %llu: %.1f us, orthonormalise %.1f us, similarity %.1f us, "
-                        "fp64 sweeps %llu: %.1f us, sort/sign %.1f us\n", N, h[6], (h[1] - h[0]) * 1e-3,
+                        "fp64 sweeps %llu (1000 + r: refined after r targeted rounds): %.1f us, sort/sign %.1f us\n", N, h[6], (h[1] - h[0]) * 1e-3,
                 (h[2] - h[1]) * 1e-3, (h[3] - h[2]) * 1e-3, h[7], (h[4] - h[3]) * 1e-3, (h[5] - h[4]) * 1e-3);
       }
     } else {
@@ -954,5 +1107,28 @@ int phde_eigensolve_batched(phde_ctx *ctx, const double *d_M, int N, int c, int 
   PHDE_LAUNCHED(ctx);
   pick_kernel<<<count, 256, 0, ctx->stream>>>(d_K, N, c, 0, d_Y);
   PHDE_LAUNCHED(ctx);
+  return PHDE_OK;
+}
+
+// Diagnostics entry: the exact (Jacobi) eigensolver of the layouts on a caller's symmetric k x k matrix.
+extern "C" int phde_symeig(phde_ctx *ctx, const double *M, int k, int c, int largest, double *evals, double *Y,
+                           int *iters) {
+  if (!ctx) return PHDE_ERR_INVALID;
+  if (!M || !evals || !Y || k < 1 || k > PHDE_MAX_K || c < 1 || c > k)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "phde_symeig: bad arguments");
+  PHDE_CK(ctx, cudaSetDevice(ctx->device));
+  double *dM = (double *)phde_buf(ctx, "symeig.M", sizeof(double) * k * k);
+  double *dK = (double *)phde_buf(ctx, "symeig.K", sizeof(double) * k * k);
+  double *dE = (double *)phde_buf(ctx, "symeig.E", sizeof(double) * k);
+  double *dY = (double *)phde_buf(ctx, "symeig.Y", sizeof(double) * k * c);
+  if (!dM || !dK || !dE || !dY) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemcpyAsync(dM, M, sizeof(double) * k * k, cudaMemcpyHostToDevice, ctx->stream));
+  int it = 0;
+  int rc = phde_eigensolve(ctx, dM, k, c, largest ? 1 : 0, PHDE_EIG_EXACT, dK, dE, dY, &it, 0);
+  if (rc) return rc;
+  PHDE_CK(ctx, cudaMemcpyAsync(evals, dE, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaMemcpyAsync(Y, dY, sizeof(double) * k * c, cudaMemcpyDeviceToHost, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (iters) *iters = it;
   return PHDE_OK;
 }

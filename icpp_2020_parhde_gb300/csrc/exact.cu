@@ -72,6 +72,7 @@ struct ZgArgs {
   ull *GI, *GD;
   int ld;
   unsigned *maxz;    // [0] largest distance, [1] largest degree
+  const unsigned *wide_only;  // non-null: run only when *wide_only > 255 (the byte kernel did not apply)
 };
 
 // A slab whose distances all fit a byte goes through byte dot products: zs4[q][col] packs rows 4q .. 4q+3 of a
@@ -79,6 +80,7 @@ struct ZgArgs {
 // as two 16-bit halves (dp2a against the bytes of zs4: two rows of Z^T D Z per instruction).  Rows whose
 // deg * z does not fit 16 bits take the one-row 32-bit path.  Every sum is still exact.
 __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
+  if (a.wide_only && __ldg(a.wide_only) <= 255u) return;  // uniform: the quad-layout kernel formed them
   extern __shared__ int zsm[];  // [ZG_ROWS][S], zs4[ZG_ROWS/4][S], ys2[ZG_ROWS/2][S], then the record columns
   __shared__ unsigned s_deg[ZG_ROWS];
   __shared__ ull red[32];
@@ -252,6 +254,332 @@ __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------------
+// The byte path of G_I, G_D from a quad layout of Z, when every distance fits a byte.
+//
+// zq_pack_kernel writes Z columns [c0, c1) as Zq[(i / 4) * ldq + t]: byte j of that word is Z[4 (i / 4) + j][t],
+// the four rows a dp4a consumes at once, so the Gram kernel stages a slab with plain coalesced word loads and
+// no repacking.  It also keeps, per slab of ZQ_ROWS rows, the largest value of every column packed so far
+// (smaxz, atomicMax over the calls of one orthogonalisation) and the largest distance and degree overall
+// (maxz[0], maxz[1]).  Rows past n pack as zeros.
+constexpr int ZQ_ROWS = 128;
+constexpr int ZQ_QUADS = ZQ_ROWS / 4;
+constexpr int ZQ_PACK_COLS = 64;  // columns staged per pass of the pack kernel
+constexpr int ZQ_THREADS = 256;
+constexpr int ZQ_GRAM_THREADS = 192;  // the Gram kernel's largest block (190 tiles at 76 columns); three per SM
+
+__global__ void __launch_bounds__(ZQ_THREADS) zq_pack_kernel(ZSrc src, const int64_t *off, int64_t n, int P, int c0,
+                                                             int c1, int ldq, uint32_t *Zq, unsigned *smaxz,
+                                                             unsigned *maxz) {
+  __shared__ uint8_t zb[ZQ_ROWS][ZQ_PACK_COLS + 4];
+  __shared__ unsigned s_m;
+  const int64_t nslab = (n + ZQ_ROWS - 1) / ZQ_ROWS;
+  const int P0 = src.P0;
+  for (int64_t s = blockIdx.x; s < nslab; s += gridDim.x) {
+    const int64_t i0 = s * ZQ_ROWS;
+    unsigned m = 0, md = 0;
+    if (c0 == 0)
+      for (int r = threadIdx.x; r < ZQ_ROWS; r += blockDim.x)
+        if (i0 + r < n) md = max(md, (unsigned)(off[i0 + r + 1] - off[i0 + r]));
+    for (int t0 = c0; t0 < c1; t0 += ZQ_PACK_COLS) {
+      const int nc = min(ZQ_PACK_COLS, c1 - t0);
+      __syncthreads();  // zb of the previous pass consumed
+      // ones, distance (D) and padding columns: consecutive threads take consecutive rows of a column; eight
+      // loads in flight per thread
+      constexpr int U = 8;
+      for (int e0 = threadIdx.x; e0 < ZQ_ROWS * nc; e0 += U * blockDim.x) {
+        int v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = e0 + u * blockDim.x;
+          const int j = e / ZQ_ROWS, r = e - j * ZQ_ROWS, t = t0 + j;
+          const int64_t i = i0 + r;
+          v[u] = -2;  // nothing to store here
+          if (e < ZQ_ROWS * nc && !(t >= 1 && t <= P && t > P0))
+            v[u] = i >= n ? 0 : (t == 0 ? 1 : (t <= P ? __ldg(src.D + (int64_t)(t - 1) * n + i) : 0));
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = e0 + u * blockDim.x;
+          if (v[u] == -2) continue;
+          const int j = e / ZQ_ROWS, r = e - j * ZQ_ROWS;
+          m = max(m, (unsigned)v[u]);
+          zb[r][j] = (uint8_t)v[u];
+        }
+      }
+      // record columns: consecutive threads take consecutive chosen columns of a row
+      for (int e0 = threadIdx.x; e0 < ZQ_ROWS * nc; e0 += U * blockDim.x) {
+        int v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = e0 + u * blockDim.x;
+          const int r = e / nc, j = e - r * nc, t = t0 + j;
+          const int64_t i = i0 + r;
+          v[u] = -2;
+          if (e < ZQ_ROWS * nc && t >= 1 && t <= P && t > P0)
+            v[u] = i >= n ? 0 : (int)__ldg(src.R + i * src.RW + src.rmap[t - 1 - P0]) - 1;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = e0 + u * blockDim.x;
+          if (v[u] == -2) continue;
+          const int r = e / nc, j = e - r * nc;
+          m = max(m, (unsigned)v[u]);
+          zb[r][j] = (uint8_t)v[u];
+        }
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < ZQ_QUADS * nc; e += blockDim.x) {
+        const int q = e / nc, j = e - q * nc;
+        const uint32_t w = (uint32_t)zb[4 * q][j] | ((uint32_t)zb[4 * q + 1][j] << 8) |
+                           ((uint32_t)zb[4 * q + 2][j] << 16) | ((uint32_t)zb[4 * q + 3][j] << 24);
+        Zq[(s * ZQ_QUADS + q) * ldq + t0 + j] = w;
+      }
+    }
+    if (threadIdx.x == 0) s_m = 0;
+    __syncthreads();
+    m = warp_max_u32(m);
+    md = warp_max_u32(md);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&s_m, m);
+      if (md) atomicMax(maxz + 1, md);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      atomicMax(smaxz + s, s_m);
+      atomicMax(maxz, s_m);
+    }
+  }
+}
+
+// G_I, G_D (upper triangle, Z columns p < c1 against q in [c0, c1)) from the quad layout.  Per slab: the rows'
+// degrees, the rows whose deg * (slab's largest value) exceeds 16 bits (heavy: the one-row 32-bit path, their
+// bytes masked out of the quads), then the staged quads zs4 and the deg * z pairs ys (two 16-bit halves per
+// word: rows 4q, 4q+1 in ys[2q], rows 4q+2, 4q+3 in ys[2q+1]).  Thread t owns the 4 x 4 tile tile_of(t):
+// per quad 16 dp4a (Z^T Z) and 32 dp2a (Z^T D Z).  32-bit partial sums, flushed to the 64-bit Grams before a
+// slab's bound (sum of its light rows' max(deg, 1) times the square of its largest value; below 2^32 since
+// 128 * 65535 * 255 is) could carry them past 2^32.  Every sum is exact.
+struct ZqArgs {
+  const uint32_t *Zq;
+  int ldq;
+  const int64_t *off;
+  int64_t n;
+  int c0, c1;  // multiples of 4
+  int ntiles;
+  ull *GI, *GD;
+  int ld;
+  const unsigned *smaxz, *maxz;
+};
+
+// Copies of slab s (its quad words and its rows' offsets) into one staging buffer, as one cp.async group.
+__device__ __forceinline__ void zq_stage(const ZqArgs &a, int64_t s, uint32_t *raw, int64_t *soff) {
+  const int C = a.c1, c4 = C / 4;
+  const int64_t i0 = s * ZQ_ROWS;
+  for (int e = threadIdx.x; e < ZQ_QUADS * c4; e += blockDim.x) {
+    const int q = e / c4, w = e - q * c4;
+    cp_async16(raw + q * C + 4 * w, a.Zq + (s * ZQ_QUADS + q) * a.ldq + 4 * w);
+  }
+  for (int r = threadIdx.x; r <= ZQ_ROWS; r += blockDim.x)
+    if (i0 + r <= a.n) cp_async8(soff + r, a.off + i0 + r);
+  cp_async_commit();
+}
+
+__global__ void __launch_bounds__(ZQ_GRAM_THREADS, 3) zgram_q_kernel(ZqArgs a) {
+  if (__ldg(a.maxz) > 255u) return;  // uniform: a distance wider than a byte, the 32-bit kernel forms them
+  // raw[2][ZQ_QUADS][c1] (the slabs in flight), zs4[ZQ_QUADS][c1], ys[2 * ZQ_QUADS][c1], soff[2][ZQ_ROWS + 2]
+  extern __shared__ __align__(16) uint32_t zqs[];
+  __shared__ unsigned s_deg[ZQ_ROWS];  // light rows: degree; heavy rows: ~0u
+  __shared__ int s_hv[ZQ_ROWS];
+  __shared__ int s_nh;
+  __shared__ ull s_dsum;
+  const int C = a.c1;
+  uint32_t *raw0 = zqs, *raw1 = zqs + ZQ_QUADS * C, *zs4 = zqs + 2 * ZQ_QUADS * C, *ys = zs4 + ZQ_QUADS * C;
+  int64_t *soff0 = (int64_t *)(ys + 2 * ZQ_QUADS * C), *soff1 = soff0 + (ZQ_ROWS + 2);
+  const int t = blockIdx.y * blockDim.x + threadIdx.x;
+  int pb, qb;
+  tile_of(t, a.c0 / 4, a.c1 / 4, pb, qb);
+  const bool active = t < a.ntiles && pb >= 0;
+  uint32_t aI[4][4], aD[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) aI[i][j] = aD[i][j] = 0;
+  auto flush = [&]() {
+    if (!active) return;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int p = 4 * pb + i, q = 4 * qb + j;
+        if (p <= q) {
+          if (aI[i][j]) atomicAdd(a.GI + (int64_t)p * a.ld + q, (ull)aI[i][j]);
+          if (aD[i][j]) atomicAdd(a.GD + (int64_t)p * a.ld + q, (ull)aD[i][j]);
+        }
+        aI[i][j] = aD[i][j] = 0;
+      }
+  };
+  const int64_t nslab = (a.n + ZQ_ROWS - 1) / ZQ_ROWS;
+  ull run = 0;  // bound on every partial sum since the last flush (uniform across the block)
+  if ((int64_t)blockIdx.x < nslab) zq_stage(a, blockIdx.x, raw0, soff0);
+  int buf = 0;
+  for (int64_t s = blockIdx.x; s < nslab; s += gridDim.x, buf ^= 1) {
+    const int64_t i0 = s * ZQ_ROWS;
+    uint32_t *raw = buf ? raw1 : raw0;
+    const int64_t *soff = buf ? soff1 : soff0;
+    cp_async_wait<0>();  // this thread's copies of slab s
+    const unsigned mz = __ldg(a.smaxz + s);
+    const ull mz2 = (ull)mz * mz;
+    __syncthreads();  // slab s visible; the last slab (its buffer, zs4, ys, s_deg, s_hv) consumed
+    // the next slab's copies fly while this one is transformed and multiplied
+    if (s + gridDim.x < nslab) zq_stage(a, s + gridDim.x, buf ? raw0 : raw1, buf ? soff0 : soff1);
+    if (threadIdx.x == 0) {
+      s_nh = 0;
+      s_dsum = 0;
+    }
+    __syncthreads();
+    ull dsum = 0;
+    for (int r = threadIdx.x; r < ZQ_ROWS; r += blockDim.x) {
+      const int64_t i = i0 + r;
+      const unsigned d = i < a.n ? (unsigned)(soff[r + 1] - soff[r]) : 0u;
+      const bool light = (ull)max(d, 1u) * mz <= 65535ull;
+      s_deg[r] = light ? d : ~0u;
+      if (!light) s_hv[atomicAdd(&s_nh, 1)] = r;
+      else if (i < a.n) dsum += max(d, 1u);
+    }
+    dsum = warp_sum(dsum);
+    if ((threadIdx.x & 31) == 0 && dsum) atomicAdd(&s_dsum, dsum);
+    __syncthreads();
+    for (int e = threadIdx.x; e < ZQ_QUADS * C; e += blockDim.x) {
+      const int q = e / C;
+      const uint32_t w = raw[e];
+      uint32_t mask = 0, lo = 0, hi = 0;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const unsigned d = s_deg[4 * q + j];
+        if (d != ~0u) {
+          mask |= 0xffu << (8 * j);
+          const uint32_t y = ((w >> (8 * j)) & 0xffu) * d;  // <= 65535
+          if (j < 2) lo |= y << (16 * j);
+          else hi |= y << (16 * (j - 2));
+        }
+      }
+      const int col = e - q * C;
+      zs4[e] = w & mask;
+      ys[(2 * q) * C + col] = lo;
+      ys[(2 * q + 1) * C + col] = hi;
+    }
+    __syncthreads();
+    const ull b = s_dsum * mz2;
+    if (run + b >= B32) {
+      flush();
+      run = 0;
+    }
+    run += b;
+    if (active) {
+#pragma unroll 1
+      for (int q = 0; q < ZQ_QUADS; q++) {
+        const uint4 zp = *(const uint4 *)(zs4 + q * C + 4 * pb);
+        const uint4 zq = *(const uint4 *)(zs4 + q * C + 4 * qb);
+        const uint4 y0 = *(const uint4 *)(ys + (2 * q) * C + 4 * pb);
+        const uint4 y1 = *(const uint4 *)(ys + (2 * q + 1) * C + 4 * pb);
+        const uint32_t p4[4] = {zp.x, zp.y, zp.z, zp.w}, q4[4] = {zq.x, zq.y, zq.z, zq.w};
+        const uint32_t ya[4] = {y0.x, y0.y, y0.z, y0.w}, yb[4] = {y1.x, y1.y, y1.z, y1.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            aI[i][j] = __dp4a(p4[i], q4[j], aI[i][j]);
+            aD[i][j] = __dp2a_lo(ya[i], q4[j], aD[i][j]);
+            aD[i][j] = __dp2a_hi(yb[i], q4[j], aD[i][j]);
+          }
+      }
+    }
+    // heavy rows of the slab, one at a time (their bytes from the staged words, their degree from the offsets)
+    const int nh = s_nh;
+    for (int h = 0; h < nh; h++) {
+      const int r = s_hv[h];
+      const unsigned d = (unsigned)(soff[r + 1] - soff[r]);
+      const ull bh = (ull)max(d, 1u) * mz2;  // every product of this row is at most bh
+      uint32_t p4[4] = {0, 0, 0, 0}, q4[4] = {0, 0, 0, 0};
+      if (active) {
+        const int sh = 8 * (r & 3);
+        const uint32_t *rq = raw + (r >> 2) * C;
+#pragma unroll
+        for (int ii = 0; ii < 4; ii++) {
+          p4[ii] = (rq[4 * pb + ii] >> sh) & 0xffu;
+          q4[ii] = (rq[4 * qb + ii] >> sh) & 0xffu;
+        }
+      }
+      if (bh >= B32) {  // products that may not fit 32 bits: 64-bit atomics directly (rare hubs)
+        if (active) {
+#pragma unroll
+          for (int ii = 0; ii < 4; ii++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int p = 4 * pb + ii, q = 4 * qb + j;
+              const ull zz = (ull)p4[ii] * q4[j];
+              if (p <= q && zz) {
+                atomicAdd(a.GI + (int64_t)p * a.ld + q, zz);
+                atomicAdd(a.GD + (int64_t)p * a.ld + q, zz * d);
+              }
+            }
+        }
+        continue;
+      }
+      if (run + bh >= B32) {
+        flush();
+        run = 0;
+      }
+      run += bh;
+      if (active) {
+#pragma unroll
+        for (int ii = 0; ii < 4; ii++) {
+          const uint32_t y = p4[ii] * d;
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            aI[ii][j] += p4[ii] * q4[j];
+            aD[ii][j] += y * q4[j];
+          }
+        }
+      }
+    }
+  }
+  flush();
+}
+
+// Z_acc (row-major bytes, n x kp) from the quad layout: thread per (quad, 16 accepted columns); row 4q + r,
+// column t is byte r of Zq[q * ldq + acc_idx[t]]; columns t >= k are zero.
+__global__ void pack_from_zq_kernel(const uint32_t *Zq, int ldq, int64_t n, const int *acc_idx, int k, int kp,
+                                    uint8_t *Z) {
+  __shared__ int s_idx[PHDE_MAX_K];
+  for (int t = threadIdx.x; t < kp; t += blockDim.x) s_idx[t] = t < k ? acc_idx[t] : -1;
+  __syncthreads();
+  const int ng = kp / 16;
+  const int64_t nq = (n + 3) / 4;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nq * ng; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = e / ng;
+    const int g = (int)(e - q * ng);
+    uint32_t w[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int z = s_idx[16 * g + j];
+      w[j] = z >= 0 ? __ldg(Zq + q * ldq + z) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int64_t i = 4 * q + r;
+      if (i >= n) break;
+      const unsigned sel = (unsigned)r | ((unsigned)(r + 4) << 4);  // byte r of x, byte r of y
+      uint32_t o[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        o[c] = __byte_perm(__byte_perm(w[4 * c], w[4 * c + 1], sel), __byte_perm(w[4 * c + 2], w[4 * c + 3], sel),
+                           0x5410);
+      *(uint4 *)(Z + i * kp + 16 * g) = make_uint4(o[0], o[1], o[2], o[3]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
 // The reference's candidate loop (ParHDE.cpp:190-285) on coefficient vectors over Z.  Accepted vector q
 // is S_q = Z A[q][*] (A[q][i] = 0 for i > acc_idx[q]); the candidate with Z index r is x = d_r / ||d_r||,
 // i.e. the vector inv * e_r with inv = 1 / sqrt(G_I[r][r]).  Per candidate:
@@ -271,84 +599,145 @@ struct CoefArgs {
   int *acc_idx;   // [k]
   int *state;     // [0] accepted, [1] discarded, [2] examined, [3] next Z index
   double *dlog;   // [P]: norm of each discarded candidate (by candidate index = Z index - 1); NaN otherwise
+  int sa;         // the accepted rows of A are staged in shared memory too
 };
 
-__global__ void __launch_bounds__(CF_THREADS) coef_kernel(CoefArgs a) {
-  extern __shared__ double cs[];  // rr[ld], gdr[ld], cq[k], then (nc > 0) GIs[nc][nc], GDs[nc][nc]
-  __shared__ double red[32];
+// GB300 issues FP64 at two lanes per clock per SM: a warp-wide FP64 instruction holds the pipe for 16 clocks
+// whatever it computes, so the loop keeps FP64 work in full warps and leaves the scalars (square roots,
+// reciprocals, the final sums) to one thread, broadcast through shared memory.
+__global__ void __launch_bounds__(CF_THREADS, 1) coef_kernel(CoefArgs a) {
+  // rr[ld], gdr[ld], cq[k], rden[k], part[CF_THREADS], then (nc > 0) GIs[nc][nc], GDs[nc][nc], then (sa) As[k][ld]
+  extern __shared__ double cs[];
   __shared__ int s_idx[PHDE_MAX_K];
-  double *rr = cs, *gdr = cs + a.ld, *cq = cs + 2 * a.ld;
-  double *GIs = cq + a.k, *GDs = GIs + (size_t)a.nc * a.nc;
+  __shared__ double s_inv, s_c0, s_nrm;
+  const int ld = a.ld;
+  double *rr = cs, *gdr = cs + ld, *cq = cs + 2 * ld, *rden = cq + a.k, *part = rden + a.k;
+  double *GIs = part + CF_THREADS, *GDs = GIs + (size_t)a.nc * a.nc;
   const int nc = a.nc;
   for (int e = threadIdx.x; e < nc * nc; e += CF_THREADS) {
     const int i = e / nc, j = e - i * nc;
-    GIs[e] = gsym(a.GI, a.ld, i, j);
-    GDs[e] = gsym(a.GD, a.ld, i, j);
+    GIs[e] = gsym(a.GI, ld, i, j);
+    GDs[e] = gsym(a.GD, ld, i, j);
+  }
+  int nacc = a.state[0], ndisc = a.state[1], nexam = a.state[2];
+  // the accepted coefficient rows (zero past each row's own Z index), staged when they fit
+  double *As = a.sa ? GDs + (size_t)nc * nc : a.A;
+  if (a.sa)
+    for (int e = threadIdx.x; e < a.k * ld; e += CF_THREADS) As[e] = e < nacc * ld ? a.A[e] : 0.0;
+  for (int q = threadIdx.x; q < nacc; q += CF_THREADS) {
+    s_idx[q] = a.acc_idx[q];
+    rden[q] = 1.0 / a.den[q];
   }
   __syncthreads();
   // G_I / G_D entry (i, j): from shared memory when staged (every index the loop reads is below r_end <= nc)
-  auto gi = [&](int i, int j) { return nc ? GIs[i * nc + j] : gsym(a.GI, a.ld, i, j); };
-  auto gd = [&](int i, int j) { return nc ? GDs[i * nc + j] : gsym(a.GD, a.ld, i, j); };
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = CF_THREADS / 32;
-  int nacc = a.state[0], ndisc = a.state[1], nexam = a.state[2];
-  for (int q = threadIdx.x; q < nacc; q += CF_THREADS) s_idx[q] = a.acc_idx[q];
+  auto gi = [&](int i, int j) { return nc ? GIs[i * nc + j] : gsym(a.GI, ld, i, j); };
+  auto gd = [&](int i, int j) { return nc ? GDs[i * nc + j] : gsym(a.GD, ld, i, j); };
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double rsn = 1.0 / sqrt((double)a.n);
-  const double den0 = gsym(a.GD, a.ld, 0, 0) * rsn * rsn;  // <u0, D u0> = nnz / n
+  const double den0 = gsym(a.GD, ld, 0, 0) * rsn * rsn;  // <u0, D u0> = nnz / n
   int r = a.state[3];
+  // the per-thread partials in part[] summed by warp 0 in a fixed order; the total lands in thread 0
+  auto total0 = [&](double v) -> double {
+    part[threadIdx.x] = v;
+    __syncthreads();
+    double t = 0;
+    if (warp == 0) {
+      for (int w = lane; w < CF_THREADS; w += 32) t += part[w];
+      t = warp_sum(t);
+    }
+    return t;
+  };
+  // rr^T G rr over the upper triangle: thread (p, sub) takes the rows p and r - p (the middle row once), so
+  // every thread has r + 1 terms, and the columns j > i with j = i + 1 + sub (mod 4)
+  auto quad = [&](auto g) -> double {
+    const int np = (r + 2) / 2;
+    double s = 0;
+    for (int t = threadIdx.x; t < 4 * np; t += CF_THREADS) {
+      const int p = t >> 2, sub = t & 3;
+      for (int h = 0; h < 2; h++) {
+        const int i = h ? r - p : p;
+        if (h && i == p) break;
+        double acc = 0;
+        for (int j = i + 1 + sub; j <= r; j += 4) acc = fma(g(i, j), rr[j], acc);
+        const double ri = rr[i];
+        s += fma(2.0 * ri, acc, sub == 0 ? ri * g(i, i) * ri : 0.0);
+      }
+    }
+    return total0(s);
+  };
   for (; r < a.r_end && nacc < a.k; r++) {
     __syncthreads();
     for (int i = threadIdx.x; i <= r; i += CF_THREADS) gdr[i] = gd(i, r);
-    const double inv = 1.0 / sqrt(gi(r, r));
-    __syncthreads();
-    for (int q = warp; q < nacc; q += nw) {
-      const int top = s_idx[q];
-      const double *Aq = a.A + (int64_t)q * a.ld;
-      double s = 0;
-      for (int i = lane; i <= top; i += 32) s = fma(gdr[i], Aq[i], s);
-      s = warp_sum(s);
-      if (lane == 0) cq[q] = (inv * s) * (1.0 / a.den[q]);
-    }
-    const double c0 = (inv * gdr[0] * rsn) * (1.0 / den0);
-    __syncthreads();
-    for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
-      double v = i == r ? inv : 0.0;
-      if (i == 0) v -= c0 * rsn;
-      for (int q = 0; q < nacc; q++)
-        if (s_idx[q] >= i) v -= cq[q] * a.A[(int64_t)q * a.ld + i];
-      rr[i] = v;
+    if (threadIdx.x == 0) {
+      const double inv = 1.0 / sqrt(gi(r, r));
+      s_inv = inv;
+      s_c0 = (inv * gd(0, r) * rsn) * (1.0 / den0);
     }
     __syncthreads();
-    double s = 0;
-    for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
-      double ti = 0;
-      for (int j = 0; j <= r; j++) ti = fma(gi(i, j), rr[j], ti);
-      s = fma(rr[i], ti, s);
+    const double inv = s_inv, c0 = s_c0;
+    // cq[q] = inv <G_D[r], A[q]> / den[q]: four threads per accepted vector
+    for (int base = 0; base < nacc; base += CF_THREADS / 4) {
+      const int q = base + (threadIdx.x >> 2), sub = threadIdx.x & 3;
+      double v = 0;
+      if (q < nacc) {
+        const int top = s_idx[q];
+        const double *Aq = As + (int64_t)q * ld;
+        for (int i = sub; i <= top; i += 4) v = fma(gdr[i], Aq[i], v);
+      }
+      v += __shfl_xor_sync(PHDE_FULL_MASK, v, 1);
+      v += __shfl_xor_sync(PHDE_FULL_MASK, v, 2);
+      if (q < nacc && sub == 0) cq[q] = (inv * v) * rden[q];
     }
-    const double nrm = sqrt(fmax(block_sum(s, red), 0.0));
+    __syncthreads();
+    // rr = inv e_r - c0 e_0 / sqrt(n) - sum_q cq[q] A[q]: four threads per index i, the terms q of accepted index
+    // >= i (the accepted indices increase with q: a binary search finds the first)
+    for (int base = 0; base <= r; base += CF_THREADS / 4) {
+      const int i = base + (threadIdx.x >> 2), sub = threadIdx.x & 3;
+      double v = 0;
+      if (i <= r) {
+        int lo = 0, hi = nacc;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (s_idx[mid] < i) lo = mid + 1;
+          else hi = mid;
+        }
+        for (int q = lo + sub; q < nacc; q += 4) v = fma(cq[q], As[(int64_t)q * ld + i], v);
+      }
+      v += __shfl_xor_sync(PHDE_FULL_MASK, v, 1);
+      v += __shfl_xor_sync(PHDE_FULL_MASK, v, 2);
+      if (i <= r && sub == 0) {
+        double b = i == r ? inv : 0.0;
+        if (i == 0) b -= c0 * rsn;
+        rr[i] = b - v;
+      }
+    }
+    __syncthreads();
+    const double n2 = quad(gi);
+    if (threadIdx.x == 0) s_nrm = sqrt(fmax(n2, 0.0));
+    __syncthreads();
+    const double nrm = s_nrm;
     nexam++;
     if (nrm < 0.001) {
       if (threadIdx.x == 0) a.dlog[r - 1] = nrm;
       ndisc++;
       continue;
     }
-    const double sc = 1.0 / nrm;
-    double *An = a.A + (int64_t)nacc * a.ld;
+    if (threadIdx.x == 0) s_inv = 1.0 / nrm;
+    __syncthreads();
+    const double sc = s_inv;
+    double *An = a.A + (int64_t)nacc * ld;
     for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
       const double v = rr[i] * sc;
       rr[i] = v;
       An[i] = v;
+      if (a.sa) As[(int64_t)nacc * ld + i] = v;
     }
     __syncthreads();
-    double dsum = 0;
-    for (int i = threadIdx.x; i <= r; i += CF_THREADS) {
-      double ti = 0;
-      for (int j = 0; j <= r; j++) ti = fma(gd(i, j), rr[j], ti);
-      dsum = fma(rr[i], ti, dsum);
-    }
-    dsum = block_sum(dsum, red);
+    const double dsum = quad(gd);
     if (threadIdx.x == 0) {
       a.den[nacc] = dsum;
       a.acc_idx[nacc] = r;
+      rden[nacc] = 1.0 / dsum;
     }
     s_idx[nacc] = r;  // every thread writes the same value
     nacc++;
@@ -401,27 +790,55 @@ __global__ void pack_kernel(ZSrc src, int64_t n, const int *acc_idx, int k, int 
 // Sums: for uint8 rows two columns share a 32-bit register as 16-bit halves (bytes moved apart by one byte
 // permute; an item has at most 256 neighbours of at most 255, so no half ever carries into the next, also
 // after the groups are added together); uint16 rows sum each column in its own register.
-template <typename T>
+// SMALL (uint8 rows whose values are at most 15): the words of up to 16 neighbours are added as they are, four
+// byte lanes per register (16 * 15 < 256: no lane carries into the next), and spread into the 16-bit halves
+// every 16 rows -- one add per four columns instead of two permutes and two adds.
+template <typename T, bool SMALL = false>
 struct Sum16 {  // the sums of one 16-byte slice of a row: 16 uint8 or 8 uint16 columns, in 8 registers
   uint32_t s[8];
+  uint32_t b[SMALL ? 4 : 1];  // SMALL: byte-lane sums not yet spread
+  int pend;                   // SMALL: rows in b
   __device__ __forceinline__ void zero() {
 #pragma unroll
     for (int i = 0; i < 8; i++) s[i] = 0;
+    if constexpr (SMALL) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) b[i] = 0;
+      pend = 0;
+    }
+  }
+  __device__ __forceinline__ void spread() {
+    if constexpr (SMALL) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        s[2 * i] += __byte_perm(b[i], 0u, 0x4140);
+        s[2 * i + 1] += __byte_perm(b[i], 0u, 0x4342);
+        b[i] = 0;
+      }
+      pend = 0;
+    }
   }
   __device__ __forceinline__ void add(const uint4 &v) {
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    if constexpr (SMALL) {
+      if (pend == 16) spread();
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-      if (sizeof(T) == 1) {
-        s[2 * i] += __byte_perm(w[i], 0u, 0x4140);
-        s[2 * i + 1] += __byte_perm(w[i], 0u, 0x4342);
-      } else {
-        s[2 * i] += w[i] & 0xffffu;
-        s[2 * i + 1] += w[i] >> 16;
+      for (int i = 0; i < 4; i++) b[i] += w[i];
+      pend++;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        if (sizeof(T) == 1) {
+          s[2 * i] += __byte_perm(w[i], 0u, 0x4140);
+          s[2 * i + 1] += __byte_perm(w[i], 0u, 0x4342);
+        } else {
+          s[2 * i] += w[i] & 0xffffu;
+          s[2 * i + 1] += w[i] >> 16;
+        }
       }
     }
   }
-  __device__ __forceinline__ void add_from(int lane_mask) {  // add the sums of lane ^ lane_mask
+  __device__ __forceinline__ void add_from(int lane_mask) {  // add the sums of lane ^ lane_mask (after spread())
 #pragma unroll
     for (int i = 0; i < 8; i++) s[i] += __shfl_xor_sync(PHDE_FULL_MASK, s[i], lane_mask);
   }
@@ -451,11 +868,13 @@ struct LgArgs {
   int ntiles;
 };
 
-template <typename T, int KP, int TS>
-__global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
+template <typename T, int KP, int TS, bool SMALL = false>
+__global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgArgs a) {
   constexpr int V = 16 / (int)sizeof(T);  // columns per 16-byte slice
   constexpr int LPR = KP / V;             // lanes per row
   constexpr int G = 32 / LPR;             // neighbour rows per load instruction
+  constexpr int CPL = V / G;              // columns of a slice each lane finishes (2, 4 or 8)
+  constexpr int RPL = sizeof(T) == 1 ? CPL / 2 : CPL;  // sum registers those columns sit in
   constexpr int SL = KP + 4;
   extern __shared__ int lsm[];  // zs[LG_ITEMS][SL], rs[LG_ITEMS][SL]
   __shared__ ull s_bnd[LG_ITEMS];
@@ -517,7 +936,7 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
       }
       unsigned zm = 0, rm = 0;
       if (row >= 0) {
-        Sum16<T> nb;
+        Sum16<T, SMALL> nb;
         nb.zero();
         // the packed rows are gathered again and again (evict-last in L2), the adjacency streams by once
         const uint64_t keep = l2_policy_evict_last(), stream = l2_policy_evict_first();
@@ -530,30 +949,48 @@ __global__ void __launch_bounds__(LG_THREADS) lgram_kernel(LgArgs a) {
           nb.add(x1);
         }
         if (e < e1) nb.add(ld_nc_hint16((const uint4 *)(Z + (int64_t)ld_nc_hint(a.adj + e, stream) * KP) + pi, keep));
+        nb.spread();
 #pragma unroll
         for (int m = LPR; m < 32; m <<= 1) nb.add_from(m);
-        if (gi == 0) {
-          const uint4 own = __ldg((const uint4 *)(Z + row * KP) + pi);
-          const int deg = diag ? (int)(a.off[row + 1] - a.off[row]) : 0;
+        // every group of the warp now holds the row's sums: lane (gi, pi) finishes columns gi * CPL .. + CPL of
+        // slice pi (sum registers gi * RPL .. + RPL, picked by selects: no indexed register arrays)
+        const uint4 own = __ldg((const uint4 *)(Z + row * KP) + pi);
+        const int deg = diag ? (int)(a.off[row + 1] - a.off[row]) : 0;
+        int zi[CPL], r[CPL];
 #pragma unroll
-          for (int c4 = 0; c4 < V; c4 += 4) {
-            int zi[4], r[4];
+        for (int k2 = 0; k2 < RPL; k2++) {
+          const int want = gi * RPL + k2;
+          uint32_t sv = nb.s[0];
 #pragma unroll
-            for (int c = 0; c < 4; c++) {
-              zi[c] = slice_val<T>(own, c4 + c);
-              r[c] = deg * zi[c] - nb.get(c4 + c);
-              zm = max(zm, (unsigned)zi[c]);
-              rm = max(rm, (unsigned)abs(r[c]));
-            }
-            *(int4 *)(zs + slot * SL + pi * V + c4) = make_int4(zi[0], zi[1], zi[2], zi[3]);
-            *(int4 *)(rs + slot * SL + pi * V + c4) = make_int4(r[0], r[1], r[2], r[3]);
+          for (int j = 1; j < 8; j++) sv = want == j ? nb.s[j] : sv;
+          // the own row's word holding these columns
+          const int c0 = gi * CPL + k2 * (CPL / RPL);
+          const int wi = sizeof(T) == 1 ? c0 >> 2 : c0 >> 1;
+          const uint32_t ow = wi == 0 ? own.x : wi == 1 ? own.y : wi == 2 ? own.z : own.w;
+#pragma unroll
+          for (int h = 0; h < CPL / RPL; h++) {
+            const int c = k2 * (CPL / RPL) + h;
+            const int z = sizeof(T) == 1 ? (int)((ow >> (8 * ((c0 + h) & 3))) & 0xffu)
+                                         : (int)((ow >> (16 * ((c0 + h) & 1))) & 0xffffu);
+            const int sum = sizeof(T) == 1 ? (int)((sv >> (16 * h)) & 0xffffu) : (int)sv;
+            zi[c] = z;
+            r[c] = deg * z - sum;
+            zm = max(zm, (unsigned)z);
+            rm = max(rm, (unsigned)abs(r[c]));
           }
         }
-      } else if (gi == 0) {
+        int *zd = zs + slot * SL + pi * V + gi * CPL, *rd = rs + slot * SL + pi * V + gi * CPL;
 #pragma unroll
-        for (int c4 = 0; c4 < V; c4 += 4) {
-          *(int4 *)(zs + slot * SL + pi * V + c4) = make_int4(0, 0, 0, 0);
-          *(int4 *)(rs + slot * SL + pi * V + c4) = make_int4(0, 0, 0, 0);
+        for (int c = 0; c < CPL; c += 2) {
+          *(int2 *)(zd + c) = make_int2(zi[c], zi[c + 1]);
+          *(int2 *)(rd + c) = make_int2(r[c], r[c + 1]);
+        }
+      } else {
+        int *zd = zs + slot * SL + pi * V + gi * CPL, *rd = rs + slot * SL + pi * V + gi * CPL;
+#pragma unroll
+        for (int c = 0; c < CPL; c += 2) {
+          *(int2 *)(zd + c) = make_int2(0, 0);
+          *(int2 *)(rd + c) = make_int2(0, 0);
         }
       }
       zm = __reduce_max_sync(PHDE_FULL_MASK, zm);
@@ -819,18 +1256,53 @@ int grid_n(phde_ctx *ctx, int64_t work, int threads, int per_sm) {
 // ==================================================================================================
 // host side
 
-// G_I, G_D for Z columns p < c1, q in [c0, c1).
+// G_I, G_D for Z columns p < c1, q in [c0, c1).  byte_state: 1 every distance fits a byte (the quad layout:
+// pack Z columns [c0, c1), then the byte kernel), 0 some does not (the 32-bit kernel), -1 not known yet (both
+// are launched; each checks maxz, which the pack kernel completes first, and one returns at once).
 static int exact_zgram(phde_ctx *ctx, const ZSrc &src, int P, int c0, int c1, ull *GI, ull *GD, int ld,
-                       unsigned *maxz) {
+                       unsigned *maxz, uint32_t *Zq, unsigned *smaxz, int byte_state) {
   const int nq = (c1 - c0) / 4;
   const int ntiles = nq * (c0 / 4) + nq * (nq + 1) / 2;
+  if (byte_state != 0) {
+    const int64_t nslab = (ctx->n + ZQ_ROWS - 1) / ZQ_ROWS;
+    int pk_sm = 0;
+    PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pk_sm, zq_pack_kernel, ZQ_THREADS, 0));
+    const int gp = (int)std::max<int64_t>(1, std::min<int64_t>(nslab, (int64_t)ctx->nsm * std::max(pk_sm, 1)));
+    zq_pack_kernel<<<gp, ZQ_THREADS, 0, ctx->stream>>>(src, ctx->d_off, ctx->n, P, c0, c1, ld, Zq, smaxz, maxz);
+    PHDE_LAUNCHED(ctx);
+    const int threads = std::min(ZQ_GRAM_THREADS, (ntiles + 31) / 32 * 32);
+    const int gy = (ntiles + threads - 1) / threads;
+    const size_t smem = sizeof(uint32_t) * 5 * ZQ_QUADS * (size_t)c1 + sizeof(int64_t) * 2 * (ZQ_ROWS + 2);
+    PHDE_CK(ctx, cudaFuncSetAttribute(zgram_q_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zgram_q_kernel, threads, smem));
+    per_sm = std::max(1, std::min(per_sm, 4));
+    // every CTA resident at once: the slabs are dealt out evenly, so a partial second wave would double the time
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm / gy, nslab));
+    ZqArgs q;
+    q.Zq = Zq;
+    q.ldq = ld;
+    q.off = ctx->d_off;
+    q.n = ctx->n;
+    q.c0 = c0;
+    q.c1 = c1;
+    q.ntiles = ntiles;
+    q.GI = GI;
+    q.GD = GD;
+    q.ld = ld;
+    q.smaxz = smaxz;
+    q.maxz = maxz;
+    zgram_q_kernel<<<dim3(gx, gy), threads, smem, ctx->stream>>>(q);
+    PHDE_LAUNCHED(ctx);
+    if (byte_state == 1) return PHDE_OK;
+  }
   const int gy = (ntiles + ZG_THREADS - 1) / ZG_THREADS;
   const size_t smem = sizeof(int) * ((ZG_ROWS + ZG_ROWS / 4 + ZG_ROWS / 2) * (size_t)(c1 + 4) + c1);
   PHDE_CK(ctx, cudaFuncSetAttribute(zgram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zgram_kernel, ZG_THREADS, smem));
   per_sm = std::max(1, std::min(per_sm, 4));
-  const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm / gy + 1,
+  const int gx = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->nsm * per_sm / gy,
                                                               (ctx->n + ZG_ROWS - 1) / ZG_ROWS));
   ZgArgs a;
   a.src = src;
@@ -844,6 +1316,7 @@ static int exact_zgram(phde_ctx *ctx, const ZSrc &src, int P, int c0, int c1, ul
   a.GD = GD;
   a.ld = ld;
   a.maxz = maxz;
+  a.wide_only = byte_state < 0 ? maxz : nullptr;
   zgram_kernel<<<dim3(gx, gy), ZG_THREADS, smem, ctx->stream>>>(a);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
@@ -866,7 +1339,11 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
   int *state = (int *)phde_buf(ctx, "ex.state", sizeof(int) * 4);
   unsigned *maxz = (unsigned *)phde_buf(ctx, "ex.maxz", sizeof(unsigned) * 2);
   double *dlog = (double *)phde_buf(ctx, "ex.dlog", sizeof(double) * P);
-  if (!GI || !GD || !A || !den || !acc_idx || !state || !maxz || !dlog) return PHDE_ERR_OOM;
+  const int64_t nslab = (n + ZQ_ROWS - 1) / ZQ_ROWS;
+  uint32_t *Zq = (uint32_t *)phde_buf(ctx, "ex.Zq", sizeof(uint32_t) * (size_t)nslab * ZQ_QUADS * ld);
+  unsigned *smaxz = (unsigned *)phde_buf(ctx, "ex.smaxz", sizeof(unsigned) * nslab);
+  if (!GI || !GD || !A || !den || !acc_idx || !state || !maxz || !dlog || !Zq || !smaxz) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemsetAsync(smaxz, 0, sizeof(unsigned) * nslab, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(GI, 0, sizeof(ull) * ld * ld, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(GD, 0, sizeof(ull) * ld * ld, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(A, 0, sizeof(double) * (size_t)k * ld, ctx->stream));
@@ -874,17 +1351,19 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
   PHDE_CK(ctx, cudaMemsetAsync(maxz, 0, sizeof(unsigned) * 2, ctx->stream));
   const int st0[4] = {0, 0, 0, 1};
   PHDE_CK(ctx, cudaMemcpyAsync(state, st0, sizeof(st0), cudaMemcpyHostToDevice, ctx->stream));
-  const size_t csmem0 = sizeof(double) * (2 * (size_t)ld + k);
+  const size_t csmem0 = sizeof(double) * (2 * (size_t)ld + 2 * (size_t)k + CF_THREADS);
   constexpr size_t CF_SMEM_MAX = 200 * 1024;
   PHDE_CK(ctx, cudaFuncSetAttribute(coef_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_SMEM_MAX));
   int c0 = 0, c1 = std::min(ld, (1 + std::min(P, k + std::max(4, k / 8)) + 3) / 4 * 4);
   int hs[4] = {0, 0, 0, 1};
   unsigned hm[2] = {0, 0};
+  int byte_state = -1;
   for (;;) {
-    int rc = exact_zgram(ctx, src, P, c0, c1, GI, GD, ld, maxz);
+    int rc = exact_zgram(ctx, src, P, c0, c1, GI, GD, ld, maxz, Zq, smaxz, byte_state);
     if (rc) return rc;
     PHDE_CK(ctx, cudaMemcpyAsync(hm, maxz, sizeof(hm), cudaMemcpyDeviceToHost, ctx->stream));
     PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    byte_state = hm[0] <= 255u ? 1 : 0;
     // G_I, G_D, Z^T L Z entries are at most nnz * maxz^2 (and n * maxz^2): exact in FP64 below 2^53; the
     // Laplacian rows r = deg z - sum z stay in 32 bits; distances fit 16 bits
     const double mz = (double)hm[0];
@@ -898,7 +1377,9 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
     // stage the Gram blocks the loop reads when both fit next to the vectors
     const int rend = std::min(c1, P + 1);
     ca.nc = csmem0 + sizeof(double) * 2 * (size_t)rend * rend <= CF_SMEM_MAX ? rend : 0;
-    const size_t csmem = csmem0 + sizeof(double) * 2 * (size_t)ca.nc * ca.nc;
+    size_t csmem = csmem0 + sizeof(double) * 2 * (size_t)ca.nc * ca.nc;
+    ca.sa = csmem + sizeof(double) * (size_t)k * ld <= CF_SMEM_MAX;
+    if (ca.sa) csmem += sizeof(double) * (size_t)k * ld;
     ca.n = n;
     ca.r_end = std::min(c1, P + 1);
     ca.k = k;
@@ -927,6 +1408,7 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
   eb->maxz = hm[0];
   eb->maxdeg = hm[1];
   eb->Z = nullptr;
+  eb->Zq = byte_state == 1 ? Zq : nullptr;  // every accepted column is packed (examined blocks only)
   return PHDE_OK;
 }
 
@@ -941,6 +1423,9 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
   const int gp = grid_n(ctx, n, 256, 8);
   if (z16)
     pack_kernel<uint16_t><<<gp, 256, 0, ctx->stream>>>(src, n, eb->acc_idx, k, kp, (uint16_t *)Z);
+  else if (eb->Zq)
+    pack_from_zq_kernel<<<grid_n(ctx, (n + 3) / 4 * (kp / 16), 256, 8), 256, 0, ctx->stream>>>(
+        eb->Zq, eb->ld, n, eb->acc_idx, k, kp, (uint8_t *)Z);
   else
     pack_kernel<uint8_t><<<gp, 256, 0, ctx->stream>>>(src, n, eb->acc_idx, k, kp, (uint8_t *)Z);
   PHDE_LAUNCHED(ctx);
@@ -987,6 +1472,10 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
     if (kp == 64) rc = launch(lgram_kernel<uint16_t, 64, 4>);
     else if (kp == 128) rc = launch(lgram_kernel<uint16_t, 128, 8>);
     else rc = launch(lgram_kernel<uint16_t, 256, 8>);
+  } else if (eb->maxz <= 15u) {
+    if (kp == 64) rc = launch(lgram_kernel<uint8_t, 64, 4, true>);
+    else if (kp == 128) rc = launch(lgram_kernel<uint8_t, 128, 8, true>);
+    else rc = launch(lgram_kernel<uint8_t, 256, 8, true>);
   } else {
     if (kp == 64) rc = launch(lgram_kernel<uint8_t, 64, 4>);
     else if (kp == 128) rc = launch(lgram_kernel<uint8_t, 128, 8>);

@@ -58,7 +58,16 @@ __global__ void feature_raw_kernel(const int64_t *off, const uint32_t *adj, cons
         act = false;
       } else {
         const int32_t dv = d0[v];
-        for (int64_t e = e0 + gl; e < e1; e += 8) feature_edge(__ldg(pk + __ldg(adj + e)), dv, h, o);
+        int64_t e = e0 + gl;
+        for (; e + 24 < e1; e += 32) {  // four gathers in flight per lane: the loop is latency bound
+          const uint32_t u0 = __ldg(adj + e), u1 = __ldg(adj + e + 8), u2 = __ldg(adj + e + 16), u3 = __ldg(adj + e + 24);
+          const ull p0 = __ldg(pk + u0), p1 = __ldg(pk + u1), p2 = __ldg(pk + u2), p3 = __ldg(pk + u3);
+          feature_edge(p0, dv, h, o);
+          feature_edge(p1, dv, h, o);
+          feature_edge(p2, dv, h, o);
+          feature_edge(p3, dv, h, o);
+        }
+        for (; e < e1; e += 8) feature_edge(__ldg(pk + __ldg(adj + e)), dv, h, o);
       }
     }
     for (int s = 4; s > 0; s >>= 1) {
@@ -297,6 +306,16 @@ __global__ void cand_distances_kernel(const int32_t *D, int P0, const uint16_t *
   }
 }
 
+// The scoring grid: every CTA resident at once (a grid-stride loop over 128-vertex tiles gives each the same
+// share, and a second, partial wave of CTAs would double the time of the first).
+int mlp_grid(phde_ctx *ctx, int64_t n, size_t smem, int *grid) {
+  int per_sm = 0;
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_score_kernel, 256, smem));
+  per_sm = std::max(per_sm, 1);
+  *grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * per_sm));
+  return PHDE_OK;
+}
+
 }  // namespace
 
 int phde_default_pivot_model(const float **w, int *count) {
@@ -340,9 +359,10 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
   PHDE_LAUNCHED(ctx);
   feature_max_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, n, maxes);
   PHDE_LAUNCHED(ctx);
-  const int gm = (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * 4));
   const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE + sizeof(unsigned) * nbins;
   PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
+  int gm = 0;
+  if ((rc = mlp_grid(ctx, n, mlp_smem, &gm))) return rc;
   mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts, score, hist,
                                                        nbins, nullptr);
   PHDE_LAUNCHED(ctx);
@@ -425,9 +445,10 @@ int phde_batch_scores(phde_ctx *ctx, const float *d_weights, const int32_t *d_d0
   PHDE_LAUNCHED(ctx);
   feature_max_batched_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, ctx->d_gid, n, maxes);
   PHDE_LAUNCHED(ctx);
-  const int gm = (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * 4));
   const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE;
   PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
+  int gm = 0;
+  if (int rc2 = mlp_grid(ctx, n, mlp_smem, &gm)) return rc2;
   mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, d_weights, score,
                                                        nullptr, 0, ctx->d_gid);
   PHDE_LAUNCHED(ctx);

@@ -46,7 +46,13 @@ struct MsArgs {
   // candidates share the bit positions, the components never meet; the level-0 frontier list is left for
   // the first level to build (built_f false)
   int nlist, period;
-  uint16_t *R;     // row-major n x RW distance record: R[v*RW + b] = level + 1 (0 = unreached)
+  uint16_t *R;     // row-major n x RW distance record: R[v*RW + b] = level + 1 (0 = unreached); null in level mode
+  // level mode (lvl non-null): no record; the frontier words of every level stay, level L's in
+  // lvl[L * n * W ..] (array 0: the sources; arrays 0 and 1 zeroed by the host, array L + 2 cleared during
+  // level L), so bit b of vertex v is set in exactly the array of its distance from source b.  lcap: the
+  // last array allocated.
+  ull *lvl;
+  int lcap;
   int RW;          // row width (all sources of all sweeps, a multiple of 64)
   int col0;        // first source of this sweep within the row
   ull *seen;       // [n*W]
@@ -86,7 +92,9 @@ struct MsArgs {
 // Frontier words of one vertex, kept in L2 (evict-last): every level gathers them from many neighbours.
 template <int W>
 __device__ __forceinline__ void ld_front(const ull *p, ull (&x)[W], uint64_t keep) {
-  if constexpr (W == 4 || W == 2) {
+  if constexpr (W == 4) {
+    ld_cg_hint32(p, keep, x);  // one L2 request for the vertex's 32 bytes
+  } else if constexpr (W == 2) {
 #pragma unroll
     for (int h = 0; h < W / 2; h++) {
       const uint4 a = ld_cg_hint(p + 2 * h, keep);
@@ -102,11 +110,7 @@ __device__ __forceinline__ void ld_front(const ull *p, ull (&x)[W], uint64_t kee
 template <int W>
 __device__ __forceinline__ void ld_words(const ull *p, ull (&x)[W]) {
   if constexpr (W == 4) {
-    const uint4 a = __ldcg((const uint4 *)p), b = __ldcg((const uint4 *)(p + 2));
-    x[0] = ((ull)a.y << 32) | a.x;
-    x[1] = ((ull)a.w << 32) | a.z;
-    x[2] = ((ull)b.y << 32) | b.x;
-    x[3] = ((ull)b.w << 32) | b.z;
+    asm volatile("ld.global.cg.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(x[0]), "=l"(x[1]), "=l"(x[2]), "=l"(x[3]) : "l"(p));
   } else if constexpr (W == 2) {
     const uint4 a = __ldcg((const uint4 *)p);
     x[0] = ((ull)a.y << 32) | a.x;
@@ -137,12 +141,14 @@ __device__ __forceinline__ bool ms_group_finalise(const MsArgs &a, int64_t v, co
     nw[w] = acc[w] & ~s[w];
     any |= nw[w] != 0ull;
   }
-  ull *row = (ull *)(a.R + v * a.RW + a.col0);
+  if (a.R) {
+    ull *row = (ull *)(a.R + v * a.RW + a.col0);
 #pragma unroll
-  for (int i = 0; i < 2 * W; i++) {
-    const int gi = gl + 8 * (i & 1);
-    const unsigned nib = (unsigned)(nw[i >> 1] >> (4 * gi)) & 15u;
-    if (nib) red_or_hint(row + gl + 8 * i, nibble_lanes(nib, val), l2_policy_evict_first());  // a reduction in L2
+    for (int i = 0; i < 2 * W; i++) {
+      const int gi = gl + 8 * (i & 1);
+      const unsigned nib = (unsigned)(nw[i >> 1] >> (4 * gi)) & 15u;
+      if (nib) red_or_hint(row + gl + 8 * i, nibble_lanes(nib, val), l2_policy_evict_first());  // a reduction in L2
+    }
   }
 #pragma unroll
   for (int w = 0; w < W; w++)
@@ -159,7 +165,7 @@ __device__ __forceinline__ bool ms_thread_finalise(const MsArgs &a, int64_t v, c
                                                    int32_t L) {
   const unsigned val = (unsigned)(L + 2);
   bool any = false;
-  ull *row = (ull *)(a.R + v * a.RW + a.col0);
+  ull *row = a.R ? (ull *)(a.R + v * a.RW + a.col0) : nullptr;
 #pragma unroll
   for (int w = 0; w < W; w++) {
     const ull s = a.seen[v * W + w];
@@ -168,10 +174,11 @@ __device__ __forceinline__ bool ms_thread_finalise(const MsArgs &a, int64_t v, c
     if (nw) {
       any = true;
       a.seen[v * W + w] = s | nw;
-      for (int gi = 0; gi < 16; gi++) {
-        const unsigned nib = (unsigned)(nw >> (4 * gi)) & 15u;
-        if (nib) atomicOr(row + 16 * w + gi, nibble_lanes(nib, val));
-      }
+      if (row)
+        for (int gi = 0; gi < 16; gi++) {
+          const unsigned nib = (unsigned)(nw >> (4 * gi)) & 15u;
+          if (nib) atomicOr(row + 16 * w + gi, nibble_lanes(nib, val));
+        }
     }
   }
   return any;
@@ -270,7 +277,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       atomicOr(a.seen + s * W + (b >> 6), 1ull << (b & 63));
       atomicOr(a.front[0] + s * W + (b >> 6), 1ull << (b & 63));
       atomicOr(a.fbm[0] + (s >> 5), 1u << (s & 31));
-      a.R[s * a.RW + a.col0 + b] = 1;
+      if (a.R) a.R[s * a.RW + a.col0 + b] = 1;
       my += (1ull << 32) | (ull)(a.off[s + 1] - a.off[s]);
     }
     my = warp_sum(my);
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       atomicOr(a.seen + s * W + (b >> 6), 1ull << (b & 63));
       atomicOr(a.front[0] + s * W + (b >> 6), 1ull << (b & 63));
       atomicOr(a.fbm[0] + (s >> 5), 1u << (s & 31));
-      a.R[s * a.RW + a.col0 + b] = 1;  // level 0
+      if (a.R) a.R[s * a.RW + a.col0 + b] = 1;  // level 0
     }
   for (int64_t h = gt; h < a.nheavy; h += gts) {
     const int64_t v = a.heavy_rows[h];
@@ -308,8 +315,17 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       if (gt == 0) atomicCAS(a.err, 0, PHDE_ERR_TOO_LARGE);
       return;
     }
-    const ull *fcur = a.front[L & 1];
-    ull *fnext = a.front[(L + 1) & 1];
+    if (a.lvl && L + 1 > a.lcap) {  // more levels than the arrays allow (uniform): the caller uses the record
+      if (gt == 0) atomicCAS(a.err, 0, PHDE_ERR_TOO_LARGE);
+      return;
+    }
+    const int64_t nW = n * W;
+    const ull *fcur = a.lvl ? a.lvl + (int64_t)L * nW : a.front[L & 1];
+    ull *fnext = a.lvl ? a.lvl + (int64_t)(L + 1) * nW : a.front[(L + 1) & 1];
+    if (a.lvl && L + 2 <= a.lcap) {  // the array level L + 1 writes, cleared one level ahead
+      ull *ahead = a.lvl + (int64_t)(L + 2) * nW;
+      for (int64_t i = gt; i < nW; i += gts) ahead[i] = 0ull;
+    }
     const uint32_t *fbm_cur = a.fbm[L % 3];
     uint32_t *fbm_next = a.fbm[(L + 1) % 3];
     {
@@ -350,8 +366,10 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
           block_push(nz, (uint32_t)v, dv, a.qv[sf], a.qe[sf], a.lctr + sf, &psc);
         }
       }
-      // stale output words (the vertices given bits at level L-2) go to zero: from its list, or all
-      if (built_z) {
+      // stale output words (the vertices given bits at level L-2) go to zero: from its list, or all (level
+      // mode: the array is fresh)
+      if (a.lvl) {
+      } else if (built_z) {
         const uint32_t zcnt = (uint32_t)(__ldcg(a.lctr + sz) >> 32);
         for (int64_t i = gt; i < zcnt; i += gts) {
           const int64_t v = a.qv[sz][i];
@@ -599,16 +617,30 @@ int phde_heavy_chunks(phde_ctx *ctx, const int64_t **chunk_row, const int64_t **
 
 // The sweep: sources d_src (nlist entries; bit = entry, or entry % period for batches), optionally without
 // host synchronisation (sync false: no error read-back and no level count -- for captured sequences).
+// Level mode (lvl_cap > 0, one sweep of at most 256 sources, no batch): no record, the per-level frontier arrays
+// 0 .. lvl_cap are kept and returned through *lv; more levels than lvl_cap give PHDE_ERR_TOO_LARGE.
 static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, int period, bool sync, uint16_t **R_out,
-                     int *RW_out) {
+                     int *RW_out, int lvl_cap = 0, MsLevels *lv = nullptr) {
   const int64_t n = ctx->n;
   if (nsrc < 1 || (period > 0 && (nsrc != period || period > 64 * MS_MAXW))) return PHDE_ERR_INVALID;
+  if (lvl_cap > 0 && (nsrc > 64 * MS_MAXW || period > 0 || !lv || !sync)) return PHDE_ERR_INVALID;
+  int last_nlev = 0;
   const int RW = (nsrc + 63) / 64 * 64;
   const int Wmax = MS_MAXW;
-  uint16_t *R = (uint16_t *)phde_buf(ctx, "ms.R", sizeof(uint16_t) * n * RW);
+  uint16_t *R = nullptr;
   ull *seen = (ull *)phde_buf(ctx, "ms.seen", sizeof(ull) * n * Wmax);
-  ull *f0 = (ull *)phde_buf(ctx, "ms.f0", sizeof(ull) * n * Wmax);
-  ull *f1 = (ull *)phde_buf(ctx, "ms.f1", sizeof(ull) * n * Wmax);
+  ull *f0, *f1, *lvl = nullptr;
+  if (lvl_cap > 0) {
+    const int W1 = (nsrc + 63) / 64;
+    lvl = (ull *)phde_buf(ctx, "ms.lvl", sizeof(ull) * (size_t)(lvl_cap + 1) * n * W1);
+    if (!lvl) return PHDE_ERR_OOM;
+    f0 = lvl;
+    f1 = lvl + n * W1;
+  } else {
+    R = (uint16_t *)phde_buf(ctx, "ms.R", sizeof(uint16_t) * n * RW);
+    f0 = (ull *)phde_buf(ctx, "ms.f0", sizeof(ull) * n * Wmax);
+    f1 = (ull *)phde_buf(ctx, "ms.f1", sizeof(ull) * n * Wmax);
+  }
   ull *hacc = (ull *)phde_buf(ctx, "ms.hacc", sizeof(ull) * n * Wmax);
   int *levels = (int *)phde_buf(ctx, "ms.levels", sizeof(int));
   const int64_t nw32 = (n + 31) / 32, lcap = n + 256;  // a level list holds each vertex once; the sources' may repeat
@@ -620,14 +652,14 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
   // lctr[4], lstat[4], ccount[2], tctr[4]
   const size_t ctr_bytes = sizeof(ull) * 8 + sizeof(unsigned) * 6;
   ull *lctr = (ull *)phde_buf(ctx, "ms.lctr", ctr_bytes);
-  if (!R || !seen || !f0 || !f1 || !hacc || !levels || !bms || !fbm || !lists || !cand || !stamp || !lctr)
+  if ((!R && !lvl) || !seen || !f0 || !f1 || !hacc || !levels || !bms || !fbm || !lists || !cand || !stamp || !lctr)
     return PHDE_ERR_OOM;
   const int64_t *crow, *ce0;
   int64_t nch, chunk;
   int rc0 = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
   if (rc0) return rc0;
   const int64_t *hrows = (const int64_t *)phde_buf(ctx, "ms.hrows", 0);
-  PHDE_CK(ctx, cudaMemsetAsync(R, 0, sizeof(uint16_t) * (size_t)n * RW, ctx->stream));
+  if (R) PHDE_CK(ctx, cudaMemsetAsync(R, 0, sizeof(uint16_t) * (size_t)n * RW, ctx->stream));
   PHDE_CK(ctx, cudaMemsetAsync(hacc, 0, sizeof(ull) * n * Wmax, ctx->stream));
   // optional per-level trace (PHDE_MSBFS_TRACE=<file>): end time and vertices given new bits per level
   const char *trace_path = getenv("PHDE_MSBFS_TRACE");
@@ -664,6 +696,8 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
     a.R = R;
     a.RW = RW;
     a.col0 = s0;
+    a.lvl = lvl;
+    a.lcap = lvl_cap;
     a.seen = seen;
     a.front[0] = f0;
     a.front[1] = f1;
@@ -709,6 +743,7 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
     PHDE_CK(ctx, cudaMemcpyAsync(&nlev, levels, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->msbfs_levels += nlev;
+    last_nlev = nlev;
     if (trace) {
       int nl = 0;
       std::vector<ull> h(2 * trace_cap);
@@ -726,6 +761,11 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
   }
   *R_out = R;
   *RW_out = RW;
+  if (lv) {
+    lv->lvl = lvl;
+    lv->W = (nsrc + 63) / 64;
+    lv->nlev = last_nlev;  // one sweep
+  }
   return PHDE_OK;
 }
 
@@ -733,6 +773,13 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
 // record R (n x RW uint16, RW = nsrc rounded up to 64; level + 1, 0 = unreached), returned through *R_out.
 int phde_msbfs_record(phde_ctx *ctx, const int64_t *d_src, int nsrc, uint16_t **R_out, int *RW_out) {
   return msbfs_run(ctx, d_src, nsrc, nsrc, 0, true, R_out, RW_out);
+}
+
+// The same search in level mode (no record; see msbfs_run): the frontier arrays of levels 0 .. lv->nlev - 1.
+int phde_msbfs_levels(phde_ctx *ctx, const int64_t *d_src, int nsrc, int lvl_cap, MsLevels *lv) {
+  uint16_t *R;
+  int RW;
+  return msbfs_run(ctx, d_src, nsrc, nsrc, 0, true, &R, &RW, lvl_cap, lv);
 }
 
 // A batch's candidates in one sweep: d_src holds nlist vertices, entry i searching with bit i % period

@@ -272,6 +272,15 @@ int phde_selftest_barrier_timeout(phde_ctx *ctx, int timeout_ms);
 int phde_gram_f32(phde_ctx *ctx, const float *A, int lda, int acols, const float *B, int ldb, int bcols,
                   const double *w, int64_t n, int nsplit, double *G);
 
+/* Diagnostics used by the tests: the exact eigensolver of the layouts (PHDE_EIG_EXACT: FP32 Jacobi sweeps, FP64
+ * orthonormalisation and similarity, FP64 rotations of unseparated pairs, perturbation refinement; FP64 sweeps
+ * when a wanted eigenvalue is not separated) on a symmetric k x k matrix M (column-major host array; the
+ * symmetric part is used).  evals: the k eigenvalues ascending; Y: k x c column-major, the eigenvectors of the
+ * c smallest eigenvalues (largest != 0: the c largest, largest first), each signed so that its entry of largest
+ * magnitude is positive.  iters (may be NULL): FP32 plus FP64 sweeps.  The reference calls LAPACK's dsyev
+ * for this step (DrawingBase.cpp). */
+int phde_symeig(phde_ctx *ctx, const double *M, int k, int c, int largest, double *evals, double *Y, int *iters);
+
 /* Replace the pivot-scoring MLP used by PHDE_STRAT_LEARNED (4 -> 64 -> 64 -> 1, ReLU): `count` floats,
  * W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3[1] (row-major).  The library starts with the
  * weights trained by train/train_pivot_mlp.py.  No counterpart in the reference. */

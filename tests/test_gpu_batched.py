@@ -140,7 +140,9 @@ def test_batched_learned_matches_single_learned_layouts(k, c):
         np.testing.assert_allclose(np.linalg.norm(xb, axis=0), 1.0, rtol=1e-9)
         np.testing.assert_allclose(q, rayleigh(g, r.coords), rtol=1e-4)
         assert principal_cosines(xb, r.coords).min() > 1 - 1e-5
-        np.testing.assert_allclose(rq_lib[i], q, rtol=1e-5)
+        # the library's quotient is y^T M y / ||S y||^2 over the FP32 basis in FP64; q is taken from the
+        # coordinates, which are rounded to FP32 before their normalisation: ~1e-5 apart on these graphs
+        np.testing.assert_allclose(rq_lib[i], q, rtol=1e-4)
     # a replay of the captured sequence gives the same layouts bit for bit
     xs2, st2 = cb.layout_batched(k, c, strategy="Learned")
     xs3, st3 = cb.layout_batched(k, c, strategy="Learned")

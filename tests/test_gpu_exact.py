@@ -61,16 +61,19 @@ def hub_mesh():
     return CSRGraph(B.indptr.astype(np.uint32), B.indices.astype(np.uint32), None)
 
 
-@pytest.mark.parametrize("make,k,c", [
-    (lambda: graphs.rmat(16, seed=7), 64, 3),
-    (lambda: graphs.rmat(16, seed=7), 50, 3),
-    (lambda: graphs.rgg(60000, dim=3, avg_degree=12, seed=2), 64, 3),
-    (lambda: graphs.mesh(150, 80, seed=31), 130, 3),
-    (lambda: graphs.mesh(900, 12, seed=5), 24, 2),   # diameter above 255: 16-bit packed columns
-    (lambda: graphs.rmat(14, seed=3), 20, 7),        # more than four coordinates
-    (hub_mesh, 20, 2),                               # a row too heavy for the byte dot products
+# Basis tolerance: 1e-9 absolute, except on the hub mesh, where every distance is 0, 1 or 2 and the columns
+# are nearly collinear: there the oracle's own FP64 basis is 3.8e-9 away from the same Gram-Schmidt run in
+# extended precision (np.longdouble), so the two FP64 computations are compared at 1e-8.
+@pytest.mark.parametrize("make,k,c,btol", [
+    (lambda: graphs.rmat(16, seed=7), 64, 3, 1e-9),
+    (lambda: graphs.rmat(16, seed=7), 50, 3, 1e-9),
+    (lambda: graphs.rgg(60000, dim=3, avg_degree=12, seed=2), 64, 3, 1e-9),
+    (lambda: graphs.mesh(150, 80, seed=31), 130, 3, 1e-9),
+    (lambda: graphs.mesh(900, 12, seed=5), 24, 2, 1e-9),   # diameter above 255: 16-bit packed columns
+    (lambda: graphs.rmat(14, seed=3), 20, 7, 1e-9),        # more than four coordinates
+    (hub_mesh, 20, 2, 1e-8),                               # a row too heavy for the byte dot products
 ], ids=["rmat16-k64", "rmat16-k50", "rgg3d-k64", "mesh-k130", "long-mesh-u16", "rmat14-c7", "hub-mesh"])
-def test_exact_vs_fp64_oracle(gpu_ctx, make, k, c):
+def test_exact_vs_fp64_oracle(gpu_ctx, make, k, c, btol):
     g = make()
     gpu_ctx.upload(g)
     r = gpu_ctx.layout("ParHDE", "Kcenters", k, c, precision="exact", eig="exact", extra=True)
@@ -78,7 +81,7 @@ def test_exact_vs_fp64_oracle(gpu_ctx, make, k, c):
     assert L.status == 0
     assert np.array_equal(r.sources, L.sources)
     assert r.stats["naccepted"] == L.stats.naccepted and r.stats["ndiscarded"] == L.stats.ndiscarded
-    np.testing.assert_allclose(r.basis, L.S, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(r.basis, L.S, rtol=0, atol=btol)
     # S^T L S from the GPU's own basis: the exact integer products leave only the k x k rounding
     Mb = r.basis.T @ (laplacian(g) @ r.basis)
     np.testing.assert_allclose(r.gram, Mb, rtol=0, atol=1e-10 * np.abs(Mb).max())
