@@ -129,11 +129,15 @@ class ClockSampler:
             self.t.join(timeout=5)
             self.proc = None
 
-    # A polling nvidia-smi slows host<->device copies several-fold on these machines (the adjacency upload
-    # took 13-15 ms with it running and 2.6 ms without, the same pinned buffers), so the end-to-end loops run
-    # with the sampler paused; the device-timed regions are sampled.
+    # A polling nvidia-smi slows host -> device copies several-fold on these machines, and for a moment after it
+    # exits: the R-MAT 22 adjacency upload took 2.6 ms with no sampler, 9.5-11.5 ms with one running or just
+    # stopped, 2.6 ms again a second later (same pinned buffers, same process).  So the end-to-end loops run
+    # with the sampler stopped and settled; the device-timed regions are sampled.
     def pause(self):
+        was = self.proc is not None
         self.__exit__(None, None, None)
+        if was:
+            time.sleep(2.0)
 
     def resume(self):
         if self.proc is None:

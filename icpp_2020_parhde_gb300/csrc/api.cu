@@ -40,7 +40,8 @@ int phde_default_pivot_model(const float **w, int *count);
 int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const int32_t *d_d0,
                           std::vector<int64_t> &h_cand, std::vector<float> &h_score);
 int phde_cand_distances(phde_ctx *ctx, const int32_t *D, int P0, const uint16_t *R, int RW, const int64_t *d_cand,
-                        int M, std::vector<int32_t> &h_sub, std::vector<int32_t> &h_csub);
+                        int M, std::vector<int32_t> &h_sub, std::vector<int32_t> &h_csub,
+                        const MsLevels *lv = nullptr);
 int phde_eigensolve(phde_ctx *ctx, const double *d_M, int N, int c, int largest, int eig, double *d_K,
                     double *d_evals, double *d_Y, int *h_iters, int seq);
 
@@ -336,6 +337,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
   bool exact = o->precision == PHDE_PREC_EXACT;  // cleared when the inputs are out of the exact path's range
   ExactBasis eb;
   ZSrc zsrc;                   // where the exact path reads the candidate columns
+  MsLevels lvl_sweep;          // learned pivots, exact path: the multi-source sweep's per-level frontier arrays
   std::vector<int> rec_order;  // learned pivots: the record columns of candidates P0.. (exact path)
   float *S32 = nullptr;
   if (mixed) {
@@ -425,11 +427,30 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), M, mind0, cand, cscore))) return rc;
       const int Mc = (int)cand.size();
       PHDE_CK(ctx, cudaMemcpyAsync(dc, cand.data(), sizeof(int64_t) * Mc, cudaMemcpyHostToDevice, ctx->stream));
-      uint16_t *R;
-      int RW;
-      if ((rc = phde_msbfs_record(ctx, dc, Mc, &R, &RW))) return rc;
+      uint16_t *R = nullptr;
+      int RW = 0;
+      // the candidates' distances are read straight from the sweep's per-level frontier arrays (no record) when
+      // their number fits: the sweep has at most diameter + 1 <= 2 ecc + 1 levels, ecc the first warm-start
+      // source's eccentricity (the Kcenters key of pass 0), and the exact path's byte layout needs distances < 255
+      bool level_mode = false;
+      {
+        unsigned long long key0 = 0;
+        const ull *keys = (const ull *)phde_buf(ctx, "kc.keys", 0);
+        if (!keys) return PHDE_ERR_OOM;
+        PHDE_CK(ctx, cudaMemcpyAsync(&key0, keys, sizeof(key0), cudaMemcpyDeviceToHost, ctx->stream));
+        PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        const int64_t cap = 2 * (int64_t)(key0 >> 32) + 1;
+        const int64_t bytes = (cap + 1) * n * ((Mc + 63) / 64) * (int64_t)sizeof(ull);
+        if (cap <= 254 && bytes <= PHDE_LEVEL_MODE_BYTES) {
+          rc = phde_msbfs_levels(ctx, dc, Mc, (int)cap, &lvl_sweep);
+          if (rc == PHDE_OK) level_mode = true;
+          else if (rc != PHDE_ERR_TOO_LARGE) return rc;
+        }
+      }
+      if (!level_mode && (rc = phde_msbfs_record(ctx, dc, Mc, &R, &RW))) return rc;
       std::vector<int32_t> sub, csub;
-      if ((rc = phde_cand_distances(ctx, D, P0, R, RW, dc, Mc, sub, csub))) return rc;
+      if ((rc = phde_cand_distances(ctx, D, P0, R, RW, dc, Mc, sub, csub, level_mode ? &lvl_sweep : nullptr)))
+        return rc;
       // farthest-point selection over the candidates: distance to the pivots chosen so far (warm start
       // included), best score first on ties
       const int Pl = std::min(P, P0 + Mc);
@@ -460,11 +481,18 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
         zsrc.R = R;
         zsrc.RW = RW;
         zsrc.rmap = rmap;
+        if (level_mode) {
+          zsrc.lvl = lvl_sweep.lvl;
+          zsrc.nlev = lvl_sweep.nlev;
+          zsrc.W = lvl_sweep.W;
+        }
         rec_order = order;
       } else {
         int unreached = 0;
-        if ((rc = phde_record_columns(ctx, R, RW, order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0, &unreached)))
-          return rc;
+        rc = level_mode
+                 ? phde_level_columns(ctx, &lvl_sweep, order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0, &unreached)
+                 : phde_record_columns(ctx, R, RW, order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0, &unreached);
+        if (rc) return rc;
         if (unreached) return phde_fail(ctx, PHDE_ERR_DISCONNECTED, "distance passes: the graph is not connected");
       }
       std::vector<int64_t> srcs(Pn);
@@ -495,19 +523,23 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       int state[4] = {0, 0, 0, 0};
       std::vector<double> dlog(P);
       if (exact) {
-        if (!zsrc.R) {
+        if (!zsrc.R && !zsrc.lvl) {
           zsrc.D = D;
           zsrc.P0 = P_used;
         }
         rc = phde_exact_orth(ctx, zsrc, P_used, k, &eb, state, dlog.data());
         if (rc == PHDE_ERR_TOO_LARGE) {  // distances or degrees beyond the exact sums: the FP64 vector kernels
           exact = false;
-          if (zsrc.R) {  // they need the learned candidates' columns in D, with their sums of squares
+          if (zsrc.R || zsrc.lvl) {  // they need the learned candidates' columns in D, with their sums of squares
             int unreached = 0;
             const int P0 = zsrc.P0, Pn = (int)rec_order.size();
-            if ((rc = phde_record_columns(ctx, zsrc.R, zsrc.RW, rec_order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0,
-                                          &unreached)))
-              return rc;
+            if (zsrc.lvl)
+              rc = phde_level_columns(ctx, &lvl_sweep, rec_order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0,
+                                      &unreached);
+            else
+              rc = phde_record_columns(ctx, zsrc.R, zsrc.RW, rec_order.data(), Pn, D + (int64_t)P0 * n, sumsq + P0,
+                                       &unreached);
+            if (rc) return rc;
           }
           rc = phde_cgs(ctx, D, P_used, sumsq, deg, Sbuf, k, state, dlog.data());
         }

@@ -138,6 +138,10 @@ struct ZSrc {
   const uint16_t *R = nullptr;
   int RW = 0;
   const int *rmap = nullptr;  // device array
+  // level mode instead of R (lvl non-null): record column c is the distance from source c, read from the
+  // sweep's per-level frontier arrays (MsLevels)
+  const unsigned long long *lvl = nullptr;
+  int nlev = 0, W = 0;
 };
 // The accepted basis as coefficients over the integer columns Z = [1, D columns]: S_q = Z A[q][*].
 struct ExactBasis {
@@ -174,12 +178,15 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
 // ---- kernels (msbfs.cu) ----
 // The frontier words of every level of a level-mode sweep: bit b of word w of vertex v is set in level L's
 // array, lvl[(L * n + v) * W + w], exactly when source 64 w + b reaches v first at level L; levels 0 .. nlev - 1.
+constexpr int64_t PHDE_LEVEL_MODE_BYTES = 16ll << 30;  // largest frontier-array set a level-mode sweep keeps
 struct MsLevels {
   const ull *lvl = nullptr;
   int nlev = 0;
   int W = 0;
 };
 int phde_msbfs_levels(phde_ctx *ctx, const int64_t *d_src, int nsrc, int lvl_cap, MsLevels *lv);
+int phde_level_columns(phde_ctx *ctx, const MsLevels *lv, const int *h_cols, int ncols, int32_t *D,
+                       unsigned long long *sumsq, int *h_unreached);
 // Distance columns for nsrc given sources (device array) into D (n * nsrc int32, -1 unreached), up to 256
 // sources per sweep.  With sumsq: exact per-column sums of squares and *h_unreached (synchronises).
 int phde_msbfs(phde_ctx *ctx, const int64_t *d_src, int nsrc, int32_t *D, unsigned long long *sumsq,

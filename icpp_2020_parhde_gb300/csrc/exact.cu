@@ -263,15 +263,61 @@ __global__ void __launch_bounds__(ZG_THREADS) zgram_kernel(ZgArgs a) {
 // (maxz[0], maxz[1]).  Rows past n pack as zeros.
 constexpr int ZQ_ROWS = 128;
 constexpr int ZQ_QUADS = ZQ_ROWS / 4;
-constexpr int ZQ_PACK_COLS = 64;  // columns staged per pass of the pack kernel
+constexpr int ZQ_PACK_COLS = 160;  // columns staged per pass of the pack kernel (the first block of k <= 140 in one)
 constexpr int ZQ_THREADS = 256;
 constexpr int ZQ_GRAM_THREADS = 192;  // the Gram kernel's largest block (190 tiles at 76 columns); three per SM
+
+// Level mode of zq_pack_kernel: thread per (row, source word), the 128 rows of a word on four whole warps (one
+// chosen-bit mask per warp: no divergence).  The levels fold into NB bit planes (plane k = OR of the arrays
+// whose level has bit k set) and every chosen source's distance is read off the planes; chosen sources that
+// never reached the row give -1 (the exact path then refuses the basis), rows past n pack as zeros.
+template <int NB>
+__device__ __forceinline__ void zq_level_fill(const ZSrc &src, int64_t n, int64_t i0, const ull *s_cmask,
+                                              const int *s_cmap, uint8_t (*zb)[ZQ_PACK_COLS + 4], unsigned &m) {
+  constexpr int U = 8;
+  const int W = src.W;
+  for (int e = threadIdx.x; e < ZQ_ROWS * W; e += blockDim.x) {
+    const int w = e / ZQ_ROWS, r = e - w * ZQ_ROWS;
+    const int64_t i = i0 + r;
+    const ull want = s_cmask[w];
+    if (!want) continue;
+    ull pl[NB], seen = 0;
+#pragma unroll
+    for (int k = 0; k < NB; k++) pl[k] = 0ull;
+    if (i < n) {
+      for (int L0 = 0; L0 < src.nlev; L0 += U) {
+        ull x[U];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          x[u] = L0 + u < src.nlev ? __ldg(src.lvl + ((int64_t)(L0 + u) * n + i) * W + w) & want : 0ull;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          seen |= x[u];
+#pragma unroll
+          for (int k = 0; k < NB; k++)
+            if (((L0 + u) >> k) & 1) pl[k] |= x[u];
+        }
+      }
+    }
+    for (ull y = want; y; y &= y - 1) {
+      const int b = __ffsll((long long)y) - 1;
+      unsigned d = 0;
+#pragma unroll
+      for (int k = 0; k < NB; k++) d |= (unsigned)((pl[k] >> b) & 1ull) << k;
+      const bool reached = (seen >> b) & 1ull;
+      zb[r][s_cmap[64 * w + b]] = i >= n ? (uint8_t)0 : reached ? (uint8_t)d : (uint8_t)0xff;
+      if (i < n) m = max(m, reached ? d : 0xffffffffu);
+    }
+  }
+}
 
 __global__ void __launch_bounds__(ZQ_THREADS) zq_pack_kernel(ZSrc src, const int64_t *off, int64_t n, int P, int c0,
                                                              int c1, int ldq, uint32_t *Zq, unsigned *smaxz,
                                                              unsigned *maxz) {
   __shared__ uint8_t zb[ZQ_ROWS][ZQ_PACK_COLS + 4];
   __shared__ unsigned s_m;
+  __shared__ int s_cmap[64 * 4];  // level mode: source -> column of the pass (-1: not chosen)
+  __shared__ ull s_cmask[4];      // level mode: chosen sources of the pass, per source word
   const int64_t nslab = (n + ZQ_ROWS - 1) / ZQ_ROWS;
   const int P0 = src.P0;
   for (int64_t s = blockIdx.x; s < nslab; s += gridDim.x) {
@@ -283,29 +329,57 @@ __global__ void __launch_bounds__(ZQ_THREADS) zq_pack_kernel(ZSrc src, const int
     for (int t0 = c0; t0 < c1; t0 += ZQ_PACK_COLS) {
       const int nc = min(ZQ_PACK_COLS, c1 - t0);
       __syncthreads();  // zb of the previous pass consumed
-      // ones, distance (D) and padding columns: consecutive threads take consecutive rows of a column; eight
-      // loads in flight per thread
+      // ones, distance (D) and padding columns -- the pass's prefix up to Z index P0 and its suffix past P (the
+      // record columns lie between): consecutive threads take consecutive rows of a column; eight loads in
+      // flight per thread
       constexpr int U = 8;
-      for (int e0 = threadIdx.x; e0 < ZQ_ROWS * nc; e0 += U * blockDim.x) {
+      const int nd1 = max(0, min(t0 + nc, P0 + 1) - t0);
+      const int ts = max(t0, P + 1), nd = nd1 + max(0, t0 + nc - ts);
+      for (int e0 = threadIdx.x; e0 < ZQ_ROWS * nd; e0 += U * blockDim.x) {
         int v[U];
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const int e = e0 + u * blockDim.x;
-          const int j = e / ZQ_ROWS, r = e - j * ZQ_ROWS, t = t0 + j;
+          const int jj = e / ZQ_ROWS, r = e - jj * ZQ_ROWS;
+          const int t = jj < nd1 ? t0 + jj : ts + (jj - nd1);
           const int64_t i = i0 + r;
           v[u] = -2;  // nothing to store here
-          if (e < ZQ_ROWS * nc && !(t >= 1 && t <= P && t > P0))
-            v[u] = i >= n ? 0 : (t == 0 ? 1 : (t <= P ? __ldg(src.D + (int64_t)(t - 1) * n + i) : 0));
+          if (e < ZQ_ROWS * nd) v[u] = i >= n ? 0 : (t == 0 ? 1 : (t <= P ? __ldg(src.D + (int64_t)(t - 1) * n + i) : 0));
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const int e = e0 + u * blockDim.x;
           if (v[u] == -2) continue;
-          const int j = e / ZQ_ROWS, r = e - j * ZQ_ROWS;
+          const int jj = e / ZQ_ROWS, r = e - jj * ZQ_ROWS;
+          const int j = jj < nd1 ? jj : (ts - t0) + (jj - nd1);
           m = max(m, (unsigned)v[u]);
           zb[r][j] = (uint8_t)v[u];
         }
       }
+      if (src.lvl) {
+        // level mode: thread per (row, source word), the 128 rows of a word on four whole warps (one chosen-bit
+        // mask per warp: no divergence).  The levels fold into bit planes (plane k = OR of the arrays whose
+        // level has bit k) and every chosen source's distance is read off the planes; chosen sources that
+        // never reached the row give -1 (the exact path then refuses the basis), rows past n pack as zeros
+        const int W = src.W, nb = 64 * W;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) s_cmap[b] = -1;
+        if (threadIdx.x < W) s_cmask[threadIdx.x] = 0ull;
+        __syncthreads();
+        for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+          const int t = t0 + j;
+          if (t >= 1 && t <= P && t > P0) {
+            const int b = src.rmap[t - 1 - P0];
+            s_cmap[b] = j;
+            atomicOr(s_cmask + (b >> 6), 1ull << (b & 63));
+          }
+        }
+        __syncthreads();
+        const int nbits = src.nlev > 1 ? 32 - __clz(src.nlev - 1) : 0;  // planes for levels 0 .. nlev - 1 (<= 8)
+        if (nbits <= 4)
+          zq_level_fill<4>(src, n, i0, s_cmask, s_cmap, zb, m);
+        else
+          zq_level_fill<8>(src, n, i0, s_cmask, s_cmap, zb, m);
+      } else
       // record columns: consecutive threads take consecutive chosen columns of a row
       for (int e0 = threadIdx.x; e0 < ZQ_ROWS * nc; e0 += U * blockDim.x) {
         int v[U];
@@ -790,55 +864,27 @@ __global__ void pack_kernel(ZSrc src, int64_t n, const int *acc_idx, int k, int 
 // Sums: for uint8 rows two columns share a 32-bit register as 16-bit halves (bytes moved apart by one byte
 // permute; an item has at most 256 neighbours of at most 255, so no half ever carries into the next, also
 // after the groups are added together); uint16 rows sum each column in its own register.
-// SMALL (uint8 rows whose values are at most 15): the words of up to 16 neighbours are added as they are, four
-// byte lanes per register (16 * 15 < 256: no lane carries into the next), and spread into the 16-bit halves
-// every 16 rows -- one add per four columns instead of two permutes and two adds.
-template <typename T, bool SMALL = false>
+template <typename T>
 struct Sum16 {  // the sums of one 16-byte slice of a row: 16 uint8 or 8 uint16 columns, in 8 registers
   uint32_t s[8];
-  uint32_t b[SMALL ? 4 : 1];  // SMALL: byte-lane sums not yet spread
-  int pend;                   // SMALL: rows in b
   __device__ __forceinline__ void zero() {
 #pragma unroll
     for (int i = 0; i < 8; i++) s[i] = 0;
-    if constexpr (SMALL) {
-#pragma unroll
-      for (int i = 0; i < 4; i++) b[i] = 0;
-      pend = 0;
-    }
-  }
-  __device__ __forceinline__ void spread() {
-    if constexpr (SMALL) {
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        s[2 * i] += __byte_perm(b[i], 0u, 0x4140);
-        s[2 * i + 1] += __byte_perm(b[i], 0u, 0x4342);
-        b[i] = 0;
-      }
-      pend = 0;
-    }
   }
   __device__ __forceinline__ void add(const uint4 &v) {
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-    if constexpr (SMALL) {
-      if (pend == 16) spread();
 #pragma unroll
-      for (int i = 0; i < 4; i++) b[i] += w[i];
-      pend++;
-    } else {
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        if (sizeof(T) == 1) {
-          s[2 * i] += __byte_perm(w[i], 0u, 0x4140);
-          s[2 * i + 1] += __byte_perm(w[i], 0u, 0x4342);
-        } else {
-          s[2 * i] += w[i] & 0xffffu;
-          s[2 * i + 1] += w[i] >> 16;
-        }
+    for (int i = 0; i < 4; i++) {
+      if (sizeof(T) == 1) {
+        s[2 * i] += __byte_perm(w[i], 0u, 0x4140);
+        s[2 * i + 1] += __byte_perm(w[i], 0u, 0x4342);
+      } else {
+        s[2 * i] += w[i] & 0xffffu;
+        s[2 * i + 1] += w[i] >> 16;
       }
     }
   }
-  __device__ __forceinline__ void add_from(int lane_mask) {  // add the sums of lane ^ lane_mask (after spread())
+  __device__ __forceinline__ void add_from(int lane_mask) {  // add the sums of lane ^ lane_mask
 #pragma unroll
     for (int i = 0; i < 8; i++) s[i] += __shfl_xor_sync(PHDE_FULL_MASK, s[i], lane_mask);
   }
@@ -868,7 +914,7 @@ struct LgArgs {
   int ntiles;
 };
 
-template <typename T, int KP, int TS, bool SMALL = false>
+template <typename T, int KP, int TS>
 __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgArgs a) {
   constexpr int V = 16 / (int)sizeof(T);  // columns per 16-byte slice
   constexpr int LPR = KP / V;             // lanes per row
@@ -936,7 +982,7 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
       }
       unsigned zm = 0, rm = 0;
       if (row >= 0) {
-        Sum16<T, SMALL> nb;
+        Sum16<T> nb;
         nb.zero();
         // the packed rows are gathered again and again (evict-last in L2), the adjacency streams by once
         const uint64_t keep = l2_policy_evict_last(), stream = l2_policy_evict_first();
@@ -949,7 +995,6 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
           nb.add(x1);
         }
         if (e < e1) nb.add(ld_nc_hint16((const uint4 *)(Z + (int64_t)ld_nc_hint(a.adj + e, stream) * KP) + pi, keep));
-        nb.spread();
 #pragma unroll
         for (int m = LPR; m < 32; m <<= 1) nb.add_from(m);
         // every group of the warp now holds the row's sums: lane (gi, pi) finishes columns gi * CPL .. + CPL of
@@ -1069,6 +1114,21 @@ __global__ void __launch_bounds__(256) mgram_kernel(const ull *GL, int kp, const
 }
 
 // S (row-major n x k) = Z A^T restricted to the accepted columns, for callers that ask for the basis.
+// S from the packed accepted columns Z_acc (row-major n x kp, uint8 or uint16): column t of Z_acc is Z index
+// acc_idx[t].
+template <typename T>
+__global__ void basis_packed_kernel(const T *Z, int kp, int64_t n, const double *A, int ld, const int *acc_idx, int k,
+                                    double *S) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / k;
+    const int q = (int)(e - i * k);
+    const double *Aq = A + (int64_t)q * ld;
+    double s = Aq[0];
+    for (int t = 0; t <= q; t++) s = fma(Aq[acc_idx[t]], (double)Z[i * kp + t], s);
+    S[e] = s;
+  }
+}
+
 __global__ void basis_kernel(ZSrc src, int64_t n, const double *A, int ld, const int *acc_idx, int k,
                              double *S) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (int64_t)gridDim.x * blockDim.x) {
@@ -1296,6 +1356,7 @@ static int exact_zgram(phde_ctx *ctx, const ZSrc &src, int P, int c0, int c1, ul
     PHDE_LAUNCHED(ctx);
     if (byte_state == 1) return PHDE_OK;
   }
+  if (src.lvl) return PHDE_OK;  // level mode: distances above 254 cannot occur; an unreached one (maxz) is refused
   const int gy = (ntiles + ZG_THREADS - 1) / ZG_THREADS;
   const size_t smem = sizeof(int) * ((ZG_ROWS + ZG_ROWS / 4 + ZG_ROWS / 2) * (size_t)(c1 + 4) + c1);
   PHDE_CK(ctx, cudaFuncSetAttribute(zgram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1421,6 +1482,8 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
   ull *GL = (ull *)phde_buf(ctx, "ex.GL", sizeof(ull) * kp * kp);
   if (!Z || !GL) return PHDE_ERR_OOM;
   const int gp = grid_n(ctx, n, 256, 8);
+  if (src.lvl && !eb->Zq)  // level-mode columns exist only in the quad layout (distances below 255)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "exact path: level-mode columns without the byte layout");
   if (z16)
     pack_kernel<uint16_t><<<gp, 256, 0, ctx->stream>>>(src, n, eb->acc_idx, k, kp, (uint16_t *)Z);
   else if (eb->Zq)
@@ -1472,10 +1535,6 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
     if (kp == 64) rc = launch(lgram_kernel<uint16_t, 64, 4>);
     else if (kp == 128) rc = launch(lgram_kernel<uint16_t, 128, 8>);
     else rc = launch(lgram_kernel<uint16_t, 256, 8>);
-  } else if (eb->maxz <= 15u) {
-    if (kp == 64) rc = launch(lgram_kernel<uint8_t, 64, 4, true>);
-    else if (kp == 128) rc = launch(lgram_kernel<uint8_t, 128, 8, true>);
-    else rc = launch(lgram_kernel<uint8_t, 256, 8, true>);
   } else {
     if (kp == 64) rc = launch(lgram_kernel<uint8_t, 64, 4>);
     else if (kp == 128) rc = launch(lgram_kernel<uint8_t, 128, 8>);
@@ -1526,7 +1585,17 @@ int phde_exact_coords(phde_ctx *ctx, const double *M, const double *Y, int k, in
 
 // The basis S = Z A (row-major n x k FP64), only for callers that ask for it.
 int phde_exact_basis(phde_ctx *ctx, const ZSrc &src, int k, const ExactBasis *eb, double *S) {
-  basis_kernel<<<grid_n(ctx, ctx->n * k, 256, 8), 256, 0, ctx->stream>>>(src, ctx->n, eb->A, eb->ld, eb->acc_idx, k, S);
+  const int g = grid_n(ctx, ctx->n * k, 256, 8);
+  if (eb->Z && eb->z16)
+    basis_packed_kernel<uint16_t><<<g, 256, 0, ctx->stream>>>((const uint16_t *)eb->Z, eb->kp, ctx->n, eb->A, eb->ld,
+                                                               eb->acc_idx, k, S);
+  else if (eb->Z)
+    basis_packed_kernel<uint8_t><<<g, 256, 0, ctx->stream>>>((const uint8_t *)eb->Z, eb->kp, ctx->n, eb->A, eb->ld,
+                                                              eb->acc_idx, k, S);
+  else if (src.lvl)
+    return phde_fail(ctx, PHDE_ERR_INVALID, "exact basis: level-mode columns need the packed accepted columns");
+  else
+    basis_kernel<<<g, 256, 0, ctx->stream>>>(src, ctx->n, eb->A, eb->ld, eb->acc_idx, k, S);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }

@@ -207,13 +207,20 @@ __global__ void __launch_bounds__(KC_THREADS) kcenters_bfs_kernel(KcArgs a) {
           uint32_t dv = 0;
           if (v < n && Dp[v] == -1) {
             const int64_t j0 = a.off[v], j1 = a.off[v + 1];
-            for (int64_t j = j0; j < j1; j++) {
-              edges_local++;
-              const uint32_t u = __ldg(a.adj + j);
-              const uint32_t word = a.smem_bm ? front[u >> 5] : __ldcg(front + (u >> 5));
-              if ((word >> (u & 31)) & 1u) {
-                found = true;
-                break;
+            // four neighbours per round (their adjacency entries, then their bitmap words, all in flight): a
+            // vertex far from the frontier tests every neighbour, one dependent L2 round trip each otherwise
+            for (int64_t j = j0; j < j1 && !found; j += 4) {
+              uint32_t u[4], word[4];
+#pragma unroll
+              for (int q = 0; q < 4; q++) u[q] = j + q < j1 ? __ldg(a.adj + j + q) : 0u;
+#pragma unroll
+              for (int q = 0; q < 4; q++)
+                word[q] = j + q < j1 ? (a.smem_bm ? front[u[q] >> 5] : __ldcg(front + (u[q] >> 5))) : 0u;
+#pragma unroll
+              for (int q = 0; q < 4; q++) {
+                if (found || j + q >= j1) continue;
+                edges_local++;  // counted up to the first frontier neighbour, as a one-at-a-time scan would
+                found = (word[q] >> (u[q] & 31)) & 1u;
               }
             }
             if (found) {

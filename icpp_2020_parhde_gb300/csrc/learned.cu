@@ -301,8 +301,27 @@ __global__ void cand_distances_kernel(const int32_t *D, int P0, const uint16_t *
     const int i = idx / (M + P0), j = idx % (M + P0);
     if (j < P0)
       sub[i * P0 + j] = D[(int64_t)j * n + cand[i]];
-    else
+    else if (R)
       csub[i * M + (j - P0)] = (int32_t)R[cand[i] * RW + (j - P0)] - 1;
+  }
+}
+
+// Level mode: csub[i][j] = the level whose frontier array has source j's bit at vertex cand[i] (-1: none);
+// thread per (candidate, source word).
+__global__ void cand_distances_lvl_kernel(const ull *lvl, int nlev, int W, int64_t n, const int64_t *cand, int M,
+                                          int32_t *csub) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < M * W; idx += gridDim.x * blockDim.x) {
+    const int i = idx / W, w = idx - i * W;
+    const int64_t v = cand[i];
+    const int nb = min(64, M - 64 * w);
+    const ull valid = nb >= 64 ? ~0ull : ((1ull << nb) - 1ull);
+    ull seen = 0;
+    for (int L = 0; L < nlev; L++) {
+      const ull x = lvl[((int64_t)L * n + v) * W + w] & valid;
+      seen |= x;
+      for (ull y = x; y; y &= y - 1) csub[i * M + 64 * w + __ffsll((long long)y) - 1] = L;
+    }
+    for (ull y = valid & ~seen; y; y &= y - 1) csub[i * M + 64 * w + __ffsll((long long)y) - 1] = -1;
   }
 }
 
@@ -402,13 +421,19 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
 }
 
 int phde_cand_distances(phde_ctx *ctx, const int32_t *D, int P0, const uint16_t *R, int RW, const int64_t *d_cand,
-                        int M, std::vector<int32_t> &h_sub, std::vector<int32_t> &h_csub) {
+                        int M, std::vector<int32_t> &h_sub, std::vector<int32_t> &h_csub, const MsLevels *lv) {
   int32_t *sub = (int32_t *)phde_buf(ctx, "lp.sub", sizeof(int32_t) * (size_t)M * std::max(P0, 1));
   int32_t *csub = (int32_t *)phde_buf(ctx, "lp.csub", sizeof(int32_t) * (size_t)M * M);
   if (!sub || !csub) return PHDE_ERR_OOM;
   const int total = M * (M + P0);
-  cand_distances_kernel<<<(total + 255) / 256, 256, 0, ctx->stream>>>(D, P0, R, RW, ctx->n, d_cand, M, sub, csub);
+  cand_distances_kernel<<<(total + 255) / 256, 256, 0, ctx->stream>>>(D, P0, lv ? nullptr : R, RW, ctx->n, d_cand, M,
+                                                                      sub, csub);
   PHDE_LAUNCHED(ctx);
+  if (lv) {
+    cand_distances_lvl_kernel<<<(M * lv->W + 127) / 128, 128, 0, ctx->stream>>>(lv->lvl, lv->nlev, lv->W, ctx->n,
+                                                                                d_cand, M, csub);
+    PHDE_LAUNCHED(ctx);
+  }
   h_sub.resize((size_t)M * P0);
   h_csub.resize((size_t)M * M);
   if (P0 > 0)

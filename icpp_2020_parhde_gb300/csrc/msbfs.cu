@@ -583,6 +583,54 @@ __global__ void gather_columns_kernel(const uint16_t *R, int64_t n, int RW, cons
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(unreached, 1);
 }
 
+// The same columns from a level-mode sweep: per 32-vertex tile, thread (row, source word) walks the levels and
+// writes every source's distance into the tile (-1: never reached), then the columns are taken as above.
+__global__ void level_columns_kernel(const ull *lvl, int nlev, int W, int64_t n, const int *cols, int ncols, int32_t *D,
+                                     ull *sumsq, int *unreached) {
+  __shared__ int16_t tile[32][64 * MS_MAXW + 2];
+  __shared__ ull s_ssq[GATHER_SMEM_COLS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int p = threadIdx.x; p < GATHER_SMEM_COLS; p += blockDim.x) s_ssq[p] = 0ull;
+  int bad = 0;
+  for (int64_t v0 = (int64_t)blockIdx.x * 32; v0 < n; v0 += (int64_t)gridDim.x * 32) {
+    const int rows = n - v0 < 32 ? (int)(n - v0) : 32;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * W; e += blockDim.x) {
+      const int r = e / W, w = e - r * W;
+      if (r >= rows) continue;
+      ull seen = 0;
+      for (int L = 0; L < nlev; L++) {
+        const ull x = __ldg(lvl + ((int64_t)L * n + v0 + r) * W + w);
+        seen |= x;
+        for (ull y = x; y; y &= y - 1) tile[r][64 * w + __ffsll((long long)y) - 1] = (int16_t)L;
+      }
+      for (ull y = ~seen; y; y &= y - 1) tile[r][64 * w + __ffsll((long long)y) - 1] = (int16_t)-1;
+    }
+    __syncthreads();
+    for (int p = warp; p < ncols; p += nw) {
+      int d = -1;
+      if (lane < rows) {
+        d = (int)tile[lane][cols[p]];
+        D[(int64_t)p * n + v0 + lane] = d;
+        bad |= d < 0;
+      }
+      const uint32_t sq = d > 0 ? (uint32_t)d * (uint32_t)d : 0u;
+      const ull tot = ((ull)__reduce_add_sync(PHDE_FULL_MASK, sq >> 16) << 16) +
+                      (ull)__reduce_add_sync(PHDE_FULL_MASK, sq & 0xffffu);
+      if (lane == 0 && tot) {
+        if (p < GATHER_SMEM_COLS)
+          s_ssq[p] += tot;
+        else
+          atomicAdd(sumsq + p, tot);
+      }
+    }
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < ncols && p < GATHER_SMEM_COLS; p += blockDim.x)
+    if (s_ssq[p]) atomicAdd(sumsq + p, s_ssq[p]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(unreached, 1);
+}
+
 }  // namespace
 
 // Heavy-row chunk plan of the multi-source BFS (rows above MS_HEAVY, chunks of MS_CHUNK edges), built once
@@ -805,6 +853,29 @@ int phde_record_columns(phde_ctx *ctx, const uint16_t *R, int RW, const int *h_c
   PHDE_CK(ctx, cudaFuncSetAttribute(gather_columns_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 31) / 32, (int64_t)ctx->nsm * 4));
   gather_columns_kernel<<<g, 512, smem, ctx->stream>>>(R, n, RW, dcols, ncols, D, ssq, unr);
+  PHDE_LAUNCHED(ctx);
+  if (sumsq || h_unreached) {
+    int h = 0;
+    PHDE_CK(ctx, cudaMemcpyAsync(&h, unr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h_unreached) *h_unreached = h;
+  }
+  return PHDE_OK;
+}
+
+// Columns `h_cols` (source indices) of a level-mode sweep into D, as phde_record_columns.
+int phde_level_columns(phde_ctx *ctx, const MsLevels *lv, const int *h_cols, int ncols, int32_t *D,
+                       unsigned long long *sumsq, int *h_unreached) {
+  const int64_t n = ctx->n;
+  int *dcols = (int *)phde_buf(ctx, "ms.cols", sizeof(int) * ncols);
+  ull *ssq = sumsq ? sumsq : (ull *)phde_buf(ctx, "ms.ssq_tmp", sizeof(ull) * ncols);
+  int *unr = (int *)phde_buf(ctx, "ms.unreached", sizeof(int));
+  if (!dcols || !ssq || !unr) return PHDE_ERR_OOM;
+  PHDE_CK(ctx, cudaMemcpyAsync(dcols, h_cols, sizeof(int) * ncols, cudaMemcpyHostToDevice, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(ssq, 0, sizeof(ull) * ncols, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(unr, 0, sizeof(int), ctx->stream));
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 31) / 32, (int64_t)ctx->nsm * 4));
+  level_columns_kernel<<<g, 256, 0, ctx->stream>>>(lv->lvl, lv->nlev, lv->W, n, dcols, ncols, D, ssq, unr);
   PHDE_LAUNCHED(ctx);
   if (sumsq || h_unreached) {
     int h = 0;
