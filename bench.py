@@ -129,19 +129,6 @@ class ClockSampler:
             self.t.join(timeout=5)
             self.proc = None
 
-    # A polling nvidia-smi slows host -> device copies several-fold on these machines, and for a moment after it
-    # exits: the R-MAT 22 adjacency upload took 2.6 ms with no sampler, 9.5-11.5 ms with one running or just
-    # stopped, 2.6 ms again a second later (same pinned buffers, same process).  So the end-to-end loops run
-    # with the sampler stopped and settled; the device-timed regions are sampled.
-    def pause(self):
-        was = self.proc is not None
-        self.__exit__(None, None, None)
-        if was:
-            time.sleep(2.0)
-
-    def resume(self):
-        if self.proc is None:
-            self.__enter__()
 
     def summary(self):
         sm, mx, reasons = [], [], set()
@@ -277,10 +264,9 @@ def cpu_layout(g, algo, k, c, reps, desc):
 class Runner:
     """Timed layouts of one uploaded graph: device time (library events) and end to end (upload + layout)."""
 
-    def __init__(self, ctx, g, gp, algo, k, c, xy, flush_l2, ws, clk=None):
+    def __init__(self, ctx, g, gp, algo, k, c, xy, flush_l2, ws):
         self.ctx, self.g, self.gp, self.algo, self.k, self.c = ctx, g, gp, algo, k, c
         self.xy, self.flush_l2, self.ws = xy, flush_l2, ws
-        self.clk = clk  # the clock sampler, paused around the end-to-end loops
 
     def run(self, p):
         return self.ctx.layout(self.algo, k=self.k, c=self.c, coords_out=self.xy.numpy(), **p)
@@ -309,21 +295,15 @@ class Runner:
 
     def e2e(self, p, steps):
         ts, tu = [], []
-        if self.clk:
-            self.clk.pause()
-        try:
-            for _ in range(steps):
-                self.flush_l2()
-                barrier(self.ws)
-                t1 = time.perf_counter()
-                self.ctx.upload(self.gp)
-                t2 = time.perf_counter()
-                self.run(p)
-                ts.append(time.perf_counter() - t1)
-                tu.append(t2 - t1)
-        finally:
-            if self.clk:
-                self.clk.resume()
+        for _ in range(steps):
+            self.flush_l2()
+            barrier(self.ws)
+            t1 = time.perf_counter()
+            self.ctx.upload(self.gp)
+            t2 = time.perf_counter()
+            self.run(p)
+            ts.append(time.perf_counter() - t1)
+            tu.append(t2 - t1)
         self.upload_ms = float(np.mean(tu)) * 1e3
         return allmax(self.ws, float(np.mean(ts))) * 1e3
 
@@ -444,25 +424,32 @@ def run_gb300(args):
         flush.fill_(1.0)
         torch.cuda.synchronize()
 
+    R = Runner(ctx, g, gp, "ParHDE", k, c, xy, flush_l2, ws)
+    sub_steps = max(3, args.steps // 4)
+    controls = [x for x in args.controls.split(",") if x]
+    pipes = [(name, p) for name, p in (("plain", P_PLAIN), ("kcenters_exact", P_KC), ("learned_checked", P_CHECKED),
+                                       ("learned_mixed", P_MIXED)) if name in controls]
+    # ---- end to end through the C ABI first, before the clock sampler ever runs: a polling nvidia-smi slows
+    #      host <-> device copies several-fold on these machines, also for seconds after it exits (the R-MAT 22
+    #      adjacency upload: 2.6 ms without it, 9.5-15 ms with it running or recently stopped) ----
+    R.run(P_LEARNED)
+    e2e_head = R.e2e(P_LEARNED, args.steps)
+    upload_head = R.upload_ms
+    e2e_ctl = {}
+    for name, p in pipes:
+        R.run(p)
+        e2e_ctl[name] = R.e2e(p, sub_steps)
+    # ---- device-resident timed regions, clocks sampled: the headline, then the reference pipeline on the GPU,
+    #      the pivot control, the checked strategy, mixed precision ----
     clk = ClockSampler(local).__enter__()
-    R = Runner(ctx, g, gp, "ParHDE", k, c, xy, flush_l2, ws, clk)
-    # ---- headline: device-resident timed region, then end to end through the C ABI ----
     head = R.timed(P_LEARNED, args.steps, args.warmup)
     xy_head = R.coords()
     st_head = head["stats"][-1]
-    e2e_head = R.e2e(P_LEARNED, args.steps)
-    upload_head = R.upload_ms
-    # ---- the reference pipeline on the GPU, the pivot control, the checked strategy, mixed precision ----
-    sub_steps = max(3, args.steps // 4)
-    controls = [x for x in args.controls.split(",") if x]
     ctl = {}
-    for name, p in (("plain", P_PLAIN), ("kcenters_exact", P_KC), ("learned_checked", P_CHECKED),
-                    ("learned_mixed", P_MIXED)):
-        if name not in controls:
-            continue
+    for name, p in pipes:
         r = R.timed(p, sub_steps, 1 if name == "learned_checked" else 2)
         r["rq"] = rayleigh_quotients(g, R.coords())
-        r["e2e"] = R.e2e(p, sub_steps)
+        r["e2e"] = e2e_ctl[name]
         ctl[name] = r
     clk.__exit__(None, None, None)
     rq_head = rayleigh_quotients(g, xy_head)
@@ -618,6 +605,8 @@ def run_single(args, local, kind, k, c, flush_l2):
 
 
 def run_weighted(args, local, flush_l2, clk=None):
+    # clk: a ClockSampler (not yet started) to run around the device-timed region only, after the end-to-end
+    # loop (see the headline's note on nvidia-smi)
     """The weighted configuration: WParHDE (Kcenters pivots by delta-stepping SSSP, coupled MGS, FP64 as the
     reference) on the weighted 3-D grid; CPU baseline: one oracle layout of the same graph."""
     import torch
@@ -628,11 +617,16 @@ def run_weighted(args, local, flush_l2, clk=None):
     gp = pinned_graph(g)
     xy = torch.empty(g.n * c, dtype=torch.float64).pin_memory()
     ctx.upload(gp)
-    R = Runner(ctx, g, gp, "wParHDE", k, c, xy, flush_l2, 1, clk)
+    R = Runner(ctx, g, gp, "wParHDE", k, c, xy, flush_l2, 1)
     p = dict(strategy="Kcenters", precision="fp64", eig="power")
     steps = max(3, args.steps // 5)
-    r = R.timed(p, steps, 2)
+    R.run(p)
     e = R.e2e(p, steps)
+    if clk:
+        clk.__enter__()
+    r = R.timed(p, steps, 2)
+    if clk:
+        clk.__exit__(None, None, None)
     st = r["stats"]
     out = summary(r, k, g.nnz, 1, e, R.h2d(), R.d2h(), rayleigh_quotients(g, R.coords()))
     out.update({"config": workload_config("wParHDE", desc, g, k, c), "graph_gen_s": round(gen_s, 1),
@@ -656,9 +650,8 @@ def run_weighted_headline(args, ws, rank, local):
         flush.fill_(1.0)
         torch.cuda.synchronize()
 
-    clk = ClockSampler(local).__enter__()
+    clk = ClockSampler(local)
     out = run_weighted(args, local, flush_l2, clk)
-    clk.__exit__(None, None, None)
     if rank != 0:
         return
     line = {"metric": METRIC, "value": out["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,

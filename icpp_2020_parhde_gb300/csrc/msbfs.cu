@@ -380,12 +380,15 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         for (int64_t i = gt; i < n * W; i += gts) fnext[i] = 0ull;
       }
       if (!built_f && !grid_sync(a.gs, a.err, a.timeout_ns)) return;
-      // new bits can only appear next to the frontier: claim those neighbours once (stamp L+1),
-      // edge-balanced over the frontier's edges
+      // push: new bits can only appear next to the frontier, so every out-edge (u, v) of the frontier ORs u's
+      // frontier word into v's accumulator (hacc, zero outside this level) and claims v once (stamp L+1) as a
+      // candidate -- work in proportion to the frontier's edges, where pulling would scan every candidate's
+      // whole adjacency (hubs next to a small frontier cost far more).  Finished vertices are skipped.
       const ull fctr = __ldcg(a.lctr + sf);
       const uint32_t fcnt = (uint32_t)(fctr >> 32), fe = (uint32_t)(fctr & 0xffffffffull);
       const uint32_t *fqv = a.qv[sf], *fqe = a.qe[sf];
       unsigned *cc = a.ccount + (L & 1);
+      const uint64_t keep = l2_policy_evict_last();
       for (int64_t base = gw * 32; base < fe; base += gws * 32) {
         const int64_t e = base + lane;
         bool mine = false;
@@ -394,7 +397,17 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
           const uint32_t slot = owner_slot(fqe, fcnt, (uint32_t)e);
           const uint32_t u = fqv[slot];
           v = __ldg(a.adj + a.off[u] + (e - (int64_t)fqe[slot]));
-          mine = atomicMax(a.stamp + v, L + 1) < L + 1;
+          // `done` also marks the hub rows (dense levels pull them by chunks): those still take pushes
+          bool skip = (__ldcg(a.done + (v >> 5)) >> (v & 31)) & 1u;
+          if (skip) skip = a.off[v + 1] - a.off[v] <= MS_HEAVY;
+          if (!skip) {
+            ull x[W];
+            ld_front<W>(fcur + (int64_t)u * W, x, keep);
+#pragma unroll
+            for (int w = 0; w < W; w++)
+              if (x[w]) red_or_hint(a.hacc + (int64_t)v * W + w, x[w], keep);
+            mine = atomicMax(a.stamp + v, L + 1) < L + 1;
+          }
         }
         const unsigned bal = __ballot_sync(PHDE_FULL_MASK, mine);
         unsigned slot0 = 0;
@@ -403,17 +416,34 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         if (mine) a.cand[slot0 + __popc(bal & ((1u << lane) - 1u))] = v;
       }
       if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-      // pull the candidates; the block-uniform loop lets block_push list the vertices given new bits
+      // finalise the candidates (thread per candidate, the accumulator cleared for the next sparse level); the
+      // block-uniform loop lets block_push list the vertices given new bits
       const unsigned nc = __ldcg(cc);
-      const int gpb = blockDim.x / MS_GROUP;  // groups per block
-      for (int64_t i0 = (int64_t)blockIdx.x * gpb; i0 < nc; i0 += (int64_t)gridDim.x * gpb) {
-        const int64_t i = i0 + threadIdx.x / MS_GROUP;
-        const bool act = i < nc;
-        const int64_t v = act ? (int64_t)a.cand[i] : 0;
-        bool nb;
-        uint32_t dv;
-        ms_pull_vertex<W>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, v, act, gl, true, nb, dv);
-        block_push(nb, (uint32_t)v, dv, a.qv[so], a.qe[so], a.lctr + so, &psc);
+      for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < nc; i0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = i0 + threadIdx.x;
+        bool nb = false;
+        uint32_t v = 0, dv = 0;
+        if (i < nc) {
+          v = a.cand[i];
+          ull acc[W];
+#pragma unroll
+          for (int w = 0; w < W; w++) {
+            acc[w] = __ldcg(a.hacc + (int64_t)v * W + w);
+            a.hacc[(int64_t)v * W + w] = 0ull;
+          }
+          nb = ms_thread_finalise<W>(a, v, acc, fnext, L);
+          if (nb) {
+            atomicOr(fbm_next + (v >> 5), 1u << (v & 31));
+            dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+          } else {
+            // saturated (or nothing new): finished for the rest of the sweep once its current word is empty too
+            bool sat = true;
+#pragma unroll
+            for (int w = 0; w < W; w++) sat &= __ldcg(a.seen + (int64_t)v * W + w) == full[w];
+            if (sat && !fbit(fbm_cur, v)) atomicOr(a.done + (v >> 5), 1u << (v & 31));
+          }
+        }
+        block_push(nb, v, dv, a.qv[so], a.qe[so], a.lctr + so, &psc);
       }
     } else {
       // light rows, 32-vertex tiles per warp: one load of the done bitmap skips finished vertices; the
@@ -449,10 +479,10 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         }
       }
     }
-    // heavy-row chunks: one warp per chunk, OR-reduced, combined with atomicOr
-    for (int64_t c = gw; c < a.nchunks; c += gws) {
+    // heavy-row chunks (dense levels; a sparse level pushed into every candidate, hubs included): one warp
+    // per chunk, OR-reduced, combined with atomicOr
+    for (int64_t c = sparse ? a.nchunks : gw; c < a.nchunks; c += gws) {
       const int64_t v = a.chunk_row[c], e0 = a.chunk_e0[c], e1 = min(a.off[v + 1], e0 + MS_CHUNK);
-      if (sparse && __ldcg(a.stamp + v) != L + 1) continue;  // a sparse level pulls its candidates only
       ull acc[W];
       ld_words<W>(a.seen + v * W, acc);  // seen changes only in the finalisation after the barrier
       bool sat = true;
@@ -480,7 +510,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       }
     }
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-    for (int64_t h = gt; h < a.nheavy; h += gts) {
+    for (int64_t h = sparse ? a.nheavy : gt; h < a.nheavy; h += gts) {
       const int64_t v = a.heavy_rows[h];
       ull acc[W];
 #pragma unroll
