@@ -499,12 +499,12 @@ def run_gb300(args):
         b = 8 * (n + 1) + 4 * nnz + n * kp * zb  # CSR once, the packed distance rows once
         kern_ms = float(np.mean([s["ms_lap_kernel"] for s in head["stats"]]))
         ach = b / (kern_ms * 1e-3) / 1e9
-        roof_lap = {"kernel": "lgram_kernel<uint8_t,2,4>", "bound": "hbm", "achieved": ach, "peak": peak,
+        roof_lap = {"kernel": "lgram_kernel<uint8_t,64,4>", "bound": "hbm", "achieved": ach, "peak": peak,
                     "unit": "GB/s", "frac": ach / peak,
                     "traffic": profiled_traffic("lgram_kernel_rmat22.md" if args.rmat_scale == 22 and kind == "rmat"
                                                 else "none"),
                     "peak_source": pk_src, "algorithmic_bytes_per_launch": b, "kernel_ms": kern_ms,
-                    "gathered_bytes_per_launch": nnz * kp * zb}
+                    "gathered_bytes_per_launch": nnz // 2 * kp * zb}  # each undirected edge's upper end
     if rank != 0:
         return
     h2d, d2h = R.h2d(), R.d2h()

@@ -147,6 +147,7 @@ struct ZSrc {
 struct ExactBasis {
   double *A = nullptr;   // [k][ld]
   const ull *GI = nullptr;  // [ld][ld] Z^T Z (upper triangle)
+  const ull *GD = nullptr;  // [ld][ld] Z^T D Z (upper triangle)
   int *acc_idx = nullptr;  // [k] Z index of each accepted column (D column + 1)
   int ld = 0;
   unsigned maxz = 0, maxdeg = 0;

@@ -19,9 +19,10 @@
 //                    32-bit partial sums flushed to 64-bit atomics under a per-row magnitude bound)
 //   coef_kernel      the candidate loop in coefficient space (one CTA, FP64)
 //   pack_kernel      the accepted columns as a row-major uint8 / uint16 matrix Z_acc (n x kp)
-//   lgram_kernel     Z_acc^T L Z_acc: per row (or heavy-row chunk) r = deg z_i - sum_j z_j gathered by a
-//                    warp (16-bit lanes packed two to a register for uint8 rows), then the outer product
-//                    z_i (x) r accumulated in register tiles -- the Laplacian product never reaches memory
+//   lgram_kernel     Z_acc^T A Z_acc from each undirected edge once: per row (or heavy-row chunk) the sum of
+//                    the neighbours above it gathered by a warp (16-bit lanes packed two to a register for uint8
+//                    rows), then the outer product with z_i accumulated in register tiles -- the adjacency
+//                    product never reaches memory; lfin_kernel subtracts it from G_D's accepted entries
 //   mgram_kernel     M = A_acc^T (Z_acc^T L Z_acc) A_acc (FP64, k x k)
 //   coords kernels   X = Z (A Y) in fixed point: A Y scaled to 62-bit integers per coordinate, exact
 //                    integer row sums, one rounding to FP64; then the unit-norm scaling of getCoordinates
@@ -854,10 +855,12 @@ __global__ void pack_kernel(ZSrc src, int64_t n, const int *acc_idx, int k, int 
 }
 
 // ------------------------------------------------------------------------------------------------
-// Z_acc^T L Z_acc.  Items: rows 0..n-1 (rows of degree > heavy contribute nothing as rows) and the
-// heavy rows' chunks of at most `chunk` (<= 256) edges.  Item u of row i has z = Z_acc[i] and
-// r = (deg_i z if the item holds the row's diagonal term) - sum over its edges of Z_acc[j]; the items'
-// z (x) r sum to Z^T (D Z - A Z) = Z^T L Z.
+// Z_acc^T L Z_acc = Z_acc^T D Z_acc - Z_acc^T A Z_acc, the first term read off G_D (the candidates' exact
+// Z^T D Z), the second from each undirected edge once: with T2 = sum over items of z (x) u, item u of row i
+// having z = Z_acc[i] and u = 2 * (sum of Z_acc[j] over its edges with j > i) + (its self-loops) * z,
+// Z^T A Z = (T2 + T2^T) / 2 for a symmetric adjacency (lfin_kernel forms the difference).  Items: rows
+// 0..n-1 (rows of degree > heavy contribute nothing as rows) and the heavy rows' chunks of at most `chunk`
+// (<= 256) edges.  Only half the neighbour rows are gathered, at the price of the full (not symmetric) T2.
 //
 // Gathers: a row of Z_acc is KP values; LPR lanes read it with one 16-byte load each, so a warp is
 // G = 32 / LPR lane groups, each on its own neighbour, and one load instruction fetches G neighbour rows.
@@ -910,7 +913,7 @@ struct LgArgs {
   int64_t heavy;  // rows of degree > heavy are done as chunks
   const int64_t *chunk_row, *chunk_e0;
   int64_t nchunks, chunk;
-  ull *GL;        // [kp x kp], p <= q at p * kp + q, two's complement
+  ull *GL;        // T2 [kp x kp], every entry (p, q) at p * kp + q, two's complement
   int ntiles;
 };
 
@@ -930,9 +933,9 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
   const int gi = lane / LPR, pi = lane % LPR;  // lane group (neighbour) and slice within the row
   const T *Z = (const T *)a.Z;
   const int t = blockIdx.y * LG_THREADS + threadIdx.x;
-  int pb, qb;
-  tile_of(t, 0, KP / TS, pb, qb);
-  const bool active = t < a.ntiles && pb >= 0;
+  constexpr int NBK = KP / TS;
+  const int pb = t / NBK, qb = t - (t / NBK) * NBK;  // every tile of the (not symmetric) T2
+  const bool active = t < a.ntiles;
   int acc[TS][TS];
 #pragma unroll
   for (int i = 0; i < TS; i++)
@@ -945,7 +948,7 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
 #pragma unroll
       for (int j = 0; j < TS; j++) {
         const int p = TS * pb + i, q = TS * qb + j;
-        if (p <= q && acc[i][j]) atomicAdd(a.GL + (int64_t)p * KP + q, (ull)(long long)acc[i][j]);
+        if (acc[i][j]) atomicAdd(a.GL + (int64_t)p * KP + q, (ull)(long long)acc[i][j]);
         acc[i][j] = 0;
       }
   };
@@ -964,21 +967,15 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
       if (slot >= LG_ITEMS) break;
       const int64_t u = u0 + slot;
       int64_t row = -1, e0 = 0, e1 = 0;
-      bool diag = false;
       if (u < a.n) {
         e0 = a.off[u];
         e1 = a.off[u + 1];
-        if (e1 - e0 <= a.heavy) {
-          row = u;
-          diag = true;
-        }
+        if (e1 - e0 <= a.heavy) row = u;
       } else if (u < items) {
         const int64_t c = u - a.n;
         row = a.chunk_row[c];
         e0 = a.chunk_e0[c];
-        const int64_t re0 = a.off[row], re1 = a.off[row + 1];
-        e1 = min(e0 + a.chunk, re1);
-        diag = e0 == re0;
+        e1 = min(e0 + a.chunk, a.off[row + 1]);
       }
       unsigned zm = 0, rm = 0;
       if (row >= 0) {
@@ -986,21 +983,32 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
         nb.zero();
         // the packed rows are gathered again and again (evict-last in L2), the adjacency streams by once
         const uint64_t keep = l2_policy_evict_last(), stream = l2_policy_evict_first();
+        // only the neighbours above the row: every undirected edge once (ZtAZ = T + T^T, T = sum_i z_i (x)
+        // sum_{j > i} z_j); self-loops counted (their z_i z_i^T goes in once)
+        int selfc = 0;
         int64_t e = e0 + gi;
         for (; e + G < e1; e += 2 * G) {
           const int64_t v0 = ld_nc_hint(a.adj + e, stream), v1 = ld_nc_hint(a.adj + e + G, stream);
-          const uint4 x0 = ld_nc_hint16((const uint4 *)(Z + v0 * KP) + pi, keep);
-          const uint4 x1 = ld_nc_hint16((const uint4 *)(Z + v1 * KP) + pi, keep);
+          uint4 x0 = make_uint4(0, 0, 0, 0), x1 = make_uint4(0, 0, 0, 0);
+          if (v0 > row) x0 = ld_nc_hint16((const uint4 *)(Z + v0 * KP) + pi, keep);
+          if (v1 > row) x1 = ld_nc_hint16((const uint4 *)(Z + v1 * KP) + pi, keep);
+          selfc += (v0 == row) + (v1 == row);
           nb.add(x0);
           nb.add(x1);
         }
-        if (e < e1) nb.add(ld_nc_hint16((const uint4 *)(Z + (int64_t)ld_nc_hint(a.adj + e, stream) * KP) + pi, keep));
+        if (e < e1) {
+          const int64_t v0 = ld_nc_hint(a.adj + e, stream);
+          if (v0 > row) nb.add(ld_nc_hint16((const uint4 *)(Z + v0 * KP) + pi, keep));
+          selfc += v0 == row;
+        }
 #pragma unroll
-        for (int m = LPR; m < 32; m <<= 1) nb.add_from(m);
+        for (int m = LPR; m < 32; m <<= 1) {
+          nb.add_from(m);
+          selfc += __shfl_xor_sync(PHDE_FULL_MASK, selfc, m);
+        }
         // every group of the warp now holds the row's sums: lane (gi, pi) finishes columns gi * CPL .. + CPL of
         // slice pi (sum registers gi * RPL .. + RPL, picked by selects: no indexed register arrays)
         const uint4 own = __ldg((const uint4 *)(Z + row * KP) + pi);
-        const int deg = diag ? (int)(a.off[row + 1] - a.off[row]) : 0;
         int zi[CPL], r[CPL];
 #pragma unroll
         for (int k2 = 0; k2 < RPL; k2++) {
@@ -1019,7 +1027,7 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
                                          : (int)((ow >> (16 * ((c0 + h) & 1))) & 0xffffu);
             const int sum = sizeof(T) == 1 ? (int)((sv >> (16 * h)) & 0xffffu) : (int)sv;
             zi[c] = z;
-            r[c] = deg * z - sum;
+            r[c] = 2 * sum + selfc * z;  // the row's u = 2 sum_{j > i} z_j + (self-loops) z_i
             zm = max(zm, (unsigned)z);
             rm = max(rm, (unsigned)abs(r[c]));
           }
@@ -1056,7 +1064,7 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
             for (int j = 0; j < TS; j++) {
               const int p = TS * pb + i, q = TS * qb + j;
               const long long v = (long long)zr[p] * (long long)rr[q];
-              if (p <= q && v) atomicAdd(a.GL + (int64_t)p * KP + q, (ull)v);
+              if (v) atomicAdd(a.GL + (int64_t)p * KP + q, (ull)v);
             }
         }
         continue;
@@ -1083,6 +1091,18 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
     }
   }
   flush();
+}
+
+// G_L (upper triangle, p <= q < k) = G_D[acc_idx[p]][acc_idx[q]] - (T2[p][q] + T2[q][p]) / 2 (the sum is even:
+// it is twice Z^T A Z).  acc_idx increases, so the G_D entry is in G_D's upper triangle.
+__global__ void lfin_kernel(const ull *T2, int kp, const ull *GD, int ld, const int *acc_idx, int k, ull *GL) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < k * k; e += gridDim.x * blockDim.x) {
+    const int p = e / k, q = e - p * k;
+    if (p > q) continue;
+    const long long t = (long long)T2[(int64_t)p * kp + q] + (long long)T2[(int64_t)q * kp + p];
+    const long long d = (long long)GD[(int64_t)acc_idx[p] * ld + acc_idx[q]];
+    GL[(int64_t)p * kp + q] = (ull)(d - t / 2);
+  }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1464,6 +1484,7 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
   eb->A = A;
   eb->GI = GI;
+  eb->GD = GD;
   eb->acc_idx = acc_idx;
   eb->ld = ld;
   eb->maxz = hm[0];
@@ -1479,8 +1500,9 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
   const bool z16 = eb->maxz > 255u;
   const int kp = k <= 64 ? 64 : k <= 128 ? 128 : 256;
   void *Z = phde_buf(ctx, "ex.Z", (size_t)n * kp * (z16 ? 2 : 1));
+  ull *T2 = (ull *)phde_buf(ctx, "ex.T2", sizeof(ull) * kp * kp);
   ull *GL = (ull *)phde_buf(ctx, "ex.GL", sizeof(ull) * kp * kp);
-  if (!Z || !GL) return PHDE_ERR_OOM;
+  if (!Z || !T2 || !GL) return PHDE_ERR_OOM;
   const int gp = grid_n(ctx, n, 256, 8);
   if (src.lvl && !eb->Zq)  // level-mode columns exist only in the quad layout (distances below 255)
     return phde_fail(ctx, PHDE_ERR_INVALID, "exact path: level-mode columns without the byte layout");
@@ -1499,7 +1521,7 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
   int64_t nch, chunk;
   int rc = phde_heavy_chunks(ctx, &crow, &ce0, &nch, &chunk);
   if (rc) return rc;
-  PHDE_CK(ctx, cudaMemsetAsync(GL, 0, sizeof(ull) * kp * kp, ctx->stream));
+  PHDE_CK(ctx, cudaMemsetAsync(T2, 0, sizeof(ull) * kp * kp, ctx->stream));
   LgArgs a;
   a.off = ctx->d_off;
   a.adj = ctx->d_adj;
@@ -1511,10 +1533,10 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
   a.chunk_e0 = ce0;
   a.nchunks = nch;
   a.chunk = chunk;
-  a.GL = GL;
+  a.GL = T2;
   const int TS = kp <= 64 ? 4 : 8;
   const int nb = kp / TS;
-  a.ntiles = nb * (nb + 1) / 2;
+  a.ntiles = nb * nb;
   const int gy = (a.ntiles + LG_THREADS - 1) / LG_THREADS;
   const size_t smem = sizeof(int) * 2 * LG_ITEMS * (size_t)(kp + 4);
   const int64_t nslab = (n + nch + LG_ITEMS - 1) / LG_ITEMS;
@@ -1541,6 +1563,8 @@ int phde_exact_lap(phde_ctx *ctx, const ZSrc &src, int k, ExactBasis *eb, double
     else rc = launch(lgram_kernel<uint8_t, 256, 8>);
   }
   if (rc) return rc;
+  lfin_kernel<<<(k * k + 255) / 256, 256, 0, ctx->stream>>>(T2, kp, eb->GD, eb->ld, eb->acc_idx, k, GL);
+  PHDE_LAUNCHED(ctx);
   mgram_kernel<<<k, 256, 0, ctx->stream>>>(GL, kp, eb->A, eb->ld, eb->acc_idx, k, M);
   PHDE_LAUNCHED(ctx);
   return PHDE_OK;
