@@ -418,6 +418,13 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
         ctx->pivot_model.assign(w0, w0 + cnt);
       }
       if ((rc = phde_run_bfs_passes(ctx, P0, 0, nullptr, D, d_src, sumsq, edges, 1))) return rc;
+      // the first warm-start pass's Kcenters key (its eccentricity in the high word), read with the error word
+      unsigned long long key0 = 0;
+      {
+        const ull *keys = (const ull *)phde_buf(ctx, "kc.keys", 0);
+        if (!keys) return PHDE_ERR_OOM;
+        PHDE_CK(ctx, cudaMemcpyAsync(&key0, keys, sizeof(key0), cudaMemcpyDeviceToHost, ctx->stream));
+      }
       if ((rc = phde_check_device_err(ctx, "learned pivots: warm start"))) return rc;
       std::vector<int64_t> cand, warm(P0);
       std::vector<float> cscore;
@@ -434,11 +441,6 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       // source's eccentricity (the Kcenters key of pass 0), and the exact path's byte layout needs distances < 255
       bool level_mode = false;
       {
-        unsigned long long key0 = 0;
-        const ull *keys = (const ull *)phde_buf(ctx, "kc.keys", 0);
-        if (!keys) return PHDE_ERR_OOM;
-        PHDE_CK(ctx, cudaMemcpyAsync(&key0, keys, sizeof(key0), cudaMemcpyDeviceToHost, ctx->stream));
-        PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
         const int64_t cap = 2 * (int64_t)(key0 >> 32) + 1;
         const int64_t bytes = (cap + 1) * n * ((Mc + 63) / 64) * (int64_t)sizeof(ull);
         if (cap <= 254 && bytes <= PHDE_LEVEL_MODE_BYTES) {

@@ -675,6 +675,10 @@ struct CoefArgs {
   int *state;     // [0] accepted, [1] discarded, [2] examined, [3] next Z index
   double *dlog;   // [P]: norm of each discarded candidate (by candidate index = Z index - 1); NaN otherwise
   int sa;         // the accepted rows of A are staged in shared memory too
+  // [0] largest distance, [1] largest degree (the Gram kernels': launched before this one with no host
+  // round trip, so the range check is repeated here); nmax = max(nnz, n)
+  const unsigned *maxz;
+  double nmax;
 };
 
 // GB300 issues FP64 at two lanes per clock per SM: a warp-wide FP64 instruction holds the pipe for 16 clocks
@@ -685,6 +689,10 @@ __global__ void __launch_bounds__(CF_THREADS, 1) coef_kernel(CoefArgs a) {
   extern __shared__ double cs[];
   __shared__ int s_idx[PHDE_MAX_K];
   __shared__ double s_inv, s_c0, s_nrm;
+  {  // out of the exact path's range (the host reads the same words and takes the FP64 vector kernels)
+    const double mz = (double)__ldg(a.maxz), md = (double)__ldg(a.maxz + 1);
+    if (mz > 65535.0 || a.nmax * mz * mz >= 9007199254740992.0 || md * mz >= 2147483647.0) return;
+  }
   const int ld = a.ld;
   double *rr = cs, *gdr = cs + ld, *cq = cs + 2 * ld, *rden = cq + a.k, *part = rden + a.k;
   double *GIs = part + CF_THREADS, *GDs = GIs + (size_t)a.nc * a.nc;
@@ -925,10 +933,19 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
   constexpr int CPL = V / G;              // columns of a slice each lane finishes (2, 4 or 8)
   constexpr int RPL = sizeof(T) == 1 ? CPL / 2 : CPL;  // sum registers those columns sit in
   constexpr int SL = KP + 4;
-  extern __shared__ int lsm[];  // zs[LG_ITEMS][SL], rs[LG_ITEMS][SL]
+  // uint8 rows (PK): the items' z bytes and neighbour sums s (< 2^16: at most 256 neighbours of at most 255) are
+  // staged four items to a word -- Zb[quad][col] = the z bytes of items 4 quad .. +3, Sh[quad][h][col] = the s
+  // of items 4 quad + 2h, +1 as 16-bit halves -- and the outer products go by dp2a, four items in two
+  // instructions; T = sum z (x) s is accumulated and flushed doubled, self-loops (c z (x) z) go to T2 directly.
+  // uint16 rows: zs[LG_ITEMS][SL], rs[LG_ITEMS][SL] as ints, u = 2 s + c z, one IMAD per item.
+  constexpr bool PK = sizeof(T) == 1;
+  extern __shared__ int lsm[];
   __shared__ ull s_bnd[LG_ITEMS];
+  __shared__ int s_self[LG_ITEMS];
   __shared__ int s_next;
   int *zs = lsm, *rs = lsm + LG_ITEMS * SL;
+  uint8_t *Zb = (uint8_t *)lsm;
+  uint16_t *Sh = (uint16_t *)(Zb + LG_ITEMS * KP);
   const int lane = threadIdx.x & 31;
   const int gi = lane / LPR, pi = lane % LPR;  // lane group (neighbour) and slice within the row
   const T *Z = (const T *)a.Z;
@@ -936,7 +953,7 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
   constexpr int NBK = KP / TS;
   const int pb = t / NBK, qb = t - (t / NBK) * NBK;  // every tile of the (not symmetric) T2
   const bool active = t < a.ntiles;
-  int acc[TS][TS];
+  uint32_t acc[TS][TS];  // PK: T (unsigned); uint16 rows: T2 (signed, two's complement)
 #pragma unroll
   for (int i = 0; i < TS; i++)
 #pragma unroll
@@ -948,7 +965,8 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
 #pragma unroll
       for (int j = 0; j < TS; j++) {
         const int p = TS * pb + i, q = TS * qb + j;
-        if (acc[i][j]) atomicAdd(a.GL + (int64_t)p * KP + q, (ull)(long long)acc[i][j]);
+        if (acc[i][j])
+          atomicAdd(a.GL + (int64_t)p * KP + q, PK ? 2ull * (ull)acc[i][j] : (ull)(long long)(int)acc[i][j]);
         acc[i][j] = 0;
       }
   };
@@ -1027,23 +1045,44 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
                                          : (int)((ow >> (16 * ((c0 + h) & 1))) & 0xffffu);
             const int sum = sizeof(T) == 1 ? (int)((sv >> (16 * h)) & 0xffffu) : (int)sv;
             zi[c] = z;
-            r[c] = 2 * sum + selfc * z;  // the row's u = 2 sum_{j > i} z_j + (self-loops) z_i
+            // uint8 rows stage s itself; uint16 rows the row's u = 2 sum_{j > i} z_j + (self-loops) z_i
+            r[c] = PK ? sum : 2 * sum + selfc * z;
             zm = max(zm, (unsigned)z);
             rm = max(rm, (unsigned)abs(r[c]));
           }
         }
-        int *zd = zs + slot * SL + pi * V + gi * CPL, *rd = rs + slot * SL + pi * V + gi * CPL;
+        if constexpr (PK) {
 #pragma unroll
-        for (int c = 0; c < CPL; c += 2) {
-          *(int2 *)(zd + c) = make_int2(zi[c], zi[c + 1]);
-          *(int2 *)(rd + c) = make_int2(r[c], r[c + 1]);
+          for (int c = 0; c < CPL; c++) {
+            const int col = pi * V + gi * CPL + c;
+            Zb[((slot >> 2) * KP + col) * 4 + (slot & 3)] = (uint8_t)zi[c];
+            Sh[(((slot >> 2) * 2 + ((slot & 3) >> 1)) * KP + col) * 2 + (slot & 1)] = (uint16_t)r[c];
+          }
+          if (lane == 0) s_self[slot] = selfc;
+        } else {
+          int *zd = zs + slot * SL + pi * V + gi * CPL, *rd = rs + slot * SL + pi * V + gi * CPL;
+#pragma unroll
+          for (int c = 0; c < CPL; c += 2) {
+            *(int2 *)(zd + c) = make_int2(zi[c], zi[c + 1]);
+            *(int2 *)(rd + c) = make_int2(r[c], r[c + 1]);
+          }
         }
       } else {
-        int *zd = zs + slot * SL + pi * V + gi * CPL, *rd = rs + slot * SL + pi * V + gi * CPL;
+        if constexpr (PK) {
 #pragma unroll
-        for (int c = 0; c < CPL; c += 2) {
-          *(int2 *)(zd + c) = make_int2(0, 0);
-          *(int2 *)(rd + c) = make_int2(0, 0);
+          for (int c = 0; c < CPL; c++) {
+            const int col = pi * V + gi * CPL + c;
+            Zb[((slot >> 2) * KP + col) * 4 + (slot & 3)] = 0;
+            Sh[(((slot >> 2) * 2 + ((slot & 3) >> 1)) * KP + col) * 2 + (slot & 1)] = 0;
+          }
+          if (lane == 0) s_self[slot] = 0;
+        } else {
+          int *zd = zs + slot * SL + pi * V + gi * CPL, *rd = rs + slot * SL + pi * V + gi * CPL;
+#pragma unroll
+          for (int c = 0; c < CPL; c += 2) {
+            *(int2 *)(zd + c) = make_int2(0, 0);
+            *(int2 *)(rd + c) = make_int2(0, 0);
+          }
         }
       }
       zm = __reduce_max_sync(PHDE_FULL_MASK, zm);
@@ -1052,6 +1091,50 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
     }
     __syncthreads();
     const int nit = active ? (int)min((int64_t)LG_ITEMS, items - u0) : 0;  // threads without a tile skip it
+    if constexpr (PK) {
+      const uint32_t *Zw = (const uint32_t *)Zb, *Sw = (const uint32_t *)Sh;
+      for (int q4 = 0; q4 < (nit + 3) / 4; q4++) {
+        // every product is at most z_max * s_max of its item (< 2^24), the quad's sum below 2^26
+        const ull b = s_bnd[4 * q4] + s_bnd[4 * q4 + 1] + s_bnd[4 * q4 + 2] + s_bnd[4 * q4 + 3];
+        if (b == 0) continue;
+        if (run + b >= B32) {
+          flush();
+          run = 0;
+        }
+        run += b;
+        uint32_t zq[TS], alo[TS], ahi[TS];
+#pragma unroll
+        for (int i = 0; i < TS; i += 4) {
+          const uint4 x = *(const uint4 *)(Zw + q4 * KP + TS * pb + i);
+          const uint4 y0 = *(const uint4 *)(Sw + (2 * q4) * KP + TS * qb + i);
+          const uint4 y1 = *(const uint4 *)(Sw + (2 * q4 + 1) * KP + TS * qb + i);
+          zq[i] = x.x, zq[i + 1] = x.y, zq[i + 2] = x.z, zq[i + 3] = x.w;
+          alo[i] = y0.x, alo[i + 1] = y0.y, alo[i + 2] = y0.z, alo[i + 3] = y0.w;
+          ahi[i] = y1.x, ahi[i + 1] = y1.y, ahi[i + 2] = y1.z, ahi[i + 3] = y1.w;
+        }
+#pragma unroll
+        for (int i = 0; i < TS; i++)
+#pragma unroll
+          for (int j = 0; j < TS; j++) {
+            acc[i][j] = __dp2a_lo(alo[j], zq[i], acc[i][j]);
+            acc[i][j] = __dp2a_hi(ahi[j], zq[i], acc[i][j]);
+          }
+      }
+      // self-loops (rare): c z (x) z straight into T2
+      for (int slot = 0; slot < nit; slot++) {
+        const int c = s_self[slot];
+        if (c == 0) continue;
+#pragma unroll
+        for (int i = 0; i < TS; i++)
+#pragma unroll
+          for (int j = 0; j < TS; j++) {
+            const int p = TS * pb + i, q = TS * qb + j;
+            const ull v = (ull)c * Zb[((slot >> 2) * KP + p) * 4 + (slot & 3)] * Zb[((slot >> 2) * KP + q) * 4 + (slot & 3)];
+            if (v) atomicAdd(a.GL + (int64_t)p * KP + q, v);
+          }
+      }
+      continue;
+    }
     for (int slot = 0; slot < nit; slot++) {
       const ull b = s_bnd[slot];
       if (b == 0) continue;
@@ -1086,7 +1169,7 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
 #pragma unroll
         for (int i = 0; i < TS; i++)
 #pragma unroll
-          for (int j = 0; j < TS; j++) acc[i][j] += zp[i] * rq[j];
+          for (int j = 0; j < TS; j++) acc[i][j] += (uint32_t)(zp[i] * rq[j]);
       }
     }
   }
@@ -1442,16 +1525,9 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
   for (;;) {
     int rc = exact_zgram(ctx, src, P, c0, c1, GI, GD, ld, maxz, Zq, smaxz, byte_state);
     if (rc) return rc;
-    PHDE_CK(ctx, cudaMemcpyAsync(hm, maxz, sizeof(hm), cudaMemcpyDeviceToHost, ctx->stream));
-    PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    byte_state = hm[0] <= 255u ? 1 : 0;
-    // G_I, G_D, Z^T L Z entries are at most nnz * maxz^2 (and n * maxz^2): exact in FP64 below 2^53; the
-    // Laplacian rows r = deg z - sum z stay in 32 bits; distances fit 16 bits
-    const double mz = (double)hm[0];
-    if (hm[0] > 65535u || (double)std::max<int64_t>(ctx->nnz, n) * mz * mz >= 9007199254740992.0 ||
-        (double)hm[1] * mz >= 2147483647.0)
-      return phde_fail(ctx, PHDE_ERR_TOO_LARGE, "exact path: distances or degrees too large");
     CoefArgs ca;
+    ca.maxz = maxz;
+    ca.nmax = (double)std::max<int64_t>(ctx->nnz, n);
     ca.GI = GI;
     ca.GD = GD;
     ca.ld = ld;
@@ -1471,8 +1547,16 @@ int phde_exact_orth(phde_ctx *ctx, const ZSrc &src, int P, int k, ExactBasis *eb
     ca.dlog = dlog;
     coef_kernel<<<1, CF_THREADS, csmem, ctx->stream>>>(ca);
     PHDE_LAUNCHED(ctx);
+    PHDE_CK(ctx, cudaMemcpyAsync(hm, maxz, sizeof(hm), cudaMemcpyDeviceToHost, ctx->stream));
     PHDE_CK(ctx, cudaMemcpyAsync(hs, state, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
     PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    byte_state = hm[0] <= 255u ? 1 : 0;
+    // G_I, G_D, Z^T L Z entries are at most nnz * maxz^2 (and n * maxz^2): exact in FP64 below 2^53; the
+    // Laplacian sums stay in 32 bits; distances fit 16 bits (coef_kernel made the same check and did nothing)
+    const double mz = (double)hm[0];
+    if (hm[0] > 65535u || (double)std::max<int64_t>(ctx->nnz, n) * mz * mz >= 9007199254740992.0 ||
+        (double)hm[1] * mz >= 2147483647.0)
+      return phde_fail(ctx, PHDE_ERR_TOO_LARGE, "exact path: distances or degrees too large");
     if (hs[0] >= k || c1 >= P + 1) break;
     c0 = c1;
     c1 = std::min(ld, c1 + 16);

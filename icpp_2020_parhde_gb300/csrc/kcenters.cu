@@ -16,10 +16,12 @@
 //               membership test is a shared-memory hit;
 //   both append the new frontier with block-aggregated 64-bit atomics that keep (slot, edge prefix)
 //   together, so the next top-down step is load balanced even around hub vertices.
-// The top-down / bottom-up switch follows the reference rule (alpha = 15, beta = 18): go bottom-up
-// when the frontier's out-edges exceed edges_to_check / alpha, stay there while the frontier grows
-// or exceeds n / beta (bfs.cc:159-183).  Hop distances are unique, so the result is bit-exact
-// whatever the direction schedule.
+// The top-down / bottom-up switch has the reference's form (bfs.cc:159-183): go bottom-up when the
+// frontier's out-edges exceed edges_to_check / alpha, stay there while the frontier grows or exceeds
+// n / beta, beta = 18 as there, alpha = 6 instead of 15: on the GPU a bottom-up level scans every
+// unvisited vertex, and at the frontier sizes between the two rules (R-MAT 22: 8.7 M out-edges) the
+// top-down level is the faster one (130-235 us against 300-320 us).  Hop distances are unique, so the
+// result is bit-exact whatever the direction schedule.
 //
 // Selection (ParHDE.cpp:127-155): min_d[v] = min(min_d[v], d_p[v]); the next source is the vertex of
 // largest min_d, lowest index first (a 64-bit atomicMax on (min_d << 32) | ~v); if that vertex is in
@@ -585,7 +587,7 @@ int phde_run_bfs_passes(phde_ctx *ctx, int P, int variant, const int64_t *d_fixe
   a.gs = ctx->d_sync;
   a.err = ctx->d_err;
   a.timeout_ns = ctx->timeout_ns;
-  a.alpha = 15;
+  a.alpha = 6;
   a.beta = 18;
   void *args[] = {&a};
   cudaEventRecord(ctx->kev[0], ctx->stream);

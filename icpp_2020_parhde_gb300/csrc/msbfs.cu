@@ -72,6 +72,7 @@ struct MsArgs {
   int32_t *stamp;             // [n] claim stamps of sparse levels (L + 1), zeroed
   uint32_t *cand;             // [n] candidates of a sparse level
   unsigned *ccount;           // [2] candidate counters, by level parity
+  ull *cedge;                 // [2] the candidates' total degree, by level parity
   unsigned *tctr;             // [4] dense levels: next 32-vertex tile to hand out, slot L % 4 (reset one level ahead)
   int64_t sparse_edges;       // a level runs sparse when its frontier has fewer out-edges
   int *levels_out;
@@ -338,6 +339,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       a.lctr[(L + 1) & 3] = 0ull;
       a.lstat[(L + 1) & 3] = 0ull;
       a.ccount[(L + 1) & 1] = 0u;
+      a.cedge[(L + 1) & 1] = 0ull;
       a.tctr[(L + 1) & 3] = 0u;
     }
     if (threadIdx.x == 0) s_stat = 0ull;
@@ -349,6 +351,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
     // (above that, most neighbours are in it and the test only lengthens the dependent chain)
     const bool use_bm = (int64_t)(fstat >> 32) <= n / 4;
     const bool sparse = (int64_t)fedges < a.sparse_edges;
+    bool push = false;  // a sparse level that pushes (set below, uniform)
     if (sparse) {
       if (!built_f) {
         // the previous level ran dense: list its frontier (the vertices with a nonzero current word)
@@ -380,70 +383,111 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         for (int64_t i = gt; i < n * W; i += gts) fnext[i] = 0ull;
       }
       if (!built_f && !grid_sync(a.gs, a.err, a.timeout_ns)) return;
-      // push: new bits can only appear next to the frontier, so every out-edge (u, v) of the frontier ORs u's
-      // frontier word into v's accumulator (hacc, zero outside this level) and claims v once (stamp L+1) as a
-      // candidate -- work in proportion to the frontier's edges, where pulling would scan every candidate's
-      // whole adjacency (hubs next to a small frontier cost far more).  Finished vertices are skipped.
+      // new bits can only appear next to the frontier: claim those neighbours once (stamp L+1), edge-balanced
+      // over the frontier's edges, skipping finished vertices, and add up the candidates' degrees.  Then either
+      // pull every candidate's neighbours (work in proportion to the candidates' edges) or, when those are
+      // more than twice the frontier's -- hubs next to a small frontier, as in R-MAT's first levels -- push:
+      // every frontier edge (u, v) ORs u's frontier word into v's accumulator (hacc, zero outside a level),
+      // work in proportion to the frontier's edges but an L2 reduction per word.
       const ull fctr = __ldcg(a.lctr + sf);
       const uint32_t fcnt = (uint32_t)(fctr >> 32), fe = (uint32_t)(fctr & 0xffffffffull);
       const uint32_t *fqv = a.qv[sf], *fqe = a.qe[sf];
       unsigned *cc = a.ccount + (L & 1);
+      ull *ce = a.cedge + (L & 1);
       const uint64_t keep = l2_policy_evict_last();
+      // `done` also marks the hub rows (dense levels pull them by chunks): those stay candidates
+      auto target = [&](int64_t e, uint32_t &u) -> int64_t {  // v of frontier edge e, or -1 when finished
+        const uint32_t slot = owner_slot(fqe, fcnt, (uint32_t)e);
+        u = fqv[slot];
+        const uint32_t v = __ldg(a.adj + a.off[u] + (e - (int64_t)fqe[slot]));
+        bool skip = (__ldcg(a.done + (v >> 5)) >> (v & 31)) & 1u;
+        if (skip) skip = a.off[v + 1] - a.off[v] <= MS_HEAVY;
+        return skip ? -1 : (int64_t)v;
+      };
       for (int64_t base = gw * 32; base < fe; base += gws * 32) {
         const int64_t e = base + lane;
         bool mine = false;
         uint32_t v = 0;
+        ull dsum = 0;
         if (e < fe) {
-          const uint32_t slot = owner_slot(fqe, fcnt, (uint32_t)e);
-          const uint32_t u = fqv[slot];
-          v = __ldg(a.adj + a.off[u] + (e - (int64_t)fqe[slot]));
-          // `done` also marks the hub rows (dense levels pull them by chunks): those still take pushes
-          bool skip = (__ldcg(a.done + (v >> 5)) >> (v & 31)) & 1u;
-          if (skip) skip = a.off[v + 1] - a.off[v] <= MS_HEAVY;
-          if (!skip) {
-            ull x[W];
-            ld_front<W>(fcur + (int64_t)u * W, x, keep);
-#pragma unroll
-            for (int w = 0; w < W; w++)
-              if (x[w]) red_or_hint(a.hacc + (int64_t)v * W + w, x[w], keep);
+          uint32_t u;
+          const int64_t t = target(e, u);
+          if (t >= 0) {
+            v = (uint32_t)t;
             mine = atomicMax(a.stamp + v, L + 1) < L + 1;
+            if (mine) dsum = (ull)(a.off[v + 1] - a.off[v]);
           }
         }
         const unsigned bal = __ballot_sync(PHDE_FULL_MASK, mine);
         unsigned slot0 = 0;
-        if (lane == 0 && bal) slot0 = atomicAdd(cc, (unsigned)__popc(bal));
+        dsum = warp_sum(dsum);
+        if (lane == 0 && bal) {
+          slot0 = atomicAdd(cc, (unsigned)__popc(bal));
+          atomicAdd(ce, dsum);
+        }
         slot0 = __shfl_sync(PHDE_FULL_MASK, slot0, 0);
         if (mine) a.cand[slot0 + __popc(bal & ((1u << lane) - 1u))] = v;
       }
       if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-      // finalise the candidates (thread per candidate, the accumulator cleared for the next sparse level); the
-      // block-uniform loop lets block_push list the vertices given new bits
       const unsigned nc = __ldcg(cc);
-      for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < nc; i0 += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = i0 + threadIdx.x;
-        bool nb = false;
-        uint32_t v = 0, dv = 0;
-        if (i < nc) {
-          v = a.cand[i];
-          ull acc[W];
+      push = __ldcg(ce) > 2ull * fe;  // uniform
+      if (push) {
+        for (int64_t base = gw * 32; base < fe; base += gws * 32) {
+          const int64_t e = base + lane;
+          if (e < fe) {
+            uint32_t u;
+            const int64_t v = target(e, u);
+            if (v >= 0) {
+              ull x[W];
+              ld_front<W>(fcur + (int64_t)u * W, x, keep);
 #pragma unroll
-          for (int w = 0; w < W; w++) {
-            acc[w] = __ldcg(a.hacc + (int64_t)v * W + w);
-            a.hacc[(int64_t)v * W + w] = 0ull;
-          }
-          nb = ms_thread_finalise<W>(a, v, acc, fnext, L);
-          if (nb) {
-            atomicOr(fbm_next + (v >> 5), 1u << (v & 31));
-            dv = (uint32_t)(a.off[v + 1] - a.off[v]);
-          } else {
-            // saturated (or nothing new): finished for the rest of the sweep once its current word is empty too
-            bool sat = true;
-#pragma unroll
-            for (int w = 0; w < W; w++) sat &= __ldcg(a.seen + (int64_t)v * W + w) == full[w];
-            if (sat && !fbit(fbm_cur, v)) atomicOr(a.done + (v >> 5), 1u << (v & 31));
+              for (int w = 0; w < W; w++)
+                if (x[w]) red_or_hint(a.hacc + v * W + w, x[w], keep);
+            }
           }
         }
-        block_push(nb, v, dv, a.qv[so], a.qe[so], a.lctr + so, &psc);
+        if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
+        // finalise the candidates (thread per candidate, the accumulator cleared for the next level); the
+        // block-uniform loop lets block_push list the vertices given new bits
+        for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < nc; i0 += (int64_t)gridDim.x * blockDim.x) {
+          const int64_t i = i0 + threadIdx.x;
+          bool nb = false;
+          uint32_t v = 0, dv = 0;
+          if (i < nc) {
+            v = a.cand[i];
+            ull acc[W];
+#pragma unroll
+            for (int w = 0; w < W; w++) {
+              acc[w] = __ldcg(a.hacc + (int64_t)v * W + w);
+              a.hacc[(int64_t)v * W + w] = 0ull;
+            }
+            nb = ms_thread_finalise<W>(a, v, acc, fnext, L);
+            if (nb) {
+              atomicOr(fbm_next + (v >> 5), 1u << (v & 31));
+              dv = (uint32_t)(a.off[v + 1] - a.off[v]);
+            } else {
+              // saturated (or nothing new): finished for the rest of the sweep once its current word is empty
+              bool sat = true;
+#pragma unroll
+              for (int w = 0; w < W; w++) sat &= __ldcg(a.seen + (int64_t)v * W + w) == full[w];
+              if (sat && !fbit(fbm_cur, v)) atomicOr(a.done + (v >> 5), 1u << (v & 31));
+            }
+          }
+          block_push(nb, v, dv, a.qv[so], a.qe[so], a.lctr + so, &psc);
+        }
+      } else {
+        // pull the candidates (hub rows by chunks below); the block-uniform loop lets block_push list the
+        // vertices given new bits
+        const int gpb = blockDim.x / MS_GROUP;  // groups per block
+        for (int64_t i0 = (int64_t)blockIdx.x * gpb; i0 < nc; i0 += (int64_t)gridDim.x * gpb) {
+          const int64_t i = i0 + threadIdx.x / MS_GROUP;
+          const bool act = i < nc;
+          const int64_t v = act ? (int64_t)a.cand[i] : 0;
+          bool nb;
+          uint32_t dv;
+          ms_pull_vertex<W>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, v, act, gl, true, nb, dv);
+          block_push(nb, (uint32_t)v, dv, a.qv[so], a.qe[so], a.lctr + so, &psc);
+        }
       }
     } else {
       // light rows, 32-vertex tiles per warp: one load of the done bitmap skips finished vertices; the
@@ -479,10 +523,11 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         }
       }
     }
-    // heavy-row chunks (dense levels; a sparse level pushed into every candidate, hubs included): one warp
-    // per chunk, OR-reduced, combined with atomicOr
-    for (int64_t c = sparse ? a.nchunks : gw; c < a.nchunks; c += gws) {
+    // heavy-row chunks (a push level finalised every candidate, hubs included): one warp per chunk,
+    // OR-reduced, combined with atomicOr; a pull level takes its candidates only
+    for (int64_t c = push ? a.nchunks : gw; c < a.nchunks; c += gws) {
       const int64_t v = a.chunk_row[c], e0 = a.chunk_e0[c], e1 = min(a.off[v + 1], e0 + MS_CHUNK);
+      if (sparse && __ldcg(a.stamp + v) != L + 1) continue;
       ull acc[W];
       ld_words<W>(a.seen + v * W, acc);  // seen changes only in the finalisation after the barrier
       bool sat = true;
@@ -510,7 +555,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
       }
     }
     if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
-    for (int64_t h = sparse ? a.nheavy : gt; h < a.nheavy; h += gts) {
+    for (int64_t h = push ? a.nheavy : gt; h < a.nheavy; h += gts) {
       const int64_t v = a.heavy_rows[h];
       ull acc[W];
 #pragma unroll
@@ -727,8 +772,7 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
   uint32_t *lists = (uint32_t *)phde_buf(ctx, "ms.lists", sizeof(uint32_t) * 8 * lcap);  // qv[4], qe[4]
   uint32_t *cand = (uint32_t *)phde_buf(ctx, "ms.cand", sizeof(uint32_t) * n);
   int32_t *stamp = (int32_t *)phde_buf(ctx, "ms.stamp", sizeof(int32_t) * n);
-  // lctr[4], lstat[4], ccount[2], tctr[4]
-  const size_t ctr_bytes = sizeof(ull) * 8 + sizeof(unsigned) * 6;
+  const size_t ctr_bytes = sizeof(ull) * 10 + sizeof(unsigned) * 6;  // lctr[4], lstat[4], cedge[2], ccount[2], tctr[4]
   ull *lctr = (ull *)phde_buf(ctx, "ms.lctr", ctr_bytes);
   if ((!R && !lvl) || !seen || !f0 || !f1 || !hacc || !levels || !bms || !fbm || !lists || !cand || !stamp || !lctr)
     return PHDE_ERR_OOM;
@@ -791,7 +835,8 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
     }
     a.lctr = lctr;
     a.lstat = lctr + 4;
-    a.ccount = (unsigned *)(lctr + 8);
+    a.cedge = lctr + 8;
+    a.ccount = (unsigned *)(lctr + 10);
     a.tctr = a.ccount + 2;
     a.stamp = stamp;
     a.cand = cand;
