@@ -201,6 +201,7 @@ int phde_create(phde_ctx **out, int device) {
   for (auto &e : c->ev) cudaEventCreate(&e);
   for (auto &e : c->kev) cudaEventCreate(&e);
   for (auto &e : c->lev) cudaEventCreate(&e);
+  for (auto &e : c->tev) cudaEventCreate(&e);
   if (const char *t = getenv("PHDE_WAIT_LIMIT_MS")) c->timeout_ns = (uint64_t)atoll(t) * 1000000ull;
   if (const char *t = getenv("PHDE_CGS2")) c->column_cgs2 = std::string(t) == "column";
   if (const char *t = getenv("PHDE_TC_GRAM")) {
@@ -417,7 +418,14 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
         if ((rc = phde_default_pivot_model(&w0, &cnt))) return phde_fail(ctx, rc, "built-in pivot model has the wrong size");
         ctx->pivot_model.assign(w0, w0 + cnt);
       }
+      const bool ltrace = getenv("PHDE_LAYOUT_TRACE") != nullptr;
+      auto tmark = [&]() {
+        if (ltrace && ctx->ntev < 8) cudaEventRecord(ctx->tev[ctx->ntev++], ctx->stream);
+      };
+      ctx->ntev = 0;
+      tmark();
       if ((rc = phde_run_bfs_passes(ctx, P0, 0, nullptr, D, d_src, sumsq, edges, 1))) return rc;
+      tmark();
       // the first warm-start pass's Kcenters key (its eccentricity in the high word), read with the error word
       unsigned long long key0 = 0;
       {
@@ -432,6 +440,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       const int32_t *mind0 = (const int32_t *)phde_buf(ctx, "kc.min_d", sizeof(int32_t) * n);
       if (!mind0) return PHDE_ERR_OOM;
       if ((rc = phde_pivot_candidates(ctx, ctx->pivot_model.data(), M, mind0, cand, cscore))) return rc;
+      tmark();
       const int Mc = (int)cand.size();
       PHDE_CK(ctx, cudaMemcpyAsync(dc, cand.data(), sizeof(int64_t) * Mc, cudaMemcpyHostToDevice, ctx->stream));
       uint16_t *R = nullptr;
@@ -450,6 +459,7 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
         }
       }
       if (!level_mode && (rc = phde_msbfs_record(ctx, dc, Mc, &R, &RW))) return rc;
+      tmark();
       std::vector<int32_t> sub, csub;
       if ((rc = phde_cand_distances(ctx, D, P0, R, RW, dc, Mc, sub, csub, level_mode ? &lvl_sweep : nullptr)))
         return rc;
@@ -502,6 +512,17 @@ static int layout_impl(phde_ctx *ctx, const phde_layout_opts *o, double *coords_
       if (Pn > 0)
         PHDE_CK(ctx, cudaMemcpyAsync(d_src + P0, srcs.data(), sizeof(int64_t) * Pn, cudaMemcpyHostToDevice, ctx->stream));
       P_used = P0 + Pn;
+      tmark();
+      if (ltrace) {
+        PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        static const char *names[] = {"warm start", "features, scores, candidates", "multi-source BFS",
+                                      "candidate distances, order, columns"};
+        for (int i = 1; i < ctx->ntev; i++) {
+          float t = 0;
+          cudaEventElapsedTime(&t, ctx->tev[i - 1], ctx->tev[i]);
+          fprintf(stderr, "learned pivots: %s %.3f ms\n", i <= 4 ? names[i - 1] : "?", t);
+        }
+      }
     } else if (random) {
       std::vector<int32_t> r;
       glibc_rand_host((uint32_t)o->seed, P, r);

@@ -80,6 +80,9 @@ struct phde_ctx {
   // events bracketing each distance-kernel launch; kev_pending says a pair was recorded
   cudaEvent_t kev[2] = {};
   cudaEvent_t lev[2] = {};  // around the exact path's Laplacian Gram kernel; lev_pending says they were recorded
+  // PHDE_LAYOUT_TRACE=1: events at the learned pivot path's steps, printed after each layout
+  cudaEvent_t tev[8] = {};
+  int ntev = 0;
   bool lev_pending = false;
   bool kev_pending = false;
   double kernel_ms = 0;  // accumulated by phde_collect_kernel_time()
