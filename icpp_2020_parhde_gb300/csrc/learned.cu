@@ -20,6 +20,7 @@
 
 #include "ctx.h"
 #include "pivot_mlp_weights.h"
+#include "tc_common.cuh"
 
 namespace {
 
@@ -325,6 +326,185 @@ __global__ void cand_distances_lvl_kernel(const ull *lvl, int nlev, int W, int64
   }
 }
 
+// The same scores with layer 2 on the tensor cores (tcgen05): per tile of 128 vertices the layer-1 outputs H
+// (128 x 64, FP32) and, once per CTA, W2 (64 x 64) are split into three BF16 parts each and stored K-major in
+// shared memory; one thread issues the MMAs of six part products (hi.hi, hi.mid, mid.hi, hi.lo, lo.hi, mid.mid
+// -- the three dropped ones are below 2^-24 of the product) into an FP32 accumulator of 128 TMEM lanes x 64
+// columns; warps 0..3 read their lane quarter (one vertex per lane) and finish: bias, ReLU, the output unit,
+// the sigmoid and the histogram, while warps 4..7 compute the next tile's features.  FP32-faithful: the scores
+// agree with the CUDA-core kernel to FP32 rounding.
+// Every mbarrier wait is bounded; on expiry the kernel records PHDE_ERR_TIMEOUT and returns after its MMAs.
+constexpr int TM_THREADS = 256;
+constexpr int TM_B_PART = MLP_H * MLP_H * 2;     // one BF16 part of W2: 64 x 64 (8 KB)
+constexpr int TM_A_PART = MLP_TILE * MLP_H * 2;  // one BF16 part of H: 128 x 64 (16 KB)
+constexpr int TM_SMEM = 3 * TM_B_PART + 3 * TM_A_PART;
+constexpr uint32_t TM_IDESC = idesc_bf16(128, MLP_H);
+
+__global__ void __launch_bounds__(TM_THREADS) mlp_score_tc_kernel(const int64_t *off, const int32_t *d0,
+                                                                  const ull *hop2, const uint32_t *outw,
+                                                                  const ull *maxes, int64_t n, const float *weights,
+                                                                  float *score, unsigned *hist, int nbins,
+                                                                  const int32_t *gid, int *err,
+                                                                  uint64_t timeout_ns) {
+  extern __shared__ __align__(1024) uint8_t tsm[];  // B parts [3][64 x 64], A parts [3][128 x 64], histogram
+  uint8_t *Bp = tsm, *Ap = tsm + 3 * TM_B_PART;
+  unsigned *s_hist = (unsigned *)(tsm + TM_SMEM);
+  __shared__ float W1[MLP_H][MLP_IN], b1[MLP_H], b2[MLP_H], w3[MLP_H];
+  __shared__ float F[MLP_TILE][MLP_IN + 1];
+  __shared__ float s_b3;
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < MLP_H * MLP_IN; i += blockDim.x) W1[i / MLP_IN][i % MLP_IN] = weights[i];
+  const float *gb1 = weights + MLP_H * MLP_IN, *gW2 = gb1 + MLP_H, *gb2 = gW2 + MLP_H * MLP_H, *gw3 = gb2 + MLP_H;
+  for (int i = tid; i < MLP_H; i += blockDim.x) {
+    b1[i] = gb1[i];
+    b2[i] = gb2[i];
+    w3[i] = gw3[i];
+  }
+  if (tid == 0) s_b3 = gw3[MLP_H];
+  for (int i = tid; i < nbins; i += blockDim.x) s_hist[i] = 0u;
+  // B = W2 (row o = output unit, K = input unit), K-major: unit (o, 8-group g)
+  for (int u = tid; u < MLP_H * (MLP_H / 8); u += blockDim.x) {
+    const int o = u / (MLP_H / 8), g = u % (MLP_H / 8);
+    float v[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = gW2[o * MLP_H + 8 * g + i];
+    store_split8(v, Bp + core_off(o, g), Bp + TM_B_PART + core_off(o, g), Bp + 2 * TM_B_PART + core_off(o, g));
+  }
+  if (tid == 0) {
+    mbar_init(smem_u32(&s_bar), 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  if (warp == 0) tmem_alloc(smem_u32(&s_tmem), MLP_H);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const float ldeg = logf(1.f + (float)maxes[0]), lhop = logf(1.f + (float)maxes[1]);
+  const float md0 = maxes[2] ? (float)maxes[2] : 1.f;
+  // warps 4..7 compute the features of tile vertex tid - 128, one tile ahead: their loads for the next tile
+  // are in flight while the tensor core and warps 0..3 finish the current one
+  float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+  auto features = [&](int64_t t0) {
+    const int64_t v = t0 + (tid - MLP_TILE);
+    f0 = f1 = f2 = f3 = 0.f;
+    if (v < n) {
+      float ld = ldeg, lh = lhop, m0 = md0;
+      if (gid) {  // this vertex's graph's maxima
+        const ull *mx = maxes + 3 * (int64_t)gid[v];
+        ld = logf(1.f + (float)mx[0]);
+        lh = logf(1.f + (float)mx[1]);
+        m0 = mx[2] ? (float)mx[2] : 1.f;
+      }
+      const float deg = (float)(off[v + 1] - off[v]);
+      f0 = ld > 0.f ? logf(1.f + deg) / ld : 0.f;
+      f1 = lh > 0.f ? logf(1.f + (float)hop2[v]) / lh : 0.f;
+      f2 = (float)(d0[v] < 0 ? 0 : d0[v]) / m0;
+      f3 = deg > 0.f ? (float)outw[v] / deg : 0.f;
+    }
+  };
+  const int64_t tstride = (int64_t)gridDim.x * MLP_TILE;
+  if (tid >= MLP_TILE) features((int64_t)blockIdx.x * MLP_TILE);
+  uint32_t parity = 0;
+  bool issued = false;  // an MMA group not yet waited for (thread 0's view; all threads wait below)
+  for (int64_t t0 = (int64_t)blockIdx.x * MLP_TILE; t0 < n; t0 += tstride) {
+    if (tid >= MLP_TILE) {
+      F[tid - MLP_TILE][0] = f0;
+      F[tid - MLP_TILE][1] = f1;
+      F[tid - MLP_TILE][2] = f2;
+      F[tid - MLP_TILE][3] = f3;
+    }
+    __syncthreads();  // F ready; the previous tile's accumulator read (the barrier at the loop's end)
+    // layer 1 (4 -> 64, ReLU) into the A parts: thread (v = tid % 128, half = tid / 128) takes hidden units
+    // 32 half .. 32 half + 31, four 8-unit K groups
+    {
+      const int v = tid & (MLP_TILE - 1), half = tid >> 7;
+#pragma unroll
+      for (int gq = 0; gq < 4; gq++) {
+        const int g = 4 * half + gq;
+        float h[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int o = 8 * g + i;
+          float acc = b1[o];
+#pragma unroll
+          for (int f = 0; f < MLP_IN; f++) acc = fmaf(W1[o][f], F[v][f], acc);
+          h[i] = acc > 0.f ? acc : 0.f;
+        }
+        store_split8(h, Ap + core_off(v, g), Ap + TM_A_PART + core_off(v, g), Ap + 2 * TM_A_PART + core_off(v, g));
+      }
+    }
+    fence_async_smem();  // the A stores, visible to the tensor core
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      const uint32_t a0 = smem_u32(Ap), b0 = smem_u32(Bp);
+      const int pa[6] = {0, 0, 1, 0, 2, 1}, pb[6] = {0, 1, 0, 2, 0, 1};
+#pragma unroll
+      for (int ks = 0; ks < MLP_H / 16; ks++)
+#pragma unroll
+        for (int q = 0; q < 6; q++)
+          mma_bf16(tmem, smem_desc(a0 + pa[q] * TM_A_PART + ks * 2 * CORE_LBO),
+                   smem_desc(b0 + pb[q] * TM_B_PART + ks * 2 * CORE_LBO), TM_IDESC, (ks > 0 || q > 0) ? 1u : 0u);
+      mma_commit(smem_u32(&s_bar));
+    }
+    issued = true;
+    if (tid >= MLP_TILE && t0 + tstride < n) features(t0 + tstride);
+    const bool ok = mbar_wait(smem_u32(&s_bar), parity, timeout_ns, nullptr);
+    parity ^= 1u;
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicCAS(err, 0, PHDE_ERR_TIMEOUT);
+      s_fail = 1;
+      break;
+    }
+    issued = false;
+    tc_fence_after();
+    // output unit: lane l of warp w < 4 holds vertex 32 w + l's 64 layer-2 sums
+    int bin = -1;
+    if (warp < 4) {
+      float sum = 0.f;
+#pragma unroll
+      for (int c0 = 0; c0 < MLP_H; c0 += 16) {
+        float vv[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, vv);
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const float a = vv[i] + b2[c0 + i];
+          sum = fmaf(w3[c0 + i], a > 0.f ? a : 0.f, sum);
+        }
+      }
+      const int64_t v = t0 + 32 * warp + lane;
+      if (v < n) {
+        const float pr = 1.f / (1.f + expf(-(s_b3 + sum)));
+        score[v] = pr;
+        if (nbins > 0) {
+          bin = (int)(pr * nbins);
+          bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+        }
+      }
+      const unsigned same = __match_any_sync(PHDE_FULL_MASK, bin);
+      if (bin >= 0 && lane == __ffs(same) - 1) atomicAdd(s_hist + bin, (unsigned)__popc(same));
+    }
+    tc_fence_before();
+    __syncthreads();  // the accumulator and the A parts are free for the next tile
+  }
+  if (s_fail && issued) {  // a timed-out MMA group: wait once more (bounded) before the TMEM goes
+    mbar_wait(smem_u32(&s_bar), parity ^ 1u, timeout_ns, nullptr);
+  }
+  __syncthreads();
+  for (int i = tid; i < nbins; i += blockDim.x)
+    if (s_hist[i]) atomicAdd(hist + i, s_hist[i]);
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, MLP_H);
+  }
+}
+
 // The scoring grid: every CTA resident at once (a grid-stride loop over 128-vertex tiles gives each the same
 // share, and a second, partial wave of CTAs would double the time of the first).
 int mlp_grid(phde_ctx *ctx, int64_t n, size_t smem, int *grid) {
@@ -332,6 +512,33 @@ int mlp_grid(phde_ctx *ctx, int64_t n, size_t smem, int *grid) {
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_score_kernel, 256, smem));
   per_sm = std::max(per_sm, 1);
   *grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * per_sm));
+  return PHDE_OK;
+}
+
+// The scores of every vertex: the tensor-core kernel (PHDE_MLP_CUDA_CORES=1: the CUDA-core one).  Every CTA
+// resident at once (grid-stride over 128-vertex tiles).
+int launch_scores(phde_ctx *ctx, const int32_t *d_d0, const ull *hop2, const uint32_t *outw, const ull *maxes,
+                  int64_t n, const float *wts, float *score, unsigned *hist, int nbins, const int32_t *gid) {
+  if (getenv("PHDE_MLP_CUDA_CORES")) {
+    const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE + sizeof(unsigned) * nbins;
+    PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
+    int gm = 0;
+    if (int rc = mlp_grid(ctx, n, mlp_smem, &gm)) return rc;
+    mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts, score, hist,
+                                                         nbins, gid);
+    PHDE_LAUNCHED(ctx);
+    return PHDE_OK;
+  }
+  const size_t smem = TM_SMEM + sizeof(unsigned) * nbins;
+  PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_score_tc_kernel, TM_THREADS, smem));
+  per_sm = std::max(1, std::min(per_sm, 4));  // 64 TMEM columns each
+  const int grid =
+      (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * per_sm));
+  mlp_score_tc_kernel<<<grid, TM_THREADS, smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts, score,
+                                                               hist, nbins, gid, ctx->d_err, ctx->timeout_ns);
+  PHDE_LAUNCHED(ctx);
   return PHDE_OK;
 }
 
@@ -378,13 +585,8 @@ int phde_pivot_candidates(phde_ctx *ctx, const float *h_weights, int M, const in
   PHDE_LAUNCHED(ctx);
   feature_max_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, n, maxes);
   PHDE_LAUNCHED(ctx);
-  const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE + sizeof(unsigned) * nbins;
-  PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
-  int gm = 0;
-  if ((rc = mlp_grid(ctx, n, mlp_smem, &gm))) return rc;
-  mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, wts, score, hist,
-                                                       nbins, nullptr);
-  PHDE_LAUNCHED(ctx);
+  PHDE_CK(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+  if ((rc = launch_scores(ctx, d_d0, hop2, outw, maxes, n, wts, score, hist, nbins, nullptr))) return rc;
   std::vector<unsigned> hh(nbins);
   PHDE_CK(ctx, cudaMemcpyAsync(hh.data(), hist, sizeof(unsigned) * nbins, cudaMemcpyDeviceToHost, ctx->stream));
   PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -470,13 +672,7 @@ int phde_batch_scores(phde_ctx *ctx, const float *d_weights, const int32_t *d_d0
   PHDE_LAUNCHED(ctx);
   feature_max_batched_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, d_d0, hop2, ctx->d_gid, n, maxes);
   PHDE_LAUNCHED(ctx);
-  const size_t mlp_smem = sizeof(float) * MLP_H * MLP_TILE;
-  PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem));
-  int gm = 0;
-  if (int rc2 = mlp_grid(ctx, n, mlp_smem, &gm)) return rc2;
-  mlp_score_kernel<<<gm, 256, mlp_smem, ctx->stream>>>(ctx->d_off, d_d0, hop2, outw, maxes, n, d_weights, score,
-                                                       nullptr, 0, ctx->d_gid);
-  PHDE_LAUNCHED(ctx);
+  if (int rc2 = launch_scores(ctx, d_d0, hop2, outw, maxes, n, d_weights, score, nullptr, 0, ctx->d_gid)) return rc2;
   *score_out = score;
   return PHDE_OK;
 }
