@@ -12,7 +12,8 @@
 //             stale output words of two levels back are cleared from their list.  The frontier of a
 //             sparse level is a (vertex, edge prefix) list that the previous level built (or that is
 //             rebuilt by one scan of the frontier words after a dense level), walked edge-balanced.
-// Light rows are pulled by groups of 8 lanes; rows above MS_HEAVY neighbours (R-MAT hubs) are cut into
+// In dense levels rows of at most MS_SMALL neighbours are pulled by one lane each (a tile's 32 rows by one warp),
+// the other light rows by groups of 8 lanes; rows above MS_HEAVY neighbours (R-MAT hubs) are cut into
 // chunks whose partial ORs are combined with atomicOr before the same finalisation.  OR is order-free, so
 // the result is deterministic.
 //
@@ -34,6 +35,7 @@ constexpr int64_t MS_HEAVY = 256;  // rows above this are cut into chunks (one w
 constexpr int64_t MS_CHUNK = 256;
 constexpr int MS_GROUP = 8;        // lanes per light row
 constexpr int MS_TILE_CHUNK = 4;   // dense levels: 32-vertex tiles a warp takes from the level counter at once
+constexpr int64_t MS_SMALL = 24;  // dense levels: rows up to this many neighbours are pulled by one lane each
 constexpr int GATHER_SMEM_COLS = 1024;  // columns whose sums of squares are kept per CTA
 
 struct MsArgs {
@@ -252,6 +254,63 @@ __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full
     } else if (ms_group_finalise<W>(a, v, acc, s, fnext, L, gl) && gl == 0) {
       newbits = true;
       atomicOr(fbm_next + (v >> 5), 1u << (v & 31));
+    }
+  }
+}
+
+// One light row v (neighbours e0 .. e1, at most MS_SMALL) pulled by one lane: the gathers four at a time, then
+// the finalisation (record nibbles by L2 reductions).  newbits: v got new bits; finished: v is saturated and
+// not in this level's frontier (its `done` bit may be set).
+template <int W>
+__device__ __forceinline__ void ms_pull_light(const MsArgs &a, const ull (&full)[W], const ull *fcur, ull *fnext,
+                                              const uint32_t *fbm_cur, bool use_bm, int32_t L, int64_t v, int64_t e0,
+                                              int64_t e1, bool &newbits, bool &finished) {
+  newbits = finished = false;
+  ull s[W];
+  ld_words<W>(a.seen + v * W, s);
+  bool sat = true;
+#pragma unroll
+  for (int w = 0; w < W; w++) sat &= (s[w] == full[w]);
+  if (sat) {
+#pragma unroll
+    for (int w = 0; w < W; w++) fnext[v * W + w] = 0ull;
+    finished = !fbit(fbm_cur, (uint32_t)v);
+    return;
+  }
+  const uint64_t stream = l2_policy_evict_first(), keep = l2_policy_evict_last();
+  ull acc[W];
+#pragma unroll
+  for (int w = 0; w < W; w++) acc[w] = 0ull;
+  for (int64_t e = e0; e < e1; e += 4) {
+    uint32_t u[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) u[j] = e + j < e1 ? ld_nc_hint(a.adj + e + j, stream) : 0u;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (e + j < e1 && (!use_bm || fbit(fbm_cur, u[j]))) {
+        ull x[W];
+        ld_front<W>(fcur + (int64_t)u[j] * W, x, keep);
+#pragma unroll
+        for (int w = 0; w < W; w++) acc[w] |= x[w];
+      }
+    }
+  }
+  const unsigned val = (unsigned)(L + 2);  // level L+1, stored +1
+  ull *row = a.R ? (ull *)(a.R + v * a.RW + a.col0) : nullptr;
+  const uint64_t rec = l2_policy_evict_first();
+#pragma unroll
+  for (int w = 0; w < W; w++) {
+    const ull nw = acc[w] & ~s[w];
+    fnext[v * W + w] = nw;
+    if (nw) {
+      newbits = true;
+      a.seen[v * W + w] = s[w] | nw;
+      if (row)
+        for (ull m = nw; m;) {
+          const int gi = (__ffsll((long long)m) - 1) >> 2;
+          red_or_hint(row + 16 * w + gi, nibble_lanes((unsigned)(nw >> (4 * gi)) & 15u, val), rec);
+          m &= ~(15ull << (4 * gi));
+        }
     }
   }
 }
@@ -509,6 +568,26 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         // one read of the tile's word, broadcast: the warp sets bits of it below
         unsigned todo = __shfl_sync(PHDE_FULL_MASK, lane == 0 ? __ldcg(a.done + t) : 0u, 0);
         todo = ~todo & valid;
+        // light rows (at most MS_SMALL neighbours): lane i pulls vertex v0 + i alone; the tile's frontier-bitmap
+        // and `done` bits go out as one atomic each
+        if (todo) {
+          const int64_t v = v0 + lane;
+          const bool mine = (todo >> lane) & 1u;
+          int64_t e0 = 0, e1 = 0;
+          if (mine) {
+            e0 = a.off[v];
+            e1 = a.off[v + 1];
+          }
+          const bool light = mine && e1 - e0 <= MS_SMALL;
+          const unsigned lmask = __ballot_sync(PHDE_FULL_MASK, light);
+          todo &= ~lmask;
+          bool nb = false, fin = false;
+          if (light) ms_pull_light<W>(a, full, fcur, fnext, fbm_cur, use_bm, L, v, e0, e1, nb, fin);
+          const unsigned nbm = __ballot_sync(PHDE_FULL_MASK, nb), finm = __ballot_sync(PHDE_FULL_MASK, fin);
+          if (lane == 0 && nbm) atomicOr(fbm_next + t, nbm);
+          if (lane == 0 && finm) atomicOr(a.done + t, finm);
+          if (nb) my_stat += (1ull << 32) | (ull)(e1 - e0);
+        }
         while (todo) {
           // the grp-th set bit of todo (none: act = false)
           unsigned rest = todo;
