@@ -70,6 +70,7 @@ struct phde_ctx {
   bool want_rq = false;            // compute the Rayleigh quotients of every layout (the checked strategy's reference)
   long long ms_plan_epoch = -1;  // multi-source BFS heavy-row plan
   int64_t ms_nheavy = 0, ms_nchunks = 0;
+  bool ms_local = false;  // index-local numbering: the multi-source BFS stages frontier windows
 
   // device control block for persistent kernels: barrier + error word
   GridSync *d_sync = nullptr;

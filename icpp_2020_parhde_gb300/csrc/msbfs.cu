@@ -35,7 +35,12 @@ constexpr int64_t MS_HEAVY = 256;  // rows above this are cut into chunks (one w
 constexpr int64_t MS_CHUNK = 256;
 constexpr int MS_GROUP = 8;        // lanes per light row
 constexpr int MS_TILE_CHUNK = 4;   // dense levels: 32-vertex tiles a warp takes from the level counter at once
-constexpr int64_t MS_SMALL = 24;  // dense levels: rows up to this many neighbours are pulled by one lane each
+constexpr int64_t MS_SMALL = 40;  // dense levels: rows up to this many neighbours are pulled by one lane each
+// dense levels on index-local graphs (mesh-like numberings): a CTA takes MS_WIN consecutive vertices and
+// stages the frontier words of those and of MS_WIN on each side in shared memory, where most of their
+// neighbours' words are then found
+constexpr int MS_WIN = 1024;
+constexpr int MS_WIN_SAMPLE = 16;  // the locality estimate reads the rows of every 16th vertex
 constexpr int GATHER_SMEM_COLS = 1024;  // columns whose sums of squares are kept per CTA
 
 struct MsArgs {
@@ -86,6 +91,7 @@ struct MsArgs {
   // small frontier skip most gathers.  Level L reads fbm[L % 3], sets fbm[(L+1) % 3] and clears fbm[(L+2) % 3]
   // (read during level L-1, written again during level L+1).
   uint32_t *fbm[3];
+  int win;                    // dense levels stage frontier windows in shared memory (MS_WIN)
   GridSync *gs;
   int *err;
   uint64_t timeout_ns;
@@ -122,6 +128,25 @@ __device__ __forceinline__ void ld_words(const ull *p, ull (&x)[W]) {
 #pragma unroll
     for (int w = 0; w < W; w++) x[w] = __ldcg(p + w);
   }
+}
+
+// A neighbour's frontier words: from the shared-memory window when u lies in it (WIN), else through L2 --
+// after the frontier-bitmap test when use_bm (the window holds zero words for vertices outside the frontier).
+// Returns false when the words are known to be zero (not read).
+template <int W, bool WIN>
+__device__ __forceinline__ bool gather_front(const ull *fcur, const ull *swin, int64_t wlo, const uint32_t *fbm_cur,
+                                             bool use_bm, uint32_t u, ull (&x)[W], uint64_t keep) {
+  if constexpr (WIN) {
+    const uint64_t d = (uint64_t)((int64_t)u - wlo);
+    if (d < (uint64_t)(3 * MS_WIN)) {
+#pragma unroll
+      for (int w = 0; w < W; w++) x[w] = swin[d * W + w];
+      return true;
+    }
+  }
+  if (use_bm && !((__ldcg(fbm_cur + (u >> 5)) >> (u & 31)) & 1u)) return false;
+  ld_front<W>(fcur + (int64_t)u * W, x, keep);
+  return true;
 }
 
 // Record word for 4 sources: the 4 bits of `nib` select which of the four 16-bit lanes get value `val`.
@@ -192,11 +217,11 @@ __device__ __forceinline__ bool ms_thread_finalise(const MsArgs &a, int64_t v, c
 // group has no vertex pass act = false.  Returns through `newbits` whether v got new bits (group leader).
 __device__ __forceinline__ bool fbit(const uint32_t *bm, uint32_t u) { return (__ldcg(bm + (u >> 5)) >> (u & 31)) & 1u; }
 
-template <int W>
+template <int W, bool WIN = false>
 __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full)[W], const ull *fcur, ull *fnext,
                                                const uint32_t *fbm_cur, uint32_t *fbm_next, bool use_bm, int32_t L,
                                                int64_t v, bool act, int gl, bool mark_done, bool &newbits,
-                                               uint32_t &deg) {
+                                               uint32_t &deg, const ull *swin = nullptr, int64_t wlo = 0) {
   newbits = false;
   int64_t e0 = 0, e1 = 0;
   deg = 0;
@@ -225,15 +250,13 @@ __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full
       const uint32_t u0 = ld_nc_hint(a.adj + e, stream);
       const uint32_t u1 = e2 < e1 ? ld_nc_hint(a.adj + e2, stream) : u0;
       // gather only the neighbours in this level's frontier (their bitmap bit): an empty word adds nothing
-      if (!use_bm || fbit(fbm_cur, u0)) {
-        ull x0[W];
-        ld_front<W>(fcur + (int64_t)u0 * W, x0, keep);
+      ull x0[W];
+      if (gather_front<W, WIN>(fcur, swin, wlo, fbm_cur, use_bm, u0, x0, keep)) {
 #pragma unroll
         for (int w = 0; w < W; w++) acc[w] |= x0[w];
       }
-      if (e2 < e1 && (!use_bm || fbit(fbm_cur, u1))) {
-        ull x1[W];
-        ld_front<W>(fcur + (int64_t)u1 * W, x1, keep);
+      ull x1[W];
+      if (e2 < e1 && gather_front<W, WIN>(fcur, swin, wlo, fbm_cur, use_bm, u1, x1, keep)) {
 #pragma unroll
         for (int w = 0; w < W; w++) acc[w] |= x1[w];
       }
@@ -261,10 +284,11 @@ __device__ __forceinline__ void ms_pull_vertex(const MsArgs &a, const ull (&full
 // One light row v (neighbours e0 .. e1, at most MS_SMALL) pulled by one lane: the gathers four at a time, then
 // the finalisation (record nibbles by L2 reductions).  newbits: v got new bits; finished: v is saturated and
 // not in this level's frontier (its `done` bit may be set).
-template <int W>
+template <int W, bool WIN>
 __device__ __forceinline__ void ms_pull_light(const MsArgs &a, const ull (&full)[W], const ull *fcur, ull *fnext,
                                               const uint32_t *fbm_cur, bool use_bm, int32_t L, int64_t v, int64_t e0,
-                                              int64_t e1, bool &newbits, bool &finished) {
+                                              int64_t e1, bool &newbits, bool &finished, const ull *swin,
+                                              int64_t wlo) {
   newbits = finished = false;
   ull s[W];
   ld_words<W>(a.seen + v * W, s);
@@ -287,9 +311,8 @@ __device__ __forceinline__ void ms_pull_light(const MsArgs &a, const ull (&full)
     for (int j = 0; j < 4; j++) u[j] = e + j < e1 ? ld_nc_hint(a.adj + e + j, stream) : 0u;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      if (e + j < e1 && (!use_bm || fbit(fbm_cur, u[j]))) {
-        ull x[W];
-        ld_front<W>(fcur + (int64_t)u[j] * W, x, keep);
+      ull x[W];
+      if (e + j < e1 && gather_front<W, WIN>(fcur, swin, wlo, fbm_cur, use_bm, u[j], x, keep)) {
 #pragma unroll
         for (int w = 0; w < W; w++) acc[w] |= x[w];
       }
@@ -315,8 +338,56 @@ __device__ __forceinline__ void ms_pull_light(const MsArgs &a, const ull (&full)
   }
 }
 
+// One 32-vertex tile t of a dense level, by one warp: the unfinished vertices (the tile's `done` word); rows of
+// at most MS_SMALL neighbours by their own lane (the tile's frontier-bitmap and `done` bits out as one atomic
+// each), the other light rows by the warp's four 8-lane groups in turn.  WIN: neighbours' words from the
+// shared-memory window starting at vertex wlo where they lie in it.
+template <int W, bool WIN>
+__device__ __forceinline__ void ms_dense_tile(const MsArgs &a, const ull (&full)[W], const ull *fcur, ull *fnext,
+                                              const uint32_t *fbm_cur, uint32_t *fbm_next, bool use_bm, int32_t L,
+                                              int64_t t, const ull *swin, int64_t wlo, ull &my_stat) {
+  const int64_t n = a.n;
+  const int lane = threadIdx.x & 31, gl = lane & (MS_GROUP - 1), grp = lane / MS_GROUP;
+  const int64_t v0 = t * 32;
+  const unsigned valid = n - v0 >= 32 ? 0xffffffffu : ((1u << (n - v0)) - 1u);
+  // one read of the tile's word, broadcast: the warp sets bits of it below
+  unsigned todo = __shfl_sync(PHDE_FULL_MASK, lane == 0 ? __ldcg(a.done + t) : 0u, 0);
+  todo = ~todo & valid;
+  if (todo) {
+    const int64_t v = v0 + lane;
+    const bool mine = (todo >> lane) & 1u;
+    int64_t e0 = 0, e1 = 0;
+    if (mine) {
+      e0 = a.off[v];
+      e1 = a.off[v + 1];
+    }
+    const bool light = mine && e1 - e0 <= MS_SMALL;
+    const unsigned lmask = __ballot_sync(PHDE_FULL_MASK, light);
+    todo &= ~lmask;
+    bool nb = false, fin = false;
+    if (light) ms_pull_light<W, WIN>(a, full, fcur, fnext, fbm_cur, use_bm, L, v, e0, e1, nb, fin, swin, wlo);
+    const unsigned nbm = __ballot_sync(PHDE_FULL_MASK, nb), finm = __ballot_sync(PHDE_FULL_MASK, fin);
+    if (lane == 0 && nbm) atomicOr(fbm_next + t, nbm);
+    if (lane == 0 && finm) atomicOr(a.done + t, finm);
+    if (nb) my_stat += (1ull << 32) | (ull)(e1 - e0);
+  }
+  while (todo) {
+    // the grp-th set bit of todo (none: act = false)
+    unsigned rest = todo;
+    for (int j = 0; j < grp && rest; j++) rest &= rest - 1u;
+    const bool act = rest != 0u;
+    const int64_t v = v0 + (act ? __ffs(rest) - 1 : 0);
+    bool nb;
+    uint32_t dv;
+    ms_pull_vertex<W, WIN>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, v, act, gl, true, nb, dv, swin, wlo);
+    if (nb) my_stat += (1ull << 32) | (ull)dv;
+    for (int j = 0; j < 32 / MS_GROUP && todo; j++) todo &= todo - 1u;
+  }
+}
+
 template <int W>
 __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
+  extern __shared__ __align__(16) ull ms_dyn[];  // the frontier window of index-local dense levels (a.win)
   const int64_t n = a.n;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gts = (int64_t)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31, gl = lane & (MS_GROUP - 1), grp = lane / MS_GROUP;
@@ -367,6 +438,7 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
   }
   __shared__ PushScratch psc;
   __shared__ ull s_stat;
+  __shared__ unsigned s_tile;
   bool built_f = a.period == 0, built_z = true;  // lists of levels L-1 and L-2 exist (sparse levels build them)
   if (!grid_sync(a.gs, a.err, a.timeout_ns)) return;
   int32_t L = 0;
@@ -549,56 +621,55 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
         }
       }
     } else {
-      // light rows, 32-vertex tiles per warp: one load of the done bitmap skips finished vertices; the
-      // unfinished ones go to the warp's four 8-lane groups in turn.  Warps take MS_TILE_CHUNK tiles at a time
-      // from a level counter, so warps that meet heavy neighbourhoods do not hold the level's end back.
+      // light rows, 32-vertex tiles per warp: one load of the done bitmap skips finished vertices (ms_dense_tile)
       const int64_t ntiles = (n + 31) / 32;
       unsigned *tc = a.tctr + (L & 3);
-      int64_t t = 0, tend = 0;
-      for (;; t++) {
-        if (t >= tend) {
-          unsigned tb = 0;
-          if (lane == 0) tb = atomicAdd(tc, (unsigned)MS_TILE_CHUNK);
-          t = (int64_t)__shfl_sync(PHDE_FULL_MASK, tb, 0);
-          if (t >= ntiles) break;
-          tend = min(t + MS_TILE_CHUNK, ntiles);
-        }
-        const int64_t v0 = t * 32;
-        const unsigned valid = n - v0 >= 32 ? 0xffffffffu : ((1u << (n - v0)) - 1u);
-        // one read of the tile's word, broadcast: the warp sets bits of it below
-        unsigned todo = __shfl_sync(PHDE_FULL_MASK, lane == 0 ? __ldcg(a.done + t) : 0u, 0);
-        todo = ~todo & valid;
-        // light rows (at most MS_SMALL neighbours): lane i pulls vertex v0 + i alone; the tile's frontier-bitmap
-        // and `done` bits go out as one atomic each
-        if (todo) {
-          const int64_t v = v0 + lane;
-          const bool mine = (todo >> lane) & 1u;
-          int64_t e0 = 0, e1 = 0;
-          if (mine) {
-            e0 = a.off[v];
-            e1 = a.off[v + 1];
+      if (a.win) {
+        // index-local graph: the CTA takes MS_WIN vertices at a time from the level counter, stages the frontier
+        // words of [vs - MS_WIN, vs + 2 MS_WIN) and its warps work through the tiles with that window
+        const int64_t nst = (n + MS_WIN - 1) / MS_WIN;
+        const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        for (;;) {
+          __syncthreads();  // the previous window is consumed and s_tile read
+          if (threadIdx.x == 0) s_tile = atomicAdd(tc, 1u);
+          __syncthreads();
+          const int64_t st = s_tile;
+          if (st >= nst) break;  // uniform
+          const int64_t vs = st * MS_WIN, wlo = vs - MS_WIN;
+          const int64_t t0 = vs / 32, t1 = min(t0 + MS_WIN / 32, ntiles);
+          bool any = false;  // an unfinished vertex in the super-tile (else no staging)
+          for (int64_t tt = t0 + threadIdx.x; tt < t1; tt += blockDim.x) {
+            const int64_t b0 = tt * 32;
+            const unsigned valid = n - b0 >= 32 ? 0xffffffffu : ((1u << (n - b0)) - 1u);
+            any |= (~__ldcg(a.done + tt) & valid) != 0u;
           }
-          const bool light = mine && e1 - e0 <= MS_SMALL;
-          const unsigned lmask = __ballot_sync(PHDE_FULL_MASK, light);
-          todo &= ~lmask;
-          bool nb = false, fin = false;
-          if (light) ms_pull_light<W>(a, full, fcur, fnext, fbm_cur, use_bm, L, v, e0, e1, nb, fin);
-          const unsigned nbm = __ballot_sync(PHDE_FULL_MASK, nb), finm = __ballot_sync(PHDE_FULL_MASK, fin);
-          if (lane == 0 && nbm) atomicOr(fbm_next + t, nbm);
-          if (lane == 0 && finm) atomicOr(a.done + t, finm);
-          if (nb) my_stat += (1ull << 32) | (ull)(e1 - e0);
+          if (!__syncthreads_or(any)) continue;
+          for (int64_t j = threadIdx.x; j < 3 * MS_WIN; j += blockDim.x) {
+            const int64_t gv = wlo + j;
+            ull x[W];
+#pragma unroll
+            for (int w = 0; w < W; w++) x[w] = 0ull;
+            if (gv >= 0 && gv < n) ld_words<W>(fcur + gv * W, x);
+#pragma unroll
+            for (int w = 0; w < W; w++) ms_dyn[j * W + w] = x[w];
+          }
+          __syncthreads();
+          for (int64_t tt = t0 + warp; tt < t1; tt += nwarps)
+            ms_dense_tile<W, true>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, tt, ms_dyn, wlo, my_stat);
         }
-        while (todo) {
-          // the grp-th set bit of todo (none: act = false)
-          unsigned rest = todo;
-          for (int j = 0; j < grp && rest; j++) rest &= rest - 1u;
-          const bool act = rest != 0u;
-          const int64_t v = v0 + (act ? __ffs(rest) - 1 : 0);
-          bool nb;
-          uint32_t dv;
-          ms_pull_vertex<W>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, v, act, gl, true, nb, dv);
-          if (nb) my_stat += (1ull << 32) | (ull)dv;
-          for (int j = 0; j < 32 / MS_GROUP && todo; j++) todo &= todo - 1u;
+      } else {
+        // warps take MS_TILE_CHUNK tiles at a time from a level counter, so warps that meet heavy
+        // neighbourhoods do not hold the level's end back
+        int64_t t = 0, tend = 0;
+        for (;; t++) {
+          if (t >= tend) {
+            unsigned tb = 0;
+            if (lane == 0) tb = atomicAdd(tc, (unsigned)MS_TILE_CHUNK);
+            t = (int64_t)__shfl_sync(PHDE_FULL_MASK, tb, 0);
+            if (t >= ntiles) break;
+            tend = min(t + MS_TILE_CHUNK, ntiles);
+          }
+          ms_dense_tile<W, false>(a, full, fcur, fnext, fbm_cur, fbm_next, use_bm, L, t, nullptr, 0, my_stat);
         }
       }
     }
@@ -675,10 +746,19 @@ __global__ void __launch_bounds__(MS_THREADS, 2) msbfs_kernel(MsArgs a) {
   if (gt == 0) *a.levels_out = L + 1;
 }
 
-__global__ void ms_heavy_plan_kernel(const int64_t *off, int64_t n, int64_t *heavy_rows, int64_t *chunk_row,
-                                     int64_t *chunk_e0, ull *counts) {
+// The heavy-row plan, and the graph's index locality: over the rows of every MS_WIN_SAMPLE-th vertex (their
+// first 64 neighbours), the neighbours within MS_WIN of the row's index (counts[2]) against all (counts[3]).
+__global__ void ms_heavy_plan_kernel(const int64_t *off, const uint32_t *adj, int64_t n, int64_t *heavy_rows,
+                                     int64_t *chunk_row, int64_t *chunk_e0, ull *counts) {
+  ull near = 0, seen = 0;
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e0 = off[v], deg = off[v + 1] - e0;
+    if (v % MS_WIN_SAMPLE == 0)
+      for (int64_t e = e0; e < e0 + min(deg, (int64_t)64); e++) {
+        const int64_t d = (int64_t)adj[e] - v;
+        near += (d >= -MS_WIN && d <= MS_WIN) ? 1ull : 0ull;
+        seen++;
+      }
     if (deg <= MS_HEAVY) continue;
     heavy_rows[atomicAdd(counts, 1ull)] = v;
     const int64_t nch = (deg + MS_CHUNK - 1) / MS_CHUNK;
@@ -687,6 +767,12 @@ __global__ void ms_heavy_plan_kernel(const int64_t *off, int64_t n, int64_t *hea
       chunk_row[base + c] = v;
       chunk_e0[base + c] = e0 + c * MS_CHUNK;
     }
+  }
+  near = warp_sum(near);
+  seen = warp_sum(seen);
+  if ((threadIdx.x & 31) == 0 && seen) {
+    atomicAdd(counts + 2, near);
+    atomicAdd(counts + 3, seen);
   }
 }
 
@@ -796,18 +882,22 @@ int phde_heavy_chunks(phde_ctx *ctx, const int64_t **chunk_row, const int64_t **
   int64_t *hrows = (int64_t *)phde_buf(ctx, "ms.hrows", sizeof(int64_t) * cap_h);
   int64_t *crow = (int64_t *)phde_buf(ctx, "ms.crow", sizeof(int64_t) * cap_c);
   int64_t *ce0 = (int64_t *)phde_buf(ctx, "ms.ce0", sizeof(int64_t) * cap_c);
-  ull *counts = (ull *)phde_buf(ctx, "ms.counts", sizeof(ull) * 2);
+  ull *counts = (ull *)phde_buf(ctx, "ms.counts", sizeof(ull) * 4);
   if (!hrows || !crow || !ce0 || !counts) return PHDE_ERR_OOM;
   if (ctx->ms_plan_epoch != ctx->graph_epoch) {
-    PHDE_CK(ctx, cudaMemsetAsync(counts, 0, sizeof(ull) * 2, ctx->stream));
+    PHDE_CK(ctx, cudaMemsetAsync(counts, 0, sizeof(ull) * 4, ctx->stream));
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->nsm * 8));
-    ms_heavy_plan_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, n, hrows, crow, ce0, counts);
+    ms_heavy_plan_kernel<<<g, 256, 0, ctx->stream>>>(ctx->d_off, ctx->d_adj, n, hrows, crow, ce0, counts);
     PHDE_LAUNCHED(ctx);
-    ull h[2];
+    ull h[4];
     PHDE_CK(ctx, cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->ms_nheavy = (int64_t)h[0];
     ctx->ms_nchunks = (int64_t)h[1];
+    // index-local when at least 90 % of the sampled neighbours lie within MS_WIN: 2-D RGGs and meshes numbered
+    // by cell (100 %; the window pays there), not 3-D RGGs (63 %: the staging costs more than the gathers it
+    // saves) nor R-MAT (a few per cent)
+    ctx->ms_local = h[3] > 0 && 10 * h[2] >= 9 * h[3];
     ctx->ms_plan_epoch = ctx->graph_epoch;
   }
   *chunk_row = crow;
@@ -873,8 +963,13 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
                    : W == 2 ? (const void *)msbfs_kernel<2>
                    : W == 3 ? (const void *)msbfs_kernel<3>
                             : (const void *)msbfs_kernel<4>;
+    // dense levels of index-local graphs stage frontier windows (PHDE_MSBFS_WINDOW=0 or 1 picks outright)
+    const char *we = getenv("PHDE_MSBFS_WINDOW");
+    const bool win = we ? atoi(we) != 0 : ctx->ms_local;
+    const size_t dyn = win ? sizeof(ull) * 3 * MS_WIN * W : 0;
+    PHDE_CK(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     int per_sm = 0;
-    PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, MS_THREADS, 0));
+    PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, MS_THREADS, dyn));
     if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "msbfs kernel cannot be resident");
     per_sm = std::min(per_sm, 4);
     PHDE_CK(ctx, cudaMemsetAsync(seen, 0, sizeof(ull) * n * W, ctx->stream));
@@ -925,13 +1020,14 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
     a.trace_cap = trace_cap;
     a.done = bms;
     for (int i = 0; i < 3; i++) a.fbm[i] = fbm + (int64_t)i * nw32;
+    a.win = win ? 1 : 0;
     a.gs = ctx->d_sync;
     a.err = ctx->d_err;
     a.timeout_ns = ctx->timeout_ns;
     void *args[] = {&a};
     const double before = ctx->kernel_ms;
     cudaEventRecord(ctx->kev[0], ctx->stream);
-    PHDE_CK(ctx, cudaLaunchCooperativeKernel(fn, dim3(ctx->nsm * per_sm), dim3(MS_THREADS), args, 0, ctx->stream));
+    PHDE_CK(ctx, cudaLaunchCooperativeKernel(fn, dim3(ctx->nsm * per_sm), dim3(MS_THREADS), args, dyn, ctx->stream));
     PHDE_LAUNCHED(ctx);
     cudaEventRecord(ctx->kev[1], ctx->stream);
     ctx->kev_pending = true;

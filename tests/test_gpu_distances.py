@@ -156,6 +156,25 @@ def test_multi_source_bfs_bit_exact(gpu_ctx, nsrc):
     assert np.array_equal(d[:, 0], d[:, 1])
 
 
+@pytest.mark.parametrize("window", ["0", "1"])
+@pytest.mark.parametrize("make,nsrc", [
+    (lambda: graphs.rgg(40000, dim=3, avg_degree=12, seed=3), 256),
+    (lambda: graphs.rgg(30000, dim=2, avg_degree=8, seed=5), 100),
+    (lambda: graphs.rmat(14, seed=2), 256),
+], ids=["rgg3d-256", "rgg2d-100", "rmat14-256"])
+def test_multi_source_bfs_window_modes(gpu_ctx, monkeypatch, make, nsrc, window):
+    """Dense levels with and without the shared-memory frontier window (chosen by index locality; forced here
+    both ways, also on the R-MAT graph whose numbering is not local) give the one-source BFS columns."""
+    monkeypatch.setenv("PHDE_MSBFS_WINDOW", window)
+    g = make()
+    gpu_ctx.upload(g)
+    rng = np.random.default_rng(nsrc + 7)
+    src = rng.integers(0, g.n, size=nsrc)
+    d = gpu_ctx.distances(src)
+    for i in range(0, nsrc, max(1, nsrc // 9)):
+        assert np.array_equal(d[:, i], orc.bfs(g, int(src[i]))), i
+
+
 def test_multi_source_bfs_on_mesh_and_disconnected(gpu_ctx):
     g, rec = load_golden("mesh125")
     gpu_ctx.upload(g)
