@@ -39,6 +39,7 @@ constexpr int ZG_THREADS = 256;
 constexpr int ZG_ROWS = 32;   // rows per staged slab
 constexpr int LG_THREADS = 256;
 constexpr int LG_ITEMS = 64;  // rows / chunks per slab
+constexpr int64_t LG_LIGHT = 16;  // rows of at most this many neighbours are gathered by one lane group
 constexpr int CF_THREADS = 256;
 constexpr uint64_t B32 = 1ull << 32;
 constexpr uint64_t B31 = 1ull << 31;
@@ -942,7 +943,8 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
   extern __shared__ int lsm[];
   __shared__ ull s_bnd[LG_ITEMS];
   __shared__ int s_self[LG_ITEMS];
-  __shared__ int s_next;
+  __shared__ int s_list[LG_ITEMS];  // phase 2 items of the slab
+  __shared__ int s_next, s_nlist, s_lnext;
   int *zs = lsm, *rs = lsm + LG_ITEMS * SL;
   uint8_t *Zb = (uint8_t *)lsm;
   uint16_t *Sh = (uint16_t *)(Zb + LG_ITEMS * KP);
@@ -976,13 +978,99 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
   for (int64_t s = blockIdx.x; s < nslab; s += gridDim.x) {
     const int64_t u0 = s * LG_ITEMS;
     __syncthreads();  // previous slab consumed
-    if (threadIdx.x == 0) s_next = 0;
+    if (threadIdx.x == 0) s_next = s_nlist = s_lnext = 0;
     __syncthreads();
-    for (;;) {  // the warps take the slab's items one at a time
-      int slot = 0;
-      if (lane == 0) slot = atomicAdd(&s_next, 1);
-      slot = __shfl_sync(PHDE_FULL_MASK, slot, 0);
-      if (slot >= LG_ITEMS) break;
+    // phase 1: the warps take G of the slab's items at a time; a light row (at most LG_LIGHT neighbours) is
+    // done by its LPR-lane group alone (lane pi sums slice pi of the neighbours' rows, no cross-group
+    // reduction), as are the empty slots; the other items are listed for phase 2
+    for (;;) {
+      int sbase = 0;
+      if (lane == 0) sbase = atomicAdd(&s_next, G);
+      sbase = __shfl_sync(PHDE_FULL_MASK, sbase, 0);
+      if (sbase >= LG_ITEMS) break;
+      const int gslot = sbase + gi;  // LG_ITEMS is a multiple of G
+      const int64_t u = u0 + gslot;
+      int64_t row = -1, e0 = 0, e1 = 0;
+      bool listed = false;
+      if (u < a.n) {
+        e0 = a.off[u];
+        e1 = a.off[u + 1];
+        if (e1 - e0 <= LG_LIGHT)
+          row = u;
+        else if (e1 - e0 <= a.heavy)
+          listed = true;  // (heavier rows are done as chunks: their own slot stays empty)
+      } else if (u < items) {
+        listed = true;
+      }
+      unsigned zm = 0, rm = 0;
+      if (!listed) {
+        Sum16<T> nb;
+        nb.zero();
+        int selfc = 0;
+        uint4 own = make_uint4(0, 0, 0, 0);
+        if (row >= 0) {
+          const uint64_t keep = l2_policy_evict_last(), stream = l2_policy_evict_first();
+          for (int64_t e = e0; e < e1; e += 4) {  // four neighbour rows in flight per lane
+            int64_t vv[4];
+            uint4 x[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) vv[j] = e + j < e1 ? (int64_t)ld_nc_hint(a.adj + e + j, stream) : -1;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              x[j] = make_uint4(0, 0, 0, 0);
+              if (vv[j] > row) x[j] = ld_nc_hint16((const uint4 *)(Z + vv[j] * KP) + pi, keep);
+              selfc += vv[j] == row;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) nb.add(x[j]);
+          }
+          own = __ldg((const uint4 *)(Z + row * KP) + pi);
+        }
+        if constexpr (PK) {
+#pragma unroll
+          for (int c = 0; c < V; c++) {
+            const int col = pi * V + c;
+            const int z = slice_val<T>(own, c), sum = nb.get(c);
+            Zb[((gslot >> 2) * KP + col) * 4 + (gslot & 3)] = (uint8_t)z;
+            Sh[(((gslot >> 2) * 2 + ((gslot & 3) >> 1)) * KP + col) * 2 + (gslot & 1)] = (uint16_t)sum;
+            zm = max(zm, (unsigned)z);
+            rm = max(rm, (unsigned)sum);
+          }
+          if (pi == 0) s_self[gslot] = selfc;
+        } else {
+          int *zd = zs + gslot * SL + pi * V, *rd = rs + gslot * SL + pi * V;
+#pragma unroll
+          for (int c = 0; c < V; c += 2) {
+            const int z0 = slice_val<T>(own, c), z1 = slice_val<T>(own, c + 1);
+            const int r0 = 2 * nb.get(c) + selfc * z0, r1 = 2 * nb.get(c + 1) + selfc * z1;
+            *(int2 *)(zd + c) = make_int2(z0, z1);
+            *(int2 *)(rd + c) = make_int2(r0, r1);
+            zm = max(zm, (unsigned)max(z0, z1));
+            rm = max(rm, (unsigned)max(abs(r0), abs(r1)));
+          }
+        }
+      }
+#pragma unroll
+      for (int m = 1; m < LPR; m <<= 1) {  // the group's maxima
+        zm = max(zm, __shfl_xor_sync(PHDE_FULL_MASK, zm, m));
+        rm = max(rm, __shfl_xor_sync(PHDE_FULL_MASK, rm, m));
+      }
+      if (pi == 0) {
+        if (listed)
+          s_list[atomicAdd(&s_nlist, 1)] = gslot;
+        else
+          s_bnd[gslot] = (ull)zm * (ull)rm;
+      }
+    }
+    __syncthreads();
+    // phase 2: the listed items (longer rows, hub-row chunks), one at a time per warp, all lanes on one row
+    const int nlist = s_nlist;
+    for (;;) {
+      int li = 0;
+      if (lane == 0) li = atomicAdd(&s_lnext, 1);
+      li = __shfl_sync(PHDE_FULL_MASK, li, 0);
+      if (li >= nlist) break;
+      const int slot = s_list[li];
       const int64_t u = u0 + slot;
       int64_t row = -1, e0 = 0, e1 = 0;
       if (u < a.n) {
