@@ -946,8 +946,10 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
   __shared__ int s_list[LG_ITEMS];  // phase 2 items of the slab
   __shared__ int s_next, s_nlist, s_lnext;
   int *zs = lsm, *rs = lsm + LG_ITEMS * SL;
+  // Zb and Sh rows are ZR = KP + 4 words apart: the rows of a store instruction's items fall in different banks
+  constexpr int ZR = KP + 4;
   uint8_t *Zb = (uint8_t *)lsm;
-  uint16_t *Sh = (uint16_t *)(Zb + LG_ITEMS * KP);
+  uint16_t *Sh = (uint16_t *)(Zb + (LG_ITEMS / 4) * ZR * 4);
   const int lane = threadIdx.x & 31;
   const int gi = lane / LPR, pi = lane % LPR;  // lane group (neighbour) and slice within the row
   const T *Z = (const T *)a.Z;
@@ -1031,8 +1033,8 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
           for (int c = 0; c < V; c++) {
             const int col = pi * V + c;
             const int z = slice_val<T>(own, c), sum = nb.get(c);
-            Zb[((gslot >> 2) * KP + col) * 4 + (gslot & 3)] = (uint8_t)z;
-            Sh[(((gslot >> 2) * 2 + ((gslot & 3) >> 1)) * KP + col) * 2 + (gslot & 1)] = (uint16_t)sum;
+            Zb[((gslot >> 2) * ZR + col) * 4 + (gslot & 3)] = (uint8_t)z;
+            Sh[(((gslot >> 2) * 2 + ((gslot & 3) >> 1)) * ZR + col) * 2 + (gslot & 1)] = (uint16_t)sum;
             zm = max(zm, (unsigned)z);
             rm = max(rm, (unsigned)sum);
           }
@@ -1143,8 +1145,8 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
 #pragma unroll
           for (int c = 0; c < CPL; c++) {
             const int col = pi * V + gi * CPL + c;
-            Zb[((slot >> 2) * KP + col) * 4 + (slot & 3)] = (uint8_t)zi[c];
-            Sh[(((slot >> 2) * 2 + ((slot & 3) >> 1)) * KP + col) * 2 + (slot & 1)] = (uint16_t)r[c];
+            Zb[((slot >> 2) * ZR + col) * 4 + (slot & 3)] = (uint8_t)zi[c];
+            Sh[(((slot >> 2) * 2 + ((slot & 3) >> 1)) * ZR + col) * 2 + (slot & 1)] = (uint16_t)r[c];
           }
           if (lane == 0) s_self[slot] = selfc;
         } else {
@@ -1160,8 +1162,8 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
 #pragma unroll
           for (int c = 0; c < CPL; c++) {
             const int col = pi * V + gi * CPL + c;
-            Zb[((slot >> 2) * KP + col) * 4 + (slot & 3)] = 0;
-            Sh[(((slot >> 2) * 2 + ((slot & 3) >> 1)) * KP + col) * 2 + (slot & 1)] = 0;
+            Zb[((slot >> 2) * ZR + col) * 4 + (slot & 3)] = 0;
+            Sh[(((slot >> 2) * 2 + ((slot & 3) >> 1)) * ZR + col) * 2 + (slot & 1)] = 0;
           }
           if (lane == 0) s_self[slot] = 0;
         } else {
@@ -1193,9 +1195,9 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
         uint32_t zq[TS], alo[TS], ahi[TS];
 #pragma unroll
         for (int i = 0; i < TS; i += 4) {
-          const uint4 x = *(const uint4 *)(Zw + q4 * KP + TS * pb + i);
-          const uint4 y0 = *(const uint4 *)(Sw + (2 * q4) * KP + TS * qb + i);
-          const uint4 y1 = *(const uint4 *)(Sw + (2 * q4 + 1) * KP + TS * qb + i);
+          const uint4 x = *(const uint4 *)(Zw + q4 * ZR + TS * pb + i);
+          const uint4 y0 = *(const uint4 *)(Sw + (2 * q4) * ZR + TS * qb + i);
+          const uint4 y1 = *(const uint4 *)(Sw + (2 * q4 + 1) * ZR + TS * qb + i);
           zq[i] = x.x, zq[i + 1] = x.y, zq[i + 2] = x.z, zq[i + 3] = x.w;
           alo[i] = y0.x, alo[i + 1] = y0.y, alo[i + 2] = y0.z, alo[i + 3] = y0.w;
           ahi[i] = y1.x, ahi[i + 1] = y1.y, ahi[i + 2] = y1.z, ahi[i + 3] = y1.w;
@@ -1217,7 +1219,7 @@ __global__ void __launch_bounds__(LG_THREADS, KP == 64 ? 4 : 2) lgram_kernel(LgA
 #pragma unroll
           for (int j = 0; j < TS; j++) {
             const int p = TS * pb + i, q = TS * qb + j;
-            const ull v = (ull)c * Zb[((slot >> 2) * KP + p) * 4 + (slot & 3)] * Zb[((slot >> 2) * KP + q) * 4 + (slot & 3)];
+            const ull v = (ull)c * Zb[((slot >> 2) * ZR + p) * 4 + (slot & 3)] * Zb[((slot >> 2) * ZR + q) * 4 + (slot & 3)];
             if (v) atomicAdd(a.GL + (int64_t)p * KP + q, v);
           }
       }

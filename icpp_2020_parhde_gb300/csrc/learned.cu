@@ -531,6 +531,9 @@ int launch_scores(phde_ctx *ctx, const int32_t *d_d0, const ull *hop2, const uin
   }
   const size_t smem = TM_SMEM + sizeof(unsigned) * nbins;
   PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // all of the unified L1/shared storage as shared memory: two CTAs of ~92 KB per SM
+  PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    (int)cudaSharedmemCarveoutMaxShared));
   int per_sm = 0;
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_score_tc_kernel, TM_THREADS, smem));
   per_sm = std::max(1, std::min(per_sm, 4));  // 64 TMEM columns each

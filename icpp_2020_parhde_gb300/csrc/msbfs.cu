@@ -968,6 +968,10 @@ static int msbfs_run(phde_ctx *ctx, const int64_t *d_src, int nsrc, int nlist, i
     const bool win = we ? atoi(we) != 0 : ctx->ms_local;
     const size_t dyn = win ? sizeof(ull) * 3 * MS_WIN * W : 0;
     PHDE_CK(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    // with a window, all of the unified L1/shared storage as shared memory (two CTAs per SM); without, the
+    // default split
+    PHDE_CK(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      win ? (int)cudaSharedmemCarveoutMaxShared : (int)cudaSharedmemCarveoutDefault));
     int per_sm = 0;
     PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, MS_THREADS, dyn));
     if (per_sm < 1) return phde_fail(ctx, PHDE_ERR_CUDA, "msbfs kernel cannot be resident");
