@@ -531,11 +531,19 @@ int launch_scores(phde_ctx *ctx, const int32_t *d_d0, const ull *hop2, const uin
   }
   const size_t smem = TM_SMEM + sizeof(unsigned) * nbins;
   PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  // all of the unified L1/shared storage as shared memory: two CTAs of ~92 KB per SM
+  // all of the unified L1/shared storage as shared memory: two CTAs of ~96 KB per SM
   PHDE_CK(ctx, cudaFuncSetAttribute(mlp_score_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                     (int)cudaSharedmemCarveoutMaxShared));
   int per_sm = 0;
   PHDE_CK(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_score_tc_kernel, TM_THREADS, smem));
+  // the occupancy query can assume the default carveout: count the CTAs the shared memory holds as well (no
+  // CTA waits on another, so any grid is safe; the TMEM of four CTAs is half of an SM's)
+  cudaFuncAttributes fa;
+  int smem_sm = 0, resv = 0;
+  PHDE_CK(ctx, cudaFuncGetAttributes(&fa, mlp_score_tc_kernel));
+  PHDE_CK(ctx, cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device));
+  PHDE_CK(ctx, cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, ctx->device));
+  per_sm = std::max(per_sm, smem_sm / (int)(smem + fa.sharedSizeBytes + resv));
   per_sm = std::max(1, std::min(per_sm, 4));  // 64 TMEM columns each
   const int grid =
       (int)std::max<int64_t>(1, std::min<int64_t>((n + MLP_TILE - 1) / MLP_TILE, (int64_t)ctx->nsm * per_sm));
