@@ -189,11 +189,13 @@ class Context:
         self.n, self.nnz, self.weighted = sum(self.batch_sizes), sum(g.nnz for g in graphs), False
 
     def layout_batched(self, k: int = 10, c: int = 2, coords_out: np.ndarray | None = None,
-                       strategy: str = "Kcenters"):
-        """phde_layout_batched: (list of per-graph (n_b, c) coordinate arrays, stats dict).  strategy "Kcenters" or
-        "Learned"."""
-        o = _lib.LayoutOpts(_lib.ALGOS["ParHDE"], _lib.STRATEGIES[strategy], k, c, _lib.PRECISIONS["mixed"],
-                            _lib.EIGS["exact"], 1, 0)
+                       strategy: str = "Kcenters", precision: str = "mixed", eig: str = "exact",
+                       algo: str = "ParHDE"):
+        """phde_layout_batched: (list of per-graph (n_b, c) coordinate arrays, stats dict).  ParHDE with strategy
+        "Kcenters" or "Learned", precision "mixed", eig "exact", k <= 32 and c <= 4 run the fused batched
+        pipeline; other options lay the graphs out one by one with the single-graph pipeline."""
+        o = _lib.LayoutOpts(_lib.ALGOS[algo], _lib.STRATEGIES[strategy], k, c, _lib.PRECISIONS[precision],
+                            _lib.EIGS[eig], 1, 0)
         total = sum(self.batch_sizes)
         out = coords_out if coords_out is not None else np.empty(total * c, dtype=np.float64)
         st = _lib.LayoutStats()

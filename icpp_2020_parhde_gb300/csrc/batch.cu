@@ -17,6 +17,9 @@
 // Nothing between the Kcenters launch and the coordinate copy waits on the host, so after the first call
 // the whole sequence is captured once into a CUDA graph and replayed.  The segment length (rows per CTA) is
 // picked by a small autotuner: each candidate length is timed on the caller's own batch at the first call.
+// Options outside that pipeline (FP64 or exact arithmetic, k above 32, the power iteration, the other
+// algorithms) lay the graphs out one after another with the single-graph pipeline (layout_per_graph): each
+// graph's CSR is cut out of the union on the device and laid out as if uploaded alone.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -566,24 +569,128 @@ void build_segments(const std::vector<int64_t> &vb, int64_t seg_rows, std::vecto
 
 }  // namespace
 
+namespace {
+
+// Graph b's CSR cut out of the union with local vertex ids: off_b[i] = off[v0 + i] - off[v0], adj_b[e] =
+// adj[e0 + e] - v0.
+__global__ void batch_extract_kernel(const int64_t *off, const uint32_t *adj, int64_t v0, int64_t nb, int64_t e0,
+                                     int64_t mb, int64_t *off_b, uint32_t *adj_b) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nb; i += stride) off_b[i] = off[v0 + i] - e0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < mb; e += stride)
+    adj_b[e] = adj[e0 + e] - (uint32_t)v0;
+}
+
+// The context's view of the uploaded union, put back when a per-graph layout returns (also on errors).
+struct UnionView {
+  phde_ctx *ctx;
+  int64_t *off;
+  uint32_t *adj;
+  int32_t *w;
+  int64_t n, nnz;
+  int B;
+  bool weighted, want_rq;
+  explicit UnionView(phde_ctx *c)
+      : ctx(c), off(c->d_off), adj(c->d_adj), w(c->d_w), n(c->n), nnz(c->nnz), B(c->batch_B),
+        weighted(c->weighted), want_rq(c->want_rq) {}
+  ~UnionView() {
+    ctx->d_off = off;
+    ctx->d_adj = adj;
+    ctx->d_w = w;
+    ctx->n = n;
+    ctx->nnz = nnz;
+    ctx->batch_B = B;
+    ctx->weighted = weighted;
+    ctx->want_rq = want_rq;
+    ctx->graph_epoch++;  // a value no cache holds: every per-graph plan is rebuilt for the union
+  }
+};
+
+// Every graph of the batch through phde_layout in turn (options the fused pipeline does not cover).  The
+// coordinates land where phde_layout_batched puts them; the Rayleigh quotients of each graph's coordinates
+// (phde_batch_rayleigh) come from its layout; the stats add up the graphs' times, passes and launches.
+int layout_per_graph(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out, phde_layout_stats *stats) {
+  const int B = ctx->batch_B, c = o->c;
+  int64_t nmax = 0, mmax = 0;
+  for (int b = 0; b < B; b++) {
+    nmax = std::max(nmax, ctx->batch_vbase[b + 1] - ctx->batch_vbase[b]);
+    mmax = std::max(mmax, ctx->batch_ebase[b + 1] - ctx->batch_ebase[b]);
+  }
+  int64_t *off_b = (int64_t *)phde_buf(ctx, "pg.off", sizeof(int64_t) * (nmax + 1));
+  uint32_t *adj_b = (uint32_t *)phde_buf(ctx, "pg.adj", sizeof(uint32_t) * std::max<int64_t>(mmax, 1));
+  double *rq = (double *)phde_buf(ctx, "batch.rq", sizeof(double) * (size_t)B * c);
+  if (!off_b || !adj_b || !rq) return PHDE_ERR_OOM;
+  std::vector<double> h_rq((size_t)B * c, 0.0);
+  phde_layout_stats sum;
+  memset(&sum, 0, sizeof(sum));
+  const int64_t launches0 = ctx->launches;
+  {
+    UnionView keep(ctx);
+    for (int b = 0; b < B; b++) {
+      const int64_t v0 = ctx->batch_vbase[b], nb = ctx->batch_vbase[b + 1] - v0;
+      const int64_t e0 = ctx->batch_ebase[b], mb = ctx->batch_ebase[b + 1] - e0;
+      const int g = (int)std::max<int64_t>(1, std::min<int64_t>((std::max(nb + 1, mb) + 255) / 256, (int64_t)ctx->nsm * 8));
+      batch_extract_kernel<<<g, 256, 0, ctx->stream>>>(keep.off, keep.adj, v0, nb, e0, mb, off_b, adj_b);
+      PHDE_LAUNCHED(ctx);
+      ctx->d_off = off_b;
+      ctx->d_adj = adj_b;
+      ctx->d_w = nullptr;
+      ctx->weighted = false;
+      ctx->n = nb;
+      ctx->nnz = mb;
+      ctx->batch_B = 0;
+      ctx->want_rq = true;
+      ctx->graph_epoch++;  // the graph's own plans
+      phde_layout_stats sb;
+      const int rc = phde_layout(ctx, o, coords_out + (int64_t)c * v0, nullptr, nullptr, &sb);
+      if (rc) return phde_fail(ctx, rc, "phde_layout_batched: graph " + std::to_string(b) + ": " + ctx->err);
+      for (int j = 0; j < c && j < PHDE_RQ_MAX; j++) h_rq[(size_t)b * c + j] = sb.rayleigh[j];
+      sum.npasses = std::max(sum.npasses, sb.npasses);
+      sum.naccepted = b == 0 ? sb.naccepted : std::min(sum.naccepted, sb.naccepted);
+      sum.ndiscarded += sb.ndiscarded;
+      sum.eig_iters = std::max(sum.eig_iters, sb.eig_iters);
+      sum.ms_dist += sb.ms_dist;
+      sum.ms_orth += sb.ms_orth;
+      sum.ms_mmult += sb.ms_mmult;
+      sum.ms_eig += sb.ms_eig;
+      sum.ms_coords += sb.ms_coords;
+      sum.ms_total += sb.ms_total;
+      sum.edges_examined += sb.edges_examined;
+    }
+  }
+  PHDE_CK(ctx, cudaMemcpyAsync(rq, h_rq.data(), sizeof(double) * h_rq.size(), cudaMemcpyHostToDevice, ctx->stream));
+  PHDE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->batch_last_c = c;
+  if (stats) {
+    *stats = sum;
+    stats->status = PHDE_OK;
+    stats->gpu_launches = (int)(ctx->launches - launches0);
+  }
+  return PHDE_OK;
+}
+
+}  // namespace
+
 extern "C" int phde_layout_batched(phde_ctx *ctx, const phde_layout_opts *o, double *coords_out,
                                    phde_layout_stats *stats) {
   if (!ctx) return PHDE_ERR_INVALID;
   if (!o || !coords_out) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout_batched: bad arguments");
   if (ctx->batch_B < 1) return phde_fail(ctx, PHDE_ERR_NO_GRAPH, "phde_layout_batched: no batch uploaded");
-  if (o->algo != PHDE_ALGO_PARHDE || (o->strategy != PHDE_STRAT_KCENTERS && o->strategy != PHDE_STRAT_LEARNED) ||
-      o->precision != PHDE_PREC_MIXED || o->eig != PHDE_EIG_EXACT)
-    return phde_fail(ctx, PHDE_ERR_INVALID,
-                     "phde_layout_batched: supports ParHDE with Kcenters or learned pivots, PHDE_PREC_MIXED and "
-                     "PHDE_EIG_EXACT");
   const bool learned = o->strategy == PHDE_STRAT_LEARNED;
   const int k = o->k, c = o->c, B = ctx->batch_B, P = 3 * k;
-  if (k < 2 || k > BB) return phde_fail(ctx, PHDE_ERR_K_RANGE, "phde_layout_batched: k must be in 2..32");
-  if (c < 1 || c > MAXC || c > k) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout_batched: c must be in 1..min(4, k)");
-  for (int b = 0; b < B; b++) {
+  // the fused pipeline: ParHDE, Kcenters or learned pivots, mixed precision, Jacobi, k <= 32, c <= 4
+  const bool fused = o->algo == PHDE_ALGO_PARHDE && (o->strategy == PHDE_STRAT_KCENTERS || learned) &&
+                     o->precision == PHDE_PREC_MIXED && o->eig == PHDE_EIG_EXACT && k <= BB && c <= MAXC;
+  if (k < 2 || c < 1 || c > k) return phde_fail(ctx, PHDE_ERR_INVALID, "phde_layout_batched: need 2 <= k and 1 <= c <= k");
+  for (int b = 0; b < B; b++)
     if (ctx->batch_vbase[b + 1] - ctx->batch_vbase[b] <= P)
       return phde_fail(ctx, PHDE_ERR_K_RANGE,
                        "phde_layout_batched: graph " + std::to_string(b) + " has no more vertices than 3k pivots");
+  if (!fused) {
+    PHDE_CK(ctx, cudaSetDevice(ctx->device));
+    return layout_per_graph(ctx, o, coords_out, stats);
+  }
+  for (int b = 0; b < B; b++) {
     if (learned && ctx->batch_vbase[b + 1] - ctx->batch_vbase[b] <= PHDE_LEARNED_CANDIDATES)
       return phde_fail(ctx, PHDE_ERR_K_RANGE,
                        "phde_layout_batched: learned pivots need more than 256 vertices per graph (graph " +

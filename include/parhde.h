@@ -165,9 +165,13 @@ int phde_layout(phde_ctx *ctx, const phde_layout_opts *opts, double *coords_out,
  * Replaces a caller's loop of DrawingBase::run() + getCoordinates() over separate graphs
  * (variants/DrawingBase.h:41-60; spectralDrawing.cpp:186-197 per graph).  phde_batch_upload copies the
  * graphs (each its own CSR, local vertex ids; all with the same offset width) as one disjoint union;
- * phde_layout_batched lays every graph out: ParHDE with Kcenters pivots or learned pivots (PHDE_STRAT_LEARNED:
- * every graph above 256 vertices; each graph gets the pivots a single-graph learned layout picks), opts->precision PHDE_PREC_MIXED,
- * opts->eig PHDE_EIG_EXACT, 2 <= k <= 32, c <= 4, every graph connected with more than 3k vertices.
+ * phde_layout_batched lays every graph out (every graph connected with more than 3k vertices).  ParHDE with
+ * Kcenters pivots or learned pivots (PHDE_STRAT_LEARNED: every graph above 256 vertices; each graph gets the
+ * pivots a single-graph learned layout picks), opts->precision PHDE_PREC_MIXED, opts->eig PHDE_EIG_EXACT,
+ * 2 <= k <= 32 and c <= 4 run as one fused pipeline over the union; any other options phde_layout accepts
+ * (PHDE_PREC_FP64 -- the reference's arithmetic -- or PHDE_PREC_EXACT, k above 32, the power iteration, the
+ * other algorithms) lay the graphs out one after another with the single-graph pipeline, each graph's CSR
+ * cut out of the uploaded union on the device: the coordinates are those phde_layout gives that graph.
  * coords_out holds sum(n_b) * c doubles: graph b's coordinates, column-major (coordinate j of its local
  * vertex i at i + j * n_b), start at c * (n_0 + ... + n_{b-1}).  The first call on a batch autotunes and
  * captures the pipeline into a CUDA graph; later calls replay it. */

@@ -6,6 +6,7 @@ import scipy.sparse as sp
 
 from icpp_2020_parhde_gb300 import Context, ParHDEError, graphs
 from icpp_2020_parhde_gb300.csr_io import CSRGraph
+from conftest import sign_align
 
 pytestmark = pytest.mark.gpu
 
@@ -74,7 +75,7 @@ def test_batched_rejects_bad_input():
     with pytest.raises(ParHDEError) as e:
         cb.layout_batched(10, 2)  # 20 vertices <= 3k pivots
     with pytest.raises(ParHDEError):
-        cb.layout_batched(40, 2)  # k above 32
+        cb.layout_batched(40, 2)  # k above 32 (per-graph pipeline): 20 vertices <= 3k pivots as well
 
 
 def test_block_per_graph_kcenters_matches_union(monkeypatch):
@@ -161,3 +162,38 @@ def test_batched_learned_rejects_small_graphs():
     with pytest.raises(ParHDEError) as e:
         cb.layout_batched(10, 2, strategy="Learned")
     assert e.value.status == -4
+
+
+@pytest.mark.parametrize("precision,eig,k,c", [("fp64", "power", 10, 2), ("exact", "exact", 40, 3),
+                                               ("mixed", "exact", 40, 2)])
+def test_batched_other_options_match_single_layouts(precision, eig, k, c):
+    """Options outside the fused batched pipeline (the reference's FP64 arithmetic, exact arithmetic, k above
+    32, the power iteration) lay every graph out with the single-graph pipeline on its CSR cut out of the
+    union: the coordinates and Rayleigh quotients a single-graph call gives; FP64 with the power iteration
+    also against the oracle (the reference algorithm).  The fused pipeline still runs on the batch after."""
+    from oracle import oracle as orc
+    gs = [graphs.rgg(3000, dim=2, avg_degree=8, seed=41), graphs.mesh(60, 50, seed=42),
+          graphs.rmat(12, seed=43), graphs.rgg(5000, dim=3, avg_degree=12, seed=44)]
+    cb = Context(0)
+    cb.upload_batch(gs)
+    xs, st = cb.layout_batched(k, c, precision=precision, eig=eig)
+    xs = [x.copy() for x in xs]
+    rq = cb.batch_rayleigh()
+    assert st["naccepted"] == k
+    cs = Context(0)
+    for i, (g, xb) in enumerate(zip(gs, xs)):
+        cs.upload(g)
+        r = cs.layout("ParHDE", "Kcenters", k, c, precision=precision, eig=eig)
+        if precision == "exact":  # exact integer sums: the same bits
+            assert np.array_equal(xb, r.coords)
+        else:  # the same kernels; FP64 (FP32) sums may associate differently between calls
+            np.testing.assert_allclose(sign_align(xb, r.coords), r.coords, rtol=0,
+                                       atol=1e-10 if precision == "fp64" else 1e-5)
+        np.testing.assert_allclose(rq[i], rayleigh(g, xb), rtol=1e-4 if precision == "mixed" else 1e-9)
+        if precision == "fp64":
+            L = orc.layout(g, "ParHDE", "Kcenters", k, c, nthreads=4)
+            assert L.status == 0
+            np.testing.assert_allclose(sign_align(xb, L.coords), L.coords, rtol=0, atol=1e-7)
+    xf, _ = cb.layout_batched(10, 2)  # the union view is back: the fused pipeline on the same batch
+    for g, x in zip(gs, xf):
+        assert x.shape == (g.n, 2) and np.all(np.isfinite(x))
