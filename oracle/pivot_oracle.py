@@ -55,3 +55,24 @@ def scores(f: np.ndarray, w: np.ndarray) -> np.ndarray:
     h2 = np.maximum(h1 @ W2.T + b2, 0).astype(np.float32)
     z = (h2 @ w3 + b3).astype(np.float32)
     return (1.0 / (1.0 + np.exp(-z.astype(np.float64)))).astype(np.float32)
+
+
+def farthest_point_order(D_warm: np.ndarray, C: np.ndarray, npick: int) -> list[int]:
+    """The learned strategy's pivot order after the warm start (the host loop of csrc/api.cu's learned path):
+    D_warm (M, P0) = the candidates' distances to the warm-start pivots, C (M, M) = the candidates' pairwise
+    distances (C[i, j] from candidate j to candidate i); candidates in proposal order (best score first).
+    Each step takes the unused candidate farthest from every pivot taken so far -- the first in proposal order
+    on ties -- and folds its distances into the minima.  Returns candidate indices."""
+    M = C.shape[0]
+    mind = D_warm.min(axis=1).astype(np.int64) if D_warm.shape[1] else np.full(M, np.iinfo(np.int32).max, np.int64)
+    used = np.zeros(M, dtype=bool)
+    order = []
+    for _ in range(min(npick, M)):
+        cand = np.where(~used, mind, -1)
+        best = int(np.argmax(cand))  # first maximum: proposal order on ties
+        if used[best]:
+            break
+        used[best] = True
+        order.append(best)
+        mind = np.minimum(mind, C[:, best])
+    return order

@@ -177,3 +177,23 @@ def test_feature_and_mlp_kernels_vs_numpy(gpu_ctx, make):
     assert all(abs(float(ref[v]) - float(cut)) <= 1e-5 * abs(float(cut)) + 1e-7 for v in differ), sorted(differ)[:8]
     # candidates come best first: their GPU scores are non-increasing
     assert np.all(np.diff(sc[cand].astype(np.float64)) <= 0)
+
+
+@pytest.mark.parametrize("make,k", [(lambda: graphs.rmat(14, seed=51), 20), (lambda: graphs.rgg(20000, dim=3, avg_degree=12, seed=52), 16),
+                                    (lambda: graphs.mesh(120, 90, seed=53), 24)], ids=["rmat14", "rgg3d", "mesh"])
+def test_learned_pivot_order_vs_oracle(gpu_ctx, make, k):
+    """The learned strategy's whole pivot sequence against a CPU restatement, given the proposal's candidates:
+    the warm start is the oracle's Kcenters (the first 8 pivots), the candidates' distances come from the
+    oracle's one-source BFS (the GPU reads them from its multi-source sweep), and the rest is the
+    farthest-point order of oracle/pivot_oracle.py -- the same 3k sources in the same order."""
+    from oracle import pivot_oracle as po
+    g = make()
+    gpu_ctx.upload(g)
+    _, _, cand = gpu_ctx.pivot_scores(256)
+    lp = gpu_ctx.layout("ParHDE", "Learned", k, 2, precision="exact", eig="exact")
+    P = 3 * k
+    Dw, warm = orc.kcenters(g, po.WARM, 0)
+    assert np.array_equal(lp.sources[: po.WARM], warm)
+    dist = np.stack([orc.bfs(g, int(v)) for v in cand], axis=1)  # (n, M): column j from candidate j
+    order = po.farthest_point_order(Dw[cand], dist[cand], P - po.WARM)
+    assert np.array_equal(lp.sources[po.WARM:], cand[order])
