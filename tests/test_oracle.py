@@ -172,3 +172,26 @@ def test_draw_oracle_geometry_degenerate():
     (xmin, xmax, ymin, ymax, aspect), (w0, h0), (W, H) = orc.draw_geometry(np.linspace(0, 5, 10), np.full(10, 2.0))
     assert (xmin, xmax, ymin, ymax, aspect) == (0.0, 5.0, 1.0, 2.0, 5.0)
     assert (w0, h0, W, H) == (14, 70, 14, 70)
+
+
+def test_farthest_point_order_restatement():
+    """The pivot oracle's farthest-point order against a plain loop over the candidates (first in proposal order
+    on ties), on a mesh whose many equal distances make ties common, and with no warm-start columns."""
+    from icpp_2020_parhde_gb300 import graphs
+    from oracle import pivot_oracle as po
+    g = graphs.mesh(40, 30, seed=3)
+    Dw, _ = orc.kcenters(g, po.WARM, 0)
+    cand = np.arange(0, g.n, 7)[:200]
+    dist = np.stack([orc.bfs(g, int(v)) for v in cand], axis=1)[cand]  # (M, M)
+    for warm_cols in (Dw[cand], Dw[cand][:, :0]):
+        mind = warm_cols.min(axis=1).astype(np.int64) if warm_cols.shape[1] else np.full(len(cand), 2**31 - 1)
+        used, want = np.zeros(len(cand), bool), []
+        for _ in range(30):
+            best = -1
+            for i in range(len(cand)):
+                if not used[i] and (best < 0 or mind[i] > mind[best]):
+                    best = i
+            used[best] = True
+            want.append(best)
+            mind = np.minimum(mind, dist[:, best])
+        assert po.farthest_point_order(warm_cols, dist, 30) == want
